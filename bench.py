@@ -1,0 +1,327 @@
+"""Benchmark: zone-updates/s of the hydro/MHD + cooling step on one GB300.
+
+A step is one pass of the hot path over the whole block list: CFL time step
+(device min-reduction), guard-cell fill, unsplit MHD update, heating/cooling
+source term. Two paths run on the same seeded input:
+  plain : all-FP64 reconstruction/Riemann/update + the plain implicit
+          cooling integrator
+  fast  : FP32 reconstruction/Riemann, FP64 update/CT/energy recovery,
+          cooling as in `plain` (the learned surrogate replaces it when
+          available)
+`value` is the fast path's device throughput; `plain_fp64` the plain one;
+`e2e` is the fast path through the C ABI with host FLASH-layout buffers
+copied in and out every step.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="mhd_turbbox_128cubed_cooling", nbx=8, nby=8, nbz=8, seed=44, sigma_ln=1.0,
+                mach=5.0, beta=1.0, dA=0.1)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", "0"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [l.split(",") for l in open(self.path) if l.strip()]
+        except Exception:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def make_grid(G, ic, precision, cooling=True):
+    g = G.grid_from_workload(ic, mhd=True, cooling=cooling)
+    units = G.code_units()
+    gm1 = 2.0 / 3.0
+    if cooling:
+        e = g.u[:, 6]
+        g.u[:, g.slots["TEMP"]] = e * units["vel_unit"] ** 2 * gm1 * (24.0 / 11.0) * G.MP / G.KB
+        g.u[:, g.slots["TDUS"]] = 15.0
+    return g, units
+
+
+def run_path(G, g, precision, steps, warmup, cool=True, timing=None):
+    import torch
+    G.init_hydro(G.hydro_params(True, precision=precision))
+    g.register()
+    s = torch.cuda.current_stream()
+    for _ in range(warmup):
+        dt = g.compute_dt().item()
+        g.evolve_step(dt, cool=cool)
+    torch.cuda.synchronize()
+    g.status_reset()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    for _ in range(steps):
+        dt = g.compute_dt().item()
+        g.evolve_step(dt, cool=cool)
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, g.status_read()
+
+
+def phase_times(G, g, precision, cool=True, reps=2):
+    """CUDA-event time of each launch group on the launching stream."""
+    import ctypes as C
+    import torch
+    G.init_hydro(G.hydro_params(True, precision=precision))
+    g.register()
+    L = G.lib()
+    s = torch.cuda.current_stream()
+    stream = C.c_void_p(s.cuda_stream)
+    lt, n = g.list_tensor()
+    out = {}
+    dt = g.compute_dt().item()
+    for name, fn in (
+        ("guard_fill", lambda: L.gb_fill_guardcells(n, C.c_void_p(lt.data_ptr()), stream)),
+        ("hydro_update" + ("_cool" if cool else ""),
+         lambda: L.gb_evolve_step(n, C.c_void_p(lt.data_ptr()), dt, int(cool), C.c_void_p(g.status.data_ptr()), stream)),
+    ):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for _ in range(reps):
+            fn()
+        b.record(s)
+        torch.cuda.synchronize()
+        out[name] = a.elapsed_time(b) / reps
+    out["hydro_update" + ("_cool" if cool else "")] -= out["guard_fill"]
+    return out
+
+
+def cpu_baseline(nblocks_sample=8, steps=1):
+    """The oracle (C port, OpenMP over blocks) on a bounded sample of the
+    same workload: `nblocks_sample` blocks of the 128^3 box, MHD + cooling."""
+    from oracle import oracle as O
+    from torch_gb300 import gbhydro as G
+    from torch_gb300 import tables
+    from torch_gb300 import workloads as W
+    O.build()
+    wl = WORKLOAD
+    ic = W.turbulent_box(2, 2, 2, seed=wl["seed"], sigma_ln=wl["sigma_ln"], mach=wl["mach"], mhd=True,
+                         nvar=10)
+    p = O.hydro_params(True)
+    u, fx, fy, fz, dx = ic["u"], ic["fx"], ic["fy"], ic["fz"], 1.0 / (16 * wl["nbx"])
+    units = G.code_units()
+    cp = O.cool_params()
+    tab = O.table_from_ilog(*tables.read_compact())
+    nthreads = O.lib().orc_num_threads()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        O.fill_guards_periodic(p, 2, 2, 2, u, fx, fy, fz)
+        dt = 0.8 * O.dt_limit(p, u, dx, dx, dx)
+        O.unsplit_blocks(p, u, fx, fy, fz, dt, dx, dx, dx)
+        sl = (slice(None), slice(4, 20), slice(4, 20), slice(4, 20))
+        rho = (u[:, 0][sl] * units["dens_unit"]).ravel().copy()
+        ei = (u[:, 6][sl] * units["vel_unit"] ** 2).ravel().copy()
+        T = ei * (2.0 / 3.0) * (24.0 / 11.0) * G.MP / G.KB
+        td = np.full_like(T, 15.0)
+        O.radheat_cells(cp, tab, dt * units["time_unit"], rho, ei.copy(), ei, T, td)
+    el = time.perf_counter() - t0
+    zones = nblocks_sample * 4096 * steps
+    return {"value": zones / el, "unit": "zone-updates/s", "cores": int(nthreads), "kind": "port",
+            "sample": f"{nblocks_sample} blocks of 16^3 (MHD+cooling, oracle C port, OpenMP) x {steps} step(s), {el:.2f} s"}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    steps = max(1, args.steps)
+    vals = []
+    cb = None
+    for _ in range(args.warmup):
+        cpu_baseline(8, 1)
+    for _ in range(steps):
+        cb = cpu_baseline(8, 1)
+        vals.append(cb["value"])
+    v = float(np.median(vals))
+    cb["value"] = v
+    line = {"metric": "zone-updates/s", "value": v, "unit": "zone-updates/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
+            "dtype": "f64", "data": "synthetic", "scaling": "weak", "vs_baseline": None,
+            "config": {"workload": WORKLOAD["name"], "sample_blocks": 8},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "zone-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "FLASH 4.6.2 (the reference's hydro) is not in the reference tree and no Fortran "
+                    "compiler exists here; the timed reference is the oracle's C restatement of the "
+                    "reference's algorithm on host cores"}
+    print(json.dumps(line))
+
+
+def e2e_run(G, g, steps, warmup):
+    """Fast path through the C ABI with host FLASH-layout (variable-fastest)
+    pinned buffers uploaded before and downloaded after every step."""
+    import ctypes as C
+    import torch
+    nunk = g.nvar
+    nb3 = 24 * 24 * 24
+    host = torch.empty((g.nblocks, nb3, nunk), dtype=torch.float64).pin_memory()
+    host.copy_(g.u.reshape(g.nblocks, nunk, nb3).transpose(1, 2).cpu())
+    hslot = (C.c_int * G.NROLE)(*([-1] * G.NROLE))
+    for name, s in g.slots.items():
+        hslot[G.R[name]] = s
+    L = G.lib()
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    lt, n = g.list_tensor()
+
+    def one():
+        G.check(L.gb_grid_upload_flash(C.c_void_p(host.data_ptr()), nunk, hslot, g.nblocks, st), "upload")
+        dt = g.compute_dt().item()
+        g.evolve_step(dt, cool=True)
+        G.check(L.gb_grid_download_flash(C.c_void_p(host.data_ptr()), nunk, hslot, g.nblocks, st), "download")
+
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        one()
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / steps
+    nbytes = host.numel() * 8
+    return ms, nbytes
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from torch_gb300 import gbhydro as G
+    from torch_gb300 import workloads as W
+    wl = WORKLOAD
+    # replicas: every rank runs its own copy of the workload (the step has no
+    # cross-GPU exchange on one-GPU machines)
+    ic = W.turbulent_box(wl["nbx"], wl["nby"], wl["nbz"], seed=wl["seed"], sigma_ln=wl["sigma_ln"],
+                         mach=wl["mach"], mhd=True, beta=wl["beta"], dA=wl["dA"], nvar=10)
+    units = G.code_units()
+    G.init_cooling(G.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
+                                 time_unit=units["time_unit"]))
+    zones = wl["nbx"] * wl["nby"] * wl["nbz"] * 4096
+    g_plain, _ = make_grid(G, ic, 0)
+    g_fast, _ = make_grid(G, ic, 1)
+    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+    clk = ClockSampler(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv"))
+    if world > 1:
+        dist.barrier()
+    with clk:
+        ms_plain, st_plain = run_path(G, g_plain, 0, args.steps, args.warmup)
+        ms_fast, st_fast = run_path(G, g_fast, 1, args.steps, args.warmup)
+    if world > 1:
+        t = torch.tensor([ms_plain, ms_fast], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_plain, ms_fast = t.tolist()
+    # accuracy of the fast path against the plain one after the same steps
+    a, b = g_plain.u.cpu().numpy(), g_fast.u.cpu().numpy()
+    sl = (slice(None), slice(4, 20), slice(4, 20), slice(4, 20))
+    l1 = {v: float(np.abs(a[:, i][sl] - b[:, i][sl]).sum() / np.abs(a[:, i][sl]).sum())
+          for v, i in (("dens", 0), ("pres", 4))}
+    ph = phase_times(G, g_fast, 1)
+    e2e_ms, e2e_bytes = e2e_run(G, g_fast, max(2, args.steps // 2), 1)
+    hbm, hbm_kind = peaks()
+    # dominant kernel group: the update (+ fused cooling); algorithmic bytes
+    # 216 B per zone-update (12 FP64 MHD words + 3 cooling words, read+write)
+    dom = max(ph, key=ph.get)
+    algo_bytes = 216.0 * zones
+    ach = algo_bytes / (ph[dom] * 1e-3) / 1e9
+    if rank != 0:
+        return
+    line = {
+        "metric": "zone-updates/s", "value": zones * world / (ms_fast * 1e-3), "unit": "zone-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_fast,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": wl["name"], "blocks": wl["nbx"] * wl["nby"] * wl["nbz"], "block": "16^3+4gc",
+                   "physics": "MHD HLLD+CT, PPM, implicit heating/cooling", "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (state ~0.75 GB)"},
+        "plain_fp64": {"value": zones * world / (ms_plain * 1e-3), "ms_per_step": ms_plain},
+        "speedup_vs_plain_fp64": ms_plain / ms_fast,
+        "l1_err_vs_fp64": l1,
+        "phase_ms_fast": ph,
+        "status": {"plain": {k: st_plain[k] for k in ("code", "n_fallback", "n_eint_switch", "n_bracket_fail")},
+                   "fast": {k: st_fast[k] for k in ("code", "n_fallback", "n_eint_switch", "n_bracket_fail")}},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
+                     "frac": ach / hbm, "traffic": None, "peak_kind": hbm_kind},
+        "e2e": {"value": zones / (e2e_ms * 1e-3), "unit": "zone-updates/s", "h2d_bytes_per_step": e2e_bytes,
+                "d2h_bytes_per_step": e2e_bytes},
+        "gpu_launches": None,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,215 @@
+/*
+ * gbhydro: C ABI of the GB300 (sm_103a) hydro/MHD + heating/cooling step.
+ *
+ * The library replaces, for one GPU, the per-step hot path that Torch's
+ * patched FLASH 4.6.2 runs:
+ *   Hydro(blockCount, blockList, timeEndAdv, dt, dtOld, sweepOrder)
+ *     -> hy_uhd_unsplit(blockCount, blockList, dt, dtOld)
+ *        (src/flash/source/physics/Hydro/HydroMain/unsplit/hy_uhd_interface.F90:472-479;
+ *         called at src/flash/source/Driver/DriverMain/Unsplit/Couple_AMUSE/Driver_evolveFlash.F90:406)
+ *   Heat(blockCount, blockList, dt, time) -> RadHeat(...)
+ *        (src/flash/source/physics/sourceTerms/Heat/HeatMain/HeatCool/phenHeat/Heat_interface.F90:10-16;
+ *         .../phenHeat/mol_and_dust/solver/RadHeat.F90:45)
+ * Plain pointers and sizes only; every pointer to grid data is a device
+ * pointer unless the name says _host. Calls are stream-ordered on the
+ * stream given (NULL = the legacy default stream) and return a gb_rc;
+ * kernel-side failures land in a device gb_status the caller reads after
+ * synchronising (gb_status_read). No call traps, asserts or aborts.
+ */
+#ifndef GBHYDRO_H
+#define GBHYDRO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- codes */
+typedef enum gb_rc {
+    GB_OK = 0,
+    GB_ERR_ARG = -1,        /* bad argument (null pointer, size out of range) */
+    GB_ERR_CUDA = -2,       /* a CUDA runtime call failed */
+    GB_ERR_NOT_INIT = -3,   /* gb_cool_init / gb_register_grid not called */
+    GB_ERR_TABLE = -4,      /* cooling table missing or malformed */
+    GB_ERR_LIMIT = -5       /* request beyond a documented maximum */
+} gb_rc;
+
+/* kernel status codes (gb_status.code; first error wins) */
+enum {
+    GB_ST_OK = 0,
+    GB_ST_NEG_DENS = 1,     /* density <= 0 after the update */
+    GB_ST_NEG_PRES = 2,     /* pressure floored */
+    GB_ST_NONFINITE = 3,    /* NaN/Inf in the updated state */
+    GB_ST_ZERO_UNBRACKETED = 4, /* Brent entered without a sign change (Fortran `stop`) */
+    GB_ST_ZERO_MAXITER = 5, /* Brent iteration cap (Fortran `stop`) */
+    GB_ST_OVERHEAT = 6      /* T > absTmax clamped (RadHeat.F90:380-405) */
+};
+
+/* Device-resident status word: the first failure plus counters. */
+typedef struct gb_status {
+    int code;
+    int block, i, j, k;     /* where the first failure happened */
+    int pad;
+    double value;           /* offending value */
+    unsigned long long n_fallback;     /* reconstruction fell back to first order */
+    unsigned long long n_bracket_fail; /* zbrac gave up; absolute bracket used */
+    unsigned long long n_dust_noconv;  /* dust Newton hit its cap */
+    unsigned long long n_clamped;      /* T clamped at absTmax */
+    unsigned long long n_eint_switch;  /* dual-energy switch chose the advected e_int */
+    unsigned long long n_surrogate;    /* cells cooled by the learned surrogate */
+    unsigned long long n_surrogate_reject; /* surrogate rejected -> plain integrator */
+} gb_status;
+
+/* ---------------------------------------------------------------- grid */
+#define GB_NXB 16
+#define GB_NGUARD 4
+#define GB_NB (GB_NXB + 2 * GB_NGUARD) /* 24 */
+
+/* cell-variable roles; gb_grid_desc.slot[] maps each to a store slot or -1 */
+enum {
+    GB_DENS = 0, GB_VELX, GB_VELY, GB_VELZ, GB_PRES, GB_ENER, GB_EINT,
+    GB_MAGX, GB_MAGY, GB_MAGZ, GB_TEMP, GB_TDUS, GB_PHHE, GB_PEFL, GB_IHP,
+    GB_NROLE
+};
+
+/* Store layout. Cells: unk[block][slot][k][j][i] with i fastest and
+ * 24^3 padded cells per (block, slot). Faces (MHD):
+ *   facex[block][k][j][i], i in 0..24 (face i = low face of cell i),
+ *   facey[block][k][j][i], j in 0..24, facez[block][k][j][i], k in 0..24. */
+typedef struct gb_grid_desc {
+    int nvar;               /* slots per block */
+    int maxblocks;
+    int slot[GB_NROLE];
+    double* unk;
+    double* facex;
+    double* facey;
+    double* facez;
+} gb_grid_desc;
+
+/* Block tree for guard filling. Arrays of length nnodes (device pointers):
+ * level (0 = root level), integer lower corner in units of that level's
+ * block size, child node ids (8 per node, -1 for leaves; child c has
+ * offset (c&1, (c>>1)&1, (c>>2)&1)), and the root-grid lookup
+ * root[rx + nrx*(ry + nry*rz)] -> node id. Leaf blocks are addressed in
+ * the store by their node id. The domain is periodic. */
+typedef struct gb_tree_desc {
+    int nnodes;
+    int nrx, nry, nrz;      /* root grid in blocks */
+    int maxlevel;
+    const int* level;
+    const int* coord;       /* 3 ints per node */
+    const int* child;       /* 8 ints per node */
+    const int* root;
+    double xmin[3];
+    double root_dx[3];      /* cell size at level 0 */
+} gb_tree_desc;
+
+int gb_register_grid(const gb_grid_desc* grid, const gb_tree_desc* tree);
+
+/* Fill the guard cells (and guard faces) of the listed blocks from their
+ * neighbours: same-level copy, injection from a coarser neighbour,
+ * restriction (8-cell mean) from a finer one, periodic domain. The role
+ * FLASH's Grid_fillGuardCells plays before Hydro
+ * (src/flash/source/Driver/DriverMain/Unsplit/Couple_AMUSE/Driver_computeDt.F90:243). */
+int gb_fill_guardcells(int blockCount, const int* blockList_dev, void* stream);
+
+/* ---------------------------------------------------------------- hydro */
+typedef struct gb_hydro_params {
+    double gamma;
+    double cfl;             /* flash.par.turbsph_standard:163 */
+    double cvisc;           /* :198 */
+    int use_avisc;          /* :197 */
+    int mhd;                /* 0 = hydro HLLC, 1 = USM MHD HLLD + CT */
+    double eint_switch;     /* :164 */
+    double smlrho, smallp;  /* floors in grid units */
+    int precision;          /* 0 = all FP64, 1 = FP32 reconstruction/Riemann, FP64 update */
+    int pad;
+} gb_hydro_params;
+
+int gb_hydro_init(const gb_hydro_params* p);
+
+/* One unsplit step over blockCount leaf blocks (blockList: device int
+ * array of store block ids, 0-based). Replaces hy_uhd_unsplit; dtOld is
+ * accepted for signature parity and unused (as in the second-order
+ * unsplit scheme). Guard cells must have been filled. st: device status. */
+int gb_hydro_unsplit(int blockCount, const int* blockList_dev, double dt, double dtOld,
+                     gb_status* st_dev, void* stream);
+
+/* Blocks per launch chunk of the hydro kernels (scratch = chunk x per-block
+ * scratch; the autotuner picks it). Default 16. */
+int gb_set_chunk_blocks(int n);
+
+/* CFL time step: writes cfl * min over interior cells of the listed blocks
+ * of dx_d / (|v_d| + c_f,d) to *dt_dev (device double). The per-block
+ * Hydro_computeDt + MPI_AllReduce(MINLOC) of
+ * src/flash/source/Driver/DriverMain/Unsplit/Couple_AMUSE/Driver_computeDt.F90:327-335,514-515. */
+int gb_compute_dt(int blockCount, const int* blockList_dev, double* dt_dev, void* stream);
+
+/* ---------------------------------------------------------------- cooling */
+typedef struct gb_cool_params {
+    /* Heat_data / Cool_data runtime parameters (phenHeat/Config, mol_and_dust/Config) */
+    double tradmin, tradmax, dradmin, dradmax;
+    double theatmin, theatmax, absTmin, absTmax;
+    double Gzero, subfactor, smallp;
+    int use_cr_heating;
+    double crIonRate, crIonNH, crIonExp, crIonEnergy;
+    double dust_sputter_temp;
+    int pe_recipe;          /* 0 WD01, 1 BT94, 2 NOGF */
+    double pe_norm;
+    double boltz, mp;
+    double T_cool_min, nd_cool_min, nd_cool_max;
+    int useDustCool;
+    int int_method;         /* 0 Implicit (the only one on the GPU), 1 Euler */
+    double mu_mol;          /* 24/11, RadHeat.F90:278 */
+    double xHp_const;       /* ionisation fraction when the grid has no IHP slot */
+    /* grid units -> CGS (1.0 when the grid is in CGS) */
+    double dens_unit, vel_unit, time_unit;
+    double eos_abar;        /* mean molecular weight of the Gamma EOS (T from e) */
+} gb_cool_params;
+
+/* Load cool.dat (FLASH format, get_cooling_data.F90:20-55) or the compact
+ * int32 form, and set the parameters. Replaces Cool_init/Heat_init. */
+int gb_cool_init(const char* cool_dat_path, const gb_cool_params* p);
+
+/* Per-cell heating/cooling over the interior of the listed blocks:
+ * RadHeat.F90:179-457 with heating_and_cooling's "Implicit" branch
+ * (heatCool.F90:216-514). Updates EINT, ENER, TEMP, TDUS (and PRES via the
+ * Gamma EOS); zeroes PHHE/PEFL when present. */
+int gb_heat(int blockCount, const int* blockList_dev, double dt, double time,
+            gb_status* st_dev, void* stream);
+
+/* The same per-cell solve on plain CGS arrays of n cells (no grid): ei,
+ * temp, tdust updated in place; dens, xhp, phhe (erg/cm^3/s), gflux may be
+ * NULL for defaults (xHp_const, 0, 0). */
+int gb_cool_cells(int64_t n, const double* dens, double* ei, double* temp, double* tdust,
+                  const double* xhp, const double* phhe, const double* gflux, double dt,
+                  gb_status* st_dev, void* stream);
+
+/* ---------------------------------------------------------------- step */
+/* One full step over the registered grid as FLASH's Driver_evolveFlash
+ * runs it: guard fill, hydro (or MHD), then the cooling source term fused
+ * into the update's epilogue when cool != 0. */
+int gb_evolve_step(int blockCount, const int* blockList_dev, double dt, int cool,
+                   gb_status* st_dev, void* stream);
+
+/* Host<->device copies of the whole store in FLASH's unk(NUNK, i, j, k,
+ * blk) order (variable fastest), transposed on the device. nunk = number
+ * of variables in the host array; host_slot[r] = index of role r in the
+ * host's variable axis or -1. */
+int gb_grid_upload_flash(const double* unk_host, int nunk, const int* host_slot, int nblocks,
+                         void* stream);
+int gb_grid_download_flash(double* unk_host, int nunk, const int* host_slot, int nblocks,
+                           void* stream);
+
+/* ---------------------------------------------------------------- misc */
+int gb_status_reset(gb_status* st_dev, void* stream);
+int gb_status_read(const gb_status* st_dev, gb_status* st_host);
+const char* gb_last_error(void);
+int gb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,70 @@
+/*
+ * CPU oracle for the unsplit hydro / staggered-mesh MHD block update.
+ * TEST INFRASTRUCTURE ONLY (see oracle.h).
+ *
+ * FLASH 4.6.2's unsplit solver body is not in the reference tree; only the
+ * per-cell reconstruction driver hy_uhd_dataReconstOneStep.F90 and the
+ * interfaces in hy_uhd_interface.F90 are. This restatement follows that
+ * driver's control flow (normal-direction PPM per dimension, transverse
+ * corrections, multidimensional MHD terms, positivity fallback) and writes
+ * the absent pieces from the published methods the reference cites:
+ * Colella & Woodward 1984 (PPM), Stone et al. 2008 (characteristic tracing),
+ * Toro 1997 / Batten et al. 1997 (HLLC), Miyoshi & Kusano 2005 (HLLD),
+ * Gardiner & Stone 2005 (upwinded CT electric fields), Bryan et al. 1995
+ * (dual energy). Parity against FLASH itself is unpinned.
+ *
+ * Block storage: NV cell variables, each a contiguous nxg*nyg*nzg array
+ * (x fastest), guard cells included; face-centred B as three arrays of
+ * (nxg+1)*nyg*nzg, nxg*(nyg+1)*nzg, nxg*nyg*(nzg+1).
+ */
+#ifndef GB_HYDRO_ORACLE_H
+#define GB_HYDRO_ORACLE_H
+
+#include <stdint.h>
+
+/* cell-variable slots in the oracle's block layout */
+enum {
+    ORV_DENS = 0, ORV_VELX, ORV_VELY, ORV_VELZ, ORV_PRES, ORV_ENER, ORV_EINT,
+    ORV_MAGX, ORV_MAGY, ORV_MAGZ, ORV_NVAR
+};
+
+typedef struct orc_hydro_params {
+    double gamma;
+    double cvisc;      /* use_avisc/cvisc, flash.par.turbsph_standard:197-198 */
+    int use_avisc;
+    double eint_switch;/* eintSwitch, :164 */
+    double smlrho, smallp;
+    int mhd;           /* 0: hydro (HLLC), 1: USM MHD (HLLD + CT) */
+    int nxb, nguard;   /* 16, 4 */
+} orc_hydro_params;
+
+void orc_hydro_default_params(orc_hydro_params* p, int mhd);
+
+/* One unsplit step of one block. `u` holds the ORV_NVAR variables (those
+ * beyond ORV_EINT only when mhd) with guard cells filled; bx/by/bz the face
+ * fields (mhd only). Interior cells and interior faces are overwritten in
+ * place with the state at t+dt. Returns the number of cells whose
+ * reconstructed state fell back to first order. */
+int orc_unsplit_block(const orc_hydro_params* p, double* u, double* bx, double* by, double* bz,
+                      double dt, double dx, double dy, double dz);
+
+/* CFL limit over the interior cells of one block:
+ * min_d dx_d / (|v_d| + c_f,d). */
+double orc_block_dt_limit(const orc_hydro_params* p, const double* u, double dx, double dy,
+                          double dz);
+
+/* Periodic guard-cell fill for a uniform grid of nbx*nby*nbz blocks stored
+ * consecutively (block id = bx + nbx*(by + nby*bz)). Fills all NV cell
+ * variables and, when mhd, the three face arrays (guard faces and the
+ * shared boundary face taken from the lower-index owner). */
+void orc_fill_guards_periodic(const orc_hydro_params* p, int nbx, int nby, int nbz, double* u,
+                              double* bx, double* by, double* bz);
+
+/* Total mass, momentum, energy (E incl. magnetic) and max |div B| over the
+ * interior of a uniform grid. out[0..4] = M, Px, Py, Pz, E; out[5] = max
+ * |divB| * dx / max|B|. */
+void orc_conserved_totals(const orc_hydro_params* p, int nblocks, const double* u,
+                          const double* bx, const double* by, const double* bz, double dx,
+                          double dy, double dz, double* out);
+
+#endif

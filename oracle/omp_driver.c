@@ -1,0 +1,87 @@
+/*
+ * Multi-block drivers over the oracle (test infrastructure only): the
+ * block loop a FLASH rank runs, parallelised one block per OpenMP thread
+ * for the timed CPU baseline.
+ */
+#include "oracle.h"
+
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+int orc_num_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void orc_set_num_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+/* One unsplit step over nblocks consecutive blocks (block-major storage as
+ * in hydro_oracle.h). Returns the total fallback-cell count. */
+long orc_unsplit_blocks(const orc_hydro_params* p, int nblocks, double* u, double* bx, double* by,
+                        double* bz, double dt, double dx, double dy, double dz)
+{
+    const int n = p->nxb + 2 * p->nguard;
+    const int64_t n3 = (int64_t)n * n * n, fsz = n3 + (int64_t)n * n;
+    long total = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
+    for (int b = 0; b < nblocks; ++b) {
+        double* ub = u + (int64_t)b * ORV_NVAR * n3;
+        double* fx = p->mhd ? bx + (int64_t)b * fsz : NULL;
+        double* fy = p->mhd ? by + (int64_t)b * fsz : NULL;
+        double* fz = p->mhd ? bz + (int64_t)b * fsz : NULL;
+        total += orc_unsplit_block(p, ub, fx, fy, fz, dt, dx, dy, dz);
+    }
+    return total;
+}
+
+double orc_dt_limit_blocks(const orc_hydro_params* p, int nblocks, const double* u, double dx,
+                           double dy, double dz)
+{
+    const int n = p->nxb + 2 * p->nguard;
+    const int64_t n3 = (int64_t)n * n * n;
+    double best = 1e300;
+#pragma omp parallel for reduction(min : best)
+    for (int b = 0; b < nblocks; ++b) {
+        double v = orc_block_dt_limit(p, u + (int64_t)b * ORV_NVAR * n3, dx, dy, dz);
+        if (v < best) best = v;
+    }
+    return best;
+}
+
+/* RadHeat over many cells, one chunk per thread. */
+int orc_radheat_cells_omp(const orc_cool_params* p, const orc_table* t, int64_t n, double dt,
+                          const double* dens, const double* velx, const double* vely,
+                          const double* velz, double* ener, double* eint, double* temp,
+                          double* tdus, const double* xhp, double* phhe, double* pefl,
+                          int* ncount_out, int* flags_out)
+{
+    int clamped = 0;
+    const int64_t chunk = 256;
+    int64_t nchunks = (n + chunk - 1) / chunk;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : clamped)
+    for (int64_t c = 0; c < nchunks; ++c) {
+        int64_t o = c * chunk;
+        int64_t m = n - o < chunk ? n - o : chunk;
+        clamped += orc_radheat_cells(p, t, m, dt, dens + o, velx ? velx + o : NULL,
+                                     vely ? vely + o : NULL, velz ? velz + o : NULL, ener + o,
+                                     eint + o, temp + o, tdus + o, xhp ? xhp + o : NULL,
+                                     phhe ? phhe + o : NULL, pefl ? pefl + o : NULL,
+                                     ncount_out ? ncount_out + o : NULL,
+                                     flags_out ? flags_out + o : NULL);
+    }
+    return clamped;
+}

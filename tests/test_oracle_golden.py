@@ -1,0 +1,193 @@
+"""The CPU oracle pinned against the reference's own fixtures (no GPU)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _load(name):
+    with open(os.path.join(GOLD, name)) as f:
+        return json.load(f)
+
+
+def test_dopr5_known_answer(oracle):
+    """IntegratorModule/test.f95 + test.dat: the DoPr5 driver on dx/dt = t
+    reproduces every printed row. The rows are written with es15.3 (four
+    significant digits), so each value must lie within half a unit of the
+    printed last digit (rows whose exact value t^2/2 sits on a rounding
+    boundary, e.g. 14.045, may print either way)."""
+    kat = np.array(_load("dopr5_kat.json")["rows"])
+    x, t, k = oracle.dopr5_kat()
+    assert k == kat.shape[0] == 101
+    for (xr, tr), xo, to in zip(kat, x, t):
+        for ref, got in ((xr, xo), (tr, to)):
+            if ref == 0.0:
+                assert abs(got) < 5e-4
+                continue
+            half_unit = 0.5e-3 * 10.0 ** np.floor(np.log10(abs(ref)))
+            assert abs(got - ref) <= half_unit * 1.0001, (ref, got)
+
+
+def test_radloss_matches_python_restatement(oracle):
+    """docs/torch_manual/gas_cool.py's radloss equals heatCool.F90 Radloss."""
+    g = _load("gas_cool.json")
+    for T, ref in zip(g["T"], g["radloss"]):
+        assert oracle.lib().orc_radloss(T) == ref
+
+
+def test_cool_table_decodes_losslessly(oracle):
+    import hashlib
+    from torch_gb300 import tables
+    chk = _load("cool_table_check.json")
+    logT, logn, logL = tables.read_compact()
+    h = hashlib.sha256()
+    for a in (logT, logn, logL):
+        h.update(np.ascontiguousarray(a, "<i4").tobytes())
+    assert h.hexdigest() == chk["sha256_ilog"]
+    t = oracle.table_from_ilog(logT, logn, logL)
+    T, n, L = tables.table_values(logT, logn, logL)
+    assert np.array_equal(np.array(t.T), T) and np.array_equal(np.array(t.n), n)
+    assert np.array_equal(np.array(t.lam), L)
+
+
+@pytest.mark.skipif(not os.path.exists("/root/reference/cool.dat"), reason="reference tree absent")
+def test_flash_reader_equals_compact(oracle):
+    from torch_gb300 import tables
+    a = oracle.table_load_flash("/root/reference/cool.dat")
+    b = oracle.table_from_ilog(*tables.read_compact())
+    assert np.array_equal(np.array(a.lam), np.array(b.lam))
+    assert np.array_equal(np.array(a.T), np.array(b.T))
+
+
+def test_find_semantics(oracle):
+    """find.F90: largest x(i) <= x0, 0 below, N above; the repeated last
+    entries of the table axes return N-1 for x0 == x(N)."""
+    x = np.array([1.0, 2.0, 3.0, 3.0, 3.0])
+    f = lambda v: oracle.lib().orc_find(x, v, 5)
+    assert f(0.5) == 0 and f(1.0) == 1 and f(2.5) == 2 and f(3.0) == 4 and f(3.5) == 5
+
+
+@pytest.mark.parametrize("mhd", [False, True])
+def test_eigensystem(oracle, mhd):
+    """L R = I and R diag(lambda) L = A(W), the primitive Jacobian, including
+    the degenerate cases B_perp = 0 and B_n = 0."""
+    rng = np.random.default_rng(7)
+    gam = 5.0 / 3.0
+    nw = 7 if mhd else 5
+    for it in range(300):
+        q = np.array([rng.uniform(0.1, 2), rng.normal(), rng.normal(), rng.normal(),
+                      rng.uniform(0.1, 2), rng.normal(), rng.normal(), rng.normal()])
+        if it % 7 == 0:
+            q[6] = q[7] = 0.0
+        if it % 7 == 1:
+            q[5] = 0.0
+        lam, Rm, Lm = oracle.eig(mhd, gam, q)
+        Rm, Lm = Rm[:nw, :nw], Lm[:nw, :nw]
+        assert np.abs(Lm @ Rm - np.eye(nw)).max() < 1e-12
+        rho, u, v, w, p, bn, b1, b2 = q
+        A = np.zeros((nw, nw))
+        A[0, 0] = u; A[0, 1] = rho; A[1, 1] = u; A[1, 4] = 1 / rho; A[2, 2] = u; A[3, 3] = u
+        A[4, 1] = gam * p; A[4, 4] = u
+        if mhd:
+            A[1, 5] = b1 / rho; A[1, 6] = b2 / rho; A[2, 5] = -bn / rho; A[3, 6] = -bn / rho
+            A[5, 1] = b1; A[5, 2] = -bn; A[5, 5] = u; A[6, 1] = b2; A[6, 3] = -bn; A[6, 6] = u
+        assert np.abs(Rm @ np.diag(lam[:nw]) @ Lm - A).max() < 1e-12 * (1 + np.abs(A).max())
+
+
+def _box(mhd, seed, mach, sig):
+    from torch_gb300 import workloads as W
+    return W.turbulent_box(2, 2, 2, seed=seed, sigma_ln=sig, mach=mach, mhd=mhd, nvar=10)
+
+
+@pytest.mark.parametrize("mhd", [False, True])
+def test_oracle_conservation(oracle, mhd):
+    """Mass, momentum and total energy to round-off over a periodic box
+    (a Mach-1 case where the dual-energy switch never fires), div B to
+    round-off."""
+    ic = _box(mhd, 5, 1.0, 0.3)
+    p = oracle.hydro_params(mhd)
+    u, fx, fy, fz, dx = ic["u"], ic["fx"], ic["fy"], ic["fz"], ic["dx"]
+    oracle.fill_guards_periodic(p, 2, 2, 2, u, fx, fy, fz)
+    t0 = oracle.totals(p, u, fx, fy, fz, dx, dx, dx)
+    for _ in range(3):
+        dt = 0.8 * oracle.dt_limit(p, u, dx, dx, dx)
+        oracle.fill_guards_periodic(p, 2, 2, 2, u, fx, fy, fz)
+        oracle.unsplit_blocks(p, u, fx, fy, fz, dt, dx, dx, dx)
+    t1 = oracle.totals(p, u, fx, fy, fz, dx, dx, dx)
+    scale = np.sqrt(t0[0] * t0[4])
+    assert abs(t1[0] - t0[0]) < 1e-13 * t0[0]
+    assert np.all(np.abs(t1[1:4] - t0[1:4]) < 1e-13 * scale)
+    assert abs(t1[4] - t0[4]) < 1e-13 * t0[4]
+    if mhd:
+        assert t1[5] < 1e-12
+
+
+def test_oracle_sod_shock_tube(oracle):
+    """Sod's problem along x: density at t = 0.1 against the exact Riemann
+    solution (L1 error of a 2nd-order scheme at 128 cells)."""
+    from torch_gb300 import workloads as W
+    nbx = 8
+    NX = nbx * 16
+    x = (np.arange(NX) + 0.5) / NX
+    # two mirrored Sod problems on the periodic line: left state in the middle
+    left = (x > 0.25) & (x < 0.75)
+    rho = np.where(left, 1.0, 0.125)
+    pres = np.where(left, 1.0, 0.1)
+    gam = 1.4
+    shape = (NX, 16, 16)
+    rho3 = np.broadcast_to(rho[:, None, None], shape).copy()
+    p3 = np.broadcast_to(pres[:, None, None], shape).copy()
+    zero = np.zeros(shape)
+    eint = p3 / ((gam - 1) * rho3)
+    u = W.global_to_blocks({0: rho3, 1: zero, 2: zero, 3: zero, 4: p3, 5: eint, 6: eint}, nbx, 1, 1, 10)
+    p = oracle.hydro_params(False, gamma=gam)
+    dx = 1.0 / NX
+    t = 0.0
+    while t < 0.1 - 1e-12:
+        oracle.fill_guards_periodic(p, nbx, 1, 1, u)
+        dt = min(0.8 * oracle.dt_limit(p, u, dx, dx, dx), 0.1 - t)
+        oracle.unsplit_blocks(p, u, None, None, None, dt, dx, dx, dx)
+        t += dt
+    num = np.concatenate([u[b, 0, 10, 10, 4:20] for b in range(nbx)])
+    ex = _sod_exact(x, 0.1, gam)
+    l1 = np.mean(np.abs(num - ex))
+    assert l1 < 0.01, l1
+
+
+def _sod_exact(x, t, gam):
+    """Exact density of the mirrored Sod problem: high state (1, 1) on
+    (0.25, 0.75), low state (0.125, 0.1) outside, at time t."""
+    from scipy.optimize import brentq
+    rl, pl, rr, pr = 1.0, 1.0, 0.125, 0.1
+    cl, cr = np.sqrt(gam * pl / rl), np.sqrt(gam * pr / rr)
+
+    def f(p, rk, pk, ck):
+        if p > pk:
+            A, B = 2 / ((gam + 1) * rk), (gam - 1) / (gam + 1) * pk
+            return (p - pk) * np.sqrt(A / (p + B))
+        return 2 * ck / (gam - 1) * ((p / pk) ** ((gam - 1) / (2 * gam)) - 1)
+
+    ps = brentq(lambda p: f(p, rl, pl, cl) + f(p, rr, pr, cr), 1e-6, 10)
+    us = 0.5 * (f(ps, rr, pr, cr) - f(ps, rl, pl, cl))
+    rsl = rl * (ps / pl) ** (1 / gam)
+    g1 = (gam - 1) / (gam + 1)
+    rsr = rr * ((ps / pr + g1) / (g1 * ps / pr + 1))
+    s_shock = rsr * us / (rsr - rr)
+    csl = cl * (ps / pl) ** ((gam - 1) / (2 * gam))
+
+    def standard(xi):  # high state left of the interface, xi = (x - x0) / t
+        if xi < -cl:
+            return rl
+        if xi < us - csl:
+            c = 2 / (gam + 1) * (cl - (gam - 1) / 2 * xi)
+            return rl * (c / cl) ** (2 / (gam - 1))
+        if xi < us:
+            return rsl
+        if xi < s_shock:
+            return rsr
+        return rr
+
+    return np.array([standard((0.25 - xv) / t) if xv < 0.5 else standard((xv - 0.75) / t) for xv in x])

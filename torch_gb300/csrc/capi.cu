@@ -1,0 +1,490 @@
+// C ABI entry points, registration, guard-cell fill and host-side driving
+// of the hydro step.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "gb_state.h"
+#include "hydro_dev.cuh"
+
+gb_state_t g_gb;
+
+static char g_err[512] = "";
+
+void gb_set_error(const char* fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+}
+
+int gb_check(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return 0;
+    gb_set_error("%s: %s", what, cudaGetErrorString(e));
+    return 1;
+}
+
+extern "C" const char* gb_last_error(void) { return g_err; }
+extern "C" int gb_version(void) { return 1; }
+
+int gb_ensure_scratch(size_t bytes)
+{
+    if (bytes <= g_gb.scratch_bytes) return GB_OK;
+    if (g_gb.d_scratch) cudaFree(g_gb.d_scratch);
+    g_gb.d_scratch = nullptr;
+    g_gb.scratch_bytes = 0;
+    if (gb_check(cudaMalloc(&g_gb.d_scratch, bytes), "cudaMalloc(scratch)")) return GB_ERR_CUDA;
+    g_gb.scratch_bytes = bytes;
+    return GB_OK;
+}
+
+int gb_ensure_stage(size_t bytes)
+{
+    if (bytes <= g_gb.stage_bytes) return GB_OK;
+    if (g_gb.d_stage) cudaFree(g_gb.d_stage);
+    g_gb.d_stage = nullptr;
+    g_gb.stage_bytes = 0;
+    if (gb_check(cudaMalloc(&g_gb.d_stage, bytes), "cudaMalloc(stage)")) return GB_ERR_CUDA;
+    g_gb.stage_bytes = bytes;
+    return GB_OK;
+}
+
+// ---------------------------------------------------------------- status
+extern "C" int gb_status_reset(gb_status* st, void* stream)
+{
+    if (!st) return GB_ERR_ARG;
+    return gb_check(cudaMemsetAsync(st, 0, sizeof(gb_status), (cudaStream_t)stream), "status reset")
+               ? GB_ERR_CUDA
+               : GB_OK;
+}
+
+extern "C" int gb_status_read(const gb_status* st, gb_status* host)
+{
+    if (!st || !host) return GB_ERR_ARG;
+    return gb_check(cudaMemcpy(host, st, sizeof(gb_status), cudaMemcpyDeviceToHost), "status read")
+               ? GB_ERR_CUDA
+               : GB_OK;
+}
+
+// ---------------------------------------------------------------- registration
+extern "C" int gb_register_grid(const gb_grid_desc* grid, const gb_tree_desc* tree)
+{
+    if (!grid || !grid->unk || grid->nvar <= 0 || grid->maxblocks <= 0) {
+        gb_set_error("gb_register_grid: bad grid descriptor");
+        return GB_ERR_ARG;
+    }
+    for (int r = 0; r < GB_NROLE; ++r)
+        if (grid->slot[r] >= grid->nvar) {
+            gb_set_error("gb_register_grid: slot of role %d beyond nvar", r);
+            return GB_ERR_ARG;
+        }
+    for (int r = GB_DENS; r <= GB_EINT; ++r)
+        if (grid->slot[r] < 0) {
+            gb_set_error("gb_register_grid: hydro role %d has no slot", r);
+            return GB_ERR_ARG;
+        }
+    g_gb.desc = *grid;
+    g_gb.grid.nvar = grid->nvar;
+    g_gb.grid.maxblocks = grid->maxblocks;
+    memcpy(g_gb.grid.slot, grid->slot, sizeof grid->slot);
+    g_gb.grid.unk = grid->unk;
+    g_gb.grid.f[0] = grid->facex;
+    g_gb.grid.f[1] = grid->facey;
+    g_gb.grid.f[2] = grid->facez;
+    g_gb.grid.level = nullptr;
+    g_gb.grid_ok = true;
+    g_gb.tree_ok = false;
+    if (tree) {
+        if (tree->nnodes < grid->maxblocks || !tree->level || !tree->coord || !tree->child || !tree->root ||
+            tree->nrx <= 0 || tree->nry <= 0 || tree->nrz <= 0 || tree->maxlevel < 0 || tree->maxlevel > 20) {
+            gb_set_error("gb_register_grid: bad tree descriptor");
+            return GB_ERR_ARG;
+        }
+        g_gb.tree = *tree;
+        g_gb.grid.level = tree->level;
+        g_gb.tree_ok = true;
+    }
+    return GB_OK;
+}
+
+extern "C" int gb_hydro_init(const gb_hydro_params* p)
+{
+    if (!p || !(p->gamma > 1.0) || p->precision < 0 || p->precision > 1) {
+        gb_set_error("gb_hydro_init: bad parameters");
+        return GB_ERR_ARG;
+    }
+    g_gb.hp = *p;
+    g_gb.hydro_ok = true;
+    if (!g_gb.d_dtmin && gb_check(cudaMalloc(&g_gb.d_dtmin, sizeof(unsigned long long)), "cudaMalloc(dtmin)"))
+        return GB_ERR_CUDA;
+    return GB_OK;
+}
+
+// ---------------------------------------------------------------- guard fill
+namespace {
+
+struct leaf_hit {
+    int node, level;
+};
+
+__device__ __forceinline__ leaf_hit find_leaf(const gb_tree_desc& t, long long X, long long Y, long long Z)
+{
+    const long long S0 = (long long)GB_NXB << t.maxlevel;
+    int rx = (int)(X / S0), ry = (int)(Y / S0), rz = (int)(Z / S0);
+    int node = t.root[rx + t.nrx * (ry + t.nry * rz)];
+    int l = 0;
+    for (int it = 0; it <= t.maxlevel && node >= 0; ++it) {
+        int c0 = t.child[8 * node];
+        if (c0 < 0) break;
+        long long half = S0 >> (l + 1);
+        int cx = (int)((X / half) & 1), cy = (int)((Y / half) & 1), cz = (int)((Z / half) & 1);
+        node = t.child[8 * node + (cx | (cy << 1) | (cz << 2))];
+        ++l;
+    }
+    leaf_hit h;
+    h.node = node;
+    h.level = node >= 0 ? t.level[node] : 0;
+    return h;
+}
+
+__device__ __forceinline__ long long wrap(long long x, long long n) { return ((x % n) + n) % n; }
+
+__global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list)
+{
+    const int blk = list[blockIdx.y];
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= GB_N3) return;
+    const int i = c % GB_N, j = (c / GB_N) % GB_N, k = c / (GB_N * GB_N);
+    if (i >= GB_NGUARD && i < GB_NGUARD + GB_NXB && j >= GB_NGUARD && j < GB_NGUARD + GB_NXB &&
+        k >= GB_NGUARD && k < GB_NGUARD + GB_NXB)
+        return;
+    const int L = t.level[blk];
+    const long long s = 1LL << (t.maxlevel - L);
+    const long long N[3] = {(long long)t.nrx * GB_NXB << t.maxlevel, (long long)t.nry * GB_NXB << t.maxlevel,
+                            (long long)t.nrz * GB_NXB << t.maxlevel};
+    const int* cd = t.coord + 3 * blk;
+    const int loc[3] = {i, j, k};
+    long long lo[3], X[3];
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = wrap(((long long)cd[d] * GB_NXB + loc[d] - GB_NGUARD) * s, N[d]);
+        X[d] = lo[d] + s / 2;
+    }
+    leaf_hit h = find_leaf(t, X[0], X[1], X[2]);
+    if (h.node < 0) return;
+    const long long sl = 1LL << (t.maxlevel - h.level);
+    const int* sc = t.coord + 3 * h.node;
+    double* dst = g.unk + (int64_t)blk * g.nvar * GB_N3 + c;
+    const double* src = g.unk + (int64_t)h.node * g.nvar * GB_N3;
+    if (h.level <= L) {
+        // same level: copy; coarser: injection of the covering coarse cell
+        int si = (int)(X[0] / sl - (long long)sc[0] * GB_NXB) + GB_NGUARD;
+        int sj = (int)(X[1] / sl - (long long)sc[1] * GB_NXB) + GB_NGUARD;
+        int sk = (int)(X[2] / sl - (long long)sc[2] * GB_NXB) + GB_NGUARD;
+        int sci = gb_cidx(si, sj, sk);
+        for (int v = 0; v < g.nvar; ++v) dst[(int64_t)v * GB_N3] = src[(int64_t)v * GB_N3 + sci];
+    } else {
+        // finer neighbour: mean of the fine cells covering this cell
+        int r = (int)(s / sl);
+        int bi = (int)(lo[0] / sl - (long long)sc[0] * GB_NXB) + GB_NGUARD;
+        int bj = (int)(lo[1] / sl - (long long)sc[1] * GB_NXB) + GB_NGUARD;
+        int bk = (int)(lo[2] / sl - (long long)sc[2] * GB_NXB) + GB_NGUARD;
+        double inv = 1.0 / (double)(r * r * r);
+        for (int v = 0; v < g.nvar; ++v) {
+            double acc = 0.0;
+            for (int z = 0; z < r; ++z)
+                for (int y = 0; y < r; ++y)
+                    for (int x = 0; x < r; ++x) acc += src[(int64_t)v * GB_N3 + gb_cidx(bi + x, bj + y, bk + z)];
+            dst[(int64_t)v * GB_N3] = acc * inv;
+        }
+    }
+}
+
+__global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list)
+{
+    const int a = blockIdx.z;
+    const int blk = list[blockIdx.y];
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= GB_FSZ) return;
+    int I[3];
+    if (a == 0) { I[0] = f % (GB_N + 1); I[1] = (f / (GB_N + 1)) % GB_N; I[2] = f / ((GB_N + 1) * GB_N); }
+    else if (a == 1) { I[0] = f % GB_N; I[1] = (f / GB_N) % (GB_N + 1); I[2] = f / (GB_N * (GB_N + 1)); }
+    else { I[0] = f % GB_N; I[1] = (f / GB_N) % GB_N; I[2] = f / (GB_N * GB_N); }
+    bool own = true;
+    for (int e = 0; e < 3; ++e) {
+        int top = GB_NGUARD + GB_NXB - 1 + (e == a);
+        if (I[e] < GB_NGUARD || I[e] > top) own = false;
+    }
+    if (own) return;
+    const int L = t.level[blk];
+    const long long s = 1LL << (t.maxlevel - L);
+    const long long N[3] = {(long long)t.nrx * GB_NXB << t.maxlevel, (long long)t.nry * GB_NXB << t.maxlevel,
+                            (long long)t.nrz * GB_NXB << t.maxlevel};
+    const int* cd = t.coord + 3 * blk;
+    long long lo[3], X[3];
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = wrap(((long long)cd[d] * GB_NXB + I[d] - GB_NGUARD) * s, N[d]);
+        X[d] = lo[d] + (d == a ? 0 : s / 2);
+    }
+    leaf_hit h = find_leaf(t, X[0], X[1], X[2]);
+    if (h.node < 0) return;
+    const long long sl = 1LL << (t.maxlevel - h.level);
+    const int* sc = t.coord + 3 * h.node;
+    const double* src = g.f[a] + (int64_t)h.node * GB_FSZ;
+    double* dst = g.f[a] + (int64_t)blk * GB_FSZ + f;
+    if (h.level <= L) {
+        int S[3];
+        for (int d = 0; d < 3; ++d) S[d] = (int)(X[d] / sl - (long long)sc[d] * GB_NXB) + GB_NGUARD;
+        if (X[a] % sl == 0) {
+            *dst = src[gb_fidx(a, S[0], S[1], S[2])];
+        } else {
+            // fine face inside a coarse cell: mean of the two coarse faces
+            int S1[3] = {S[0], S[1], S[2]};
+            S1[a] += 1;
+            *dst = 0.5 * (src[gb_fidx(a, S[0], S[1], S[2])] + src[gb_fidx(a, S1[0], S1[1], S1[2])]);
+        }
+    } else {
+        // finer neighbour: area mean of the fine faces on this face
+        int r = (int)(s / sl);
+        int B[3];
+        for (int d = 0; d < 3; ++d) B[d] = (int)(lo[d] / sl - (long long)sc[d] * GB_NXB) + GB_NGUARD;
+        int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+        double acc = 0.0;
+        for (int y = 0; y < r; ++y)
+            for (int x = 0; x < r; ++x) {
+                int Q[3] = {B[0], B[1], B[2]};
+                Q[t1] += x;
+                Q[t2] += y;
+                acc += src[gb_fidx(a, Q[0], Q[1], Q[2])];
+            }
+        *dst = acc / (double)(r * r);
+    }
+}
+
+__global__ void k_dt_finish(const unsigned long long* bits, double cfl, double* out)
+{
+    *out = cfl * __longlong_as_double((long long)*bits);
+}
+
+__global__ void k_flash_to_soa(const double* __restrict__ in, int nunk, const int* __restrict__ hslot,
+                               gb_dev_grid g, int nblocks)
+{
+    // in: unk(nunk, 24, 24, 24, nblocks) Fortran order (variable fastest)
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t total = (int64_t)nblocks * GB_N3;
+    if (idx >= total) return;
+    int blk = (int)(idx / GB_N3), c = (int)(idx % GB_N3);
+    const double* cell = in + idx * nunk;
+    for (int r = 0; r < GB_NROLE; ++r) {
+        int hs = hslot[r], ds = g.slot[r];
+        if (hs >= 0 && ds >= 0) g.unk[((int64_t)blk * g.nvar + ds) * GB_N3 + c] = cell[hs];
+    }
+}
+
+__global__ void k_soa_to_flash(double* __restrict__ out, int nunk, const int* __restrict__ hslot,
+                               gb_dev_grid g, int nblocks)
+{
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t total = (int64_t)nblocks * GB_N3;
+    if (idx >= total) return;
+    int blk = (int)(idx / GB_N3), c = (int)(idx % GB_N3);
+    double* cell = out + idx * nunk;
+    for (int r = 0; r < GB_NROLE; ++r) {
+        int hs = hslot[r], ds = g.slot[r];
+        if (hs >= 0 && ds >= 0) cell[hs] = g.unk[((int64_t)blk * g.nvar + ds) * GB_N3 + c];
+    }
+}
+
+}  // namespace
+
+int gb_launch_guardfill(int nblk, const int* list, cudaStream_t s)
+{
+    dim3 gc((GB_N3 + 127) / 128, nblk);
+    k_guard_cells<<<gc, 128, 0, s>>>(g_gb.grid, g_gb.tree, list);
+    if (g_gb.hp.mhd && g_gb.grid.f[0]) {
+        dim3 gf((GB_FSZ + 127) / 128, nblk, 3);
+        k_guard_faces<<<gf, 128, 0, s>>>(g_gb.grid, g_gb.tree, list);
+    }
+    return gb_check(cudaGetLastError(), "guard fill") ? GB_ERR_CUDA : GB_OK;
+}
+
+extern "C" int gb_fill_guardcells(int blockCount, const int* list, void* stream)
+{
+    if (!g_gb.grid_ok || !g_gb.tree_ok) {
+        gb_set_error("gb_fill_guardcells: register a grid with a block tree first");
+        return GB_ERR_NOT_INIT;
+    }
+    if (blockCount < 0 || (blockCount > 0 && !list)) return GB_ERR_ARG;
+    if (blockCount == 0) return GB_OK;
+    // the face pass needs to know whether face fields exist; it is keyed on
+    // the hydro parameters when set and on the grid otherwise
+    dim3 gc((GB_N3 + 127) / 128, blockCount);
+    k_guard_cells<<<gc, 128, 0, (cudaStream_t)stream>>>(g_gb.grid, g_gb.tree, list);
+    if (g_gb.grid.f[0] && g_gb.grid.f[1] && g_gb.grid.f[2]) {
+        dim3 gf((GB_FSZ + 127) / 128, blockCount, 3);
+        k_guard_faces<<<gf, 128, 0, (cudaStream_t)stream>>>(g_gb.grid, g_gb.tree, list);
+    }
+    return gb_check(cudaGetLastError(), "guard fill") ? GB_ERR_CUDA : GB_OK;
+}
+
+// ---------------------------------------------------------------- hydro
+size_t gb_hydro_scratch_bytes_fp64();
+size_t gb_hydro_scratch_bytes_mixed();
+int gb_hydro_chunk_fp64(const gbh::hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
+                        void* scratch, gb_status* st, cudaStream_t s);
+int gb_hydro_chunk_mixed(const gbh::hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
+                         void* scratch, gb_status* st, cudaStream_t s);
+int gb_dt_launch(const gbh::hydro_kparams& kp, int mhd, int nblk, const int* list,
+                 unsigned long long* bits, cudaStream_t s);
+
+static int g_chunk_blocks = 16;
+
+extern "C" int gb_set_chunk_blocks(int n)
+{
+    if (n < 1 || n > 65535) return GB_ERR_ARG;
+    g_chunk_blocks = n;
+    return GB_OK;
+}
+
+static gbh::hydro_kparams make_kp(double dt)
+{
+    gbh::hydro_kparams kp;
+    kp.gamma = g_gb.hp.gamma;
+    kp.cvisc = g_gb.hp.cvisc;
+    kp.eint_switch = g_gb.hp.eint_switch;
+    kp.smlrho = g_gb.hp.smlrho;
+    kp.smallp = g_gb.hp.smallp;
+    kp.use_avisc = g_gb.hp.use_avisc;
+    kp.dt = dt;
+    if (g_gb.tree_ok) {
+        kp.dx[0] = g_gb.tree.root_dx[0];
+        kp.dx[1] = g_gb.tree.root_dx[1];
+        kp.dx[2] = g_gb.tree.root_dx[2];
+    } else {
+        kp.dx[0] = kp.dx[1] = kp.dx[2] = 1.0;
+    }
+    return kp;
+}
+
+int gb_launch_hydro(int nblk, const int* list, double dt, int cool, gb_status* st, cudaStream_t s)
+{
+    const int chunk = g_chunk_blocks < nblk ? g_chunk_blocks : nblk;
+    const bool mixed = g_gb.hp.precision == 1;
+    size_t per = mixed ? gb_hydro_scratch_bytes_mixed() : gb_hydro_scratch_bytes_fp64();
+    int rc = gb_ensure_scratch(per * (size_t)chunk);
+    if (rc) return rc;
+    gbh::hydro_kparams kp = make_kp(dt);
+    for (int b0 = 0; b0 < nblk; b0 += chunk) {
+        int nb = nblk - b0 < chunk ? nblk - b0 : chunk;
+        rc = mixed ? gb_hydro_chunk_mixed(kp, g_gb.hp.mhd, cool, nb, list + b0, g_gb.d_scratch, st, s)
+                   : gb_hydro_chunk_fp64(kp, g_gb.hp.mhd, cool, nb, list + b0, g_gb.d_scratch, st, s);
+        if (rc) return rc;
+    }
+    return GB_OK;
+}
+
+extern "C" int gb_hydro_unsplit(int blockCount, const int* list, double dt, double dtOld, gb_status* st,
+                                void* stream)
+{
+    (void)dtOld;
+    if (!g_gb.grid_ok || !g_gb.hydro_ok) {
+        gb_set_error("gb_hydro_unsplit: call gb_register_grid and gb_hydro_init first");
+        return GB_ERR_NOT_INIT;
+    }
+    if (blockCount < 0 || (blockCount > 0 && !list) || !(dt > 0.0)) return GB_ERR_ARG;
+    if (g_gb.hp.mhd && (!g_gb.grid.f[0] || !g_gb.grid.f[1] || !g_gb.grid.f[2] || g_gb.grid.slot[GB_MAGX] < 0 ||
+                        g_gb.grid.slot[GB_MAGY] < 0 || g_gb.grid.slot[GB_MAGZ] < 0)) {
+        gb_set_error("gb_hydro_unsplit: MHD needs face fields and MAG slots");
+        return GB_ERR_ARG;
+    }
+    if (blockCount == 0) return GB_OK;
+    return gb_launch_hydro(blockCount, list, dt, 0, st, (cudaStream_t)stream);
+}
+
+int gb_launch_dt(int nblk, const int* list, double* dt_out, cudaStream_t s)
+{
+    const unsigned long long inf_bits = 0x7FF0000000000000ULL;
+    if (gb_check(cudaMemcpyAsync(g_gb.d_dtmin, &inf_bits, sizeof inf_bits, cudaMemcpyHostToDevice, s),
+                 "dt init"))
+        return GB_ERR_CUDA;
+    gbh::hydro_kparams kp = make_kp(1.0);
+    int rc = gb_dt_launch(kp, g_gb.hp.mhd, nblk, list, (unsigned long long*)g_gb.d_dtmin, s);
+    if (rc) return rc;
+    k_dt_finish<<<1, 1, 0, s>>>((const unsigned long long*)g_gb.d_dtmin, g_gb.hp.cfl, dt_out);
+    return gb_check(cudaGetLastError(), "k_dt_finish") ? GB_ERR_CUDA : GB_OK;
+}
+
+extern "C" int gb_compute_dt(int blockCount, const int* list, double* dt_dev, void* stream)
+{
+    if (!g_gb.grid_ok || !g_gb.hydro_ok) {
+        gb_set_error("gb_compute_dt: call gb_register_grid and gb_hydro_init first");
+        return GB_ERR_NOT_INIT;
+    }
+    if (blockCount <= 0 || !list || !dt_dev) return GB_ERR_ARG;
+    return gb_launch_dt(blockCount, list, dt_dev, (cudaStream_t)stream);
+}
+
+extern "C" int gb_evolve_step(int blockCount, const int* list, double dt, int cool, gb_status* st,
+                              void* stream)
+{
+    if (!g_gb.grid_ok || !g_gb.hydro_ok || !g_gb.tree_ok) {
+        gb_set_error("gb_evolve_step: register grid + tree and call gb_hydro_init first");
+        return GB_ERR_NOT_INIT;
+    }
+    if (cool && !g_gb.cool_ok) {
+        gb_set_error("gb_evolve_step: cooling requested before gb_cool_init");
+        return GB_ERR_NOT_INIT;
+    }
+    if (cool && (g_gb.grid.slot[GB_TEMP] < 0 || g_gb.grid.slot[GB_TDUS] < 0)) {
+        gb_set_error("gb_evolve_step: cooling needs TEMP and TDUS slots");
+        return GB_ERR_ARG;
+    }
+    if (blockCount <= 0 || !list || !(dt > 0.0)) return GB_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = gb_launch_guardfill(blockCount, list, s);
+    if (rc) return rc;
+    return gb_launch_hydro(blockCount, list, dt, cool, st, s);
+}
+
+// ---------------------------------------------------------------- host I/O
+static int flash_copy(bool up, double* host, int nunk, const int* host_slot, int nblocks, void* stream)
+{
+    if (!g_gb.grid_ok) {
+        gb_set_error("grid transfer before gb_register_grid");
+        return GB_ERR_NOT_INIT;
+    }
+    if (!host || !host_slot || nunk <= 0 || nblocks <= 0 || nblocks > g_gb.grid.maxblocks) return GB_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    size_t bytes = (size_t)nblocks * GB_N3 * nunk * sizeof(double);
+    int rc = gb_ensure_stage(bytes + GB_NROLE * sizeof(int));
+    if (rc) return rc;
+    int* dslot = (int*)((char*)g_gb.d_stage + bytes);
+    if (gb_check(cudaMemcpyAsync(dslot, host_slot, GB_NROLE * sizeof(int), cudaMemcpyHostToDevice, s), "slot copy"))
+        return GB_ERR_CUDA;
+    int64_t total = (int64_t)nblocks * GB_N3;
+    unsigned nb = (unsigned)((total + 255) / 256);
+    if (up) {
+        if (gb_check(cudaMemcpyAsync(g_gb.d_stage, host, bytes, cudaMemcpyHostToDevice, s), "upload")) return GB_ERR_CUDA;
+        k_flash_to_soa<<<nb, 256, 0, s>>>(g_gb.d_stage, nunk, dslot, g_gb.grid, nblocks);
+        if (gb_check(cudaGetLastError(), "k_flash_to_soa")) return GB_ERR_CUDA;
+    } else {
+        k_soa_to_flash<<<nb, 256, 0, s>>>(g_gb.d_stage, nunk, dslot, g_gb.grid, nblocks);
+        if (gb_check(cudaGetLastError(), "k_soa_to_flash")) return GB_ERR_CUDA;
+        if (gb_check(cudaMemcpyAsync(host, g_gb.d_stage, bytes, cudaMemcpyDeviceToHost, s), "download"))
+            return GB_ERR_CUDA;
+    }
+    return GB_OK;
+}
+
+extern "C" int gb_grid_upload_flash(const double* unk_host, int nunk, const int* host_slot, int nblocks,
+                                    void* stream)
+{
+    return flash_copy(true, const_cast<double*>(unk_host), nunk, host_slot, nblocks, stream);
+}
+
+extern "C" int gb_grid_download_flash(double* unk_host, int nunk, const int* host_slot, int nblocks,
+                                      void* stream)
+{
+    return flash_copy(false, unk_host, nunk, host_slot, nblocks, stream);
+}

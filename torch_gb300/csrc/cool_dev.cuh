@@ -1,0 +1,499 @@
+// Per-cell heating/cooling solver on the device (FP64).
+//
+// Device restatement of heating_and_cooling's "Implicit" branch and the
+// rate terms it calls, from
+//   src/flash/source/physics/sourceTerms/Heat/HeatMain/HeatCool/phenHeat/
+//   mol_and_dust/solver/heatCool.F90
+// Operand order follows the Fortran; the file that includes this header is
+// compiled with -fmad=false so rounding matches a plain -O2 Fortran build
+// except where CUDA's pow/exp differ from the host libm by an ulp. Every
+// loop has the Fortran's iteration cap; where the Fortran prints and stops
+// the device records a status code and returns a defined value.
+#pragma once
+
+#include "gb_common.cuh"
+
+#define GB_TEMP_PTS 320
+#define GB_DENS_PTS 190
+
+struct gb_cool_ctx {
+    gb_cool_params p;
+    const double* T;    // cool_dat(1, :, 1), TEMP_PTS
+    const double* n;    // cool_dat(:, 1, 2), DENS_PTS
+    const double* lam;  // cool_dat(:, :, 3), dens fastest
+    double T_min, nd_min;
+};
+
+struct gb_cool_vars {
+    double ndens, rho, conf, Gflux, ephen, tdust, TtoEI, xHp, strat_factor, mu_mol;
+};
+
+struct gb_cool_diag {
+    int bracket_fail, dust_noconv, unbracketed, maxiter, iters;
+};
+
+namespace gbcool {
+
+__device__ __forceinline__ double fmx(double a, double b) { return a > b ? a : b; }
+__device__ __forceinline__ double fmn(double a, double b) { return a < b ? a : b; }
+
+__device__ __forceinline__ double lin_interp(double x1, double y1, double x2, double y2, double x)
+{
+    // heatCool.F90:2379-2392
+    double ms = (y2 - y1) / (x2 - x1);
+    return ms * (x - x1) + y1;
+}
+
+__device__ __forceinline__ int find(const double* x, double x0, int N)
+{
+    // find.F90:9-42 (1-based result)
+    if (x0 < __ldg(x)) return 0;
+    if (x0 > __ldg(x + N - 1)) return N;
+    int il = 1, ir = N;
+    while (ir != il + 1) {
+        int im = (il + ir) / 2;
+        if (__ldg(x + im - 1) > x0) ir = im;
+        else il = im;
+    }
+    return il;
+}
+
+static __device__ double radloss(double T)
+{
+    // heatCool.F90:1590-1667
+    double radia;
+    if (T >= 1.70e4) {
+        if (T >= 5.62e5) {
+            if (T >= 2.75e6) {
+                if (T >= 3.16e7) radia = 3.090e-27 * sqrt(T);
+                else radia = 5.188e-21 / pow(T, 0.33);
+            } else {
+                if (T >= 1.78e6) radia = 3.890e-4 / pow(T, 2.95);
+                else radia = 1.3e-22 * pow(T / 1.5e5, 0.01);
+            }
+        } else {
+            if (T >= 7.94e4) {
+                if (T >= 2.51e5) radia = 3.98e-11 / (T * T);
+                else radia = 6.31e-22 * pow(T / 1.e6, 0.01);
+            } else {
+                if (T >= 3.98e4) radia = 1.e-31 * (T * T);
+                else radia = 1.479e-21 / pow(T, 0.216);
+            }
+        }
+    } else {
+        if (T >= 1.e3) {
+            if (T >= 6.31e3) {
+                if (T >= 1.0e4) radia = 7.63e-81 * pow(T, 13.8);
+                else radia = 3.13e-27 * pow(T, 0.396);
+            } else {
+                if (T >= 3.16e3) radia = 2.64e-26 * pow(T, 0.152);
+                else radia = 5.28e-27 * pow(T, 0.352);
+            }
+        } else {
+            if (T >= 3.98e1) {
+                if (T >= 2.00e2) radia = 3.06e-27 * pow(T, 0.431);
+                else radia = 1.52e-28 * pow(T, 0.997);
+            } else {
+                if (T >= 2.51e1) radia = 2.39e-29 * pow(T, 1.50);
+                else radia = 1.095e-32 * pow(T, 3.885);
+            }
+        }
+    }
+    return radia;
+}
+
+__device__ __forceinline__ double lam_jeans(const gb_cool_params& p, double rho, double n, double T)
+{
+    // heatCool.F90:1687
+    const double pi = 3.1415926535897932384, newton = 6.6725985e-8;
+    return 1.0 / (rho / n) * sqrt(5. / 3. * pi * p.boltz * T / n / newton);
+}
+
+__device__ __forceinline__ double f_ext(const gb_cool_params& p, double rho, double n, double T)
+{
+    // heatCool.F90:1693-1722
+    double lam_j = lam_jeans(p, rho, n, T);
+    double Av = lam_j * n * 0.01 / 1.87e21;
+    return exp(-3.5 * Av);
+}
+
+static __device__ double heating(const gb_cool_params& p, double T, double n, double rho, double strat)
+{
+    // heatCool.F90:890-964
+    double eplus = 0.0, lin;
+    if ((T <= p.theatmax) && (T >= p.theatmin)) {
+        if (p.use_cr_heating) {
+            if (p.crIonNH == 1.0 && p.crIonExp == 1.0) {
+                eplus = strat * p.crIonRate * p.crIonEnergy / (rho / n);
+            } else {
+                double ncol = lam_jeans(p, rho, n, T) * n;
+                eplus = strat * (p.crIonRate * p.crIonEnergy *
+                                 pow(fmx(p.crIonNH, ncol) / p.crIonNH, -p.crIonExp)) /
+                        (rho / n);
+            }
+        }
+        double ll = p.theatmin, ll10 = ll + 0.1 * ll;
+        double ul = p.theatmax, ul10 = ul - 0.1 * ul;
+        if (T >= ul10) lin = lin_interp(ul10, 1.0, ul, 0.0, T);
+        else if (T <= ll10) lin = lin_interp(ll, 0.0, ll10, 1.0, T);
+        else lin = 1.0;
+        eplus = eplus * lin;
+    }
+    return eplus;
+}
+
+static __device__ void pe_heating(const gb_cool_params& p, double G, double xHp, double n, double T,
+                           double rho, double* PeHeat, double* dust_heating)
+{
+    // heatCool.F90:970-1110
+    const double C0 = 7.64, C1 = 4.52, C2 = 0.04371, C3 = 0.00557, C4 = 0.132, C5 = 0.452,
+                 C6 = 0.675;
+    *PeHeat = 0.0;
+    *dust_heating = 0.0;
+    if ((T <= fmn(p.theatmax, p.dust_sputter_temp)) && (T >= p.theatmin)) {
+        double xl = (xHp == 0.0) ? 1e-8 : xHp;
+        double Gfactor, eff;
+        if (p.pe_recipe == 1) {
+            Gfactor = G * sqrt(T) / (xl * n * 0.5);
+            eff = 4.9e-2 / (1.0 + 4.0e-3 * pow(Gfactor, 0.73)) +
+                  (3.7e-2 * pow(T / 1.0e4, 0.7)) / (1.0 + 2.0e-4 * Gfactor);
+            *PeHeat = p.pe_norm * eff * G / (rho / n);
+            *dust_heating = p.pe_norm * fmx(0.0, (1.0 - eff)) * G * n;
+        } else if (p.pe_recipe == 0) {
+            Gfactor = G * sqrt(T) / (xl * n);
+            eff = (C0 + C1 * pow(T, C4)) / (1.0 + (C2 * pow(Gfactor, C5)) * (1.0 + C3 * pow(Gfactor, C6)));
+            *PeHeat = 1e-26 * eff * G / (rho / n);
+            *dust_heating = (p.pe_norm - 1e-26 * eff) * G * n;
+            *dust_heating = fmx(*dust_heating, 0.0);
+        } else {
+            eff = 0.05;
+            *PeHeat = p.pe_norm * eff * G / (rho / n);
+            *dust_heating = p.pe_norm * (1.0 - eff) * G * n;
+        }
+        double ll = p.theatmin, ll10 = ll + 0.1 * ll;
+        double ul = fmn(p.theatmax, p.dust_sputter_temp), ul10 = ul - 0.1 * ul, lin;
+        if (T >= ul10) lin = lin_interp(ul10, 1.0, ul, 0.0, T);
+        else if (T <= ll10) lin = lin_interp(ll, 0.0, ll10, 1.0, T);
+        else lin = 1.0;
+        *PeHeat = *PeHeat * lin;
+    }
+}
+
+static __device__ double cooling(const gb_cool_params& p, double T, double n, double conf, double xHp)
+{
+    // heatCool.F90:1116-1200
+    double emin = 0.0;
+    if ((T <= p.tradmax && T >= p.tradmin) && (n >= p.dradmin && n <= p.dradmax)) {
+        emin = radloss(T);
+        if (xHp > 1e-2 && T < 1.2e4) {
+            double DG = lin_interp(1e-2, 1.0, 1e-1, 5.0, fmn(1e-1, xHp));
+            emin = emin * DG;
+            if (T > 1e4) {
+                double q = lin_interp(1e4, 1.0, 1.2e4, pow(DG, 0.5), T);
+                emin = emin / (q * q);
+            }
+        } else if (xHp < 1e-2 && T < 1e4) {
+            double DG = lin_interp(1e-4, 0.35, 1e-2, 1.0, fmx(1e-4, xHp));
+            emin = emin * DG;
+            if (T > 9e3) emin = emin / lin_interp(9e3, 1.0, 1e4, DG, T);
+        }
+        double ll = p.tradmin, ll10 = ll + 0.1 * ll;
+        double ul = p.tradmax, ul10 = ul - 0.1 * ul, lin;
+        if (T >= ul10) lin = lin_interp(ul10, 1.0, ul, 0.0, T);
+        else if (T <= ll10) lin = lin_interp(ll, 0.0, ll10, 1.0, T);
+        else lin = 1.0;
+        emin = emin * lin;
+        emin = emin * conf;
+    }
+    return emin;
+}
+
+static __device__ double molecular_cooling(const gb_cool_ctx& c, double n, double T, double mu)
+{
+    // heatCool.F90:1211-1303
+    const gb_cool_params& p = c.p;
+    double cool_pw = 0.0;
+    if ((n >= p.nd_cool_min) && (n <= p.nd_cool_max) && (T >= p.T_cool_min) && (T <= p.theatmax)) {
+        int ixtemp = find(c.T, fmx(T, c.T_min), GB_TEMP_PTS);
+        int ixdens = find(c.n, fmx(n, c.nd_min), GB_DENS_PTS);
+        if (ixtemp > 0 && ixtemp <= GB_TEMP_PTS && ixdens > 0 && ixdens <= GB_DENS_PTS)
+            cool_pw = __ldg(c.lam + (ixdens - 1) + GB_DENS_PTS * (ixtemp - 1)) / (mu * p.mp);
+        double ll = p.T_cool_min, ll10 = ll + 0.1 * ll;
+        double ul = p.theatmax, ul10 = ul - 0.1 * ul, lin;
+        if (T >= ul10) lin = lin_interp(ul10, 1.0, ul, 0.0, T);
+        else if (T <= ll10) lin = lin_interp(ll, 0.0, ll10, 1.0, T);
+        else lin = 1.0;
+        cool_pw = cool_pw * lin;
+        ll = p.nd_cool_min; ll10 = ll + 0.1 * ll;
+        ul = p.nd_cool_max; ul10 = ul - 0.1 * ul;
+        if (n >= ul10) lin = lin_interp(ul10, 1.0, ul, 0.0, n);
+        else if (n <= ll10) lin = lin_interp(ll, 0.0, ll10, 1.0, n);
+        else lin = 1.0;
+        cool_pw = cool_pw * lin;
+    }
+    return cool_pw;
+}
+
+__device__ __forceinline__ double dust_cooling(const gb_cool_params& p, double n, double T,
+                                               double tdust, double rho)
+{
+    // heatCool.F90:1305-1390
+    double cool_dg = 0.0;
+    if (T <= p.dust_sputter_temp) {
+        double lambda_gd = 3.8e-33 * (n * n) * (1.0 - 0.8 * exp(-75.0 / T)) * (T - tdust) * sqrt(T);
+        cool_dg = lambda_gd / rho;
+        double ul = p.dust_sputter_temp, ul10 = ul - 0.1 * ul, lin;
+        if (T >= ul10) lin = lin_interp(ul10, 1.0, ul, 0.0, T);
+        else lin = 1.0;
+        cool_dg = cool_dg * lin;
+    }
+    return cool_dg;
+}
+
+// The state-independent part of dei_dt: cooling evaluated at the floors
+// (heatCool.F90:1509-1519). It depends only on ndens/conf, so it is
+// computed once per cell; the value is identical to recomputing it.
+__device__ __forceinline__ double cooling_floor(const gb_cool_ctx& c, const gb_cool_vars& v)
+{
+    double emin = cooling(c.p, c.p.tradmin, v.ndens, v.conf, v.xHp);
+    double pw = 0.0;
+    if (c.p.useDustCool) pw = molecular_cooling(c, v.ndens, c.p.T_cool_min, v.mu_mol);
+    return emin + pw;
+}
+
+static __device__ double dei_dt(const gb_cool_ctx& c, const gb_cool_vars& v, double floor_, double ei_in)
+{
+    // heatCool.F90:1397-1588
+    const gb_cool_params& p = c.p;
+    double tmp_temp = ei_in / v.TtoEI;
+    if (tmp_temp < 0.0) tmp_temp = 1.0;
+    double eplus = heating(p, tmp_temp, v.ndens, v.rho, v.strat_factor);
+    double fuv = v.Gflux + p.Gzero * f_ext(p, v.rho, v.ndens, tmp_temp) * v.strat_factor;
+    double PeHeat, dust_heating;
+    pe_heating(p, fuv, v.xHp, v.ndens, tmp_temp, v.rho, &PeHeat, &dust_heating);
+    eplus = eplus + v.ephen;
+    double emin = cooling(p, tmp_temp, v.ndens, v.conf, v.xHp);
+    double cool_pw = 0.0, cool_dg = 0.0;
+    if (p.useDustCool) {
+        cool_pw = molecular_cooling(c, v.ndens, tmp_temp, v.mu_mol);
+        cool_dg = dust_cooling(p, v.ndens, tmp_temp, v.tdust, v.rho);
+    }
+    return eplus + PeHeat - emin - cool_pw - cool_dg + floor_;
+}
+
+static __device__ double get_dust_temperature(const gb_cool_params& p, double tdust_in, double temp_in,
+                                       double nden, double phen_heat, gb_cool_diag* d)
+{
+    // heatCool.F90:703-884
+    const double tol = 1.e-4, smallt = .1;
+    double error = 10. * tol;
+    double tdust = tdust_in;
+    if (tdust < p.absTmin) tdust = p.absTmin;
+    double tg = (temp_in < p.absTmin) ? p.absTmin : temp_in;
+    int l = 1;
+    while ((l <= 100) && (error > tol)) {
+        double lambda_dust = 6.8 * pow(tdust, 6.0);
+        double coll = 3.8 * nden * (1.0 - 0.8 * exp(-75.0 / tg)) * (tg - tdust) * sqrt(tg);
+        double eqfunc = phen_heat + coll - lambda_dust;
+        double det = -(6.0 * lambda_dust / tdust) - 3.8 * nden * (1.0 - 0.8 * exp(-75.0 / tg)) * sqrt(tg);
+        double tnew = tdust - eqfunc / det;
+        error = fabs(tnew - tdust) / tdust;
+        tdust = tnew;
+        if (tdust < smallt) {
+            tdust = smallt;
+            error = 0.1 * tol;
+        }
+        l = l + 1;
+    }
+    if (l > 100) d->dust_noconv = 1;
+    if (tdust < p.absTmin) tdust = p.absTmin;
+    return tdust;
+}
+
+static __device__ void dust_update(const gb_cool_ctx& c, gb_cool_vars& v, double temp, gb_cool_diag* d)
+{
+    // heatCool.F90:430-443
+    const gb_cool_params& p = c.p;
+    double fuv = v.Gflux + p.Gzero * f_ext(p, v.rho, v.ndens, temp) * v.strat_factor;
+    double PeHeat, dust_heat;
+    pe_heating(p, fuv, v.xHp, v.ndens, temp, v.rho, &PeHeat, &dust_heat);
+    double cr = heating(p, temp, v.ndens, v.rho, v.strat_factor);
+    cr = cr * v.rho;
+    dust_heat = dust_heat + cr;
+    dust_heat = dust_heat / (v.ndens * 1e-33);
+    v.tdust = get_dust_temperature(p, v.tdust, temp, v.ndens, dust_heat, d);
+}
+
+__device__ __forceinline__ double one_step(const gb_cool_ctx& c, const gb_cool_vars& v,
+                                           double floor_, double dx, double y, double yold)
+{
+    // heatCool.F90:1928-1950
+    return y - dx * dei_dt(c, v, floor_, y) - yold;
+}
+
+static __device__ double zero(const gb_cool_ctx& c, const gb_cool_vars& v, double floor_, double a,
+                       double b, double a_old, double machep, double tt, double dt,
+                       gb_cool_diag* d)
+{
+    // heatCool.F90:1981-2197 (Brent)
+    double sa = a, sb = b;
+    double fa = one_step(c, v, floor_, dt, sa, a_old);
+    double fb = one_step(c, v, floor_, dt, sb, a_old);
+    double cc = sa, fc = fa, e = sb - sa, dd = e;
+    int n_tries = 0;
+    if ((fa > 0.0 && fb > 0.0) || (fa < 0.0 && fb < 0.0)) {
+        d->unbracketed = 1;
+        return sb;
+    }
+    for (;;) {
+        if (fabs(fc) < fabs(fb)) {
+            sa = sb; sb = cc; cc = sa;
+            fa = fb; fb = fc; fc = fa;
+        }
+        double tol = 2.0 * machep * fabs(sb) + tt;
+        double m = 0.5 * (cc - sb);
+        if (fabs(m) <= tol || fb == 0.0) break;
+        if (fabs(e) < tol || fabs(fa) <= fabs(fb)) {
+            e = m;
+            dd = e;
+        } else {
+            double s = fb / fa, pp, q, r;
+            if (sa == cc) {
+                pp = 2.0 * m * s;
+                q = 1.0 - s;
+            } else {
+                q = fa / fc;
+                r = fb / fc;
+                pp = s * (2.0 * m * q * (q - r) - (sb - sa) * (r - 1.0));
+                q = (q - 1.0) * (r - 1.0) * (s - 1.0);
+            }
+            if (0.0 < pp) q = -q;
+            else pp = -pp;
+            s = e;
+            e = dd;
+            if (2.0 * pp < 3.0 * m * q - fabs(tol * q) && pp < fabs(0.5 * s * q)) {
+                dd = pp / q;
+            } else {
+                e = m;
+                dd = e;
+            }
+        }
+        sa = sb;
+        fa = fb;
+        if (tol < fabs(dd)) sb = sb + dd;
+        else if (0.0 < m) sb = sb + tol;
+        else sb = sb - tol;
+        fb = one_step(c, v, floor_, dt, sb, a_old);
+        if ((0.0 < fb && 0.0 < fc) || (fb <= 0.0 && fc <= 0.0)) {
+            cc = sa;
+            fc = fa;
+            e = sb - sa;
+            dd = e;
+        }
+        n_tries = n_tries + 1;
+        if (n_tries > 10000) {
+            d->maxiter = 1;
+            break;
+        }
+    }
+    d->iters = n_tries;
+    return sb;
+}
+
+static __device__ int zbrac(const gb_cool_ctx& c, const gb_cool_vars& v, double floor_, double* x1,
+                     double* x2, double xold, double dt)
+{
+    // heatCool.F90:2294-2348
+    const double FACTOR = 1.6;
+    double f1 = one_step(c, v, floor_, dt, *x1, xold);
+    double f2 = one_step(c, v, floor_, dt, *x2, xold);
+    for (int j = 1; j <= 5000; ++j) {
+        if (f1 * f2 < 0.0) return 1;
+        if (fabs(f1) < fabs(f2)) {
+            *x1 = *x1 + FACTOR * (*x1 - *x2);
+            if (*x1 < 0.0) *x1 = v.TtoEI * 1.0;
+            f1 = one_step(c, v, floor_, dt, *x1, xold);
+        } else {
+            *x2 = *x2 + FACTOR * (*x2 - *x1);
+            if (*x2 < 0.0) *x2 = v.TtoEI * 1.0;
+            f2 = one_step(c, v, floor_, dt, *x2, xold);
+        }
+    }
+    return 0;
+}
+
+// heating_and_cooling, "Implicit" (default) or "Euler" branch, for one
+// cell. v must hold rho, Gflux, ephen, tdust, xHp, strat_factor, mu_mol.
+static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v, double* ei_io,
+                                    double timestep, double* temp_io, gb_cool_diag* d)
+{
+    const gb_cool_params& p = c.p;
+    const double err_tol = 1e-6;
+    double ei = *ei_io, temp = *temp_io;
+    double total_time = 0.0;
+    v.ndens = v.rho / (v.mu_mol * p.mp);
+    v.TtoEI = ei / temp;
+    v.conf = v.ndens * v.ndens / v.rho;
+    double fl = cooling_floor(c, v);
+    if (p.int_method == 1) {
+        // Euler, heatCool.F90:119-214
+        int ncount = 0;
+        for (;;) {
+            double dei = dei_dt(c, v, fl, ei);
+            double dt1 = p.subfactor * ei / fmx(fabs(dei), 1e-50);
+            double dt0 = fmn((timestep - total_time), dt1);
+            ei = ei + dei * dt0;
+            temp = ei / v.TtoEI;
+            total_time = total_time + dt0;
+            ncount = ncount + 1;
+            if (ncount > 100000) break;
+            if ((timestep - total_time) < 1e-6) break;
+        }
+        if (temp < p.absTmin) {
+            temp = p.absTmin;
+            ei = p.absTmin * v.TtoEI;
+        }
+        if (p.useDustCool && temp <= p.dust_sputter_temp)
+            v.tdust = get_dust_temperature(p, v.tdust, temp, v.ndens, 0.0, d);
+    } else {
+        // Implicit, heatCool.F90:216-514 (one pass: dt0 = timestep)
+        while ((timestep - total_time) > (1e-6 * timestep)) {
+            double eiolder = ei;
+            double eiold = ei;
+            double dei = dei_dt(c, v, fl, eiold);
+            double dt0 = timestep;
+            eiold = eiolder + dei * dt0 * 1.0e-3;
+            double ei1 = eiolder, ei2 = eiold;
+            if (fabs((ei1 - ei2) / ei1) < (err_tol * dt0 / (timestep - total_time))) {
+                dt0 = (timestep - total_time);
+                ei = eiolder + dei * dt0;
+                temp = ei / v.TtoEI;
+                if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update(c, v, temp, d);
+                total_time = total_time + dt0;
+                continue;
+            }
+            int found = zbrac(c, v, fl, &ei1, &ei2, eiolder, dt0);
+            if (!found) d->bracket_fail = 1;
+            if (ei1 < 0.0 || ei2 < 0.0) {
+                ei1 = fmx(ei1, v.TtoEI * 1.0);
+                ei2 = fmx(ei2, v.TtoEI * 1.0);
+            }
+            if (found)
+                ei = zero(c, v, fl, ei1, ei2, eiolder, 3e-16, fmx(v.TtoEI * 1.0, eiold * err_tol), dt0, d);
+            else
+                ei = zero(c, v, fl, v.TtoEI * 1.0, v.TtoEI * 1.0e9, eiolder, 3e-16,
+                          fmx(v.TtoEI * 1.0, eiold * err_tol), dt0, d);
+            temp = ei / v.TtoEI;
+            if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update(c, v, temp, d);
+            total_time = total_time + dt0;
+        }
+        if (temp < p.absTmin) {
+            temp = p.absTmin;
+            ei = p.absTmin * v.TtoEI;
+        }
+    }
+    *ei_io = ei;
+    *temp_io = temp;
+}
+
+}  // namespace gbcool

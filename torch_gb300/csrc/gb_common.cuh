@@ -1,0 +1,79 @@
+// Shared device-side definitions of the gbhydro library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gbhydro.h"
+
+#define GB_N GB_NB
+#define GB_N3 (GB_NB * GB_NB * GB_NB)
+#define GB_FSZ (GB_NB * GB_NB * (GB_NB + 1))
+
+// Record the first failure in the status word and count it.
+__device__ __forceinline__ void gb_fail(gb_status* st, int code, int blk, int i, int j, int k,
+                                        double v)
+{
+    if (!st) return;
+    if (atomicCAS(&st->code, 0, code) == 0) {
+        st->block = blk;
+        st->i = i;
+        st->j = j;
+        st->k = k;
+        st->value = v;
+    }
+}
+
+__device__ __forceinline__ void gb_count(unsigned long long* c, unsigned long long n = 1)
+{
+    if (c) atomicAdd(c, n);
+}
+
+// Warp-aggregated counter increment (one atomic per warp).
+__device__ __forceinline__ void gb_count_warp(unsigned long long* c, bool pred)
+{
+    unsigned m = __ballot_sync(__activemask(), pred);
+    if (m && (threadIdx.x & 31) == (__ffs(__activemask()) - 1)) {
+        if (c) atomicAdd(c, (unsigned long long)__popc(m));
+    }
+}
+
+// Grid state shared by the kernels of one registration.
+struct gb_dev_grid {
+    int nvar;
+    int maxblocks;
+    int slot[GB_NROLE];
+    double* unk;
+    double* f[3];
+    const int* level; // refinement level per store block (NULL: all level 0)
+};
+
+// cell size of a block: root cell size scaled by 2^-level (exact)
+__device__ __forceinline__ void gb_block_dx(const gb_dev_grid& g, const double* dx0, int blk, double* dx)
+{
+    double sc = g.level ? ldexp(1.0, -__ldg(g.level + blk)) : 1.0;
+    dx[0] = dx0[0] * sc;
+    dx[1] = dx0[1] * sc;
+    dx[2] = dx0[2] * sc;
+}
+
+__device__ __forceinline__ double* gb_var(const gb_dev_grid& g, int blk, int role)
+{
+    return g.unk + ((int64_t)blk * g.nvar + g.slot[role]) * GB_N3;
+}
+
+__host__ __device__ __forceinline__ int gb_cidx(int i, int j, int k)
+{
+    return i + GB_N * (j + GB_N * k);
+}
+
+// face index of face array d (face coordinate along d runs 0..GB_N)
+__host__ __device__ __forceinline__ int gb_fidx(int d, int i, int j, int k)
+{
+    return d == 0 ? i + (GB_N + 1) * (j + GB_N * k)
+                  : (d == 1 ? i + GB_N * (j + (GB_N + 1) * k) : i + GB_N * (j + GB_N * k));
+}
+
+// ---- host-side helpers implemented in capi.cu
+void gb_set_error(const char* fmt, ...);
+int gb_check(cudaError_t e, const char* what);

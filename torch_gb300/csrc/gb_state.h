@@ -1,0 +1,39 @@
+// Host-side state of one gbhydro library instance (one registered grid,
+// one parameter set). Internal header.
+#pragma once
+
+#include "cool_dev.cuh"
+#include "gb_common.cuh"
+
+struct gb_state_t {
+    bool grid_ok = false;
+    gb_grid_desc desc{};
+    gb_dev_grid grid{};
+    bool tree_ok = false;
+    gb_tree_desc tree{};
+    bool hydro_ok = false;
+    gb_hydro_params hp{};
+    bool cool_ok = false;
+    gb_cool_ctx cool{};
+    double* d_table = nullptr; // T axis, n axis, lambda (one allocation)
+    // staging buffers reused across calls
+    double* d_stage = nullptr;
+    size_t stage_bytes = 0;
+    void* d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    double* d_dtmin = nullptr;
+    int* d_all_blocks = nullptr;
+    int all_blocks_n = 0;
+};
+
+extern gb_state_t g_gb;
+
+// scratch allocation helper (grows, never shrinks)
+int gb_ensure_scratch(size_t bytes);
+int gb_ensure_stage(size_t bytes);
+
+// kernels launched from other translation units
+int gb_launch_cool_blocks(int nblk, const int* list, double dt, gb_status* st, cudaStream_t s);
+int gb_launch_hydro(int nblk, const int* list, double dt, int cool, gb_status* st, cudaStream_t s);
+int gb_launch_dt(int nblk, const int* list, double* dt_out, cudaStream_t s);
+int gb_launch_guardfill(int nblk, const int* list, cudaStream_t s);

@@ -1,0 +1,974 @@
+// Unsplit PPM + HLLC hydro / PPM + HLLD + CT MHD step, device code.
+//
+// One step over a chunk of blocks runs five kernels:
+//   k_recon   per cell (18^3 band of each block, one warp per direction):
+//             normal-direction PPM with characteristic limiting and tracing,
+//             transverse corrections and multidimensional MHD terms in the
+//             order of hy_uhd_dataReconstOneStep.F90:1006-1089, positivity
+//             fallback (:1230-1272) -> face states in scratch
+//   k_flux    per face: HLLC / HLLD + artificial viscosity -> fluxes
+//   k_emf     per edge (MHD): contact-upwinded CT electric field
+//   k_faceb   per face (MHD): Faraday update of the face-centred field
+//   k_update  per interior cell: FP64 flux-difference update, dual-energy
+//             recovery, Gamma-law EOS, optional fused cooling epilogue
+// The reconstruction and Riemann solve run in T (double for the plain path,
+// float for the mixed path); every accumulation into conserved variables,
+// the electric fields and the face-field update run in double.
+#pragma once
+
+#include "cool_dev.cuh"
+#include "gb_common.cuh"
+
+namespace gbh {
+
+constexpr int NP = 8;      // rho, vx, vy, vz, p, Bx, By, Bz
+constexpr int MAXW = 7;
+constexpr int RB = 18;     // reconstruction band: cells 3..20
+constexpr int RLO = GB_NGUARD - 1;
+constexpr int NRC = RB * RB * RB;
+constexpr int LO = GB_NGUARD, HI = GB_NGUARD + GB_NXB - 1;
+constexpr int NFC = 17 * RB * RB;             // faces per direction in the flux box
+constexpr int NFLX = 10;                      // 8 fluxes + rho*e_int flux + face velocity
+constexpr int NEDGE = 16 * 17 * 17;           // edges per direction
+constexpr int NFB = 17 * 16 * 16;             // interior faces per direction
+constexpr int RECON_TILE = 32;
+
+// scratch sizes per block (elements)
+template <typename T>
+struct scratch_layout {
+    static constexpr size_t recon = (size_t)NRC * 6 * NP;     // T
+    static constexpr size_t flux = (size_t)3 * NFC * NFLX;    // T
+    static constexpr size_t emf = (size_t)3 * NEDGE;          // double
+    static constexpr size_t fb = (size_t)3 * NFB;             // double
+    static constexpr size_t bytes = recon * sizeof(T) + flux * sizeof(T) + (emf + fb) * sizeof(double);
+};
+
+template <typename T>
+__device__ __forceinline__ T two3() { return (T)(2.0 / 3.0); }
+template <>
+__device__ __forceinline__ float two3<float>() { return 2.0f / 3.0f; }
+
+template <typename T>
+__device__ __forceinline__ T minmod(T a, T b)
+{
+    if (a * b <= (T)0) return (T)0;
+    return (fabs(a) <= fabs(b)) ? a : b;
+}
+
+// rotated slot -> unrotated primitive slot
+__device__ __forceinline__ int rot_slot(int d, int s)
+{
+    // d = 0: identity; 1: (0,2,3,1,4,6,7,5); 2: (0,3,1,2,4,7,5,6)
+    if (d == 0 || s == 0 || s == 4) return s;
+    int base = s < 4 ? 1 : 5, o = s - base;
+    return base + (o + d) % 3;
+}
+__device__ __forceinline__ int wslot(int s) { return s < 5 ? s : s + 1; }
+
+// ---------------------------------------------------------------- eigensystems
+template <typename T>
+__device__ __forceinline__ void eig_hydro(T gam, const T* q, T* lam, T (*R)[MAXW], T (*L)[MAXW])
+{
+    T rho = q[0], vn = q[1], p = q[4];
+    T a2 = gam * p / rho;
+    T a = sqrt(a2);
+#pragma unroll
+    for (int r = 0; r < MAXW; ++r)
+#pragma unroll
+        for (int c = 0; c < MAXW; ++c) { R[r][c] = (T)0; L[r][c] = (T)0; }
+    lam[0] = vn - a; lam[1] = vn; lam[2] = vn; lam[3] = vn; lam[4] = vn + a;
+    R[0][0] = (T)1; R[1][0] = -a / rho; R[4][0] = a2;
+    R[0][1] = (T)1;
+    R[2][2] = (T)1;
+    R[3][3] = (T)1;
+    R[0][4] = (T)1; R[1][4] = a / rho; R[4][4] = a2;
+    L[0][1] = -rho / ((T)2 * a); L[0][4] = (T)1 / ((T)2 * a2);
+    L[1][0] = (T)1; L[1][4] = (T)-1 / a2;
+    L[2][2] = (T)1;
+    L[3][3] = (T)1;
+    L[4][1] = rho / ((T)2 * a); L[4][4] = (T)1 / ((T)2 * a2);
+}
+
+template <typename T>
+__device__ __forceinline__ void eig_mhd(T gam, const T* q, T* lam, T (*R)[MAXW], T (*L)[MAXW])
+{
+    T rho = q[0], vn = q[1], p = q[4], bn = q[5], bt1 = q[6], bt2 = q[7];
+    T a2 = gam * p / rho;
+    T sr = sqrt(rho);
+    T bnx2 = bn * bn / rho;
+    T bt2s = (bt1 * bt1 + bt2 * bt2) / rho;
+    T term = a2 + bnx2 + bt2s;
+    T d1 = a2 - bnx2;
+    T disc = sqrt(d1 * d1 + bt2s * ((T)2 * (a2 + bnx2) + bt2s));
+    T cf2 = (T)0.5 * (term + disc);
+    T cs2 = a2 * bnx2 / cf2;
+    T cf = sqrt(cf2), cs = sqrt(cs2), ca = sqrt(bnx2);
+    T bperp = sqrt(bt1 * bt1 + bt2 * bt2);
+    T by, bz;
+    if (bperp > (T)0) { by = bt1 / bperp; bz = bt2 / bperp; }
+    else { by = (T)0.70710678118654752440; bz = (T)0.70710678118654752440; }
+    T af, as;
+    if (disc > (T)0) {
+        T af2 = ((d1 - bt2s) + disc) / ((T)2 * disc);
+        T as2 = ((bt2s - d1) + disc) / ((T)2 * disc);
+        af2 = af2 < (T)0 ? (T)0 : (af2 > (T)1 ? (T)1 : af2);
+        as2 = as2 < (T)0 ? (T)0 : (as2 > (T)1 ? (T)1 : as2);
+        af = sqrt(af2);
+        as = sqrt(as2);
+    } else {
+        af = (T)1;
+        as = (T)0;
+    }
+    T S = bn >= (T)0 ? (T)1 : (T)-1;
+    T a = sqrt(a2);
+    T n2 = af * af * cf2 + as * as * cs2;
+    T sra = sr * a;
+#pragma unroll
+    for (int r = 0; r < MAXW; ++r)
+#pragma unroll
+        for (int c = 0; c < MAXW; ++c) { R[r][c] = (T)0; L[r][c] = (T)0; }
+    lam[0] = vn - cf; lam[1] = vn - ca; lam[2] = vn - cs; lam[3] = vn;
+    lam[4] = vn + cs; lam[5] = vn + ca; lam[6] = vn + cf;
+    R[0][0] = rho * af; R[1][0] = -af * cf; R[2][0] = as * cs * by * S; R[3][0] = as * cs * bz * S;
+    R[4][0] = rho * af * a2; R[5][0] = as * sra * by; R[6][0] = as * sra * bz;
+    R[2][1] = -bz; R[3][1] = by; R[5][1] = -S * sr * bz; R[6][1] = S * sr * by;
+    R[0][2] = rho * as; R[1][2] = -as * cs; R[2][2] = -af * cf * by * S; R[3][2] = -af * cf * bz * S;
+    R[4][2] = rho * as * a2; R[5][2] = -af * sra * by; R[6][2] = -af * sra * bz;
+    R[0][3] = (T)1;
+    R[0][4] = rho * as; R[1][4] = as * cs; R[2][4] = af * cf * by * S; R[3][4] = af * cf * bz * S;
+    R[4][4] = rho * as * a2; R[5][4] = -af * sra * by; R[6][4] = -af * sra * bz;
+    R[2][5] = -bz; R[3][5] = by; R[5][5] = S * sr * bz; R[6][5] = -S * sr * by;
+    R[0][6] = rho * af; R[1][6] = af * cf; R[2][6] = -as * cs * by * S; R[3][6] = -as * cs * bz * S;
+    R[4][6] = rho * af * a2; R[5][6] = as * sra * by; R[6][6] = as * sra * bz;
+    T hn = (T)0.5 / n2, hra = (T)0.5 / (rho * a2), hsa = (T)0.5 / sra, hs = (T)0.5 / sr;
+    L[0][1] = -af * cf * hn; L[0][2] = as * cs * S * by * hn; L[0][3] = as * cs * S * bz * hn;
+    L[0][4] = af * hra; L[0][5] = as * by * hsa; L[0][6] = as * bz * hsa;
+    L[1][2] = (T)-0.5 * bz; L[1][3] = (T)0.5 * by; L[1][5] = -bz * S * hs; L[1][6] = by * S * hs;
+    L[2][1] = -as * cs * hn; L[2][2] = -af * cf * S * by * hn; L[2][3] = -af * cf * S * bz * hn;
+    L[2][4] = as * hra; L[2][5] = -af * by * hsa; L[2][6] = -af * bz * hsa;
+    L[3][0] = (T)1; L[3][4] = (T)-1 / a2;
+    L[4][1] = as * cs * hn; L[4][2] = af * cf * S * by * hn; L[4][3] = af * cf * S * bz * hn;
+    L[4][4] = as * hra; L[4][5] = -af * by * hsa; L[4][6] = -af * bz * hsa;
+    L[5][2] = (T)-0.5 * bz; L[5][3] = (T)0.5 * by; L[5][5] = bz * S * hs; L[5][6] = -by * S * hs;
+    L[6][1] = af * cf * hn; L[6][2] = -as * cs * S * by * hn; L[6][3] = -as * cs * S * bz * hn;
+    L[6][4] = af * hra; L[6][5] = as * by * hsa; L[6][6] = as * bz * hsa;
+}
+
+// ---------------------------------------------------------------- PPM
+// qs[m][s]: rotated stencil (m = 0..4), outputs rotated wp, wn, sig.
+template <typename T, bool MHD>
+__device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* wp, T* wn, T* sig)
+{
+    constexpr int nw = MHD ? 7 : 5;
+    T lam[MAXW], R[MAXW][MAXW], L[MAXW][MAXW];
+    if (MHD) eig_mhd<T>(gam, qs[2], lam, R, L);
+    else eig_hydro<T>(gam, qs[2], lam, R, L);
+    T dwm[3][MAXW];
+#pragma unroll
+    for (int m = 1; m <= 3; ++m) {
+        T da[MAXW];
+#pragma unroll
+        for (int k = 0; k < nw; ++k) {
+            T sl = (T)0, srr = (T)0;
+#pragma unroll
+            for (int s = 0; s < nw; ++s) {
+                const int qq = wslot(s);
+                sl = sl + L[k][s] * (qs[m][qq] - qs[m - 1][qq]);
+                srr = srr + L[k][s] * (qs[m + 1][qq] - qs[m][qq]);
+            }
+            da[k] = minmod<T>(sl, srr);
+        }
+#pragma unroll
+        for (int s = 0; s < nw; ++s) {
+            T acc = (T)0;
+#pragma unroll
+            for (int k = 0; k < nw; ++k) acc = acc + R[s][k] * da[k];
+            dwm[m - 1][s] = acc;
+        }
+    }
+    T WL[MAXW], WR[MAXW], dW[MAXW], W6[MAXW];
+#pragma unroll
+    for (int s = 0; s < nw; ++s) {
+        const int qq = wslot(s);
+        T qm = qs[1][qq], q0 = qs[2][qq], qp = qs[3][qq];
+        T wl = (T)0.5 * (qm + q0) - (dwm[1][s] - dwm[0][s]) / (T)6;
+        T wr = (T)0.5 * (q0 + qp) - (dwm[2][s] - dwm[1][s]) / (T)6;
+        wl = fmax(fmin(q0, qm), wl);
+        wl = fmin(fmax(q0, qm), wl);
+        wr = fmax(fmin(q0, qp), wr);
+        wr = fmin(fmax(q0, qp), wr);
+        T qa = (wr - q0) * (q0 - wl);
+        if (qa <= (T)0) {
+            wl = q0;
+            wr = q0;
+        } else {
+            T qb = wr - wl;
+            T qc = (T)6 * (q0 - (T)0.5 * (wl + wr));
+            if (qb * qc > qb * qb) wl = (T)3 * q0 - (T)2 * wr;
+            else if (qb * qc < -(qb * qb)) wr = (T)3 * q0 - (T)2 * wl;
+        }
+        WL[s] = wl;
+        WR[s] = wr;
+        dW[s] = wr - wl;
+        W6[s] = (T)6 * (q0 - (T)0.5 * (wl + wr));
+    }
+    T ldW[MAXW], lW6[MAXW];
+#pragma unroll
+    for (int k = 0; k < nw; ++k) {
+        T a = (T)0, b = (T)0;
+#pragma unroll
+        for (int s = 0; s < nw; ++s) {
+            a = a + L[k][s] * dW[s];
+            b = b + L[k][s] * W6[s];
+        }
+        ldW[k] = a;
+        lW6[k] = b;
+    }
+    const T t3 = two3<T>();
+    T sK = lam[nw - 1] * dtdx;
+    bool refK = lam[nw - 1] > (T)0;
+    T Wp[MAXW], Wn[MAXW];
+#pragma unroll
+    for (int s = 0; s < nw; ++s)
+        Wp[s] = refK ? WR[s] - (T)0.5 * sK * (dW[s] - ((T)1 - t3 * sK) * W6[s]) : WR[s];
+#pragma unroll
+    for (int k = 0; k < nw; ++k) {
+        if (lam[k] > (T)0) {
+            T sg = lam[k] * dtdx;
+            T gK = refK ? (T)0.5 * sK * (ldW[k] - ((T)1 - t3 * sK) * lW6[k]) : (T)0;
+            T c = gK - (T)0.5 * sg * (ldW[k] - ((T)1 - t3 * sg) * lW6[k]);
+#pragma unroll
+            for (int s = 0; s < nw; ++s) Wp[s] = Wp[s] + c * R[s][k];
+        }
+    }
+    T s0 = lam[0] * dtdx;
+    bool ref0 = lam[0] < (T)0;
+#pragma unroll
+    for (int s = 0; s < nw; ++s)
+        Wn[s] = ref0 ? WL[s] - (T)0.5 * s0 * (dW[s] + ((T)1 + t3 * s0) * W6[s]) : WL[s];
+#pragma unroll
+    for (int k = 0; k < nw; ++k) {
+        if (lam[k] < (T)0) {
+            T sg = lam[k] * dtdx;
+            T g0 = ref0 ? (T)0.5 * s0 * (ldW[k] + ((T)1 + t3 * s0) * lW6[k]) : (T)0;
+            T c = g0 - (T)0.5 * sg * (ldW[k] + ((T)1 + t3 * sg) * lW6[k]);
+#pragma unroll
+            for (int s = 0; s < nw; ++s) Wn[s] = Wn[s] + c * R[s][k];
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < NP; ++s) { wp[s] = (T)0; wn[s] = (T)0; sig[s] = (T)0; }
+#pragma unroll
+    for (int s = 0; s < nw; ++s) {
+        T acc = (T)0;
+#pragma unroll
+        for (int k = 0; k < nw; ++k) acc = acc + (lam[k] * ldW[k]) * R[s][k];
+        wp[wslot(s)] = Wp[s];
+        wn[wslot(s)] = Wn[s];
+        sig[wslot(s)] = acc;
+    }
+    wp[5] = qs[2][5];
+    wn[5] = qs[2][5];
+}
+
+struct hydro_kparams {
+    double gamma, cvisc, eint_switch, smlrho, smallp;
+    int use_avisc;
+    double dt, dx[3];
+};
+
+// primitive 8-vector of a cell of the padded block
+template <typename T, bool MHD>
+__device__ __forceinline__ void load_w(const gb_dev_grid& g, int blk, int ci, T* w)
+{
+    const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3 + ci;
+    w[0] = (T)base[(int64_t)g.slot[GB_DENS] * GB_N3];
+    w[1] = (T)base[(int64_t)g.slot[GB_VELX] * GB_N3];
+    w[2] = (T)base[(int64_t)g.slot[GB_VELY] * GB_N3];
+    w[3] = (T)base[(int64_t)g.slot[GB_VELZ] * GB_N3];
+    w[4] = (T)base[(int64_t)g.slot[GB_PRES] * GB_N3];
+    if (MHD) {
+        w[5] = (T)base[(int64_t)g.slot[GB_MAGX] * GB_N3];
+        w[6] = (T)base[(int64_t)g.slot[GB_MAGY] * GB_N3];
+        w[7] = (T)base[(int64_t)g.slot[GB_MAGZ] * GB_N3];
+    } else {
+        w[5] = (T)0; w[6] = (T)0; w[7] = (T)0;
+    }
+}
+
+// ---------------------------------------------------------------- k_recon
+// blockDim = 3 * RECON_TILE: warp d reconstructs direction d for 32 cells.
+template <typename T, bool MHD>
+__global__ void __launch_bounds__(3 * RECON_TILE)
+k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __restrict__ scr,
+        size_t scr_stride, gb_status* st)
+{
+    constexpr int nv = MHD ? 8 : 5;
+    __shared__ T s_sig[3][NP][RECON_TILE];
+    __shared__ T s_abn[3][NP][RECON_TILE];
+    __shared__ T s_dnb[3][RECON_TILE];
+    const int lane = threadIdx.x % RECON_TILE;
+    const int d = threadIdx.x / RECON_TILE;
+    const int cb = blockIdx.y;
+    const int blk = list[cb];
+    const int cell = blockIdx.x * RECON_TILE + lane;
+    const bool active = cell < NRC;
+    const int cc = active ? cell : 0;
+    const int i = RLO + cc % RB, j = RLO + (cc / RB) % RB, k = RLO + cc / (RB * RB);
+    const T gam = (T)kp.gamma;
+    double dxl[3];
+    gb_block_dx(g, kp.dx, blk, dxl);
+    const T hd[3] = {(T)(0.5 * kp.dt / dxl[0]), (T)(0.5 * kp.dt / dxl[1]), (T)(0.5 * kp.dt / dxl[2])};
+
+    // normal-direction PPM in direction d
+    T qs[5][NP];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+        int ii = i + (d == 0 ? m - 2 : 0), jj = j + (d == 1 ? m - 2 : 0), kk = k + (d == 2 ? m - 2 : 0);
+        T w[NP];
+        load_w<T, MHD>(g, blk, gb_cidx(ii, jj, kk), w);
+#pragma unroll
+        for (int s = 0; s < NP; ++s) qs[m][s] = w[rot_slot(d, s)];
+    }
+    T wpr[NP], wnr[NP], sgr[NP];
+    ppm_normal<T, MHD>(gam, qs, (T)(kp.dt / dxl[d]), wpr, wnr, sgr);
+    T wp[NP], wn[NP];
+#pragma unroll
+    for (int s = 0; s < NP; ++s) {
+        int v = rot_slot(d, s);
+        wp[v] = wpr[s];
+        wn[v] = wnr[s];
+        s_sig[d][v][lane] = sgr[s];
+    }
+    T wc[NP];
+    load_w<T, MHD>(g, blk, gb_cidx(i, j, k), wc);
+    if (MHD) {
+        // multidimensional terms (hy_uhd_dataReconstOneStep.F90:364-424)
+        T uB = wc[1] * wc[5] + wc[2] * wc[6] + wc[3] * wc[7];
+        T row[NP] = {(T)0, -wc[5] / wc[0], -wc[6] / wc[0], -wc[7] / wc[0], (gam - (T)1) * uB,
+                     (T)0, -wc[2], -wc[3]};
+        if (d == 1) { row[5] = -wc[1]; row[6] = (T)0; row[7] = -wc[3]; }
+        if (d == 2) { row[5] = -wc[1]; row[6] = -wc[2]; row[7] = (T)0; }
+        const double* fd = g.f[d] + (int64_t)blk * GB_FSZ;
+        int ip = i + (d == 0), jp = j + (d == 1), kp2 = k + (d == 2);
+        T dnb = (T)fd[gb_fidx(d, ip, jp, kp2)] - (T)fd[gb_fidx(d, i, j, k)];
+#pragma unroll
+        for (int v = 0; v < NP; ++v) {
+            s_abn[d][v][lane] = row[v];
+            wp[v] = wp[v] - hd[d] * row[v] * dnb;
+            wn[v] = wn[v] - hd[d] * row[v] * dnb;
+        }
+        s_dnb[d][lane] = dnb;
+    }
+    __syncthreads();
+    // transverse corrections for direction d, vendored order
+    const int a = (d + 1) % 3, b = (d + 2) % 3;
+    (void)a;
+    (void)b;
+#pragma unroll
+    for (int v = 0; v < nv; ++v) {
+        if (d == 0) {
+            wn[v] = wn[v] - hd[1] * s_sig[1][v][lane];
+            wp[v] = wp[v] - hd[1] * s_sig[1][v][lane];
+        } else if (d == 1) {
+            wn[v] = wn[v] - hd[0] * s_sig[0][v][lane];
+            wp[v] = wp[v] - hd[0] * s_sig[0][v][lane];
+        }
+    }
+    if (MHD) {
+#pragma unroll
+        for (int v = 0; v < nv; ++v) {
+            if (d == 0) {
+                wn[v] = wn[v] - hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
+                wp[v] = wp[v] - hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
+            } else if (d == 1) {
+                wn[v] = wn[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane];
+                wp[v] = wp[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane];
+            }
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < nv; ++v) {
+        if (d < 2) {
+            wn[v] = wn[v] - hd[2] * s_sig[2][v][lane];
+            wp[v] = wp[v] - hd[2] * s_sig[2][v][lane];
+        } else {
+            wn[v] = wn[v] - hd[0] * s_sig[0][v][lane] - hd[1] * s_sig[1][v][lane];
+            wp[v] = wp[v] - hd[0] * s_sig[0][v][lane] - hd[1] * s_sig[1][v][lane];
+        }
+    }
+    if (MHD) {
+#pragma unroll
+        for (int v = 0; v < nv; ++v) {
+            if (d < 2) {
+                wn[v] = wn[v] - hd[2] * s_abn[2][v][lane] * s_dnb[2][lane];
+                wp[v] = wp[v] - hd[2] * s_abn[2][v][lane] * s_dnb[2][lane];
+            } else {
+                wn[v] = wn[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane] -
+                        hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
+                wp[v] = wp[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane] -
+                        hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
+            }
+        }
+    }
+    // positivity fallback
+    bool fell = (wn[0] < (T)0 || wp[0] < (T)0 || wn[4] < (T)0 || wp[4] < (T)0);
+    if (fell) {
+#pragma unroll
+        for (int v = 0; v < NP; ++v) { wn[v] = wc[v]; wp[v] = wc[v]; }
+    }
+    if (!active) return;
+    if (st) gb_count_warp(&st->n_fallback, fell);
+    T* out = scr + (size_t)cb * scr_stride;
+#pragma unroll
+    for (int v = 0; v < NP; ++v) {
+        out[((size_t)(0 * 3 + d) * NP + v) * NRC + cell] = wp[v];
+        out[((size_t)(1 * 3 + d) * NP + v) * NRC + cell] = wn[v];
+    }
+}
+
+// ---------------------------------------------------------------- Riemann
+template <typename T>
+__device__ __forceinline__ void hllc(T gam, const T* L, const T* R, T* F, T* un)
+{
+    T gm1 = gam - (T)1;
+    T aL = sqrt(gam * L[4] / L[0]), aR = sqrt(gam * R[4] / R[0]);
+    T SL = fmin(L[1] - aL, R[1] - aR);
+    T SR = fmax(L[1] + aL, R[1] + aR);
+    T EL = L[4] / gm1 + (T)0.5 * L[0] * (L[1] * L[1] + L[2] * L[2] + L[3] * L[3]);
+    T ER = R[4] / gm1 + (T)0.5 * R[0] * (R[1] * R[1] + R[2] * R[2] + R[3] * R[3]);
+    T FL[5] = {L[0] * L[1], L[0] * L[1] * L[1] + L[4], L[0] * L[1] * L[2], L[0] * L[1] * L[3], L[1] * (EL + L[4])};
+    T FR[5] = {R[0] * R[1], R[0] * R[1] * R[1] + R[4], R[0] * R[1] * R[2], R[0] * R[1] * R[3], R[1] * (ER + R[4])};
+#pragma unroll
+    for (int s = 0; s < NP; ++s) F[s] = (T)0;
+    if (SL >= (T)0) {
+#pragma unroll
+        for (int s = 0; s < 5; ++s) F[s] = FL[s];
+        *un = L[1];
+        return;
+    }
+    if (SR <= (T)0) {
+#pragma unroll
+        for (int s = 0; s < 5; ++s) F[s] = FR[s];
+        *un = R[1];
+        return;
+    }
+    T SM = (R[4] - L[4] + L[0] * L[1] * (SL - L[1]) - R[0] * R[1] * (SR - R[1])) /
+           (L[0] * (SL - L[1]) - R[0] * (SR - R[1]));
+    *un = SM;
+    const bool left = SM >= (T)0;
+    const T* W = left ? L : R;
+    T S = left ? SL : SR;
+    T E = left ? EL : ER;
+    T fac = W[0] * (S - W[1]) / (S - SM);
+    T Us[5] = {fac, fac * SM, fac * W[2], fac * W[3],
+               fac * (E / W[0] + (SM - W[1]) * (SM + W[4] / (W[0] * (S - W[1]))))};
+    T Uw[5] = {W[0], W[0] * W[1], W[0] * W[2], W[0] * W[3], E};
+#pragma unroll
+    for (int s = 0; s < 5; ++s) F[s] = (left ? FL[s] : FR[s]) + S * (Us[s] - Uw[s]);
+}
+
+template <typename T>
+__device__ __forceinline__ void mhd_flux(const T* W, T bx, T E, T pT, T* F)
+{
+    T vB = W[1] * bx + W[2] * W[6] + W[3] * W[7];
+    F[0] = W[0] * W[1];
+    F[1] = W[0] * W[1] * W[1] + pT - bx * bx;
+    F[2] = W[0] * W[1] * W[2] - bx * W[6];
+    F[3] = W[0] * W[1] * W[3] - bx * W[7];
+    F[4] = (E + pT) * W[1] - bx * vB;
+    F[5] = (T)0;
+    F[6] = W[6] * W[1] - bx * W[2];
+    F[7] = W[7] * W[1] - bx * W[3];
+}
+
+template <typename T>
+__device__ __forceinline__ T hlld_eps();
+template <>
+__device__ __forceinline__ double hlld_eps<double>() { return 1e-12; }
+template <>
+__device__ __forceinline__ float hlld_eps<float>() { return 1e-6f; }
+
+template <typename T>
+__device__ __forceinline__ void hlld(T gam, const T* L, const T* R, T* F, T* un)
+{
+    const T gm1 = gam - (T)1;
+    const T bx = L[5];
+    T bx2 = bx * bx;
+    T BL2 = bx2 + L[6] * L[6] + L[7] * L[7];
+    T BR2 = bx2 + R[6] * R[6] + R[7] * R[7];
+    T pTL = L[4] + (T)0.5 * BL2, pTR = R[4] + (T)0.5 * BR2;
+    T EL = L[4] / gm1 + (T)0.5 * L[0] * (L[1] * L[1] + L[2] * L[2] + L[3] * L[3]) + (T)0.5 * BL2;
+    T ER = R[4] / gm1 + (T)0.5 * R[0] * (R[1] * R[1] + R[2] * R[2] + R[3] * R[3]) + (T)0.5 * BR2;
+    T gpl = gam * L[4], gpr = gam * R[4];
+    T tl = (gpl + BL2) / L[0], tr = (gpr + BR2) / R[0];
+    T cfL = sqrt((T)0.5 * (tl + sqrt(fmax(tl * tl - (T)4 * gpl * bx2 / (L[0] * L[0]), (T)0))));
+    T cfR = sqrt((T)0.5 * (tr + sqrt(fmax(tr * tr - (T)4 * gpr * bx2 / (R[0] * R[0]), (T)0))));
+    T cmax = fmax(cfL, cfR);
+    T SL = fmin(L[1], R[1]) - cmax;
+    T SR = fmax(L[1], R[1]) + cmax;
+    T FL[NP], FR[NP];
+    mhd_flux<T>(L, bx, EL, pTL, FL);
+    mhd_flux<T>(R, bx, ER, pTR, FR);
+    if (SL >= (T)0) {
+#pragma unroll
+        for (int s = 0; s < NP; ++s) F[s] = FL[s];
+        *un = L[1];
+        return;
+    }
+    if (SR <= (T)0) {
+#pragma unroll
+        for (int s = 0; s < NP; ++s) F[s] = FR[s];
+        *un = R[1];
+        return;
+    }
+    T sdl = SL - L[1], sdr = SR - R[1];
+    T den = sdr * R[0] - sdl * L[0];
+    T SM = (sdr * R[0] * R[1] - sdl * L[0] * L[1] - pTR + pTL) / den;
+    T pTs = (sdr * R[0] * pTL - sdl * L[0] * pTR + L[0] * R[0] * sdr * sdl * (R[1] - L[1])) / den;
+    *un = SM;
+    T Us[2][NP], Uo[2][NP], sqs[2], vst[2], wst[2], byst[2], bzst[2], vBst[2];
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        const T* W = a == 0 ? L : R;
+        T S = a == 0 ? SL : SR;
+        T Ea = a == 0 ? EL : ER;
+        T pTa = a == 0 ? pTL : pTR;
+        T sd = S - W[1];
+        T rs = W[0] * sd / (S - SM);
+        T t1 = W[0] * sd * (S - SM);
+        T dd = t1 - bx2;
+        T vs, ws, bys, bzs;
+        if (fabs(dd) < hlld_eps<T>() * (fabs(t1) + bx2)) {
+            vs = W[2]; ws = W[3]; bys = W[6]; bzs = W[7];
+        } else {
+            T q = (SM - W[1]) / dd;
+            vs = W[2] - bx * W[6] * q;
+            ws = W[3] - bx * W[7] * q;
+            T r = (W[0] * sd * sd - bx2) / dd;
+            bys = W[6] * r;
+            bzs = W[7] * r;
+        }
+        T vB = W[1] * bx + W[2] * W[6] + W[3] * W[7];
+        T vBs = SM * bx + vs * bys + ws * bzs;
+        T Est = (sd * Ea - pTa * W[1] + pTs * SM + bx * (vB - vBs)) / (S - SM);
+        Us[a][0] = rs; Us[a][1] = rs * SM; Us[a][2] = rs * vs; Us[a][3] = rs * ws;
+        Us[a][4] = Est; Us[a][5] = bx; Us[a][6] = bys; Us[a][7] = bzs;
+        Uo[a][0] = W[0]; Uo[a][1] = W[0] * W[1]; Uo[a][2] = W[0] * W[2]; Uo[a][3] = W[0] * W[3];
+        Uo[a][4] = Ea; Uo[a][5] = bx; Uo[a][6] = W[6]; Uo[a][7] = W[7];
+        sqs[a] = sqrt(rs);
+        vst[a] = vs; wst[a] = ws; byst[a] = bys; bzst[a] = bzs; vBst[a] = vBs;
+    }
+    T Ss0 = SM - fabs(bx) / sqs[0];
+    T Ss1 = SM + fabs(bx) / sqs[1];
+    if (Ss0 >= (T)0) {
+#pragma unroll
+        for (int s = 0; s < NP; ++s) F[s] = FL[s] + SL * (Us[0][s] - Uo[0][s]);
+        return;
+    }
+    if (Ss1 <= (T)0) {
+#pragma unroll
+        for (int s = 0; s < NP; ++s) F[s] = FR[s] + SR * (Us[1][s] - Uo[1][s]);
+        return;
+    }
+    T sgn = bx >= (T)0 ? (T)1 : (T)-1;
+    T isum = (T)1 / (sqs[0] + sqs[1]);
+    T vss = (sqs[0] * vst[0] + sqs[1] * vst[1] + (byst[1] - byst[0]) * sgn) * isum;
+    T wss = (sqs[0] * wst[0] + sqs[1] * wst[1] + (bzst[1] - bzst[0]) * sgn) * isum;
+    T byss = (sqs[0] * byst[1] + sqs[1] * byst[0] + sqs[0] * sqs[1] * (vst[1] - vst[0]) * sgn) * isum;
+    T bzss = (sqs[0] * bzst[1] + sqs[1] * bzst[0] + sqs[0] * sqs[1] * (wst[1] - wst[0]) * sgn) * isum;
+    T vBss = SM * bx + vss * byss + wss * bzss;
+    const int a = SM >= (T)0 ? 0 : 1;
+    T Ess = a == 0 ? Us[0][4] - sqs[0] * (vBst[0] - vBss) * sgn : Us[1][4] + sqs[1] * (vBst[1] - vBss) * sgn;
+    T Uss[NP] = {Us[a][0], Us[a][0] * SM, Us[a][0] * vss, Us[a][0] * wss, Ess, bx, byss, bzss};
+    T S = a == 0 ? SL : SR;
+    T Sst = a == 0 ? Ss0 : Ss1;
+#pragma unroll
+    for (int s = 0; s < NP; ++s)
+        F[s] = (a == 0 ? FL[s] : FR[s]) + S * (Us[a][s] - Uo[a][s]) + Sst * (Uss[s] - Us[a][s]);
+}
+
+// flux box of direction d: normal faces 4..20 (17), transverse cells 3..20 (18)
+__device__ __forceinline__ void flux_coords(int d, int f, int* I)
+{
+    int e0 = f % 17, e1 = (f / 17) % RB, e2 = f / (17 * RB);
+    // axis order: normal first, then the two transverse axes in x<y<z order
+    int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
+    I[d] = LO + e0;
+    I[t1] = RLO + e1;
+    I[t2] = RLO + e2;
+}
+__device__ __forceinline__ int flux_index(int d, int i, int j, int k)
+{
+    int I[3] = {i, j, k};
+    int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
+    return (I[d] - LO) + 17 * ((I[t1] - RLO) + RB * (I[t2] - RLO));
+}
+__device__ __forceinline__ int rc_index(int i, int j, int k)
+{
+    return (i - RLO) + RB * ((j - RLO) + RB * (k - RLO));
+}
+
+// ---------------------------------------------------------------- k_flux
+template <typename T, bool MHD>
+__global__ void __launch_bounds__(128)
+k_flux(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* __restrict__ rscr,
+       T* __restrict__ fscr, size_t scr_stride)
+{
+    const int d = blockIdx.y;
+    const int cb = blockIdx.z;
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= NFC) return;
+    const int blk = list[cb];
+    int I[3];
+    flux_coords(d, f, I);
+    int Il[3] = {I[0], I[1], I[2]};
+    Il[d] -= 1;
+    const T* rs = rscr + (size_t)cb * scr_stride;
+    const int cl = rc_index(Il[0], Il[1], Il[2]), cr = rc_index(I[0], I[1], I[2]);
+    T wl[NP], wr[NP];
+#pragma unroll
+    for (int v = 0; v < NP; ++v) {
+        wl[v] = rs[((size_t)(0 * 3 + d) * NP + v) * NRC + cl];
+        wr[v] = rs[((size_t)(1 * 3 + d) * NP + v) * NRC + cr];
+    }
+    T Lr[NP], Rr[NP], Fr[NP], un;
+#pragma unroll
+    for (int s = 0; s < NP; ++s) {
+        Lr[s] = wl[rot_slot(d, s)];
+        Rr[s] = wr[rot_slot(d, s)];
+    }
+    const T gam = (T)kp.gamma;
+    if (MHD) {
+        T bnf = (T)g.f[d][(int64_t)blk * GB_FSZ + gb_fidx(d, I[0], I[1], I[2])];
+        Lr[5] = bnf;
+        Rr[5] = bnf;
+        hlld<T>(gam, Lr, Rr, Fr, &un);
+    } else {
+        hllc<T>(gam, Lr, Rr, Fr, &un);
+    }
+    T out[NP];
+#pragma unroll
+    for (int s = 0; s < NP; ++s) out[rot_slot(d, s)] = Fr[s];
+    const T gm1 = gam - (T)1;
+    T eL = Lr[4] / (gm1 * Lr[0]), eR = Rr[4] / (gm1 * Rr[0]);
+    T feint = Fr[0] * (Fr[0] >= (T)0 ? eL : eR);
+    if (kp.use_avisc) {
+        const int cil = gb_cidx(Il[0], Il[1], Il[2]), cir = gb_cidx(I[0], I[1], I[2]);
+        const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
+        auto U = [&](int role, int ci) -> T { return (T)base[(int64_t)g.slot[role] * GB_N3 + ci]; };
+        T dv = U(GB_VELX + d, cir) - U(GB_VELX + d, cil);
+        T vis = (T)kp.cvisc * fmax(-dv, (T)0);
+        if (vis > (T)0) {
+            T rl = U(GB_DENS, cil), rr = U(GB_DENS, cir);
+            T vl[3] = {U(GB_VELX, cil), U(GB_VELY, cil), U(GB_VELZ, cil)};
+            T vr[3] = {U(GB_VELX, cir), U(GB_VELY, cir), U(GB_VELZ, cir)};
+            T Bl[3] = {(T)0, (T)0, (T)0}, Br[3] = {(T)0, (T)0, (T)0};
+            if (MHD) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) { Bl[c] = U(GB_MAGX + c, cil); Br[c] = U(GB_MAGX + c, cir); }
+            }
+            T pl = U(GB_PRES, cil), pr = U(GB_PRES, cir);
+            T ul[NP], ur[NP];
+            ul[0] = rl; ur[0] = rr;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { ul[1 + c] = rl * vl[c]; ur[1 + c] = rr * vr[c]; }
+            ul[4] = pl / gm1 + (T)0.5 * rl * (vl[0] * vl[0] + vl[1] * vl[1] + vl[2] * vl[2]) +
+                    (T)0.5 * (Bl[0] * Bl[0] + Bl[1] * Bl[1] + Bl[2] * Bl[2]);
+            ur[4] = pr / gm1 + (T)0.5 * rr * (vr[0] * vr[0] + vr[1] * vr[1] + vr[2] * vr[2]) +
+                    (T)0.5 * (Br[0] * Br[0] + Br[1] * Br[1] + Br[2] * Br[2]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { ul[5 + c] = Bl[c]; ur[5 + c] = Br[c]; }
+#pragma unroll
+            for (int s = 0; s < NP; ++s) {
+                if (s == 5 + d) continue;
+                if (!MHD && s >= 5) continue;
+                out[s] = out[s] + vis * (ul[s] - ur[s]);
+            }
+            T el = rl * U(GB_EINT, cil), er = rr * U(GB_EINT, cir);
+            feint = feint + vis * (el - er);
+        }
+    }
+    T* fs = fscr + (size_t)cb * scr_stride + (size_t)d * NFLX * NFC;
+#pragma unroll
+    for (int s = 0; s < NP; ++s) fs[(size_t)s * NFC + f] = out[s];
+    fs[(size_t)8 * NFC + f] = feint;
+    fs[(size_t)9 * NFC + f] = un;
+}
+
+// ---------------------------------------------------------------- k_emf
+__device__ __forceinline__ double upw(double f, double a, double b)
+{
+    return f > 0.0 ? a : (f < 0.0 ? b : 0.5 * (a + b));
+}
+
+// edge box of direction c: along c cells 4..19 (16), along a and b faces 4..20 (17)
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_emf(gb_dev_grid g, const int* __restrict__ list, const T* __restrict__ fscr, size_t fstride,
+      double* __restrict__ escr, size_t estride)
+{
+    const int c = blockIdx.y;
+    const int cb = blockIdx.z;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= NEDGE) return;
+    const int blk = list[cb];
+    const int a = (c + 1) % 3, b = (c + 2) % 3;
+    const int A = LO + e % 17, B = LO + (e / 17) % 17, C = LO + e / (17 * 17);
+    const T* fs = fscr + (size_t)cb * fstride;
+    auto fl = [&](int d, int var, int x0, int x1, int x2) -> double {
+        return (double)fs[(size_t)d * NFLX * NFC + (size_t)var * NFC + flux_index(d, x0, x1, x2)];
+    };
+    int t[3];
+    auto at = [&](int av, int bv, int cv) { t[a] = av; t[b] = bv; t[c] = cv; };
+    at(A, B - 1, C); double ea0 = -fl(a, 5 + b, t[0], t[1], t[2]); double ma0 = fl(a, 0, t[0], t[1], t[2]);
+    at(A, B, C);     double ea1 = -fl(a, 5 + b, t[0], t[1], t[2]); double ma1 = fl(a, 0, t[0], t[1], t[2]);
+    at(A - 1, B, C); double eb0 = fl(b, 5 + a, t[0], t[1], t[2]);  double mb0 = fl(b, 0, t[0], t[1], t[2]);
+    at(A, B, C);     double eb1 = fl(b, 5 + a, t[0], t[1], t[2]);  double mb1 = fl(b, 0, t[0], t[1], t[2]);
+    const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
+    double ecc[2][2];
+#pragma unroll
+    for (int ia = 0; ia < 2; ++ia)
+#pragma unroll
+        for (int ib = 0; ib < 2; ++ib) {
+            at(A - 1 + ia, B - 1 + ib, C);
+            int ci = gb_cidx(t[0], t[1], t[2]);
+            double va = base[(int64_t)g.slot[GB_VELX + a] * GB_N3 + ci];
+            double vb = base[(int64_t)g.slot[GB_VELX + b] * GB_N3 + ci];
+            double Ba = base[(int64_t)g.slot[GB_MAGX + a] * GB_N3 + ci];
+            double Bb = base[(int64_t)g.slot[GB_MAGX + b] * GB_N3 + ci];
+            ecc[ia][ib] = vb * Ba - va * Bb;
+        }
+    double eavg = 0.25 * (ea0 + ea1 + eb0 + eb1);
+    double dbm = upw(ma0, 2.0 * (eb0 - ecc[0][0]), 2.0 * (eb1 - ecc[1][0]));
+    double dbp = upw(ma1, 2.0 * (ecc[0][1] - eb0), 2.0 * (ecc[1][1] - eb1));
+    double dam = upw(mb0, 2.0 * (ea0 - ecc[0][0]), 2.0 * (ea1 - ecc[0][1]));
+    double dap = upw(mb1, 2.0 * (ecc[1][0] - ea0), 2.0 * (ecc[1][1] - ea1));
+    escr[(size_t)cb * estride + (size_t)c * NEDGE + e] = eavg + 0.125 * (dbm - dbp) + 0.125 * (dam - dap);
+}
+
+__device__ __forceinline__ int edge_index(int c, int i, int j, int k)
+{
+    int I[3] = {i, j, k};
+    int a = (c + 1) % 3, b = (c + 2) % 3;
+    return (I[a] - LO) + 17 * ((I[b] - LO) + 17 * (I[c] - LO));
+}
+
+// interior face box of direction a: normal 4..20 (17), transverse 4..19 (16)
+__device__ __forceinline__ void fb_coords(int a, int f, int* I)
+{
+    int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+    I[a] = LO + f % 17;
+    I[t1] = LO + (f / 17) % 16;
+    I[t2] = LO + f / (17 * 16);
+}
+__device__ __forceinline__ int fb_index(int a, int i, int j, int k)
+{
+    int I[3] = {i, j, k};
+    int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+    return (I[a] - LO) + 17 * ((I[t1] - LO) + 16 * (I[t2] - LO));
+}
+
+static __global__ void __launch_bounds__(128)
+k_faceb(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const double* __restrict__ escr,
+        size_t estride, double* __restrict__ bscr, size_t bstride)
+{
+    const int a = blockIdx.y;
+    const int cb = blockIdx.z;
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= NFB) return;
+    const int blk = list[cb];
+    const int bb = (a + 1) % 3, c = (a + 2) % 3;
+    int I[3];
+    fb_coords(a, f, I);
+    int t1[3] = {I[0], I[1], I[2]}, t3[3] = {I[0], I[1], I[2]};
+    t1[bb] += 1;
+    t3[c] += 1;
+    const double* es = escr + (size_t)cb * estride;
+    double ec0 = es[(size_t)c * NEDGE + edge_index(c, I[0], I[1], I[2])];
+    double ec1 = es[(size_t)c * NEDGE + edge_index(c, t1[0], t1[1], t1[2])];
+    double eb0 = es[(size_t)bb * NEDGE + edge_index(bb, I[0], I[1], I[2])];
+    double eb1 = es[(size_t)bb * NEDGE + edge_index(bb, t3[0], t3[1], t3[2])];
+    double dxl[3];
+    gb_block_dx(g, kp.dx, blk, dxl);
+    double dtd_b = kp.dt / dxl[bb], dtd_c = kp.dt / dxl[c];
+    double old = g.f[a][(int64_t)blk * GB_FSZ + gb_fidx(a, I[0], I[1], I[2])];
+    bscr[(size_t)cb * bstride + (size_t)a * NFB + f] = old - dtd_b * (ec1 - ec0) + dtd_c * (eb1 - eb0);
+}
+
+// ---------------------------------------------------------------- k_update
+template <typename T, bool MHD, bool COOL>
+__global__ void __launch_bounds__(128)
+k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restrict__ list,
+         const T* __restrict__ fscr, size_t fstride, const double* __restrict__ bscr, size_t bstride,
+         gb_status* st)
+{
+    const int cb = blockIdx.y;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= GB_NXB * GB_NXB * GB_NXB) return;
+    const int blk = list[cb];
+    const int i = LO + t % GB_NXB, j = LO + (t / GB_NXB) % GB_NXB, k = LO + t / (GB_NXB * GB_NXB);
+    const int ci = gb_cidx(i, j, k);
+    double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
+    auto UV = [&](int role) -> double& { return base[(int64_t)g.slot[role] * GB_N3 + ci]; };
+    const double gm1 = kp.gamma - 1.0;
+    double rho = UV(GB_DENS), vx = UV(GB_VELX), vy = UV(GB_VELY), vz = UV(GB_VELZ), pr = UV(GB_PRES);
+    double Bc[3] = {0.0, 0.0, 0.0};
+    if (MHD) { Bc[0] = UV(GB_MAGX); Bc[1] = UV(GB_MAGY); Bc[2] = UV(GB_MAGZ); }
+    double Uc[NP];
+    Uc[0] = rho;
+    Uc[1] = rho * vx; Uc[2] = rho * vy; Uc[3] = rho * vz;
+    Uc[4] = pr / gm1 + 0.5 * rho * (vx * vx + vy * vy + vz * vz) + 0.5 * (Bc[0] * Bc[0] + Bc[1] * Bc[1] + Bc[2] * Bc[2]);
+    Uc[5] = Bc[0]; Uc[6] = Bc[1]; Uc[7] = Bc[2];
+    double re = rho * UV(GB_EINT);
+    const T* fs = fscr + (size_t)cb * fstride;
+    const int fm[3] = {flux_index(0, i, j, k), flux_index(1, i, j, k), flux_index(2, i, j, k)};
+    const int fp[3] = {flux_index(0, i + 1, j, k), flux_index(1, i, j + 1, k), flux_index(2, i, j, k + 1)};
+    double dxl[3];
+    gb_block_dx(g, kp.dx, blk, dxl);
+    const double dtd[3] = {kp.dt / dxl[0], kp.dt / dxl[1], kp.dt / dxl[2]};
+    auto F = [&](int d, int var, int idx) -> double {
+        return (double)fs[(size_t)d * NFLX * NFC + (size_t)var * NFC + idx];
+    };
+    double Un[5];
+#pragma unroll
+    for (int s = 0; s < 5; ++s)
+        Un[s] = Uc[s] - dtd[0] * (F(0, s, fp[0]) - F(0, s, fm[0])) - dtd[1] * (F(1, s, fp[1]) - F(1, s, fm[1])) -
+                dtd[2] * (F(2, s, fp[2]) - F(2, s, fm[2]));
+    double divv = (F(0, 9, fp[0]) - F(0, 9, fm[0])) / dxl[0] + (F(1, 9, fp[1]) - F(1, 9, fm[1])) / dxl[1] +
+                  (F(2, 9, fp[2]) - F(2, 9, fm[2])) / dxl[2];
+    double ren = re - dtd[0] * (F(0, 8, fp[0]) - F(0, 8, fm[0])) - dtd[1] * (F(1, 8, fp[1]) - F(1, 8, fm[1])) -
+                 dtd[2] * (F(2, 8, fp[2]) - F(2, 8, fm[2])) - kp.dt * pr * divv;
+    double Bn[3] = {0.0, 0.0, 0.0};
+    if (MHD) {
+        const double* bs = bscr + (size_t)cb * bstride;
+        double blo[3] = {bs[0 * NFB + fb_index(0, i, j, k)], bs[1 * NFB + fb_index(1, i, j, k)],
+                         bs[2 * NFB + fb_index(2, i, j, k)]};
+        double bhi[3] = {bs[0 * NFB + fb_index(0, i + 1, j, k)], bs[1 * NFB + fb_index(1, i, j + 1, k)],
+                         bs[2 * NFB + fb_index(2, i, j, k + 1)]};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) Bn[d] = 0.5 * (blo[d] + bhi[d]);
+        // write back the interior faces: low faces by every cell, high
+        // faces by the cells on the upper boundary
+        g.f[0][(int64_t)blk * GB_FSZ + gb_fidx(0, i, j, k)] = blo[0];
+        g.f[1][(int64_t)blk * GB_FSZ + gb_fidx(1, i, j, k)] = blo[1];
+        g.f[2][(int64_t)blk * GB_FSZ + gb_fidx(2, i, j, k)] = blo[2];
+        if (i == HI) g.f[0][(int64_t)blk * GB_FSZ + gb_fidx(0, i + 1, j, k)] = bhi[0];
+        if (j == HI) g.f[1][(int64_t)blk * GB_FSZ + gb_fidx(1, i, j + 1, k)] = bhi[1];
+        if (k == HI) g.f[2][(int64_t)blk * GB_FSZ + gb_fidx(2, i, j, k + 1)] = bhi[2];
+    }
+    double rn = fmax(Un[0], kp.smlrho);
+    double ek = 0.5 * (Un[1] * Un[1] + Un[2] * Un[2] + Un[3] * Un[3]) / rn;
+    double em = 0.5 * (Bn[0] * Bn[0] + Bn[1] * Bn[1] + Bn[2] * Bn[2]);
+    double eiE = ((Un[4] - ek) - em) / rn;
+    double eia = ren / rn;
+    bool use_E = eiE > kp.eint_switch * (Un[4] / rn);
+    double ei = use_E ? eiE : eia;
+    double pn = gm1 * rn * ei;
+    bool floored = false;
+    if (pn < kp.smallp) {
+        pn = kp.smallp;
+        ei = pn / (gm1 * rn);
+        floored = true;
+    }
+    double vxn = Un[1] / rn, vyn = Un[2] / rn, vzn = Un[3] / rn;
+    double ekin_s = 0.5 * (vxn * vxn + vyn * vyn + vzn * vzn);
+    if (COOL) {
+        // fused heating/cooling epilogue (RadHeat.F90:223-423 on the new state)
+        const gb_cool_params& p = cool.p;
+        gb_cool_vars v;
+        v.rho = rn * p.dens_unit;
+        double eic = ei * (p.vel_unit * p.vel_unit);
+        double temp = eic * (gm1 * p.eos_abar * p.mp / p.boltz);
+        v.tdust = UV(GB_TDUS);
+        v.xHp = g.slot[GB_IHP] >= 0 ? UV(GB_IHP) : p.xHp_const;
+        v.ephen = g.slot[GB_PHHE] >= 0 ? UV(GB_PHHE) / v.rho : 0.0;
+        v.Gflux = g.slot[GB_PEFL] >= 0 ? UV(GB_PEFL) : 0.0;
+        v.mu_mol = p.mu_mol;
+        v.strat_factor = 1.0;
+        gb_cool_diag dg = {0, 0, 0, 0, 0};
+        gbcool::heating_and_cooling(cool, v, &eic, kp.dt * p.time_unit, &temp, &dg);
+        bool clamped = false;
+        if (temp > p.absTmax) {
+            eic = p.absTmax * v.TtoEI;
+            temp = p.absTmax;
+            clamped = true;
+        }
+        if (eic < p.smallp / v.rho) eic = p.smallp / v.rho;
+        ei = eic / (p.vel_unit * p.vel_unit);
+        pn = gm1 * rn * ei;
+        UV(GB_TEMP) = temp;
+        UV(GB_TDUS) = v.tdust;
+        if (g.slot[GB_PHHE] >= 0) UV(GB_PHHE) = 0.0;
+        if (g.slot[GB_PEFL] >= 0) UV(GB_PEFL) = 0.0;
+        if (st) {
+            gb_count_warp(&st->n_bracket_fail, dg.bracket_fail != 0);
+            gb_count_warp(&st->n_clamped, clamped);
+            if (dg.unbracketed) gb_fail(st, GB_ST_ZERO_UNBRACKETED, blk, i, j, k, eic);
+            if (dg.maxiter) gb_fail(st, GB_ST_ZERO_MAXITER, blk, i, j, k, eic);
+        }
+    }
+    UV(GB_DENS) = rn;
+    UV(GB_VELX) = vxn;
+    UV(GB_VELY) = vyn;
+    UV(GB_VELZ) = vzn;
+    UV(GB_PRES) = pn;
+    UV(GB_EINT) = ei;
+    UV(GB_ENER) = ei + ekin_s;
+    if (MHD) { UV(GB_MAGX) = Bn[0]; UV(GB_MAGY) = Bn[1]; UV(GB_MAGZ) = Bn[2]; }
+    if (st) {
+        gb_count_warp(&st->n_eint_switch, !use_E);
+        if (!(Un[0] > 0.0)) gb_fail(st, GB_ST_NEG_DENS, blk, i, j, k, Un[0]);
+        else if (!isfinite(pn) || !isfinite(Un[4])) gb_fail(st, GB_ST_NONFINITE, blk, i, j, k, pn);
+        else if (floored) gb_fail(st, GB_ST_NEG_PRES, blk, i, j, k, eiE);
+    }
+}
+
+// ---------------------------------------------------------------- CFL
+static __global__ void __launch_bounds__(256)
+k_dtlimit(gb_dev_grid g, double gamma, int mhd, double dx0, double dx1, double dx2,
+          const int* __restrict__ list, unsigned long long* __restrict__ out_bits)
+{
+    const int blk = list[blockIdx.y];
+    const double root[3] = {dx0, dx1, dx2};
+    double del[3];
+    gb_block_dx(g, root, blk, del);
+    double best = 1e300;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < GB_NXB * GB_NXB * GB_NXB; t += gridDim.x * blockDim.x) {
+        const int i = LO + t % GB_NXB, j = LO + (t / GB_NXB) % GB_NXB, k = LO + t / (GB_NXB * GB_NXB);
+        const int ci = gb_cidx(i, j, k);
+        const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3 + ci;
+        double rho = base[(int64_t)g.slot[GB_DENS] * GB_N3], p = base[(int64_t)g.slot[GB_PRES] * GB_N3];
+        double B[3] = {0, 0, 0};
+        if (mhd) {
+            B[0] = base[(int64_t)g.slot[GB_MAGX] * GB_N3];
+            B[1] = base[(int64_t)g.slot[GB_MAGY] * GB_N3];
+            B[2] = base[(int64_t)g.slot[GB_MAGZ] * GB_N3];
+        }
+        double gp = gamma * p;
+        double B2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+        double tt = (gp + B2) / rho;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            double v = fabs(base[(int64_t)g.slot[GB_VELX + d] * GB_N3]);
+            double cf = sqrt(0.5 * (tt + sqrt(fmax(tt * tt - 4.0 * gp * B[d] * B[d] / (rho * rho), 0.0))));
+            double dtc = del[d] / (v + cf);
+            best = fmin(best, dtc);
+        }
+    }
+    // warp shuffle then block reduction of the minimum
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, o));
+    __shared__ double s_min[8];
+    if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = best;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        best = threadIdx.x < (blockDim.x >> 5) ? s_min[threadIdx.x] : 1e300;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, o));
+        // positive doubles order like their bit patterns
+        if (threadIdx.x == 0) atomicMin(out_bits, (unsigned long long)__double_as_longlong(best));
+    }
+}
+
+}  // namespace gbh

@@ -1,0 +1,47 @@
+// Launch sequence of one unsplit step over a chunk of blocks for one
+// reconstruction precision T. Included by hydro_fp64.cu (T = double,
+// compiled with -fmad=false) and hydro_mixed.cu (T = float).
+#pragma once
+
+#include "gb_state.h"
+#include "hydro_dev.cuh"
+
+namespace gbh {
+
+template <typename T>
+int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
+                 void* scratch, gb_status* st, cudaStream_t s)
+{
+    using SL = scratch_layout<T>;
+    // scratch of the chunk: [recon | flux | emf | faceb], each block-major
+    char* base = (char*)scratch;
+    T* rscr = (T*)base;
+    T* fscr = (T*)(base + (size_t)nblk * SL::recon * sizeof(T));
+    double* escr = (double*)(base + (size_t)nblk * (SL::recon + SL::flux) * sizeof(T));
+    double* bscr = escr + (size_t)nblk * SL::emf;
+    const gb_dev_grid& g = g_gb.grid;
+    dim3 rg((NRC + RECON_TILE - 1) / RECON_TILE, nblk);
+    dim3 fg((NFC + 127) / 128, 3, nblk);
+    if (mhd) {
+        k_recon<T, true><<<rg, 3 * RECON_TILE, 0, s>>>(g, kp, list, rscr, SL::recon, st);
+        k_flux<T, true><<<fg, 128, 0, s>>>(g, kp, list, rscr, fscr, SL::flux);
+        dim3 eg((NEDGE + 127) / 128, 3, nblk);
+        k_emf<T><<<eg, 128, 0, s>>>(g, list, fscr, SL::flux, escr, SL::emf);
+        dim3 bg((NFB + 127) / 128, 3, nblk);
+        k_faceb<<<bg, 128, 0, s>>>(g, kp, list, escr, SL::emf, bscr, SL::fb);
+    } else {
+        k_recon<T, false><<<rg, 3 * RECON_TILE, 0, s>>>(g, kp, list, rscr, SL::recon, st);
+        k_flux<T, false><<<fg, 128, 0, s>>>(g, kp, list, rscr, fscr, SL::flux);
+    }
+    dim3 ug((GB_NXB * GB_NXB * GB_NXB + 127) / 128, nblk);
+    if (mhd) {
+        if (cool) k_update<T, true, true><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st);
+        else k_update<T, true, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st);
+    } else {
+        if (cool) k_update<T, false, true><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st);
+        else k_update<T, false, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st);
+    }
+    return gb_check(cudaGetLastError(), "hydro chunk launch") ? GB_ERR_CUDA : GB_OK;
+}
+
+}  // namespace gbh

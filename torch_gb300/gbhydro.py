@@ -1,0 +1,367 @@
+"""Python host over libgbhydro.so (ctypes), with torch for device memory.
+
+Mirrors the reference's per-step call surface for the hot path:
+
+* ``Hydro(blockCount, blockList, timeEndAdv, dt, dtOld, sweepOrder)``
+  (src/flash/source/physics/Hydro/HydroMain/unsplit/hy_uhd_interface.F90:472-479,
+  called at src/flash/source/Driver/DriverMain/Unsplit/Couple_AMUSE/Driver_evolveFlash.F90:406)
+* ``Heat(blockCount, blockList, dt, time)``
+  (src/flash/source/physics/sourceTerms/Heat/HeatMain/HeatCool/phenHeat/Heat_interface.F90:10-16)
+* ``Driver_computeDt`` reduced to the CFL minimum over leaf blocks
+  (src/flash/source/Driver/DriverMain/Unsplit/Couple_AMUSE/Driver_computeDt.F90:327-335,514-515)
+
+FLASH's block ids are 1-based; ``blockList`` here takes FLASH ids and
+converts. Errors raise ``GBError`` (the reference aborts through
+Driver_abortFlash). There is no CPU fallback: without the CUDA library
+every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+from . import workloads as W
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+NROLE = 15
+ROLES = ["DENS", "VELX", "VELY", "VELZ", "PRES", "ENER", "EINT", "MAGX", "MAGY", "MAGZ", "TEMP",
+         "TDUS", "PHHE", "PEFL", "IHP"]
+R = {n: i for i, n in enumerate(ROLES)}
+NB = 24
+N3 = NB ** 3
+FSZ = NB * NB * (NB + 1)
+
+ST_NAMES = {0: "ok", 1: "negative density", 2: "pressure floored", 3: "non-finite state",
+            4: "root finder not bracketed", 5: "root finder iteration cap", 6: "overheated (T > absTmax)"}
+
+
+class GBError(RuntimeError):
+    pass
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("nvar", C.c_int), ("maxblocks", C.c_int), ("slot", C.c_int * NROLE),
+                ("unk", C.c_void_p), ("facex", C.c_void_p), ("facey", C.c_void_p),
+                ("facez", C.c_void_p)]
+
+
+class TreeDesc(C.Structure):
+    _fields_ = [("nnodes", C.c_int), ("nrx", C.c_int), ("nry", C.c_int), ("nrz", C.c_int),
+                ("maxlevel", C.c_int), ("level", C.c_void_p), ("coord", C.c_void_p),
+                ("child", C.c_void_p), ("root", C.c_void_p), ("xmin", C.c_double * 3),
+                ("root_dx", C.c_double * 3)]
+
+
+class HydroParams(C.Structure):
+    _fields_ = [("gamma", C.c_double), ("cfl", C.c_double), ("cvisc", C.c_double),
+                ("use_avisc", C.c_int), ("mhd", C.c_int), ("eint_switch", C.c_double),
+                ("smlrho", C.c_double), ("smallp", C.c_double), ("precision", C.c_int),
+                ("pad", C.c_int)]
+
+
+class CoolParams(C.Structure):
+    _fields_ = [
+        ("tradmin", C.c_double), ("tradmax", C.c_double), ("dradmin", C.c_double),
+        ("dradmax", C.c_double), ("theatmin", C.c_double), ("theatmax", C.c_double),
+        ("absTmin", C.c_double), ("absTmax", C.c_double), ("Gzero", C.c_double),
+        ("subfactor", C.c_double), ("smallp", C.c_double), ("use_cr_heating", C.c_int),
+        ("crIonRate", C.c_double), ("crIonNH", C.c_double), ("crIonExp", C.c_double),
+        ("crIonEnergy", C.c_double), ("dust_sputter_temp", C.c_double), ("pe_recipe", C.c_int),
+        ("pe_norm", C.c_double), ("boltz", C.c_double), ("mp", C.c_double),
+        ("T_cool_min", C.c_double), ("nd_cool_min", C.c_double), ("nd_cool_max", C.c_double),
+        ("useDustCool", C.c_int), ("int_method", C.c_int), ("mu_mol", C.c_double),
+        ("xHp_const", C.c_double), ("dens_unit", C.c_double), ("vel_unit", C.c_double),
+        ("time_unit", C.c_double), ("eos_abar", C.c_double),
+    ]
+
+
+class Status(C.Structure):
+    _fields_ = [("code", C.c_int), ("block", C.c_int), ("i", C.c_int), ("j", C.c_int),
+                ("k", C.c_int), ("pad", C.c_int), ("value", C.c_double),
+                ("n_fallback", C.c_ulonglong), ("n_bracket_fail", C.c_ulonglong),
+                ("n_dust_noconv", C.c_ulonglong), ("n_clamped", C.c_ulonglong),
+                ("n_eint_switch", C.c_ulonglong), ("n_surrogate", C.c_ulonglong),
+                ("n_surrogate_reject", C.c_ulonglong)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
+# every entry point the header declares: name -> (restype, argtypes)
+_SIG = {
+    "gb_register_grid": (C.c_int, [C.POINTER(GridDesc), C.POINTER(TreeDesc)]),
+    "gb_fill_guardcells": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p]),
+    "gb_hydro_init": (C.c_int, [C.POINTER(HydroParams)]),
+    "gb_hydro_unsplit": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_void_p]),
+    "gb_set_chunk_blocks": (C.c_int, [C.c_int]),
+    "gb_compute_dt": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gb_cool_init": (C.c_int, [C.c_char_p, C.POINTER(CoolParams)]),
+    "gb_heat": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_void_p]),
+    "gb_cool_cells": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]),
+    "gb_evolve_step": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_int, C.c_void_p, C.c_void_p]),
+    "gb_grid_upload_flash": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
+    "gb_grid_download_flash": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
+    "gb_status_reset": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gb_status_read": (C.c_int, [C.c_void_p, C.POINTER(Status)]),
+    "gb_last_error": (C.c_char_p, []),
+    "gb_version": (C.c_int, []),
+}
+
+_lib = None
+
+
+def lib(build: bool = True):
+    """Load (building if needed) the CUDA library. Raises if it cannot."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if build:
+            path = _build.build()
+        if not os.path.exists(path):
+            raise GBError(f"CUDA library missing: {path}")
+        L = C.CDLL(path)
+        for name, (res, args) in _SIG.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc: int, what: str = "") -> None:
+    if rc != 0:
+        raise GBError(f"{what}: rc={rc}: {lib().gb_last_error().decode(errors='replace')}")
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream():
+    import torch
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+# ------------------------------------------------------------------ parameters
+def hydro_params(mhd: bool, precision: int = 0, **over) -> HydroParams:
+    """Values of flash.par.turbsph_standard (:33, :163-165, :197-198) in
+    code units; floors are code-unit values."""
+    p = HydroParams(gamma=5.0 / 3.0, cfl=0.8, cvisc=0.1, use_avisc=1, mhd=int(mhd),
+                    eint_switch=1.0e-4, smlrho=1e-30, smallp=1e-30, precision=precision, pad=0)
+    for k, v in over.items():
+        setattr(p, k, v)
+    return p
+
+
+# CGS constants (CODATA 2006); FLASH's PhysicalConstants unit is not vendored
+KB = 1.3806504e-16
+MP = 1.672621637e-24
+PC = 3.0856775807e18
+
+
+def cool_params(**over) -> CoolParams:
+    """flash.par.turbsph_standard:300-390 (+ phenHeat/Config defaults)."""
+    p = CoolParams(
+        tradmin=10.0, tradmax=1.0e15, dradmin=1e-99, dradmax=1e10, theatmin=1e-99, theatmax=2.0e4,
+        absTmin=10.0, absTmax=1e9, Gzero=1.69, subfactor=0.3, smallp=1.3807e-19, use_cr_heating=1,
+        crIonRate=2.0e-17, crIonNH=1e20, crIonExp=0.021, crIonEnergy=20.0 * 1.6022e-12,
+        dust_sputter_temp=3e5, pe_recipe=0, pe_norm=1.3e-24, boltz=KB, mp=MP, T_cool_min=10.0,
+        nd_cool_min=1e1, nd_cool_max=1e10, useDustCool=1, int_method=0, mu_mol=24.0 / 11.0,
+        xHp_const=1e-4, dens_unit=1.0, vel_unit=1.0, time_unit=1.0, eos_abar=24.0 / 11.0)
+    for k, v in over.items():
+        setattr(p, k, v)
+    return p
+
+
+def code_units(n_mean: float = 10.0, T_mean: float = 100.0, box_pc: float = 1.0,
+               mu: float = 24.0 / 11.0):
+    """Code units of the turbulent-box workloads: mean density 1 <-> n_mean
+    cm^-3 of mean molecular weight mu; pressure 1 <-> rho n k T_mean/mu-ish
+    (v_unit^2 = k T_mean / (mu m_p)); box length 1 <-> box_pc parsec."""
+    rho_u = n_mean * mu * MP
+    v_u = np.sqrt(KB * T_mean / (mu * MP))
+    L_u = box_pc * PC
+    return dict(dens_unit=rho_u, vel_unit=float(v_u), time_unit=float(L_u / v_u), length_unit=L_u)
+
+
+# ------------------------------------------------------------------ block trees
+def uniform_tree(nbx: int, nby: int, nbz: int):
+    """A periodic root grid of same-level leaf blocks (block id = bx +
+    nbx*(by + nby*bz))."""
+    n = nbx * nby * nbz
+    ids = np.arange(n)
+    coord = np.stack([ids % nbx, (ids // nbx) % nby, ids // (nbx * nby)], 1).astype(np.int32)
+    return dict(level=np.zeros(n, np.int32), coord=coord, child=-np.ones((n, 8), np.int32),
+                root=ids.astype(np.int32), nr=(nbx, nby, nbz), maxlevel=0)
+
+
+class Grid:
+    """Device block store + block tree registered with the library."""
+
+    def __init__(self, nblocks: int, nvar: int, slots: dict, mhd: bool, tree: dict,
+                 root_dx: float, device: str = "cuda"):
+        import torch
+        self.torch = torch
+        self.nblocks, self.nvar, self.mhd = nblocks, nvar, mhd
+        self.u = torch.zeros((nblocks, nvar, NB, NB, NB), dtype=torch.float64, device=device)
+        if mhd:
+            self.fx = torch.zeros((nblocks, NB, NB, NB + 1), dtype=torch.float64, device=device)
+            self.fy = torch.zeros((nblocks, NB, NB + 1, NB), dtype=torch.float64, device=device)
+            self.fz = torch.zeros((nblocks, NB + 1, NB, NB), dtype=torch.float64, device=device)
+        else:
+            self.fx = self.fy = self.fz = None
+        self.slots = dict(slots)
+        t = lambda a: torch.as_tensor(np.ascontiguousarray(a, np.int32), device=device)
+        self.t_level = t(tree["level"])
+        self.t_coord = t(tree["coord"])
+        self.t_child = t(tree["child"])
+        self.t_root = t(tree["root"])
+        self.tree = tree
+        self.root_dx = root_dx
+        self.status = torch.zeros(16, dtype=torch.float64, device=device)  # >= sizeof(gb_status)
+        self.leaf = np.nonzero(tree["child"][:, 0] < 0)[0].astype(np.int32)
+        self.t_leaf = t(self.leaf)
+        self.register()
+
+    def register(self):
+        d = GridDesc()
+        d.nvar, d.maxblocks = self.nvar, self.nblocks
+        for r in range(NROLE):
+            d.slot[r] = -1
+        for name, s in self.slots.items():
+            d.slot[R[name]] = s
+        d.unk = self.u.data_ptr()
+        if self.mhd:
+            d.facex, d.facey, d.facez = self.fx.data_ptr(), self.fy.data_ptr(), self.fz.data_ptr()
+        tr = TreeDesc()
+        tr.nnodes = int(self.tree["level"].shape[0])
+        tr.nrx, tr.nry, tr.nrz = self.tree["nr"]
+        tr.maxlevel = int(self.tree["maxlevel"])
+        tr.level, tr.coord = self.t_level.data_ptr(), self.t_coord.data_ptr()
+        tr.child, tr.root = self.t_child.data_ptr(), self.t_root.data_ptr()
+        for q in range(3):
+            tr.root_dx[q] = self.root_dx
+            tr.xmin[q] = 0.0
+        self._desc, self._tree = d, tr
+        check(lib().gb_register_grid(C.byref(d), C.byref(tr)), "gb_register_grid")
+
+    # --------------------------------------------------------------- status
+    def status_reset(self):
+        check(lib().gb_status_reset(_ptr(self.status), _stream()), "gb_status_reset")
+
+    def status_read(self) -> dict:
+        self.torch.cuda.synchronize()
+        s = Status()
+        check(lib().gb_status_read(_ptr(self.status), C.byref(s)), "gb_status_read")
+        return s.as_dict()
+
+    # --------------------------------------------------------------- steps
+    def list_tensor(self, blockList=None):
+        if blockList is None:
+            return self.t_leaf, len(self.leaf)
+        ids = np.asarray(blockList, np.int32) - 1  # FLASH ids are 1-based
+        return self.torch.as_tensor(ids, device=self.u.device), len(ids)
+
+    def fill_guardcells(self, blockList=None):
+        lt, n = self.list_tensor(blockList)
+        check(lib().gb_fill_guardcells(n, _ptr(lt), _stream()), "gb_fill_guardcells")
+
+    def compute_dt(self, blockList=None):
+        lt, n = self.list_tensor(blockList)
+        out = self.torch.zeros(1, dtype=self.torch.float64, device=self.u.device)
+        check(lib().gb_compute_dt(n, _ptr(lt), _ptr(out), _stream()), "gb_compute_dt")
+        return out
+
+    def evolve_step(self, dt: float, cool: bool, blockList=None):
+        lt, n = self.list_tensor(blockList)
+        check(lib().gb_evolve_step(n, _ptr(lt), float(dt), int(cool), _ptr(self.status), _stream()),
+              "gb_evolve_step")
+
+
+def init_hydro(p: HydroParams) -> None:
+    check(lib().gb_hydro_init(C.byref(p)), "gb_hydro_init")
+
+
+def init_cooling(p: CoolParams, table_path: str | None = None) -> None:
+    from . import tables
+    path = table_path or tables.COMPACT_PATH
+    check(lib().gb_cool_init(path.encode(), C.byref(p)), "gb_cool_init")
+
+
+def set_chunk_blocks(n: int) -> None:
+    check(lib().gb_set_chunk_blocks(int(n)), "gb_set_chunk_blocks")
+
+
+# --------------------------------------------------------------- FLASH surface
+_active: Grid | None = None
+
+
+def use_grid(g: Grid) -> None:
+    global _active
+    _active = g
+
+
+def Hydro(blockCount: int, blockList, timeEndAdv: float, dt: float, dtOld: float, sweepOrder: int = 0):
+    """FLASH ``Hydro`` -> ``hy_uhd_unsplit(blockCount, blockList, dt, dtOld)``
+    on the active grid: guard-cell fill, then one unsplit step of the
+    listed (1-based) leaf blocks."""
+    g = _require()
+    lt, n = g.list_tensor(np.asarray(blockList)[:blockCount])
+    check(lib().gb_fill_guardcells(n, _ptr(lt), _stream()), "Grid_fillGuardCells")
+    check(lib().gb_hydro_unsplit(n, _ptr(lt), float(dt), float(dtOld), _ptr(g.status), _stream()),
+          "hy_uhd_unsplit")
+
+
+def Heat(blockCount: int, blockList, dt: float, time: float):
+    """FLASH ``Heat`` -> ``RadHeat`` per-cell heating/cooling on the active
+    grid (the ``he_int_method = "Implicit"`` integrator)."""
+    g = _require()
+    lt, n = g.list_tensor(np.asarray(blockList)[:blockCount])
+    check(lib().gb_heat(n, _ptr(lt), float(dt), float(time), _ptr(g.status), _stream()), "RadHeat")
+
+
+def Driver_computeDt(blockCount: int, blockList) -> float:
+    """CFL minimum over the listed leaf blocks (the device reduction that
+    replaces Hydro_computeDt + MPI_AllReduce MINLOC)."""
+    g = _require()
+    return float(g.compute_dt(np.asarray(blockList)[:blockCount]).item())
+
+
+def _require() -> Grid:
+    if _active is None:
+        raise GBError("no active grid: call use_grid(Grid(...)) first")
+    return _active
+
+
+def cool_cells(dens, ei, temp, tdust, dt, xhp=None, phhe=None, gflux=None, status=None):
+    """Per-cell solve on CGS device arrays (torch float64, updated in place)."""
+    n = dens.numel()
+    check(lib().gb_cool_cells(n, _ptr(dens), _ptr(ei), _ptr(temp), _ptr(tdust), _ptr(xhp), _ptr(phhe),
+                              _ptr(gflux), float(dt), _ptr(status), _stream()), "gb_cool_cells")
+
+
+def grid_from_workload(ic: dict, mhd: bool, cooling: bool, device: str = "cuda") -> Grid:
+    """Build a registered Grid from a workloads.turbulent_box dict."""
+    nbx, nby, nbz = ic["nbx"], ic["nby"], ic["nbz"]
+    slots = {n: i for i, n in enumerate(["DENS", "VELX", "VELY", "VELZ", "PRES", "ENER", "EINT"])}
+    nvar = 7
+    if mhd:
+        slots.update(MAGX=7, MAGY=8, MAGZ=9)
+        nvar = 10
+    if cooling:
+        slots.update(TEMP=nvar, TDUS=nvar + 1)
+        nvar += 2
+    tree = uniform_tree(nbx, nby, nbz)
+    g = Grid(nbx * nby * nbz, nvar, slots, mhd, tree, ic["dx"], device)
+    import torch
+    k = 10 if mhd else 7
+    g.u[:, :k] = torch.as_tensor(ic["u"][:, :k], device=device)
+    if mhd:
+        g.fx.copy_(torch.as_tensor(ic["fx"], device=device))
+        g.fy.copy_(torch.as_tensor(ic["fy"], device=device))
+        g.fz.copy_(torch.as_tensor(ic["fz"], device=device))
+    return g
