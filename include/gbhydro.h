@@ -203,6 +203,44 @@ int gb_grid_upload_flash(const double* unk_host, int nunk, const int* host_slot,
 int gb_grid_download_flash(double* unk_host, int nunk, const int* host_slot, int nblocks,
                            void* stream);
 
+/* ---------------------------------------------------------------- surrogate */
+/* Learned cooling surrogate (no counterpart in the reference): an MLP
+ * 4 -> 64 -> 64 -> 64 -> 1 with SiLU, BF16 weights, FP32 accumulation.
+ * Inputs per cell, normalised: log10 n [cm^-3], log10 T [K],
+ * log10(dt / t_cool) with t_cool = e / |de/dt| of the plain integrator's
+ * rate function, log10 G [G0] (FUV field). Output: (log10 T_new -
+ * log10 T) / 4. Parameters are one flat FP32 vector: W1[64][4], b1[64],
+ * W2[64][64], b2[64], W3[64][64], b3[64], W4[1][64], b4[1]. */
+#define GB_MLP_IN 4
+#define GB_MLP_HIDDEN 64
+#define GB_MLP_NPARAM (64 * 4 + 64 + 64 * 64 + 64 + 64 * 64 + 64 + 64 + 1)
+
+int gb_mlp_init_random(uint64_t seed);
+int gb_mlp_set_weights(const float* host, int n);
+int gb_mlp_get_weights(float* host, int n);
+/* Loss and gradient of the mean squared error on n device samples
+ * (feat: n x 4, target: n) into host buffers (for gradient checks). */
+int gb_mlp_grad(const float* feat_dev, const float* target_dev, int n, float* grad_host, float* loss_host,
+                void* stream);
+/* Adam training on device samples: `steps` mini-batches of `batch` drawn
+ * with a seeded generator; per-step loss written to loss_host (may be NULL). */
+int gb_mlp_train(const float* feat_dev, const float* target_dev, int64_t n, int steps, int batch, float lr,
+                 uint64_t seed, float* loss_host, void* stream);
+/* Inference on n cells; tensor_cores = 1 uses the BF16 mma path, 0 a
+ * CUDA-core FP32 path with the same BF16-rounded weights. */
+int gb_mlp_infer(int64_t n, const float* feat_dev, float* y_dev, int tensor_cores, void* stream);
+/* Training samples from the plain implicit integrator: log n ~ U[-2, 6],
+ * log T ~ U[1, 8], log(dt/t_cool) ~ U[-3, 3], log G ~ U[-1, 1]; writes
+ * normalised features (n x 4) and targets (n); rows where the root finder
+ * failed get target NaN. */
+int gb_surrogate_samples(int64_t n, uint64_t seed, float* feat_dev, float* target_dev, gb_status* st_dev,
+                         void* stream);
+/* Cooling mode of gb_evolve_step(cool = 1): 0 = plain integrator fused in
+ * the update, 1 = surrogate with per-cell acceptance test and plain
+ * fallback. rel_tol: accepted relative change of e_int per the Newton
+ * estimate of the backward-Euler residual. */
+int gb_set_cooling_mode(int mode, double rel_tol);
+
 /* ---------------------------------------------------------------- misc */
 int gb_status_reset(gb_status* st_dev, void* stream);
 int gb_status_read(const gb_status* st_dev, gb_status* st_host);

@@ -81,9 +81,10 @@ def test_heat_on_grid_matches_oracle(gb, oracle):
     out = u.cpu().numpy()
     rho = host[:, 0][sl].ravel() * units["dens_unit"]
     ei = host[:, 6][sl].ravel() * units["vel_unit"] ** 2
-    e_o, T_o, td_o, flags = _run_oracle(oracle, rho, ei, host[:, 10][sl].ravel(), host[:, 11][sl].ravel(),
+    sT, sD = g.slots["TEMP"], g.slots["TDUS"]
+    e_o, T_o, td_o, flags = _run_oracle(oracle, rho, ei, host[:, sT][sl].ravel(), host[:, sD][sl].ravel(),
                                         dt * units["time_unit"])
-    T_g = out[:, 10][sl].ravel()
+    T_g = out[:, sT][sl].ravel()
     tolT = np.maximum(1.0, 1e-6 * T_o) * 2.0
     assert np.all(np.abs(T_g - T_o) <= tolT)
     e_g = out[:, 6][sl].ravel() * units["vel_unit"] ** 2

@@ -367,6 +367,9 @@ static gbh::hydro_kparams make_kp(double dt)
     return kp;
 }
 
+int gb_cooling_mode();
+int gb_launch_surrogate(int nblk, const int* list, double dt, gb_status* st, cudaStream_t s);
+
 int gb_launch_hydro(int nblk, const int* list, double dt, int cool, gb_status* st, cudaStream_t s)
 {
     const int chunk = g_chunk_blocks < nblk ? g_chunk_blocks : nblk;
@@ -377,9 +380,14 @@ int gb_launch_hydro(int nblk, const int* list, double dt, int cool, gb_status* s
     gbh::hydro_kparams kp = make_kp(dt);
     for (int b0 = 0; b0 < nblk; b0 += chunk) {
         int nb = nblk - b0 < chunk ? nblk - b0 : chunk;
-        rc = mixed ? gb_hydro_chunk_mixed(kp, g_gb.hp.mhd, cool, nb, list + b0, g_gb.d_scratch, st, s)
-                   : gb_hydro_chunk_fp64(kp, g_gb.hp.mhd, cool, nb, list + b0, g_gb.d_scratch, st, s);
+        const int fused = cool && gb_cooling_mode() == 0;
+        rc = mixed ? gb_hydro_chunk_mixed(kp, g_gb.hp.mhd, fused, nb, list + b0, g_gb.d_scratch, st, s)
+                   : gb_hydro_chunk_fp64(kp, g_gb.hp.mhd, fused, nb, list + b0, g_gb.d_scratch, st, s);
         if (rc) return rc;
+        if (cool && !fused) {
+            rc = gb_launch_surrogate(nb, list + b0, dt, st, s);
+            if (rc) return rc;
+        }
     }
     return GB_OK;
 }
@@ -392,7 +400,10 @@ extern "C" int gb_hydro_unsplit(int blockCount, const int* list, double dt, doub
         gb_set_error("gb_hydro_unsplit: call gb_register_grid and gb_hydro_init first");
         return GB_ERR_NOT_INIT;
     }
-    if (blockCount < 0 || (blockCount > 0 && !list) || !(dt > 0.0)) return GB_ERR_ARG;
+    if (blockCount < 0 || (blockCount > 0 && !list) || !(dt > 0.0)) {
+        gb_set_error("gb_hydro_unsplit: bad block list or dt = %g", dt);
+        return GB_ERR_ARG;
+    }
     if (g_gb.hp.mhd && (!g_gb.grid.f[0] || !g_gb.grid.f[1] || !g_gb.grid.f[2] || g_gb.grid.slot[GB_MAGX] < 0 ||
                         g_gb.grid.slot[GB_MAGY] < 0 || g_gb.grid.slot[GB_MAGZ] < 0)) {
         gb_set_error("gb_hydro_unsplit: MHD needs face fields and MAG slots");
@@ -440,7 +451,10 @@ extern "C" int gb_evolve_step(int blockCount, const int* list, double dt, int co
         gb_set_error("gb_evolve_step: cooling needs TEMP and TDUS slots");
         return GB_ERR_ARG;
     }
-    if (blockCount <= 0 || !list || !(dt > 0.0)) return GB_ERR_ARG;
+    if (blockCount <= 0 || !list || !(dt > 0.0)) {
+        gb_set_error("gb_evolve_step: bad block list or dt = %g", dt);
+        return GB_ERR_ARG;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     int rc = gb_launch_guardfill(blockCount, list, s);
     if (rc) return rc;

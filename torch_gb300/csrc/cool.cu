@@ -257,3 +257,287 @@ extern "C" int gb_cool_cells(int64_t n, const double* dens, double* ei, double* 
                                                                   xhp, phhe, gflux, dt, st);
     return gb_check(cudaGetLastError(), "k_cool_cells") ? GB_ERR_CUDA : GB_OK;
 }
+
+// ---------------------------------------------------------------- surrogate
+#include "mlp.h"
+#include "sur_common.cuh"
+
+namespace {
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double uni(uint64_t seed, int64_t i, int k)
+{
+    uint64_t z = mix64(seed + 0x9E3779B97F4A7C15ULL * (uint64_t)(4 * i + k + 1));
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// t_cool and the plain integrator's solution for one training sample
+__global__ void k_sur_samples(gb_cool_ctx c, int64_t n, uint64_t seed, float* __restrict__ feat,
+                              float* __restrict__ target, gb_status* st)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double lnn = -2.0 + 8.0 * uni(seed, i, 0), lT = 1.0 + 7.0 * uni(seed, i, 1),
+                 lr = -3.0 + 6.0 * uni(seed, i, 2), lG = -1.0 + 2.0 * uni(seed, i, 3);
+    const double nden = pow(10.0, lnn), T0 = pow(10.0, lT), G = pow(10.0, lG);
+    gb_cool_ctx cc = c;
+    cc.p.Gzero = G;
+    const gb_cool_params& p = cc.p;
+    const double TtoEI = p.boltz / ((5.0 / 3.0 - 1.0) * p.eos_abar * p.mp);
+    gb_cool_vars v;
+    v.rho = nden * p.mu_mol * p.mp;
+    v.tdust = 15.0;
+    v.xHp = p.xHp_const;
+    v.ephen = 0.0;
+    v.Gflux = 0.0;
+    v.mu_mol = p.mu_mol;
+    v.strat_factor = 1.0;
+    double ei = T0 * TtoEI, temp = T0;
+    v.ndens = v.rho / (v.mu_mol * p.mp);
+    v.TtoEI = ei / temp;
+    v.conf = v.ndens * v.ndens / v.rho;
+    double f0 = dei_dt(cc, v, cooling_floor(cc, v), ei);
+    double tcool = ei / fmax(fabs(f0), 1e-300);
+    double dt = pow(10.0, lr) * tcool;
+    gb_cool_diag d = {0, 0, 0, 0, 0};
+    heating_and_cooling(cc, v, &ei, dt, &temp, &d);
+    if (temp > p.absTmax) temp = p.absTmax;
+    float x[4];
+    gbsur::features(nden, T0, dt / tcool, G, x);
+    reinterpret_cast<float4*>(feat)[i] = make_float4(x[0], x[1], x[2], x[3]);
+    bool bad = d.unbracketed || d.maxiter || !isfinite(temp) || !(temp > 0.0);
+    target[i] = bad ? __int_as_float(0x7fc00000) : (float)((log10(temp) - lT) / gbsur::Y_SCALE);
+    if (st) gb_count_warp(&st->n_bracket_fail, d.bracket_fail != 0);
+}
+
+struct sur_cell {
+    double rho, ei, temp, TtoEI;
+};
+
+// state of one interior cell after the hydro update, in CGS
+__device__ __forceinline__ void sur_load(const gb_dev_grid& g, const gb_cool_ctx& c, double gamma, int blk, int ci,
+                                         gb_cool_vars& v, double& ei, double& temp)
+{
+    const gb_cool_params& p = c.p;
+    v.rho = gb_var(g, blk, GB_DENS)[ci] * p.dens_unit;
+    ei = gb_var(g, blk, GB_EINT)[ci] * (p.vel_unit * p.vel_unit);
+    temp = ei * ((gamma - 1.0) * p.eos_abar * p.mp / p.boltz);
+    v.tdust = gb_var(g, blk, GB_TDUS)[ci];
+    v.xHp = g.slot[GB_IHP] >= 0 ? gb_var(g, blk, GB_IHP)[ci] : p.xHp_const;
+    v.ephen = g.slot[GB_PHHE] >= 0 ? gb_var(g, blk, GB_PHHE)[ci] / v.rho : 0.0;
+    v.Gflux = g.slot[GB_PEFL] >= 0 ? gb_var(g, blk, GB_PEFL)[ci] : 0.0;
+    v.mu_mol = p.mu_mol;
+    v.strat_factor = 1.0;
+    v.ndens = v.rho / (v.mu_mol * p.mp);
+    v.TtoEI = ei / temp;
+    v.conf = v.ndens * v.ndens / v.rho;
+}
+
+__device__ __forceinline__ void sur_store(const gb_dev_grid& g, const gb_cool_ctx& c, double gamma, int blk, int ci,
+                                          const gb_cool_vars& v, double ei, double temp)
+{
+    const gb_cool_params& p = c.p;
+    if (ei < p.smallp / v.rho) ei = p.smallp / v.rho;
+    double vx = gb_var(g, blk, GB_VELX)[ci], vy = gb_var(g, blk, GB_VELY)[ci], vz = gb_var(g, blk, GB_VELZ)[ci];
+    double e = ei / (p.vel_unit * p.vel_unit);
+    double rho = gb_var(g, blk, GB_DENS)[ci];
+    gb_var(g, blk, GB_EINT)[ci] = e;
+    gb_var(g, blk, GB_ENER)[ci] = e + 0.5 * (vx * vx + vy * vy + vz * vz);
+    gb_var(g, blk, GB_PRES)[ci] = (gamma - 1.0) * rho * e;
+    gb_var(g, blk, GB_TEMP)[ci] = temp;
+    gb_var(g, blk, GB_TDUS)[ci] = v.tdust;
+    if (g.slot[GB_PHHE] >= 0) gb_var(g, blk, GB_PHHE)[ci] = 0.0;
+    if (g.slot[GB_PEFL] >= 0) gb_var(g, blk, GB_PEFL)[ci] = 0.0;
+}
+
+__device__ __forceinline__ void cell_of(int64_t idx, const int* list, int& blk, int& ci, int& i, int& j, int& k)
+{
+    int cb = (int)(idx / 4096), t = (int)(idx % 4096);
+    blk = list[cb];
+    i = GB_NGUARD + t % GB_NXB;
+    j = GB_NGUARD + (t / GB_NXB) % GB_NXB;
+    k = GB_NGUARD + t / (GB_NXB * GB_NXB);
+    ci = gb_cidx(i, j, k);
+}
+
+// features + the rate at the old state
+__global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, double gamma, const int* __restrict__ list, int64_t ncell,
+                           double dt_code, float* __restrict__ feat, double* __restrict__ f0out)
+{
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= ncell) return;
+    int blk, ci, i, j, k;
+    cell_of(idx, list, blk, ci, i, j, k);
+    gb_cool_vars v;
+    double ei, temp;
+    sur_load(g, c, gamma, blk, ci, v, ei, temp);
+    double f0 = dei_dt(c, v, cooling_floor(c, v), ei);
+    double tcool = ei / fmax(fabs(f0), 1e-300);
+    double dt = dt_code * c.p.time_unit;
+    float x[4];
+    gbsur::features(v.ndens, temp, dt / tcool, c.p.Gzero + v.Gflux, x);
+    reinterpret_cast<float4*>(feat)[idx] = make_float4(x[0], x[1], x[2], x[3]);
+    f0out[idx] = f0;
+}
+
+// acceptance test: backward-Euler residual r = e - dt f(e) - e_old at the
+// predicted state, its Newton estimate of the error r / (1 - dt f') with
+// f' from the secant through the old and predicted states; accepted cells
+// take the corrected state, rejected ones go to the fallback list
+__global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const int* __restrict__ list, int64_t ncell,
+                             double dt_code, const float* __restrict__ y, const double* __restrict__ f0a,
+                             double rel_tol, int* __restrict__ rej, int* __restrict__ nrej, gb_status* st)
+{
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= ncell) return;
+    int blk, ci, i, j, k;
+    cell_of(idx, list, blk, ci, i, j, k);
+    const gb_cool_params& p = c.p;
+    gb_cool_vars v;
+    double ei0, temp0;
+    sur_load(g, c, gamma, blk, ci, v, ei0, temp0);
+    const double dt = dt_code * p.time_unit;
+    const double f0 = f0a[idx];
+    double Tp = temp0 * pow(10.0, gbsur::Y_SCALE * (double)y[idx]);
+    bool ok = isfinite(Tp) && Tp > 0.0;
+    double ein = 0.0;
+    if (ok) {
+        if (Tp < p.absTmin) Tp = p.absTmin;
+        double eip = Tp * v.TtoEI;
+        double fl = cooling_floor(c, v);
+        double f1 = dei_dt(c, v, fl, eip);
+        double r = eip - dt * f1 - ei0;
+        double de = eip - ei0;
+        double fp = fabs(de) > 1e-12 * ei0 ? (f1 - f0) / de : 0.0;
+        double J = 1.0 - dt * fp;
+        if (!(J > 0.0)) J = 1.0;
+        double delta = r / J;
+        ein = eip - delta;
+        ok = isfinite(ein) && ein > 0.0 && fabs(delta) <= rel_tol * ein;
+        // the solution moves the way the rate at the old state points
+        if (ok && f0 < 0.0 && ein > ei0 * (1.0 + rel_tol)) ok = false;
+        if (ok && f0 > 0.0 && ein < ei0 * (1.0 - rel_tol)) ok = false;
+    }
+    if (ok) {
+        double temp = ein / v.TtoEI;
+        if (temp < p.absTmin) {
+            temp = p.absTmin;
+            ein = p.absTmin * v.TtoEI;
+        }
+        gb_cool_diag d = {0, 0, 0, 0, 0};
+        if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update(c, v, temp, &d);
+        if (temp > p.absTmax) {
+            ein = p.absTmax * v.TtoEI;
+            temp = p.absTmax;
+        }
+        sur_store(g, c, gamma, blk, ci, v, ein, temp);
+    } else {
+        int slot = atomicAdd(nrej, 1);
+        rej[slot] = (int)idx;
+    }
+    if (st) {
+        gb_count_warp(&st->n_surrogate, ok);
+        gb_count_warp(&st->n_surrogate_reject, !ok);
+    }
+}
+
+// rejected cells: the plain implicit integrator (RadHeat.F90:223-423)
+__global__ void k_sur_fallback(gb_dev_grid g, gb_cool_ctx c, double gamma, const int* __restrict__ list,
+                               double dt_code, const int* __restrict__ rej, const int* __restrict__ nrej,
+                               gb_status* st)
+{
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= *nrej) return;
+    int blk, ci, i, j, k;
+    cell_of(rej[q], list, blk, ci, i, j, k);
+    gb_cool_vars v;
+    double ei, temp;
+    sur_load(g, c, gamma, blk, ci, v, ei, temp);
+    gb_cool_diag d = {0, 0, 0, 0, 0};
+    heating_and_cooling(c, v, &ei, dt_code * c.p.time_unit, &temp, &d);
+    bool clamped = false;
+    if (temp > c.p.absTmax) {
+        ei = c.p.absTmax * v.TtoEI;
+        temp = c.p.absTmax;
+        clamped = true;
+    }
+    sur_store(g, c, gamma, blk, ci, v, ei, temp);
+    if (st) {
+        gb_count_warp(&st->n_bracket_fail, d.bracket_fail != 0);
+        gb_count_warp(&st->n_clamped, clamped);
+        if (d.unbracketed) gb_fail(st, GB_ST_ZERO_UNBRACKETED, blk, i, j, k, ei);
+        if (d.maxiter) gb_fail(st, GB_ST_ZERO_MAXITER, blk, i, j, k, ei);
+    }
+}
+
+int g_cool_mode = 0;
+double g_sur_tol = 2e-3;
+struct sur_bufs {
+    float* feat = nullptr;
+    float* y = nullptr;
+    double* f0 = nullptr;
+    int* rej = nullptr;
+    int* nrej = nullptr;
+    int64_t cap = 0;
+} g_sb;
+
+int sur_ensure(int64_t ncell)
+{
+    if (ncell <= g_sb.cap) return GB_OK;
+    cudaFree(g_sb.feat);
+    cudaFree(g_sb.y);
+    cudaFree(g_sb.f0);
+    cudaFree(g_sb.rej);
+    if (!g_sb.nrej && gb_check(cudaMalloc(&g_sb.nrej, sizeof(int)), "sur nrej")) return GB_ERR_CUDA;
+    if (gb_check(cudaMalloc(&g_sb.feat, sizeof(float) * 4 * ncell), "sur feat") ||
+        gb_check(cudaMalloc(&g_sb.y, sizeof(float) * ncell), "sur y") ||
+        gb_check(cudaMalloc(&g_sb.f0, sizeof(double) * ncell), "sur f0") ||
+        gb_check(cudaMalloc(&g_sb.rej, sizeof(int) * ncell), "sur rej"))
+        return GB_ERR_CUDA;
+    g_sb.cap = ncell;
+    return GB_OK;
+}
+
+}  // namespace
+
+int gb_cooling_mode() { return g_cool_mode; }
+
+int gb_launch_surrogate(int nblk, const int* list, double dt, gb_status* st, cudaStream_t s)
+{
+    const int64_t ncell = (int64_t)nblk * 4096;
+    int rc = sur_ensure(ncell);
+    if (rc) return rc;
+    const unsigned nb = (unsigned)((ncell + 127) / 128);
+    k_sur_feat<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, ncell, dt, g_sb.feat, g_sb.f0);
+    rc = gb_mlp_launch_infer(ncell, g_sb.feat, g_sb.y, s);
+    if (rc) return rc;
+    cudaMemsetAsync(g_sb.nrej, 0, sizeof(int), s);
+    k_sur_accept<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, ncell, dt, g_sb.y, g_sb.f0, g_sur_tol,
+                                    g_sb.rej, g_sb.nrej, st);
+    k_sur_fallback<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, dt, g_sb.rej, g_sb.nrej, st);
+    return gb_check(cudaGetLastError(), "surrogate launch") ? GB_ERR_CUDA : GB_OK;
+}
+
+extern "C" int gb_set_cooling_mode(int mode, double rel_tol)
+{
+    if (mode < 0 || mode > 1 || !(rel_tol > 0.0) || rel_tol > 0.5) return GB_ERR_ARG;
+    g_cool_mode = mode;
+    g_sur_tol = rel_tol;
+    return GB_OK;
+}
+
+extern "C" int gb_surrogate_samples(int64_t n, uint64_t seed, float* feat, float* target, gb_status* st, void* stream)
+{
+    if (!g_gb.cool_ok) {
+        gb_set_error("gb_surrogate_samples: call gb_cool_init first");
+        return GB_ERR_NOT_INIT;
+    }
+    if (n <= 0 || !feat || !target) return GB_ERR_ARG;
+    k_sur_samples<<<(unsigned)((n + 127) / 128), 128, 0, (cudaStream_t)stream>>>(g_gb.cool, n, seed, feat, target, st);
+    return gb_check(cudaGetLastError(), "k_sur_samples") ? GB_ERR_CUDA : GB_OK;
+}

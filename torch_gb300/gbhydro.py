@@ -107,6 +107,15 @@ _SIG = {
     "gb_grid_download_flash": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
     "gb_status_reset": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gb_status_read": (C.c_int, [C.c_void_p, C.POINTER(Status)]),
+    "gb_mlp_init_random": (C.c_int, [C.c_uint64]),
+    "gb_mlp_set_weights": (C.c_int, [C.c_void_p, C.c_int]),
+    "gb_mlp_get_weights": (C.c_int, [C.c_void_p, C.c_int]),
+    "gb_mlp_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gb_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_uint64,
+                               C.c_void_p, C.c_void_p]),
+    "gb_mlp_infer": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "gb_surrogate_samples": (C.c_int, [C.c_int64, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gb_set_cooling_mode": (C.c_int, [C.c_int, C.c_double]),
     "gb_last_error": (C.c_char_p, []),
     "gb_version": (C.c_int, []),
 }
@@ -365,3 +374,58 @@ def grid_from_workload(ic: dict, mhd: bool, cooling: bool, device: str = "cuda")
         g.fy.copy_(torch.as_tensor(ic["fy"], device=device))
         g.fz.copy_(torch.as_tensor(ic["fz"], device=device))
     return g
+
+
+# --------------------------------------------------------------- surrogate
+NPARAM = 64 * 4 + 64 + 64 * 64 + 64 + 64 * 64 + 64 + 64 + 1
+
+
+def surrogate_samples(n: int, seed: int, status=None):
+    """n training samples from the plain integrator (device tensors)."""
+    import torch
+    feat = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    tgt = torch.empty(n, dtype=torch.float32, device="cuda")
+    check(lib().gb_surrogate_samples(n, seed, _ptr(feat), _ptr(tgt), _ptr(status), _stream()),
+          "gb_surrogate_samples")
+    return feat, tgt
+
+
+def mlp_init(seed: int = 0):
+    check(lib().gb_mlp_init_random(seed), "gb_mlp_init_random")
+
+
+def mlp_weights() -> np.ndarray:
+    w = np.zeros(NPARAM, np.float32)
+    check(lib().gb_mlp_get_weights(w.ctypes.data_as(C.c_void_p), NPARAM), "gb_mlp_get_weights")
+    return w
+
+
+def mlp_set_weights(w) -> None:
+    w = np.ascontiguousarray(w, np.float32)
+    check(lib().gb_mlp_set_weights(w.ctypes.data_as(C.c_void_p), NPARAM), "gb_mlp_set_weights")
+
+
+def mlp_grad(feat, tgt):
+    g = np.zeros(NPARAM, np.float32)
+    loss = np.zeros(1, np.float32)
+    check(lib().gb_mlp_grad(_ptr(feat), _ptr(tgt), feat.shape[0], g.ctypes.data_as(C.c_void_p),
+                            loss.ctypes.data_as(C.c_void_p), _stream()), "gb_mlp_grad")
+    return g, float(loss[0])
+
+
+def mlp_train(feat, tgt, steps: int, batch: int = 8192, lr: float = 2e-3, seed: int = 1):
+    losses = np.zeros(steps, np.float32)
+    check(lib().gb_mlp_train(_ptr(feat), _ptr(tgt), feat.shape[0], steps, batch, lr, seed,
+                             losses.ctypes.data_as(C.c_void_p), _stream()), "gb_mlp_train")
+    return losses
+
+
+def mlp_infer(feat, tensor_cores: bool = True):
+    import torch
+    y = torch.empty(feat.shape[0], dtype=torch.float32, device=feat.device)
+    check(lib().gb_mlp_infer(feat.shape[0], _ptr(feat), _ptr(y), int(tensor_cores), _stream()), "gb_mlp_infer")
+    return y
+
+
+def set_cooling_mode(surrogate: bool, rel_tol: float = 2e-3):
+    check(lib().gb_set_cooling_mode(int(surrogate), rel_tol), "gb_set_cooling_mode")
