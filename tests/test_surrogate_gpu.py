@@ -1,0 +1,98 @@
+"""Learned cooling surrogate: GPU gradients against the CPU oracle,
+training, tensor-core inference, and the inline accuracy / gain over the
+plain integrator."""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def trained(gb):
+    """A surrogate trained on plain-integrator samples (1e6 samples here;
+    the bench trains on 1e7)."""
+    import torch
+    gb.init_cooling(gb.cool_params())
+    feat, tgt = gb.surrogate_samples(1_000_000, 1234)
+    ok = torch.isfinite(tgt)
+    feat, tgt = feat[ok].contiguous(), tgt[ok].contiguous()
+    gb.mlp_init(7)
+    losses = gb.mlp_train(feat, tgt, steps=3000, batch=8192, lr=3e-3, seed=3)
+    return feat, tgt, losses
+
+
+def test_gpu_gradient_matches_cpu_oracle(gb):
+    import torch
+    from oracle import mlp_oracle as M
+    gb.mlp_init(11)
+    rng = np.random.default_rng(2)
+    x = rng.normal(0, 1, (512, 4)).astype(np.float32)
+    t = rng.normal(0, 0.3, 512).astype(np.float32)
+    g, loss = gb.mlp_grad(torch.as_tensor(x, device="cuda"), torch.as_tensor(t, device="cuda"))
+    w = gb.mlp_weights()
+    loss_o, g_o = M.loss_and_grad(w, x, t)
+    assert abs(loss - loss_o) <= 1e-4 * abs(loss_o)
+    assert np.linalg.norm(g - g_o) <= 1e-3 * np.linalg.norm(g_o)
+
+
+def test_training_reduces_loss(trained):
+    feat, tgt, losses = trained
+    assert np.isfinite(losses).all()
+    assert losses[-200:].mean() < 0.05 * losses[:20].mean()
+    assert losses[-200:].mean() < 2e-3
+
+
+def test_tensor_core_inference_matches_fp32_path(gb, trained):
+    feat, tgt, _ = trained
+    x = feat[:200_000]
+    y_tc = gb.mlp_infer(x, tensor_cores=True).cpu().numpy()
+    y_fp = gb.mlp_infer(x, tensor_cores=False).cpu().numpy()
+    assert np.abs(y_tc - y_fp).max() < 2e-2
+    from oracle import mlp_oracle as M
+    y_o = M.forward(gb.mlp_weights(), x[:2000].cpu().numpy())
+    assert np.abs(y_tc[:2000] - y_o).max() < 2e-2
+
+
+def _cooling_grid(gb, seed=9):
+    from torch_gb300 import workloads as W
+    ic = W.turbulent_box(4, 4, 4, seed=seed, sigma_ln=1.0, mach=5.0, mhd=False)
+    g = gb.grid_from_workload(ic, mhd=False, cooling=True)
+    units = gb.code_units()
+    g.u[:, g.slots["TEMP"]] = g.u[:, 6] * units["vel_unit"] ** 2 * (2.0 / 3.0) * (24.0 / 11.0) * gb.MP / gb.KB
+    g.u[:, g.slots["TDUS"]] = 15.0
+    return g, units
+
+
+def test_inline_surrogate_accuracy_and_gain(gb, trained):
+    """One hydro + cooling step with the surrogate (acceptance test +
+    plain fallback) against the plain integrator: cooled temperatures
+    within 1 % of the plain integrator, and the surrogate path is faster."""
+    import torch
+    units = gb.code_units()
+    gb.init_cooling(gb.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
+                                   time_unit=units["time_unit"]))
+    gb.init_hydro(gb.hydro_params(False))
+    out, times, stats = {}, {}, {}
+    for mode in (0, 1):
+        g, _ = _cooling_grid(gb)
+        gb.set_cooling_mode(bool(mode))
+        dt = g.compute_dt().item() * 20.0  # a long step: stiff cooling in many cells
+        g.evolve_step(dt, cool=True)  # warm-up on a copy of the state
+        g2, _ = _cooling_grid(gb)
+        g2.status_reset()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g2.evolve_step(dt, cool=True)
+        torch.cuda.synchronize()
+        times[mode] = time.perf_counter() - t0
+        stats[mode] = g2.status_read()
+        out[mode] = g2.u[:, g2.slots["TEMP"], 4:20, 4:20, 4:20].cpu().numpy()
+    gb.set_cooling_mode(False)
+    rel = np.abs(out[1] - out[0]) / out[0]
+    assert np.quantile(rel, 0.99) < 0.01, np.quantile(rel, [0.5, 0.9, 0.99, 1.0])
+    assert stats[1]["n_surrogate"] > 0
+    frac = stats[1]["n_surrogate_reject"] / (stats[1]["n_surrogate"] + stats[1]["n_surrogate_reject"])
+    print("fallback fraction", frac, "time plain", times[0], "surrogate", times[1])
+    assert times[1] < times[0]

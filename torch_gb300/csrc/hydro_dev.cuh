@@ -613,7 +613,7 @@ __device__ __forceinline__ int rc_index(int i, int j, int k)
 template <typename T, bool MHD>
 __global__ void __launch_bounds__(128)
 k_flux(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* __restrict__ rscr,
-       T* __restrict__ fscr, size_t scr_stride)
+       size_t rstride, T* __restrict__ fscr, size_t fstride)
 {
     const int d = blockIdx.y;
     const int cb = blockIdx.z;
@@ -624,7 +624,7 @@ k_flux(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* _
     flux_coords(d, f, I);
     int Il[3] = {I[0], I[1], I[2]};
     Il[d] -= 1;
-    const T* rs = rscr + (size_t)cb * scr_stride;
+    const T* rs = rscr + (size_t)cb * rstride;
     const int cl = rc_index(Il[0], Il[1], Il[2]), cr = rc_index(I[0], I[1], I[2]);
     T wl[NP], wr[NP];
 #pragma unroll
@@ -689,7 +689,7 @@ k_flux(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* _
             feint = feint + vis * (el - er);
         }
     }
-    T* fs = fscr + (size_t)cb * scr_stride + (size_t)d * NFLX * NFC;
+    T* fs = fscr + (size_t)cb * fstride + (size_t)d * NFLX * NFC;
 #pragma unroll
     for (int s = 0; s < NP; ++s) fs[(size_t)s * NFC + f] = out[s];
     fs[(size_t)8 * NFC + f] = feint;

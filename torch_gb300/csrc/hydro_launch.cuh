@@ -24,14 +24,14 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
     dim3 fg((NFC + 127) / 128, 3, nblk);
     if (mhd) {
         k_recon<T, true><<<rg, 3 * RECON_TILE, 0, s>>>(g, kp, list, rscr, SL::recon, st);
-        k_flux<T, true><<<fg, 128, 0, s>>>(g, kp, list, rscr, fscr, SL::flux);
+        k_flux<T, true><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux);
         dim3 eg((NEDGE + 127) / 128, 3, nblk);
         k_emf<T><<<eg, 128, 0, s>>>(g, list, fscr, SL::flux, escr, SL::emf);
         dim3 bg((NFB + 127) / 128, 3, nblk);
         k_faceb<<<bg, 128, 0, s>>>(g, kp, list, escr, SL::emf, bscr, SL::fb);
     } else {
         k_recon<T, false><<<rg, 3 * RECON_TILE, 0, s>>>(g, kp, list, rscr, SL::recon, st);
-        k_flux<T, false><<<fg, 128, 0, s>>>(g, kp, list, rscr, fscr, SL::flux);
+        k_flux<T, false><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux);
     }
     dim3 ug((GB_NXB * GB_NXB * GB_NXB + 127) / 128, nblk);
     if (mhd) {
