@@ -241,6 +241,16 @@ int gb_surrogate_samples(int64_t n, uint64_t seed, float* feat_dev, float* targe
  * estimate of the backward-Euler residual. */
 int gb_set_cooling_mode(int mode, double rel_tol);
 
+/* ---------------------------------------------------------------- profiling */
+/* Per-kernel CUDA-event timing on the launching stream (no counterpart in
+ * the reference; FLASH's Timers_start/stop play this role). While enabled
+ * every launch records an event pair; gb_prof_read synchronises and
+ * returns per-kernel-group milliseconds and launch counts in the order
+ * guard, recon, flux, emf, faceb, update, dt, heat, surrogate features,
+ * mlp, surrogate accept, surrogate fallback, layout copies (n >= 13). */
+int gb_prof_enable(int on);
+int gb_prof_read(double* ms, long long* launches, int n);
+
 /* ---------------------------------------------------------------- misc */
 int gb_status_reset(gb_status* st_dev, void* stream);
 int gb_status_read(const gb_status* st_dev, gb_status* st_host);

@@ -4,10 +4,78 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <vector>
+
+#include "gb_prof.h"
 #include "gb_state.h"
 #include "hydro_dev.cuh"
 
 gb_state_t g_gb;
+
+// ---------------------------------------------------------------- profiler
+namespace {
+struct prof_state {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    std::vector<int> ids;  // kernel id per recorded pair
+    cudaEvent_t open[GBP_N];
+} g_prof;
+
+cudaEvent_t prof_event()
+{
+    if (g_prof.used == g_prof.pool.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        g_prof.pool.push_back(e);
+    }
+    return g_prof.pool[g_prof.used++];
+}
+}  // namespace
+
+void gb_prof_begin(int id, cudaStream_t s)
+{
+    if (!g_prof.on) return;
+    cudaEvent_t e = prof_event();
+    cudaEventRecord(e, s);
+    g_prof.open[id] = e;
+}
+
+void gb_prof_end(int id, cudaStream_t s)
+{
+    if (!g_prof.on) return;
+    cudaEvent_t e = prof_event();
+    cudaEventRecord(e, s);
+    g_prof.ids.push_back(id);
+    // the begin event of this pair is the one recorded just before the
+    // kernel; keep pairs adjacent in the pool
+    (void)g_prof.open[id];
+}
+
+extern "C" int gb_prof_enable(int on)
+{
+    g_prof.on = on != 0;
+    g_prof.used = 0;
+    g_prof.ids.clear();
+    return GB_OK;
+}
+
+extern "C" int gb_prof_read(double* ms, long long* launches, int n)
+{
+    if (!ms || !launches || n < GBP_N) return GB_ERR_ARG;
+    for (int i = 0; i < GBP_N; ++i) {
+        ms[i] = 0.0;
+        launches[i] = 0;
+    }
+    if (gb_check(cudaDeviceSynchronize(), "profiler sync")) return GB_ERR_CUDA;
+    for (size_t q = 0; q < g_prof.ids.size(); ++q) {
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, g_prof.pool[2 * q], g_prof.pool[2 * q + 1]);
+        ms[g_prof.ids[q]] += t;
+        launches[g_prof.ids[q]] += 1;
+    }
+    return GB_OK;
+}
 
 static char g_err[512] = "";
 
@@ -301,10 +369,14 @@ __global__ void k_soa_to_flash(double* __restrict__ out, int nunk, const int* __
 int gb_launch_guardfill(int nblk, const int* list, cudaStream_t s)
 {
     dim3 gc((GB_N3 + 127) / 128, nblk);
+    gb_prof_begin(GBP_GUARD, s);
     k_guard_cells<<<gc, 128, 0, s>>>(g_gb.grid, g_gb.tree, list);
+    gb_prof_end(GBP_GUARD, s);
     if (g_gb.hp.mhd && g_gb.grid.f[0]) {
         dim3 gf((GB_FSZ + 127) / 128, nblk, 3);
+        gb_prof_begin(GBP_GUARD, s);
         k_guard_faces<<<gf, 128, 0, s>>>(g_gb.grid, g_gb.tree, list);
+        gb_prof_end(GBP_GUARD, s);
     }
     return gb_check(cudaGetLastError(), "guard fill") ? GB_ERR_CUDA : GB_OK;
 }
@@ -420,9 +492,11 @@ int gb_launch_dt(int nblk, const int* list, double* dt_out, cudaStream_t s)
                  "dt init"))
         return GB_ERR_CUDA;
     gbh::hydro_kparams kp = make_kp(1.0);
+    gb_prof_begin(GBP_DT, s);
     int rc = gb_dt_launch(kp, g_gb.hp.mhd, nblk, list, (unsigned long long*)g_gb.d_dtmin, s);
     if (rc) return rc;
     k_dt_finish<<<1, 1, 0, s>>>((const unsigned long long*)g_gb.d_dtmin, g_gb.hp.cfl, dt_out);
+    gb_prof_end(GBP_DT, s);
     return gb_check(cudaGetLastError(), "k_dt_finish") ? GB_ERR_CUDA : GB_OK;
 }
 
@@ -480,10 +554,14 @@ static int flash_copy(bool up, double* host, int nunk, const int* host_slot, int
     unsigned nb = (unsigned)((total + 255) / 256);
     if (up) {
         if (gb_check(cudaMemcpyAsync(g_gb.d_stage, host, bytes, cudaMemcpyHostToDevice, s), "upload")) return GB_ERR_CUDA;
+        gb_prof_begin(GBP_COPY, s);
         k_flash_to_soa<<<nb, 256, 0, s>>>(g_gb.d_stage, nunk, dslot, g_gb.grid, nblocks);
+        gb_prof_end(GBP_COPY, s);
         if (gb_check(cudaGetLastError(), "k_flash_to_soa")) return GB_ERR_CUDA;
     } else {
+        gb_prof_begin(GBP_COPY, s);
         k_soa_to_flash<<<nb, 256, 0, s>>>(g_gb.d_stage, nunk, dslot, g_gb.grid, nblocks);
+        gb_prof_end(GBP_COPY, s);
         if (gb_check(cudaGetLastError(), "k_soa_to_flash")) return GB_ERR_CUDA;
         if (gb_check(cudaMemcpyAsync(host, g_gb.d_stage, bytes, cudaMemcpyDeviceToHost, s), "download"))
             return GB_ERR_CUDA;

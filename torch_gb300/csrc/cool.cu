@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "cool_dev.cuh"
+#include "gb_prof.h"
 #include "gb_state.h"
 
 using namespace gbcool;
@@ -220,7 +221,9 @@ extern "C" int gb_cool_init(const char* path, const gb_cool_params* p)
 int gb_launch_cool_blocks(int nblk, const int* list, double dt, gb_status* st, cudaStream_t s)
 {
     dim3 grid((GB_NXB * GB_NXB * GB_NXB + 127) / 128, nblk);
+    gb_prof_begin(GBP_HEAT, s);
     k_heat_blocks<<<grid, 128, 0, s>>>(g_gb.grid, g_gb.cool, list, dt, g_gb.hp.gamma, st);
+    gb_prof_end(GBP_HEAT, s);
     return gb_check(cudaGetLastError(), "k_heat_blocks") ? GB_ERR_CUDA : GB_OK;
 }
 
@@ -301,14 +304,15 @@ __global__ void k_sur_samples(gb_cool_ctx c, int64_t n, uint64_t seed, float* __
     v.ndens = v.rho / (v.mu_mol * p.mp);
     v.TtoEI = ei / temp;
     v.conf = v.ndens * v.ndens / v.rho;
-    double f0 = dei_dt(cc, v, cooling_floor(cc, v), ei);
+    double gam, lam;
+    double f0 = dei_parts(cc, v, cooling_floor(cc, v), ei, &gam, &lam);
     double tcool = ei / fmax(fabs(f0), 1e-300);
     double dt = pow(10.0, lr) * tcool;
     gb_cool_diag d = {0, 0, 0, 0, 0};
     heating_and_cooling(cc, v, &ei, dt, &temp, &d);
     if (temp > p.absTmax) temp = p.absTmax;
     float x[4];
-    gbsur::features(nden, T0, dt / tcool, G, x);
+    gbsur::features(nden, T0, dt / tcool, gam, lam, x);
     reinterpret_cast<float4*>(feat)[i] = make_float4(x[0], x[1], x[2], x[3]);
     bool bad = d.unbracketed || d.maxiter || !isfinite(temp) || !(temp > 0.0);
     target[i] = bad ? __int_as_float(0x7fc00000) : (float)((log10(temp) - lT) / gbsur::Y_SCALE);
@@ -376,19 +380,24 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, double gamma, const int
     gb_cool_vars v;
     double ei, temp;
     sur_load(g, c, gamma, blk, ci, v, ei, temp);
-    double f0 = dei_dt(c, v, cooling_floor(c, v), ei);
+    double gam, lam;
+    double f0 = dei_parts(c, v, cooling_floor(c, v), ei, &gam, &lam);
     double tcool = ei / fmax(fabs(f0), 1e-300);
     double dt = dt_code * c.p.time_unit;
     float x[4];
-    gbsur::features(v.ndens, temp, dt / tcool, c.p.Gzero + v.Gflux, x);
+    gbsur::features(v.ndens, temp, dt / tcool, gam, lam, x);
     reinterpret_cast<float4*>(feat)[idx] = make_float4(x[0], x[1], x[2], x[3]);
     f0out[idx] = f0;
 }
 
-// acceptance test: backward-Euler residual r = e - dt f(e) - e_old at the
-// predicted state, its Newton estimate of the error r / (1 - dt f') with
-// f' from the secant through the old and predicted states; accepted cells
-// take the corrected state, rejected ones go to the fallback list
+// acceptance test: starting from the network's prediction, at most three
+// secant-Newton iterations on the backward-Euler residual
+//   g(e) = e - dt f(e) - e_old   (heatCool.F90:1928-1950),
+// the slope taken through the last two rate evaluations (the first pair is
+// the old state, whose rate the feature kernel kept). A cell is accepted
+// when the last Newton correction is below rel_tol of e and the energy
+// moved the way the rate at the old state points; otherwise it goes to the
+// fallback list and the plain integrator solves it.
 __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const int* __restrict__ list, int64_t ncell,
                              double dt_code, const float* __restrict__ y, const double* __restrict__ f0a,
                              double rel_tol, int* __restrict__ rej, int* __restrict__ nrej, gb_status* st)
@@ -403,22 +412,35 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const i
     sur_load(g, c, gamma, blk, ci, v, ei0, temp0);
     const double dt = dt_code * p.time_unit;
     const double f0 = f0a[idx];
+    const double emin_ = 0.5 * p.absTmin * v.TtoEI;
     double Tp = temp0 * pow(10.0, gbsur::Y_SCALE * (double)y[idx]);
     bool ok = isfinite(Tp) && Tp > 0.0;
     double ein = 0.0;
     if (ok) {
-        if (Tp < p.absTmin) Tp = p.absTmin;
-        double eip = Tp * v.TtoEI;
-        double fl = cooling_floor(c, v);
-        double f1 = dei_dt(c, v, fl, eip);
-        double r = eip - dt * f1 - ei0;
-        double de = eip - ei0;
-        double fp = fabs(de) > 1e-12 * ei0 ? (f1 - f0) / de : 0.0;
-        double J = 1.0 - dt * fp;
-        if (!(J > 0.0)) J = 1.0;
-        double delta = r / J;
-        ein = eip - delta;
-        ok = isfinite(ein) && ein > 0.0 && fabs(delta) <= rel_tol * ein;
+        const double fl = cooling_floor(c, v);
+        double ea = ei0, fa = f0;
+        double eb = fmax(Tp * v.TtoEI, emin_);
+        ok = false;
+        for (int it = 0; it < 3; ++it) {
+            double fb = dei_dt(c, v, fl, eb);
+            double gb = eb - dt * fb - ei0;
+            double de = eb - ea;
+            double slope = fabs(de) > 1e-14 * eb ? (fb - fa) / de : 0.0;
+            double J = 1.0 - dt * slope;
+            if (!(J > 0.0)) break;
+            double delta = gb / J;
+            double en = eb - delta;
+            if (!isfinite(en)) break;
+            if (en < emin_) en = emin_;
+            if (fabs(en - eb) <= rel_tol * en) {
+                ein = en;
+                ok = true;
+                break;
+            }
+            ea = eb;
+            fa = fb;
+            eb = en;
+        }
         // the solution moves the way the rate at the old state points
         if (ok && f0 < 0.0 && ein > ei0 * (1.0 + rel_tol)) ok = false;
         if (ok && f0 > 0.0 && ein < ei0 * (1.0 - rel_tol)) ok = false;
@@ -513,13 +535,21 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, gb_status* st, cud
     int rc = sur_ensure(ncell);
     if (rc) return rc;
     const unsigned nb = (unsigned)((ncell + 127) / 128);
+    gb_prof_begin(GBP_SUR_FEAT, s);
     k_sur_feat<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, ncell, dt, g_sb.feat, g_sb.f0);
+    gb_prof_end(GBP_SUR_FEAT, s);
+    gb_prof_begin(GBP_MLP, s);
     rc = gb_mlp_launch_infer(ncell, g_sb.feat, g_sb.y, s);
+    gb_prof_end(GBP_MLP, s);
     if (rc) return rc;
     cudaMemsetAsync(g_sb.nrej, 0, sizeof(int), s);
+    gb_prof_begin(GBP_SUR_ACCEPT, s);
     k_sur_accept<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, ncell, dt, g_sb.y, g_sb.f0, g_sur_tol,
                                     g_sb.rej, g_sb.nrej, st);
+    gb_prof_end(GBP_SUR_ACCEPT, s);
+    gb_prof_begin(GBP_SUR_FALLBACK, s);
     k_sur_fallback<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, dt, g_sb.rej, g_sb.nrej, st);
+    gb_prof_end(GBP_SUR_FALLBACK, s);
     return gb_check(cudaGetLastError(), "surrogate launch") ? GB_ERR_CUDA : GB_OK;
 }
 

@@ -281,6 +281,32 @@ static __device__ double dei_dt(const gb_cool_ctx& c, const gb_cool_vars& v, dou
     return eplus + PeHeat - emin - cool_pw - cool_dg + floor_;
 }
 
+// dei_dt split into its heating part (Gamma) and cooling part (Lambda):
+// Gamma = CR + stellar + photoelectric heating + the floor term + any gas
+// heating by warmer dust, Lambda = atomic + molecular + dust cooling. The
+// return value is dei_dt itself, summed in dei_dt's order.
+static __device__ double dei_parts(const gb_cool_ctx& c, const gb_cool_vars& v, double floor_, double ei_in,
+                                   double* gam, double* lam)
+{
+    const gb_cool_params& p = c.p;
+    double tmp_temp = ei_in / v.TtoEI;
+    if (tmp_temp < 0.0) tmp_temp = 1.0;
+    double eplus = heating(p, tmp_temp, v.ndens, v.rho, v.strat_factor);
+    double fuv = v.Gflux + p.Gzero * f_ext(p, v.rho, v.ndens, tmp_temp) * v.strat_factor;
+    double PeHeat, dust_heating;
+    pe_heating(p, fuv, v.xHp, v.ndens, tmp_temp, v.rho, &PeHeat, &dust_heating);
+    eplus = eplus + v.ephen;
+    double emin = cooling(p, tmp_temp, v.ndens, v.conf, v.xHp);
+    double cool_pw = 0.0, cool_dg = 0.0;
+    if (p.useDustCool) {
+        cool_pw = molecular_cooling(c, v.ndens, tmp_temp, v.mu_mol);
+        cool_dg = dust_cooling(p, v.ndens, tmp_temp, v.tdust, v.rho);
+    }
+    *gam = eplus + PeHeat + floor_ + fmx(-cool_dg, 0.0);
+    *lam = emin + cool_pw + fmx(cool_dg, 0.0);
+    return eplus + PeHeat - emin - cool_pw - cool_dg + floor_;
+}
+
 static __device__ double get_dust_temperature(const gb_cool_params& p, double tdust_in, double temp_in,
                                        double nden, double phen_heat, gb_cool_diag* d)
 {

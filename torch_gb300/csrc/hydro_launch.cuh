@@ -3,6 +3,7 @@
 // compiled with -fmad=false) and hydro_mixed.cu (T = float).
 #pragma once
 
+#include "gb_prof.h"
 #include "gb_state.h"
 #include "hydro_dev.cuh"
 
@@ -23,17 +24,30 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
     dim3 rg((NRC + RECON_TILE - 1) / RECON_TILE, nblk);
     dim3 fg((NFC + 127) / 128, 3, nblk);
     if (mhd) {
+        gb_prof_begin(GBP_RECON, s);
         k_recon<T, true><<<rg, 3 * RECON_TILE, 0, s>>>(g, kp, list, rscr, SL::recon, st);
+        gb_prof_end(GBP_RECON, s);
+        gb_prof_begin(GBP_FLUX, s);
         k_flux<T, true><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux);
+        gb_prof_end(GBP_FLUX, s);
         dim3 eg((NEDGE + 127) / 128, 3, nblk);
+        gb_prof_begin(GBP_EMF, s);
         k_emf<T><<<eg, 128, 0, s>>>(g, list, fscr, SL::flux, escr, SL::emf);
+        gb_prof_end(GBP_EMF, s);
         dim3 bg((NFB + 127) / 128, 3, nblk);
+        gb_prof_begin(GBP_FACEB, s);
         k_faceb<<<bg, 128, 0, s>>>(g, kp, list, escr, SL::emf, bscr, SL::fb);
+        gb_prof_end(GBP_FACEB, s);
     } else {
+        gb_prof_begin(GBP_RECON, s);
         k_recon<T, false><<<rg, 3 * RECON_TILE, 0, s>>>(g, kp, list, rscr, SL::recon, st);
+        gb_prof_end(GBP_RECON, s);
+        gb_prof_begin(GBP_FLUX, s);
         k_flux<T, false><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux);
+        gb_prof_end(GBP_FLUX, s);
     }
     dim3 ug((GB_NXB * GB_NXB * GB_NXB + 127) / 128, nblk);
+    gb_prof_begin(GBP_UPDATE, s);
     if (mhd) {
         if (cool) k_update<T, true, true><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st);
         else k_update<T, true, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st);
@@ -41,6 +55,7 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
         if (cool) k_update<T, false, true><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st);
         else k_update<T, false, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st);
     }
+    gb_prof_end(GBP_UPDATE, s);
     return gb_check(cudaGetLastError(), "hydro chunk launch") ? GB_ERR_CUDA : GB_OK;
 }
 

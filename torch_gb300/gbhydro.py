@@ -116,6 +116,8 @@ _SIG = {
     "gb_mlp_infer": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "gb_surrogate_samples": (C.c_int, [C.c_int64, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gb_set_cooling_mode": (C.c_int, [C.c_int, C.c_double]),
+    "gb_prof_enable": (C.c_int, [C.c_int]),
+    "gb_prof_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "gb_last_error": (C.c_char_p, []),
     "gb_version": (C.c_int, []),
 }
@@ -429,3 +431,19 @@ def mlp_infer(feat, tensor_cores: bool = True):
 
 def set_cooling_mode(surrogate: bool, rel_tol: float = 2e-3):
     check(lib().gb_set_cooling_mode(int(surrogate), rel_tol), "gb_set_cooling_mode")
+
+
+PROF_NAMES = ["guard_fill", "recon", "flux", "emf", "faceb", "update", "dt", "heat", "sur_feat", "mlp_infer",
+              "sur_accept", "sur_fallback", "layout_copy"]
+
+
+def prof_enable(on: bool = True):
+    check(lib().gb_prof_enable(int(on)), "gb_prof_enable")
+
+
+def prof_read() -> dict:
+    n = len(PROF_NAMES)
+    ms = np.zeros(n)
+    cnt = np.zeros(n, np.int64)
+    check(lib().gb_prof_read(ms.ctypes.data_as(C.c_void_p), cnt.ctypes.data_as(C.c_void_p), n), "gb_prof_read")
+    return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(PROF_NAMES) if cnt[i]}
