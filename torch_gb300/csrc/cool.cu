@@ -390,13 +390,14 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, double gamma, const int
     f0out[idx] = f0;
 }
 
-// acceptance test: starting from the network's prediction, at most three
+// acceptance test: starting from the network's prediction, at most four
 // secant-Newton iterations on the backward-Euler residual
 //   g(e) = e - dt f(e) - e_old   (heatCool.F90:1928-1950),
 // the slope taken through the last two rate evaluations (the first pair is
 // the old state, whose rate the feature kernel kept). A cell is accepted
-// when the last Newton correction is below rel_tol of e and the energy
-// moved the way the rate at the old state points; otherwise it goes to the
+// once a Newton correction below rel_tol of e was computed from a local
+// slope (its two points within 5 % of each other) and the energy moved
+// the way the rate at the old state points; otherwise it goes to the
 // fallback list and the plain integrator solves it.
 __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const int* __restrict__ list, int64_t ncell,
                              double dt_code, const float* __restrict__ y, const double* __restrict__ f0a,
@@ -421,7 +422,7 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const i
         double ea = ei0, fa = f0;
         double eb = fmax(Tp * v.TtoEI, emin_);
         ok = false;
-        for (int it = 0; it < 3; ++it) {
+        for (int it = 0; it < 4; ++it) {
             double fb = dei_dt(c, v, fl, eb);
             double gb = eb - dt * fb - ei0;
             double de = eb - ea;
@@ -432,7 +433,7 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const i
             double en = eb - delta;
             if (!isfinite(en)) break;
             if (en < emin_) en = emin_;
-            if (fabs(en - eb) <= rel_tol * en) {
+            if (fabs(en - eb) <= rel_tol * en && fabs(de) <= 0.05 * eb) {
                 ein = en;
                 ok = true;
                 break;
