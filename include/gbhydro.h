@@ -137,6 +137,22 @@ int gb_hydro_init(const gb_hydro_params* p);
 int gb_hydro_unsplit(int blockCount, const int* blockList_dev, double dt, double dtOld,
                      gb_status* st_dev, void* stream);
 
+/* Allocation-free FP64 unsplit step (no counterpart in the reference).
+ * For callers that cannot let the library allocate device memory: a host
+ * that owns all device memory through its own pool, or a step loop that
+ * must not call cudaMalloc because it can synchronise the whole device.
+ * Runs the same plain FP64 kernels as gb_hydro_unsplit (no fused cooling,
+ * whatever gb_hydro_params.precision says) with their scratch in a static
+ * device array sized for GB_NOALLOC_MAX_BLOCKS blocks (about 3.6 MB per
+ * block, ~14.4 MB held on every GPU that loads the library until exit).
+ * blockCount above GB_NOALLOC_MAX_BLOCKS returns GB_ERR_LIMIT. The first
+ * call on each device looks up the array's device address (make it before
+ * any stream capture). Calls share the array: calls that overlap on the GPU
+ * race. The profiler must be off. */
+#define GB_NOALLOC_MAX_BLOCKS 4
+int gb_hydro_unsplit_noalloc(int blockCount, const int* blockList_dev, double dt, double dtOld,
+                             gb_status* st_dev, void* stream);
+
 /* Blocks per launch chunk of the hydro kernels (scratch = chunk x per-block
  * scratch; the autotuner picks it). Default 16. */
 int gb_set_chunk_blocks(int n);

@@ -26,6 +26,7 @@ UNITS = {
     "hydro_fp64.cu": ["-fmad=false"],
     "hydro_mixed.cu": [],
     "mlp.cu": [],
+    "noalloc.cu": ["-fmad=false"],
 }
 
 

@@ -52,6 +52,8 @@ void gb_prof_end(int id, cudaStream_t s)
     (void)g_prof.open[id];
 }
 
+int gb_prof_is_on() { return g_prof.on ? 1 : 0; }
+
 extern "C" int gb_prof_enable(int on)
 {
     g_prof.on = on != 0;

@@ -97,6 +97,8 @@ _SIG = {
     "gb_hydro_init": (C.c_int, [C.POINTER(HydroParams)]),
     "gb_hydro_unsplit": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_void_p]),
     "gb_set_chunk_blocks": (C.c_int, [C.c_int]),
+    "gb_hydro_unsplit_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p,
+                                           C.c_void_p]),
     "gb_compute_dt": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gb_cool_init": (C.c_int, [C.c_char_p, C.POINTER(CoolParams)]),
     "gb_heat": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_void_p]),
