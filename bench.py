@@ -281,6 +281,7 @@ def main():
           for v, i in (("dens", 0), ("pres", 4))}
     sT = g_plain.slots["TEMP"]
     relT = np.abs(a[:, sT][sl] - b[:, sT][sl]) / a[:, sT][sl]
+    tolT = np.abs(a[:, sT][sl] - b[:, sT][sl]) <= 0.01 * a[:, sT][sl] + 2.0
     e2e_ms, e2e_bytes = e2e_run(G, g_fast, max(2, args.steps // 2), 1)
     hbm, hbm_kind = peaks()
     # dominant kernel: largest share of the timed region. Algorithmic bytes
@@ -308,7 +309,10 @@ def main():
         "kernel_ms_per_step_fast": {k: v[0] / args.steps for k, v in prof.items()},
         "kernel_launches_per_step_fast": {k: v[1] / args.steps for k, v in prof.items()},
         "temp_rel_err_vs_plain": {"p50": float(np.median(relT)), "p99": float(np.quantile(relT, 0.99)),
-                                  "max": float(relT.max()), "frac_within_1pct": float((relT <= 0.01).mean())},
+                                  "max": float(relT.max()), "frac_within_1pct": float((relT <= 0.01).mean()),
+                                  "frac_within_1pct_plus_brent_tol": float(tolT.mean()),
+                                  "note": "after the same steps of two different paths (mixed hydro + surrogate vs "
+                                          "FP64 hydro + plain integrator); Brent's own tolerance is ~2 K"},
         "surrogate": {"samples": 10_000_000, "sample_s": t_samples, "train_s": t_train,
                       "train_loss_final": float(np.mean(losses[-200:])),
                       "accepted": st_fast["n_surrogate"], "fallback": st_fast["n_surrogate_reject"],

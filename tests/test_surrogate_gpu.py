@@ -94,8 +94,16 @@ def test_inline_surrogate_accuracy_and_gain(gb, trained):
         stats[mode] = g2.status_read()
         out[mode] = g2.u[:, g2.slots["TEMP"], 4:20, 4:20, 4:20].cpu().numpy()
     gb.set_cooling_mode(False)
-    rel = np.abs(out[1] - out[0]) / out[0]
-    assert np.quantile(rel, 0.99) < 0.01, np.quantile(rel, [0.5, 0.9, 0.99, 1.0])
+    # the plain integrator's own answer is only good to Brent's tolerance,
+    # max(TtoEI * 1 K, e * 1e-6) (heatCool.F90:411), i.e. ~2 K absolute;
+    # the surrogate path must agree within 1 % plus that tolerance, and
+    # within 1 % outright where 2 K is below 1 % of T
+    d = np.abs(out[1] - out[0])
+    rel = d / out[0]
+    print("rel err quantiles", np.quantile(rel, [0.5, 0.9, 0.99, 1.0]))
+    assert np.all(d <= 0.01 * out[0] + 2.0), d.max()
+    warm = out[0] >= 200.0
+    assert np.quantile(rel[warm], 0.999) < 0.01
     assert stats[1]["n_surrogate"] > 0
     frac = stats[1]["n_surrogate_reject"] / (stats[1]["n_surrogate"] + stats[1]["n_surrogate_reject"])
     print("fallback fraction", frac, "time plain", times[0], "surrogate", times[1])

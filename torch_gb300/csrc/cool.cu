@@ -196,18 +196,28 @@ extern "C" int gb_cool_init(const char* path, const gb_cool_params* p)
     int rc = read_table(path, lt, ln, ll);
     if (rc != GB_OK) return rc;
     // 10.e0**x on the host, as get_cooling_data computes it
-    std::vector<double> h(GB_TEMP_PTS + GB_DENS_PTS + (size_t)GB_TEMP_PTS * GB_DENS_PTS);
+    const size_t ntab = GB_TEMP_PTS + GB_DENS_PTS + (size_t)GB_TEMP_PTS * GB_DENS_PTS;
+    std::vector<double> h(ntab);
     for (int j = 0; j < GB_TEMP_PTS; ++j) h[j] = pow(10.e0, (double)lt[j] / 10000.0);
     for (int i = 0; i < GB_DENS_PTS; ++i) h[GB_TEMP_PTS + i] = pow(10.e0, (double)ln[i] / 10000.0);
     for (size_t q = 0; q < ll.size(); ++q)
         h[GB_TEMP_PTS + GB_DENS_PTS + q] = pow(10.e0, (double)ll[q] / 10000.0);
+    // FP32 copies: axes, and the molecular power per gram cool_dat / (mu_mol m_p)
+    std::vector<float> hf(ntab);
+    for (size_t q = 0; q < GB_TEMP_PTS + GB_DENS_PTS; ++q) hf[q] = (float)h[q];
+    for (size_t q = GB_TEMP_PTS + GB_DENS_PTS; q < ntab; ++q) hf[q] = (float)(h[q] / (p->mu_mol * p->mp));
     if (!g_gb.d_table) {
-        if (gb_check(cudaMalloc(&g_gb.d_table, h.size() * sizeof(double)), "cudaMalloc(table)"))
+        if (gb_check(cudaMalloc(&g_gb.d_table, ntab * (sizeof(double) + sizeof(float))), "cudaMalloc(table)"))
             return GB_ERR_CUDA;
     }
-    if (gb_check(cudaMemcpy(g_gb.d_table, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice),
-                 "cudaMemcpy(table)"))
+    float* d_tabf = (float*)(g_gb.d_table + ntab);
+    if (gb_check(cudaMemcpy(g_gb.d_table, h.data(), ntab * sizeof(double), cudaMemcpyHostToDevice),
+                 "cudaMemcpy(table)") ||
+        gb_check(cudaMemcpy(d_tabf, hf.data(), ntab * sizeof(float), cudaMemcpyHostToDevice), "cudaMemcpy(table f32)"))
         return GB_ERR_CUDA;
+    g_gb.cool.Tf = d_tabf;
+    g_gb.cool.nf = d_tabf + GB_TEMP_PTS;
+    g_gb.cool.lamf = d_tabf + GB_TEMP_PTS + GB_DENS_PTS;
     g_gb.cool.p = *p;
     g_gb.cool.T = g_gb.d_table;
     g_gb.cool.n = g_gb.d_table + GB_TEMP_PTS;
@@ -262,6 +272,7 @@ extern "C" int gb_cool_cells(int64_t n, const double* dens, double* ei, double* 
 }
 
 // ---------------------------------------------------------------- surrogate
+#include "cool_f32.cuh"
 #include "mlp.h"
 #include "sur_common.cuh"
 
@@ -371,7 +382,8 @@ __device__ __forceinline__ void cell_of(int64_t idx, const int* list, int& blk, 
 
 // features + the rate at the old state
 __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, double gamma, const int* __restrict__ list, int64_t ncell,
-                           double dt_code, float* __restrict__ feat, double* __restrict__ f0out)
+                           double dt_code, float* __restrict__ feat, double* __restrict__ f0out,
+                           double* __restrict__ flout)
 {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= ncell) return;
@@ -380,14 +392,19 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, double gamma, const int
     gb_cool_vars v;
     double ei, temp;
     sur_load(g, c, gamma, blk, ci, v, ei, temp);
-    double gam, lam;
-    double f0 = dei_parts(c, v, cooling_floor(c, v), ei, &gam, &lam);
-    double tcool = ei / fmax(fabs(f0), 1e-300);
+    const double fl = cooling_floor(c, v);
+    gb_cool_varsf vf;
+    gbcoolf::make_vars(c.p, v, vf);
+    const gb_cool_tabf tf = {c.Tf, c.nf, c.lamf, (float)c.T_min, (float)c.nd_min};
+    float gam, lam;
+    float f0 = gbcoolf::dei_parts(c.p, tf, vf, (float)fl, (float)ei, &gam, &lam);
+    double tcool = ei / fmax(fabs((double)f0), 1e-300);
     double dt = dt_code * c.p.time_unit;
     float x[4];
     gbsur::features(v.ndens, temp, dt / tcool, gam, lam, x);
     reinterpret_cast<float4*>(feat)[idx] = make_float4(x[0], x[1], x[2], x[3]);
     f0out[idx] = f0;
+    flout[idx] = fl;
 }
 
 // acceptance test: starting from the network's prediction, at most four
@@ -401,7 +418,8 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, double gamma, const int
 // fallback list and the plain integrator solves it.
 __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const int* __restrict__ list, int64_t ncell,
                              double dt_code, const float* __restrict__ y, const double* __restrict__ f0a,
-                             double rel_tol, int* __restrict__ rej, int* __restrict__ nrej, gb_status* st)
+                             const double* __restrict__ fla, double rel_tol, int* __restrict__ rej,
+                             int* __restrict__ nrej, gb_status* st)
 {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= ncell) return;
@@ -411,36 +429,50 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const i
     gb_cool_vars v;
     double ei0, temp0;
     sur_load(g, c, gamma, blk, ci, v, ei0, temp0);
+    gb_cool_varsf vf;
+    gbcoolf::make_vars(p, v, vf);
+    const gb_cool_tabf tf = {c.Tf, c.nf, c.lamf, (float)c.T_min, (float)c.nd_min};
     const double dt = dt_code * p.time_unit;
-    const double f0 = f0a[idx];
+    const double f0 = f0a[idx], fl = fla[idx];
     const double emin_ = 0.5 * p.absTmin * v.TtoEI;
     double Tp = temp0 * pow(10.0, gbsur::Y_SCALE * (double)y[idx]);
     bool ok = isfinite(Tp) && Tp > 0.0;
     double ein = 0.0;
     if (ok) {
-        const double fl = cooling_floor(c, v);
+        // FP32 secant-Newton from the prediction
         double ea = ei0, fa = f0;
         double eb = fmax(Tp * v.TtoEI, emin_);
-        ok = false;
+        double J = 1.0;
+        bool conv = false;
         for (int it = 0; it < 4; ++it) {
-            double fb = dei_dt(c, v, fl, eb);
+            float gm, lm;
+            double fb = (double)gbcoolf::dei_parts(p, tf, vf, (float)fl, (float)eb, &gm, &lm);
             double gb = eb - dt * fb - ei0;
             double de = eb - ea;
-            double slope = fabs(de) > 1e-14 * eb ? (fb - fa) / de : 0.0;
-            double J = 1.0 - dt * slope;
+            double slope = fabs(de) > 1e-7 * eb ? (fb - fa) / de : 0.0;
+            J = 1.0 - dt * slope;
             if (!(J > 0.0)) break;
-            double delta = gb / J;
-            double en = eb - delta;
+            double en = eb - gb / J;
             if (!isfinite(en)) break;
             if (en < emin_) en = emin_;
-            if (fabs(en - eb) <= rel_tol * en && fabs(de) <= 0.05 * eb) {
-                ein = en;
-                ok = true;
-                break;
-            }
             ea = eb;
             fa = fb;
             eb = en;
+            if (fabs(eb - ea) <= 0.25 * rel_tol * eb && fabs(de) <= 0.05 * ea) {
+                conv = true;
+                break;
+            }
+        }
+        // FP64 check of the backward-Euler residual (heatCool.F90:1928-1950)
+        // at the converged state, with the last secant slope
+        if (conv) {
+            double f64 = dei_dt(c, v, fl, eb);
+            double g64 = eb - dt * f64 - ei0;
+            double delta = g64 / J;
+            ein = eb - delta;
+            ok = isfinite(ein) && ein > 0.0 && fabs(delta) <= rel_tol * ein;
+        } else {
+            ok = false;
         }
         // the solution moves the way the rate at the old state points
         if (ok && f0 < 0.0 && ein > ei0 * (1.0 + rel_tol)) ok = false;
@@ -452,8 +484,7 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const i
             temp = p.absTmin;
             ein = p.absTmin * v.TtoEI;
         }
-        gb_cool_diag d = {0, 0, 0, 0, 0};
-        if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update(c, v, temp, &d);
+        if (p.useDustCool && temp <= p.dust_sputter_temp) v.tdust = gbcoolf::dust_temperature(p, vf, (float)temp, vf.tdust);
         if (temp > p.absTmax) {
             ein = p.absTmax * v.TtoEI;
             temp = p.absTmax;
@@ -504,6 +535,7 @@ struct sur_bufs {
     float* feat = nullptr;
     float* y = nullptr;
     double* f0 = nullptr;
+    double* fl = nullptr;
     int* rej = nullptr;
     int* nrej = nullptr;
     int64_t cap = 0;
@@ -515,11 +547,13 @@ int sur_ensure(int64_t ncell)
     cudaFree(g_sb.feat);
     cudaFree(g_sb.y);
     cudaFree(g_sb.f0);
+    cudaFree(g_sb.fl);
     cudaFree(g_sb.rej);
     if (!g_sb.nrej && gb_check(cudaMalloc(&g_sb.nrej, sizeof(int)), "sur nrej")) return GB_ERR_CUDA;
     if (gb_check(cudaMalloc(&g_sb.feat, sizeof(float) * 4 * ncell), "sur feat") ||
         gb_check(cudaMalloc(&g_sb.y, sizeof(float) * ncell), "sur y") ||
         gb_check(cudaMalloc(&g_sb.f0, sizeof(double) * ncell), "sur f0") ||
+        gb_check(cudaMalloc(&g_sb.fl, sizeof(double) * ncell), "sur fl") ||
         gb_check(cudaMalloc(&g_sb.rej, sizeof(int) * ncell), "sur rej"))
         return GB_ERR_CUDA;
     g_sb.cap = ncell;
@@ -537,7 +571,7 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, gb_status* st, cud
     if (rc) return rc;
     const unsigned nb = (unsigned)((ncell + 127) / 128);
     gb_prof_begin(GBP_SUR_FEAT, s);
-    k_sur_feat<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, ncell, dt, g_sb.feat, g_sb.f0);
+    k_sur_feat<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, ncell, dt, g_sb.feat, g_sb.f0, g_sb.fl);
     gb_prof_end(GBP_SUR_FEAT, s);
     gb_prof_begin(GBP_MLP, s);
     rc = gb_mlp_launch_infer(ncell, g_sb.feat, g_sb.y, s);
@@ -545,8 +579,8 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, gb_status* st, cud
     if (rc) return rc;
     cudaMemsetAsync(g_sb.nrej, 0, sizeof(int), s);
     gb_prof_begin(GBP_SUR_ACCEPT, s);
-    k_sur_accept<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, ncell, dt, g_sb.y, g_sb.f0, g_sur_tol,
-                                    g_sb.rej, g_sb.nrej, st);
+    k_sur_accept<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, ncell, dt, g_sb.y, g_sb.f0, g_sb.fl,
+                                    g_sur_tol, g_sb.rej, g_sb.nrej, st);
     gb_prof_end(GBP_SUR_ACCEPT, s);
     gb_prof_begin(GBP_SUR_FALLBACK, s);
     k_sur_fallback<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, dt, g_sb.rej, g_sb.nrej, st);

@@ -22,6 +22,11 @@ struct gb_cool_ctx {
     const double* n;    // cool_dat(:, 1, 2), DENS_PTS
     const double* lam;  // cool_dat(:, :, 3), dens fastest
     double T_min, nd_min;
+    // FP32 copies for the learned-cooling path: axes, and cool_dat(:, :, 3)
+    // divided by mu_mol m_p (the molecular power per gram)
+    const float* Tf;
+    const float* nf;
+    const float* lamf;
 };
 
 struct gb_cool_vars {

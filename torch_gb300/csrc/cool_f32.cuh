@@ -1,0 +1,235 @@
+// FP32 restatement of the heating/cooling rate function de/dt
+// (heatCool.F90:1397-1588 and the terms it calls) for the learned-cooling
+// path: the surrogate's features and its Newton iterations use it; the
+// final acceptance check re-evaluates the residual in FP64 with
+// cool_dev.cuh. Power laws are evaluated as exp(ln C + a ln T) so that
+// terms such as 7.63e-81 T^13.8 stay inside FP32's range; intermediate
+// quantities are scaled the same way where a product would leave it.
+#pragma once
+
+#include "cool_dev.cuh"
+
+struct gb_cool_tabf {
+    const float* T;    // TEMP_PTS
+    const float* n;    // DENS_PTS
+    const float* lam;  // cool_dat(:, :, 3) / (mu_mol m_p): molecular power per gram
+    float T_min, nd_min;
+};
+
+struct gb_cool_varsf {
+    float ndens, rho, conf, Gflux, ephen, tdust, TtoEI, xHp, mu_mol;
+    float cr_pref;  // strat * crIonRate * crIonEnergy / (rho / n)
+    float lnNH;     // ln(crIonNH)
+};
+
+namespace gbcoolf {
+
+__device__ __forceinline__ float lin(float x1, float y1, float x2, float y2, float x)
+{
+    return (y2 - y1) / (x2 - x1) * (x - x1) + y1;
+}
+
+__device__ __forceinline__ float pw(float lnC, float a, float lnT) { return __expf(lnC + a * lnT); }
+
+// Radloss (heatCool.F90:1590-1667) in log space
+__device__ __forceinline__ float radloss(float T)
+{
+    const float l = __logf(T);
+    if (T >= 1.70e4f) {
+        if (T >= 5.62e5f) {
+            if (T >= 2.75e6f) return T >= 3.16e7f ? pw(-61.0416264f, 0.5f, l) : pw(-46.7079387f, -0.33f, l);
+            return T >= 1.78e6f ? pw(-7.85193121f, -2.95f, l) : pw(-50.5136917f, 0.01f, l);
+        }
+        if (T >= 7.94e4f) return T >= 2.51e5f ? pw(-23.9471542f, -2.0f, l) : pw(-48.9528915f, 0.01f, l);
+        return T >= 3.98e4f ? pw(-71.3801379f, 2.0f, l) : pw(-47.9629208f, -0.216f, l);
+    }
+    if (T >= 1.e3f) {
+        if (T >= 6.31e3f) return T >= 1.0e4f ? pw(-184.477305f, 13.8f, l) : pw(-61.0287645f, 0.396f, l);
+        return T >= 3.16e3f ? pw(-58.8964335f, 0.152f, l) : pw(-60.5058714f, 0.352f, l);
+    }
+    if (T >= 3.98e1f) return T >= 2.00e2f ? pw(-61.0513826f, 0.431f, l) : pw(-64.0536723f, 0.997f, l);
+    return T >= 2.51e1f ? pw(-65.9036743f, 1.5f, l) : pw(-73.5919686f, 3.885f, l);
+}
+
+__device__ __forceinline__ float fmx(float a, float b) { return a > b ? a : b; }
+__device__ __forceinline__ float fmn(float a, float b) { return a < b ? a : b; }
+
+__device__ __forceinline__ float ramp_T(float T, float lo, float hi)
+{
+    float ll10 = lo + 0.1f * lo, ul10 = hi - 0.1f * hi;
+    if (T >= ul10) return lin(ul10, 1.0f, hi, 0.0f, T);
+    if (T <= ll10) return lin(lo, 0.0f, ll10, 1.0f, T);
+    return 1.0f;
+}
+
+__device__ __forceinline__ int find(const float* x, float x0, int N)
+{
+    if (x0 < __ldg(x)) return 0;
+    if (x0 > __ldg(x + N - 1)) return N;
+    int il = 1, ir = N;
+    while (ir != il + 1) {
+        int im = (il + ir) / 2;
+        if (__ldg(x + im - 1) > x0) ir = im;
+        else il = im;
+    }
+    return il;
+}
+
+// de/dt split into heating Gamma and cooling Lambda (as dei_parts);
+// floor_ is the cooling at the floors (state-independent per cell)
+__device__ float dei_parts(const gb_cool_params& p, const gb_cool_tabf& t, const gb_cool_varsf& v, float floor_,
+                           float ei, float* gam, float* lam)
+{
+    float T = ei / v.TtoEI;
+    if (T < 0.0f) T = 1.0f;
+    const float sqT = sqrtf(T);
+    // Jeans-length column density (heatCool.F90:1669-1722)
+    const float lam_j = v.ndens / v.rho * sqrtf((float)(5.0 / 3.0 * 3.14159265358979 * (double)p.boltz / 6.6725985e-8) * T / v.ndens);
+    const float ncol = lam_j * v.ndens;
+    float eplus = 0.0f;
+    if (T <= (float)p.theatmax && T >= (float)p.theatmin) {
+        if (p.use_cr_heating) {
+            if (p.crIonNH == 1.0 && p.crIonExp == 1.0) eplus = v.cr_pref;
+            else eplus = v.cr_pref * __expf(-(float)p.crIonExp * (__logf(fmx((float)p.crIonNH, ncol)) - v.lnNH));
+        }
+        eplus *= ramp_T(T, (float)p.theatmin, (float)p.theatmax);
+    }
+    const float fext = __expf(-3.5f * (ncol * 0.01f / 1.87e21f));
+    const float G = v.Gflux + (float)p.Gzero * fext;
+    float PeHeat = 0.0f;
+    const float ulpe = fmn((float)p.theatmax, (float)p.dust_sputter_temp);
+    if (T <= ulpe && T >= (float)p.theatmin) {
+        const float xl = v.xHp == 0.0f ? 1e-8f : v.xHp;
+        float eff;
+        if (p.pe_recipe == 1) {
+            float Gf = G * sqT / (xl * v.ndens * 0.5f);
+            eff = 4.9e-2f / (1.0f + 4.0e-3f * __powf(Gf, 0.73f)) + 3.7e-2f * __powf(T * 1e-4f, 0.7f) / (1.0f + 2.0e-4f * Gf);
+            PeHeat = (float)p.pe_norm * eff * G * (v.ndens / v.rho);
+        } else if (p.pe_recipe == 0) {
+            float Gf = G * sqT / (xl * v.ndens);
+            float gp = Gf > 0.0f ? __logf(Gf) : -1e30f;
+            eff = (7.64f + 4.52f * __expf(0.132f * __logf(T))) /
+                  (1.0f + (0.04371f * __expf(0.452f * gp)) * (1.0f + 0.00557f * __expf(0.675f * gp)));
+            // 1e-26 * eff * G / (rho / n), with rho/n ~ 4e-24 kept in range
+            PeHeat = 1e-26f * eff * G * (v.ndens / v.rho);
+        } else {
+            PeHeat = (float)p.pe_norm * 0.05f * G * (v.ndens / v.rho);
+        }
+        PeHeat *= ramp_T(T, (float)p.theatmin, ulpe);
+    }
+    eplus += v.ephen;
+    // atomic cooling (heatCool.F90:1116-1200)
+    float emin = 0.0f;
+    if (T <= (float)p.tradmax && T >= (float)p.tradmin && v.ndens >= (float)p.dradmin && v.ndens <= (float)p.dradmax) {
+        emin = radloss(T);
+        if (v.xHp > 1e-2f && T < 1.2e4f) {
+            float DG = lin(1e-2f, 1.0f, 1e-1f, 5.0f, fmn(1e-1f, v.xHp));
+            emin *= DG;
+            if (T > 1e4f) {
+                float q = lin(1e4f, 1.0f, 1.2e4f, sqrtf(DG), T);
+                emin /= q * q;
+            }
+        } else if (v.xHp < 1e-2f && T < 1e4f) {
+            float DG = lin(1e-4f, 0.35f, 1e-2f, 1.0f, fmx(1e-4f, v.xHp));
+            emin *= DG;
+            if (T > 9e3f) emin /= lin(9e3f, 1.0f, 1e4f, DG, T);
+        }
+        emin *= ramp_T(T, (float)p.tradmin, (float)p.tradmax) * v.conf;
+    }
+    float cool_pw = 0.0f, cool_dg = 0.0f;
+    if (p.useDustCool) {
+        if (v.ndens >= (float)p.nd_cool_min && v.ndens <= (float)p.nd_cool_max && T >= (float)p.T_cool_min &&
+            T <= (float)p.theatmax) {
+            int it = find(t.T, fmx(T, t.T_min), GB_TEMP_PTS);
+            int id = find(t.n, fmx(v.ndens, t.nd_min), GB_DENS_PTS);
+            if (it > 0 && it <= GB_TEMP_PTS && id > 0 && id <= GB_DENS_PTS)
+                cool_pw = __ldg(t.lam + (id - 1) + GB_DENS_PTS * (it - 1));
+            cool_pw *= ramp_T(T, (float)p.T_cool_min, (float)p.theatmax) *
+                       ramp_T(v.ndens, (float)p.nd_cool_min, (float)p.nd_cool_max);
+        }
+        if (T <= (float)p.dust_sputter_temp) {
+            // 3.8e-33 n^2 (...) / rho  ->  3.8e-33 n (n / rho) (...)
+            cool_dg = 3.8e-33f * v.ndens * (v.ndens / v.rho) * (1.0f - 0.8f * __expf(-75.0f / T)) * (T - v.tdust) * sqT;
+            float ul = (float)p.dust_sputter_temp, ul10 = ul - 0.1f * ul;
+            if (T >= ul10) cool_dg *= lin(ul10, 1.0f, ul, 0.0f, T);
+        }
+    }
+    *gam = eplus + PeHeat + floor_ + fmx(-cool_dg, 0.0f);
+    *lam = emin + cool_pw + fmx(cool_dg, 0.0f);
+    return eplus + PeHeat - emin - cool_pw - cool_dg + floor_;
+}
+
+// T_dust after a step (heatCool.F90:430-443 + get_dust_temperature,
+// :703-884) in FP32: dust heating by FUV photons that did not eject
+// photo-electrons plus cosmic rays, Newton on the dust energy balance
+__device__ float dust_temperature(const gb_cool_params& p, const gb_cool_varsf& v, float T, float tdust_in)
+{
+    const float sqT = sqrtf(T);
+    const float lam_j = v.ndens / v.rho * sqrtf((float)(5.0 / 3.0 * 3.14159265358979 * (double)p.boltz / 6.6725985e-8) * T / v.ndens);
+    const float ncol = lam_j * v.ndens;
+    const float G = v.Gflux + (float)p.Gzero * __expf(-3.5f * (ncol * 0.01f / 1.87e21f));
+    // dust heating / (n 1e-33): photo-electric remainder + CR heating * rho
+    float heat = 0.0f;
+    const float ulpe = fmn((float)p.theatmax, (float)p.dust_sputter_temp);
+    if (T <= ulpe && T >= (float)p.theatmin) {
+        const float xl = v.xHp == 0.0f ? 1e-8f : v.xHp;
+        float eff = 0.05f, dh;
+        if (p.pe_recipe == 0) {
+            float Gf = G * sqT / (xl * v.ndens);
+            float gp = Gf > 0.0f ? __logf(Gf) : -1e30f;
+            eff = (7.64f + 4.52f * __expf(0.132f * __logf(T))) /
+                  (1.0f + (0.04371f * __expf(0.452f * gp)) * (1.0f + 0.00557f * __expf(0.675f * gp)));
+            dh = fmx(((float)p.pe_norm * 1e26f - eff) * G * 1e7f, 0.0f);  // (pe_norm - 1e-26 eff) G n / (n 1e-33)
+        } else if (p.pe_recipe == 1) {
+            float Gf = G * sqT / (xl * v.ndens * 0.5f);
+            eff = 4.9e-2f / (1.0f + 4.0e-3f * __powf(Gf, 0.73f)) + 3.7e-2f * __powf(T * 1e-4f, 0.7f) / (1.0f + 2.0e-4f * Gf);
+            dh = (float)p.pe_norm * 1e33f * fmx(0.0f, 1.0f - eff) * G;
+        } else {
+            dh = (float)p.pe_norm * 1e33f * 0.95f * G;
+        }
+        heat = dh;
+    }
+    if (p.use_cr_heating && T <= (float)p.theatmax && T >= (float)p.theatmin) {
+        float cr = v.cr_pref;
+        if (!(p.crIonNH == 1.0 && p.crIonExp == 1.0))
+            cr *= __expf(-(float)p.crIonExp * (__logf(fmx((float)p.crIonNH, ncol)) - v.lnNH));
+        cr *= ramp_T(T, (float)p.theatmin, (float)p.theatmax);
+        heat += cr * (v.rho / v.ndens) * 1e33f;
+    }
+    const float absTmin = (float)p.absTmin;
+    float td = tdust_in < absTmin ? absTmin : tdust_in;
+    const float tg = T < absTmin ? absTmin : T;
+    const float cfac = 3.8f * v.ndens * (1.0f - 0.8f * __expf(-75.0f / tg)) * sqrtf(tg);
+    float err = 1e-3f;
+    for (int l = 0; l < 100 && err > 1e-4f; ++l) {
+        float t3 = td * td * td;
+        float lamd = 6.8f * t3 * t3;
+        float eq = heat + cfac * (tg - td) - lamd;
+        float det = -(6.0f * lamd / td) - cfac;
+        float tn = td - eq / det;
+        err = fabsf(tn - td) / td;
+        td = tn;
+        if (td < 0.1f) {
+            td = 0.1f;
+            err = 1e-5f;
+        }
+    }
+    return td < absTmin ? absTmin : td;
+}
+
+__device__ __forceinline__ void make_vars(const gb_cool_params& p, const gb_cool_vars& v, gb_cool_varsf& f)
+{
+    f.ndens = (float)v.ndens;
+    f.rho = (float)v.rho;
+    f.conf = (float)v.conf;
+    f.Gflux = (float)v.Gflux;
+    f.ephen = (float)v.ephen;
+    f.tdust = (float)v.tdust;
+    f.TtoEI = (float)v.TtoEI;
+    f.xHp = (float)v.xHp;
+    f.mu_mol = (float)v.mu_mol;
+    f.cr_pref = (float)(v.strat_factor * p.crIonRate * p.crIonEnergy / (v.rho / v.ndens));
+    f.lnNH = (float)log(p.crIonNH);
+}
+
+}  // namespace gbcoolf
