@@ -93,7 +93,7 @@ def make_grid(G, ic, precision, cooling=True):
     return g, units
 
 
-def run_path(G, g, precision, steps, warmup, cool=True, surrogate=False, profile=False):
+def run_path(G, g, precision, steps, warmup, cool=True, surrogate=False, profile=False, ncu_range=False):
     import torch
     G.init_hydro(G.hydro_params(True, precision=precision))
     G.set_cooling_mode(surrogate)
@@ -108,50 +108,59 @@ def run_path(G, g, precision, steps, warmup, cool=True, surrogate=False, profile
     torch.cuda.synchronize()
     if profile:
         G.prof_enable(True)
+    if ncu_range:
+        torch.cuda.cudart().cudaProfilerStart()
     e0.record(s)
     for _ in range(steps):
         dt = g.compute_dt().item()
         g.evolve_step(dt, cool=cool)
     e1.record(s)
     torch.cuda.synchronize()
+    if ncu_range:
+        torch.cuda.cudart().cudaProfilerStop()
     prof = G.prof_read() if profile else None
     G.prof_enable(False)
     G.set_cooling_mode(False)
     return e0.elapsed_time(e1) / steps, g.status_read(), prof
 
 
-def cpu_baseline(nblocks_sample=8, steps=1):
-    """The oracle (C port, OpenMP over blocks) on a bounded sample of the
-    same workload: `nblocks_sample` blocks of the 128^3 box, MHD + cooling."""
+def cpu_baseline(ic=None, steps=1):
+    """The oracle (C port of the reference's algorithm, OpenMP over blocks,
+    all host cores) on the same workload: `steps` full steps of the 512-block
+    MHD + cooling box (guard fill, dt, unsplit MHD, per-cell cooling)."""
     from oracle import oracle as O
     from torch_gb300 import gbhydro as G
     from torch_gb300 import tables
     from torch_gb300 import workloads as W
     O.build()
     wl = WORKLOAD
-    ic = W.turbulent_box(2, 2, 2, seed=wl["seed"], sigma_ln=wl["sigma_ln"], mach=wl["mach"], mhd=True,
-                         nvar=10)
+    if ic is None:
+        ic = W.turbulent_box(wl["nbx"], wl["nby"], wl["nbz"], seed=wl["seed"], sigma_ln=wl["sigma_ln"],
+                             mach=wl["mach"], mhd=True, beta=wl["beta"], dA=wl["dA"], nvar=10)
+    nb = (wl["nbx"], wl["nby"], wl["nbz"])
     p = O.hydro_params(True)
-    u, fx, fy, fz, dx = ic["u"], ic["fx"], ic["fy"], ic["fz"], 1.0 / (16 * wl["nbx"])
+    u, fx, fy, fz = ic["u"].copy(), ic["fx"].copy(), ic["fy"].copy(), ic["fz"].copy()
+    dx = ic["dx"]
     units = G.code_units()
     cp = O.cool_params()
     tab = O.table_from_ilog(*tables.read_compact())
     nthreads = O.lib().orc_num_threads()
+    sl = (slice(None), slice(4, 20), slice(4, 20), slice(4, 20))
     t0 = time.perf_counter()
     for _ in range(steps):
-        O.fill_guards_periodic(p, 2, 2, 2, u, fx, fy, fz)
+        O.fill_guards_periodic(p, *nb, u, fx, fy, fz)
         dt = 0.8 * O.dt_limit(p, u, dx, dx, dx)
         O.unsplit_blocks(p, u, fx, fy, fz, dt, dx, dx, dx)
-        sl = (slice(None), slice(4, 20), slice(4, 20), slice(4, 20))
-        rho = (u[:, 0][sl] * units["dens_unit"]).ravel().copy()
-        ei = (u[:, 6][sl] * units["vel_unit"] ** 2).ravel().copy()
+        rho = np.ascontiguousarray(u[:, 0][sl] * units["dens_unit"]).ravel()
+        ei = np.ascontiguousarray(u[:, 6][sl] * units["vel_unit"] ** 2).ravel()
         T = ei * (2.0 / 3.0) * (24.0 / 11.0) * G.MP / G.KB
         td = np.full_like(T, 15.0)
         O.radheat_cells(cp, tab, dt * units["time_unit"], rho, ei.copy(), ei, T, td)
     el = time.perf_counter() - t0
-    zones = nblocks_sample * 4096 * steps
+    zones = int(np.prod(nb)) * 4096 * steps
     return {"value": zones / el, "unit": "zone-updates/s", "cores": int(nthreads), "kind": "port",
-            "sample": f"{nblocks_sample} blocks of 16^3 (MHD+cooling, oracle C port, OpenMP) x {steps} step(s), {el:.2f} s"}
+            "sample": f"{steps} full step(s) of the {int(np.prod(nb))}-block MHD+cooling workload on the oracle "
+                      f"(C port, OpenMP over blocks), {el:.2f} s"}
 
 
 def reference_arm(args):
@@ -161,17 +170,21 @@ def reference_arm(args):
     steps = max(1, args.steps)
     vals = []
     cb = None
-    for _ in range(args.warmup):
-        cpu_baseline(8, 1)
+    from torch_gb300 import workloads as W
+    wl = WORKLOAD
+    ic = W.turbulent_box(wl["nbx"], wl["nby"], wl["nbz"], seed=wl["seed"], sigma_ln=wl["sigma_ln"],
+                         mach=wl["mach"], mhd=True, beta=wl["beta"], dA=wl["dA"], nvar=10)
+    for _ in range(min(args.warmup, 1)):
+        cpu_baseline(ic, 1)
     for _ in range(steps):
-        cb = cpu_baseline(8, 1)
+        cb = cpu_baseline(ic, 1)
         vals.append(cb["value"])
     v = float(np.median(vals))
     cb["value"] = v
     line = {"metric": "zone-updates/s", "value": v, "unit": "zone-updates/s", "n_gpus": args.gpus,
             "steps": steps, "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
             "dtype": "f64", "data": "synthetic", "scaling": "weak", "vs_baseline": None,
-            "config": {"workload": WORKLOAD["name"], "sample_blocks": 8},
+            "config": {"workload": WORKLOAD["name"], "blocks": 512},
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "zone-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "FLASH 4.6.2 (the reference's hydro) is not in the reference tree and no Fortran "
@@ -224,6 +237,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--weights", default=None, help="load surrogate weights (.npy) instead of training")
+    ap.add_argument("--save-weights", default=None)
+    ap.add_argument("--ncu-range", action="store_true",
+                    help="bracket the fast path's timed region with cudaProfilerStart/Stop")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -247,29 +264,40 @@ def main():
     zones = wl["nbx"] * wl["nby"] * wl["nbz"] * 4096
     # learned cooling: 1e7 samples from the plain integrator, then training
     # (outside the timed region; reported)
-    t0 = time.perf_counter()
-    G.init_cooling(G.cool_params())
-    feat, tgt = G.surrogate_samples(10_000_000, 2024)
-    keep = torch.isfinite(tgt)
-    feat, tgt = feat[keep].contiguous(), tgt[keep].contiguous()
-    torch.cuda.synchronize()
-    t_samples = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    G.mlp_init(7)
-    losses = G.mlp_train(feat, tgt, steps=8000, batch=16384, lr=3e-3, seed=5)
-    t_train = time.perf_counter() - t0
-    del feat, tgt
+    if args.weights:
+        G.mlp_init(7)
+        G.mlp_set_weights(np.load(args.weights))
+        t_samples = t_train = 0.0
+        losses = np.array([np.nan])
+    else:
+        t0 = time.perf_counter()
+        G.init_cooling(G.cool_params())
+        feat, tgt = G.surrogate_samples(10_000_000, 2024)
+        keep = torch.isfinite(tgt)
+        feat, tgt = feat[keep].contiguous(), tgt[keep].contiguous()
+        torch.cuda.synchronize()
+        t_samples = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        G.mlp_init(7)
+        losses = G.mlp_train(feat, tgt, steps=8000, batch=16384, lr=3e-3, seed=5)
+        t_train = time.perf_counter() - t0
+        del feat, tgt
+    if args.save_weights:
+        np.save(args.save_weights, G.mlp_weights())
     G.init_cooling(G.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
                                  time_unit=units["time_unit"]))
     g_plain, _ = make_grid(G, ic, 0)
     g_fast, _ = make_grid(G, ic, 1)
+    g_mixed, _ = make_grid(G, ic, 1)
     os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
     clk = ClockSampler(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv"))
     if world > 1:
         dist.barrier()
     with clk:
         ms_plain, st_plain, _ = run_path(G, g_plain, 0, args.steps, args.warmup)
-        ms_fast, st_fast, prof = run_path(G, g_fast, 1, args.steps, args.warmup, surrogate=True, profile=True)
+        ms_fast, st_fast, prof = run_path(G, g_fast, 1, args.steps, args.warmup, surrogate=True, profile=True,
+                                          ncu_range=args.ncu_range)
+        ms_mixed, st_mixed, _ = run_path(G, g_mixed, 1, args.steps, args.warmup)
     if world > 1:
         t = torch.tensor([ms_plain, ms_fast], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -279,6 +307,9 @@ def main():
     sl = (slice(None), slice(4, 20), slice(4, 20), slice(4, 20))
     l1 = {v: float(np.abs(a[:, i][sl] - b[:, i][sl]).sum() / np.abs(a[:, i][sl]).sum())
           for v, i in (("dens", 0), ("pres", 4))}
+    cmx = g_mixed.u.cpu().numpy()
+    l1_mixed = {v: float(np.abs(a[:, i][sl] - cmx[:, i][sl]).sum() / np.abs(a[:, i][sl]).sum())
+                for v, i in (("dens", 0), ("pres", 4))}
     sT = g_plain.slots["TEMP"]
     relT = np.abs(a[:, sT][sl] - b[:, sT][sl]) / a[:, sT][sl]
     tolT = np.abs(a[:, sT][sl] - b[:, sT][sl]) <= 0.01 * a[:, sT][sl] + 2.0
@@ -306,6 +337,8 @@ def main():
         "plain_fp64": {"value": zones * world / (ms_plain * 1e-3), "ms_per_step": ms_plain},
         "speedup_vs_plain_fp64": ms_plain / ms_fast,
         "l1_err_vs_fp64": l1,
+        "l1_err_mixed_hydro_vs_fp64": l1_mixed,
+        "mixed_plain_cooling": {"value": zones * world / (ms_mixed * 1e-3), "ms_per_step": ms_mixed},
         "kernel_ms_per_step_fast": {k: v[0] / args.steps for k, v in prof.items()},
         "kernel_launches_per_step_fast": {k: v[1] / args.steps for k, v in prof.items()},
         "temp_rel_err_vs_plain": {"p50": float(np.median(relT)), "p99": float(np.quantile(relT, 0.99)),
@@ -328,7 +361,7 @@ def main():
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline()
+        line["cpu_baseline"] = cpu_baseline(ic, 1)
     print(json.dumps(line))
 
 
