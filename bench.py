@@ -209,11 +209,25 @@ def e2e_run(G, g, steps, warmup):
     st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     lt, n = g.list_tensor()
 
-    def one():
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    parts = np.zeros(3)
+
+    def one(timed=False):
+        if timed:
+            ev[0].record()
         G.check(L.gb_grid_upload_flash(C.c_void_p(host.data_ptr()), nunk, hslot, g.nblocks, st), "upload")
+        if timed:
+            ev[1].record()
         dt = g.compute_dt().item()
         g.evolve_step(dt, cool=True)
+        if timed:
+            ev[2].record()
         G.check(L.gb_grid_download_flash(C.c_void_p(host.data_ptr()), nunk, hslot, g.nblocks, st), "download")
+        if timed:
+            ev[3].record()
+            torch.cuda.synchronize()
+            for q in range(3):
+                parts[q] += ev[q].elapsed_time(ev[q + 1])
 
     for _ in range(warmup):
         one()
@@ -227,7 +241,8 @@ def e2e_run(G, g, steps, warmup):
     torch.cuda.synchronize()
     ms = a.elapsed_time(b) / steps
     nbytes = host.numel() * 8
-    return ms, nbytes
+    one(timed=True)
+    return ms, nbytes, {"upload_ms": parts[0], "step_ms": parts[1], "download_ms": parts[2]}
 
 
 def main():
@@ -313,7 +328,9 @@ def main():
     sT = g_plain.slots["TEMP"]
     relT = np.abs(a[:, sT][sl] - b[:, sT][sl]) / a[:, sT][sl]
     tolT = np.abs(a[:, sT][sl] - b[:, sT][sl]) <= 0.01 * a[:, sT][sl] + 2.0
-    e2e_ms, e2e_bytes = e2e_run(G, g_fast, max(2, args.steps // 2), 1)
+    G.set_cooling_mode(True)
+    e2e_ms, e2e_bytes, e2e_parts = e2e_run(G, g_fast, max(2, args.steps // 2), 1)
+    G.set_cooling_mode(False)
     hbm, hbm_kind = peaks()
     # dominant kernel: largest share of the timed region. Algorithmic bytes
     # per launch = 216 B per zone-update (12 FP64 MHD words + 3 cooling
@@ -356,7 +373,7 @@ def main():
                      "frac": ach / hbm, "traffic": None, "peak_kind": hbm_kind, "launch_ms": dom_ms,
                      "algo_bytes_per_launch": 216.0 * per_launch_zones[dom]},
         "e2e": {"value": zones / (e2e_ms * 1e-3), "unit": "zone-updates/s", "h2d_bytes_per_step": e2e_bytes,
-                "d2h_bytes_per_step": e2e_bytes},
+                "d2h_bytes_per_step": e2e_bytes, "parts": e2e_parts},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

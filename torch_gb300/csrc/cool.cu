@@ -381,9 +381,8 @@ __device__ __forceinline__ void cell_of(int64_t idx, const int* list, int& blk, 
 }
 
 // features + the rate at the old state
-__global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, double gamma, const int* __restrict__ list, int64_t ncell,
-                           double dt_code, float* __restrict__ feat, double* __restrict__ f0out,
-                           double* __restrict__ flout)
+__global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double gamma, const int* __restrict__ list,
+                           int64_t ncell, double dt_code, float* __restrict__ feat, float2* __restrict__ f0out)
 {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= ncell) return;
@@ -392,19 +391,25 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, double gamma, const int
     gb_cool_vars v;
     double ei, temp;
     sur_load(g, c, gamma, blk, ci, v, ei, temp);
-    const double fl = cooling_floor(c, v);
     gb_cool_varsf vf;
-    gbcoolf::make_vars(c.p, v, vf);
+    gbcoolf::make_vars(pf, v, vf);
     const gb_cool_tabf tf = {c.Tf, c.nf, c.lamf, (float)c.T_min, (float)c.nd_min};
+    const float fl = gbcoolf::cooling_floor(pf, tf, vf);
     float gam, lam;
-    float f0 = gbcoolf::dei_parts(c.p, tf, vf, (float)fl, (float)ei, &gam, &lam);
-    double tcool = ei / fmax(fabs((double)f0), 1e-300);
-    double dt = dt_code * c.p.time_unit;
-    float x[4];
-    gbsur::features(v.ndens, temp, dt / tcool, gam, lam, x);
-    reinterpret_cast<float4*>(feat)[idx] = make_float4(x[0], x[1], x[2], x[3]);
-    f0out[idx] = f0;
-    flout[idx] = fl;
+    const float eif = (float)ei;
+    float f0 = gbcoolf::dei_parts(pf, tf, vf, fl, eif, &gam, &lam);
+    const float dt = (float)(dt_code * c.p.time_unit);
+    // features in FP32: dt / t_cool = dt |f| / e
+    const float r = dt * fabsf(f0) / eif;
+    float lr = log10f(fmaxf(r, 1e-30f));
+    lr = fminf(fmaxf(lr, (float)-gbsur::R_CLAMP), (float)gbsur::R_CLAMP);
+    float lh = log10f(fmaxf(gam, 1e-30f)) - log10f(fmaxf(lam, 1e-30f));
+    lh = fminf(fmaxf(lh, (float)-gbsur::H_CLAMP), (float)gbsur::H_CLAMP);
+    reinterpret_cast<float4*>(feat)[idx] =
+        make_float4((log10f(vf.ndens) - (float)gbsur::N_MID) / (float)gbsur::N_HALF,
+                    (log10f((float)temp) - (float)gbsur::T_MID) / (float)gbsur::T_HALF, lr / (float)gbsur::R_HALF,
+                    lh / (float)gbsur::H_HALF);
+    f0out[idx] = make_float2(f0, fl);
 }
 
 // acceptance test: starting from the network's prediction, at most four
@@ -416,10 +421,9 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, double gamma, const int
 // slope (its two points within 5 % of each other) and the energy moved
 // the way the rate at the old state points; otherwise it goes to the
 // fallback list and the plain integrator solves it.
-__global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const int* __restrict__ list, int64_t ncell,
-                             double dt_code, const float* __restrict__ y, const double* __restrict__ f0a,
-                             const double* __restrict__ fla, double rel_tol, int* __restrict__ rej,
-                             int* __restrict__ nrej, gb_status* st)
+__global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double gamma, const int* __restrict__ list,
+                             int64_t ncell, double dt_code, const float* __restrict__ y, const float2* __restrict__ f0a,
+                             double rel_tol, int* __restrict__ rej, int* __restrict__ nrej, gb_status* st)
 {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= ncell) return;
@@ -430,12 +434,14 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const i
     double ei0, temp0;
     sur_load(g, c, gamma, blk, ci, v, ei0, temp0);
     gb_cool_varsf vf;
-    gbcoolf::make_vars(p, v, vf);
+    gbcoolf::make_vars(pf, v, vf);
     const gb_cool_tabf tf = {c.Tf, c.nf, c.lamf, (float)c.T_min, (float)c.nd_min};
     const double dt = dt_code * p.time_unit;
-    const double f0 = f0a[idx], fl = fla[idx];
+    const float2 f0fl = f0a[idx];
+    const double f0 = f0fl.x;
+    const float flf = f0fl.y;
     const double emin_ = 0.5 * p.absTmin * v.TtoEI;
-    double Tp = temp0 * pow(10.0, gbsur::Y_SCALE * (double)y[idx]);
+    double Tp = (double)((float)temp0 * exp10f((float)gbsur::Y_SCALE * y[idx]));
     bool ok = isfinite(Tp) && Tp > 0.0;
     double ein = 0.0;
     if (ok) {
@@ -446,7 +452,7 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const i
         bool conv = false;
         for (int it = 0; it < 4; ++it) {
             float gm, lm;
-            double fb = (double)gbcoolf::dei_parts(p, tf, vf, (float)fl, (float)eb, &gm, &lm);
+            double fb = (double)gbcoolf::dei_parts(pf, tf, vf, flf, (float)eb, &gm, &lm);
             double gb = eb - dt * fb - ei0;
             double de = eb - ea;
             double slope = fabs(de) > 1e-7 * eb ? (fb - fa) / de : 0.0;
@@ -466,7 +472,7 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const i
         // FP64 check of the backward-Euler residual (heatCool.F90:1928-1950)
         // at the converged state, with the last secant slope
         if (conv) {
-            double f64 = dei_dt(c, v, fl, eb);
+            double f64 = dei_dt(c, v, cooling_floor(c, v), eb);
             double g64 = eb - dt * f64 - ei0;
             double delta = g64 / J;
             ein = eb - delta;
@@ -484,7 +490,7 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, double gamma, const i
             temp = p.absTmin;
             ein = p.absTmin * v.TtoEI;
         }
-        if (p.useDustCool && temp <= p.dust_sputter_temp) v.tdust = gbcoolf::dust_temperature(p, vf, (float)temp, vf.tdust);
+        if (p.useDustCool && temp <= p.dust_sputter_temp) v.tdust = gbcoolf::dust_temperature(pf, vf, (float)temp, vf.tdust);
         if (temp > p.absTmax) {
             ein = p.absTmax * v.TtoEI;
             temp = p.absTmax;
@@ -534,12 +540,39 @@ double g_sur_tol = 2e-3;
 struct sur_bufs {
     float* feat = nullptr;
     float* y = nullptr;
-    double* f0 = nullptr;
-    double* fl = nullptr;
+    float2* f0 = nullptr;
     int* rej = nullptr;
     int* nrej = nullptr;
     int64_t cap = 0;
 } g_sb;
+
+gb_cool_pf make_pf(const gb_cool_params& p)
+{
+    gb_cool_pf f;
+    f.theatmin = (float)p.theatmin;
+    f.theatmax = (float)p.theatmax;
+    f.tradmin = (float)p.tradmin;
+    f.tradmax = (float)p.tradmax;
+    f.dradmin = (float)p.dradmin;
+    f.dradmax = (float)p.dradmax;
+    f.dust_sputter_temp = (float)p.dust_sputter_temp;
+    f.Gzero = (float)p.Gzero;
+    f.pe_norm = (float)p.pe_norm;
+    f.crIonExp = (float)p.crIonExp;
+    f.crIonNH = (float)p.crIonNH;
+    f.lnNH = (float)log(p.crIonNH);
+    f.crRE = (float)(p.crIonRate * p.crIonEnergy);
+    f.T_cool_min = (float)p.T_cool_min;
+    f.nd_cool_min = (float)p.nd_cool_min;
+    f.nd_cool_max = (float)p.nd_cool_max;
+    f.absTmin = (float)p.absTmin;
+    f.jeansK = (float)(5.0 / 3.0 * 3.1415926535897932384 * p.boltz / 6.6725985e-8);
+    f.use_cr_heating = p.use_cr_heating;
+    f.cr_uniform = (p.crIonNH == 1.0 && p.crIonExp == 1.0) ? 1 : 0;
+    f.pe_recipe = p.pe_recipe;
+    f.useDustCool = p.useDustCool;
+    return f;
+}
 
 int sur_ensure(int64_t ncell)
 {
@@ -547,13 +580,11 @@ int sur_ensure(int64_t ncell)
     cudaFree(g_sb.feat);
     cudaFree(g_sb.y);
     cudaFree(g_sb.f0);
-    cudaFree(g_sb.fl);
     cudaFree(g_sb.rej);
     if (!g_sb.nrej && gb_check(cudaMalloc(&g_sb.nrej, sizeof(int)), "sur nrej")) return GB_ERR_CUDA;
     if (gb_check(cudaMalloc(&g_sb.feat, sizeof(float) * 4 * ncell), "sur feat") ||
         gb_check(cudaMalloc(&g_sb.y, sizeof(float) * ncell), "sur y") ||
-        gb_check(cudaMalloc(&g_sb.f0, sizeof(double) * ncell), "sur f0") ||
-        gb_check(cudaMalloc(&g_sb.fl, sizeof(double) * ncell), "sur fl") ||
+        gb_check(cudaMalloc(&g_sb.f0, sizeof(float2) * ncell), "sur f0") ||
         gb_check(cudaMalloc(&g_sb.rej, sizeof(int) * ncell), "sur rej"))
         return GB_ERR_CUDA;
     g_sb.cap = ncell;
@@ -571,7 +602,8 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, gb_status* st, cud
     if (rc) return rc;
     const unsigned nb = (unsigned)((ncell + 127) / 128);
     gb_prof_begin(GBP_SUR_FEAT, s);
-    k_sur_feat<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, ncell, dt, g_sb.feat, g_sb.f0, g_sb.fl);
+    const gb_cool_pf pf = make_pf(g_gb.cool.p);
+    k_sur_feat<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, g_sb.feat, g_sb.f0);
     gb_prof_end(GBP_SUR_FEAT, s);
     gb_prof_begin(GBP_MLP, s);
     rc = gb_mlp_launch_infer(ncell, g_sb.feat, g_sb.y, s);
@@ -579,7 +611,7 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, gb_status* st, cud
     if (rc) return rc;
     cudaMemsetAsync(g_sb.nrej, 0, sizeof(int), s);
     gb_prof_begin(GBP_SUR_ACCEPT, s);
-    k_sur_accept<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, ncell, dt, g_sb.y, g_sb.f0, g_sb.fl,
+    k_sur_accept<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, g_sb.y, g_sb.f0,
                                     g_sur_tol, g_sb.rej, g_sb.nrej, st);
     gb_prof_end(GBP_SUR_ACCEPT, s);
     gb_prof_begin(GBP_SUR_FALLBACK, s);

@@ -29,6 +29,9 @@ struct gb_cool_ctx {
     const float* lamf;
 };
 
+// FP32 parameter block of the learned-cooling path (cool_f32.cuh)
+struct gb_cool_pf;
+
 struct gb_cool_vars {
     double ndens, rho, conf, Gflux, ephen, tdust, TtoEI, xHp, strat_factor, mu_mol;
 };

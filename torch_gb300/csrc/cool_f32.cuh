@@ -19,7 +19,16 @@ struct gb_cool_tabf {
 struct gb_cool_varsf {
     float ndens, rho, conf, Gflux, ephen, tdust, TtoEI, xHp, mu_mol;
     float cr_pref;  // strat * crIonRate * crIonEnergy / (rho / n)
-    float lnNH;     // ln(crIonNH)
+};
+
+// the runtime parameters in FP32, converted once on the host (values far
+// below FP32's range, such as 1e-99, become 0, which leaves every
+// comparison they take part in unchanged)
+struct gb_cool_pf {
+    float theatmin, theatmax, tradmin, tradmax, dradmin, dradmax, dust_sputter_temp;
+    float Gzero, pe_norm, crIonExp, crIonNH, lnNH, crRE, T_cool_min, nd_cool_min, nd_cool_max, absTmin;
+    float jeansK;  // 5/3 pi k_B / G_Newton (heatCool.F90:1687)
+    int use_cr_heating, cr_uniform, pe_recipe, useDustCool;
 };
 
 namespace gbcoolf {
@@ -77,34 +86,34 @@ __device__ __forceinline__ int find(const float* x, float x0, int N)
 
 // de/dt split into heating Gamma and cooling Lambda (as dei_parts);
 // floor_ is the cooling at the floors (state-independent per cell)
-__device__ float dei_parts(const gb_cool_params& p, const gb_cool_tabf& t, const gb_cool_varsf& v, float floor_,
+__device__ float dei_parts(const gb_cool_pf& p, const gb_cool_tabf& t, const gb_cool_varsf& v, float floor_,
                            float ei, float* gam, float* lam)
 {
     float T = ei / v.TtoEI;
     if (T < 0.0f) T = 1.0f;
     const float sqT = sqrtf(T);
     // Jeans-length column density (heatCool.F90:1669-1722)
-    const float lam_j = v.ndens / v.rho * sqrtf((float)(5.0 / 3.0 * 3.14159265358979 * (double)p.boltz / 6.6725985e-8) * T / v.ndens);
+    const float lam_j = v.ndens / v.rho * sqrtf(p.jeansK * T / v.ndens);
     const float ncol = lam_j * v.ndens;
     float eplus = 0.0f;
-    if (T <= (float)p.theatmax && T >= (float)p.theatmin) {
+    if (T <= p.theatmax && T >= p.theatmin) {
         if (p.use_cr_heating) {
-            if (p.crIonNH == 1.0 && p.crIonExp == 1.0) eplus = v.cr_pref;
-            else eplus = v.cr_pref * __expf(-(float)p.crIonExp * (__logf(fmx((float)p.crIonNH, ncol)) - v.lnNH));
+            if (p.cr_uniform) eplus = v.cr_pref;
+            else eplus = v.cr_pref * __expf(-p.crIonExp * (__logf(fmx(p.crIonNH, ncol)) - p.lnNH));
         }
-        eplus *= ramp_T(T, (float)p.theatmin, (float)p.theatmax);
+        eplus *= ramp_T(T, p.theatmin, p.theatmax);
     }
     const float fext = __expf(-3.5f * (ncol * 0.01f / 1.87e21f));
-    const float G = v.Gflux + (float)p.Gzero * fext;
+    const float G = v.Gflux + p.Gzero * fext;
     float PeHeat = 0.0f;
-    const float ulpe = fmn((float)p.theatmax, (float)p.dust_sputter_temp);
-    if (T <= ulpe && T >= (float)p.theatmin) {
+    const float ulpe = fmn(p.theatmax, p.dust_sputter_temp);
+    if (T <= ulpe && T >= p.theatmin) {
         const float xl = v.xHp == 0.0f ? 1e-8f : v.xHp;
         float eff;
         if (p.pe_recipe == 1) {
             float Gf = G * sqT / (xl * v.ndens * 0.5f);
             eff = 4.9e-2f / (1.0f + 4.0e-3f * __powf(Gf, 0.73f)) + 3.7e-2f * __powf(T * 1e-4f, 0.7f) / (1.0f + 2.0e-4f * Gf);
-            PeHeat = (float)p.pe_norm * eff * G * (v.ndens / v.rho);
+            PeHeat = p.pe_norm * eff * G * (v.ndens / v.rho);
         } else if (p.pe_recipe == 0) {
             float Gf = G * sqT / (xl * v.ndens);
             float gp = Gf > 0.0f ? __logf(Gf) : -1e30f;
@@ -113,14 +122,14 @@ __device__ float dei_parts(const gb_cool_params& p, const gb_cool_tabf& t, const
             // 1e-26 * eff * G / (rho / n), with rho/n ~ 4e-24 kept in range
             PeHeat = 1e-26f * eff * G * (v.ndens / v.rho);
         } else {
-            PeHeat = (float)p.pe_norm * 0.05f * G * (v.ndens / v.rho);
+            PeHeat = p.pe_norm * 0.05f * G * (v.ndens / v.rho);
         }
-        PeHeat *= ramp_T(T, (float)p.theatmin, ulpe);
+        PeHeat *= ramp_T(T, p.theatmin, ulpe);
     }
     eplus += v.ephen;
     // atomic cooling (heatCool.F90:1116-1200)
     float emin = 0.0f;
-    if (T <= (float)p.tradmax && T >= (float)p.tradmin && v.ndens >= (float)p.dradmin && v.ndens <= (float)p.dradmax) {
+    if (T <= p.tradmax && T >= p.tradmin && v.ndens >= p.dradmin && v.ndens <= p.dradmax) {
         emin = radloss(T);
         if (v.xHp > 1e-2f && T < 1.2e4f) {
             float DG = lin(1e-2f, 1.0f, 1e-1f, 5.0f, fmn(1e-1f, v.xHp));
@@ -134,23 +143,23 @@ __device__ float dei_parts(const gb_cool_params& p, const gb_cool_tabf& t, const
             emin *= DG;
             if (T > 9e3f) emin /= lin(9e3f, 1.0f, 1e4f, DG, T);
         }
-        emin *= ramp_T(T, (float)p.tradmin, (float)p.tradmax) * v.conf;
+        emin *= ramp_T(T, p.tradmin, p.tradmax) * v.conf;
     }
     float cool_pw = 0.0f, cool_dg = 0.0f;
     if (p.useDustCool) {
-        if (v.ndens >= (float)p.nd_cool_min && v.ndens <= (float)p.nd_cool_max && T >= (float)p.T_cool_min &&
-            T <= (float)p.theatmax) {
+        if (v.ndens >= p.nd_cool_min && v.ndens <= p.nd_cool_max && T >= p.T_cool_min &&
+            T <= p.theatmax) {
             int it = find(t.T, fmx(T, t.T_min), GB_TEMP_PTS);
             int id = find(t.n, fmx(v.ndens, t.nd_min), GB_DENS_PTS);
             if (it > 0 && it <= GB_TEMP_PTS && id > 0 && id <= GB_DENS_PTS)
                 cool_pw = __ldg(t.lam + (id - 1) + GB_DENS_PTS * (it - 1));
-            cool_pw *= ramp_T(T, (float)p.T_cool_min, (float)p.theatmax) *
-                       ramp_T(v.ndens, (float)p.nd_cool_min, (float)p.nd_cool_max);
+            cool_pw *= ramp_T(T, p.T_cool_min, p.theatmax) *
+                       ramp_T(v.ndens, p.nd_cool_min, p.nd_cool_max);
         }
-        if (T <= (float)p.dust_sputter_temp) {
+        if (T <= p.dust_sputter_temp) {
             // 3.8e-33 n^2 (...) / rho  ->  3.8e-33 n (n / rho) (...)
             cool_dg = 3.8e-33f * v.ndens * (v.ndens / v.rho) * (1.0f - 0.8f * __expf(-75.0f / T)) * (T - v.tdust) * sqT;
-            float ul = (float)p.dust_sputter_temp, ul10 = ul - 0.1f * ul;
+            float ul = p.dust_sputter_temp, ul10 = ul - 0.1f * ul;
             if (T >= ul10) cool_dg *= lin(ul10, 1.0f, ul, 0.0f, T);
         }
     }
@@ -162,16 +171,16 @@ __device__ float dei_parts(const gb_cool_params& p, const gb_cool_tabf& t, const
 // T_dust after a step (heatCool.F90:430-443 + get_dust_temperature,
 // :703-884) in FP32: dust heating by FUV photons that did not eject
 // photo-electrons plus cosmic rays, Newton on the dust energy balance
-__device__ float dust_temperature(const gb_cool_params& p, const gb_cool_varsf& v, float T, float tdust_in)
+__device__ float dust_temperature(const gb_cool_pf& p, const gb_cool_varsf& v, float T, float tdust_in)
 {
     const float sqT = sqrtf(T);
-    const float lam_j = v.ndens / v.rho * sqrtf((float)(5.0 / 3.0 * 3.14159265358979 * (double)p.boltz / 6.6725985e-8) * T / v.ndens);
+    const float lam_j = v.ndens / v.rho * sqrtf(p.jeansK * T / v.ndens);
     const float ncol = lam_j * v.ndens;
-    const float G = v.Gflux + (float)p.Gzero * __expf(-3.5f * (ncol * 0.01f / 1.87e21f));
+    const float G = v.Gflux + p.Gzero * __expf(-3.5f * (ncol * 0.01f / 1.87e21f));
     // dust heating / (n 1e-33): photo-electric remainder + CR heating * rho
     float heat = 0.0f;
-    const float ulpe = fmn((float)p.theatmax, (float)p.dust_sputter_temp);
-    if (T <= ulpe && T >= (float)p.theatmin) {
+    const float ulpe = fmn(p.theatmax, p.dust_sputter_temp);
+    if (T <= ulpe && T >= p.theatmin) {
         const float xl = v.xHp == 0.0f ? 1e-8f : v.xHp;
         float eff = 0.05f, dh;
         if (p.pe_recipe == 0) {
@@ -179,24 +188,24 @@ __device__ float dust_temperature(const gb_cool_params& p, const gb_cool_varsf& 
             float gp = Gf > 0.0f ? __logf(Gf) : -1e30f;
             eff = (7.64f + 4.52f * __expf(0.132f * __logf(T))) /
                   (1.0f + (0.04371f * __expf(0.452f * gp)) * (1.0f + 0.00557f * __expf(0.675f * gp)));
-            dh = fmx(((float)p.pe_norm * 1e26f - eff) * G * 1e7f, 0.0f);  // (pe_norm - 1e-26 eff) G n / (n 1e-33)
+            dh = fmx((p.pe_norm * 1e26f - eff) * G * 1e7f, 0.0f);  // (pe_norm - 1e-26 eff) G n / (n 1e-33)
         } else if (p.pe_recipe == 1) {
             float Gf = G * sqT / (xl * v.ndens * 0.5f);
             eff = 4.9e-2f / (1.0f + 4.0e-3f * __powf(Gf, 0.73f)) + 3.7e-2f * __powf(T * 1e-4f, 0.7f) / (1.0f + 2.0e-4f * Gf);
-            dh = (float)p.pe_norm * 1e33f * fmx(0.0f, 1.0f - eff) * G;
+            dh = p.pe_norm * 1e33f * fmx(0.0f, 1.0f - eff) * G;
         } else {
-            dh = (float)p.pe_norm * 1e33f * 0.95f * G;
+            dh = p.pe_norm * 1e33f * 0.95f * G;
         }
         heat = dh;
     }
-    if (p.use_cr_heating && T <= (float)p.theatmax && T >= (float)p.theatmin) {
+    if (p.use_cr_heating && T <= p.theatmax && T >= p.theatmin) {
         float cr = v.cr_pref;
-        if (!(p.crIonNH == 1.0 && p.crIonExp == 1.0))
-            cr *= __expf(-(float)p.crIonExp * (__logf(fmx((float)p.crIonNH, ncol)) - v.lnNH));
-        cr *= ramp_T(T, (float)p.theatmin, (float)p.theatmax);
+        if (!p.cr_uniform)
+            cr *= __expf(-p.crIonExp * (__logf(fmx(p.crIonNH, ncol)) - p.lnNH));
+        cr *= ramp_T(T, p.theatmin, p.theatmax);
         heat += cr * (v.rho / v.ndens) * 1e33f;
     }
-    const float absTmin = (float)p.absTmin;
+    const float absTmin = p.absTmin;
     float td = tdust_in < absTmin ? absTmin : tdust_in;
     const float tg = T < absTmin ? absTmin : T;
     const float cfac = 3.8f * v.ndens * (1.0f - 0.8f * __expf(-75.0f / tg)) * sqrtf(tg);
@@ -217,7 +226,7 @@ __device__ float dust_temperature(const gb_cool_params& p, const gb_cool_varsf& 
     return td < absTmin ? absTmin : td;
 }
 
-__device__ __forceinline__ void make_vars(const gb_cool_params& p, const gb_cool_vars& v, gb_cool_varsf& f)
+__device__ __forceinline__ void make_vars(const gb_cool_pf& p, const gb_cool_vars& v, gb_cool_varsf& f)
 {
     f.ndens = (float)v.ndens;
     f.rho = (float)v.rho;
@@ -228,8 +237,40 @@ __device__ __forceinline__ void make_vars(const gb_cool_params& p, const gb_cool
     f.TtoEI = (float)v.TtoEI;
     f.xHp = (float)v.xHp;
     f.mu_mol = (float)v.mu_mol;
-    f.cr_pref = (float)(v.strat_factor * p.crIonRate * p.crIonEnergy / (v.rho / v.ndens));
-    f.lnNH = (float)log(p.crIonNH);
+    f.cr_pref = p.crRE * (f.ndens / f.rho);
+}
+
+// cooling at the floors (heatCool.F90:1509-1519) in FP32
+__device__ float cooling_floor(const gb_cool_pf& p, const gb_cool_tabf& t, const gb_cool_varsf& v)
+{
+    float emin = 0.0f;
+    const float T = p.tradmin;
+    if (T <= p.tradmax && T >= p.tradmin && v.ndens >= p.dradmin && v.ndens <= p.dradmax) {
+        emin = radloss(T);
+        if (v.xHp > 1e-2f && T < 1.2e4f) {
+            float DG = lin(1e-2f, 1.0f, 1e-1f, 5.0f, fmn(1e-1f, v.xHp));
+            emin *= DG;
+            if (T > 1e4f) {
+                float q = lin(1e4f, 1.0f, 1.2e4f, sqrtf(DG), T);
+                emin /= q * q;
+            }
+        } else if (v.xHp < 1e-2f && T < 1e4f) {
+            float DG = lin(1e-4f, 0.35f, 1e-2f, 1.0f, fmx(1e-4f, v.xHp));
+            emin *= DG;
+            if (T > 9e3f) emin /= lin(9e3f, 1.0f, 1e4f, DG, T);
+        }
+        emin *= ramp_T(T, p.tradmin, p.tradmax) * v.conf;
+    }
+    float pw_ = 0.0f;
+    const float Tm = p.T_cool_min;
+    if (p.useDustCool && v.ndens >= p.nd_cool_min && v.ndens <= p.nd_cool_max && Tm >= p.T_cool_min &&
+        Tm <= p.theatmax) {
+        int it = find(t.T, fmx(Tm, t.T_min), GB_TEMP_PTS);
+        int id = find(t.n, fmx(v.ndens, t.nd_min), GB_DENS_PTS);
+        if (it > 0 && it <= GB_TEMP_PTS && id > 0 && id <= GB_DENS_PTS) pw_ = __ldg(t.lam + (id - 1) + GB_DENS_PTS * (it - 1));
+        pw_ *= ramp_T(Tm, p.T_cool_min, p.theatmax) * ramp_T(v.ndens, p.nd_cool_min, p.nd_cool_max);
+    }
+    return emin + pw_;
 }
 
 }  // namespace gbcoolf

@@ -16,6 +16,8 @@
 // the electric fields and the face-field update run in double.
 #pragma once
 
+#include <type_traits>
+
 #include "cool_dev.cuh"
 #include "gb_common.cuh"
 
@@ -33,6 +35,8 @@ constexpr int NEDGE = 16 * 17 * 17;           // edges per direction
 constexpr int NFB = 17 * 16 * 16;             // interior faces per direction
 constexpr int RECON_TILE = 32;
 
+constexpr int NP32 = 9;  // FP32 copy of the primitives: rho, vx, vy, vz, p, Bx, By, Bz, e_int
+
 // scratch sizes per block (elements)
 template <typename T>
 struct scratch_layout {
@@ -40,8 +44,34 @@ struct scratch_layout {
     static constexpr size_t flux = (size_t)3 * NFC * NFLX;    // T
     static constexpr size_t emf = (size_t)3 * NEDGE;          // double
     static constexpr size_t fb = (size_t)3 * NFB;             // double
-    static constexpr size_t bytes = recon * sizeof(T) + flux * sizeof(T) + (emf + fb) * sizeof(double);
+    // FP32 primitives of the padded block (mixed path only)
+    static constexpr size_t prim32 = std::is_same<T, float>::value ? (size_t)NP32 * GB_N3 : 0;  // float
+    static constexpr size_t bytes =
+        recon * sizeof(T) + flux * sizeof(T) + (emf + fb) * sizeof(double) + prim32 * sizeof(float);
 };
+
+// FP32 copy of the primitive variables of the padded blocks: the mixed
+// path converts each double once here instead of at every stencil read
+// (conversions issue on the FP64 pipe)
+template <bool MHD>
+__global__ void __launch_bounds__(128)
+k_prim32(gb_dev_grid g, const int* __restrict__ list, float* __restrict__ p32, size_t stride)
+{
+    const int cb = blockIdx.y;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= GB_N3) return;
+    const double* base = g.unk + (int64_t)list[cb] * g.nvar * GB_N3 + c;
+    float* out = p32 + (size_t)cb * stride + c;
+    const int roles[NP32] = {GB_DENS, GB_VELX, GB_VELY, GB_VELZ, GB_PRES, GB_MAGX, GB_MAGY, GB_MAGZ, GB_EINT};
+#pragma unroll
+    for (int v = 0; v < NP32; ++v) {
+        if (!MHD && v >= 5 && v < 8) {
+            out[(size_t)v * GB_N3] = 0.0f;
+            continue;
+        }
+        out[(size_t)v * GB_N3] = (float)base[(int64_t)g.slot[roles[v]] * GB_N3];
+    }
+}
 
 template <typename T>
 __device__ __forceinline__ T two3() { return (T)(2.0 / 3.0); }
@@ -296,12 +326,24 @@ __device__ __forceinline__ void load_w(const gb_dev_grid& g, int blk, int ci, T*
     }
 }
 
+// primitives of a cell: FP32 copy on the mixed path, the FP64 store on the plain one
+template <typename T, bool MHD>
+__device__ __forceinline__ void load_prim(const gb_dev_grid& g, int blk, int ci, const float* p32, T* w)
+{
+    if constexpr (std::is_same<T, float>::value) {
+#pragma unroll
+        for (int v = 0; v < NP; ++v) w[v] = p32[(size_t)v * GB_N3 + ci];
+    } else {
+        load_w<T, MHD>(g, blk, ci, w);
+    }
+}
+
 // ---------------------------------------------------------------- k_recon
 // blockDim = 3 * RECON_TILE: warp d reconstructs direction d for 32 cells.
 template <typename T, bool MHD>
 __global__ void __launch_bounds__(3 * RECON_TILE)
 k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __restrict__ scr,
-        size_t scr_stride, gb_status* st)
+        size_t scr_stride, const float* __restrict__ p32, size_t p32_stride, gb_status* st)
 {
     constexpr int nv = MHD ? 8 : 5;
     __shared__ T s_sig[3][NP][RECON_TILE];
@@ -326,7 +368,7 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
     for (int m = 0; m < 5; ++m) {
         int ii = i + (d == 0 ? m - 2 : 0), jj = j + (d == 1 ? m - 2 : 0), kk = k + (d == 2 ? m - 2 : 0);
         T w[NP];
-        load_w<T, MHD>(g, blk, gb_cidx(ii, jj, kk), w);
+        load_prim<T, MHD>(g, blk, gb_cidx(ii, jj, kk), p32 + (size_t)cb * p32_stride, w);
 #pragma unroll
         for (int s = 0; s < NP; ++s) qs[m][s] = w[rot_slot(d, s)];
     }
@@ -341,7 +383,7 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
         s_sig[d][v][lane] = sgr[s];
     }
     T wc[NP];
-    load_w<T, MHD>(g, blk, gb_cidx(i, j, k), wc);
+    load_prim<T, MHD>(g, blk, gb_cidx(i, j, k), p32 + (size_t)cb * p32_stride, wc);
     if (MHD) {
         // multidimensional terms (hy_uhd_dataReconstOneStep.F90:364-424)
         T uB = wc[1] * wc[5] + wc[2] * wc[6] + wc[3] * wc[7];
@@ -613,7 +655,7 @@ __device__ __forceinline__ int rc_index(int i, int j, int k)
 template <typename T, bool MHD>
 __global__ void __launch_bounds__(128)
 k_flux(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* __restrict__ rscr,
-       size_t rstride, T* __restrict__ fscr, size_t fstride)
+       size_t rstride, T* __restrict__ fscr, size_t fstride, const float* __restrict__ p32, size_t p32_stride)
 {
     const int d = blockIdx.y;
     const int cb = blockIdx.z;
@@ -656,7 +698,15 @@ k_flux(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* _
     if (kp.use_avisc) {
         const int cil = gb_cidx(Il[0], Il[1], Il[2]), cir = gb_cidx(I[0], I[1], I[2]);
         const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
-        auto U = [&](int role, int ci) -> T { return (T)base[(int64_t)g.slot[role] * GB_N3 + ci]; };
+        const float* pb = p32 + (size_t)cb * p32_stride;
+        auto U = [&](int role, int ci) -> T {
+            if constexpr (std::is_same<T, float>::value) {
+                const int v = role == GB_EINT ? 8 : (role >= GB_MAGX ? 5 + (role - GB_MAGX) : role);
+                return pb[(size_t)v * GB_N3 + ci];
+            } else {
+                return (T)base[(int64_t)g.slot[role] * GB_N3 + ci];
+            }
+        };
         T dv = U(GB_VELX + d, cir) - U(GB_VELX + d, cil);
         T vis = (T)kp.cvisc * fmax(-dv, (T)0);
         if (vis > (T)0) {

@@ -20,15 +20,23 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
     T* fscr = (T*)(base + (size_t)nblk * SL::recon * sizeof(T));
     double* escr = (double*)(base + (size_t)nblk * (SL::recon + SL::flux) * sizeof(T));
     double* bscr = escr + (size_t)nblk * SL::emf;
+    float* p32 = (float*)(bscr + (size_t)nblk * SL::fb);
     const gb_dev_grid& g = g_gb.grid;
+    if constexpr (SL::prim32 > 0) {
+        dim3 pg((GB_N3 + 127) / 128, nblk);
+        gb_prof_begin(GBP_RECON, s);
+        if (mhd) k_prim32<true><<<pg, 128, 0, s>>>(g, list, p32, SL::prim32);
+        else k_prim32<false><<<pg, 128, 0, s>>>(g, list, p32, SL::prim32);
+        gb_prof_end(GBP_RECON, s);
+    }
     dim3 rg((NRC + RECON_TILE - 1) / RECON_TILE, nblk);
     dim3 fg((NFC + 127) / 128, 3, nblk);
     if (mhd) {
         gb_prof_begin(GBP_RECON, s);
-        k_recon<T, true><<<rg, 3 * RECON_TILE, 0, s>>>(g, kp, list, rscr, SL::recon, st);
+        k_recon<T, true><<<rg, 3 * RECON_TILE, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
         gb_prof_end(GBP_RECON, s);
         gb_prof_begin(GBP_FLUX, s);
-        k_flux<T, true><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux);
+        k_flux<T, true><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);
         gb_prof_end(GBP_FLUX, s);
         dim3 eg((NEDGE + 127) / 128, 3, nblk);
         gb_prof_begin(GBP_EMF, s);
@@ -40,10 +48,10 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
         gb_prof_end(GBP_FACEB, s);
     } else {
         gb_prof_begin(GBP_RECON, s);
-        k_recon<T, false><<<rg, 3 * RECON_TILE, 0, s>>>(g, kp, list, rscr, SL::recon, st);
+        k_recon<T, false><<<rg, 3 * RECON_TILE, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
         gb_prof_end(GBP_RECON, s);
         gb_prof_begin(GBP_FLUX, s);
-        k_flux<T, false><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux);
+        k_flux<T, false><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);
         gb_prof_end(GBP_FLUX, s);
     }
     dim3 ug((GB_NXB * GB_NXB * GB_NXB + 127) / 128, nblk);
