@@ -253,9 +253,12 @@ int gb_surrogate_samples(int64_t n, uint64_t seed, float* feat_dev, float* targe
                          void* stream);
 /* Cooling mode of gb_evolve_step(cool = 1): 0 = plain integrator fused in
  * the update, 1 = surrogate with per-cell acceptance test and plain
- * fallback. rel_tol: accepted relative change of e_int per the Newton
- * estimate of the backward-Euler residual. */
-int gb_set_cooling_mode(int mode, double rel_tol);
+ * fallback. The network's prediction starts at most four FP32 secant-Newton
+ * iterations on the backward-Euler residual; a cell is accepted when a
+ * correction below rel_tol * e came from a local slope and the energy
+ * moved the way the initial rate points. check_fp64 = 1 re-evaluates the
+ * residual in FP64 at the converged state before accepting. */
+int gb_set_cooling_mode(int mode, double rel_tol, int check_fp64);
 
 /* ---------------------------------------------------------------- profiling */
 /* Per-kernel CUDA-event timing on the launching stream (no counterpart in

@@ -69,7 +69,8 @@ def _cooling_grid(gb, seed=9):
     return g, units
 
 
-def test_inline_surrogate_accuracy_and_gain(gb, trained):
+@pytest.mark.parametrize("check64", [False, True])
+def test_inline_surrogate_accuracy_and_gain(gb, trained, check64):
     """One hydro + cooling step with the surrogate (acceptance test +
     plain fallback) against the plain integrator: cooled temperatures
     within 1 % of the plain integrator, and the surrogate path is faster."""
@@ -81,7 +82,7 @@ def test_inline_surrogate_accuracy_and_gain(gb, trained):
     out, times, stats = {}, {}, {}
     for mode in (0, 1):
         g, _ = _cooling_grid(gb)
-        gb.set_cooling_mode(bool(mode))
+        gb.set_cooling_mode(bool(mode), check_fp64=check64)
         dt = g.compute_dt().item() * 20.0  # a long step: stiff cooling in many cells
         g.evolve_step(dt, cool=True)  # warm-up on a copy of the state
         g2, _ = _cooling_grid(gb)

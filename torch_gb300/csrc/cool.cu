@@ -421,6 +421,7 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double g
 // slope (its two points within 5 % of each other) and the energy moved
 // the way the rate at the old state points; otherwise it goes to the
 // fallback list and the plain integrator solves it.
+template <bool CHECK64>
 __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double gamma, const int* __restrict__ list,
                              int64_t ncell, double dt_code, const float* __restrict__ y, const float2* __restrict__ f0a,
                              double rel_tol, int* __restrict__ rej, int* __restrict__ nrej, gb_status* st)
@@ -469,16 +470,18 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double
                 break;
             }
         }
-        // FP64 check of the backward-Euler residual (heatCool.F90:1928-1950)
-        // at the converged state, with the last secant slope
-        if (conv) {
+        // the converged FP32 iterate is the answer; optionally re-check the
+        // backward-Euler residual (heatCool.F90:1928-1950) in FP64 with the
+        // last secant slope
+        if (conv && CHECK64) {
             double f64 = dei_dt(c, v, cooling_floor(c, v), eb);
             double g64 = eb - dt * f64 - ei0;
             double delta = g64 / J;
             ein = eb - delta;
             ok = isfinite(ein) && ein > 0.0 && fabs(delta) <= rel_tol * ein;
         } else {
-            ok = false;
+            ein = eb;
+            ok = conv && isfinite(ein) && ein > 0.0;
         }
         // the solution moves the way the rate at the old state points
         if (ok && f0 < 0.0 && ein > ei0 * (1.0 + rel_tol)) ok = false;
@@ -537,6 +540,7 @@ __global__ void k_sur_fallback(gb_dev_grid g, gb_cool_ctx c, double gamma, const
 
 int g_cool_mode = 0;
 double g_sur_tol = 2e-3;
+int g_sur_check64 = 0;
 struct sur_bufs {
     float* feat = nullptr;
     float* y = nullptr;
@@ -611,8 +615,12 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, gb_status* st, cud
     if (rc) return rc;
     cudaMemsetAsync(g_sb.nrej, 0, sizeof(int), s);
     gb_prof_begin(GBP_SUR_ACCEPT, s);
-    k_sur_accept<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, g_sb.y, g_sb.f0,
-                                    g_sur_tol, g_sb.rej, g_sb.nrej, st);
+    if (g_sur_check64)
+        k_sur_accept<true><<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, g_sb.y, g_sb.f0,
+                                              g_sur_tol, g_sb.rej, g_sb.nrej, st);
+    else
+        k_sur_accept<false><<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, g_sb.y, g_sb.f0,
+                                               g_sur_tol, g_sb.rej, g_sb.nrej, st);
     gb_prof_end(GBP_SUR_ACCEPT, s);
     gb_prof_begin(GBP_SUR_FALLBACK, s);
     k_sur_fallback<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, dt, g_sb.rej, g_sb.nrej, st);
@@ -620,11 +628,12 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, gb_status* st, cud
     return gb_check(cudaGetLastError(), "surrogate launch") ? GB_ERR_CUDA : GB_OK;
 }
 
-extern "C" int gb_set_cooling_mode(int mode, double rel_tol)
+extern "C" int gb_set_cooling_mode(int mode, double rel_tol, int check_fp64)
 {
     if (mode < 0 || mode > 1 || !(rel_tol > 0.0) || rel_tol > 0.5) return GB_ERR_ARG;
     g_cool_mode = mode;
     g_sur_tol = rel_tol;
+    g_sur_check64 = check_fp64 ? 1 : 0;
     return GB_OK;
 }
 

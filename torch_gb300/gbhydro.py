@@ -117,7 +117,7 @@ _SIG = {
                                C.c_void_p, C.c_void_p]),
     "gb_mlp_infer": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "gb_surrogate_samples": (C.c_int, [C.c_int64, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
-    "gb_set_cooling_mode": (C.c_int, [C.c_int, C.c_double]),
+    "gb_set_cooling_mode": (C.c_int, [C.c_int, C.c_double, C.c_int]),
     "gb_prof_enable": (C.c_int, [C.c_int]),
     "gb_prof_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "gb_last_error": (C.c_char_p, []),
@@ -431,8 +431,8 @@ def mlp_infer(feat, tensor_cores: bool = True):
     return y
 
 
-def set_cooling_mode(surrogate: bool, rel_tol: float = 2e-3):
-    check(lib().gb_set_cooling_mode(int(surrogate), rel_tol), "gb_set_cooling_mode")
+def set_cooling_mode(surrogate: bool, rel_tol: float = 2e-3, check_fp64: bool = False):
+    check(lib().gb_set_cooling_mode(int(surrogate), rel_tol, int(check_fp64)), "gb_set_cooling_mode")
 
 
 PROF_NAMES = ["guard_fill", "recon", "flux", "emf", "faceb", "update", "dt", "heat", "sur_feat", "mlp_infer",
