@@ -998,3 +998,131 @@ void orc_test_eig(int mhd, double gam, const double* q8, double* lam, double* Ro
     memcpy(Rout, R, sizeof R);
     memcpy(Lout, L, sizeof L);
 }
+
+/* ------------------------------------------------------------ AMR guard fill */
+
+static int orc_leaf_at(const int* level, const int* child, const int* root, int nr0, int nr1, int maxlevel,
+                       long long X, long long Y, long long Z)
+{
+    const long long S0 = 16LL << maxlevel;
+    long long r[3] = {X / S0, Y / S0, Z / S0};
+    int node = root[r[0] + nr0 * (r[1] + nr1 * r[2])];
+    for (int l = 0; l <= maxlevel; ++l) {
+        if (child[8 * node] < 0) break;
+        long long half = S0 >> (l + 1);
+        int c = (int)((X / half) & 1) | ((int)((Y / half) & 1) << 1) | ((int)((Z / half) & 1) << 2);
+        node = child[8 * node + c];
+    }
+    (void)level;
+    return node;
+}
+
+static long long orc_wrap(long long x, long long n) { return ((x % n) + n) % n; }
+
+/* Guard cells and guard faces of every leaf of a block tree (periodic
+ * domain): same-level neighbours are copied, a coarser neighbour's covering
+ * cell is injected, a finer neighbour's covering cells are averaged
+ * (8 cells; faces: the 4 fine faces on the coarse face); a fine guard face
+ * that falls inside a coarse cell takes the mean of the two coarse faces. */
+void orc_fill_guards_tree(const orc_hydro_params* p, int nnodes, const int* level, const int* coord,
+                          const int* child, const int* root, int nr0, int nr1, int nr2, int maxlevel,
+                          double* u, double* bx, double* by, double* bz)
+{
+    const int ng = p->nguard, nxb = p->nxb, n = nxb + 2 * ng;
+    const int64_t n3 = (int64_t)n * n * n, fsz = n3 + (int64_t)n * n;
+    const int nv = p->mhd ? ORV_NVAR : ORV_MAGX;
+    const long long N[3] = {(long long)nr0 * nxb << maxlevel, (long long)nr1 * nxb << maxlevel,
+                            (long long)nr2 * nxb << maxlevel};
+    double* fa[3] = {bx, by, bz};
+    for (int b = 0; b < nnodes; ++b) {
+        if (child[8 * b] >= 0) continue;
+        const int L = level[b];
+        const long long s = 1LL << (maxlevel - L);
+        const int* cd = coord + 3 * b;
+        for (int k = 0; k < n; ++k)
+            for (int j = 0; j < n; ++j)
+                for (int i = 0; i < n; ++i) {
+                    int l3[3] = {i, j, k};
+                    int guard = 0;
+                    for (int d = 0; d < 3; ++d) if (l3[d] < ng || l3[d] >= ng + nxb) guard = 1;
+                    if (!guard) continue;
+                    long long lo[3], X[3];
+                    for (int d = 0; d < 3; ++d) {
+                        lo[d] = orc_wrap(((long long)cd[d] * nxb + l3[d] - ng) * s, N[d]);
+                        X[d] = lo[d] + s / 2;
+                    }
+                    int m = orc_leaf_at(level, child, root, nr0, nr1, maxlevel, X[0], X[1], X[2]);
+                    const long long sl = 1LL << (maxlevel - level[m]);
+                    const int* sc = coord + 3 * m;
+                    double* dst = u + (int64_t)b * ORV_NVAR * n3 + cidx(n, i, j, k);
+                    const double* src = u + (int64_t)m * ORV_NVAR * n3;
+                    if (level[m] <= L) {
+                        int si = (int)(X[0] / sl - (long long)sc[0] * nxb) + ng;
+                        int sj = (int)(X[1] / sl - (long long)sc[1] * nxb) + ng;
+                        int sk = (int)(X[2] / sl - (long long)sc[2] * nxb) + ng;
+                        for (int v = 0; v < nv; ++v) dst[v * n3] = src[v * n3 + cidx(n, si, sj, sk)];
+                    } else {
+                        int r = (int)(s / sl);
+                        int bi = (int)(lo[0] / sl - (long long)sc[0] * nxb) + ng;
+                        int bj = (int)(lo[1] / sl - (long long)sc[1] * nxb) + ng;
+                        int bk = (int)(lo[2] / sl - (long long)sc[2] * nxb) + ng;
+                        double inv = 1.0 / (double)(r * r * r);
+                        for (int v = 0; v < nv; ++v) {
+                            double acc = 0.0;
+                            for (int z = 0; z < r; ++z)
+                                for (int y = 0; y < r; ++y)
+                                    for (int x = 0; x < r; ++x) acc += src[v * n3 + cidx(n, bi + x, bj + y, bk + z)];
+                            dst[v * n3] = acc * inv;
+                        }
+                    }
+                }
+        if (!p->mhd) continue;
+        for (int a = 0; a < 3; ++a)
+            for (int k = 0; k < n + (a == 2); ++k)
+                for (int j = 0; j < n + (a == 1); ++j)
+                    for (int i = 0; i < n + (a == 0); ++i) {
+                        int I[3] = {i, j, k};
+                        int own = 1;
+                        for (int e = 0; e < 3; ++e) {
+                            int top = ng + nxb - 1 + (e == a);
+                            if (I[e] < ng || I[e] > top) own = 0;
+                        }
+                        if (own) continue;
+                        long long lo[3], X[3];
+                        for (int d = 0; d < 3; ++d) {
+                            lo[d] = orc_wrap(((long long)cd[d] * nxb + I[d] - ng) * s, N[d]);
+                            X[d] = lo[d] + (d == a ? 0 : s / 2);
+                        }
+                        int m = orc_leaf_at(level, child, root, nr0, nr1, maxlevel, X[0], X[1], X[2]);
+                        const long long sl = 1LL << (maxlevel - level[m]);
+                        const int* sc = coord + 3 * m;
+                        const double* src = fa[a] + (int64_t)m * fsz;
+                        double* dst = fa[a] + (int64_t)b * fsz + fidx(n, a, i, j, k);
+                        if (level[m] <= L) {
+                            int S[3];
+                            for (int d = 0; d < 3; ++d) S[d] = (int)(X[d] / sl - (long long)sc[d] * nxb) + ng;
+                            if (X[a] % sl == 0) {
+                                *dst = src[fidx(n, a, S[0], S[1], S[2])];
+                            } else {
+                                int S1[3] = {S[0], S[1], S[2]};
+                                S1[a] += 1;
+                                *dst = 0.5 * (src[fidx(n, a, S[0], S[1], S[2])] + src[fidx(n, a, S1[0], S1[1], S1[2])]);
+                            }
+                        } else {
+                            int r = (int)(s / sl);
+                            int B[3];
+                            for (int d = 0; d < 3; ++d) B[d] = (int)(lo[d] / sl - (long long)sc[d] * nxb) + ng;
+                            int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+                            double acc = 0.0;
+                            for (int y = 0; y < r; ++y)
+                                for (int x = 0; x < r; ++x) {
+                                    int Q[3] = {B[0], B[1], B[2]};
+                                    Q[t1] += x;
+                                    Q[t2] += y;
+                                    acc += src[fidx(n, a, Q[0], Q[1], Q[2])];
+                                }
+                            *dst = acc / (double)(r * r);
+                        }
+                    }
+    }
+}

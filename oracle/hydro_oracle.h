@@ -60,6 +60,14 @@ double orc_block_dt_limit(const orc_hydro_params* p, const double* u, double dx,
 void orc_fill_guards_periodic(const orc_hydro_params* p, int nbx, int nby, int nbz, double* u,
                               double* bx, double* by, double* bz);
 
+/* Guard cells and faces of every leaf of a block tree (gb_tree_desc
+ * arrays; node id = store block id): copy from a same-level neighbour,
+ * injection from a coarser one, 8-cell (face: 4-face) mean from a finer
+ * one, mean of two coarse faces for a fine face inside a coarse cell. */
+void orc_fill_guards_tree(const orc_hydro_params* p, int nnodes, const int* level, const int* coord,
+                          const int* child, const int* root, int nr0, int nr1, int nr2, int maxlevel,
+                          double* u, double* bx, double* by, double* bz);
+
 /* Total mass, momentum, energy (E incl. magnetic) and max |div B| over the
  * interior of a uniform grid. out[0..4] = M, Px, Py, Pz, E; out[5] = max
  * |divB| * dx / max|B|. */

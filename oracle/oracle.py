@@ -109,6 +109,8 @@ def lib():
         L.orc_conserved_totals.argtypes = [C.POINTER(HydroParams), C.c_int, optd, optd, optd,
                                            optd, C.c_double, C.c_double, C.c_double, dp]
         L.orc_test_eig.argtypes = [C.c_int, C.c_double, dp, dp, dp, dp]
+        L.orc_fill_guards_tree.argtypes = [C.POINTER(HydroParams), C.c_int, optd, optd, optd, optd, C.c_int,
+                                           C.c_int, C.c_int, C.c_int, optd, optd, optd, optd]
         L.orc_num_threads.restype = C.c_int
         L.orc_set_num_threads.argtypes = [C.c_int]
         _lib = L
@@ -178,6 +180,15 @@ def unsplit_blocks(p: HydroParams, u, bx, by, bz, dt, dx, dy, dz, threads: int |
 
 def fill_guards_periodic(p: HydroParams, nbx, nby, nbz, u, bx=None, by=None, bz=None):
     lib().orc_fill_guards_periodic(C.byref(p), nbx, nby, nbz, _p(u), _p(bx), _p(by), _p(bz))
+
+
+def fill_guards_tree(p: HydroParams, tree: dict, u, bx=None, by=None, bz=None):
+    """AMR guard fill over a torch_gb300.amr tree dict."""
+    a = {k: np.ascontiguousarray(tree[k], np.int32) for k in ("level", "coord", "child", "root")}
+    nr = tree["nr"]
+    lib().orc_fill_guards_tree(C.byref(p), len(a["level"]), _p(a["level"]), _p(a["coord"]), _p(a["child"]),
+                               _p(a["root"]), nr[0], nr[1], nr[2], int(tree["maxlevel"]), _p(u), _p(bx),
+                               _p(by), _p(bz))
 
 
 def dt_limit(p: HydroParams, u, dx, dy, dz) -> float:

@@ -449,3 +449,24 @@ def prof_read() -> dict:
     cnt = np.zeros(n, np.int64)
     check(lib().gb_prof_read(ms.ctypes.data_as(C.c_void_p), cnt.ctypes.data_as(C.c_void_p), n), "gb_prof_read")
     return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(PROF_NAMES) if cnt[i]}
+
+
+def grid_from_amr(tree: dict, state: dict, mhd: bool = True, cooling: bool = True, device: str = "cuda") -> Grid:
+    """Registered Grid over an amr.build_tree tree with an amr.amr_box state."""
+    slots = {n: i for i, n in enumerate(["DENS", "VELX", "VELY", "VELZ", "PRES", "ENER", "EINT"])}
+    nvar = 7
+    if mhd:
+        slots.update(MAGX=7, MAGY=8, MAGZ=9)
+        nvar = 10
+    if cooling:
+        slots.update(TEMP=nvar, TDUS=nvar + 1)
+        nvar += 2
+    nn = len(tree["level"])
+    g = Grid(nn, nvar, slots, mhd, tree, state["root_dx"], device)
+    k = 10 if mhd else 7
+    g.u[:, :k] = state["u"][:, :k].to(device)
+    if mhd:
+        g.fx.copy_(state["fx"])
+        g.fy.copy_(state["fy"])
+        g.fz.copy_(state["fz"])
+    return g
