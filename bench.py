@@ -28,8 +28,38 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = dict(name="mhd_turbbox_128cubed_cooling", nbx=8, nby=8, nbz=8, seed=44, sigma_ln=1.0,
-                mach=5.0, beta=1.0, dA=0.1)
+WORKLOADS = {
+    # 4101 leaf blocks over levels 0-3 (2057 / 1020 / 768 / 256) of a 13^3-root
+    # periodic tree refined around 8 seeded Gaussian overdensities (contrast
+    # 100, FWHM 4 finest cells): 16.8 M zones, 256^3-equivalent
+    "amr": dict(name="amr_mhd_4101_leaf_blocks_cooling", kind="amr", tree_seed=45, ic_seed=46, sigma_ln=1.0,
+                mach=5.0, beta=1.0, dA=0.1, contrast=100.0, fwhm_cells=4.0, cpu_stride=4),
+    # 8^3 blocks = 128^3 uniform periodic box
+    "box128": dict(name="mhd_turbbox_128cubed_cooling", kind="box", nbx=8, nby=8, nbz=8, seed=44, sigma_ln=1.0,
+                   mach=5.0, beta=1.0, dA=0.1, cpu_stride=1),
+}
+TDUST0 = 18.0  # initial dust temperature [K] (sim_tdust, flash.par.turbsph_standard:19)
+
+
+def build_workload(wl, device):
+    """(tree, state) of a workload: state = dict(u, fx, fy, fz, root_dx) with
+    u[nnodes, 10, 24, 24, 24] (hydro + cell B) and face B, torch FP64."""
+    import torch
+    from torch_gb300 import amr
+    from torch_gb300 import gbhydro as G
+    from torch_gb300 import workloads as W
+    if wl["kind"] == "amr":
+        tree, centres = amr.config3_tree(wl["tree_seed"])
+        st = amr.amr_box(tree, centres, seed=wl["ic_seed"], sigma_ln=wl["sigma_ln"], mach=wl["mach"],
+                         beta=wl["beta"], dA=wl["dA"], contrast=wl["contrast"], fwhm_cells=wl["fwhm_cells"],
+                         nvar=10, device=device)
+        return tree, st
+    ic = W.turbulent_box(wl["nbx"], wl["nby"], wl["nbz"], seed=wl["seed"], sigma_ln=wl["sigma_ln"],
+                         mach=wl["mach"], mhd=True, beta=wl["beta"], dA=wl["dA"], nvar=10)
+    tree = G.uniform_tree(wl["nbx"], wl["nby"], wl["nbz"])
+    st = {k: torch.as_tensor(ic[k], device=device) for k in ("u", "fx", "fy", "fz")}
+    st["root_dx"] = ic["dx"]
+    return tree, st
 
 
 def peaks():
@@ -82,15 +112,15 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def make_grid(G, ic, precision, cooling=True):
-    g = G.grid_from_workload(ic, mhd=True, cooling=cooling)
+def make_grid(G, tree, st, cooling=True):
+    g = G.grid_from_amr(tree, st, mhd=True, cooling=cooling)
     units = G.code_units()
     gm1 = 2.0 / 3.0
     if cooling:
-        e = g.u[:, 6]
+        e = g.u[:, g.slots["EINT"]]
         g.u[:, g.slots["TEMP"]] = e * units["vel_unit"] ** 2 * gm1 * (24.0 / 11.0) * G.MP / G.KB
-        g.u[:, g.slots["TDUS"]] = 15.0
-    return g, units
+        g.u[:, g.slots["TDUS"]] = TDUST0
+    return g
 
 
 def run_path(G, g, precision, steps, warmup, cool=True, surrogate=False, profile=False, ncu_range=False):
@@ -124,68 +154,73 @@ def run_path(G, g, precision, steps, warmup, cool=True, surrogate=False, profile
     return e0.elapsed_time(e1) / steps, g.status_read(), prof
 
 
-def cpu_baseline(ic=None, steps=1):
-    """The oracle (C port of the reference's algorithm, OpenMP over blocks,
-    all host cores) on the same workload: `steps` full steps of the 512-block
-    MHD + cooling box (guard fill, dt, unsplit MHD, per-cell cooling)."""
-    from oracle import oracle as O
-    from torch_gb300 import gbhydro as G
-    from torch_gb300 import tables
-    from torch_gb300 import workloads as W
-    O.build()
-    wl = WORKLOAD
-    if ic is None:
-        ic = W.turbulent_box(wl["nbx"], wl["nby"], wl["nbz"], seed=wl["seed"], sigma_ln=wl["sigma_ln"],
-                             mach=wl["mach"], mhd=True, beta=wl["beta"], dA=wl["dA"], nvar=10)
-    nb = (wl["nbx"], wl["nby"], wl["nbz"])
-    p = O.hydro_params(True)
-    u, fx, fy, fz = ic["u"].copy(), ic["fx"].copy(), ic["fy"].copy(), ic["fz"].copy()
-    dx = ic["dx"]
-    units = G.code_units()
-    cp = O.cool_params()
-    tab = O.table_from_ilog(*tables.read_compact())
-    nthreads = O.lib().orc_num_threads()
-    sl = (slice(None), slice(4, 20), slice(4, 20), slice(4, 20))
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        O.fill_guards_periodic(p, *nb, u, fx, fy, fz)
-        dt = 0.8 * O.dt_limit(p, u, dx, dx, dx)
-        O.unsplit_blocks(p, u, fx, fy, fz, dt, dx, dx, dx)
-        rho = np.ascontiguousarray(u[:, 0][sl] * units["dens_unit"]).ravel()
-        ei = np.ascontiguousarray(u[:, 6][sl] * units["vel_unit"] ** 2).ravel()
+class CpuStep:
+    """The oracle (C restatement of the reference's algorithm, OpenMP over
+    leaf blocks, all host cores) on a fixed sample of the workload's leaves:
+    one step = guard fill of the sampled leaves, CFL limit over them, one
+    unsplit MHD step of each (cell size per level), implicit heating/cooling
+    of their interior cells."""
+
+    def __init__(self, wl, tree, st):
+        from oracle import oracle as O
+        from torch_gb300 import gbhydro as G
+        from torch_gb300 import tables
+        O.build()
+        self.O, self.G = O, G
+        self.p = O.hydro_params(True)
+        self.tl = O.TreeLists(tree)
+        self.sample = np.ascontiguousarray(tree["leaf"][::wl["cpu_stride"]], np.int32)
+        self.u = np.ascontiguousarray(st["u"][:, :10].cpu().numpy())
+        self.f = [np.ascontiguousarray(st[k].cpu().numpy()) for k in ("fx", "fy", "fz")]
+        self.root_dx = st["root_dx"]
+        self.units = G.code_units()
+        self.cp = O.cool_params()
+        self.tab = O.table_from_ilog(*tables.read_compact())
+        self.cores = int(O.lib().orc_num_threads())
+        self.zones = len(self.sample) * 4096
+        self.desc = (f"{len(self.sample)} of {len(tree['leaf'])} leaf blocks (every {wl['cpu_stride']}th leaf, "
+                     f"all levels) of the {wl['name']} workload")
+
+    def step(self):
+        O, G, u, (fx, fy, fz) = self.O, self.G, self.u, self.f
+        sl = (self.sample[:, None, None, None], slice(4, 20), slice(4, 20), slice(4, 20))
+        t0 = time.perf_counter()
+        O.fill_guards_list(self.p, self.tl, self.sample, u, fx, fy, fz)
+        dt = 0.8 * O.dt_limit_list(self.p, self.tl, self.sample, u, self.root_dx)
+        O.unsplit_list(self.p, self.tl, self.sample, u, fx, fy, fz, dt, self.root_dx)
+        rho = np.ascontiguousarray(u[:, 0][sl] * self.units["dens_unit"]).ravel()
+        ei = np.ascontiguousarray(u[:, 6][sl] * self.units["vel_unit"] ** 2).ravel()
         T = ei * (2.0 / 3.0) * (24.0 / 11.0) * G.MP / G.KB
-        td = np.full_like(T, 15.0)
-        O.radheat_cells(cp, tab, dt * units["time_unit"], rho, ei.copy(), ei, T, td)
-    el = time.perf_counter() - t0
-    zones = int(np.prod(nb)) * 4096 * steps
-    return {"value": zones / el, "unit": "zone-updates/s", "cores": int(nthreads), "kind": "port",
-            "sample": f"{steps} full step(s) of the {int(np.prod(nb))}-block MHD+cooling workload on the oracle "
-                      f"(C port, OpenMP over blocks), {el:.2f} s"}
+        td = np.full_like(T, TDUST0)
+        O.radheat_cells(self.cp, self.tab, dt * self.units["time_unit"], rho, ei.copy(), ei, T, td)
+        return time.perf_counter() - t0
+
+
+def cpu_baseline(cs: CpuStep, steps=1):
+    el = sum(cs.step() for _ in range(steps))
+    return {"value": cs.zones * steps / el, "unit": "zone-updates/s", "cores": cs.cores, "kind": "port",
+            "sample": f"{steps} step(s) of {cs.desc} on the oracle (C port, OpenMP over blocks), {el:.2f} s"}
 
 
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    steps = max(1, args.steps)
-    vals = []
-    cb = None
-    from torch_gb300 import workloads as W
-    wl = WORKLOAD
-    ic = W.turbulent_box(wl["nbx"], wl["nby"], wl["nbz"], seed=wl["seed"], sigma_ln=wl["sigma_ln"],
-                         mach=wl["mach"], mhd=True, beta=wl["beta"], dA=wl["dA"], nvar=10)
-    for _ in range(min(args.warmup, 1)):
-        cpu_baseline(ic, 1)
-    for _ in range(steps):
-        cb = cpu_baseline(ic, 1)
-        vals.append(cb["value"])
-    v = float(np.median(vals))
-    cb["value"] = v
+    wl = WORKLOADS[args.workload]
+    tree, st = build_workload(wl, "cpu")
+    cs = CpuStep(wl, tree, st)
+    del st
+    for _ in range(args.warmup):
+        cs.step()
+    times = [cs.step() for _ in range(max(1, args.steps))]
+    v = cs.zones * len(times) / sum(times)
     line = {"metric": "zone-updates/s", "value": v, "unit": "zone-updates/s", "n_gpus": args.gpus,
-            "steps": steps, "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
-            "dtype": "f64", "data": "synthetic", "scaling": "weak", "vs_baseline": None,
-            "config": {"workload": WORKLOAD["name"], "blocks": 512},
-            "cpu_baseline": cb,
+            "steps": len(times), "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "impl": "reference", "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None,
+            "config": {"workload": wl["name"], "sampled_blocks": len(cs.sample), "block": "16^3+4gc"},
+            "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": cs.cores, "kind": "port",
+                             "sample": cs.desc + " per step"},
             "e2e": {"value": v, "unit": "zone-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "FLASH 4.6.2 (the reference's hydro) is not in the reference tree and no Fortran "
                     "compiler exists here; the timed reference is the oracle's C restatement of the "
@@ -194,35 +229,45 @@ def reference_arm(args):
 
 
 def e2e_run(G, g, steps, warmup):
-    """Fast path through the C ABI with host FLASH-layout (variable-fastest)
-    pinned buffers uploaded before and downloaded after every step."""
+    """Fast path through the C ABI as a FLASH host would drive it: the host
+    owns unk (FLASH order, variable fastest) and facevar{x,y,z} in pinned
+    memory; every step uploads the leaf blocks, computes dt, runs the step
+    and downloads the leaf blocks."""
     import ctypes as C
     import torch
-    nunk = g.nvar
-    nb3 = 24 * 24 * 24
-    host = torch.empty((g.nblocks, nb3, nunk), dtype=torch.float64).pin_memory()
-    host.copy_(g.u.reshape(g.nblocks, nunk, nb3).transpose(1, 2).cpu())
+    G.init_hydro(G.hydro_params(True, precision=1))
+    g.register()
+    nunk, nn = g.nvar, g.nblocks
+    host = torch.empty((nn, 24 ** 3, nunk), dtype=torch.float64).pin_memory()
+    hf = [torch.empty(a.shape, dtype=torch.float64).pin_memory() for a in (g.fx, g.fy, g.fz)]
     hslot = (C.c_int * G.NROLE)(*([-1] * G.NROLE))
     for name, s in g.slots.items():
         hslot[G.R[name]] = s
     L = G.lib()
     st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    lt, n = g.list_tensor()
-
+    G.check(L.gb_grid_download_flash(C.c_void_p(host.data_ptr()), nunk, hslot, nn, st), "init")
+    for h, d in zip(hf, (g.fx, g.fy, g.fz)):
+        h.copy_(d.cpu())
+    leaves = np.ascontiguousarray(g.leaf, np.int32)
+    lp, nl = leaves.ctypes.data_as(C.c_void_p), len(leaves)
+    hp = C.c_void_p(host.data_ptr())
+    fp = [C.c_void_p(h.data_ptr()) for h in hf]
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     parts = np.zeros(3)
 
     def one(timed=False):
         if timed:
             ev[0].record()
-        G.check(L.gb_grid_upload_flash(C.c_void_p(host.data_ptr()), nunk, hslot, g.nblocks, st), "upload")
+        G.check(L.gb_grid_upload_flash_list(hp, nunk, hslot, nl, lp, st), "upload")
+        G.check(L.gb_grid_upload_faces_list(*fp, nl, lp, st), "upload faces")
         if timed:
             ev[1].record()
         dt = g.compute_dt().item()
         g.evolve_step(dt, cool=True)
         if timed:
             ev[2].record()
-        G.check(L.gb_grid_download_flash(C.c_void_p(host.data_ptr()), nunk, hslot, g.nblocks, st), "download")
+        G.check(L.gb_grid_download_flash_list(hp, nunk, hslot, nl, lp, st), "download")
+        G.check(L.gb_grid_download_faces_list(*fp, nl, lp, st), "download faces")
         if timed:
             ev[3].record()
             torch.cuda.synchronize()
@@ -232,7 +277,6 @@ def e2e_run(G, g, steps, warmup):
     for _ in range(warmup):
         one()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record()
     for _ in range(steps):
@@ -240,9 +284,15 @@ def e2e_run(G, g, steps, warmup):
     b.record()
     torch.cuda.synchronize()
     ms = a.elapsed_time(b) / steps
-    nbytes = host.numel() * 8
+    nbytes = nl * (24 ** 3 * nunk + 3 * 24 * 24 * 25) * 8
     one(timed=True)
     return ms, nbytes, {"upload_ms": parts[0], "step_ms": parts[1], "download_ms": parts[2]}
+
+
+def l1(a, b, leaves, v):
+    x = a[leaves, v, 4:20, 4:20, 4:20]
+    y = b[leaves, v, 4:20, 4:20, 4:20]
+    return float((x - y).abs().sum() / x.abs().sum())
 
 
 def main():
@@ -251,6 +301,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb")
+    ap.add_argument("--workload", default="amr", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--weights", default=None, help="load surrogate weights (.npy) instead of training")
     ap.add_argument("--save-weights", default=None)
@@ -267,19 +318,19 @@ def main():
         dist.init_process_group("nccl")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     from torch_gb300 import gbhydro as G
-    from torch_gb300 import workloads as W
-    wl = WORKLOAD
+    wl = WORKLOADS[args.workload]
     # replicas: every rank runs its own copy of the workload (the step has no
     # cross-GPU exchange on one-GPU machines)
-    ic = W.turbulent_box(wl["nbx"], wl["nby"], wl["nbz"], seed=wl["seed"], sigma_ln=wl["sigma_ln"],
-                         mach=wl["mach"], mhd=True, beta=wl["beta"], dA=wl["dA"], nvar=10)
+    t0 = time.perf_counter()
+    tree, st = build_workload(wl, "cuda")
+    t_ic = time.perf_counter() - t0
+    leaves = tree["leaf"]
+    zones = len(leaves) * 4096
     units = G.code_units()
-    G.init_cooling(G.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
-                                 time_unit=units["time_unit"]))
-    zones = wl["nbx"] * wl["nby"] * wl["nbz"] * 4096
     # learned cooling: 1e7 samples from the plain integrator, then training
     # (outside the timed region; reported)
     if args.weights:
+        G.init_cooling(G.cool_params())
         G.mlp_init(7)
         G.mlp_set_weights(np.load(args.weights))
         t_samples = t_train = 0.0
@@ -301,9 +352,13 @@ def main():
         np.save(args.save_weights, G.mlp_weights())
     G.init_cooling(G.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
                                  time_unit=units["time_unit"]))
-    g_plain, _ = make_grid(G, ic, 0)
-    g_fast, _ = make_grid(G, ic, 1)
-    g_mixed, _ = make_grid(G, ic, 1)
+    g_plain = make_grid(G, tree, st)
+    g_fast = make_grid(G, tree, st)
+    g_mixed = make_grid(G, tree, st)
+    cs = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cs = CpuStep(wl, tree, st)
+    del st
     os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
     clk = ClockSampler(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv"))
     if world > 1:
@@ -318,49 +373,51 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_plain, ms_fast = t.tolist()
     # accuracy of the fast path against the plain one after the same steps
-    a, b = g_plain.u.cpu().numpy(), g_fast.u.cpu().numpy()
-    sl = (slice(None), slice(4, 20), slice(4, 20), slice(4, 20))
-    l1 = {v: float(np.abs(a[:, i][sl] - b[:, i][sl]).sum() / np.abs(a[:, i][sl]).sum())
-          for v, i in (("dens", 0), ("pres", 4))}
-    cmx = g_mixed.u.cpu().numpy()
-    l1_mixed = {v: float(np.abs(a[:, i][sl] - cmx[:, i][sl]).sum() / np.abs(a[:, i][sl]).sum())
-                for v, i in (("dens", 0), ("pres", 4))}
+    lv = torch.as_tensor(leaves.astype(np.int64), device="cuda")
+    a, b, c = g_plain.u, g_fast.u, g_mixed.u
+    l1_fast = {v: l1(a, b, lv, i) for v, i in (("dens", 0), ("pres", 4))}
+    l1_mixed = {v: l1(a, c, lv, i) for v, i in (("dens", 0), ("pres", 4))}
     sT = g_plain.slots["TEMP"]
-    relT = np.abs(a[:, sT][sl] - b[:, sT][sl]) / a[:, sT][sl]
-    tolT = np.abs(a[:, sT][sl] - b[:, sT][sl]) <= 0.01 * a[:, sT][sl] + 2.0
+    Ta, Tb = a[lv, sT, 4:20, 4:20, 4:20], b[lv, sT, 4:20, 4:20, 4:20]
+    relT = ((Ta - Tb).abs() / Ta).flatten()
+    tolT = float(((Ta - Tb).abs() <= 0.01 * Ta + 2.0).double().mean())
+    relT_q = torch.quantile(relT[torch.randperm(relT.numel(), device="cuda")[:1 << 22]],
+                            torch.tensor([0.5, 0.99], dtype=torch.float64, device="cuda")).tolist()
+    del a, b, c, Ta, Tb
     G.set_cooling_mode(True)
     e2e_ms, e2e_bytes, e2e_parts = e2e_run(G, g_fast, max(2, args.steps // 2), 1)
     G.set_cooling_mode(False)
     hbm, hbm_kind = peaks()
-    # dominant kernel: largest share of the timed region. Algorithmic bytes
-    # per launch = 216 B per zone-update (12 FP64 MHD words + 3 cooling
-    # words, read + write) x the zones that launch covers.
-    per_launch_zones = {k: (zones if k in ("guard_fill", "dt") else min(16, wl["nbx"] * wl["nby"] * wl["nbz"]) * 4096)
-                        for k in prof}
+    # dominant kernel: largest share of the fast path's timed region.
+    # Algorithmic bytes = 216 B per zone-update (12 FP64 MHD words + 3
+    # cooling words, read once + written once) x the zones a launch covers.
     dom = max(prof, key=lambda k: prof[k][0])
-    dom_ms = prof[dom][0] / prof[dom][1]
-    ach = 216.0 * per_launch_zones[dom] / (dom_ms * 1e-3) / 1e9
+    dom_ms, dom_n = prof[dom][0], prof[dom][1]
+    zones_per_launch = zones * args.steps / dom_n
+    ach = 216.0 * zones_per_launch / (dom_ms / dom_n * 1e-3) / 1e9
     launches = int(sum(c for _, c in prof.values()))
     if rank != 0:
         return
+    lvl = np.bincount(tree["level"][leaves]).tolist()
     line = {
         "metric": "zone-updates/s", "value": zones * world / (ms_fast * 1e-3), "unit": "zone-updates/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_fast,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic",
-        "config": {"workload": wl["name"], "blocks": wl["nbx"] * wl["nby"] * wl["nbz"], "block": "16^3+4gc",
+        "config": {"workload": wl["name"], "leaf_blocks": len(leaves), "leaves_per_level": lvl,
+                   "zones": zones, "block": "16^3+4gc",
                    "physics": "MHD HLLD+CT, PPM, implicit heating/cooling", "parallelism": f"replicas{world}",
-                   "l2": "inputs larger than L2 (state ~0.75 GB)"},
+                   "l2": "inputs larger than L2 (state %.1f GB)" % (g_fast.u.numel() * 8 / 1e9)},
         "plain_fp64": {"value": zones * world / (ms_plain * 1e-3), "ms_per_step": ms_plain},
         "speedup_vs_plain_fp64": ms_plain / ms_fast,
-        "l1_err_vs_fp64": l1,
+        "l1_err_vs_fp64": l1_fast,
         "l1_err_mixed_hydro_vs_fp64": l1_mixed,
         "mixed_plain_cooling": {"value": zones * world / (ms_mixed * 1e-3), "ms_per_step": ms_mixed},
         "kernel_ms_per_step_fast": {k: v[0] / args.steps for k, v in prof.items()},
         "kernel_launches_per_step_fast": {k: v[1] / args.steps for k, v in prof.items()},
-        "temp_rel_err_vs_plain": {"p50": float(np.median(relT)), "p99": float(np.quantile(relT, 0.99)),
-                                  "max": float(relT.max()), "frac_within_1pct": float((relT <= 0.01).mean()),
-                                  "frac_within_1pct_plus_brent_tol": float(tolT.mean()),
+        "temp_rel_err_vs_plain": {"p50": relT_q[0], "p99": relT_q[1], "max": float(relT.max()),
+                                  "frac_within_1pct": float((relT <= 0.01).double().mean()),
+                                  "frac_within_1pct_plus_brent_tol": tolT,
                                   "note": "after the same steps of two different paths (mixed hydro + surrogate vs "
                                           "FP64 hydro + plain integrator); Brent's own tolerance is ~2 K"},
         "surrogate": {"samples": 10_000_000, "sample_s": t_samples, "train_s": t_train,
@@ -370,15 +427,16 @@ def main():
         "status": {"plain": {k: st_plain[k] for k in ("code", "n_fallback", "n_eint_switch", "n_bracket_fail")},
                    "fast": {k: st_fast[k] for k in ("code", "n_fallback", "n_eint_switch", "n_bracket_fail")}},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
-                     "frac": ach / hbm, "traffic": None, "peak_kind": hbm_kind, "launch_ms": dom_ms,
-                     "algo_bytes_per_launch": 216.0 * per_launch_zones[dom]},
+                     "frac": ach / hbm, "traffic": None, "peak_kind": hbm_kind, "launch_ms": dom_ms / dom_n,
+                     "algo_bytes_per_launch": 216.0 * zones_per_launch},
         "e2e": {"value": zones / (e2e_ms * 1e-3), "unit": "zone-updates/s", "h2d_bytes_per_step": e2e_bytes,
                 "d2h_bytes_per_step": e2e_bytes, "parts": e2e_parts},
         "gpu_launches": launches,
         "clocks": clk.summary(),
+        "ic_s": t_ic,
     }
-    if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(ic, 1)
+    if cs is not None:
+        line["cpu_baseline"] = cpu_baseline(cs, 1)
     print(json.dumps(line))
 
 

@@ -219,6 +219,23 @@ int gb_grid_upload_flash(const double* unk_host, int nunk, const int* host_slot,
 int gb_grid_download_flash(double* unk_host, int nunk, const int* host_slot, int nblocks,
                            void* stream);
 
+/* The same for the listed store blocks only (host list of 0-based store
+ * ids, e.g. the leaf blocks FLASH passes to Hydro): block list[q] of the
+ * host unk array <-> store block list[q]. Runs of consecutive ids move as
+ * one copy. */
+int gb_grid_upload_flash_list(const double* unk_host, int nunk, const int* host_slot, int blockCount,
+                              const int* blockList_host, void* stream);
+int gb_grid_download_flash_list(double* unk_host, int nunk, const int* host_slot, int blockCount,
+                                const int* blockList_host, void* stream);
+
+/* Face-centred B of the listed blocks in FLASH's facevar{x,y,z}(1, ...,
+ * blk) order (one face variable: the same element order as the store's
+ * face arrays, so no transpose). */
+int gb_grid_upload_faces_list(const double* fx_host, const double* fy_host, const double* fz_host,
+                              int blockCount, const int* blockList_host, void* stream);
+int gb_grid_download_faces_list(double* fx_host, double* fy_host, double* fz_host, int blockCount,
+                                const int* blockList_host, void* stream);
+
 /* ---------------------------------------------------------------- surrogate */
 /* Learned cooling surrogate (no counterpart in the reference): an MLP
  * 4 -> 64 -> 64 -> 64 -> 1 with SiLU, BF16 weights, FP32 accumulation.

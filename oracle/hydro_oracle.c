@@ -1024,7 +1024,7 @@ static long long orc_wrap(long long x, long long n) { return ((x % n) + n) % n; 
  * cell is injected, a finer neighbour's covering cells are averaged
  * (8 cells; faces: the 4 fine faces on the coarse face); a fine guard face
  * that falls inside a coarse cell takes the mean of the two coarse faces. */
-void orc_fill_guards_tree(const orc_hydro_params* p, int nnodes, const int* level, const int* coord,
+void orc_fill_guards_leaf(const orc_hydro_params* p, int b, const int* level, const int* coord,
                           const int* child, const int* root, int nr0, int nr1, int nr2, int maxlevel,
                           double* u, double* bx, double* by, double* bz)
 {
@@ -1034,8 +1034,7 @@ void orc_fill_guards_tree(const orc_hydro_params* p, int nnodes, const int* leve
     const long long N[3] = {(long long)nr0 * nxb << maxlevel, (long long)nr1 * nxb << maxlevel,
                             (long long)nr2 * nxb << maxlevel};
     double* fa[3] = {bx, by, bz};
-    for (int b = 0; b < nnodes; ++b) {
-        if (child[8 * b] >= 0) continue;
+    {
         const int L = level[b];
         const long long s = 1LL << (maxlevel - L);
         const int* cd = coord + 3 * b;
@@ -1076,7 +1075,7 @@ void orc_fill_guards_tree(const orc_hydro_params* p, int nnodes, const int* leve
                         }
                     }
                 }
-        if (!p->mhd) continue;
+        if (!p->mhd) return;
         for (int a = 0; a < 3; ++a)
             for (int k = 0; k < n + (a == 2); ++k)
                 for (int j = 0; j < n + (a == 1); ++j)
@@ -1125,4 +1124,13 @@ void orc_fill_guards_tree(const orc_hydro_params* p, int nnodes, const int* leve
                         }
                     }
     }
+}
+
+void orc_fill_guards_tree(const orc_hydro_params* p, int nnodes, const int* level, const int* coord,
+                          const int* child, const int* root, int nr0, int nr1, int nr2, int maxlevel,
+                          double* u, double* bx, double* by, double* bz)
+{
+    for (int b = 0; b < nnodes; ++b)
+        if (child[8 * b] < 0)
+            orc_fill_guards_leaf(p, b, level, coord, child, root, nr0, nr1, nr2, maxlevel, u, bx, by, bz);
 }

@@ -68,6 +68,22 @@ void orc_fill_guards_tree(const orc_hydro_params* p, int nnodes, const int* leve
                           const int* child, const int* root, int nr0, int nr1, int nr2, int maxlevel,
                           double* u, double* bx, double* by, double* bz);
 
+/* The same fill for one leaf b (reads only interior cells and owned faces
+ * of other leaves, so leaves can be filled concurrently). */
+void orc_fill_guards_leaf(const orc_hydro_params* p, int b, const int* level, const int* coord,
+                          const int* child, const int* root, int nr0, int nr1, int nr2, int maxlevel,
+                          double* u, double* bx, double* by, double* bz);
+
+/* OpenMP drivers over a list of leaves of a block tree (omp_driver.c): guard
+ * fill, CFL limit and one unsplit step with cell size root_dx / 2^level. */
+void orc_fill_guards_list(const orc_hydro_params* p, int nlist, const int* list, const int* level,
+                          const int* coord, const int* child, const int* root, int nr0, int nr1, int nr2,
+                          int maxlevel, double* u, double* bx, double* by, double* bz);
+double orc_dt_limit_list(const orc_hydro_params* p, int nlist, const int* list, const int* level,
+                         const double* u, double root_dx);
+long orc_unsplit_list(const orc_hydro_params* p, int nlist, const int* list, const int* level, double* u,
+                      double* bx, double* by, double* bz, double dt, double root_dx);
+
 /* Total mass, momentum, energy (E incl. magnetic) and max |div B| over the
  * interior of a uniform grid. out[0..4] = M, Px, Py, Pz, E; out[5] = max
  * |divB| * dx / max|B|. */

@@ -9,6 +9,7 @@
 #include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
+#include <math.h>
 #endif
 
 int orc_num_threads(void)
@@ -84,4 +85,50 @@ int orc_radheat_cells_omp(const orc_cool_params* p, const orc_table* t, int64_t 
                                      flags_out ? flags_out + o : NULL);
     }
     return clamped;
+}
+
+/* ---------------------------------------------------- block-tree leaf lists */
+
+void orc_fill_guards_list(const orc_hydro_params* p, int nlist, const int* list, const int* level,
+                          const int* coord, const int* child, const int* root, int nr0, int nr1, int nr2,
+                          int maxlevel, double* u, double* bx, double* by, double* bz)
+{
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int q = 0; q < nlist; ++q)
+        orc_fill_guards_leaf(p, list[q], level, coord, child, root, nr0, nr1, nr2, maxlevel, u, bx, by, bz);
+}
+
+double orc_dt_limit_list(const orc_hydro_params* p, int nlist, const int* list, const int* level,
+                         const double* u, double root_dx)
+{
+    const int n = p->nxb + 2 * p->nguard;
+    const int64_t n3 = (int64_t)n * n * n;
+    double best = 1e300;
+#pragma omp parallel for reduction(min : best)
+    for (int q = 0; q < nlist; ++q) {
+        const int b = list[q];
+        const double dx = ldexp(root_dx, -level[b]);
+        double v = orc_block_dt_limit(p, u + (int64_t)b * ORV_NVAR * n3, dx, dx, dx);
+        if (v < best) best = v;
+    }
+    return best;
+}
+
+long orc_unsplit_list(const orc_hydro_params* p, int nlist, const int* list, const int* level, double* u,
+                      double* bx, double* by, double* bz, double dt, double root_dx)
+{
+    const int n = p->nxb + 2 * p->nguard;
+    const int64_t n3 = (int64_t)n * n * n, fsz = n3 + (int64_t)n * n;
+    long total = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
+    for (int q = 0; q < nlist; ++q) {
+        const int b = list[q];
+        const double dx = ldexp(root_dx, -level[b]);
+        double* ub = u + (int64_t)b * ORV_NVAR * n3;
+        double* fx = p->mhd ? bx + (int64_t)b * fsz : NULL;
+        double* fy = p->mhd ? by + (int64_t)b * fsz : NULL;
+        double* fz = p->mhd ? bz + (int64_t)b * fsz : NULL;
+        total += orc_unsplit_block(p, ub, fx, fy, fz, dt, dx, dx, dx);
+    }
+    return total;
 }

@@ -111,6 +111,13 @@ def lib():
         L.orc_test_eig.argtypes = [C.c_int, C.c_double, dp, dp, dp, dp]
         L.orc_fill_guards_tree.argtypes = [C.POINTER(HydroParams), C.c_int, optd, optd, optd, optd, C.c_int,
                                            C.c_int, C.c_int, C.c_int, optd, optd, optd, optd]
+        L.orc_fill_guards_list.argtypes = [C.POINTER(HydroParams), C.c_int, optd, optd, optd, optd, optd,
+                                           C.c_int, C.c_int, C.c_int, C.c_int, optd, optd, optd, optd]
+        L.orc_dt_limit_list.argtypes = [C.POINTER(HydroParams), C.c_int, optd, optd, optd, C.c_double]
+        L.orc_dt_limit_list.restype = C.c_double
+        L.orc_unsplit_list.argtypes = [C.POINTER(HydroParams), C.c_int, optd, optd, optd, optd, optd, optd,
+                                       C.c_double, C.c_double]
+        L.orc_unsplit_list.restype = C.c_long
         L.orc_num_threads.restype = C.c_int
         L.orc_set_num_threads.argtypes = [C.c_int]
         _lib = L
@@ -189,6 +196,35 @@ def fill_guards_tree(p: HydroParams, tree: dict, u, bx=None, by=None, bz=None):
     lib().orc_fill_guards_tree(C.byref(p), len(a["level"]), _p(a["level"]), _p(a["coord"]), _p(a["child"]),
                                _p(a["root"]), nr[0], nr[1], nr[2], int(tree["maxlevel"]), _p(u), _p(bx),
                                _p(by), _p(bz))
+
+
+class TreeLists:
+    """int32 copies of a block tree's arrays for the leaf-list drivers."""
+
+    def __init__(self, tree: dict):
+        self.a = {k: np.ascontiguousarray(tree[k], np.int32) for k in ("level", "coord", "child", "root")}
+        self.nr = tree["nr"]
+        self.maxlevel = int(tree["maxlevel"])
+
+
+def fill_guards_list(p: HydroParams, tl: TreeLists, leaves, u, bx=None, by=None, bz=None):
+    """OpenMP guard fill of the listed leaves (every leaf read must be up to date)."""
+    a = tl.a
+    ls = np.ascontiguousarray(leaves, np.int32)
+    lib().orc_fill_guards_list(C.byref(p), len(ls), _p(ls), _p(a["level"]), _p(a["coord"]), _p(a["child"]),
+                               _p(a["root"]), tl.nr[0], tl.nr[1], tl.nr[2], tl.maxlevel, _p(u), _p(bx), _p(by),
+                               _p(bz))
+
+
+def dt_limit_list(p: HydroParams, tl: TreeLists, leaves, u, root_dx) -> float:
+    ls = np.ascontiguousarray(leaves, np.int32)
+    return lib().orc_dt_limit_list(C.byref(p), len(ls), _p(ls), _p(tl.a["level"]), _p(u), root_dx)
+
+
+def unsplit_list(p: HydroParams, tl: TreeLists, leaves, u, bx, by, bz, dt, root_dx):
+    ls = np.ascontiguousarray(leaves, np.int32)
+    return lib().orc_unsplit_list(C.byref(p), len(ls), _p(ls), _p(tl.a["level"]), _p(u), _p(bx), _p(by),
+                                  _p(bz), dt, root_dx)
 
 
 def dt_limit(p: HydroParams, u, dx, dy, dz) -> float:

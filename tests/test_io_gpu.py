@@ -1,0 +1,91 @@
+"""FLASH-layout host <-> device transfers of the block store."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _grid(gb):
+    from torch_gb300 import amr
+    t, c = amr.small_tree()
+    st = amr.amr_box(t, c, seed=5, device="cuda")
+    return t, gb.grid_from_amr(t, st, mhd=True, cooling=True)
+
+
+def _slots(gb, g):
+    hs = (C.c_int * gb.NROLE)(*([-1] * gb.NROLE))
+    for name, s in g.slots.items():
+        hs[gb.R[name]] = s
+    return hs
+
+
+def test_flash_layout_roundtrip_whole_store(gb):
+    import torch
+    t, g = _grid(gb)
+    L, nunk, nb = gb.lib(), g.nvar, g.nblocks
+    ref = g.u.clone()
+    host = torch.empty((nb, 24 ** 3, nunk), dtype=torch.float64).pin_memory()
+    gb.check(L.gb_grid_download_flash(C.c_void_p(host.data_ptr()), nunk, _slots(gb, g), nb, None), "down")
+    torch.cuda.synchronize()
+    # variable-fastest order: host[b, cell, v] == store[b, v, cell]
+    assert torch.equal(host, ref.reshape(nb, nunk, -1).transpose(1, 2).cpu())
+    g.u.zero_()
+    gb.check(L.gb_grid_upload_flash(C.c_void_p(host.data_ptr()), nunk, _slots(gb, g), nb, None), "up")
+    torch.cuda.synchronize()
+    assert torch.equal(g.u, ref)
+
+
+def test_flash_layout_list_transfers(gb):
+    """Leaf-list transfers move exactly the listed blocks, cells and faces,
+    and agree with the whole-store transfer on them."""
+    import torch
+    t, g = _grid(gb)
+    L, nunk, nb = gb.lib(), g.nvar, g.nblocks
+    leaves = np.ascontiguousarray(t["leaf"][::2], np.int32)   # runs and gaps
+    lp = leaves.ctypes.data_as(C.c_void_p)
+    host = torch.zeros((nb, 24 ** 3, nunk), dtype=torch.float64).pin_memory()
+    hf = [torch.zeros(a.shape, dtype=torch.float64).pin_memory() for a in (g.fx, g.fy, g.fz)]
+    gb.check(L.gb_grid_download_flash_list(C.c_void_p(host.data_ptr()), nunk, _slots(gb, g), len(leaves), lp,
+                                           None), "down list")
+    gb.check(L.gb_grid_download_faces_list(*[C.c_void_p(h.data_ptr()) for h in hf], len(leaves), lp, None),
+             "faces down")
+    torch.cuda.synchronize()
+    full = g.u.reshape(nb, nunk, -1).transpose(1, 2).cpu()
+    mask = np.zeros(nb, bool)
+    mask[leaves] = True
+    assert torch.equal(host[mask], full[mask])
+    assert not host[~mask].any()
+    for h, d in zip(hf, (g.fx, g.fy, g.fz)):
+        assert torch.equal(h[mask], d.cpu()[mask])
+        assert not h[~mask].any()
+    # upload a modified copy of the listed blocks into a cleared store
+    ref_u, ref_f = g.u.clone(), [a.clone() for a in (g.fx, g.fy, g.fz)]
+    host[mask] *= 2.0
+    for h in hf:
+        h[mask] += 1.0
+    g.u.zero_()
+    for a in (g.fx, g.fy, g.fz):
+        a.zero_()
+    gb.check(L.gb_grid_upload_flash_list(C.c_void_p(host.data_ptr()), nunk, _slots(gb, g), len(leaves), lp,
+                                         None), "up list")
+    gb.check(L.gb_grid_upload_faces_list(*[C.c_void_p(h.data_ptr()) for h in hf], len(leaves), lp, None),
+             "faces up")
+    torch.cuda.synchronize()
+    m = torch.as_tensor(mask, device="cuda")
+    assert torch.equal(g.u[m], 2.0 * ref_u[m])
+    assert not g.u[~m].any()
+    for a, r in zip((g.fx, g.fy, g.fz), ref_f):
+        assert torch.equal(a[m], r[m] + 1.0)
+        assert not a[~m].any()
+
+
+def test_list_transfer_rejects_bad_ids(gb):
+    t, g = _grid(gb)
+    L = gb.lib()
+    bad = np.array([0, g.nblocks], np.int32)
+    host = np.zeros((2, 24 ** 3, g.nvar))
+    rc = L.gb_grid_upload_flash_list(host.ctypes.data_as(C.c_void_p), g.nvar, _slots(gb, g), 2,
+                                     bad.ctypes.data_as(C.c_void_p), None)
+    assert rc != 0

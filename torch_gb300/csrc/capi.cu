@@ -338,13 +338,15 @@ __global__ void k_dt_finish(const unsigned long long* bits, double cfl, double* 
 }
 
 __global__ void k_flash_to_soa(const double* __restrict__ in, int nunk, const int* __restrict__ hslot,
-                               gb_dev_grid g, int nblocks)
+                               gb_dev_grid g, int nblocks, const int* __restrict__ list)
 {
-    // in: unk(nunk, 24, 24, 24, nblocks) Fortran order (variable fastest)
+    // in: unk(nunk, 24, 24, 24, nblocks) Fortran order (variable fastest);
+    // staged block q goes to store block list[q] (q itself without a list)
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t total = (int64_t)nblocks * GB_N3;
     if (idx >= total) return;
-    int blk = (int)(idx / GB_N3), c = (int)(idx % GB_N3);
+    int q = (int)(idx / GB_N3), c = (int)(idx % GB_N3);
+    int blk = list ? list[q] : q;
     const double* cell = in + idx * nunk;
     for (int r = 0; r < GB_NROLE; ++r) {
         int hs = hslot[r], ds = g.slot[r];
@@ -353,12 +355,13 @@ __global__ void k_flash_to_soa(const double* __restrict__ in, int nunk, const in
 }
 
 __global__ void k_soa_to_flash(double* __restrict__ out, int nunk, const int* __restrict__ hslot,
-                               gb_dev_grid g, int nblocks)
+                               gb_dev_grid g, int nblocks, const int* __restrict__ list)
 {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t total = (int64_t)nblocks * GB_N3;
     if (idx >= total) return;
-    int blk = (int)(idx / GB_N3), c = (int)(idx % GB_N3);
+    int q = (int)(idx / GB_N3), c = (int)(idx % GB_N3);
+    int blk = list ? list[q] : q;
     double* cell = out + idx * nunk;
     for (int r = 0; r < GB_NROLE; ++r) {
         int hs = hslot[r], ds = g.slot[r];
@@ -557,12 +560,12 @@ static int flash_copy(bool up, double* host, int nunk, const int* host_slot, int
     if (up) {
         if (gb_check(cudaMemcpyAsync(g_gb.d_stage, host, bytes, cudaMemcpyHostToDevice, s), "upload")) return GB_ERR_CUDA;
         gb_prof_begin(GBP_COPY, s);
-        k_flash_to_soa<<<nb, 256, 0, s>>>(g_gb.d_stage, nunk, dslot, g_gb.grid, nblocks);
+        k_flash_to_soa<<<nb, 256, 0, s>>>(g_gb.d_stage, nunk, dslot, g_gb.grid, nblocks, nullptr);
         gb_prof_end(GBP_COPY, s);
         if (gb_check(cudaGetLastError(), "k_flash_to_soa")) return GB_ERR_CUDA;
     } else {
         gb_prof_begin(GBP_COPY, s);
-        k_soa_to_flash<<<nb, 256, 0, s>>>(g_gb.d_stage, nunk, dslot, g_gb.grid, nblocks);
+        k_soa_to_flash<<<nb, 256, 0, s>>>(g_gb.d_stage, nunk, dslot, g_gb.grid, nblocks, nullptr);
         gb_prof_end(GBP_COPY, s);
         if (gb_check(cudaGetLastError(), "k_soa_to_flash")) return GB_ERR_CUDA;
         if (gb_check(cudaMemcpyAsync(host, g_gb.d_stage, bytes, cudaMemcpyDeviceToHost, s), "download"))
@@ -581,4 +584,128 @@ extern "C" int gb_grid_download_flash(double* unk_host, int nunk, const int* hos
                                       void* stream)
 {
     return flash_copy(false, unk_host, nunk, host_slot, nblocks, stream);
+}
+
+// Runs of consecutive store ids in a host block list: [q0, q0 + len) of the
+// list covers store blocks list[q0] .. list[q0] + len - 1.
+template <typename F>
+static int for_each_run(int n, const int* list, F&& f)
+{
+    for (int q0 = 0; q0 < n;) {
+        int len = 1;
+        while (q0 + len < n && list[q0 + len] == list[q0] + len) ++len;
+        int rc = f(q0, list[q0], len);
+        if (rc) return rc;
+        q0 += len;
+    }
+    return GB_OK;
+}
+
+static int check_host_list(int n, const int* list, const char* who)
+{
+    if (n < 0 || (n > 0 && !list)) {
+        gb_set_error("%s: bad block list", who);
+        return GB_ERR_ARG;
+    }
+    for (int q = 0; q < n; ++q)
+        if (list[q] < 0 || list[q] >= g_gb.grid.maxblocks) {
+            gb_set_error("%s: block id %d outside the store (maxblocks %d)", who, list[q], g_gb.grid.maxblocks);
+            return GB_ERR_ARG;
+        }
+    return GB_OK;
+}
+
+static int flash_copy_list(bool up, double* host, int nunk, const int* host_slot, int n, const int* list,
+                           void* stream)
+{
+    if (!g_gb.grid_ok) {
+        gb_set_error("grid transfer before gb_register_grid");
+        return GB_ERR_NOT_INIT;
+    }
+    if (!host || !host_slot || nunk <= 0) return GB_ERR_ARG;
+    int rc = check_host_list(n, list, up ? "gb_grid_upload_flash_list" : "gb_grid_download_flash_list");
+    if (rc || n == 0) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t per = (size_t)GB_N3 * nunk;  // doubles per FLASH block
+    const size_t bytes = (size_t)n * per * sizeof(double);
+    rc = gb_ensure_stage(bytes + (GB_NROLE + (size_t)n) * sizeof(int));
+    if (rc) return rc;
+    double* stage = (double*)g_gb.d_stage;
+    int* dslot = (int*)((char*)g_gb.d_stage + bytes);
+    int* dlist = dslot + GB_NROLE;
+    if (gb_check(cudaMemcpyAsync(dslot, host_slot, GB_NROLE * sizeof(int), cudaMemcpyHostToDevice, s), "slot copy") ||
+        gb_check(cudaMemcpyAsync(dlist, list, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s), "list copy"))
+        return GB_ERR_CUDA;
+    const unsigned nb = (unsigned)(((int64_t)n * GB_N3 + 255) / 256);
+    if (up) {
+        rc = for_each_run(n, list, [&](int q0, int b0, int len) {
+            return gb_check(cudaMemcpyAsync(stage + (size_t)q0 * per, host + (size_t)b0 * per,
+                                            (size_t)len * per * sizeof(double), cudaMemcpyHostToDevice, s),
+                            "upload") ? GB_ERR_CUDA : GB_OK;
+        });
+        if (rc) return rc;
+        gb_prof_begin(GBP_COPY, s);
+        k_flash_to_soa<<<nb, 256, 0, s>>>(stage, nunk, dslot, g_gb.grid, n, dlist);
+        gb_prof_end(GBP_COPY, s);
+        return gb_check(cudaGetLastError(), "k_flash_to_soa") ? GB_ERR_CUDA : GB_OK;
+    }
+    gb_prof_begin(GBP_COPY, s);
+    k_soa_to_flash<<<nb, 256, 0, s>>>(stage, nunk, dslot, g_gb.grid, n, dlist);
+    gb_prof_end(GBP_COPY, s);
+    if (gb_check(cudaGetLastError(), "k_soa_to_flash")) return GB_ERR_CUDA;
+    return for_each_run(n, list, [&](int q0, int b0, int len) {
+        return gb_check(cudaMemcpyAsync(host + (size_t)b0 * per, stage + (size_t)q0 * per,
+                                        (size_t)len * per * sizeof(double), cudaMemcpyDeviceToHost, s),
+                        "download") ? GB_ERR_CUDA : GB_OK;
+    });
+}
+
+extern "C" int gb_grid_upload_flash_list(const double* unk_host, int nunk, const int* host_slot, int blockCount,
+                                         const int* blockList_host, void* stream)
+{
+    return flash_copy_list(true, const_cast<double*>(unk_host), nunk, host_slot, blockCount, blockList_host, stream);
+}
+
+extern "C" int gb_grid_download_flash_list(double* unk_host, int nunk, const int* host_slot, int blockCount,
+                                           const int* blockList_host, void* stream)
+{
+    return flash_copy_list(false, unk_host, nunk, host_slot, blockCount, blockList_host, stream);
+}
+
+static int face_copy_list(bool up, double* const host[3], int n, const int* list, void* stream)
+{
+    if (!g_gb.grid_ok || !g_gb.grid.f[0] || !g_gb.grid.f[1] || !g_gb.grid.f[2]) {
+        gb_set_error("face transfer: the registered grid has no face fields");
+        return GB_ERR_NOT_INIT;
+    }
+    if (!host[0] || !host[1] || !host[2]) return GB_ERR_ARG;
+    int rc = check_host_list(n, list, up ? "gb_grid_upload_faces_list" : "gb_grid_download_faces_list");
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int a = 0; a < 3; ++a) {
+        double* dev = g_gb.grid.f[a];
+        double* h = host[a];
+        rc = for_each_run(n, list, [&](int, int b0, int len) {
+            const size_t off = (size_t)b0 * GB_FSZ, cnt = (size_t)len * GB_FSZ * sizeof(double);
+            return gb_check(up ? cudaMemcpyAsync(dev + off, h + off, cnt, cudaMemcpyHostToDevice, s)
+                               : cudaMemcpyAsync(h + off, dev + off, cnt, cudaMemcpyDeviceToHost, s),
+                            up ? "face upload" : "face download") ? GB_ERR_CUDA : GB_OK;
+        });
+        if (rc) return rc;
+    }
+    return GB_OK;
+}
+
+extern "C" int gb_grid_upload_faces_list(const double* fx_host, const double* fy_host, const double* fz_host,
+                                         int blockCount, const int* blockList_host, void* stream)
+{
+    double* h[3] = {const_cast<double*>(fx_host), const_cast<double*>(fy_host), const_cast<double*>(fz_host)};
+    return face_copy_list(true, h, blockCount, blockList_host, stream);
+}
+
+extern "C" int gb_grid_download_faces_list(double* fx_host, double* fy_host, double* fz_host, int blockCount,
+                                           const int* blockList_host, void* stream)
+{
+    double* h[3] = {fx_host, fy_host, fz_host};
+    return face_copy_list(false, h, blockCount, blockList_host, stream);
 }

@@ -107,6 +107,11 @@ _SIG = {
     "gb_evolve_step": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_int, C.c_void_p, C.c_void_p]),
     "gb_grid_upload_flash": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
     "gb_grid_download_flash": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
+    "gb_grid_upload_flash_list": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "gb_grid_download_flash_list": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "gb_grid_upload_faces_list": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "gb_grid_download_faces_list": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                              C.c_void_p]),
     "gb_status_reset": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gb_status_read": (C.c_int, [C.c_void_p, C.POINTER(Status)]),
     "gb_mlp_init_random": (C.c_int, [C.c_uint64]),
@@ -209,7 +214,7 @@ def uniform_tree(nbx: int, nby: int, nbz: int):
     ids = np.arange(n)
     coord = np.stack([ids % nbx, (ids // nbx) % nby, ids // (nbx * nby)], 1).astype(np.int32)
     return dict(level=np.zeros(n, np.int32), coord=coord, child=-np.ones((n, 8), np.int32),
-                root=ids.astype(np.int32), nr=(nbx, nby, nbz), maxlevel=0)
+                root=ids.astype(np.int32), nr=(nbx, nby, nbz), maxlevel=0, leaf=ids.astype(np.int32))
 
 
 class Grid:
