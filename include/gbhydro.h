@@ -189,6 +189,14 @@ typedef struct gb_cool_params {
  * int32 form, and set the parameters. Replaces Cool_init/Heat_init. */
 int gb_cool_init(const char* cool_dat_path, const gb_cool_params* p);
 
+/* Temperature floor of the implicit step's Brent tolerance, in kelvin.
+ * heatCool.F90 stops Brent's method at max(TtoEI * 1 K, 1e-6 e_old), so
+ * the default, 1.0, is the reference integrator; a smaller value solves the
+ * same backward-Euler equation more tightly (a diagnostic: it measures how
+ * far the reference's answer sits from the equation's root). No counterpart
+ * in the reference's interface. */
+int gb_set_brent_tolerance(double kelvin);
+
 /* Per-cell heating/cooling over the interior of the listed blocks:
  * RadHeat.F90:179-457 with heating_and_cooling's "Implicit" branch
  * (heatCool.F90:216-514). Updates EINT, ENER, TEMP, TDUS (and PRES via the

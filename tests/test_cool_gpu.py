@@ -90,3 +90,35 @@ def test_heat_on_grid_matches_oracle(gb, oracle):
     e_g = out[:, 6][sl].ravel() * units["vel_unit"] ** 2
     assert np.all(np.abs(e_g - e_o) <= tolT / T_o * e_o)
     assert st["code"] in (0, 6)
+
+
+def test_brent_tolerance_knob(gb, oracle):
+    """A tighter Brent floor solves the same backward-Euler equation closer
+    to its root: the answers move by at most the reference's bracket (2 K
+    or 2e-6 e), and 1 K restores the reference integrator exactly."""
+    import torch
+    gb.init_cooling(gb.cool_params())
+    rho, ei, T, tdust, _ = _cells(20000, 12)
+    dt = 3e11
+    e_o, T_o, td_o, flags = _run_oracle(oracle, rho, ei, T, tdust, dt)
+    dev = lambda a: torch.as_tensor(a.copy(), device="cuda")
+
+    def run(tol):
+        gb.set_brent_tolerance(tol)
+        d = [dev(a) for a in (rho, ei, T, tdust)]
+        gb.cool_cells(*d, dt)
+        torch.cuda.synchronize()
+        return d[2].cpu().numpy()
+
+    try:
+        T_tight = run(1e-3)
+        T_ref = run(1.0)
+    finally:
+        gb.set_brent_tolerance(1.0)
+    ok = (flags & (4 | 8)) == 0
+    tolT = np.maximum(1.0, 1e-6 * T_o) * 2.0 + 1e-9 * T_o
+    assert np.all(np.abs(T_ref - T_o)[ok] <= tolT[ok])
+    assert np.all(np.abs(T_tight - T_o)[ok] <= 2 * tolT[ok])
+    assert np.any(T_tight[ok] != T_ref[ok])
+    with pytest.raises(gb.GBError):
+        gb.set_brent_tolerance(0.0)

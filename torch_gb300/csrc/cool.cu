@@ -186,6 +186,19 @@ __global__ void k_cool_cells(gb_cool_ctx c, int64_t n, const double* __restrict_
 
 }  // namespace
 
+static double g_brent_tol_K = 1.0;
+
+extern "C" int gb_set_brent_tolerance(double kelvin)
+{
+    if (!(kelvin > 0.0) || !(kelvin <= 1e6)) {
+        gb_set_error("gb_set_brent_tolerance: tolerance %g K outside (0, 1e6]", kelvin);
+        return GB_ERR_ARG;
+    }
+    g_brent_tol_K = kelvin;
+    g_gb.cool.brent_tol_K = kelvin;
+    return GB_OK;
+}
+
 extern "C" int gb_cool_init(const char* path, const gb_cool_params* p)
 {
     if (!path || !p) {
@@ -222,6 +235,7 @@ extern "C" int gb_cool_init(const char* path, const gb_cool_params* p)
     g_gb.cool.T = g_gb.d_table;
     g_gb.cool.n = g_gb.d_table + GB_TEMP_PTS;
     g_gb.cool.lam = g_gb.d_table + GB_TEMP_PTS + GB_DENS_PTS;
+    g_gb.cool.brent_tol_K = g_brent_tol_K;
     g_gb.cool.T_min = h[0];
     g_gb.cool.nd_min = h[GB_TEMP_PTS];
     g_gb.cool_ok = true;

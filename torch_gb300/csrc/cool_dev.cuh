@@ -22,6 +22,9 @@ struct gb_cool_ctx {
     const double* n;    // cool_dat(:, 1, 2), DENS_PTS
     const double* lam;  // cool_dat(:, :, 3), dens fastest
     double T_min, nd_min;
+    // Brent tolerance floor of the implicit step in kelvin (heatCool.F90
+    // passes TtoEI * 1 K; other values are a diagnostic of that tolerance)
+    double brent_tol_K;
     // FP32 copies for the learned-cooling path: axes, and cool_dat(:, :, 3)
     // divided by mu_mol m_p (the molecular power per gram)
     const float* Tf;
@@ -513,10 +516,10 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
                 ei2 = fmx(ei2, v.TtoEI * 1.0);
             }
             if (found)
-                ei = zero(c, v, fl, ei1, ei2, eiolder, 3e-16, fmx(v.TtoEI * 1.0, eiold * err_tol), dt0, d);
+                ei = zero(c, v, fl, ei1, ei2, eiolder, 3e-16, fmx(v.TtoEI * c.brent_tol_K, eiold * err_tol), dt0, d);
             else
                 ei = zero(c, v, fl, v.TtoEI * 1.0, v.TtoEI * 1.0e9, eiolder, 3e-16,
-                          fmx(v.TtoEI * 1.0, eiold * err_tol), dt0, d);
+                          fmx(v.TtoEI * c.brent_tol_K, eiold * err_tol), dt0, d);
             temp = ei / v.TtoEI;
             if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update(c, v, temp, d);
             total_time = total_time + dt0;

@@ -101,6 +101,7 @@ _SIG = {
                                            C.c_void_p]),
     "gb_compute_dt": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gb_cool_init": (C.c_int, [C.c_char_p, C.POINTER(CoolParams)]),
+    "gb_set_brent_tolerance": (C.c_int, [C.c_double]),
     "gb_heat": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_void_p]),
     "gb_cool_cells": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                 C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]),
@@ -308,6 +309,11 @@ def init_cooling(p: CoolParams, table_path: str | None = None) -> None:
     from . import tables
     path = table_path or tables.COMPACT_PATH
     check(lib().gb_cool_init(path.encode(), C.byref(p)), "gb_cool_init")
+
+
+def set_brent_tolerance(kelvin: float = 1.0) -> None:
+    """Brent tolerance floor of the plain implicit step (1 K = heatCool.F90)."""
+    check(lib().gb_set_brent_tolerance(float(kelvin)), "gb_set_brent_tolerance")
 
 
 def set_chunk_blocks(n: int) -> None:
