@@ -123,15 +123,30 @@ def make_grid(G, tree, st, cooling=True):
     return g
 
 
-def run_path(G, g, precision, steps, warmup, cool=True, surrogate=False, profile=False, ncu_range=False):
+def run_path(G, g, precision, steps, warmup, cool=True, surrogate=False, profile=False, ncu_range=False,
+             graph=False, tune=False, tune_kw=None):
+    """Time `steps` steps of one path after `warmup` untimed ones. Eager: dt
+    read back by the host each step, then the step's launches; graph: the
+    whole step (dt on the device) replayed as one CUDA graph."""
     import torch
     G.init_hydro(G.hydro_params(True, precision=precision))
     G.set_cooling_mode(surrogate)
     g.register()
     s = torch.cuda.current_stream()
+    tuned = None
+    if tune:
+        from torch_gb300 import autotune
+        tuned = autotune.tune(g, cool=cool, **(tune_kw or {}))
+
+    def step():
+        if graph:
+            g.step_graph(cool)
+        else:
+            dt = g.compute_dt().item()
+            g.evolve_step(dt, cool=cool)
+
     for _ in range(warmup):
-        dt = g.compute_dt().item()
-        g.evolve_step(dt, cool=cool)
+        step()
     torch.cuda.synchronize()
     g.status_reset()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -142,8 +157,7 @@ def run_path(G, g, precision, steps, warmup, cool=True, surrogate=False, profile
         torch.cuda.cudart().cudaProfilerStart()
     e0.record(s)
     for _ in range(steps):
-        dt = g.compute_dt().item()
-        g.evolve_step(dt, cool=cool)
+        step()
     e1.record(s)
     torch.cuda.synchronize()
     if ncu_range:
@@ -151,6 +165,8 @@ def run_path(G, g, precision, steps, warmup, cool=True, surrogate=False, profile
     prof = G.prof_read() if profile else None
     G.prof_enable(False)
     G.set_cooling_mode(False)
+    if graph:
+        prof = {"graph_kernels_per_step": G.graph_info()[2], "tuned": tuned}
     return e0.elapsed_time(e1) / steps, g.status_read(), prof
 
 
@@ -262,8 +278,7 @@ def e2e_run(G, g, steps, warmup):
         G.check(L.gb_grid_upload_faces_list(*fp, nl, lp, st), "upload faces")
         if timed:
             ev[1].record()
-        dt = g.compute_dt().item()
-        g.evolve_step(dt, cool=True)
+        g.step_graph(cool=True)
         if timed:
             ev[2].record()
         G.check(L.gb_grid_download_flash_list(hp, nunk, hslot, nl, lp, st), "download")
@@ -348,6 +363,7 @@ def main():
     ap.add_argument("--impl", default="gb")
     ap.add_argument("--workload", default="amr", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (16 blocks, tile 32)")
     ap.add_argument("--weights", default=None, help="load surrogate weights (.npy) instead of training")
     ap.add_argument("--save-weights", default=None)
     ap.add_argument("--ncu-range", action="store_true",
@@ -401,6 +417,7 @@ def main():
     g_fast = make_grid(G, tree, st)
     g_mixed = make_grid(G, tree, st)
     g_tight = make_grid(G, tree, st)
+    g_eager = make_grid(G, tree, st)
     cs = None
     if rank == 0 and not args.no_cpu_baseline:
         cs = CpuStep(wl, tree, st)
@@ -410,9 +427,14 @@ def main():
     if world > 1:
         dist.barrier()
     with clk:
-        ms_plain, st_plain, _ = run_path(G, g_plain, 0, args.steps, args.warmup)
-        ms_fast, st_fast, prof = run_path(G, g_fast, 1, args.steps, args.warmup, surrogate=True, profile=True,
-                                          ncu_range=args.ncu_range)
+        ms_plain, st_plain, pinfo = run_path(G, g_plain, 0, args.steps, args.warmup, graph=True,
+                                             tune=not args.no_tune,
+                                             tune_kw={"chunks": (16, 32, 64), "steps": 1})
+        ms_fast, st_fast, ginfo = run_path(G, g_fast, 1, args.steps, args.warmup, surrogate=True, graph=True,
+                                           tune=not args.no_tune, ncu_range=args.ncu_range)
+        # the same path launched eagerly with the in-library profiler on:
+        # per-kernel times (the profiler cannot time inside a graph)
+        ms_eager, _, prof = run_path(G, g_eager, 1, args.steps, args.warmup, surrogate=True, profile=True)
         ms_mixed, st_mixed, _ = run_path(G, g_mixed, 1, args.steps, args.warmup)
     # diagnostic, untimed: mixed hydro + the plain integrator with Brent's
     # tolerance floor at 1e-3 K (the backward-Euler trajectory)
@@ -448,7 +470,7 @@ def main():
     dom_ms, dom_n = prof[dom][0], prof[dom][1]
     zones_per_launch = zones * args.steps / dom_n
     ach = 216.0 * zones_per_launch / (dom_ms / dom_n * 1e-3) / 1e9
-    launches = int(sum(c for _, c in prof.values()))
+    launches = int(ginfo["graph_kernels_per_step"]) * args.steps
     if rank != 0:
         return
     lvl = np.bincount(tree["level"][leaves]).tolist()
@@ -461,7 +483,8 @@ def main():
                    "zones": zones, "block": "16^3+4gc",
                    "physics": "MHD HLLD+CT, PPM, implicit heating/cooling", "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (state %.1f GB)" % (g_fast.u.numel() * 8 / 1e9)},
-        "plain_fp64": {"value": zones * world / (ms_plain * 1e-3), "ms_per_step": ms_plain},
+        "plain_fp64": {"value": zones * world / (ms_plain * 1e-3), "ms_per_step": ms_plain,
+                       "launch_config": {k: pinfo["tuned"][k] for k in ("chunk", "tile")} if pinfo["tuned"] else None},
         "speedup_vs_plain_fp64": ms_plain / ms_fast,
         "l1_err_vs_fp64": l1_fast,
         "l1_err_mixed_hydro_vs_fp64": l1_mixed,
@@ -473,6 +496,10 @@ def main():
                    "(the reference) vs at 1e-3 K, both on mixed hydro; l1_err_vs_backward_euler_root: fast "
                    "path vs the 1e-3 K run",
         "mixed_plain_cooling": {"value": zones * world / (ms_mixed * 1e-3), "ms_per_step": ms_mixed},
+        "fast_eager": {"ms_per_step": ms_eager, "value": zones * world / (ms_eager * 1e-3),
+                       "note": "the same fast path launched kernel by kernel with the host reading dt each step"},
+        "launch_config": {k: ginfo["tuned"][k] for k in ("chunk", "tile", "cached")} if ginfo["tuned"] else
+                         {"chunk": 16, "tile": 32, "tuned": False},
         "kernel_ms_per_step_fast": {k: v[0] / args.steps for k, v in prof.items()},
         "kernel_launches_per_step_fast": {k: v[1] / args.steps for k, v in prof.items()},
         "temp_rel_err_vs_plain_after_steps": temp_steps,

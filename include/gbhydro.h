@@ -157,6 +157,13 @@ int gb_hydro_unsplit_noalloc(int blockCount, const int* blockList_dev, double dt
  * scratch; the autotuner picks it). Default 16. */
 int gb_set_chunk_blocks(int n);
 
+/* Launch shapes of the hydro step: blocks per chunk (the scratch of one
+ * chunk is reused across chunks; 16 blocks of mixed-precision scratch fit
+ * in L2) and cells per reconstruction CTA per direction (32 or 64). Chosen
+ * by torch_gb300.autotune; no counterpart in the reference. */
+int gb_set_launch_config(int chunk_blocks, int recon_tile);
+int gb_get_launch_config(int* chunk_blocks, int* recon_tile);
+
 /* CFL time step: writes cfl * min over interior cells of the listed blocks
  * of dx_d / (|v_d| + c_f,d) to *dt_dev (device double). The per-block
  * Hydro_computeDt + MPI_AllReduce(MINLOC) of
@@ -217,6 +224,26 @@ int gb_cool_cells(int64_t n, const double* dens, double* ei, double* temp, doubl
  * into the update's epilogue when cool != 0. */
 int gb_evolve_step(int blockCount, const int* blockList_dev, double dt, int cool,
                    gb_status* st_dev, void* stream);
+
+/* The same step with dt on the device, as one CUDA graph: the CFL limit of
+ * the listed blocks is written to dt_dev (CFL * min dx / (|v| + c_f), as
+ * gb_compute_dt), then guard fill, hydro/MHD and (cool != 0) cooling run
+ * with that dt, read by the kernels from dt_dev; the host does not wait.
+ * The graph is captured on the first call and replayed while the
+ * arguments and the library's configuration (grid, parameters, cooling
+ * mode, tables, surrogate weights, chunk size) stay the same; any change
+ * re-captures it. blockList_dev, dt_dev and st_dev must stay valid while
+ * the graph may run. Replaces the Driver_computeDt + Hydro + Heat sequence
+ * of one FLASH step (Driver_evolveFlash.F90:405-408, Driver_sourceTerms.F90:67,
+ * Driver_computeDt.F90:327-335,514-515), with dt computed at the start of
+ * the step. Not re-entrant. */
+int gb_step_graph(int blockCount, const int* blockList_dev, int cool, double* dt_dev, gb_status* st_dev,
+                  void* stream);
+/* Drops the captured step graph. */
+int gb_graph_reset(void);
+/* Number of captures and replays of the step graph so far, and the kernel
+ * launches one replay of the current graph makes. */
+int gb_graph_info(long long* captures, long long* launches, long long* kernel_nodes);
 
 /* Host<->device copies of the whole store in FLASH's unk(NUNK, i, j, k,
  * blk) order (variable fastest), transposed on the device. nunk = number

@@ -1,0 +1,114 @@
+"""The whole step as a replayed CUDA graph with dt on the device gives the
+eager step's state bit for bit."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _grid(gb):
+    from torch_gb300 import amr
+    t, c = amr.small_tree()
+    st = amr.amr_box(t, c, seed=7, device="cuda")
+    g = gb.grid_from_amr(t, st, mhd=True, cooling=True)
+    units = gb.code_units()
+    g.u[:, g.slots["TEMP"]] = g.u[:, g.slots["EINT"]] * units["vel_unit"] ** 2 * (2.0 / 3.0) * (24.0 / 11.0) \
+        * gb.MP / gb.KB
+    g.u[:, g.slots["TDUS"]] = 18.0
+    return g
+
+
+@pytest.mark.parametrize("precision,surrogate", [(0, False), (1, False), (1, True)])
+def test_graph_step_matches_eager(gb, precision, surrogate):
+    import torch
+    units = gb.code_units()
+    gb.init_cooling(gb.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
+                                   time_unit=units["time_unit"]))
+    if surrogate:
+        gb.mlp_init(3)
+    gb.init_hydro(gb.hydro_params(True, precision=precision))
+    a, b = _grid(gb), _grid(gb)
+    gb.set_chunk_blocks(16)
+    dts = []
+    a.register()
+    gb.set_cooling_mode(surrogate)
+    for _ in range(3):
+        dt = a.compute_dt().item()
+        dts.append(dt)
+        a.evolve_step(dt, cool=True)
+    b.register()
+    c0, l0, _ = gb.graph_info()
+    for q in range(3):
+        d = b.step_graph(cool=True)
+        torch.cuda.synchronize()
+        assert d.item() == dts[q]
+    c1, l1, kn = gb.graph_info()
+    gb.set_cooling_mode(False)
+    assert (c1 - c0, l1 - l0) == (1, 3)
+    assert kn > 0
+    assert torch.equal(a.u[a.t_leaf.long()], b.u[b.t_leaf.long()])
+    for x, y in ((a.fx, b.fx), (a.fy, b.fy), (a.fz, b.fz)):
+        assert torch.equal(x[a.t_leaf.long()], y[b.t_leaf.long()])
+
+
+def test_graph_recaptured_on_configuration_change(gb):
+    import torch
+    units = gb.code_units()
+    gb.init_cooling(gb.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
+                                   time_unit=units["time_unit"]))
+    gb.init_hydro(gb.hydro_params(True, precision=1))
+    g = _grid(gb)
+    c0, _, _ = gb.graph_info()
+    g.step_graph(cool=True)
+    g.step_graph(cool=True)
+    gb.set_chunk_blocks(8)
+    g.step_graph(cool=True)
+    g.step_graph(cool=False)
+    gb.set_chunk_blocks(16)
+    torch.cuda.synchronize()
+    c1, _, _ = gb.graph_info()
+    assert c1 - c0 == 3
+    assert g.status_read()["code"] == 0
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_launch_shapes_do_not_change_results(gb, precision):
+    """Chunk size and reconstruction tile only change the launch grid: the
+    state after a step is identical for every shape."""
+    import torch
+    gb.init_hydro(gb.hydro_params(True, precision=precision))
+    out = []
+    try:
+        for chunk, tile in ((16, 32), (5, 64), (64, 32)):
+            gb.set_launch_config(chunk, tile)
+            g = _grid(gb)
+            dt = g.compute_dt().item()
+            g.evolve_step(dt, cool=False)
+            torch.cuda.synchronize()
+            out.append(g.u[g.t_leaf.long()].clone())
+            del g
+    finally:
+        gb.set_launch_config(16, 32)
+    assert torch.equal(out[0], out[1]) and torch.equal(out[0], out[2])
+
+
+def test_autotuner_picks_a_candidate_and_restores_state(gb, tmp_path, monkeypatch):
+    import torch
+    from torch_gb300 import autotune
+    monkeypatch.setattr(autotune, "CACHE", str(tmp_path / "tune.json"))
+    units = gb.code_units()
+    gb.init_cooling(gb.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
+                                   time_unit=units["time_unit"]))
+    gb.init_hydro(gb.hydro_params(True, precision=1))
+    g = _grid(gb)
+    before = g.u.clone()
+    try:
+        r = autotune.tune(g, cool=True, chunks=(8, 16), tiles=(32, 64), steps=1)
+        assert (r["chunk"], r["tile"]) in {(8, 32), (8, 64), (16, 32), (16, 64)}
+        assert gb.get_launch_config() == (r["chunk"], r["tile"])
+        assert len(r["trials"]) == 4 and not r["cached"]
+        assert torch.equal(g.u, before)
+        r2 = autotune.tune(g, cool=True, chunks=(8, 16), tiles=(32, 64), steps=1)
+        assert r2["cached"] and (r2["chunk"], r2["tile"]) == (r["chunk"], r["tile"])
+    finally:
+        gb.set_launch_config(16, 32)

@@ -1,0 +1,96 @@
+"""Autotuner for the launch shapes of the step.
+
+Times the whole step (the replayed CUDA graph of gb_step_graph) for each
+candidate (blocks per chunk, reconstruction tile) on the registered grid,
+restoring the grid's state after every trial so tuning does not advance the
+simulation, and keeps the fastest. Results are cached per device, block
+count, physics and precision in a JSON file beside this module (or the path
+in GBHYDRO_TUNE_CACHE).
+"""
+from __future__ import annotations
+
+import json
+import os
+
+CHUNKS = (8, 16, 32, 64)
+TILES = (32, 64)
+CACHE = os.environ.get("GBHYDRO_TUNE_CACHE",
+                       os.path.join(os.path.dirname(os.path.abspath(__file__)), "_tune_cache.json"))
+
+
+def _key(grid, cool: bool) -> str:
+    import torch
+    from . import gbhydro as G
+    st = G.state
+    return (f"{torch.cuda.get_device_name()}|leaves={len(grid.leaf)}|mhd={int(grid.mhd)}|"
+            f"precision={st['precision']}|cool={int(cool)}|surrogate={int(st['surrogate'])}")
+
+
+def _load() -> dict:
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _save(d: dict) -> None:
+    tmp = CACHE + ".tmp"
+    try:
+        with open(tmp, "w") as f:
+            json.dump(d, f, indent=1, sort_keys=True)
+        os.replace(tmp, CACHE)
+    except OSError:
+        pass
+
+
+def time_config(grid, cool: bool, chunk: int, tile: int, steps: int = 3, warmup: int = 1) -> float:
+    """ms per step of the graph-replayed step at one launch shape."""
+    import torch
+    from . import gbhydro as G
+    G.set_launch_config(chunk, tile)
+    s = torch.cuda.current_stream()
+    for _ in range(warmup):
+        grid.step_graph(cool)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s)
+    for _ in range(steps):
+        grid.step_graph(cool)
+    b.record(s)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def tune(grid, cool: bool = True, chunks=CHUNKS, tiles=TILES, steps: int = 3, use_cache: bool = True) -> dict:
+    """Pick and set the fastest (chunk, tile) for `grid` (registered, with
+    hydro/cooling configured). Returns {"chunk", "tile", "ms", "trials",
+    "cached"}."""
+    import torch
+    from . import gbhydro as G
+    key = _key(grid, cool)
+    cache = _load() if use_cache else {}
+    if key in cache:
+        r = dict(cache[key], cached=True)
+        G.set_launch_config(r["chunk"], r["tile"])
+        return r
+    saved = [grid.u.clone()] + ([a.clone() for a in (grid.fx, grid.fy, grid.fz)] if grid.mhd else [])
+    trials = []
+    try:
+        for c in chunks:
+            for t in tiles:
+                ms = time_config(grid, cool, c, t, steps=steps)
+                trials.append({"chunk": c, "tile": t, "ms": ms})
+                grid.u.copy_(saved[0])
+                if grid.mhd:
+                    for a, b in zip((grid.fx, grid.fy, grid.fz), saved[1:]):
+                        a.copy_(b)
+    finally:
+        del saved
+        torch.cuda.synchronize()
+    best = min(trials, key=lambda r: r["ms"])
+    G.set_launch_config(best["chunk"], best["tile"])
+    r = {"chunk": best["chunk"], "tile": best["tile"], "ms": best["ms"], "trials": trials}
+    if use_cache:
+        cache[key] = r
+        _save(cache)
+    return dict(r, cached=False)

@@ -165,6 +165,7 @@ extern "C" int gb_register_grid(const gb_grid_desc* grid, const gb_tree_desc* tr
     g_gb.grid.f[2] = grid->facez;
     g_gb.grid.level = nullptr;
     g_gb.grid_ok = true;
+    g_gb.gen += 1;
     g_gb.tree_ok = false;
     if (tree) {
         if (tree->nnodes < grid->maxblocks || !tree->level || !tree->coord || !tree->child || !tree->root ||
@@ -187,6 +188,7 @@ extern "C" int gb_hydro_init(const gb_hydro_params* p)
     }
     g_gb.hp = *p;
     g_gb.hydro_ok = true;
+    g_gb.gen += 1;
     if (!g_gb.d_dtmin && gb_check(cudaMalloc(&g_gb.d_dtmin, sizeof(unsigned long long)), "cudaMalloc(dtmin)"))
         return GB_ERR_CUDA;
     return GB_OK;
@@ -332,6 +334,8 @@ __global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restri
     }
 }
 
+__global__ void k_dt_init(unsigned long long* bits) { *bits = 0x7FF0000000000000ULL; }  // +inf
+
 __global__ void k_dt_finish(const unsigned long long* bits, double cfl, double* out)
 {
     *out = cfl * __longlong_as_double((long long)*bits);
@@ -416,17 +420,42 @@ int gb_dt_launch(const gbh::hydro_kparams& kp, int mhd, int nblk, const int* lis
                  unsigned long long* bits, cudaStream_t s);
 
 static int g_chunk_blocks = 16;
+static int g_recon_tile = 32;
+
+int gb_chunk_blocks() { return g_chunk_blocks; }
+int gb_recon_tile() { return g_recon_tile; }
+
+extern "C" int gb_set_launch_config(int chunk_blocks, int recon_tile)
+{
+    if (chunk_blocks < 1 || chunk_blocks > 65535 || (recon_tile != 32 && recon_tile != 64)) {
+        gb_set_error("gb_set_launch_config: chunk %d (1..65535), recon tile %d (32 or 64)", chunk_blocks, recon_tile);
+        return GB_ERR_ARG;
+    }
+    g_chunk_blocks = chunk_blocks;
+    g_recon_tile = recon_tile;
+    g_gb.gen += 1;
+    return GB_OK;
+}
+
+extern "C" int gb_get_launch_config(int* chunk_blocks, int* recon_tile)
+{
+    if (chunk_blocks) *chunk_blocks = g_chunk_blocks;
+    if (recon_tile) *recon_tile = g_recon_tile;
+    return GB_OK;
+}
 
 extern "C" int gb_set_chunk_blocks(int n)
 {
     if (n < 1 || n > 65535) return GB_ERR_ARG;
     g_chunk_blocks = n;
+    g_gb.gen += 1;
     return GB_OK;
 }
 
-static gbh::hydro_kparams make_kp(double dt)
+static gbh::hydro_kparams make_kp(double dt, const double* dtp = nullptr)
 {
     gbh::hydro_kparams kp;
+    kp.dtp = dtp;
     kp.gamma = g_gb.hp.gamma;
     kp.cvisc = g_gb.hp.cvisc;
     kp.eint_switch = g_gb.hp.eint_switch;
@@ -445,16 +474,17 @@ static gbh::hydro_kparams make_kp(double dt)
 }
 
 int gb_cooling_mode();
-int gb_launch_surrogate(int nblk, const int* list, double dt, gb_status* st, cudaStream_t s);
+int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp, gb_status* st, cudaStream_t s);
 
-int gb_launch_hydro(int nblk, const int* list, double dt, int cool, gb_status* st, cudaStream_t s)
+int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int cool, gb_status* st,
+                    cudaStream_t s)
 {
     const int chunk = g_chunk_blocks < nblk ? g_chunk_blocks : nblk;
     const bool mixed = g_gb.hp.precision == 1;
     size_t per = mixed ? gb_hydro_scratch_bytes_mixed() : gb_hydro_scratch_bytes_fp64();
     int rc = gb_ensure_scratch(per * (size_t)chunk);
     if (rc) return rc;
-    gbh::hydro_kparams kp = make_kp(dt);
+    gbh::hydro_kparams kp = make_kp(dt, dtp);
     for (int b0 = 0; b0 < nblk; b0 += chunk) {
         int nb = nblk - b0 < chunk ? nblk - b0 : chunk;
         const int fused = cool && gb_cooling_mode() == 0;
@@ -462,7 +492,7 @@ int gb_launch_hydro(int nblk, const int* list, double dt, int cool, gb_status* s
                    : gb_hydro_chunk_fp64(kp, g_gb.hp.mhd, fused, nb, list + b0, g_gb.d_scratch, st, s);
         if (rc) return rc;
         if (cool && !fused) {
-            rc = gb_launch_surrogate(nb, list + b0, dt, st, s);
+            rc = gb_launch_surrogate(nb, list + b0, dt, dtp, st, s);
             if (rc) return rc;
         }
     }
@@ -487,15 +517,12 @@ extern "C" int gb_hydro_unsplit(int blockCount, const int* list, double dt, doub
         return GB_ERR_ARG;
     }
     if (blockCount == 0) return GB_OK;
-    return gb_launch_hydro(blockCount, list, dt, 0, st, (cudaStream_t)stream);
+    return gb_launch_hydro(blockCount, list, dt, nullptr, 0, st, (cudaStream_t)stream);
 }
 
 int gb_launch_dt(int nblk, const int* list, double* dt_out, cudaStream_t s)
 {
-    const unsigned long long inf_bits = 0x7FF0000000000000ULL;
-    if (gb_check(cudaMemcpyAsync(g_gb.d_dtmin, &inf_bits, sizeof inf_bits, cudaMemcpyHostToDevice, s),
-                 "dt init"))
-        return GB_ERR_CUDA;
+    k_dt_init<<<1, 1, 0, s>>>((unsigned long long*)g_gb.d_dtmin);
     gbh::hydro_kparams kp = make_kp(1.0);
     gb_prof_begin(GBP_DT, s);
     int rc = gb_dt_launch(kp, g_gb.hp.mhd, nblk, list, (unsigned long long*)g_gb.d_dtmin, s);
@@ -537,7 +564,127 @@ extern "C" int gb_evolve_step(int blockCount, const int* list, double dt, int co
     cudaStream_t s = (cudaStream_t)stream;
     int rc = gb_launch_guardfill(blockCount, list, s);
     if (rc) return rc;
-    return gb_launch_hydro(blockCount, list, dt, cool, st, s);
+    return gb_launch_hydro(blockCount, list, dt, nullptr, cool, st, s);
+}
+
+// ---------------------------------------------------------------- step graph
+// The whole step -- CFL reduction into dt_dev, guard fill, every hydro
+// chunk, cooling -- captured once as a CUDA graph on a private stream and
+// replayed on the caller's stream. Kernels read dt from dt_dev, so the
+// host never waits inside a step. The graph is re-captured whenever an
+// argument or anything it baked in (gen) changes.
+namespace {
+struct step_graph {
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cap = nullptr;
+    const int* list = nullptr;
+    int n = 0, cool = -1;
+    double* dt_dev = nullptr;
+    gb_status* st = nullptr;
+    unsigned long long gen = ~0ULL;
+    long long launches = 0, captures = 0, kernel_nodes = 0;
+} g_graph;
+
+void graph_drop()
+{
+    if (g_graph.exec) cudaGraphExecDestroy(g_graph.exec);
+    g_graph.exec = nullptr;
+}
+
+int record_step(int n, const int* list, int cool, double* dt_dev, gb_status* st, cudaStream_t s)
+{
+    int rc = gb_launch_dt(n, list, dt_dev, s);
+    if (rc) return rc;
+    rc = gb_launch_guardfill(n, list, s);
+    if (rc) return rc;
+    return gb_launch_hydro(n, list, 1.0, dt_dev, cool, st, s);
+}
+}  // namespace
+
+int gb_cooling_mode();
+
+extern "C" int gb_step_graph(int blockCount, const int* list, int cool, double* dt_dev, gb_status* st,
+                             void* stream)
+{
+    if (!g_gb.grid_ok || !g_gb.hydro_ok || !g_gb.tree_ok) {
+        gb_set_error("gb_step_graph: register grid + tree and call gb_hydro_init first");
+        return GB_ERR_NOT_INIT;
+    }
+    if (cool && (!g_gb.cool_ok || g_gb.grid.slot[GB_TEMP] < 0 || g_gb.grid.slot[GB_TDUS] < 0)) {
+        gb_set_error("gb_step_graph: cooling needs gb_cool_init and TEMP/TDUS slots");
+        return GB_ERR_NOT_INIT;
+    }
+    if (blockCount <= 0 || !list || !dt_dev) {
+        gb_set_error("gb_step_graph: bad block list or dt pointer");
+        return GB_ERR_ARG;
+    }
+    if (gb_prof_is_on()) {
+        gb_set_error("gb_step_graph: the in-library profiler times launches one by one; disable it first");
+        return GB_ERR_ARG;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool same = g_graph.exec && g_graph.list == list && g_graph.n == blockCount && g_graph.cool == cool &&
+                      g_graph.dt_dev == dt_dev && g_graph.st == st && g_graph.gen == g_gb.gen;
+    if (!same) {
+        graph_drop();
+        if (!g_graph.cap && gb_check(cudaStreamCreateWithFlags(&g_graph.cap, cudaStreamNonBlocking), "graph stream"))
+            return GB_ERR_CUDA;
+        // everything that allocates or uploads happens before the capture
+        const int chunk = gb_chunk_blocks() < blockCount ? gb_chunk_blocks() : blockCount;
+        size_t per = g_gb.hp.precision == 1 ? gb_hydro_scratch_bytes_mixed() : gb_hydro_scratch_bytes_fp64();
+        int rc = gb_ensure_scratch(per * (size_t)chunk);
+        if (!rc && cool && gb_cooling_mode() == 1) rc = gb_sur_prepare((int64_t)chunk * 4096, s);
+        if (rc) return rc;
+        if (gb_check(cudaStreamSynchronize(s), "graph prepare")) return GB_ERR_CUDA;
+        if (gb_check(cudaStreamBeginCapture(g_graph.cap, cudaStreamCaptureModeThreadLocal), "begin capture"))
+            return GB_ERR_CUDA;
+        rc = record_step(blockCount, list, cool, dt_dev, st, g_graph.cap);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(g_graph.cap, &graph);
+        if (rc || gb_check(e, "end capture")) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc ? rc : GB_ERR_CUDA;
+        }
+        size_t nn = 0;
+        cudaGraphGetNodes(graph, nullptr, &nn);
+        std::vector<cudaGraphNode_t> nodes(nn);
+        long long kn = 0;
+        if (nn && cudaGraphGetNodes(graph, nodes.data(), &nn) == cudaSuccess)
+            for (size_t q = 0; q < nn; ++q) {
+                cudaGraphNodeType ty;
+                if (cudaGraphNodeGetType(nodes[q], &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) ++kn;
+            }
+        g_graph.kernel_nodes = kn;
+        e = cudaGraphInstantiate(&g_graph.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (gb_check(e, "graph instantiate")) {
+            g_graph.exec = nullptr;
+            return GB_ERR_CUDA;
+        }
+        g_graph.list = list;
+        g_graph.n = blockCount;
+        g_graph.cool = cool;
+        g_graph.dt_dev = dt_dev;
+        g_graph.st = st;
+        g_graph.gen = g_gb.gen;
+        g_graph.captures += 1;
+    }
+    g_graph.launches += 1;
+    return gb_check(cudaGraphLaunch(g_graph.exec, s), "graph launch") ? GB_ERR_CUDA : GB_OK;
+}
+
+extern "C" int gb_graph_info(long long* captures, long long* launches, long long* kernel_nodes)
+{
+    if (captures) *captures = g_graph.captures;
+    if (launches) *launches = g_graph.launches;
+    if (kernel_nodes) *kernel_nodes = g_graph.exec ? g_graph.kernel_nodes : 0;
+    return GB_OK;
+}
+
+extern "C" int gb_graph_reset(void)
+{
+    graph_drop();
+    return GB_OK;
 }
 
 // ---------------------------------------------------------------- host I/O

@@ -196,6 +196,7 @@ extern "C" int gb_set_brent_tolerance(double kelvin)
     }
     g_brent_tol_K = kelvin;
     g_gb.cool.brent_tol_K = kelvin;
+    g_gb.gen += 1;
     return GB_OK;
 }
 
@@ -239,6 +240,7 @@ extern "C" int gb_cool_init(const char* path, const gb_cool_params* p)
     g_gb.cool.T_min = h[0];
     g_gb.cool.nd_min = h[GB_TEMP_PTS];
     g_gb.cool_ok = true;
+    g_gb.gen += 1;
     return GB_OK;
 }
 
@@ -396,10 +398,12 @@ __device__ __forceinline__ void cell_of(int64_t idx, const int* list, int& blk, 
 
 // features + the rate at the old state
 __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double gamma, const int* __restrict__ list,
-                           int64_t ncell, double dt_code, float* __restrict__ feat, float2* __restrict__ f0out)
+                           int64_t ncell, double dt_code, const double* __restrict__ dtp, float* __restrict__ feat,
+                           float2* __restrict__ f0out)
 {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= ncell) return;
+    if (dtp) dt_code = *dtp;
     int blk, ci, i, j, k;
     cell_of(idx, list, blk, ci, i, j, k);
     gb_cool_vars v;
@@ -437,11 +441,13 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double g
 // fallback list and the plain integrator solves it.
 template <bool CHECK64>
 __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double gamma, const int* __restrict__ list,
-                             int64_t ncell, double dt_code, const float* __restrict__ y, const float2* __restrict__ f0a,
-                             double rel_tol, int* __restrict__ rej, int* __restrict__ nrej, gb_status* st)
+                             int64_t ncell, double dt_code, const double* __restrict__ dtp, const float* __restrict__ y,
+                             const float2* __restrict__ f0a, double rel_tol, int* __restrict__ rej,
+                             int* __restrict__ nrej, gb_status* st)
 {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= ncell) return;
+    if (dtp) dt_code = *dtp;
     int blk, ci, i, j, k;
     cell_of(idx, list, blk, ci, i, j, k);
     const gb_cool_params& p = c.p;
@@ -525,11 +531,12 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double
 
 // rejected cells: the plain implicit integrator (RadHeat.F90:223-423)
 __global__ void k_sur_fallback(gb_dev_grid g, gb_cool_ctx c, double gamma, const int* __restrict__ list,
-                               double dt_code, const int* __restrict__ rej, const int* __restrict__ nrej,
+                               double dt_code, const double* __restrict__ dtp, const int* __restrict__ rej, const int* __restrict__ nrej,
                                gb_status* st)
 {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= *nrej) return;
+    if (dtp) dt_code = *dtp;
     int blk, ci, i, j, k;
     cell_of(rej[q], list, blk, ci, i, j, k);
     gb_cool_vars v;
@@ -613,7 +620,13 @@ int sur_ensure(int64_t ncell)
 
 int gb_cooling_mode() { return g_cool_mode; }
 
-int gb_launch_surrogate(int nblk, const int* list, double dt, gb_status* st, cudaStream_t s)
+int gb_sur_prepare(int64_t ncell, cudaStream_t s)
+{
+    int rc = sur_ensure(ncell);
+    return rc ? rc : gb_mlp_pack(s);
+}
+
+int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp, gb_status* st, cudaStream_t s)
 {
     const int64_t ncell = (int64_t)nblk * 4096;
     int rc = sur_ensure(ncell);
@@ -621,7 +634,7 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, gb_status* st, cud
     const unsigned nb = (unsigned)((ncell + 127) / 128);
     gb_prof_begin(GBP_SUR_FEAT, s);
     const gb_cool_pf pf = make_pf(g_gb.cool.p);
-    k_sur_feat<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, g_sb.feat, g_sb.f0);
+    k_sur_feat<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, dtp, g_sb.feat, g_sb.f0);
     gb_prof_end(GBP_SUR_FEAT, s);
     gb_prof_begin(GBP_MLP, s);
     rc = gb_mlp_launch_infer(ncell, g_sb.feat, g_sb.y, s);
@@ -630,14 +643,14 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, gb_status* st, cud
     cudaMemsetAsync(g_sb.nrej, 0, sizeof(int), s);
     gb_prof_begin(GBP_SUR_ACCEPT, s);
     if (g_sur_check64)
-        k_sur_accept<true><<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, g_sb.y, g_sb.f0,
+        k_sur_accept<true><<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, dtp, g_sb.y, g_sb.f0,
                                               g_sur_tol, g_sb.rej, g_sb.nrej, st);
     else
-        k_sur_accept<false><<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, g_sb.y, g_sb.f0,
+        k_sur_accept<false><<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, dtp, g_sb.y, g_sb.f0,
                                                g_sur_tol, g_sb.rej, g_sb.nrej, st);
     gb_prof_end(GBP_SUR_ACCEPT, s);
     gb_prof_begin(GBP_SUR_FALLBACK, s);
-    k_sur_fallback<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, dt, g_sb.rej, g_sb.nrej, st);
+    k_sur_fallback<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, dt, dtp, g_sb.rej, g_sb.nrej, st);
     gb_prof_end(GBP_SUR_FALLBACK, s);
     return gb_check(cudaGetLastError(), "surrogate launch") ? GB_ERR_CUDA : GB_OK;
 }
@@ -646,6 +659,7 @@ extern "C" int gb_set_cooling_mode(int mode, double rel_tol, int check_fp64)
 {
     if (mode < 0 || mode > 1 || !(rel_tol > 0.0) || rel_tol > 0.5) return GB_ERR_ARG;
     g_cool_mode = mode;
+    g_gb.gen += 1;
     g_sur_tol = rel_tol;
     g_sur_check64 = check_fp64 ? 1 : 0;
     return GB_OK;

@@ -24,6 +24,9 @@ struct gb_state_t {
     double* d_dtmin = nullptr;
     int* d_all_blocks = nullptr;
     int all_blocks_n = 0;
+    // bumped by every call that changes what a captured step graph baked
+    // in (grid, tree, parameters, tables, weights, modes)
+    unsigned long long gen = 0;
 };
 
 extern gb_state_t g_gb;
@@ -34,6 +37,11 @@ int gb_ensure_stage(size_t bytes);
 
 // kernels launched from other translation units
 int gb_launch_cool_blocks(int nblk, const int* list, double dt, gb_status* st, cudaStream_t s);
-int gb_launch_hydro(int nblk, const int* list, double dt, int cool, gb_status* st, cudaStream_t s);
+int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int cool, gb_status* st,
+                    cudaStream_t s);
 int gb_launch_dt(int nblk, const int* list, double* dt_out, cudaStream_t s);
 int gb_launch_guardfill(int nblk, const int* list, cudaStream_t s);
+int gb_sur_prepare(int64_t ncell, cudaStream_t s);
+// launch shapes chosen by the autotuner (gb_set_launch_config)
+int gb_chunk_blocks();
+int gb_recon_tile();

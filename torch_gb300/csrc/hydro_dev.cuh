@@ -33,7 +33,6 @@ constexpr int NFC = 17 * RB * RB;             // faces per direction in the flux
 constexpr int NFLX = 10;                      // 8 fluxes + rho*e_int flux + face velocity
 constexpr int NEDGE = 16 * 17 * 17;           // edges per direction
 constexpr int NFB = 17 * 16 * 16;             // interior faces per direction
-constexpr int RECON_TILE = 32;
 
 constexpr int NP32 = 9;  // FP32 copy of the primitives: rho, vx, vy, vz, p, Bx, By, Bz, e_int
 
@@ -305,7 +304,12 @@ struct hydro_kparams {
     double gamma, cvisc, eint_switch, smlrho, smallp;
     int use_avisc;
     double dt, dx[3];
+    // when set, the step's dt is read from device memory (written by the
+    // CFL reduction earlier in the same stream or graph) instead of dt
+    const double* dtp;
 };
+
+__device__ __forceinline__ double kp_dt(const hydro_kparams& kp) { return kp.dtp ? *kp.dtp : kp.dt; }
 
 // primitive 8-vector of a cell of the padded block
 template <typename T, bool MHD>
@@ -339,28 +343,29 @@ __device__ __forceinline__ void load_prim(const gb_dev_grid& g, int blk, int ci,
 }
 
 // ---------------------------------------------------------------- k_recon
-// blockDim = 3 * RECON_TILE: warp d reconstructs direction d for 32 cells.
-template <typename T, bool MHD>
-__global__ void __launch_bounds__(3 * RECON_TILE)
+// blockDim = 3 * TILE: threads [d TILE, (d + 1) TILE) reconstruct direction d
+// for TILE cells (TILE a multiple of 32, so every warp has one direction).
+template <typename T, bool MHD, int TILE>
+__global__ void __launch_bounds__(3 * TILE)
 k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __restrict__ scr,
         size_t scr_stride, const float* __restrict__ p32, size_t p32_stride, gb_status* st)
 {
     constexpr int nv = MHD ? 8 : 5;
-    __shared__ T s_sig[3][NP][RECON_TILE];
-    __shared__ T s_abn[3][NP][RECON_TILE];
-    __shared__ T s_dnb[3][RECON_TILE];
-    const int lane = threadIdx.x % RECON_TILE;
-    const int d = threadIdx.x / RECON_TILE;
+    __shared__ T s_sig[3][NP][TILE];
+    __shared__ T s_abn[3][NP][TILE];
+    __shared__ T s_dnb[3][TILE];
+    const int lane = threadIdx.x % TILE;
+    const int d = threadIdx.x / TILE;
     const int cb = blockIdx.y;
     const int blk = list[cb];
-    const int cell = blockIdx.x * RECON_TILE + lane;
+    const int cell = blockIdx.x * TILE + lane;
     const bool active = cell < NRC;
     const int cc = active ? cell : 0;
     const int i = RLO + cc % RB, j = RLO + (cc / RB) % RB, k = RLO + cc / (RB * RB);
     const T gam = (T)kp.gamma;
     double dxl[3];
     gb_block_dx(g, kp.dx, blk, dxl);
-    const T hd[3] = {(T)(0.5 * kp.dt / dxl[0]), (T)(0.5 * kp.dt / dxl[1]), (T)(0.5 * kp.dt / dxl[2])};
+    const T hd[3] = {(T)(0.5 * kp_dt(kp) / dxl[0]), (T)(0.5 * kp_dt(kp) / dxl[1]), (T)(0.5 * kp_dt(kp) / dxl[2])};
 
     // normal-direction PPM in direction d
     T qs[5][NP];
@@ -373,7 +378,7 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
         for (int s = 0; s < NP; ++s) qs[m][s] = w[rot_slot(d, s)];
     }
     T wpr[NP], wnr[NP], sgr[NP];
-    ppm_normal<T, MHD>(gam, qs, (T)(kp.dt / dxl[d]), wpr, wnr, sgr);
+    ppm_normal<T, MHD>(gam, qs, (T)(kp_dt(kp) / dxl[d]), wpr, wnr, sgr);
     T wp[NP], wn[NP];
 #pragma unroll
     for (int s = 0; s < NP; ++s) {
@@ -841,7 +846,7 @@ k_faceb(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const dou
     double eb1 = es[(size_t)bb * NEDGE + edge_index(bb, t3[0], t3[1], t3[2])];
     double dxl[3];
     gb_block_dx(g, kp.dx, blk, dxl);
-    double dtd_b = kp.dt / dxl[bb], dtd_c = kp.dt / dxl[c];
+    double dtd_b = kp_dt(kp) / dxl[bb], dtd_c = kp_dt(kp) / dxl[c];
     double old = g.f[a][(int64_t)blk * GB_FSZ + gb_fidx(a, I[0], I[1], I[2])];
     bscr[(size_t)cb * bstride + (size_t)a * NFB + f] = old - dtd_b * (ec1 - ec0) + dtd_c * (eb1 - eb0);
 }
@@ -876,7 +881,7 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
     const int fp[3] = {flux_index(0, i + 1, j, k), flux_index(1, i, j + 1, k), flux_index(2, i, j, k + 1)};
     double dxl[3];
     gb_block_dx(g, kp.dx, blk, dxl);
-    const double dtd[3] = {kp.dt / dxl[0], kp.dt / dxl[1], kp.dt / dxl[2]};
+    const double dtd[3] = {kp_dt(kp) / dxl[0], kp_dt(kp) / dxl[1], kp_dt(kp) / dxl[2]};
     auto F = [&](int d, int var, int idx) -> double {
         return (double)fs[(size_t)d * NFLX * NFC + (size_t)var * NFC + idx];
     };
@@ -888,7 +893,7 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
     double divv = (F(0, 9, fp[0]) - F(0, 9, fm[0])) / dxl[0] + (F(1, 9, fp[1]) - F(1, 9, fm[1])) / dxl[1] +
                   (F(2, 9, fp[2]) - F(2, 9, fm[2])) / dxl[2];
     double ren = re - dtd[0] * (F(0, 8, fp[0]) - F(0, 8, fm[0])) - dtd[1] * (F(1, 8, fp[1]) - F(1, 8, fm[1])) -
-                 dtd[2] * (F(2, 8, fp[2]) - F(2, 8, fm[2])) - kp.dt * pr * divv;
+                 dtd[2] * (F(2, 8, fp[2]) - F(2, 8, fm[2])) - kp_dt(kp) * pr * divv;
     double Bn[3] = {0.0, 0.0, 0.0};
     if (MHD) {
         const double* bs = bscr + (size_t)cb * bstride;
@@ -937,7 +942,7 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
         v.mu_mol = p.mu_mol;
         v.strat_factor = 1.0;
         gb_cool_diag dg = {0, 0, 0, 0, 0};
-        gbcool::heating_and_cooling(cool, v, &eic, kp.dt * p.time_unit, &temp, &dg);
+        gbcool::heating_and_cooling(cool, v, &eic, kp_dt(kp) * p.time_unit, &temp, &dg);
         bool clamped = false;
         if (temp > p.absTmax) {
             eic = p.absTmax * v.TtoEI;

@@ -29,11 +29,13 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
         else k_prim32<false><<<pg, 128, 0, s>>>(g, list, p32, SL::prim32);
         gb_prof_end(GBP_RECON, s);
     }
-    dim3 rg((NRC + RECON_TILE - 1) / RECON_TILE, nblk);
+    const int tile = gb_recon_tile();
+    dim3 rg((NRC + tile - 1) / tile, nblk);
     dim3 fg((NFC + 127) / 128, 3, nblk);
     if (mhd) {
         gb_prof_begin(GBP_RECON, s);
-        k_recon<T, true><<<rg, 3 * RECON_TILE, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+        if (tile == 64) k_recon<T, true, 64><<<rg, 3 * 64, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+        else k_recon<T, true, 32><<<rg, 3 * 32, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
         gb_prof_end(GBP_RECON, s);
         gb_prof_begin(GBP_FLUX, s);
         k_flux<T, true><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);
@@ -48,7 +50,8 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
         gb_prof_end(GBP_FACEB, s);
     } else {
         gb_prof_begin(GBP_RECON, s);
-        k_recon<T, false><<<rg, 3 * RECON_TILE, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+        if (tile == 64) k_recon<T, false, 64><<<rg, 3 * 64, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+        else k_recon<T, false, 32><<<rg, 3 * 32, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
         gb_prof_end(GBP_RECON, s);
         gb_prof_begin(GBP_FLUX, s);
         k_flux<T, false><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);

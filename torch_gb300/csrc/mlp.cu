@@ -411,6 +411,7 @@ extern "C" int gb_mlp_set_weights(const float* host, int n)
     cudaMemset(g_mlp.v, 0, sizeof(float) * NPAR);
     g_mlp.step = 0;
     g_mlp.packed = false;
+    g_gb.gen += 1;
     return GB_OK;
 }
 
@@ -483,6 +484,7 @@ extern "C" int gb_mlp_train(const float* feat, const float* target, int64_t n, i
     cudaStreamSynchronize(s);
     cudaFreeHost(hidx);
     g_mlp.packed = false;
+    g_gb.gen += 1;
     return gb_check(cudaGetLastError(), "mlp train") ? GB_ERR_CUDA : GB_OK;
 }
 

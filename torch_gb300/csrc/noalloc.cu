@@ -90,6 +90,7 @@ extern "C" int gb_hydro_unsplit_noalloc(int blockCount, const int* blockList_dev
     kp.smallp = g_gb.hp.smallp;
     kp.use_avisc = g_gb.hp.use_avisc;
     kp.dt = dt;
+    kp.dtp = nullptr;
     for (int d = 0; d < 3; ++d) kp.dx[d] = g_gb.tree_ok ? g_gb.tree.root_dx[d] : 1.0;
     return gbh::launch_chunk<double>(kp, g_gb.hp.mhd, 0, blockCount, blockList_dev, scratch, st_dev,
                                      (cudaStream_t)stream);

@@ -97,6 +97,11 @@ _SIG = {
     "gb_hydro_init": (C.c_int, [C.POINTER(HydroParams)]),
     "gb_hydro_unsplit": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_void_p]),
     "gb_set_chunk_blocks": (C.c_int, [C.c_int]),
+    "gb_set_launch_config": (C.c_int, [C.c_int, C.c_int]),
+    "gb_get_launch_config": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "gb_step_graph": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gb_graph_reset": (C.c_int, []),
+    "gb_graph_info": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "gb_hydro_unsplit_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p,
                                            C.c_void_p]),
     "gb_compute_dt": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -295,14 +300,33 @@ class Grid:
         check(lib().gb_compute_dt(n, _ptr(lt), _ptr(out), _stream()), "gb_compute_dt")
         return out
 
+    def step_graph(self, cool: bool, dt_out=None, blockList=None):
+        """One whole step (device dt, guard fill, hydro, cooling) as a
+        replayed CUDA graph; returns the device tensor holding its dt."""
+        lt, n = self.list_tensor(blockList)
+        if blockList is not None:
+            self._graph_list = lt  # the graph keeps the pointer
+        if dt_out is None:
+            if getattr(self, "_dt_dev", None) is None:
+                self._dt_dev = self.torch.zeros(1, dtype=self.torch.float64, device=self.u.device)
+            dt_out = self._dt_dev
+        check(lib().gb_step_graph(n, _ptr(lt), int(cool), _ptr(dt_out), _ptr(self.status), _stream()),
+              "gb_step_graph")
+        return dt_out
+
     def evolve_step(self, dt: float, cool: bool, blockList=None):
         lt, n = self.list_tensor(blockList)
         check(lib().gb_evolve_step(n, _ptr(lt), float(dt), int(cool), _ptr(self.status), _stream()),
               "gb_evolve_step")
 
 
+# what the Python side last configured (keys of the autotuner's cache)
+state = {"precision": None, "mhd": None, "surrogate": False}
+
+
 def init_hydro(p: HydroParams) -> None:
     check(lib().gb_hydro_init(C.byref(p)), "gb_hydro_init")
+    state["precision"], state["mhd"] = int(p.precision), int(p.mhd)
 
 
 def init_cooling(p: CoolParams, table_path: str | None = None) -> None:
@@ -311,9 +335,26 @@ def init_cooling(p: CoolParams, table_path: str | None = None) -> None:
     check(lib().gb_cool_init(path.encode(), C.byref(p)), "gb_cool_init")
 
 
+def graph_info() -> tuple:
+    """(captures, replays, kernel launches per replay of the current graph)."""
+    a, b, k = C.c_longlong(), C.c_longlong(), C.c_longlong()
+    check(lib().gb_graph_info(C.byref(a), C.byref(b), C.byref(k)), "gb_graph_info")
+    return a.value, b.value, k.value
+
+
 def set_brent_tolerance(kelvin: float = 1.0) -> None:
     """Brent tolerance floor of the plain implicit step (1 K = heatCool.F90)."""
     check(lib().gb_set_brent_tolerance(float(kelvin)), "gb_set_brent_tolerance")
+
+
+def set_launch_config(chunk_blocks: int, recon_tile: int) -> None:
+    check(lib().gb_set_launch_config(int(chunk_blocks), int(recon_tile)), "gb_set_launch_config")
+
+
+def get_launch_config() -> tuple:
+    a, b = C.c_int(), C.c_int()
+    check(lib().gb_get_launch_config(C.byref(a), C.byref(b)), "gb_get_launch_config")
+    return a.value, b.value
 
 
 def set_chunk_blocks(n: int) -> None:
@@ -444,6 +485,7 @@ def mlp_infer(feat, tensor_cores: bool = True):
 
 def set_cooling_mode(surrogate: bool, rel_tol: float = 2e-3, check_fp64: bool = False):
     check(lib().gb_set_cooling_mode(int(surrogate), rel_tol, int(check_fp64)), "gb_set_cooling_mode")
+    state["surrogate"] = bool(surrogate)
 
 
 PROF_NAMES = ["guard_fill", "recon", "flux", "emf", "faceb", "update", "dt", "heat", "sur_feat", "mlp_infer",
