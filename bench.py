@@ -442,9 +442,8 @@ def main():
     run_path(G, g_tight, 1, args.steps, args.warmup)
     G.set_brent_tolerance(1.0)
     if world > 1:
-        t = torch.tensor([ms_plain, ms_fast], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_plain, ms_fast = t.tolist()
+        from torch_gb300.blocklist import max_over_ranks
+        ms_plain, ms_fast = max_over_ranks(ms_plain), max_over_ranks(ms_fast)
     # accuracy of the fast path against the plain one after the same steps
     lv = torch.as_tensor(leaves.astype(np.int64), device="cuda")
     a, b, c, d = g_plain.u, g_fast.u, g_mixed.u, g_tight.u
