@@ -813,9 +813,11 @@ int orc_unsplit_block(const orc_hydro_params* p, double* u, double* bxf, double*
                 for (int s = 0; s < NP; ++s)
                     Un[s] = Uc[s] - dtd[0] * (fxp->f[s] - fxm->f[s]) - dtd[1] * (fyp->f[s] - fym->f[s]) -
                             dtd[2] * (fzp->f[s] - fzm->f[s]);
-                double divv = (fxp->un - fxm->un) / dx + (fyp->un - fym->un) / dy + (fzp->un - fzm->un) / dz;
+                /* dt * div v from the face velocities, as sum_d (dt/dx_d) dv_d */
+                double dtdivv = dtd[0] * (fxp->un - fxm->un) + dtd[1] * (fyp->un - fym->un) +
+                                dtd[2] * (fzp->un - fzm->un);
                 double ren = re - dtd[0] * (fxp->feint - fxm->feint) - dtd[1] * (fyp->feint - fym->feint) -
-                             dtd[2] * (fzp->feint - fzm->feint) - dt * pr * divv;
+                             dtd[2] * (fzp->feint - fzm->feint) - pr * dtdivv;
                 double Bn[3] = {0, 0, 0};
                 if (p->mhd) {
                     Bn[0] = 0.5 * (fnew[0][fidx(n, 0, i, j, k)] + fnew[0][fidx(n, 0, i + 1, j, k)]);

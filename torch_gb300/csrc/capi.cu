@@ -189,7 +189,8 @@ extern "C" int gb_hydro_init(const gb_hydro_params* p)
     g_gb.hp = *p;
     g_gb.hydro_ok = true;
     g_gb.gen += 1;
-    if (!g_gb.d_dtmin && gb_check(cudaMalloc(&g_gb.d_dtmin, sizeof(unsigned long long)), "cudaMalloc(dtmin)"))
+    // [0]: bits of the CFL minimum, [1..3]: dt / root_dx of the last dt
+    if (!g_gb.d_dtmin && gb_check(cudaMalloc(&g_gb.d_dtmin, 4 * sizeof(double)), "cudaMalloc(dtmin)"))
         return GB_ERR_CUDA;
     return GB_OK;
 }
@@ -201,18 +202,23 @@ struct leaf_hit {
     int node, level;
 };
 
+// All positions are non-negative finest-cell coordinates and every size is
+// a power of two, so divisions are shifts: GB_NXB = 2^4 cells per block.
+static_assert(GB_NXB == 16, "block size 16 assumed by the shifts below");
+constexpr int LOG2_NXB = 4;
+
 __device__ __forceinline__ leaf_hit find_leaf(const gb_tree_desc& t, long long X, long long Y, long long Z)
 {
-    const long long S0 = (long long)GB_NXB << t.maxlevel;
-    int rx = (int)(X / S0), ry = (int)(Y / S0), rz = (int)(Z / S0);
+    const int sh0 = LOG2_NXB + t.maxlevel;
+    int rx = (int)(X >> sh0), ry = (int)(Y >> sh0), rz = (int)(Z >> sh0);
     int node = t.root[rx + t.nrx * (ry + t.nry * rz)];
     int l = 0;
     for (int it = 0; it <= t.maxlevel && node >= 0; ++it) {
-        int c0 = t.child[8 * node];
+        int c0 = __ldg(t.child + 8 * node);
         if (c0 < 0) break;
-        long long half = S0 >> (l + 1);
-        int cx = (int)((X / half) & 1), cy = (int)((Y / half) & 1), cz = (int)((Z / half) & 1);
-        node = t.child[8 * node + (cx | (cy << 1) | (cz << 2))];
+        const int sh = sh0 - 1 - l;
+        int cx = (int)((X >> sh) & 1), cy = (int)((Y >> sh) & 1), cz = (int)((Z >> sh) & 1);
+        node = __ldg(t.child + 8 * node + (cx | (cy << 1) | (cz << 2)));
         ++l;
     }
     leaf_hit h;
@@ -221,7 +227,9 @@ __device__ __forceinline__ leaf_hit find_leaf(const gb_tree_desc& t, long long X
     return h;
 }
 
-__device__ __forceinline__ long long wrap(long long x, long long n) { return ((x % n) + n) % n; }
+// periodic wrap of a guard position: x lies in (-n, 2n) (a guard region is
+// narrower than the domain)
+__device__ __forceinline__ long long wrap(long long x, long long n) { return x < 0 ? x + n : (x >= n ? x - n : x); }
 
 __global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list)
 {
@@ -233,7 +241,8 @@ __global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restri
         k >= GB_NGUARD && k < GB_NGUARD + GB_NXB)
         return;
     const int L = t.level[blk];
-    const long long s = 1LL << (t.maxlevel - L);
+    const int ls = t.maxlevel - L;  // log2 of this block's cell size in finest cells
+    const long long s = 1LL << ls;
     const long long N[3] = {(long long)t.nrx * GB_NXB << t.maxlevel, (long long)t.nry * GB_NXB << t.maxlevel,
                             (long long)t.nrz * GB_NXB << t.maxlevel};
     const int* cd = t.coord + 3 * blk;
@@ -241,27 +250,27 @@ __global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restri
     long long lo[3], X[3];
     for (int d = 0; d < 3; ++d) {
         lo[d] = wrap(((long long)cd[d] * GB_NXB + loc[d] - GB_NGUARD) * s, N[d]);
-        X[d] = lo[d] + s / 2;
+        X[d] = lo[d] + (s >> 1);
     }
     leaf_hit h = find_leaf(t, X[0], X[1], X[2]);
     if (h.node < 0) return;
-    const long long sl = 1LL << (t.maxlevel - h.level);
+    const int lsl = t.maxlevel - h.level;
     const int* sc = t.coord + 3 * h.node;
     double* dst = g.unk + (int64_t)blk * g.nvar * GB_N3 + c;
     const double* src = g.unk + (int64_t)h.node * g.nvar * GB_N3;
     if (h.level <= L) {
         // same level: copy; coarser: injection of the covering coarse cell
-        int si = (int)(X[0] / sl - (long long)sc[0] * GB_NXB) + GB_NGUARD;
-        int sj = (int)(X[1] / sl - (long long)sc[1] * GB_NXB) + GB_NGUARD;
-        int sk = (int)(X[2] / sl - (long long)sc[2] * GB_NXB) + GB_NGUARD;
+        int si = (int)((X[0] >> lsl) - (long long)sc[0] * GB_NXB) + GB_NGUARD;
+        int sj = (int)((X[1] >> lsl) - (long long)sc[1] * GB_NXB) + GB_NGUARD;
+        int sk = (int)((X[2] >> lsl) - (long long)sc[2] * GB_NXB) + GB_NGUARD;
         int sci = gb_cidx(si, sj, sk);
         for (int v = 0; v < g.nvar; ++v) dst[(int64_t)v * GB_N3] = src[(int64_t)v * GB_N3 + sci];
     } else {
         // finer neighbour: mean of the fine cells covering this cell
-        int r = (int)(s / sl);
-        int bi = (int)(lo[0] / sl - (long long)sc[0] * GB_NXB) + GB_NGUARD;
-        int bj = (int)(lo[1] / sl - (long long)sc[1] * GB_NXB) + GB_NGUARD;
-        int bk = (int)(lo[2] / sl - (long long)sc[2] * GB_NXB) + GB_NGUARD;
+        int r = 1 << (ls - lsl);
+        int bi = (int)((lo[0] >> lsl) - (long long)sc[0] * GB_NXB) + GB_NGUARD;
+        int bj = (int)((lo[1] >> lsl) - (long long)sc[1] * GB_NXB) + GB_NGUARD;
+        int bk = (int)((lo[2] >> lsl) - (long long)sc[2] * GB_NXB) + GB_NGUARD;
         double inv = 1.0 / (double)(r * r * r);
         for (int v = 0; v < g.nvar; ++v) {
             double acc = 0.0;
@@ -290,25 +299,26 @@ __global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restri
     }
     if (own) return;
     const int L = t.level[blk];
-    const long long s = 1LL << (t.maxlevel - L);
+    const int ls = t.maxlevel - L;  // log2 of this block's cell size in finest cells
+    const long long s = 1LL << ls;
     const long long N[3] = {(long long)t.nrx * GB_NXB << t.maxlevel, (long long)t.nry * GB_NXB << t.maxlevel,
                             (long long)t.nrz * GB_NXB << t.maxlevel};
     const int* cd = t.coord + 3 * blk;
     long long lo[3], X[3];
     for (int d = 0; d < 3; ++d) {
         lo[d] = wrap(((long long)cd[d] * GB_NXB + I[d] - GB_NGUARD) * s, N[d]);
-        X[d] = lo[d] + (d == a ? 0 : s / 2);
+        X[d] = lo[d] + (d == a ? 0 : (s >> 1));
     }
     leaf_hit h = find_leaf(t, X[0], X[1], X[2]);
     if (h.node < 0) return;
-    const long long sl = 1LL << (t.maxlevel - h.level);
+    const int lsl = t.maxlevel - h.level;
     const int* sc = t.coord + 3 * h.node;
     const double* src = g.f[a] + (int64_t)h.node * GB_FSZ;
     double* dst = g.f[a] + (int64_t)blk * GB_FSZ + f;
     if (h.level <= L) {
         int S[3];
-        for (int d = 0; d < 3; ++d) S[d] = (int)(X[d] / sl - (long long)sc[d] * GB_NXB) + GB_NGUARD;
-        if (X[a] % sl == 0) {
+        for (int d = 0; d < 3; ++d) S[d] = (int)((X[d] >> lsl) - (long long)sc[d] * GB_NXB) + GB_NGUARD;
+        if ((X[a] & ((1LL << lsl) - 1)) == 0) {
             *dst = src[gb_fidx(a, S[0], S[1], S[2])];
         } else {
             // fine face inside a coarse cell: mean of the two coarse faces
@@ -318,9 +328,9 @@ __global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restri
         }
     } else {
         // finer neighbour: area mean of the fine faces on this face
-        int r = (int)(s / sl);
+        int r = 1 << (ls - lsl);
         int B[3];
-        for (int d = 0; d < 3; ++d) B[d] = (int)(lo[d] / sl - (long long)sc[d] * GB_NXB) + GB_NGUARD;
+        for (int d = 0; d < 3; ++d) B[d] = (int)((lo[d] >> lsl) - (long long)sc[d] * GB_NXB) + GB_NGUARD;
         int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
         double acc = 0.0;
         for (int y = 0; y < r; ++y)
@@ -336,9 +346,15 @@ __global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restri
 
 __global__ void k_dt_init(unsigned long long* bits) { *bits = 0x7FF0000000000000ULL; }  // +inf
 
-__global__ void k_dt_finish(const unsigned long long* bits, double cfl, double* out)
+// dt = CFL x the minimum limit; also dt / root_dx for the step's kernels
+__global__ void k_dt_finish(const unsigned long long* bits, double cfl, double* out, double* dtdx, double dx0,
+                            double dx1, double dx2)
 {
-    *out = cfl * __longlong_as_double((long long)*bits);
+    const double dt = cfl * __longlong_as_double((long long)*bits);
+    *out = dt;
+    dtdx[0] = dt / dx0;
+    dtdx[1] = dt / dx1;
+    dtdx[2] = dt / dx2;
 }
 
 __global__ void k_flash_to_soa(const double* __restrict__ in, int nunk, const int* __restrict__ hslot,
@@ -456,6 +472,7 @@ static gbh::hydro_kparams make_kp(double dt, const double* dtp = nullptr)
 {
     gbh::hydro_kparams kp;
     kp.dtp = dtp;
+    kp.dtdxp = dtp ? g_gb.d_dtmin + 1 : nullptr;  // written by k_dt_finish
     kp.gamma = g_gb.hp.gamma;
     kp.cvisc = g_gb.hp.cvisc;
     kp.eint_switch = g_gb.hp.eint_switch;
@@ -470,6 +487,7 @@ static gbh::hydro_kparams make_kp(double dt, const double* dtp = nullptr)
     } else {
         kp.dx[0] = kp.dx[1] = kp.dx[2] = 1.0;
     }
+    for (int d = 0; d < 3; ++d) kp.dtdx0[d] = dt / kp.dx[d];
     return kp;
 }
 
@@ -527,7 +545,8 @@ int gb_launch_dt(int nblk, const int* list, double* dt_out, cudaStream_t s)
     gb_prof_begin(GBP_DT, s);
     int rc = gb_dt_launch(kp, g_gb.hp.mhd, nblk, list, (unsigned long long*)g_gb.d_dtmin, s);
     if (rc) return rc;
-    k_dt_finish<<<1, 1, 0, s>>>((const unsigned long long*)g_gb.d_dtmin, g_gb.hp.cfl, dt_out);
+    k_dt_finish<<<1, 1, 0, s>>>((const unsigned long long*)g_gb.d_dtmin, g_gb.hp.cfl, dt_out, g_gb.d_dtmin + 1,
+                                kp.dx[0], kp.dx[1], kp.dx[2]);
     gb_prof_end(GBP_DT, s);
     return gb_check(cudaGetLastError(), "k_dt_finish") ? GB_ERR_CUDA : GB_OK;
 }

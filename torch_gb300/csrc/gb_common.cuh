@@ -49,6 +49,11 @@ struct gb_dev_grid {
 };
 
 // cell size of a block: root cell size scaled by 2^-level (exact)
+// 2^l as a double, built from its exponent bits (0 <= l < 1023)
+__device__ __forceinline__ double gb_pow2(int l) { return __longlong_as_double((long long)(1023 + l) << 52); }
+
+__device__ __forceinline__ int gb_block_level(const gb_dev_grid& g, int blk) { return g.level ? __ldg(g.level + blk) : 0; }
+
 __device__ __forceinline__ void gb_block_dx(const gb_dev_grid& g, const double* dx0, int blk, double* dx)
 {
     double sc = g.level ? ldexp(1.0, -__ldg(g.level + blk)) : 1.0;

@@ -307,9 +307,28 @@ struct hydro_kparams {
     // when set, the step's dt is read from device memory (written by the
     // CFL reduction earlier in the same stream or graph) instead of dt
     const double* dtp;
+    // dt / root_dx per direction (dtdxp: its device copy, used with dtp).
+    // A level-l block has dx = root_dx 2^-l, so its dt/dx is this times 2^l,
+    // exactly, with no division in the kernels.
+    double dtdx0[3];
+    const double* dtdxp;
 };
 
 __device__ __forceinline__ double kp_dt(const hydro_kparams& kp) { return kp.dtp ? *kp.dtp : kp.dt; }
+
+__device__ __forceinline__ void kp_dtdx(const hydro_kparams& kp, int level, double* out)
+{
+    const double sc = gb_pow2(level);
+    if (kp.dtdxp) {
+        out[0] = kp.dtdxp[0] * sc;
+        out[1] = kp.dtdxp[1] * sc;
+        out[2] = kp.dtdxp[2] * sc;
+    } else {
+        out[0] = kp.dtdx0[0] * sc;
+        out[1] = kp.dtdx0[1] * sc;
+        out[2] = kp.dtdx0[2] * sc;
+    }
+}
 
 // primitive 8-vector of a cell of the padded block
 template <typename T, bool MHD>
@@ -363,9 +382,9 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
     const int cc = active ? cell : 0;
     const int i = RLO + cc % RB, j = RLO + (cc / RB) % RB, k = RLO + cc / (RB * RB);
     const T gam = (T)kp.gamma;
-    double dxl[3];
-    gb_block_dx(g, kp.dx, blk, dxl);
-    const T hd[3] = {(T)(0.5 * kp_dt(kp) / dxl[0]), (T)(0.5 * kp_dt(kp) / dxl[1]), (T)(0.5 * kp_dt(kp) / dxl[2])};
+    double dtd[3];
+    kp_dtdx(kp, gb_block_level(g, blk), dtd);
+    const T hd[3] = {(T)(0.5 * dtd[0]), (T)(0.5 * dtd[1]), (T)(0.5 * dtd[2])};
 
     // normal-direction PPM in direction d
     T qs[5][NP];
@@ -378,7 +397,7 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
         for (int s = 0; s < NP; ++s) qs[m][s] = w[rot_slot(d, s)];
     }
     T wpr[NP], wnr[NP], sgr[NP];
-    ppm_normal<T, MHD>(gam, qs, (T)(kp_dt(kp) / dxl[d]), wpr, wnr, sgr);
+    ppm_normal<T, MHD>(gam, qs, (T)dtd[d], wpr, wnr, sgr);
     T wp[NP], wn[NP];
 #pragma unroll
     for (int s = 0; s < NP; ++s) {
@@ -752,17 +771,24 @@ k_flux(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* _
 }
 
 // ---------------------------------------------------------------- k_emf
-__device__ __forceinline__ double upw(double f, double a, double b)
+template <typename R>
+__device__ __forceinline__ R upw(R f, R a, R b)
 {
-    return f > 0.0 ? a : (f < 0.0 ? b : 0.5 * (a + b));
+    return f > (R)0 ? a : (f < (R)0 ? b : (R)0.5 * (a + b));
 }
 
-// edge box of direction c: along c cells 4..19 (16), along a and b faces 4..20 (17)
+// edge box of direction c: along c cells 4..19 (16), along a and b faces 4..20 (17).
+// The electric field is computed in the reconstruction precision T from the
+// Riemann fluxes and the cell-centred v x B (FP32 copies of the primitives
+// in the mixed path); it is stored as double and the face-B update that
+// consumes it stays FP64. Every edge value is shared by the four faces
+// around the edge, so div B is kept to round-off in either precision.
 template <typename T>
 __global__ void __launch_bounds__(128)
 k_emf(gb_dev_grid g, const int* __restrict__ list, const T* __restrict__ fscr, size_t fstride,
-      double* __restrict__ escr, size_t estride)
+      double* __restrict__ escr, size_t estride, const float* __restrict__ p32, size_t p32_stride)
 {
+    using R = T;
     const int c = blockIdx.y;
     const int cb = blockIdx.z;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -771,35 +797,45 @@ k_emf(gb_dev_grid g, const int* __restrict__ list, const T* __restrict__ fscr, s
     const int a = (c + 1) % 3, b = (c + 2) % 3;
     const int A = LO + e % 17, B = LO + (e / 17) % 17, C = LO + e / (17 * 17);
     const T* fs = fscr + (size_t)cb * fstride;
-    auto fl = [&](int d, int var, int x0, int x1, int x2) -> double {
-        return (double)fs[(size_t)d * NFLX * NFC + (size_t)var * NFC + flux_index(d, x0, x1, x2)];
+    auto fl = [&](int d, int var, int x0, int x1, int x2) -> R {
+        return (R)fs[(size_t)d * NFLX * NFC + (size_t)var * NFC + flux_index(d, x0, x1, x2)];
     };
     int t[3];
     auto at = [&](int av, int bv, int cv) { t[a] = av; t[b] = bv; t[c] = cv; };
-    at(A, B - 1, C); double ea0 = -fl(a, 5 + b, t[0], t[1], t[2]); double ma0 = fl(a, 0, t[0], t[1], t[2]);
-    at(A, B, C);     double ea1 = -fl(a, 5 + b, t[0], t[1], t[2]); double ma1 = fl(a, 0, t[0], t[1], t[2]);
-    at(A - 1, B, C); double eb0 = fl(b, 5 + a, t[0], t[1], t[2]);  double mb0 = fl(b, 0, t[0], t[1], t[2]);
-    at(A, B, C);     double eb1 = fl(b, 5 + a, t[0], t[1], t[2]);  double mb1 = fl(b, 0, t[0], t[1], t[2]);
+    at(A, B - 1, C); R ea0 = -fl(a, 5 + b, t[0], t[1], t[2]); R ma0 = fl(a, 0, t[0], t[1], t[2]);
+    at(A, B, C);     R ea1 = -fl(a, 5 + b, t[0], t[1], t[2]); R ma1 = fl(a, 0, t[0], t[1], t[2]);
+    at(A - 1, B, C); R eb0 = fl(b, 5 + a, t[0], t[1], t[2]);  R mb0 = fl(b, 0, t[0], t[1], t[2]);
+    at(A, B, C);     R eb1 = fl(b, 5 + a, t[0], t[1], t[2]);  R mb1 = fl(b, 0, t[0], t[1], t[2]);
     const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
-    double ecc[2][2];
+    const float* pb = p32 + (size_t)cb * p32_stride;
+    R ecc[2][2];
 #pragma unroll
     for (int ia = 0; ia < 2; ++ia)
 #pragma unroll
         for (int ib = 0; ib < 2; ++ib) {
             at(A - 1 + ia, B - 1 + ib, C);
             int ci = gb_cidx(t[0], t[1], t[2]);
-            double va = base[(int64_t)g.slot[GB_VELX + a] * GB_N3 + ci];
-            double vb = base[(int64_t)g.slot[GB_VELX + b] * GB_N3 + ci];
-            double Ba = base[(int64_t)g.slot[GB_MAGX + a] * GB_N3 + ci];
-            double Bb = base[(int64_t)g.slot[GB_MAGX + b] * GB_N3 + ci];
+            R va, vb, Ba, Bb;
+            if constexpr (std::is_same<T, float>::value) {
+                va = pb[(size_t)(1 + a) * GB_N3 + ci];
+                vb = pb[(size_t)(1 + b) * GB_N3 + ci];
+                Ba = pb[(size_t)(5 + a) * GB_N3 + ci];
+                Bb = pb[(size_t)(5 + b) * GB_N3 + ci];
+            } else {
+                va = base[(int64_t)g.slot[GB_VELX + a] * GB_N3 + ci];
+                vb = base[(int64_t)g.slot[GB_VELX + b] * GB_N3 + ci];
+                Ba = base[(int64_t)g.slot[GB_MAGX + a] * GB_N3 + ci];
+                Bb = base[(int64_t)g.slot[GB_MAGX + b] * GB_N3 + ci];
+            }
             ecc[ia][ib] = vb * Ba - va * Bb;
         }
-    double eavg = 0.25 * (ea0 + ea1 + eb0 + eb1);
-    double dbm = upw(ma0, 2.0 * (eb0 - ecc[0][0]), 2.0 * (eb1 - ecc[1][0]));
-    double dbp = upw(ma1, 2.0 * (ecc[0][1] - eb0), 2.0 * (ecc[1][1] - eb1));
-    double dam = upw(mb0, 2.0 * (ea0 - ecc[0][0]), 2.0 * (ea1 - ecc[0][1]));
-    double dap = upw(mb1, 2.0 * (ecc[1][0] - ea0), 2.0 * (ecc[1][1] - ea1));
-    escr[(size_t)cb * estride + (size_t)c * NEDGE + e] = eavg + 0.125 * (dbm - dbp) + 0.125 * (dam - dap);
+    const R two = (R)2, eighth = (R)0.125;
+    R eavg = (R)0.25 * (ea0 + ea1 + eb0 + eb1);
+    R dbm = upw<R>(ma0, two * (eb0 - ecc[0][0]), two * (eb1 - ecc[1][0]));
+    R dbp = upw<R>(ma1, two * (ecc[0][1] - eb0), two * (ecc[1][1] - eb1));
+    R dam = upw<R>(mb0, two * (ea0 - ecc[0][0]), two * (ea1 - ecc[0][1]));
+    R dap = upw<R>(mb1, two * (ecc[1][0] - ea0), two * (ecc[1][1] - ea1));
+    escr[(size_t)cb * estride + (size_t)c * NEDGE + e] = (double)(eavg + eighth * (dbm - dbp) + eighth * (dam - dap));
 }
 
 __device__ __forceinline__ int edge_index(int c, int i, int j, int k)
@@ -844,9 +880,9 @@ k_faceb(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const dou
     double ec1 = es[(size_t)c * NEDGE + edge_index(c, t1[0], t1[1], t1[2])];
     double eb0 = es[(size_t)bb * NEDGE + edge_index(bb, I[0], I[1], I[2])];
     double eb1 = es[(size_t)bb * NEDGE + edge_index(bb, t3[0], t3[1], t3[2])];
-    double dxl[3];
-    gb_block_dx(g, kp.dx, blk, dxl);
-    double dtd_b = kp_dt(kp) / dxl[bb], dtd_c = kp_dt(kp) / dxl[c];
+    double dtd[3];
+    kp_dtdx(kp, gb_block_level(g, blk), dtd);
+    double dtd_b = dtd[bb], dtd_c = dtd[c];
     double old = g.f[a][(int64_t)blk * GB_FSZ + gb_fidx(a, I[0], I[1], I[2])];
     bscr[(size_t)cb * bstride + (size_t)a * NFB + f] = old - dtd_b * (ec1 - ec0) + dtd_c * (eb1 - eb0);
 }
@@ -879,9 +915,8 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
     const T* fs = fscr + (size_t)cb * fstride;
     const int fm[3] = {flux_index(0, i, j, k), flux_index(1, i, j, k), flux_index(2, i, j, k)};
     const int fp[3] = {flux_index(0, i + 1, j, k), flux_index(1, i, j + 1, k), flux_index(2, i, j, k + 1)};
-    double dxl[3];
-    gb_block_dx(g, kp.dx, blk, dxl);
-    const double dtd[3] = {kp_dt(kp) / dxl[0], kp_dt(kp) / dxl[1], kp_dt(kp) / dxl[2]};
+    double dtd[3];
+    kp_dtdx(kp, gb_block_level(g, blk), dtd);
     auto F = [&](int d, int var, int idx) -> double {
         return (double)fs[(size_t)d * NFLX * NFC + (size_t)var * NFC + idx];
     };
@@ -890,10 +925,11 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
     for (int s = 0; s < 5; ++s)
         Un[s] = Uc[s] - dtd[0] * (F(0, s, fp[0]) - F(0, s, fm[0])) - dtd[1] * (F(1, s, fp[1]) - F(1, s, fm[1])) -
                 dtd[2] * (F(2, s, fp[2]) - F(2, s, fm[2]));
-    double divv = (F(0, 9, fp[0]) - F(0, 9, fm[0])) / dxl[0] + (F(1, 9, fp[1]) - F(1, 9, fm[1])) / dxl[1] +
-                  (F(2, 9, fp[2]) - F(2, 9, fm[2])) / dxl[2];
+    // dt * div v from the face velocities, as sum_d (dt/dx_d) dv_d
+    double dtdivv = dtd[0] * (F(0, 9, fp[0]) - F(0, 9, fm[0])) + dtd[1] * (F(1, 9, fp[1]) - F(1, 9, fm[1])) +
+                    dtd[2] * (F(2, 9, fp[2]) - F(2, 9, fm[2]));
     double ren = re - dtd[0] * (F(0, 8, fp[0]) - F(0, 8, fm[0])) - dtd[1] * (F(1, 8, fp[1]) - F(1, 8, fm[1])) -
-                 dtd[2] * (F(2, 8, fp[2]) - F(2, 8, fm[2])) - kp_dt(kp) * pr * divv;
+                 dtd[2] * (F(2, 8, fp[2]) - F(2, 8, fm[2])) - pr * dtdivv;
     double Bn[3] = {0.0, 0.0, 0.0};
     if (MHD) {
         const double* bs = bscr + (size_t)cb * bstride;

@@ -42,7 +42,7 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
         gb_prof_end(GBP_FLUX, s);
         dim3 eg((NEDGE + 127) / 128, 3, nblk);
         gb_prof_begin(GBP_EMF, s);
-        k_emf<T><<<eg, 128, 0, s>>>(g, list, fscr, SL::flux, escr, SL::emf);
+        k_emf<T><<<eg, 128, 0, s>>>(g, list, fscr, SL::flux, escr, SL::emf, p32, SL::prim32);
         gb_prof_end(GBP_EMF, s);
         dim3 bg((NFB + 127) / 128, 3, nblk);
         gb_prof_begin(GBP_FACEB, s);
