@@ -225,20 +225,39 @@ int gb_cool_cells(int64_t n, const double* dens, double* ei, double* temp, doubl
 int gb_evolve_step(int blockCount, const int* blockList_dev, double dt, int cool,
                    gb_status* st_dev, void* stream);
 
+/* Device-resident driver clock of a run (Driver_data's dr_simTime, dr_dt,
+ * dr_dtOld, dr_tmax, dr_nstep), read and advanced by gb_step_graph. */
+typedef struct gb_driver_state {
+    double sim_time;  /* time at the start of the next step */
+    double dt;        /* dt of the last step taken */
+    double dt_old;    /* dt of the step before it (0: none yet) */
+    double t_max;     /* the step that would pass t_max is shortened to end on it */
+    double nstep;     /* steps taken */
+} gb_driver_state;
+
+/* Limits applied to every CFL time step, as Driver_computeDt.F90:588,596:
+ * dt = min(dt, dt_old * change_factor) when dt_old > 0, then
+ * dt = min(max(dt, dtmin), dtmax). Defaults 0, +inf, +inf (no limit);
+ * flash.par.turbsph_standard:106-109 sets dtmin 3.15e7 s, dtmax 3.15e12 s,
+ * tstep_change_factor 2 (pass them in code units). */
+int gb_set_dt_limits(double dtmin, double dtmax, double change_factor);
+
 /* The same step with dt on the device, as one CUDA graph: the CFL limit of
- * the listed blocks is written to dt_dev (CFL * min dx / (|v| + c_f), as
- * gb_compute_dt), then guard fill, hydro/MHD and (cool != 0) cooling run
- * with that dt, read by the kernels from dt_dev; the host does not wait.
+ * the listed blocks (CFL * min dx / (|v| + c_f), as gb_compute_dt), limited
+ * as gb_set_dt_limits says and shortened to end on drv->t_max, is written
+ * to drv->dt; then guard fill, hydro/MHD and (cool != 0) cooling run with
+ * that dt, read by the kernels from drv; then drv advances (sim_time += dt,
+ * dt_old = dt, nstep += 1). The host does not wait.
  * The graph is captured on the first call and replayed while the
  * arguments and the library's configuration (grid, parameters, cooling
  * mode, tables, surrogate weights, chunk size) stay the same; any change
- * re-captures it. blockList_dev, dt_dev and st_dev must stay valid while
+ * re-captures it. blockList_dev, drv_dev and st_dev must stay valid while
  * the graph may run. Replaces the Driver_computeDt + Hydro + Heat sequence
  * of one FLASH step (Driver_evolveFlash.F90:405-408, Driver_sourceTerms.F90:67,
  * Driver_computeDt.F90:327-335,514-515), with dt computed at the start of
  * the step. Not re-entrant. */
-int gb_step_graph(int blockCount, const int* blockList_dev, int cool, double* dt_dev, gb_status* st_dev,
-                  void* stream);
+int gb_step_graph(int blockCount, const int* blockList_dev, int cool, gb_driver_state* drv_dev,
+                  gb_status* st_dev, void* stream);
 /* Drops the captured step graph. */
 int gb_graph_reset(void);
 /* Number of captures and replays of the step graph so far, and the kernel

@@ -346,15 +346,37 @@ __global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restri
 
 __global__ void k_dt_init(unsigned long long* bits) { *bits = 0x7FF0000000000000ULL; }  // +inf
 
-// dt = CFL x the minimum limit; also dt / root_dx for the step's kernels
+struct dt_limits {
+    double dtmin, dtmax, change_factor;
+};
+
+// dt = CFL x the minimum limit; with a driver clock, limited as
+// Driver_computeDt.F90:588,596 and shortened to end on t_max. Also
+// dt / root_dx for the step's kernels.
 __global__ void k_dt_finish(const unsigned long long* bits, double cfl, double* out, double* dtdx, double dx0,
-                            double dx1, double dx2)
+                            double dx1, double dx2, gb_driver_state* drv, dt_limits lim)
 {
-    const double dt = cfl * __longlong_as_double((long long)*bits);
+    double dt = cfl * __longlong_as_double((long long)*bits);
+    if (drv) {
+        if (drv->dt_old > 0.0) dt = fmin(dt, drv->dt_old * lim.change_factor);
+        dt = fmin(fmax(dt, lim.dtmin), lim.dtmax);
+        const double left = drv->t_max - drv->sim_time;
+        if (dt > left) dt = left > 0.0 ? left : 0.0;
+        drv->dt = dt;
+    }
     *out = dt;
     dtdx[0] = dt / dx0;
     dtdx[1] = dt / dx1;
     dtdx[2] = dt / dx2;
+}
+
+__global__ void k_advance_clock(gb_driver_state* drv)
+{
+    // a step shortened to end on t_max lands on it exactly
+    const double left = drv->t_max - drv->sim_time;
+    drv->sim_time = drv->dt >= left ? drv->t_max : drv->sim_time + drv->dt;
+    drv->dt_old = drv->dt;
+    drv->nstep += 1.0;
 }
 
 __global__ void k_flash_to_soa(const double* __restrict__ in, int nunk, const int* __restrict__ hslot,
@@ -538,7 +560,20 @@ extern "C" int gb_hydro_unsplit(int blockCount, const int* list, double dt, doub
     return gb_launch_hydro(blockCount, list, dt, nullptr, 0, st, (cudaStream_t)stream);
 }
 
-int gb_launch_dt(int nblk, const int* list, double* dt_out, cudaStream_t s)
+static dt_limits g_dt_limits = {0.0, __builtin_huge_val(), __builtin_huge_val()};
+
+extern "C" int gb_set_dt_limits(double dtmin, double dtmax, double change_factor)
+{
+    if (!(dtmin >= 0.0) || !(dtmax > 0.0) || !(dtmin <= dtmax) || !(change_factor > 0.0)) {
+        gb_set_error("gb_set_dt_limits: need 0 <= dtmin <= dtmax and change_factor > 0");
+        return GB_ERR_ARG;
+    }
+    g_dt_limits = {dtmin, dtmax, change_factor};
+    g_gb.gen += 1;
+    return GB_OK;
+}
+
+static int launch_dt(int nblk, const int* list, double* dt_out, gb_driver_state* drv, cudaStream_t s)
 {
     k_dt_init<<<1, 1, 0, s>>>((unsigned long long*)g_gb.d_dtmin);
     gbh::hydro_kparams kp = make_kp(1.0);
@@ -546,9 +581,14 @@ int gb_launch_dt(int nblk, const int* list, double* dt_out, cudaStream_t s)
     int rc = gb_dt_launch(kp, g_gb.hp.mhd, nblk, list, (unsigned long long*)g_gb.d_dtmin, s);
     if (rc) return rc;
     k_dt_finish<<<1, 1, 0, s>>>((const unsigned long long*)g_gb.d_dtmin, g_gb.hp.cfl, dt_out, g_gb.d_dtmin + 1,
-                                kp.dx[0], kp.dx[1], kp.dx[2]);
+                                kp.dx[0], kp.dx[1], kp.dx[2], drv, g_dt_limits);
     gb_prof_end(GBP_DT, s);
     return gb_check(cudaGetLastError(), "k_dt_finish") ? GB_ERR_CUDA : GB_OK;
+}
+
+int gb_launch_dt(int nblk, const int* list, double* dt_out, cudaStream_t s)
+{
+    return launch_dt(nblk, list, dt_out, nullptr, s);
 }
 
 extern "C" int gb_compute_dt(int blockCount, const int* list, double* dt_dev, void* stream)
@@ -598,7 +638,7 @@ struct step_graph {
     cudaStream_t cap = nullptr;
     const int* list = nullptr;
     int n = 0, cool = -1;
-    double* dt_dev = nullptr;
+    gb_driver_state* drv = nullptr;
     gb_status* st = nullptr;
     unsigned long long gen = ~0ULL;
     long long launches = 0, captures = 0, kernel_nodes = 0;
@@ -610,19 +650,23 @@ void graph_drop()
     g_graph.exec = nullptr;
 }
 
-int record_step(int n, const int* list, int cool, double* dt_dev, gb_status* st, cudaStream_t s)
+int record_step(int n, const int* list, int cool, gb_driver_state* drv, gb_status* st, cudaStream_t s)
 {
-    int rc = gb_launch_dt(n, list, dt_dev, s);
+    double* dt_dev = &drv->dt;
+    int rc = launch_dt(n, list, dt_dev, drv, s);
     if (rc) return rc;
     rc = gb_launch_guardfill(n, list, s);
     if (rc) return rc;
-    return gb_launch_hydro(n, list, 1.0, dt_dev, cool, st, s);
+    rc = gb_launch_hydro(n, list, 1.0, dt_dev, cool, st, s);
+    if (rc) return rc;
+    k_advance_clock<<<1, 1, 0, s>>>(drv);
+    return gb_check(cudaGetLastError(), "k_advance_clock") ? GB_ERR_CUDA : GB_OK;
 }
 }  // namespace
 
 int gb_cooling_mode();
 
-extern "C" int gb_step_graph(int blockCount, const int* list, int cool, double* dt_dev, gb_status* st,
+extern "C" int gb_step_graph(int blockCount, const int* list, int cool, gb_driver_state* drv, gb_status* st,
                              void* stream)
 {
     if (!g_gb.grid_ok || !g_gb.hydro_ok || !g_gb.tree_ok) {
@@ -633,8 +677,8 @@ extern "C" int gb_step_graph(int blockCount, const int* list, int cool, double* 
         gb_set_error("gb_step_graph: cooling needs gb_cool_init and TEMP/TDUS slots");
         return GB_ERR_NOT_INIT;
     }
-    if (blockCount <= 0 || !list || !dt_dev) {
-        gb_set_error("gb_step_graph: bad block list or dt pointer");
+    if (blockCount <= 0 || !list || !drv) {
+        gb_set_error("gb_step_graph: bad block list or driver state pointer");
         return GB_ERR_ARG;
     }
     if (gb_prof_is_on()) {
@@ -643,7 +687,7 @@ extern "C" int gb_step_graph(int blockCount, const int* list, int cool, double* 
     }
     cudaStream_t s = (cudaStream_t)stream;
     const bool same = g_graph.exec && g_graph.list == list && g_graph.n == blockCount && g_graph.cool == cool &&
-                      g_graph.dt_dev == dt_dev && g_graph.st == st && g_graph.gen == g_gb.gen;
+                      g_graph.drv == drv && g_graph.st == st && g_graph.gen == g_gb.gen;
     if (!same) {
         graph_drop();
         if (!g_graph.cap && gb_check(cudaStreamCreateWithFlags(&g_graph.cap, cudaStreamNonBlocking), "graph stream"))
@@ -657,7 +701,7 @@ extern "C" int gb_step_graph(int blockCount, const int* list, int cool, double* 
         if (gb_check(cudaStreamSynchronize(s), "graph prepare")) return GB_ERR_CUDA;
         if (gb_check(cudaStreamBeginCapture(g_graph.cap, cudaStreamCaptureModeThreadLocal), "begin capture"))
             return GB_ERR_CUDA;
-        rc = record_step(blockCount, list, cool, dt_dev, st, g_graph.cap);
+        rc = record_step(blockCount, list, cool, drv, st, g_graph.cap);
         cudaGraph_t graph = nullptr;
         cudaError_t e = cudaStreamEndCapture(g_graph.cap, &graph);
         if (rc || gb_check(e, "end capture")) {
@@ -683,7 +727,7 @@ extern "C" int gb_step_graph(int blockCount, const int* list, int cool, double* 
         g_graph.list = list;
         g_graph.n = blockCount;
         g_graph.cool = cool;
-        g_graph.dt_dev = dt_dev;
+        g_graph.drv = drv;
         g_graph.st = st;
         g_graph.gen = g_gb.gen;
         g_graph.captures += 1;

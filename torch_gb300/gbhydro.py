@@ -100,6 +100,7 @@ _SIG = {
     "gb_set_launch_config": (C.c_int, [C.c_int, C.c_int]),
     "gb_get_launch_config": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "gb_step_graph": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gb_set_dt_limits": (C.c_int, [C.c_double, C.c_double, C.c_double]),
     "gb_graph_reset": (C.c_int, []),
     "gb_graph_info": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "gb_hydro_unsplit_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p,
@@ -300,19 +301,27 @@ class Grid:
         check(lib().gb_compute_dt(n, _ptr(lt), _ptr(out), _stream()), "gb_compute_dt")
         return out
 
-    def step_graph(self, cool: bool, dt_out=None, blockList=None):
-        """One whole step (device dt, guard fill, hydro, cooling) as a
-        replayed CUDA graph; returns the device tensor holding its dt."""
+    # device driver clock (gb_driver_state): sim_time, dt, dt_old, t_max, nstep
+    DRV_TIME, DRV_DT, DRV_DTOLD, DRV_TMAX, DRV_NSTEP = range(5)
+
+    @property
+    def driver(self):
+        if getattr(self, "_drv", None) is None:
+            self._drv = self.torch.tensor([0.0, 0.0, 0.0, float("inf"), 0.0], dtype=self.torch.float64,
+                                          device=self.u.device)
+        return self._drv
+
+    def step_graph(self, cool: bool, blockList=None):
+        """One whole step (device dt, guard fill, hydro, cooling, clock
+        advance) as a replayed CUDA graph; returns the device tensor view
+        holding the step's dt."""
         lt, n = self.list_tensor(blockList)
         if blockList is not None:
             self._graph_list = lt  # the graph keeps the pointer
-        if dt_out is None:
-            if getattr(self, "_dt_dev", None) is None:
-                self._dt_dev = self.torch.zeros(1, dtype=self.torch.float64, device=self.u.device)
-            dt_out = self._dt_dev
-        check(lib().gb_step_graph(n, _ptr(lt), int(cool), _ptr(dt_out), _ptr(self.status), _stream()),
+        drv = self.driver
+        check(lib().gb_step_graph(n, _ptr(lt), int(cool), _ptr(drv), _ptr(self.status), _stream()),
               "gb_step_graph")
-        return dt_out
+        return drv[self.DRV_DT:self.DRV_DT + 1]
 
     def evolve_step(self, dt: float, cool: bool, blockList=None):
         lt, n = self.list_tensor(blockList)
@@ -333,6 +342,11 @@ def init_cooling(p: CoolParams, table_path: str | None = None) -> None:
     from . import tables
     path = table_path or tables.COMPACT_PATH
     check(lib().gb_cool_init(path.encode(), C.byref(p)), "gb_cool_init")
+
+
+def set_dt_limits(dtmin: float = 0.0, dtmax: float = float("inf"), change_factor: float = float("inf")) -> None:
+    """Driver_computeDt's limits on every step's dt (code units)."""
+    check(lib().gb_set_dt_limits(float(dtmin), float(dtmax), float(change_factor)), "gb_set_dt_limits")
 
 
 def graph_info() -> tuple:
