@@ -368,6 +368,8 @@ def main():
     ap.add_argument("--save-weights", default=None)
     ap.add_argument("--ncu-range", action="store_true",
                     help="bracket the fast path's timed region with cudaProfilerStart/Stop")
+    ap.add_argument("--only", choices=["plain", "fast", "eager"], default=None,
+                    help="time one path alone and print a short line (for profiler captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -413,6 +415,18 @@ def main():
         np.save(args.save_weights, G.mlp_weights())
     G.init_cooling(G.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
                                  time_unit=units["time_unit"]))
+    if args.only:
+        g = make_grid(G, tree, st)
+        del st
+        prec, sur, graph = {"plain": (0, False, True), "fast": (1, True, True), "eager": (1, True, False)}[args.only]
+        ms, stt, info = run_path(G, g, prec, args.steps, args.warmup, surrogate=sur, graph=graph,
+                                 tune=not args.no_tune and graph, profile=not graph, ncu_range=args.ncu_range)
+        if rank == 0:
+            print(json.dumps({"path": args.only, "workload": wl["name"], "ms_per_step": ms,
+                              "value": zones * world / (ms * 1e-3), "unit": "zone-updates/s",
+                              "status_code": stt["code"],
+                              "kernels": {k: v[0] / args.steps for k, v in info.items()} if not graph else info}))
+        return
     g_plain = make_grid(G, tree, st)
     g_fast = make_grid(G, tree, st)
     g_mixed = make_grid(G, tree, st)
@@ -462,6 +476,23 @@ def main():
     e2e_ms, e2e_bytes, e2e_parts = e2e_run(G, g_fast, max(2, args.steps // 2), 1)
     G.set_cooling_mode(False)
     hbm, hbm_kind = peaks()
+    # FP64-pipe roofline of the plain path: flops per zone-update counted by
+    # the oracle's counting build (roofline_constants.json) over the
+    # measured FP64 FMA peak of this GPU
+    fp64 = None
+    try:
+        with open(os.path.join(ROOT, "roofline_constants.json")) as f:
+            rc = json.load(f)
+        fpz = rc["mhd_cooling_step"]["flops"]
+        peak64 = G.measure_fp64_peak()
+        ach64 = zones * fpz / (ms_plain * 1e-3) / 1e12
+        fp64 = {"path": "plain_fp64", "flops_per_zone": fpz, "achieved_tflops": ach64, "peak_tflops": peak64,
+                "frac": ach64 / peak64, "peak_kind": "measured FP64 FMA loop on this GPU",
+                "note": "flops = + - * / sqrt of the oracle's MHD step + CFL + implicit cooling per zone; "
+                        "a division or sqrt issues several FP64 instructions, so the pipe is busier than "
+                        "this fraction"}
+    except (OSError, KeyError, ValueError, G.GBError):
+        pass
     # dominant kernel: largest share of the fast path's timed region.
     # Algorithmic bytes = 216 B per zone-update (12 FP64 MHD words + 3
     # cooling words, read once + written once) x the zones a launch covers.
@@ -514,6 +545,7 @@ def main():
                      "algo_bytes_per_launch": 216.0 * zones_per_launch},
         "e2e": {"value": zones / (e2e_ms * 1e-3), "unit": "zone-updates/s", "h2d_bytes_per_step": e2e_bytes,
                 "d2h_bytes_per_step": e2e_bytes, "parts": e2e_parts},
+        "fp64_roofline": fp64,
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "ic_s": t_ic,

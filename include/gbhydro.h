@@ -341,6 +341,11 @@ int gb_set_cooling_mode(int mode, double rel_tol, int check_fp64);
 int gb_prof_enable(int on);
 int gb_prof_read(double* ms, long long* launches, int n);
 
+/* Measured FP64 FMA throughput of the current GPU in TFLOP/s (2 flops per
+ * FMA; a few milliseconds of independent FMA chains on every SM): the
+ * denominator of the FP64-pipe roofline. */
+int gb_measure_fp64_peak(double* tflops);
+
 /* ---------------------------------------------------------------- misc */
 int gb_status_reset(gb_status* st_dev, void* stream);
 int gb_status_read(const gb_status* st_dev, gb_status* st_host);

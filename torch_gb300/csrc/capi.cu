@@ -79,6 +79,54 @@ extern "C" int gb_prof_read(double* ms, long long* launches, int n)
     return GB_OK;
 }
 
+// FP64 FMA throughput probe: 8 independent dependency chains per thread
+__global__ void __launch_bounds__(256) k_fp64_fma(double* out, int iters, double a, double b)
+{
+    double x[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = 1e-3 * (threadIdx.x + q);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) x[q] = fma(x[q], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s += x[q];
+    if (s == -1.0) out[0] = s;  // keeps the chains live; never true
+}
+
+extern "C" int gb_measure_fp64_peak(double* tflops)
+{
+    if (!tflops) return GB_ERR_ARG;
+    int dev = 0, nsm = 0;
+    if (gb_check(cudaGetDevice(&dev), "device") ||
+        gb_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "sm count"))
+        return GB_ERR_CUDA;
+    double* d = nullptr;
+    if (gb_check(cudaMalloc(&d, sizeof(double)), "probe alloc")) return GB_ERR_CUDA;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int iters = 1 << 14, blocks = nsm * 8, threads = 256;
+    k_fp64_fma<<<blocks, threads>>>(d, iters, 0.9999999, 1e-7);
+    float best = 1e30f;
+    for (int r = 0; r < 5; ++r) {
+        cudaEventRecord(e0);
+        k_fp64_fma<<<blocks, threads>>>(d, iters, 0.9999999, 1e-7);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) best = ms;
+    }
+    int rc = gb_check(cudaGetLastError(), "k_fp64_fma") ? GB_ERR_CUDA : GB_OK;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+    return rc;
+}
+
 static char g_err[512] = "";
 
 void gb_set_error(const char* fmt, ...)

@@ -101,6 +101,7 @@ _SIG = {
     "gb_get_launch_config": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "gb_step_graph": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gb_set_dt_limits": (C.c_int, [C.c_double, C.c_double, C.c_double]),
+    "gb_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
     "gb_graph_reset": (C.c_int, []),
     "gb_graph_info": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "gb_hydro_unsplit_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p,
@@ -347,6 +348,13 @@ def init_cooling(p: CoolParams, table_path: str | None = None) -> None:
 def set_dt_limits(dtmin: float = 0.0, dtmax: float = float("inf"), change_factor: float = float("inf")) -> None:
     """Driver_computeDt's limits on every step's dt (code units)."""
     check(lib().gb_set_dt_limits(float(dtmin), float(dtmax), float(change_factor)), "gb_set_dt_limits")
+
+
+def measure_fp64_peak() -> float:
+    """FP64 FMA throughput of this GPU, TFLOP/s."""
+    v = C.c_double()
+    check(lib().gb_measure_fp64_peak(C.byref(v)), "gb_measure_fp64_peak")
+    return v.value
 
 
 def graph_info() -> tuple:
