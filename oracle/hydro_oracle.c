@@ -635,8 +635,91 @@ static inline double upw(double f, double a, double b)
     return f > 0.0 ? a : (f < 0.0 ? b : 0.5 * (a + b));
 }
 
+/* Registers of one face: 16 x 16 face cells (first transverse axis
+ * fastest, axes in x, y, z order) x ORC_NREG flux values. */
+static const int reg_slots_note = ORC_NREG;
+
+static void face_axes(int d, int* t1, int* t2)
+{
+    *t1 = d == 0 ? 1 : 0;
+    *t2 = d == 2 ? 1 : 2;
+}
+
+/* Put this block's boundary fluxes (faces whose neighbour is coarser) and
+ * take the fine-face means (faces whose neighbour is finer), as
+ * Grid_putFluxData / Grid_conserveFluxes / Grid_getFluxData do on a
+ * Cartesian mesh. `fl` are the block's face fluxes, n the padded size. */
+static void flux_fix(const orc_fluxfix* fx, face_flux* const* fl, int n, int lo, int nxb)
+{
+#define FFX(d, i, j, k) fl[d][(i) + (int64_t)(n + 1) * ((j) + (int64_t)(n + 1) * (k))]
+    for (int f = 0; f < 6; ++f) {
+        const int d = f >> 1, side = f & 1;
+        if (fx->type[f] == ORC_FACE_COARSER && fx->store[f]) {
+            int t1, t2;
+            face_axes(d, &t1, &t2);
+            for (int c2 = 0; c2 < nxb; ++c2)
+                for (int c1 = 0; c1 < nxb; ++c1) {
+                    int I[3];
+                    I[d] = side ? lo + nxb : lo;
+                    I[t1] = lo + c1;
+                    I[t2] = lo + c2;
+                    const face_flux* o = &FFX(d, I[0], I[1], I[2]);
+                    double* r = fx->store[f] + (size_t)(c1 + nxb * c2) * ORC_NREG;
+                    for (int v = 0; v < 5; ++v) r[v] = o->f[v];
+                    r[5] = o->feint;
+                    r[6] = o->un;
+                }
+        }
+    }
+    for (int f = 0; f < 6; ++f) {
+        const int d = f >> 1, side = f & 1;
+        if (fx->type[f] != ORC_FACE_FINER) continue;
+        int t1, t2;
+        face_axes(d, &t1, &t2);
+        const int h = nxb / 2;
+        for (int c2 = 0; c2 < nxb; ++c2)
+            for (int c1 = 0; c1 < nxb; ++c1) {
+                const int q = (c1 >= h) + 2 * (c2 >= h);
+                const double* r = fx->fine[f][q];
+                if (!r) continue;
+                const int g1 = 2 * (c1 - h * (c1 >= h)), g2 = 2 * (c2 - h * (c2 >= h));
+                const double* r00 = r + (size_t)(g1 + nxb * g2) * ORC_NREG;
+                const double* r10 = r + (size_t)(g1 + 1 + nxb * g2) * ORC_NREG;
+                const double* r01 = r + (size_t)(g1 + nxb * (g2 + 1)) * ORC_NREG;
+                const double* r11 = r + (size_t)(g1 + 1 + nxb * (g2 + 1)) * ORC_NREG;
+                double m[ORC_NREG];
+                for (int v = 0; v < ORC_NREG; ++v) m[v] = 0.25 * (((r00[v] + r10[v]) + r01[v]) + r11[v]);
+                int I[3];
+                I[d] = side ? lo + nxb : lo;
+                I[t1] = lo + c1;
+                I[t2] = lo + c2;
+                face_flux* o = &FFX(d, I[0], I[1], I[2]);
+                for (int v = 0; v < 5; ++v) o->f[v] = m[v];
+                o->feint = m[5];
+                o->un = m[6];
+            }
+    }
+#undef FFX
+    (void)reg_slots_note;
+}
+
+static int unsplit_block(const orc_hydro_params* p, double* u, double* bxf, double* byf, double* bzf,
+                         double dt, double dx, double dy, double dz, const orc_fluxfix* fx);
+
 int orc_unsplit_block(const orc_hydro_params* p, double* u, double* bxf, double* byf, double* bzf,
                       double dt, double dx, double dy, double dz)
+{
+    return unsplit_block(p, u, bxf, byf, bzf, dt, dx, dy, dz, NULL);
+}
+
+int orc_unsplit_block_fc(const orc_hydro_params* p, double* u, double* bxf, double* byf, double* bzf,
+                         double dt, double dx, double dy, double dz, const orc_fluxfix* fx)
+{
+    return unsplit_block(p, u, bxf, byf, bzf, dt, dx, dy, dz, fx);
+}
+
+static int unsplit_block(const orc_hydro_params* p, double* u, double* bxf, double* byf, double* bzf,
+                         double dt, double dx, double dy, double dz, const orc_fluxfix* fx)
 {
     const int ng = p->nguard, nxb = p->nxb, n = nxb + 2 * ng;
     const int lo = ng, hi = ng + nxb - 1; /* interior cells */
@@ -761,6 +844,10 @@ int orc_unsplit_block(const orc_hydro_params* p, double* u, double* bxf, double*
                     }
         }
     }
+
+    /* flux conservation at fine-coarse faces (after the electric fields,
+     * which use the block's own fluxes) */
+    if (fx) flux_fix(fx, fl, n, lo, nxb);
 
     /* conservative update of the interior cells */
     double* unew = (double*)malloc(sizeof(double) * (size_t)(ORV_NVAR * n3));
@@ -1135,4 +1222,41 @@ void orc_fill_guards_tree(const orc_hydro_params* p, int nnodes, const int* leve
     for (int b = 0; b < nnodes; ++b)
         if (child[8 * b] < 0)
             orc_fill_guards_leaf(p, b, level, coord, child, root, nr0, nr1, nr2, maxlevel, u, bx, by, bz);
+}
+
+/* Face neighbours of leaf b (see hydro_oracle.h). Positions are finest-cell
+ * coordinates; the probe point lies one finest cell across the face, at the
+ * face centre (same or coarser neighbour) or at the quadrant centres. */
+void orc_face_links(int b, const int* level, const int* coord, const int* child, const int* root, int nr0,
+                    int nr1, int nr2, int maxlevel, int* type, int* fine)
+{
+    const long long nxb = 16;
+    const long long N[3] = {(long long)nr0 * nxb << maxlevel, (long long)nr1 * nxb << maxlevel,
+                            (long long)nr2 * nxb << maxlevel};
+    const int L = level[b];
+    const long long E = nxb << (maxlevel - L); /* block extent in finest cells */
+    for (int f = 0; f < 6; ++f) {
+        const int d = f >> 1, side = f & 1;
+        int t1, t2;
+        face_axes(d, &t1, &t2);
+        long long X[3];
+        X[d] = orc_wrap(side ? (coord[3 * b + d] + 1) * E : coord[3 * b + d] * E - 1, N[d]);
+        X[t1] = coord[3 * b + t1] * E + E / 2;
+        X[t2] = coord[3 * b + t2] * E + E / 2;
+        int m = orc_leaf_at(level, child, root, nr0, nr1, maxlevel, X[0], X[1], X[2]);
+        for (int q = 0; q < 4; ++q) fine[4 * f + q] = -1;
+        if (level[m] < L) {
+            type[f] = ORC_FACE_COARSER;
+        } else if (level[m] == L) {
+            type[f] = ORC_FACE_SAME;
+        } else {
+            type[f] = ORC_FACE_FINER;
+            for (int q = 0; q < 4; ++q) {
+                long long Y[3] = {X[0], X[1], X[2]};
+                Y[t1] = coord[3 * b + t1] * E + E / 4 + (q & 1) * (E / 2);
+                Y[t2] = coord[3 * b + t2] * E + E / 4 + (q >> 1) * (E / 2);
+                fine[4 * f + q] = orc_leaf_at(level, child, root, nr0, nr1, maxlevel, Y[0], Y[1], Y[2]);
+            }
+        }
+    }
 }

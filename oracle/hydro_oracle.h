@@ -48,6 +48,36 @@ void orc_hydro_default_params(orc_hydro_params* p, int mhd);
 int orc_unsplit_block(const orc_hydro_params* p, double* u, double* bx, double* by, double* bz,
                       double dt, double dx, double dy, double dz);
 
+/* Flux conservation at fine-coarse faces. Faces f = 2 d + side (side 0 =
+ * low). A face whose neighbour is coarser stores the block's boundary
+ * fluxes (rho, mx, my, mz, E, rho e_int, u_n: ORC_NREG values per face
+ * cell, 16 x 16 face cells, first transverse axis fastest) into store[f];
+ * a face whose neighbour is finer replaces its boundary fluxes by the mean
+ * of the 2 x 2 fine-face fluxes held in fine[f][q] (q = quadrant: bit 0 the
+ * upper half along the first transverse axis, bit 1 along the second). */
+#define ORC_NREG 7
+enum { ORC_FACE_SAME = 0, ORC_FACE_COARSER = 1, ORC_FACE_FINER = 2 };
+typedef struct orc_fluxfix {
+    int type[6];
+    double* store[6];
+    const double* fine[6][4];
+} orc_fluxfix;
+
+int orc_unsplit_block_fc(const orc_hydro_params* p, double* u, double* bx, double* by, double* bz,
+                         double dt, double dx, double dy, double dz, const orc_fluxfix* fx);
+
+/* Face neighbours of leaf b of a block tree: type[f] (ORC_FACE_*) and, for
+ * finer neighbours, the four fine leaves (quadrant order as above). */
+void orc_face_links(int b, const int* level, const int* coord, const int* child, const int* root, int nr0,
+                    int nr1, int nr2, int maxlevel, int* type, int* fine);
+
+/* One step of the listed leaves of a block tree with flux conservation at
+ * fine-coarse faces (flux_correct): leaves are stepped finest level first,
+ * each level OpenMP-parallel (omp_driver.c). */
+long orc_unsplit_tree(const orc_hydro_params* p, int nlist, const int* list, const int* level, const int* coord,
+                      const int* child, const int* root, int nr0, int nr1, int nr2, int maxlevel, double* u,
+                      double* bx, double* by, double* bz, double dt, double root_dx, int flux_correct);
+
 /* CFL limit over the interior cells of one block:
  * min_d dx_d / (|v_d| + c_f,d). */
 double orc_block_dt_limit(const orc_hydro_params* p, const double* u, double dx, double dy,

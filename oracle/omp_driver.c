@@ -132,3 +132,48 @@ long orc_unsplit_list(const orc_hydro_params* p, int nlist, const int* list, con
     }
     return total;
 }
+
+long orc_unsplit_tree(const orc_hydro_params* p, int nlist, const int* list, const int* level, const int* coord,
+                      const int* child, const int* root, int nr0, int nr1, int nr2, int maxlevel, double* u,
+                      double* bx, double* by, double* bz, double dt, double root_dx, int flux_correct)
+{
+    const int n = p->nxb + 2 * p->nguard;
+    const int64_t n3 = (int64_t)n * n * n, fsz = n3 + (int64_t)n * n;
+    int nnodes = 0;
+    for (int q = 0; q < nlist; ++q)
+        if (list[q] + 1 > nnodes) nnodes = list[q] + 1;
+    const size_t per_face = (size_t)p->nxb * p->nxb * ORC_NREG;
+    double* reg = NULL;
+    if (flux_correct && maxlevel > 0) reg = (double*)calloc((size_t)nnodes * 6 * per_face, sizeof(double));
+    long total = 0;
+    for (int L = maxlevel; L >= 0; --L) {
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
+        for (int q = 0; q < nlist; ++q) {
+            const int b = list[q];
+            if (level[b] != L) continue;
+            const double dx = ldexp(root_dx, -level[b]);
+            double* ub = u + (int64_t)b * ORV_NVAR * n3;
+            double* fx = p->mhd ? bx + (int64_t)b * fsz : NULL;
+            double* fy = p->mhd ? by + (int64_t)b * fsz : NULL;
+            double* fz = p->mhd ? bz + (int64_t)b * fsz : NULL;
+            if (!reg) {
+                total += orc_unsplit_block(p, ub, fx, fy, fz, dt, dx, dx, dx);
+                continue;
+            }
+            orc_fluxfix ff;
+            int fine[24];
+            orc_face_links(b, level, coord, child, root, nr0, nr1, nr2, maxlevel, ff.type, fine);
+            for (int f = 0; f < 6; ++f) {
+                ff.store[f] = reg + ((size_t)b * 6 + f) * per_face;
+                for (int qq = 0; qq < 4; ++qq) {
+                    const int m = fine[4 * f + qq];
+                    /* the fine leaf's face that touches this block is the opposite one */
+                    ff.fine[f][qq] = m >= 0 && m < nnodes ? reg + ((size_t)m * 6 + (f ^ 1)) * per_face : NULL;
+                }
+            }
+            total += orc_unsplit_block_fc(p, ub, fx, fy, fz, dt, dx, dx, dx, &ff);
+        }
+    }
+    free(reg);
+    return total;
+}

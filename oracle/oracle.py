@@ -118,6 +118,11 @@ def lib():
         L.orc_unsplit_list.argtypes = [C.POINTER(HydroParams), C.c_int, optd, optd, optd, optd, optd, optd,
                                        C.c_double, C.c_double]
         L.orc_unsplit_list.restype = C.c_long
+        L.orc_unsplit_tree.argtypes = [C.POINTER(HydroParams), C.c_int, optd, optd, optd, optd, optd, C.c_int,
+                                       C.c_int, C.c_int, C.c_int, optd, optd, optd, optd, C.c_double, C.c_double,
+                                       C.c_int]
+        L.orc_unsplit_tree.restype = C.c_long
+        L.orc_face_links.argtypes = [C.c_int, optd, optd, optd, optd, C.c_int, C.c_int, C.c_int, C.c_int, optd, optd]
         L.orc_num_threads.restype = C.c_int
         L.orc_set_num_threads.argtypes = [C.c_int]
         _lib = L
@@ -225,6 +230,26 @@ def unsplit_list(p: HydroParams, tl: TreeLists, leaves, u, bx, by, bz, dt, root_
     ls = np.ascontiguousarray(leaves, np.int32)
     return lib().orc_unsplit_list(C.byref(p), len(ls), _p(ls), _p(tl.a["level"]), _p(u), _p(bx), _p(by),
                                   _p(bz), dt, root_dx)
+
+
+def unsplit_tree(p: HydroParams, tl: TreeLists, leaves, u, bx, by, bz, dt, root_dx, flux_correct=True):
+    """One step of the listed leaves, finest level first, with flux
+    conservation at fine-coarse faces when flux_correct."""
+    a = tl.a
+    ls = np.ascontiguousarray(leaves, np.int32)
+    return lib().orc_unsplit_tree(C.byref(p), len(ls), _p(ls), _p(a["level"]), _p(a["coord"]), _p(a["child"]),
+                                  _p(a["root"]), tl.nr[0], tl.nr[1], tl.nr[2], tl.maxlevel, _p(u), _p(bx), _p(by),
+                                  _p(bz), dt, root_dx, int(flux_correct))
+
+
+def face_links(tl: TreeLists, b: int):
+    """(type[6], fine[6, 4]) of leaf b."""
+    a = tl.a
+    t = np.zeros(6, np.int32)
+    f = np.zeros(24, np.int32)
+    lib().orc_face_links(int(b), _p(a["level"]), _p(a["coord"]), _p(a["child"]), _p(a["root"]), tl.nr[0], tl.nr[1],
+                         tl.nr[2], tl.maxlevel, _p(t), _p(f))
+    return t, f.reshape(6, 4)
 
 
 def dt_limit(p: HydroParams, u, dx, dy, dz) -> float:
