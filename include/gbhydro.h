@@ -235,6 +235,18 @@ typedef struct gb_driver_state {
     double nstep;     /* steps taken */
 } gb_driver_state;
 
+/* Flux conservation at fine-coarse block faces (FLASH's flux_correct:
+ * Grid_putFluxData / Grid_conserveFluxes / Grid_getFluxData around the
+ * update in hy_uhd_unsplit; interface in Grid_interface.F90:132-135,460-468).
+ * On by default; it applies when the registered tree has more than one
+ * level: the listed leaves are stepped finest level first, a block next to
+ * a coarser one registers its boundary fluxes of rho, rho v, E, rho e_int
+ * and the face velocity, and a block next to finer ones replaces its
+ * boundary fluxes by the mean of the 2 x 2 fine fluxes before its update.
+ * Face B is not matched across levels (no edge-EMF averaging). The
+ * allocation-free entry point does not apply it. */
+int gb_set_flux_correction(int on);
+
 /* Limits applied to every CFL time step, as Driver_computeDt.F90:588,596:
  * dt = min(dt, dt_old * change_factor) when dt_old > 0, then
  * dt = min(max(dt, dtmin), dtmax). Defaults 0, +inf, +inf (no limit);

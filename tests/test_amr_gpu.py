@@ -37,25 +37,23 @@ def test_amr_guard_fill_matches_oracle(gb, oracle, mhd):
             assert np.array_equal(a.cpu().numpy()[leaf], b[leaf])
 
 
-@pytest.mark.parametrize("mhd", [False, True])
-def test_amr_fp64_step_matches_oracle(gb, oracle, mhd):
+@pytest.mark.parametrize("mhd,fc", [(False, True), (True, True), (True, False)])
+def test_amr_fp64_step_matches_oracle(gb, oracle, mhd, fc):
+    """One FP64 step over a 3-level tree (per-level cell sizes, flux
+    conservation at fine-coarse faces on or off) against the oracle."""
     t, st, g = _state(gb, mhd)
     gb.init_hydro(gb.hydro_params(mhd))
+    gb.set_flux_correction(fc)
     u, (fx, fy, fz) = _oracle_arrays(st, mhd)
     p = oracle.hydro_params(mhd)
-    dx0 = st["root_dx"]
+    tl = oracle.TreeLists(t)
     oracle.fill_guards_tree(p, t, u, fx, fy, fz)
-    dt = g.compute_dt().item()
-    g.evolve_step(dt, cool=False)
-    fsz = 24 * 24 * 25
-    for b in t["leaf"]:
-        dx = dx0 / 2 ** t["level"][b]
-        ub = u[b:b + 1]
-        fb = [None if f is None else f[b:b + 1] for f in (fx, fy, fz)]
-        oracle.unsplit_blocks(p, ub, *fb, dt, dx, dx, dx)
-        if mhd:
-            fx[b], fy[b], fz[b] = fb[0][0], fb[1][0], fb[2][0]
-        u[b] = ub[0]
+    try:
+        dt = g.compute_dt().item()
+        g.evolve_step(dt, cool=False)
+    finally:
+        gb.set_flux_correction(True)
+    oracle.unsplit_tree(p, tl, t["leaf"], u, fx, fy, fz, dt, st["root_dx"], flux_correct=fc)
     nv = 10 if mhd else 7
     leaf = t["leaf"]
     gu = g.u.cpu().numpy()[leaf, :nv, 4:20, 4:20, 4:20]
@@ -83,3 +81,33 @@ def test_amr_mixed_precision_l1(gb, mhd):
     b = g32.u.cpu().numpy()[leaf][:, :, 4:20, 4:20, 4:20]
     for v in (0, 4):
         assert np.abs(a[:, v] - b[:, v]).sum() / np.abs(a[:, v]).sum() <= 1e-4
+
+
+def test_amr_hydro_conserves_with_flux_correction(gb):
+    """Mass, momentum and energy over the periodic 3-level tree after a few
+    GPU steps: round-off with flux conservation at fine-coarse faces."""
+    import torch
+    from torch_gb300 import amr
+    t, c = amr.small_tree()
+    st = amr.amr_box(t, c, seed=5, mach=1.0, device="cuda")
+    g = gb.grid_from_amr(t, st, mhd=False, cooling=False)
+    gb.init_hydro(gb.hydro_params(False))
+    g.register()
+    lv = torch.as_tensor(np.asarray(t["level"])[g.leaf], dtype=torch.float64, device="cuda")
+    vol = (st["root_dx"] / 2 ** lv) ** 3
+
+    def totals():
+        u = g.u[g.t_leaf.long()][:, :, 4:20, 4:20, 4:20]
+        rho = u[:, 0]
+        q = [rho, rho * u[:, 1], rho * u[:, 2], rho * u[:, 3], rho * u[:, 5]]
+        return torch.stack([(x.sum(dim=(1, 2, 3)) * vol).sum() for x in q]).cpu().numpy()
+
+    before = totals()
+    g.status_reset()
+    for _ in range(3):
+        dt = g.compute_dt().item()
+        g.evolve_step(dt, cool=False)
+    after = totals()
+    assert g.status_read()["n_eint_switch"] == 0
+    rel = np.abs(after - before) / np.abs(before[[0, 0, 0, 0, 4]])
+    assert np.all(rel < 1e-13), rel

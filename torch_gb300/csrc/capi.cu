@@ -213,6 +213,7 @@ extern "C" int gb_register_grid(const gb_grid_desc* grid, const gb_tree_desc* tr
     g_gb.grid.f[2] = grid->facez;
     g_gb.grid.level = nullptr;
     g_gb.grid_ok = true;
+    g_gb.links_ok = false;
     g_gb.gen += 1;
     g_gb.tree_ok = false;
     if (tree) {
@@ -278,6 +279,71 @@ __device__ __forceinline__ leaf_hit find_leaf(const gb_tree_desc& t, long long X
 // periodic wrap of a guard position: x lies in (-n, 2n) (a guard region is
 // narrower than the domain)
 __device__ __forceinline__ long long wrap(long long x, long long n) { return x < 0 ? x + n : (x >= n ? x - n : x); }
+
+// Face neighbours of every leaf: links[(b * 6 + f) * 5] = same (0), coarser
+// (1) or finer (2) neighbour across face f = 2 d + side, then the four fine
+// leaves (finer only; quadrant q: bit 0 the upper half along the first
+// transverse axis, bit 1 along the second). The probe lies one finest cell
+// across the face, at the face centre or the quadrant centres.
+__global__ void k_face_links(gb_tree_desc t, int* __restrict__ links)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= t.nnodes * 6) return;
+    const int b = idx / 6, f = idx % 6;
+    int* out = links + (size_t)idx * 5;
+    out[0] = 0;
+    out[1] = out[2] = out[3] = out[4] = -1;
+    if (t.child[8 * b] >= 0) return;
+    const int d = f >> 1, side = f & 1;
+    const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
+    const long long N[3] = {(long long)t.nrx * GB_NXB << t.maxlevel, (long long)t.nry * GB_NXB << t.maxlevel,
+                            (long long)t.nrz * GB_NXB << t.maxlevel};
+    const int L = t.level[b];
+    const long long E = (long long)GB_NXB << (t.maxlevel - L);
+    const int* cd = t.coord + 3 * b;
+    long long X[3];
+    X[d] = wrap(side ? (cd[d] + 1) * E : cd[d] * E - 1, N[d]);
+    X[t1] = cd[t1] * E + E / 2;
+    X[t2] = cd[t2] * E + E / 2;
+    leaf_hit h = find_leaf(t, X[0], X[1], X[2]);
+    if (h.node < 0) return;
+    if (h.level < L) {
+        out[0] = 1;
+    } else if (h.level > L) {
+        out[0] = 2;
+        for (int q = 0; q < 4; ++q) {
+            long long Y[3] = {X[0], X[1], X[2]};
+            Y[t1] = cd[t1] * E + E / 4 + (q & 1) * (E / 2);
+            Y[t2] = cd[t2] * E + E / 4 + (q >> 1) * (E / 2);
+            out[1 + q] = find_leaf(t, Y[0], Y[1], Y[2]).node;
+        }
+    }
+}
+
+// The block list reordered finest level first (one CTA; order within a
+// level is arbitrary and does not change any result).
+__global__ void __launch_bounds__(1024) k_sort_levels(const int* __restrict__ list, int n, const int* __restrict__ level,
+                                                      int maxlevel, int* __restrict__ out)
+{
+    __shared__ int cnt[32], off[32];
+    if (threadIdx.x < 32) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    for (int q = threadIdx.x; q < n; q += blockDim.x) atomicAdd(&cnt[min(max(level[list[q]], 0), 31)], 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int l = 31; l >= 0; --l) {
+            off[l] = acc;
+            acc += cnt[l];
+        }
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int b = list[q];
+        out[atomicAdd(&off[min(max(level[b], 0), 31)], 1)] = b;
+    }
+    (void)maxlevel;
+}
 
 __global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list)
 {
@@ -461,6 +527,60 @@ __global__ void k_soa_to_flash(double* __restrict__ out, int nunk, const int* __
 
 }  // namespace
 
+// Allocations and the face-link table of flux conservation (before any
+// capture). Returns whether flux conservation applies to the registered
+// grid (a tree with more than one level).
+static int fc_prepare(int nblk, cudaStream_t s, bool* active)
+{
+    *active = false;
+    if (!g_gb.fc_on || !g_gb.tree_ok || g_gb.tree.maxlevel <= 0 || g_gb.hp.precision < 0) return GB_OK;
+    const int nn = g_gb.tree.nnodes;
+    if (!g_gb.links_ok || g_gb.links_n < nn) {
+        if (g_gb.links_n < nn) {
+            if (g_gb.d_links) cudaFree(g_gb.d_links);
+            g_gb.d_links = nullptr;
+            g_gb.links_n = 0;
+            if (gb_check(cudaMalloc(&g_gb.d_links, (size_t)nn * 6 * 5 * sizeof(int)), "cudaMalloc(links)"))
+                return GB_ERR_CUDA;
+            g_gb.links_n = nn;
+        }
+        k_face_links<<<(nn * 6 + 255) / 256, 256, 0, s>>>(g_gb.tree, g_gb.d_links);
+        if (gb_check(cudaGetLastError(), "k_face_links")) return GB_ERR_CUDA;
+        g_gb.links_ok = true;
+    }
+    const size_t reg = (size_t)nn * 6 * GB_NXB * GB_NXB * gbh::NREG * sizeof(double);
+    if (g_gb.fcreg_bytes < reg) {
+        if (g_gb.d_fcreg) cudaFree(g_gb.d_fcreg);
+        g_gb.d_fcreg = nullptr;
+        g_gb.fcreg_bytes = 0;
+        if (gb_check(cudaMalloc(&g_gb.d_fcreg, reg), "cudaMalloc(flux registers)")) return GB_ERR_CUDA;
+        g_gb.fcreg_bytes = reg;
+    }
+    if (g_gb.fclist_cap < nblk) {
+        if (g_gb.d_fclist) cudaFree(g_gb.d_fclist);
+        g_gb.d_fclist = nullptr;
+        g_gb.fclist_cap = 0;
+        if (gb_check(cudaMalloc(&g_gb.d_fclist, (size_t)nblk * sizeof(int)), "cudaMalloc(level list)"))
+            return GB_ERR_CUDA;
+        g_gb.fclist_cap = nblk;
+    }
+    *active = true;
+    return GB_OK;
+}
+
+int gb_fc_prepare(int nblk, cudaStream_t s)
+{
+    bool on = false;
+    return fc_prepare(nblk, s, &on);
+}
+
+extern "C" int gb_set_flux_correction(int on)
+{
+    g_gb.fc_on = on != 0;
+    g_gb.gen += 1;
+    return GB_OK;
+}
+
 int gb_launch_guardfill(int nblk, const int* list, cudaStream_t s)
 {
     dim3 gc((GB_N3 + 127) / 128, nblk);
@@ -543,6 +663,8 @@ static gbh::hydro_kparams make_kp(double dt, const double* dtp = nullptr)
     gbh::hydro_kparams kp;
     kp.dtp = dtp;
     kp.dtdxp = dtp ? g_gb.d_dtmin + 1 : nullptr;  // written by k_dt_finish
+    kp.fc_links = nullptr;
+    kp.fc_reg = nullptr;
     kp.gamma = g_gb.hp.gamma;
     kp.cvisc = g_gb.hp.cvisc;
     kp.eint_switch = g_gb.hp.eint_switch;
@@ -573,6 +695,18 @@ int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int
     int rc = gb_ensure_scratch(per * (size_t)chunk);
     if (rc) return rc;
     gbh::hydro_kparams kp = make_kp(dt, dtp);
+    bool fc = false;
+    rc = fc_prepare(nblk, s, &fc);
+    if (rc) return rc;
+    if (fc) {
+        // finest level first, so fine boundary fluxes are registered before
+        // the coarse blocks next to them are updated
+        k_sort_levels<<<1, 1024, 0, s>>>(list, nblk, g_gb.tree.level, g_gb.tree.maxlevel, g_gb.d_fclist);
+        if (gb_check(cudaGetLastError(), "k_sort_levels")) return GB_ERR_CUDA;
+        list = g_gb.d_fclist;
+        kp.fc_links = g_gb.d_links;
+        kp.fc_reg = g_gb.d_fcreg;
+    }
     for (int b0 = 0; b0 < nblk; b0 += chunk) {
         int nb = nblk - b0 < chunk ? nblk - b0 : chunk;
         const int fused = cool && gb_cooling_mode() == 0;
@@ -745,6 +879,7 @@ extern "C" int gb_step_graph(int blockCount, const int* list, int cool, gb_drive
         size_t per = g_gb.hp.precision == 1 ? gb_hydro_scratch_bytes_mixed() : gb_hydro_scratch_bytes_fp64();
         int rc = gb_ensure_scratch(per * (size_t)chunk);
         if (!rc && cool && gb_cooling_mode() == 1) rc = gb_sur_prepare((int64_t)chunk * 4096, s);
+        if (!rc) rc = gb_fc_prepare(blockCount, s);
         if (rc) return rc;
         if (gb_check(cudaStreamSynchronize(s), "graph prepare")) return GB_ERR_CUDA;
         if (gb_check(cudaStreamBeginCapture(g_graph.cap, cudaStreamCaptureModeThreadLocal), "begin capture"))

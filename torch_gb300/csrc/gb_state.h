@@ -24,6 +24,16 @@ struct gb_state_t {
     double* d_dtmin = nullptr;
     int* d_all_blocks = nullptr;
     int all_blocks_n = 0;
+    // flux conservation at fine-coarse faces: face links (per store block
+    // 6 x {type, 4 fine leaves}), boundary flux registers, level-sorted list
+    bool fc_on = true;
+    int* d_links = nullptr;
+    int links_n = 0;
+    bool links_ok = false;
+    void* d_fcreg = nullptr;
+    size_t fcreg_bytes = 0;
+    int* d_fclist = nullptr;
+    int fclist_cap = 0;
     // bumped by every call that changes what a captured step graph baked
     // in (grid, tree, parameters, tables, weights, modes)
     unsigned long long gen = 0;

@@ -312,6 +312,11 @@ struct hydro_kparams {
     // exactly, with no division in the kernels.
     double dtdx0[3];
     const double* dtdxp;
+    // flux conservation at fine-coarse faces (null: off): face links of
+    // every store block (6 faces x {type, 4 fine leaves}) and the boundary
+    // flux registers (store block x 6 faces x 256 face cells x NREG, in T)
+    const int* fc_links;
+    void* fc_reg;
 };
 
 __device__ __forceinline__ double kp_dt(const hydro_kparams& kp) { return kp.dtp ? *kp.dtp : kp.dt; }
@@ -885,6 +890,69 @@ k_faceb(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const dou
     double dtd_b = dtd[bb], dtd_c = dtd[c];
     double old = g.f[a][(int64_t)blk * GB_FSZ + gb_fidx(a, I[0], I[1], I[2])];
     bscr[(size_t)cb * bstride + (size_t)a * NFB + f] = old - dtd_b * (ec1 - ec0) + dtd_c * (eb1 - eb0);
+}
+
+// ---------------------------------------------------------------- flux conservation
+// Grid_putFluxData / Grid_conserveFluxes / Grid_getFluxData on a Cartesian
+// mesh: a block whose neighbour across face f is coarser stores its
+// boundary fluxes; a block whose neighbour is finer replaces its boundary
+// fluxes by the mean of the 2 x 2 fine-face fluxes. Blocks are stepped
+// finest level first, so the fine registers are written (put, an earlier
+// chunk or earlier in this one) before a coarse block reads them (get).
+constexpr int NREG = 7;  // rho, mx, my, mz, E, rho e_int, u_n
+enum { FACE_SAME = 0, FACE_COARSER = 1, FACE_FINER = 2 };
+__device__ __forceinline__ int reg_var(int v) { return v < 5 ? v : v + 3; }  // flux slots 0..4, 8, 9
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_fc_put(const int* __restrict__ list, const int* __restrict__ links, T* __restrict__ reg,
+         const T* __restrict__ fscr, size_t fstride)
+{
+    const int f = blockIdx.y, cb = blockIdx.z, c = threadIdx.x;
+    const int blk = list[cb];
+    if (links[((size_t)blk * 6 + f) * 5] != FACE_COARSER) return;
+    const int d = f >> 1, side = f & 1;
+    const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
+    int I[3];
+    I[d] = side ? LO + GB_NXB : LO;
+    I[t1] = LO + c % GB_NXB;
+    I[t2] = LO + c / GB_NXB;
+    const T* fs = fscr + (size_t)cb * fstride + (size_t)d * NFLX * NFC + flux_index(d, I[0], I[1], I[2]);
+    T* r = reg + (((size_t)blk * 6 + f) * (GB_NXB * GB_NXB) + c) * NREG;
+#pragma unroll
+    for (int v = 0; v < NREG; ++v) r[v] = fs[(size_t)reg_var(v) * NFC];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_fc_get(const int* __restrict__ list, const int* __restrict__ links, const T* __restrict__ reg,
+         T* __restrict__ fscr, size_t fstride)
+{
+    const int f = blockIdx.y, cb = blockIdx.z, c = threadIdx.x;
+    const int blk = list[cb];
+    const int* lk = links + ((size_t)blk * 6 + f) * 5;
+    if (lk[0] != FACE_FINER) return;
+    const int d = f >> 1, side = f & 1;
+    const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
+    constexpr int h = GB_NXB / 2;
+    const int c1 = c % GB_NXB, c2 = c / GB_NXB;
+    const int q = (c1 >= h) + 2 * (c2 >= h);
+    const int m = lk[1 + q];
+    if (m < 0) return;
+    const int g1 = 2 * (c1 - h * (c1 >= h)), g2 = 2 * (c2 - h * (c2 >= h));
+    // the fine leaf's face touching this block is the opposite one (f ^ 1)
+    const T* r = reg + ((size_t)m * 6 + (f ^ 1)) * (GB_NXB * GB_NXB) * NREG;
+    const T* r00 = r + (size_t)(g1 + GB_NXB * g2) * NREG;
+    const T* r10 = r + (size_t)(g1 + 1 + GB_NXB * g2) * NREG;
+    const T* r01 = r + (size_t)(g1 + GB_NXB * (g2 + 1)) * NREG;
+    const T* r11 = r + (size_t)(g1 + 1 + GB_NXB * (g2 + 1)) * NREG;
+    int I[3];
+    I[d] = side ? LO + GB_NXB : LO;
+    I[t1] = LO + c1;
+    I[t2] = LO + c2;
+    T* fs = fscr + (size_t)cb * fstride + (size_t)d * NFLX * NFC + flux_index(d, I[0], I[1], I[2]);
+#pragma unroll
+    for (int v = 0; v < NREG; ++v) fs[(size_t)reg_var(v) * NFC] = (T)0.25 * (((r00[v] + r10[v]) + r01[v]) + r11[v]);
 }
 
 // ---------------------------------------------------------------- k_update

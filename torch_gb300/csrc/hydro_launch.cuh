@@ -57,6 +57,11 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
         k_flux<T, false><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);
         gb_prof_end(GBP_FLUX, s);
     }
+    if (kp.fc_links) {
+        dim3 rg2(1, 6, nblk);
+        k_fc_put<T><<<rg2, GB_NXB * GB_NXB, 0, s>>>(list, kp.fc_links, (T*)kp.fc_reg, fscr, SL::flux);
+        k_fc_get<T><<<rg2, GB_NXB * GB_NXB, 0, s>>>(list, kp.fc_links, (const T*)kp.fc_reg, fscr, SL::flux);
+    }
     dim3 ug((GB_NXB * GB_NXB * GB_NXB + 127) / 128, nblk);
     gb_prof_begin(GBP_UPDATE, s);
     if (mhd) {

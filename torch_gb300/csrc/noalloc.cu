@@ -94,6 +94,8 @@ extern "C" int gb_hydro_unsplit_noalloc(int blockCount, const int* blockList_dev
     for (int d = 0; d < 3; ++d) kp.dx[d] = g_gb.tree_ok ? g_gb.tree.root_dx[d] : 1.0;
     for (int d = 0; d < 3; ++d) kp.dtdx0[d] = dt / kp.dx[d];
     kp.dtdxp = nullptr;
+    kp.fc_links = nullptr;  // no flux registers without allocation
+    kp.fc_reg = nullptr;
     return gbh::launch_chunk<double>(kp, g_gb.hp.mhd, 0, blockCount, blockList_dev, scratch, st_dev,
                                      (cudaStream_t)stream);
 }

@@ -101,6 +101,7 @@ _SIG = {
     "gb_get_launch_config": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "gb_step_graph": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gb_set_dt_limits": (C.c_int, [C.c_double, C.c_double, C.c_double]),
+    "gb_set_flux_correction": (C.c_int, [C.c_int]),
     "gb_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
     "gb_graph_reset": (C.c_int, []),
     "gb_graph_info": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
@@ -348,6 +349,11 @@ def init_cooling(p: CoolParams, table_path: str | None = None) -> None:
 def set_dt_limits(dtmin: float = 0.0, dtmax: float = float("inf"), change_factor: float = float("inf")) -> None:
     """Driver_computeDt's limits on every step's dt (code units)."""
     check(lib().gb_set_dt_limits(float(dtmin), float(dtmax), float(change_factor)), "gb_set_dt_limits")
+
+
+def set_flux_correction(on: bool = True) -> None:
+    """Flux conservation at fine-coarse faces (FLASH flux_correct)."""
+    check(lib().gb_set_flux_correction(int(on)), "gb_set_flux_correction")
 
 
 def measure_fp64_peak() -> float:
