@@ -386,6 +386,53 @@ __device__ __forceinline__ void sur_store(const gb_dev_grid& g, const gb_cool_ct
     if (g.slot[GB_PEFL] >= 0) gb_var(g, blk, GB_PEFL)[ci] = 0.0;
 }
 
+// Unit factors of the learned-cooling kernels, divided once on the host:
+// their loads and stores multiply instead of dividing per cell (FP64
+// division is a long sequence on the FP64 pipe). The fallback kernel, which
+// is the plain integrator, keeps sur_load's divisions.
+struct sur_units {
+    double T_of_e;     // (gamma - 1) abar m_p / k_B
+    double e_of_T;     // its inverse: TtoEI
+    double inv_mu_mp;  // 1 / (mu_mol m_p)
+    double vel2, inv_vel2;
+};
+
+__device__ __forceinline__ void sur_load_fast(const gb_dev_grid& g, const gb_cool_ctx& c, const sur_units& u, int blk,
+                                              int ci, gb_cool_vars& v, double& ei, double& temp)
+{
+    const gb_cool_params& p = c.p;
+    v.rho = gb_var(g, blk, GB_DENS)[ci] * p.dens_unit;
+    ei = gb_var(g, blk, GB_EINT)[ci] * u.vel2;
+    temp = ei * u.T_of_e;
+    v.tdust = gb_var(g, blk, GB_TDUS)[ci];
+    v.xHp = g.slot[GB_IHP] >= 0 ? gb_var(g, blk, GB_IHP)[ci] : p.xHp_const;
+    v.ephen = g.slot[GB_PHHE] >= 0 ? gb_var(g, blk, GB_PHHE)[ci] / v.rho : 0.0;
+    v.Gflux = g.slot[GB_PEFL] >= 0 ? gb_var(g, blk, GB_PEFL)[ci] : 0.0;
+    v.mu_mol = p.mu_mol;
+    v.strat_factor = 1.0;
+    v.ndens = v.rho * u.inv_mu_mp;
+    v.TtoEI = u.e_of_T;
+    v.conf = v.ndens * u.inv_mu_mp;  // ndens^2 / rho
+}
+
+__device__ __forceinline__ void sur_store_fast(const gb_dev_grid& g, const gb_cool_ctx& c, const sur_units& u,
+                                               double gamma, int blk, int ci, const gb_cool_vars& v, double ei,
+                                               double temp)
+{
+    const gb_cool_params& p = c.p;
+    if (ei * v.rho < p.smallp) ei = p.smallp / v.rho;
+    double vx = gb_var(g, blk, GB_VELX)[ci], vy = gb_var(g, blk, GB_VELY)[ci], vz = gb_var(g, blk, GB_VELZ)[ci];
+    double e = ei * u.inv_vel2;
+    double rho = gb_var(g, blk, GB_DENS)[ci];
+    gb_var(g, blk, GB_EINT)[ci] = e;
+    gb_var(g, blk, GB_ENER)[ci] = e + 0.5 * (vx * vx + vy * vy + vz * vz);
+    gb_var(g, blk, GB_PRES)[ci] = (gamma - 1.0) * rho * e;
+    gb_var(g, blk, GB_TEMP)[ci] = temp;
+    gb_var(g, blk, GB_TDUS)[ci] = v.tdust;
+    if (g.slot[GB_PHHE] >= 0) gb_var(g, blk, GB_PHHE)[ci] = 0.0;
+    if (g.slot[GB_PEFL] >= 0) gb_var(g, blk, GB_PEFL)[ci] = 0.0;
+}
+
 __device__ __forceinline__ void cell_of(int64_t idx, const int* list, int& blk, int& ci, int& i, int& j, int& k)
 {
     int cb = (int)(idx / 4096), t = (int)(idx % 4096);
@@ -397,7 +444,7 @@ __device__ __forceinline__ void cell_of(int64_t idx, const int* list, int& blk, 
 }
 
 // features + the rate at the old state
-__global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double gamma, const int* __restrict__ list,
+__global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_units un, const int* __restrict__ list,
                            int64_t ncell, double dt_code, const double* __restrict__ dtp, float* __restrict__ feat,
                            float2* __restrict__ f0out)
 {
@@ -408,7 +455,7 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double g
     cell_of(idx, list, blk, ci, i, j, k);
     gb_cool_vars v;
     double ei, temp;
-    sur_load(g, c, gamma, blk, ci, v, ei, temp);
+    sur_load_fast(g, c, un, blk, ci, v, ei, temp);
     gb_cool_varsf vf;
     gbcoolf::make_vars(pf, v, vf);
     const gb_cool_tabf tf = {c.Tf, c.nf, c.lamf, (float)c.T_min, (float)c.nd_min};
@@ -440,10 +487,10 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double g
 // the way the rate at the old state points; otherwise it goes to the
 // fallback list and the plain integrator solves it.
 template <bool CHECK64>
-__global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double gamma, const int* __restrict__ list,
-                             int64_t ncell, double dt_code, const double* __restrict__ dtp, const float* __restrict__ y,
-                             const float2* __restrict__ f0a, double rel_tol, int* __restrict__ rej,
-                             int* __restrict__ nrej, gb_status* st)
+__global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_units un, double gamma,
+                             const int* __restrict__ list, int64_t ncell, double dt_code, const double* __restrict__ dtp,
+                             const float* __restrict__ y, const float2* __restrict__ f0a, double rel_tol,
+                             int* __restrict__ rej, int* __restrict__ nrej, gb_status* st)
 {
     int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= ncell) return;
@@ -453,33 +500,37 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double
     const gb_cool_params& p = c.p;
     gb_cool_vars v;
     double ei0, temp0;
-    sur_load(g, c, gamma, blk, ci, v, ei0, temp0);
+    sur_load_fast(g, c, un, blk, ci, v, ei0, temp0);
     gb_cool_varsf vf;
     gbcoolf::make_vars(pf, v, vf);
     const gb_cool_tabf tf = {c.Tf, c.nf, c.lamf, (float)c.T_min, (float)c.nd_min};
     const double dt = dt_code * p.time_unit;
+    const float dtf = (float)dt;
     const float2 f0fl = f0a[idx];
-    const double f0 = f0fl.x;
+    const float f0 = f0fl.x;
     const float flf = f0fl.y;
     const double emin_ = 0.5 * p.absTmin * v.TtoEI;
     double Tp = (double)((float)temp0 * exp10f((float)gbsur::Y_SCALE * y[idx]));
     bool ok = isfinite(Tp) && Tp > 0.0;
     double ein = 0.0;
     if (ok) {
-        // FP32 secant-Newton from the prediction
-        double ea = ei0, fa = f0;
+        // secant-Newton from the prediction: the residual in FP64 (it is a
+        // small difference of energies), the rate, slope, Jacobian and
+        // Newton quotient in FP32
+        double ea = ei0;
+        float fa = f0;
         double eb = fmax(Tp * v.TtoEI, emin_);
-        double J = 1.0;
+        float J = 1.0f;
         bool conv = false;
         for (int it = 0; it < 4; ++it) {
             float gm, lm;
-            double fb = (double)gbcoolf::dei_parts(pf, tf, vf, flf, (float)eb, &gm, &lm);
-            double gb = eb - dt * fb - ei0;
-            double de = eb - ea;
-            double slope = fabs(de) > 1e-7 * eb ? (fb - fa) / de : 0.0;
-            J = 1.0 - dt * slope;
-            if (!(J > 0.0)) break;
-            double en = eb - gb / J;
+            const float fb = gbcoolf::dei_parts(pf, tf, vf, flf, (float)eb, &gm, &lm);
+            const double gb = eb - dt * (double)fb - ei0;
+            const double de = eb - ea;
+            const float slope = fabs(de) > 1e-7 * eb ? (fb - fa) / (float)de : 0.0f;
+            J = 1.0f - dtf * slope;
+            if (!(J > 0.0f)) break;
+            double en = eb - (double)((float)gb / J);
             if (!isfinite(en)) break;
             if (en < emin_) en = emin_;
             ea = eb;
@@ -496,7 +547,7 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double
         if (conv && CHECK64) {
             double f64 = dei_dt(c, v, cooling_floor(c, v), eb);
             double g64 = eb - dt * f64 - ei0;
-            double delta = g64 / J;
+            double delta = g64 / (double)J;
             ein = eb - delta;
             ok = isfinite(ein) && ein > 0.0 && fabs(delta) <= rel_tol * ein;
         } else {
@@ -508,7 +559,7 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double
         if (ok && f0 > 0.0 && ein < ei0 * (1.0 - rel_tol)) ok = false;
     }
     if (ok) {
-        double temp = ein / v.TtoEI;
+        double temp = ein * un.T_of_e;
         if (temp < p.absTmin) {
             temp = p.absTmin;
             ein = p.absTmin * v.TtoEI;
@@ -518,7 +569,7 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, double
             ein = p.absTmax * v.TtoEI;
             temp = p.absTmax;
         }
-        sur_store(g, c, gamma, blk, ci, v, ein, temp);
+        sur_store_fast(g, c, un, gamma, blk, ci, v, ein, temp);
     } else {
         int slot = atomicAdd(nrej, 1);
         rej[slot] = (int)idx;
@@ -634,7 +685,16 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp,
     const unsigned nb = (unsigned)((ncell + 127) / 128);
     gb_prof_begin(GBP_SUR_FEAT, s);
     const gb_cool_pf pf = make_pf(g_gb.cool.p);
-    k_sur_feat<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, dtp, g_sb.feat, g_sb.f0);
+    sur_units un;
+    {
+        const gb_cool_params& p = g_gb.cool.p;
+        un.T_of_e = (g_gb.hp.gamma - 1.0) * p.eos_abar * p.mp / p.boltz;
+        un.e_of_T = 1.0 / un.T_of_e;
+        un.inv_mu_mp = 1.0 / (p.mu_mol * p.mp);
+        un.vel2 = p.vel_unit * p.vel_unit;
+        un.inv_vel2 = 1.0 / un.vel2;
+    }
+    k_sur_feat<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, un, list, ncell, dt, dtp, g_sb.feat, g_sb.f0);
     gb_prof_end(GBP_SUR_FEAT, s);
     gb_prof_begin(GBP_MLP, s);
     rc = gb_mlp_launch_infer(ncell, g_sb.feat, g_sb.y, s);
@@ -643,10 +703,10 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp,
     cudaMemsetAsync(g_sb.nrej, 0, sizeof(int), s);
     gb_prof_begin(GBP_SUR_ACCEPT, s);
     if (g_sur_check64)
-        k_sur_accept<true><<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, dtp, g_sb.y, g_sb.f0,
+        k_sur_accept<true><<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, un, g_gb.hp.gamma, list, ncell, dt, dtp, g_sb.y, g_sb.f0,
                                               g_sur_tol, g_sb.rej, g_sb.nrej, st);
     else
-        k_sur_accept<false><<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, g_gb.hp.gamma, list, ncell, dt, dtp, g_sb.y, g_sb.f0,
+        k_sur_accept<false><<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, un, g_gb.hp.gamma, list, ncell, dt, dtp, g_sb.y, g_sb.f0,
                                                g_sur_tol, g_sb.rej, g_sb.nrej, st);
     gb_prof_end(GBP_SUR_ACCEPT, s);
     gb_prof_begin(GBP_SUR_FALLBACK, s);

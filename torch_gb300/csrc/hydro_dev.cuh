@@ -369,12 +369,116 @@ __device__ __forceinline__ void load_prim(const gb_dev_grid& g, int blk, int ci,
 // ---------------------------------------------------------------- k_recon
 // blockDim = 3 * TILE: threads [d TILE, (d + 1) TILE) reconstruct direction d
 // for TILE cells (TILE a multiple of 32, so every warp has one direction).
+// The work of a direction is written with the direction as a template
+// parameter, so every register array is indexed by constants; the block
+// barrier between the normal and the transverse part sits in the kernel.
+
+// normal-direction PPM and the normal MHD term of direction D
+template <typename T, bool MHD, int TILE, int D>
+__device__ __forceinline__ void recon_normal(const gb_dev_grid& g, T gam, const double* dtd, const T* hd, int blk,
+                                             int i, int j, int k, int lane, const float* p32b,
+                                             T (*s_sig)[NP][TILE], T (*s_abn)[NP][TILE], T (*s_dnb)[TILE], T* wp,
+                                             T* wn, T* wc)
+{
+    T qs[5][NP];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+        int ii = i + (D == 0 ? m - 2 : 0), jj = j + (D == 1 ? m - 2 : 0), kk = k + (D == 2 ? m - 2 : 0);
+        T w[NP];
+        load_prim<T, MHD>(g, blk, gb_cidx(ii, jj, kk), p32b, w);
+#pragma unroll
+        for (int s = 0; s < NP; ++s) qs[m][s] = w[rot_slot(D, s)];
+    }
+    T wpr[NP], wnr[NP], sgr[NP];
+    ppm_normal<T, MHD>(gam, qs, (T)dtd[D], wpr, wnr, sgr);
+#pragma unroll
+    for (int s = 0; s < NP; ++s) {
+        const int v = rot_slot(D, s);
+        wp[v] = wpr[s];
+        wn[v] = wnr[s];
+        s_sig[D][v][lane] = sgr[s];
+    }
+    load_prim<T, MHD>(g, blk, gb_cidx(i, j, k), p32b, wc);
+    if (MHD) {
+        // multidimensional terms (hy_uhd_dataReconstOneStep.F90:364-424)
+        T uB = wc[1] * wc[5] + wc[2] * wc[6] + wc[3] * wc[7];
+        T row[NP] = {(T)0, -wc[5] / wc[0], -wc[6] / wc[0], -wc[7] / wc[0], (gam - (T)1) * uB,
+                     (T)0, -wc[2], -wc[3]};
+        if (D == 1) { row[5] = -wc[1]; row[6] = (T)0; row[7] = -wc[3]; }
+        if (D == 2) { row[5] = -wc[1]; row[6] = -wc[2]; row[7] = (T)0; }
+        const double* fd = g.f[D] + (int64_t)blk * GB_FSZ;
+        const int ip = i + (D == 0), jp = j + (D == 1), kp2 = k + (D == 2);
+        T dnb = (T)fd[gb_fidx(D, ip, jp, kp2)] - (T)fd[gb_fidx(D, i, j, k)];
+#pragma unroll
+        for (int v = 0; v < NP; ++v) {
+            s_abn[D][v][lane] = row[v];
+            wp[v] = wp[v] - hd[D] * row[v] * dnb;
+            wn[v] = wn[v] - hd[D] * row[v] * dnb;
+        }
+        s_dnb[D][lane] = dnb;
+    }
+}
+
+// transverse corrections of direction D in the vendored order
+// (hy_uhd_dataReconstOneStep.F90:1006-1089)
+template <typename T, bool MHD, int TILE, int D>
+__device__ __forceinline__ void recon_transverse(const T* hd, int lane, T (*s_sig)[NP][TILE], T (*s_abn)[NP][TILE],
+                                                 T (*s_dnb)[TILE], T* wp, T* wn)
+{
+    constexpr int nv = MHD ? 8 : 5;
+#pragma unroll
+    for (int v = 0; v < nv; ++v) {
+        if (D == 0) {
+            wn[v] = wn[v] - hd[1] * s_sig[1][v][lane];
+            wp[v] = wp[v] - hd[1] * s_sig[1][v][lane];
+        } else if (D == 1) {
+            wn[v] = wn[v] - hd[0] * s_sig[0][v][lane];
+            wp[v] = wp[v] - hd[0] * s_sig[0][v][lane];
+        }
+    }
+    if (MHD) {
+#pragma unroll
+        for (int v = 0; v < nv; ++v) {
+            if (D == 0) {
+                wn[v] = wn[v] - hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
+                wp[v] = wp[v] - hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
+            } else if (D == 1) {
+                wn[v] = wn[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane];
+                wp[v] = wp[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane];
+            }
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < nv; ++v) {
+        if (D < 2) {
+            wn[v] = wn[v] - hd[2] * s_sig[2][v][lane];
+            wp[v] = wp[v] - hd[2] * s_sig[2][v][lane];
+        } else {
+            wn[v] = wn[v] - hd[0] * s_sig[0][v][lane] - hd[1] * s_sig[1][v][lane];
+            wp[v] = wp[v] - hd[0] * s_sig[0][v][lane] - hd[1] * s_sig[1][v][lane];
+        }
+    }
+    if (MHD) {
+#pragma unroll
+        for (int v = 0; v < nv; ++v) {
+            if (D < 2) {
+                wn[v] = wn[v] - hd[2] * s_abn[2][v][lane] * s_dnb[2][lane];
+                wp[v] = wp[v] - hd[2] * s_abn[2][v][lane] * s_dnb[2][lane];
+            } else {
+                wn[v] = wn[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane] -
+                        hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
+                wp[v] = wp[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane] -
+                        hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
+            }
+        }
+    }
+}
+
 template <typename T, bool MHD, int TILE>
 __global__ void __launch_bounds__(3 * TILE)
 k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __restrict__ scr,
         size_t scr_stride, const float* __restrict__ p32, size_t p32_stride, gb_status* st)
 {
-    constexpr int nv = MHD ? 8 : 5;
     __shared__ T s_sig[3][NP][TILE];
     __shared__ T s_abn[3][NP][TILE];
     __shared__ T s_dnb[3][TILE];
@@ -390,98 +494,21 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
     double dtd[3];
     kp_dtdx(kp, gb_block_level(g, blk), dtd);
     const T hd[3] = {(T)(0.5 * dtd[0]), (T)(0.5 * dtd[1]), (T)(0.5 * dtd[2])};
-
-    // normal-direction PPM in direction d
-    T qs[5][NP];
-#pragma unroll
-    for (int m = 0; m < 5; ++m) {
-        int ii = i + (d == 0 ? m - 2 : 0), jj = j + (d == 1 ? m - 2 : 0), kk = k + (d == 2 ? m - 2 : 0);
-        T w[NP];
-        load_prim<T, MHD>(g, blk, gb_cidx(ii, jj, kk), p32 + (size_t)cb * p32_stride, w);
-#pragma unroll
-        for (int s = 0; s < NP; ++s) qs[m][s] = w[rot_slot(d, s)];
-    }
-    T wpr[NP], wnr[NP], sgr[NP];
-    ppm_normal<T, MHD>(gam, qs, (T)dtd[d], wpr, wnr, sgr);
-    T wp[NP], wn[NP];
-#pragma unroll
-    for (int s = 0; s < NP; ++s) {
-        int v = rot_slot(d, s);
-        wp[v] = wpr[s];
-        wn[v] = wnr[s];
-        s_sig[d][v][lane] = sgr[s];
-    }
-    T wc[NP];
-    load_prim<T, MHD>(g, blk, gb_cidx(i, j, k), p32 + (size_t)cb * p32_stride, wc);
-    if (MHD) {
-        // multidimensional terms (hy_uhd_dataReconstOneStep.F90:364-424)
-        T uB = wc[1] * wc[5] + wc[2] * wc[6] + wc[3] * wc[7];
-        T row[NP] = {(T)0, -wc[5] / wc[0], -wc[6] / wc[0], -wc[7] / wc[0], (gam - (T)1) * uB,
-                     (T)0, -wc[2], -wc[3]};
-        if (d == 1) { row[5] = -wc[1]; row[6] = (T)0; row[7] = -wc[3]; }
-        if (d == 2) { row[5] = -wc[1]; row[6] = -wc[2]; row[7] = (T)0; }
-        const double* fd = g.f[d] + (int64_t)blk * GB_FSZ;
-        int ip = i + (d == 0), jp = j + (d == 1), kp2 = k + (d == 2);
-        T dnb = (T)fd[gb_fidx(d, ip, jp, kp2)] - (T)fd[gb_fidx(d, i, j, k)];
-#pragma unroll
-        for (int v = 0; v < NP; ++v) {
-            s_abn[d][v][lane] = row[v];
-            wp[v] = wp[v] - hd[d] * row[v] * dnb;
-            wn[v] = wn[v] - hd[d] * row[v] * dnb;
-        }
-        s_dnb[d][lane] = dnb;
-    }
+    const float* p32b = p32 + (size_t)cb * p32_stride;
+    T wp[NP], wn[NP], wc[NP];
+    if (d == 0)
+        recon_normal<T, MHD, TILE, 0>(g, gam, dtd, hd, blk, i, j, k, lane, p32b, s_sig, s_abn, s_dnb, wp, wn, wc);
+    else if (d == 1)
+        recon_normal<T, MHD, TILE, 1>(g, gam, dtd, hd, blk, i, j, k, lane, p32b, s_sig, s_abn, s_dnb, wp, wn, wc);
+    else
+        recon_normal<T, MHD, TILE, 2>(g, gam, dtd, hd, blk, i, j, k, lane, p32b, s_sig, s_abn, s_dnb, wp, wn, wc);
     __syncthreads();
-    // transverse corrections for direction d, vendored order
-    const int a = (d + 1) % 3, b = (d + 2) % 3;
-    (void)a;
-    (void)b;
-#pragma unroll
-    for (int v = 0; v < nv; ++v) {
-        if (d == 0) {
-            wn[v] = wn[v] - hd[1] * s_sig[1][v][lane];
-            wp[v] = wp[v] - hd[1] * s_sig[1][v][lane];
-        } else if (d == 1) {
-            wn[v] = wn[v] - hd[0] * s_sig[0][v][lane];
-            wp[v] = wp[v] - hd[0] * s_sig[0][v][lane];
-        }
-    }
-    if (MHD) {
-#pragma unroll
-        for (int v = 0; v < nv; ++v) {
-            if (d == 0) {
-                wn[v] = wn[v] - hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
-                wp[v] = wp[v] - hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
-            } else if (d == 1) {
-                wn[v] = wn[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane];
-                wp[v] = wp[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane];
-            }
-        }
-    }
-#pragma unroll
-    for (int v = 0; v < nv; ++v) {
-        if (d < 2) {
-            wn[v] = wn[v] - hd[2] * s_sig[2][v][lane];
-            wp[v] = wp[v] - hd[2] * s_sig[2][v][lane];
-        } else {
-            wn[v] = wn[v] - hd[0] * s_sig[0][v][lane] - hd[1] * s_sig[1][v][lane];
-            wp[v] = wp[v] - hd[0] * s_sig[0][v][lane] - hd[1] * s_sig[1][v][lane];
-        }
-    }
-    if (MHD) {
-#pragma unroll
-        for (int v = 0; v < nv; ++v) {
-            if (d < 2) {
-                wn[v] = wn[v] - hd[2] * s_abn[2][v][lane] * s_dnb[2][lane];
-                wp[v] = wp[v] - hd[2] * s_abn[2][v][lane] * s_dnb[2][lane];
-            } else {
-                wn[v] = wn[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane] -
-                        hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
-                wp[v] = wp[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane] -
-                        hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
-            }
-        }
-    }
+    if (d == 0)
+        recon_transverse<T, MHD, TILE, 0>(hd, lane, s_sig, s_abn, s_dnb, wp, wn);
+    else if (d == 1)
+        recon_transverse<T, MHD, TILE, 1>(hd, lane, s_sig, s_abn, s_dnb, wp, wn);
+    else
+        recon_transverse<T, MHD, TILE, 2>(hd, lane, s_sig, s_abn, s_dnb, wp, wn);
     // positivity fallback
     bool fell = (wn[0] < (T)0 || wp[0] < (T)0 || wn[4] < (T)0 || wp[4] < (T)0);
     if (fell) {
@@ -681,12 +708,11 @@ __device__ __forceinline__ int rc_index(int i, int j, int k)
 }
 
 // ---------------------------------------------------------------- k_flux
-template <typename T, bool MHD>
-__global__ void __launch_bounds__(128)
-k_flux(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* __restrict__ rscr,
+template <typename T, bool MHD, int D>
+__device__ __forceinline__ void flux_face(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* __restrict__ rscr,
        size_t rstride, T* __restrict__ fscr, size_t fstride, const float* __restrict__ p32, size_t p32_stride)
 {
-    const int d = blockIdx.y;
+    constexpr int d = D;
     const int cb = blockIdx.z;
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= NFC) return;
@@ -773,6 +799,17 @@ k_flux(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* _
     for (int s = 0; s < NP; ++s) fs[(size_t)s * NFC + f] = out[s];
     fs[(size_t)8 * NFC + f] = feint;
     fs[(size_t)9 * NFC + f] = un;
+}
+
+template <typename T, bool MHD>
+__global__ void __launch_bounds__(128)
+k_flux(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* __restrict__ rscr,
+       size_t rstride, T* __restrict__ fscr, size_t fstride, const float* __restrict__ p32, size_t p32_stride)
+{
+    // the direction is uniform over the CTA: a compile-time index in each branch
+    if (blockIdx.y == 0) flux_face<T, MHD, 0>(g, kp, list, rscr, rstride, fscr, fstride, p32, p32_stride);
+    else if (blockIdx.y == 1) flux_face<T, MHD, 1>(g, kp, list, rscr, rstride, fscr, fstride, p32, p32_stride);
+    else flux_face<T, MHD, 2>(g, kp, list, rscr, rstride, fscr, fstride, p32, p32_stride);
 }
 
 // ---------------------------------------------------------------- k_emf
@@ -865,11 +902,12 @@ __device__ __forceinline__ int fb_index(int a, int i, int j, int k)
     return (I[a] - LO) + 17 * ((I[t1] - LO) + 16 * (I[t2] - LO));
 }
 
-static __global__ void __launch_bounds__(128)
-k_faceb(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const double* __restrict__ escr,
-        size_t estride, double* __restrict__ bscr, size_t bstride)
+template <int A>
+__device__ __forceinline__ void faceb_face(const gb_dev_grid& g, const hydro_kparams& kp, const int* __restrict__ list,
+                                           const double* __restrict__ escr, size_t estride, double* __restrict__ bscr,
+                                           size_t bstride)
 {
-    const int a = blockIdx.y;
+    constexpr int a = A;
     const int cb = blockIdx.z;
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= NFB) return;
@@ -890,6 +928,15 @@ k_faceb(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const dou
     double dtd_b = dtd[bb], dtd_c = dtd[c];
     double old = g.f[a][(int64_t)blk * GB_FSZ + gb_fidx(a, I[0], I[1], I[2])];
     bscr[(size_t)cb * bstride + (size_t)a * NFB + f] = old - dtd_b * (ec1 - ec0) + dtd_c * (eb1 - eb0);
+}
+
+static __global__ void __launch_bounds__(128)
+k_faceb(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const double* __restrict__ escr,
+        size_t estride, double* __restrict__ bscr, size_t bstride)
+{
+    if (blockIdx.y == 0) faceb_face<0>(g, kp, list, escr, estride, bscr, bstride);
+    else if (blockIdx.y == 1) faceb_face<1>(g, kp, list, escr, estride, bscr, bstride);
+    else faceb_face<2>(g, kp, list, escr, estride, bscr, bstride);
 }
 
 // ---------------------------------------------------------------- flux conservation
@@ -974,10 +1021,15 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
     double rho = UV(GB_DENS), vx = UV(GB_VELX), vy = UV(GB_VELY), vz = UV(GB_VELZ), pr = UV(GB_PRES);
     double Bc[3] = {0.0, 0.0, 0.0};
     if (MHD) { Bc[0] = UV(GB_MAGX); Bc[1] = UV(GB_MAGY); Bc[2] = UV(GB_MAGZ); }
+    // the mixed path replaces the divisions of the conversions by one
+    // reciprocal of the density (FP64 divisions are long instruction
+    // sequences on the FP64 pipe); the FP64 path keeps the oracle's operations
+    constexpr bool RCP = std::is_same<T, float>::value;
     double Uc[NP];
     Uc[0] = rho;
     Uc[1] = rho * vx; Uc[2] = rho * vy; Uc[3] = rho * vz;
-    Uc[4] = pr / gm1 + 0.5 * rho * (vx * vx + vy * vy + vz * vz) + 0.5 * (Bc[0] * Bc[0] + Bc[1] * Bc[1] + Bc[2] * Bc[2]);
+    Uc[4] = (RCP ? pr * (1.0 / gm1) : pr / gm1) + 0.5 * rho * (vx * vx + vy * vy + vz * vz) +
+            0.5 * (Bc[0] * Bc[0] + Bc[1] * Bc[1] + Bc[2] * Bc[2]);
     Uc[5] = Bc[0]; Uc[6] = Bc[1]; Uc[7] = Bc[2];
     double re = rho * UV(GB_EINT);
     const T* fs = fscr + (size_t)cb * fstride;
@@ -1017,11 +1069,13 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
         if (k == HI) g.f[2][(int64_t)blk * GB_FSZ + gb_fidx(2, i, j, k + 1)] = bhi[2];
     }
     double rn = fmax(Un[0], kp.smlrho);
-    double ek = 0.5 * (Un[1] * Un[1] + Un[2] * Un[2] + Un[3] * Un[3]) / rn;
+    const double irn = RCP ? 1.0 / rn : 0.0;
+    auto over_rn = [&](double x) { return RCP ? x * irn : x / rn; };
+    double ek = over_rn(0.5 * (Un[1] * Un[1] + Un[2] * Un[2] + Un[3] * Un[3]));
     double em = 0.5 * (Bn[0] * Bn[0] + Bn[1] * Bn[1] + Bn[2] * Bn[2]);
-    double eiE = ((Un[4] - ek) - em) / rn;
-    double eia = ren / rn;
-    bool use_E = eiE > kp.eint_switch * (Un[4] / rn);
+    double eiE = over_rn((Un[4] - ek) - em);
+    double eia = over_rn(ren);
+    bool use_E = eiE > kp.eint_switch * over_rn(Un[4]);
     double ei = use_E ? eiE : eia;
     double pn = gm1 * rn * ei;
     bool floored = false;
@@ -1030,7 +1084,7 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
         ei = pn / (gm1 * rn);
         floored = true;
     }
-    double vxn = Un[1] / rn, vyn = Un[2] / rn, vzn = Un[3] / rn;
+    double vxn = over_rn(Un[1]), vyn = over_rn(Un[2]), vzn = over_rn(Un[3]);
     double ekin_s = 0.5 * (vxn * vxn + vyn * vyn + vzn * vzn);
     if (COOL) {
         // fused heating/cooling epilogue (RadHeat.F90:223-423 on the new state)
@@ -1084,49 +1138,53 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
 }
 
 // ---------------------------------------------------------------- CFL
+// R = double: the oracle's arithmetic; R = float (mixed path): the same
+// limit from FP32 arithmetic on the FP64 state (dt to ~1e-7 relative)
+template <typename R>
 static __global__ void __launch_bounds__(256)
 k_dtlimit(gb_dev_grid g, double gamma, int mhd, double dx0, double dx1, double dx2,
           const int* __restrict__ list, unsigned long long* __restrict__ out_bits)
 {
     const int blk = list[blockIdx.y];
     const double root[3] = {dx0, dx1, dx2};
-    double del[3];
-    gb_block_dx(g, root, blk, del);
-    double best = 1e300;
+    double deld[3];
+    gb_block_dx(g, root, blk, deld);
+    const R del[3] = {(R)deld[0], (R)deld[1], (R)deld[2]};
+    R best = (R)1e30;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < GB_NXB * GB_NXB * GB_NXB; t += gridDim.x * blockDim.x) {
         const int i = LO + t % GB_NXB, j = LO + (t / GB_NXB) % GB_NXB, k = LO + t / (GB_NXB * GB_NXB);
         const int ci = gb_cidx(i, j, k);
         const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3 + ci;
-        double rho = base[(int64_t)g.slot[GB_DENS] * GB_N3], p = base[(int64_t)g.slot[GB_PRES] * GB_N3];
-        double B[3] = {0, 0, 0};
+        R rho = (R)base[(int64_t)g.slot[GB_DENS] * GB_N3], p = (R)base[(int64_t)g.slot[GB_PRES] * GB_N3];
+        R B[3] = {0, 0, 0};
         if (mhd) {
-            B[0] = base[(int64_t)g.slot[GB_MAGX] * GB_N3];
-            B[1] = base[(int64_t)g.slot[GB_MAGY] * GB_N3];
-            B[2] = base[(int64_t)g.slot[GB_MAGZ] * GB_N3];
+            B[0] = (R)base[(int64_t)g.slot[GB_MAGX] * GB_N3];
+            B[1] = (R)base[(int64_t)g.slot[GB_MAGY] * GB_N3];
+            B[2] = (R)base[(int64_t)g.slot[GB_MAGZ] * GB_N3];
         }
-        double gp = gamma * p;
-        double B2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
-        double tt = (gp + B2) / rho;
+        R gp = (R)gamma * p;
+        R B2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+        R tt = (gp + B2) / rho;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            double v = fabs(base[(int64_t)g.slot[GB_VELX + d] * GB_N3]);
-            double cf = sqrt(0.5 * (tt + sqrt(fmax(tt * tt - 4.0 * gp * B[d] * B[d] / (rho * rho), 0.0))));
-            double dtc = del[d] / (v + cf);
+            R v = fabs((R)base[(int64_t)g.slot[GB_VELX + d] * GB_N3]);
+            R cf = sqrt((R)0.5 * (tt + sqrt(fmax(tt * tt - (R)4 * gp * B[d] * B[d] / (rho * rho), (R)0))));
+            R dtc = del[d] / (v + cf);
             best = fmin(best, dtc);
         }
     }
     // warp shuffle then block reduction of the minimum
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, o));
-    __shared__ double s_min[8];
+    __shared__ R s_min[8];
     if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = best;
     __syncthreads();
     if (threadIdx.x < 32) {
-        best = threadIdx.x < (blockDim.x >> 5) ? s_min[threadIdx.x] : 1e300;
+        best = threadIdx.x < (blockDim.x >> 5) ? s_min[threadIdx.x] : (R)1e30;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, o));
         // positive doubles order like their bit patterns
-        if (threadIdx.x == 0) atomicMin(out_bits, (unsigned long long)__double_as_longlong(best));
+        if (threadIdx.x == 0) atomicMin(out_bits, (unsigned long long)__double_as_longlong((double)best));
     }
 }
 

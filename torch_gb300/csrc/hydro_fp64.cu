@@ -10,10 +10,15 @@ int gb_hydro_chunk_fp64(const gbh::hydro_kparams& kp, int mhd, int cool, int nbl
     return gbh::launch_chunk<double>(kp, mhd, cool, nblk, list, scratch, st, s);
 }
 
+int gb_dt_launch_f32(const gbh::hydro_kparams& kp, int mhd, int nblk, const int* list,
+                     unsigned long long* bits, cudaStream_t s);
+
 int gb_dt_launch(const gbh::hydro_kparams& kp, int mhd, int nblk, const int* list,
                  unsigned long long* bits, cudaStream_t s)
 {
     dim3 g(4, nblk);
-    gbh::k_dtlimit<<<g, 256, 0, s>>>(g_gb.grid, kp.gamma, mhd, kp.dx[0], kp.dx[1], kp.dx[2], list, bits);
+    if (g_gb.hp.precision == 1)
+        return gb_dt_launch_f32(kp, mhd, nblk, list, bits, s);
+    gbh::k_dtlimit<double><<<g, 256, 0, s>>>(g_gb.grid, kp.gamma, mhd, kp.dx[0], kp.dx[1], kp.dx[2], list, bits);
     return gb_check(cudaGetLastError(), "k_dtlimit") ? GB_ERR_CUDA : GB_OK;
 }

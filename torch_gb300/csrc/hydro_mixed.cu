@@ -10,3 +10,12 @@ int gb_hydro_chunk_mixed(const gbh::hydro_kparams& kp, int mhd, int cool, int nb
 {
     return gbh::launch_chunk<float>(kp, mhd, cool, nblk, list, scratch, st, s);
 }
+
+// CFL limit of the mixed path: FP32 arithmetic on the FP64 state
+int gb_dt_launch_f32(const gbh::hydro_kparams& kp, int mhd, int nblk, const int* list,
+                     unsigned long long* bits, cudaStream_t s)
+{
+    dim3 g(4, nblk);
+    gbh::k_dtlimit<float><<<g, 256, 0, s>>>(g_gb.grid, kp.gamma, mhd, kp.dx[0], kp.dx[1], kp.dx[2], list, bits);
+    return gb_check(cudaGetLastError(), "k_dtlimit<float>") ? GB_ERR_CUDA : GB_OK;
+}
