@@ -194,18 +194,37 @@ __device__ __forceinline__ void bfrag(const __nv_bfloat16* w, int K, int kt, int
     b1 = *reinterpret_cast<const uint32_t*>(p + 8);
 }
 
-// one hidden layer: acc[8 n-tiles][4] = A(16 x K) * W^T + bias, then SiLU
-// and repack to the A fragments of the next layer
-template <int KT>
-__device__ __forceinline__ void hidden_layer(const uint32_t (*afr)[4], const __nv_bfloat16* w, const float* bias,
-                                             int lane, uint32_t (*anext)[4])
+// SiLU for inference: z sigmoid(z) = h (1 + tanh h), h = z / 2, with the
+// hardware tanh approximation (one MUFU operation; its ~2^-11 relative
+// error is below the BF16 rounding the activation gets next)
+__device__ __forceinline__ float tanh_approx(float x)
 {
-    const int g = lane >> 2, t = lane & 3;
-    float acc[8][4];
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float silu_infer(float z)
+{
+    const float h = 0.5f * z;
+    return fmaf(h, tanh_approx(h), h);
+}
+
+// one hidden layer for NT 16-row tiles: acc[tile][8 n-tiles][4] = A(16 x K)
+// W^T + bias, then SiLU and repack to the A fragments of the next layer.
+// Each B fragment is read from shared memory once for all NT tiles.
+template <int KT, int NT>
+__device__ __forceinline__ void hidden_layer(const uint32_t (*afr)[4][4], const __nv_bfloat16* w, const float* bias,
+                                             int lane, uint32_t (*anext)[4][4])
+{
+    const int t = lane & 3;
+    float acc[NT][8][4];
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt) {
         float b0 = bias[nt * 8 + t * 2], b1 = bias[nt * 8 + t * 2 + 1];
-        acc[nt][0] = b0; acc[nt][1] = b1; acc[nt][2] = b0; acc[nt][3] = b1;
+#pragma unroll
+        for (int q = 0; q < NT; ++q) {
+            acc[q][nt][0] = b0; acc[q][nt][1] = b1; acc[q][nt][2] = b0; acc[q][nt][3] = b1;
+        }
     }
 #pragma unroll
     for (int kt = 0; kt < KT; ++kt)
@@ -213,17 +232,21 @@ __device__ __forceinline__ void hidden_layer(const uint32_t (*afr)[4], const __n
         for (int nt = 0; nt < 8; ++nt) {
             uint32_t b0, b1;
             bfrag(w, KT * 16, kt, nt, lane, b0, b1);
-            mma_bf16(acc[nt], afr[kt], b0, b1);
-        }
-    (void)g;
 #pragma unroll
-    for (int kt = 0; kt < 4; ++kt) {
-        anext[kt][0] = pack2(silu(acc[2 * kt][0]), silu(acc[2 * kt][1]));
-        anext[kt][1] = pack2(silu(acc[2 * kt][2]), silu(acc[2 * kt][3]));
-        anext[kt][2] = pack2(silu(acc[2 * kt + 1][0]), silu(acc[2 * kt + 1][1]));
-        anext[kt][3] = pack2(silu(acc[2 * kt + 1][2]), silu(acc[2 * kt + 1][3]));
-    }
+            for (int q = 0; q < NT; ++q) mma_bf16(acc[q][nt], afr[q][kt], b0, b1);
+        }
+#pragma unroll
+    for (int q = 0; q < NT; ++q)
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt) {
+            anext[q][kt][0] = pack2(silu_infer(acc[q][2 * kt][0]), silu_infer(acc[q][2 * kt][1]));
+            anext[q][kt][1] = pack2(silu_infer(acc[q][2 * kt][2]), silu_infer(acc[q][2 * kt][3]));
+            anext[q][kt][2] = pack2(silu_infer(acc[q][2 * kt + 1][0]), silu_infer(acc[q][2 * kt + 1][1]));
+            anext[q][kt][3] = pack2(silu_infer(acc[q][2 * kt + 1][2]), silu_infer(acc[q][2 * kt + 1][3]));
+        }
 }
+
+constexpr int INFER_NT = 2;  // 16-row tiles per warp iteration
 
 __global__ void __launch_bounds__(128) k_mlp_infer(int64_t n, const float* __restrict__ feat,
                                                    const __nv_bfloat16* __restrict__ wpk,
@@ -237,34 +260,48 @@ __global__ void __launch_bounds__(128) k_mlp_infer(int64_t n, const float* __res
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane >> 2, t = lane & 3;
-    const int64_t ntiles = (n + 15) / 16;
-    for (int64_t tile = (int64_t)blockIdx.x * 4 + warp; tile < ntiles; tile += (int64_t)gridDim.x * 4) {
-        const int64_t r0 = tile * 16 + g, r1 = r0 + 8;
-        // layer 1 A fragment: features in columns 0..3, zero-padded to 16
-        float f0[4] = {0, 0, 0, 0}, f1[4] = {0, 0, 0, 0};
-        if (r0 < n) { float4 v = reinterpret_cast<const float4*>(feat)[r0]; f0[0] = v.x; f0[1] = v.y; f0[2] = v.z; f0[3] = v.w; }
-        if (r1 < n) { float4 v = reinterpret_cast<const float4*>(feat)[r1]; f1[0] = v.x; f1[1] = v.y; f1[2] = v.z; f1[3] = v.w; }
-        uint32_t a1[1][4];
+    constexpr int NT = INFER_NT;
+    const int64_t ngroups = (n + 16 * NT - 1) / (16 * NT);
+    for (int64_t grp = (int64_t)blockIdx.x * 4 + warp; grp < ngroups; grp += (int64_t)gridDim.x * 4) {
+        // layer 1 A fragments: features in columns 0..3, zero-padded to 16;
         // columns t*2, t*2+1 (only t < 2 carry features)
-        a1[0][0] = t < 2 ? pack2(f0[t * 2], f0[t * 2 + 1]) : 0u;
-        a1[0][1] = t < 2 ? pack2(f1[t * 2], f1[t * 2 + 1]) : 0u;
-        a1[0][2] = 0u;
-        a1[0][3] = 0u;
-        uint32_t h1[4][4], h2[4][4], h3[4][4];
-        hidden_layer<1>(a1, sw + packed_layout::W1, sbias, lane, h1);
-        hidden_layer<4>(h1, sw + packed_layout::W2, sbias + H, lane, h2);
-        hidden_layer<4>(h2, sw + packed_layout::W3, sbias + 2 * H, lane, h3);
-        float out[4] = {sbias[3 * H], 0.0f, sbias[3 * H], 0.0f};
+        uint32_t a1[NT][4][4];
+        int64_t r0[NT];
+#pragma unroll
+        for (int q = 0; q < NT; ++q) {
+            r0[q] = (grp * NT + q) * 16 + g;
+            const int64_t r1 = r0[q] + 8;
+            float f0[4] = {0, 0, 0, 0}, f1[4] = {0, 0, 0, 0};
+            if (r0[q] < n) { float4 v = reinterpret_cast<const float4*>(feat)[r0[q]]; f0[0] = v.x; f0[1] = v.y; f0[2] = v.z; f0[3] = v.w; }
+            if (r1 < n) { float4 v = reinterpret_cast<const float4*>(feat)[r1]; f1[0] = v.x; f1[1] = v.y; f1[2] = v.z; f1[3] = v.w; }
+            a1[q][0][0] = t < 2 ? pack2(f0[t * 2], f0[t * 2 + 1]) : 0u;
+            a1[q][0][1] = t < 2 ? pack2(f1[t * 2], f1[t * 2 + 1]) : 0u;
+            a1[q][0][2] = 0u;
+            a1[q][0][3] = 0u;
+        }
+        uint32_t h1[NT][4][4], h2[NT][4][4];
+        hidden_layer<1, NT>(a1, sw + packed_layout::W1, sbias, lane, h1);
+        hidden_layer<4, NT>(h1, sw + packed_layout::W2, sbias + H, lane, h2);
+        hidden_layer<4, NT>(h2, sw + packed_layout::W3, sbias + 2 * H, lane, h1);
+        float out[NT][4];
+#pragma unroll
+        for (int q = 0; q < NT; ++q) {
+            out[q][0] = sbias[3 * H]; out[q][1] = 0.0f; out[q][2] = sbias[3 * H]; out[q][3] = 0.0f;
+        }
 #pragma unroll
         for (int kt = 0; kt < 4; ++kt) {
             uint32_t b0, b1;
             bfrag(sw + packed_layout::W4, H, kt, 0, lane, b0, b1);
-            mma_bf16(out, h3[kt], b0, b1);
+#pragma unroll
+            for (int q = 0; q < NT; ++q) mma_bf16(out[q], h1[q][kt], b0, b1);
         }
         // column 0 lives in the t == 0 lanes: out[0] row g, out[2] row g + 8
         if (t == 0) {
-            if (r0 < n) y[r0] = out[0];
-            if (r1 < n) y[r1] = out[2];
+#pragma unroll
+            for (int q = 0; q < NT; ++q) {
+                if (r0[q] < n) y[r0[q]] = out[q][0];
+                if (r0[q] + 8 < n) y[r0[q] + 8] = out[q][2];
+            }
         }
     }
 }
@@ -504,9 +541,9 @@ int gb_mlp_launch_infer(int64_t n, const float* feat, float* y, cudaStream_t s)
 {
     int rc = gb_mlp_pack(s);
     if (rc) return rc;
-    int64_t tiles = (n + 15) / 16;
-    int64_t blocks = (tiles + 3) / 4;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    int64_t groups = (n + 16 * INFER_NT - 1) / (16 * INFER_NT);
+    int64_t blocks = (groups + 3) / 4;
+    if (blocks > 152 * 8) blocks = 152 * 8;
     if (blocks < 1) blocks = 1;
     k_mlp_infer<<<(unsigned)blocks, 128, 0, s>>>(n, feat, g_mlp.pk, g_mlp.pb, y);
     return gb_check(cudaGetLastError(), "k_mlp_infer") ? GB_ERR_CUDA : GB_OK;
