@@ -112,7 +112,10 @@ int gb_register_grid(const gb_grid_desc* grid, const gb_tree_desc* tree);
  * neighbours: same-level copy, injection from a coarser neighbour,
  * restriction (8-cell mean) from a finer one, periodic domain. The role
  * FLASH's Grid_fillGuardCells plays before Hydro
- * (src/flash/source/Driver/DriverMain/Unsplit/Couple_AMUSE/Driver_computeDt.F90:243). */
+ * (src/flash/source/Driver/DriverMain/Unsplit/Couple_AMUSE/Driver_computeDt.F90:243).
+ * Cell variables filled: the ones the step reads (DENS, VEL*, PRES, ENER,
+ * EINT, MAG*), as FLASH's Hydro fills with a variable mask; other slots
+ * (TEMP, TDUS, ...) keep their guard values. */
 int gb_fill_guardcells(int blockCount, const int* blockList_dev, void* stream);
 
 /* ---------------------------------------------------------------- hydro */

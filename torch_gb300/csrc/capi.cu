@@ -345,15 +345,51 @@ __global__ void __launch_bounds__(1024) k_sort_levels(const int* __restrict__ li
     (void)maxlevel;
 }
 
-__global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list)
+// The guard cells of a padded block, enumerated as slabs: the two z slabs
+// (k < 4 or k >= 20, all j, i), the two y slabs inside them, the two x slabs
+// inside those. 2 * 4 * 24 * 24 + 2 * 4 * 16 * 24 + 2 * 4 * 16 * 16 = 9728.
+constexpr int GZ = 2 * GB_NGUARD * GB_N * GB_N, GY = 2 * GB_NGUARD * GB_NXB * GB_N, GX = 2 * GB_NGUARD * GB_NXB * GB_NXB;
+constexpr int GB_NGC = GZ + GY + GX;
+static_assert(GB_NGC == GB_N3 - GB_NXB * GB_NXB * GB_NXB, "guard cell count");
+
+__device__ __forceinline__ void guard_cell(int q, int& i, int& j, int& k)
+{
+    const int lo = GB_NGUARD, hi = GB_NGUARD + GB_NXB;
+    if (q < GZ) {
+        const int zz = q / (GB_N * GB_N), r = q % (GB_N * GB_N);
+        k = zz < GB_NGUARD ? zz : hi + (zz - GB_NGUARD);
+        j = r / GB_N;
+        i = r % GB_N;
+    } else if (q < GZ + GY) {
+        q -= GZ;
+        const int yy = q / (GB_NXB * GB_N), r = q % (GB_NXB * GB_N);
+        j = yy < GB_NGUARD ? yy : hi + (yy - GB_NGUARD);
+        k = lo + r / GB_N;
+        i = r % GB_N;
+    } else {
+        q -= GZ + GY;
+        const int xx = q / (GB_NXB * GB_NXB), r = q % (GB_NXB * GB_NXB);
+        i = xx < GB_NGUARD ? xx : hi + (xx - GB_NGUARD);
+        k = lo + r / GB_NXB;
+        j = lo + r % GB_NXB;
+    }
+}
+
+// The variables the hydro step reads in guard cells (FLASH fills guard
+// cells for Hydro with a variable mask the same way); store slots, -1 = absent
+struct guard_vars {
+    int n;
+    int slot[GB_NROLE];
+};
+
+__global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list, guard_vars gv)
 {
     const int blk = list[blockIdx.y];
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= GB_N3) return;
-    const int i = c % GB_N, j = (c / GB_N) % GB_N, k = c / (GB_N * GB_N);
-    if (i >= GB_NGUARD && i < GB_NGUARD + GB_NXB && j >= GB_NGUARD && j < GB_NGUARD + GB_NXB &&
-        k >= GB_NGUARD && k < GB_NGUARD + GB_NXB)
-        return;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= GB_NGC) return;
+    int i, j, k;
+    guard_cell(q, i, j, k);
+    const int c = gb_cidx(i, j, k);
     const int L = t.level[blk];
     const int ls = t.maxlevel - L;  // log2 of this block's cell size in finest cells
     const long long s = 1LL << ls;
@@ -378,7 +414,10 @@ __global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restri
         int sj = (int)((X[1] >> lsl) - (long long)sc[1] * GB_NXB) + GB_NGUARD;
         int sk = (int)((X[2] >> lsl) - (long long)sc[2] * GB_NXB) + GB_NGUARD;
         int sci = gb_cidx(si, sj, sk);
-        for (int v = 0; v < g.nvar; ++v) dst[(int64_t)v * GB_N3] = src[(int64_t)v * GB_N3 + sci];
+        for (int q2 = 0; q2 < gv.n; ++q2) {
+            const int64_t v = gv.slot[q2];
+            dst[v * GB_N3] = src[v * GB_N3 + sci];
+        }
     } else {
         // finer neighbour: mean of the fine cells covering this cell
         int r = 1 << (ls - lsl);
@@ -386,7 +425,8 @@ __global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restri
         int bj = (int)((lo[1] >> lsl) - (long long)sc[1] * GB_NXB) + GB_NGUARD;
         int bk = (int)((lo[2] >> lsl) - (long long)sc[2] * GB_NXB) + GB_NGUARD;
         double inv = 1.0 / (double)(r * r * r);
-        for (int v = 0; v < g.nvar; ++v) {
+        for (int q2 = 0; q2 < gv.n; ++q2) {
+            const int64_t v = gv.slot[q2];
             double acc = 0.0;
             for (int z = 0; z < r; ++z)
                 for (int y = 0; y < r; ++y)
@@ -581,11 +621,21 @@ extern "C" int gb_set_flux_correction(int on)
     return GB_OK;
 }
 
+static guard_vars hydro_guard_vars()
+{
+    guard_vars gv;
+    gv.n = 0;
+    const int roles[] = {GB_DENS, GB_VELX, GB_VELY, GB_VELZ, GB_PRES, GB_ENER, GB_EINT, GB_MAGX, GB_MAGY, GB_MAGZ};
+    for (int r : roles)
+        if (g_gb.grid.slot[r] >= 0) gv.slot[gv.n++] = g_gb.grid.slot[r];
+    return gv;
+}
+
 int gb_launch_guardfill(int nblk, const int* list, cudaStream_t s)
 {
-    dim3 gc((GB_N3 + 127) / 128, nblk);
+    dim3 gc((GB_NGC + 127) / 128, nblk);
     gb_prof_begin(GBP_GUARD, s);
-    k_guard_cells<<<gc, 128, 0, s>>>(g_gb.grid, g_gb.tree, list);
+    k_guard_cells<<<gc, 128, 0, s>>>(g_gb.grid, g_gb.tree, list, hydro_guard_vars());
     gb_prof_end(GBP_GUARD, s);
     if (g_gb.hp.mhd && g_gb.grid.f[0]) {
         dim3 gf((GB_FSZ + 127) / 128, nblk, 3);
@@ -606,8 +656,8 @@ extern "C" int gb_fill_guardcells(int blockCount, const int* list, void* stream)
     if (blockCount == 0) return GB_OK;
     // the face pass needs to know whether face fields exist; it is keyed on
     // the hydro parameters when set and on the grid otherwise
-    dim3 gc((GB_N3 + 127) / 128, blockCount);
-    k_guard_cells<<<gc, 128, 0, (cudaStream_t)stream>>>(g_gb.grid, g_gb.tree, list);
+    dim3 gc((GB_NGC + 127) / 128, blockCount);
+    k_guard_cells<<<gc, 128, 0, (cudaStream_t)stream>>>(g_gb.grid, g_gb.tree, list, hydro_guard_vars());
     if (g_gb.grid.f[0] && g_gb.grid.f[1] && g_gb.grid.f[2]) {
         dim3 gf((GB_FSZ + 127) / 128, blockCount, 3);
         k_guard_faces<<<gf, 128, 0, (cudaStream_t)stream>>>(g_gb.grid, g_gb.tree, list);
