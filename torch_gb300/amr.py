@@ -135,6 +135,16 @@ def config3_tree(seed: int = 45):
     return build_tree(13, centres, [140, 100, 32]), centres
 
 
+def config5_tree(seed: int = 47):
+    """The full-scale tree: 16^3 root blocks refined (760, 600, 330, 65) ->
+    leaves 3336 / 5480 / 4470 / 2575 / 520 over 5 levels (16381 blocks,
+    67.1 M zones) around 8 seeded centres. (A cubic root grid cannot give
+    exactly 16384 leaves: nr^3 + 7 * refined never equals it.)"""
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0.1, 0.9, (8, 3))
+    return build_tree(16, centres, [760, 600, 330, 65]), centres
+
+
 def _trilinear(base, pts):
     """Periodic trilinear sample of base[x, y, z] (cell-centred values on an
     N^3 grid of the unit cube) at pts[..., 3] in unit-cube coordinates."""
