@@ -1182,6 +1182,18 @@ void orc_fill_guards_leaf(const orc_hydro_params* p, int b, const int* level, co
                             X[d] = lo[d] + (d == a ? 0 : s / 2);
                         }
                         int m = orc_leaf_at(level, child, root, nr0, nr1, maxlevel, X[0], X[1], X[2]);
+                        if (level[m] != L) {
+                            /* a face on a level boundary: the copy owned by the leaf of this
+                             * block's level on the lower side, when there is one, so that
+                             * every block of a level reads the same face */
+                            long long Y[3] = {X[0], X[1], X[2]};
+                            Y[a] = orc_wrap(X[a] - 1, N[a]);
+                            int m2 = orc_leaf_at(level, child, root, nr0, nr1, maxlevel, Y[0], Y[1], Y[2]);
+                            if (level[m2] == L) {
+                                m = m2;
+                                X[a] = Y[a] + 1; /* its upper face, unwrapped at the domain edge */
+                            }
+                        }
                         const long long sl = 1LL << (maxlevel - level[m]);
                         const int* sc = coord + 3 * m;
                         const double* src = fa[a] + (int64_t)m * fsz;

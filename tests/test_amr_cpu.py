@@ -109,10 +109,10 @@ def _amr_totals(t, st, u, fx=None):
 @pytest.mark.parametrize("mhd", [False, True])
 def test_flux_correction_conserves_across_levels(oracle, mhd):
     """Flux conservation at fine-coarse faces: over a periodic 3-level tree,
-    hydro conserves mass, momentum and energy to round-off; MHD improves by
-    orders of magnitude (what is left comes from the coarse and fine copies
-    of face B on coarse-fine faces, which edge-EMF matching would make
-    agree)."""
+    mass, momentum and energy are conserved to round-off (with MHD as well:
+    the guard faces on a level boundary come from the copy owned by the
+    reader's own level, so same-level neighbours compute the same fluxes);
+    without it they drift."""
     from torch_gb300 import amr
     t, c = amr.small_tree()
     st = amr.amr_box(t, c, seed=5, mach=1.0, device="cpu")
@@ -131,8 +131,5 @@ def test_flux_correction_conserves_across_levels(oracle, mhd):
         after = _amr_totals(t, st, u)
         scale = np.array([before[0], before[0], before[0], before[0], before[4]])
         res[fc] = np.abs(after - before) / scale
-    if not mhd:
-        assert np.all(res[True] < 1e-14), res[True]
-    else:
-        assert np.all(res[True] < 1e-2 * res[False]), (res[True], res[False])
+    assert np.all(res[True] < 1e-14), res[True]
     assert res[False][0] > 1e-7

@@ -83,15 +83,17 @@ def test_amr_mixed_precision_l1(gb, mhd):
         assert np.abs(a[:, v] - b[:, v]).sum() / np.abs(a[:, v]).sum() <= 1e-4
 
 
-def test_amr_hydro_conserves_with_flux_correction(gb):
-    """Mass, momentum and energy over the periodic 3-level tree after a few
-    GPU steps: round-off with flux conservation at fine-coarse faces."""
+@pytest.mark.parametrize("mhd", [False, True])
+def test_amr_conserves_with_flux_correction(gb, mhd):
+    """Mass, momentum and energy (gas + magnetic) over the periodic 3-level
+    tree after a few GPU steps: round-off with flux conservation at
+    fine-coarse faces."""
     import torch
     from torch_gb300 import amr
     t, c = amr.small_tree()
     st = amr.amr_box(t, c, seed=5, mach=1.0, device="cuda")
-    g = gb.grid_from_amr(t, st, mhd=False, cooling=False)
-    gb.init_hydro(gb.hydro_params(False))
+    g = gb.grid_from_amr(t, st, mhd=mhd, cooling=False)
+    gb.init_hydro(gb.hydro_params(mhd))
     g.register()
     lv = torch.as_tensor(np.asarray(t["level"])[g.leaf], dtype=torch.float64, device="cuda")
     vol = (st["root_dx"] / 2 ** lv) ** 3
@@ -99,7 +101,8 @@ def test_amr_hydro_conserves_with_flux_correction(gb):
     def totals():
         u = g.u[g.t_leaf.long()][:, :, 4:20, 4:20, 4:20]
         rho = u[:, 0]
-        q = [rho, rho * u[:, 1], rho * u[:, 2], rho * u[:, 3], rho * u[:, 5]]
+        em = 0.5 * (u[:, 7] ** 2 + u[:, 8] ** 2 + u[:, 9] ** 2) if mhd else 0.0
+        q = [rho, rho * u[:, 1], rho * u[:, 2], rho * u[:, 3], rho * u[:, 5] + em]
         return torch.stack([(x.sum(dim=(1, 2, 3)) * vol).sum() for x in q]).cpu().numpy()
 
     before = totals()

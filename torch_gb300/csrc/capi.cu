@@ -465,6 +465,17 @@ __global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restri
     }
     leaf_hit h = find_leaf(t, X[0], X[1], X[2]);
     if (h.node < 0) return;
+    if (h.level != L) {
+        // a face on a level boundary: the copy owned by the leaf of this
+        // block's level on the lower side, when there is one, so that every
+        // block of a level reads the same face
+        leaf_hit h2 = find_leaf(t, a == 0 ? wrap(X[0] - 1, N[0]) : X[0], a == 1 ? wrap(X[1] - 1, N[1]) : X[1],
+                                a == 2 ? wrap(X[2] - 1, N[2]) : X[2]);
+        if (h2.node >= 0 && h2.level == L) {
+            X[a] = wrap(X[a] - 1, N[a]) + 1;  // its upper face, unwrapped at the domain edge
+            h = h2;
+        }
+    }
     const int lsl = t.maxlevel - h.level;
     const int* sc = t.coord + 3 * h.node;
     const double* src = g.f[a] + (int64_t)h.node * GB_FSZ;
