@@ -514,33 +514,39 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_un
     bool ok = isfinite(Tp) && Tp > 0.0;
     double ein = 0.0;
     if (ok) {
-        // secant-Newton from the prediction: the residual in FP64 (it is a
-        // small difference of energies), the rate, slope, Jacobian and
-        // Newton quotient in FP32
-        double ea = ei0;
-        float fa = f0;
-        double eb = fmax(Tp * v.TtoEI, emin_);
+        // secant-Newton from the prediction, in FP32 on the change of the
+        // energy x = e - e_old (the backward-Euler residual is then
+        // g = x - dt f, with no cancellation against e_old); e is formed in
+        // FP64 once at the end
+        const float e0f = (float)ei0;
+        const float xmin = (float)(emin_ - ei0);
+        float xa = 0.0f, fa = f0;
+        float xb = (float)(fmax(Tp * v.TtoEI, emin_) - ei0);
         float J = 1.0f;
         bool conv = false;
         for (int it = 0; it < 4; ++it) {
             float gm, lm;
-            const float fb = gbcoolf::dei_parts(pf, tf, vf, flf, (float)eb, &gm, &lm);
-            const double gb = eb - dt * (double)fb - ei0;
-            const double de = eb - ea;
-            const float slope = fabs(de) > 1e-7 * eb ? (fb - fa) / (float)de : 0.0f;
+            const float eb_f = e0f + xb;
+            const float fb = gbcoolf::dei_parts(pf, tf, vf, flf, eb_f, &gm, &lm);
+            const float gb = xb - dtf * fb;
+            const float de = xb - xa;
+            const float slope = fabsf(de) > 1e-7f * eb_f ? (fb - fa) / de : 0.0f;
             J = 1.0f - dtf * slope;
             if (!(J > 0.0f)) break;
-            double en = eb - (double)((float)gb / J);
-            if (!isfinite(en)) break;
-            if (en < emin_) en = emin_;
-            ea = eb;
+            float xn = xb - gb / J;
+            if (!isfinite(xn)) break;
+            if (xn < xmin) xn = xmin;
+            xa = xb;
             fa = fb;
-            eb = en;
-            if (fabs(eb - ea) <= 0.25 * rel_tol * eb && fabs(de) <= 0.05 * ea) {
+            xb = xn;
+            // the correction is small and the secant slope local (its two
+            // points within 5 % of each other)
+            if (fabsf(xb - xa) <= 0.25f * (float)rel_tol * (e0f + xb) && fabsf(de) <= 0.05f * (e0f + xa)) {
                 conv = true;
                 break;
             }
         }
+        const double eb = ei0 + (double)xb;
         // the converged FP32 iterate is the answer; optionally re-check the
         // backward-Euler residual (heatCool.F90:1928-1950) in FP64 with the
         // last secant slope
