@@ -238,8 +238,9 @@ extern "C" int gb_hydro_init(const gb_hydro_params* p)
     g_gb.hp = *p;
     g_gb.hydro_ok = true;
     g_gb.gen += 1;
-    // [0]: bits of the CFL minimum, [1..3]: dt / root_dx of the last dt
-    if (!g_gb.d_dtmin && gb_check(cudaMalloc(&g_gb.d_dtmin, 4 * sizeof(double)), "cudaMalloc(dtmin)"))
+    // [0]: bits of the CFL minimum, [1..3]: dt / root_dx of the last dt,
+    // [4..5]: the same as three floats
+    if (!g_gb.d_dtmin && gb_check(cudaMalloc(&g_gb.d_dtmin, 8 * sizeof(double)), "cudaMalloc(dtmin)"))
         return GB_ERR_CUDA;
     return GB_OK;
 }
@@ -518,8 +519,8 @@ struct dt_limits {
 // dt = CFL x the minimum limit; with a driver clock, limited as
 // Driver_computeDt.F90:588,596 and shortened to end on t_max. Also
 // dt / root_dx for the step's kernels.
-__global__ void k_dt_finish(const unsigned long long* bits, double cfl, double* out, double* dtdx, double dx0,
-                            double dx1, double dx2, gb_driver_state* drv, dt_limits lim)
+__global__ void k_dt_finish(const unsigned long long* bits, double cfl, double* out, double* dtdx, float* dtdxf,
+                            double dx0, double dx1, double dx2, gb_driver_state* drv, dt_limits lim)
 {
     double dt = cfl * __longlong_as_double((long long)*bits);
     if (drv) {
@@ -533,6 +534,9 @@ __global__ void k_dt_finish(const unsigned long long* bits, double cfl, double* 
     dtdx[0] = dt / dx0;
     dtdx[1] = dt / dx1;
     dtdx[2] = dt / dx2;
+    dtdxf[0] = (float)dtdx[0];
+    dtdxf[1] = (float)dtdx[1];
+    dtdxf[2] = (float)dtdx[2];
 }
 
 __global__ void k_advance_clock(gb_driver_state* drv)
@@ -726,6 +730,9 @@ static gbh::hydro_kparams make_kp(double dt, const double* dtp = nullptr)
     kp.dtdxp = dtp ? g_gb.d_dtmin + 1 : nullptr;  // written by k_dt_finish
     kp.fc_links = nullptr;
     kp.fc_reg = nullptr;
+    kp.gammaf = (float)g_gb.hp.gamma;
+    kp.cviscf = (float)g_gb.hp.cvisc;
+    kp.dtdxfp = dtp ? (const float*)(g_gb.d_dtmin + 4) : nullptr;  // written by k_dt_finish
     kp.gamma = g_gb.hp.gamma;
     kp.cvisc = g_gb.hp.cvisc;
     kp.eint_switch = g_gb.hp.eint_switch;
@@ -740,7 +747,10 @@ static gbh::hydro_kparams make_kp(double dt, const double* dtp = nullptr)
     } else {
         kp.dx[0] = kp.dx[1] = kp.dx[2] = 1.0;
     }
-    for (int d = 0; d < 3; ++d) kp.dtdx0[d] = dt / kp.dx[d];
+    for (int d = 0; d < 3; ++d) {
+        kp.dtdx0[d] = dt / kp.dx[d];
+        kp.dtdxf0[d] = (float)kp.dtdx0[d];
+    }
     return kp;
 }
 
@@ -824,7 +834,7 @@ static int launch_dt(int nblk, const int* list, double* dt_out, gb_driver_state*
     int rc = gb_dt_launch(kp, g_gb.hp.mhd, nblk, list, (unsigned long long*)g_gb.d_dtmin, s);
     if (rc) return rc;
     k_dt_finish<<<1, 1, 0, s>>>((const unsigned long long*)g_gb.d_dtmin, g_gb.hp.cfl, dt_out, g_gb.d_dtmin + 1,
-                                kp.dx[0], kp.dx[1], kp.dx[2], drv, g_dt_limits);
+                                (float*)(g_gb.d_dtmin + 4), kp.dx[0], kp.dx[1], kp.dx[2], drv, g_dt_limits);
     gb_prof_end(GBP_DT, s);
     return gb_check(cudaGetLastError(), "k_dt_finish") ? GB_ERR_CUDA : GB_OK;
 }

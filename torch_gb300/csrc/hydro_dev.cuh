@@ -44,7 +44,8 @@ struct scratch_layout {
     static constexpr size_t emf = (size_t)3 * NEDGE;          // double
     static constexpr size_t fb = (size_t)3 * NFB;             // double
     // FP32 primitives of the padded block (mixed path only)
-    static constexpr size_t prim32 = std::is_same<T, float>::value ? (size_t)NP32 * GB_N3 : 0;  // float
+    // (+ the three face-B arrays, FP32, after the cell variables)
+    static constexpr size_t prim32 = std::is_same<T, float>::value ? (size_t)NP32 * GB_N3 + 3 * GB_FSZ : 0;  // float
     static constexpr size_t bytes =
         recon * sizeof(T) + flux * sizeof(T) + (emf + fb) * sizeof(double) + prim32 * sizeof(float);
 };
@@ -70,6 +71,26 @@ k_prim32(gb_dev_grid g, const int* __restrict__ list, float* __restrict__ p32, s
         }
         out[(size_t)v * GB_N3] = (float)base[(int64_t)g.slot[roles[v]] * GB_N3];
     }
+    if (MHD) {
+        // face B (GB_FSZ = 14400 > GB_N3 = 13824: the last threads of the
+        // grid cover the rest below)
+        float* fo = p32 + (size_t)cb * stride + (size_t)NP32 * GB_N3;
+        const int64_t fb = (int64_t)list[cb] * GB_FSZ;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            fo[(size_t)a * GB_FSZ + c] = (float)g.f[a][fb + c];
+            if (c < GB_FSZ - GB_N3) fo[(size_t)a * GB_FSZ + GB_N3 + c] = (float)g.f[a][fb + GB_N3 + c];
+        }
+    }
+}
+
+// face B of the padded block for reconstruction precision T: the FP32
+// copies of the mixed path, the FP64 store otherwise
+template <typename T>
+__device__ __forceinline__ T face_b(const gb_dev_grid& g, int a, int blk, int fi, const float* p32b)
+{
+    if constexpr (std::is_same<T, float>::value) return p32b[(size_t)NP32 * GB_N3 + (size_t)a * GB_FSZ + fi];
+    else return g.f[a][(int64_t)blk * GB_FSZ + fi];
 }
 
 template <typename T>
@@ -317,9 +338,30 @@ struct hydro_kparams {
     // flux registers (store block x 6 faces x 256 face cells x NREG, in T)
     const int* fc_links;
     void* fc_reg;
+    // FP32 copies for the mixed path: gamma, cvisc, dt / root_dx (and its
+    // device copy, written with dtdxp)
+    float gammaf, cviscf;
+    float dtdxf0[3];
+    const float* dtdxfp;
 };
 
 __device__ __forceinline__ double kp_dt(const hydro_kparams& kp) { return kp.dtp ? *kp.dtp : kp.dt; }
+
+// dt/dx of a level-l block in FP32 (the exact power-of-two scaling of
+// dt/root_dx, 2^l from the exponent bits)
+__device__ __forceinline__ void kp_dtdxf(const hydro_kparams& kp, int level, float* out)
+{
+    const float sc = __int_as_float((127 + level) << 23);
+    if (kp.dtdxfp) {
+        out[0] = kp.dtdxfp[0] * sc;
+        out[1] = kp.dtdxfp[1] * sc;
+        out[2] = kp.dtdxfp[2] * sc;
+    } else {
+        out[0] = kp.dtdxf0[0] * sc;
+        out[1] = kp.dtdxf0[1] * sc;
+        out[2] = kp.dtdxf0[2] * sc;
+    }
+}
 
 __device__ __forceinline__ void kp_dtdx(const hydro_kparams& kp, int level, double* out)
 {
@@ -375,7 +417,7 @@ __device__ __forceinline__ void load_prim(const gb_dev_grid& g, int blk, int ci,
 
 // normal-direction PPM and the normal MHD term of direction D
 template <typename T, bool MHD, int TILE, int D>
-__device__ __forceinline__ void recon_normal(const gb_dev_grid& g, T gam, const double* dtd, const T* hd, int blk,
+__device__ __forceinline__ void recon_normal(const gb_dev_grid& g, T gam, const T* dtd, const T* hd, int blk,
                                              int i, int j, int k, int lane, const float* p32b,
                                              T (*s_sig)[NP][TILE], T (*s_abn)[NP][TILE], T (*s_dnb)[TILE], T* wp,
                                              T* wn, T* wc)
@@ -390,7 +432,7 @@ __device__ __forceinline__ void recon_normal(const gb_dev_grid& g, T gam, const 
         for (int s = 0; s < NP; ++s) qs[m][s] = w[rot_slot(D, s)];
     }
     T wpr[NP], wnr[NP], sgr[NP];
-    ppm_normal<T, MHD>(gam, qs, (T)dtd[D], wpr, wnr, sgr);
+    ppm_normal<T, MHD>(gam, qs, dtd[D], wpr, wnr, sgr);
 #pragma unroll
     for (int s = 0; s < NP; ++s) {
         const int v = rot_slot(D, s);
@@ -406,9 +448,8 @@ __device__ __forceinline__ void recon_normal(const gb_dev_grid& g, T gam, const 
                      (T)0, -wc[2], -wc[3]};
         if (D == 1) { row[5] = -wc[1]; row[6] = (T)0; row[7] = -wc[3]; }
         if (D == 2) { row[5] = -wc[1]; row[6] = -wc[2]; row[7] = (T)0; }
-        const double* fd = g.f[D] + (int64_t)blk * GB_FSZ;
         const int ip = i + (D == 0), jp = j + (D == 1), kp2 = k + (D == 2);
-        T dnb = (T)fd[gb_fidx(D, ip, jp, kp2)] - (T)fd[gb_fidx(D, i, j, k)];
+        T dnb = face_b<T>(g, D, blk, gb_fidx(D, ip, jp, kp2), p32b) - face_b<T>(g, D, blk, gb_fidx(D, i, j, k), p32b);
 #pragma unroll
         for (int v = 0; v < NP; ++v) {
             s_abn[D][v][lane] = row[v];
@@ -490,10 +531,20 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
     const bool active = cell < NRC;
     const int cc = active ? cell : 0;
     const int i = RLO + cc % RB, j = RLO + (cc / RB) % RB, k = RLO + cc / (RB * RB);
-    const T gam = (T)kp.gamma;
-    double dtd[3];
-    kp_dtdx(kp, gb_block_level(g, blk), dtd);
-    const T hd[3] = {(T)(0.5 * dtd[0]), (T)(0.5 * dtd[1]), (T)(0.5 * dtd[2])};
+    // time step over cell size: FP32 throughout in the mixed path (no FP64
+    // instruction in this kernel), the oracle's FP64 values otherwise
+    T gam, dtd[3], hd[3];
+    if constexpr (std::is_same<T, float>::value) {
+        gam = kp.gammaf;
+        kp_dtdxf(kp, gb_block_level(g, blk), dtd);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) hd[q] = 0.5f * dtd[q];
+    } else {
+        gam = kp.gamma;
+        kp_dtdx(kp, gb_block_level(g, blk), dtd);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) hd[q] = 0.5 * dtd[q];
+    }
     const float* p32b = p32 + (size_t)cb * p32_stride;
     T wp[NP], wn[NP], wc[NP];
     if (d == 0)
@@ -735,9 +786,9 @@ __device__ __forceinline__ void flux_face(gb_dev_grid g, hydro_kparams kp, const
         Lr[s] = wl[rot_slot(d, s)];
         Rr[s] = wr[rot_slot(d, s)];
     }
-    const T gam = (T)kp.gamma;
+    const T gam = std::is_same<T, float>::value ? (T)kp.gammaf : (T)kp.gamma;
     if (MHD) {
-        T bnf = (T)g.f[d][(int64_t)blk * GB_FSZ + gb_fidx(d, I[0], I[1], I[2])];
+        T bnf = face_b<T>(g, d, blk, gb_fidx(d, I[0], I[1], I[2]), p32 + (size_t)cb * p32_stride);
         Lr[5] = bnf;
         Rr[5] = bnf;
         hlld<T>(gam, Lr, Rr, Fr, &un);
@@ -763,7 +814,7 @@ __device__ __forceinline__ void flux_face(gb_dev_grid g, hydro_kparams kp, const
             }
         };
         T dv = U(GB_VELX + d, cir) - U(GB_VELX + d, cil);
-        T vis = (T)kp.cvisc * fmax(-dv, (T)0);
+        T vis = (std::is_same<T, float>::value ? (T)kp.cviscf : (T)kp.cvisc) * fmax(-dv, (T)0);
         if (vis > (T)0) {
             T rl = U(GB_DENS, cil), rr = U(GB_DENS, cir);
             T vl[3] = {U(GB_VELX, cil), U(GB_VELY, cil), U(GB_VELZ, cil)};

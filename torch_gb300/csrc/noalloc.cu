@@ -96,6 +96,10 @@ extern "C" int gb_hydro_unsplit_noalloc(int blockCount, const int* blockList_dev
     kp.dtdxp = nullptr;
     kp.fc_links = nullptr;  // no flux registers without allocation
     kp.fc_reg = nullptr;
+    kp.gammaf = (float)kp.gamma;
+    kp.cviscf = (float)kp.cvisc;
+    for (int d = 0; d < 3; ++d) kp.dtdxf0[d] = (float)kp.dtdx0[d];
+    kp.dtdxfp = nullptr;
     return gbh::launch_chunk<double>(kp, g_gb.hp.mhd, 0, blockCount, blockList_dev, scratch, st_dev,
                                      (cudaStream_t)stream);
 }
