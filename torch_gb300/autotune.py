@@ -12,7 +12,7 @@ from __future__ import annotations
 import json
 import os
 
-CHUNKS = (8, 16, 32, 64)
+CHUNKS = (16, 32, 64, 128)
 TILES = (32, 64)
 CACHE = os.environ.get("GBHYDRO_TUNE_CACHE",
                        os.path.join(os.path.dirname(os.path.abspath(__file__)), "_tune_cache.json"))
