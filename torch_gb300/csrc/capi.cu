@@ -731,6 +731,7 @@ static gbh::hydro_kparams make_kp(double dt, const double* dtp = nullptr)
     kp.fc_links = nullptr;
     kp.fc_reg = nullptr;
     kp.gammaf = (float)g_gb.hp.gamma;
+    kp.inv_gm1 = 1.0 / (g_gb.hp.gamma - 1.0);
     kp.cviscf = (float)g_gb.hp.cvisc;
     kp.dtdxfp = dtp ? (const float*)(g_gb.d_dtmin + 4) : nullptr;  // written by k_dt_finish
     kp.gamma = g_gb.hp.gamma;

@@ -116,6 +116,23 @@ __device__ __forceinline__ int rot_slot(int d, int s)
 __device__ __forceinline__ int wslot(int s) { return s < 5 ? s : s + 1; }
 
 // ---------------------------------------------------------------- eigensystems
+// Structural non-zeros of the eigenvector matrices that eig_hydro / eig_mhd
+// fill (every other entry is 0). The projections below skip the zero
+// entries at compile time: without fast-math the compiler cannot drop 0 * x,
+// and for finite x a skipped term is +-0, which leaves every sum unchanged.
+template <bool MHD>
+__host__ __device__ constexpr bool nz_L(int k, int s)
+{
+    return MHD ? (k == 3 ? (s == 0 || s == 4)
+                         : (k == 1 || k == 5) ? (s == 2 || s == 3 || s == 5 || s == 6) : (s >= 1 && s <= 6))
+               : ((k == 0 || k == 4) ? (s == 1 || s == 4) : k == 1 ? (s == 0 || s == 4) : s == k);
+}
+template <bool MHD>
+__host__ __device__ constexpr bool nz_R(int s, int k)
+{
+    return MHD ? (k == 3 ? s == 0 : (k == 1 || k == 5) ? (s == 2 || s == 3 || s == 5 || s == 6) : true)
+               : ((k == 0 || k == 4) ? (s == 0 || s == 1 || s == 4) : k == 1 ? s == 0 : s == k);
+}
 template <typename T>
 __device__ __forceinline__ void eig_hydro(T gam, const T* q, T* lam, T (*R)[MAXW], T (*L)[MAXW])
 {
@@ -223,6 +240,7 @@ __device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* 
 #pragma unroll
             for (int s = 0; s < nw; ++s) {
                 const int qq = wslot(s);
+                if (!nz_L<MHD>(k, s)) continue;
                 sl = sl + L[k][s] * (qs[m][qq] - qs[m - 1][qq]);
                 srr = srr + L[k][s] * (qs[m + 1][qq] - qs[m][qq]);
             }
@@ -232,7 +250,8 @@ __device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* 
         for (int s = 0; s < nw; ++s) {
             T acc = (T)0;
 #pragma unroll
-            for (int k = 0; k < nw; ++k) acc = acc + R[s][k] * da[k];
+            for (int k = 0; k < nw; ++k)
+                if (nz_R<MHD>(s, k)) acc = acc + R[s][k] * da[k];
             dwm[m - 1][s] = acc;
         }
     }
@@ -268,6 +287,7 @@ __device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* 
         T a = (T)0, b = (T)0;
 #pragma unroll
         for (int s = 0; s < nw; ++s) {
+            if (!nz_L<MHD>(k, s)) continue;
             a = a + L[k][s] * dW[s];
             b = b + L[k][s] * W6[s];
         }
@@ -288,7 +308,8 @@ __device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* 
             T gK = refK ? (T)0.5 * sK * (ldW[k] - ((T)1 - t3 * sK) * lW6[k]) : (T)0;
             T c = gK - (T)0.5 * sg * (ldW[k] - ((T)1 - t3 * sg) * lW6[k]);
 #pragma unroll
-            for (int s = 0; s < nw; ++s) Wp[s] = Wp[s] + c * R[s][k];
+            for (int s = 0; s < nw; ++s)
+                if (nz_R<MHD>(s, k)) Wp[s] = Wp[s] + c * R[s][k];
         }
     }
     T s0 = lam[0] * dtdx;
@@ -303,7 +324,8 @@ __device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* 
             T g0 = ref0 ? (T)0.5 * s0 * (ldW[k] + ((T)1 + t3 * s0) * lW6[k]) : (T)0;
             T c = g0 - (T)0.5 * sg * (ldW[k] + ((T)1 + t3 * sg) * lW6[k]);
 #pragma unroll
-            for (int s = 0; s < nw; ++s) Wn[s] = Wn[s] + c * R[s][k];
+            for (int s = 0; s < nw; ++s)
+                if (nz_R<MHD>(s, k)) Wn[s] = Wn[s] + c * R[s][k];
         }
     }
 #pragma unroll
@@ -312,7 +334,8 @@ __device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* 
     for (int s = 0; s < nw; ++s) {
         T acc = (T)0;
 #pragma unroll
-        for (int k = 0; k < nw; ++k) acc = acc + (lam[k] * ldW[k]) * R[s][k];
+        for (int k = 0; k < nw; ++k)
+            if (nz_R<MHD>(s, k)) acc = acc + (lam[k] * ldW[k]) * R[s][k];
         wp[wslot(s)] = Wp[s];
         wn[wslot(s)] = Wn[s];
         sig[wslot(s)] = acc;
@@ -341,6 +364,7 @@ struct hydro_kparams {
     // FP32 copies for the mixed path: gamma, cvisc, dt / root_dx (and its
     // device copy, written with dtdxp)
     float gammaf, cviscf;
+    double inv_gm1;  // 1 / (gamma - 1), for the mixed path's update
     float dtdxf0[3];
     const float* dtdxfp;
 };
@@ -1079,7 +1103,7 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
     double Uc[NP];
     Uc[0] = rho;
     Uc[1] = rho * vx; Uc[2] = rho * vy; Uc[3] = rho * vz;
-    Uc[4] = (RCP ? pr * (1.0 / gm1) : pr / gm1) + 0.5 * rho * (vx * vx + vy * vy + vz * vz) +
+    Uc[4] = (RCP ? pr * kp.inv_gm1 : pr / gm1) + 0.5 * rho * (vx * vx + vy * vy + vz * vz) +
             0.5 * (Bc[0] * Bc[0] + Bc[1] * Bc[1] + Bc[2] * Bc[2]);
     Uc[5] = Bc[0]; Uc[6] = Bc[1]; Uc[7] = Bc[2];
     double re = rho * UV(GB_EINT);

@@ -97,6 +97,7 @@ extern "C" int gb_hydro_unsplit_noalloc(int blockCount, const int* blockList_dev
     kp.fc_links = nullptr;  // no flux registers without allocation
     kp.fc_reg = nullptr;
     kp.gammaf = (float)kp.gamma;
+    kp.inv_gm1 = 1.0 / (kp.gamma - 1.0);
     kp.cviscf = (float)kp.cvisc;
     for (int d = 0; d < 3; ++d) kp.dtdxf0[d] = (float)kp.dtdx0[d];
     kp.dtdxfp = nullptr;
