@@ -426,6 +426,8 @@ def main():
                     help="bracket the fast path's timed region with cudaProfilerStart/Stop")
     ap.add_argument("--only", choices=["plain", "fast", "eager"], default=None,
                     help="time one path alone and print a short line (for profiler captures)")
+    ap.add_argument("--chunk", type=int, default=0, help="with --only: blocks per chunk (no autotuning)")
+    ap.add_argument("--tile", type=int, default=32, help="with --chunk: reconstruction tile (32 or 64)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -474,9 +476,12 @@ def main():
     if args.only:
         g = make_grid(G, tree, st)
         del st
+        if args.chunk:
+            G.set_launch_config(args.chunk, args.tile)
         prec, sur, graph = {"plain": (0, False, True), "fast": (1, True, True), "eager": (1, True, False)}[args.only]
         ms, stt, info = run_path(G, g, prec, args.steps, args.warmup, surrogate=sur, graph=graph,
-                                 tune=not args.no_tune and graph, profile=not graph, ncu_range=args.ncu_range)
+                                 tune=not args.no_tune and graph and not args.chunk, profile=not graph,
+                                 ncu_range=args.ncu_range)
         if rank == 0:
             print(json.dumps({"path": args.only, "workload": wl["name"], "ms_per_step": ms,
                               "value": zones * world / (ms * 1e-3), "unit": "zone-updates/s",
