@@ -361,6 +361,14 @@ int gb_prof_read(double* ms, long long* launches, int n);
  * denominator of the FP64-pipe roofline. */
 int gb_measure_fp64_peak(double* tflops);
 
+/* Self-check of the mixed path's integer-pipe FP64 <-> FP32 conversions
+ * against the hardware conversions: for the n device values, counts into
+ * mismatches_dev[0] the doubles whose float differs and into [1] the floats
+ * whose double differs (NaN payloads aside). No counterpart in the
+ * reference. */
+int gb_selfcheck_conversions(int64_t n, const double* d_dev, const float* f_dev,
+                             unsigned long long* mismatches_dev, void* stream);
+
 /* ---------------------------------------------------------------- misc */
 int gb_status_reset(gb_status* st_dev, void* stream);
 int gb_status_read(const gb_status* st_dev, gb_status* st_host);

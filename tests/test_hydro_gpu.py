@@ -132,3 +132,28 @@ def test_mixed_precision_l1(gb, oracle, mhd):
     for v in (0, 4):
         l1 = np.abs(_interior(a[:, v]) - _interior(b[:, v])).sum() / np.abs(_interior(a[:, v])).sum()
         assert l1 <= 1e-4, (v, l1)
+
+
+def test_integer_pipe_conversions_match_hardware(gb):
+    """The mixed path's FP64 <-> FP32 conversions done with integer
+    instructions equal the hardware conversions bit for bit: random bit
+    patterns (all exponents, signs, ties), values of the workload's range,
+    zeros, subnormals, the float range edges, inf and nan."""
+    import torch
+    rng = np.random.default_rng(0)
+    n = 1 << 22
+    d = rng.integers(0, 2 ** 63, n, dtype=np.int64).view(np.float64).copy()
+    d[: n // 4] = rng.normal(0, 1, n // 4) * 10.0 ** rng.uniform(-40, 40, n // 4)
+    # exact ties of the 29 dropped bits (round half to even)
+    t = rng.integers(0, 2 ** 62, 4096, dtype=np.int64)
+    d[n // 4:n // 4 + 4096] = ((t & ~np.int64((1 << 29) - 1)) | (1 << 28)).view(np.float64)
+    edge = np.array([0.0, -0.0, 5e-324, -5e-324, 1e-45, 1.4e-45, 1.17549435e-38, 1.1754942e-38, 3.4028234e38,
+                     3.4028235e38, 3.40282357e38, 1e39, -1e39, np.inf, -np.inf, np.nan, 1.0, -1.0])
+    d[-len(edge):] = edge
+    f = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32).view(np.float32).copy()
+    f[: len(edge)] = edge.astype(np.float32)
+    dd, fd = torch.as_tensor(d, device="cuda"), torch.as_tensor(f, device="cuda")
+    bad = torch.zeros(2, dtype=torch.int64, device="cuda")
+    gb.check(gb.lib().gb_selfcheck_conversions(n, dd.data_ptr(), fd.data_ptr(), bad.data_ptr(), None), "conv")
+    torch.cuda.synchronize()
+    assert bad.tolist() == [0, 0]

@@ -127,6 +127,29 @@ extern "C" int gb_measure_fp64_peak(double* tflops)
     return rc;
 }
 
+// the integer-pipe conversions against the hardware ones, bit for bit
+__global__ void k_check_conv(int64_t n, const double* __restrict__ d, const float* __restrict__ f,
+                             unsigned long long* __restrict__ bad)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float a = gb_d2f(d[i]), b = (float)d[i];
+    const double c = gb_f2d(f[i]), e = (double)f[i];
+    const bool ok1 = __float_as_uint(a) == __float_as_uint(b) || (isnan(a) && isnan(b));
+    const bool ok2 = __double_as_longlong(c) == __double_as_longlong(e) || (isnan(c) && isnan(e));
+    if (!ok1) atomicAdd(bad, 1ull);
+    if (!ok2) atomicAdd(bad + 1, 1ull);
+}
+
+extern "C" int gb_selfcheck_conversions(int64_t n, const double* d_dev, const float* f_dev,
+                                        unsigned long long* mismatches_dev, void* stream)
+{
+    if (n < 0 || (n > 0 && (!d_dev || !f_dev || !mismatches_dev))) return GB_ERR_ARG;
+    if (n == 0) return GB_OK;
+    k_check_conv<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(n, d_dev, f_dev, mismatches_dev);
+    return gb_check(cudaGetLastError(), "k_check_conv") ? GB_ERR_CUDA : GB_OK;
+}
+
 static char g_err[512] = "";
 
 void gb_set_error(const char* fmt, ...)
@@ -415,10 +438,15 @@ __global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restri
         int sj = (int)((X[1] >> lsl) - (long long)sc[1] * GB_NXB) + GB_NGUARD;
         int sk = (int)((X[2] >> lsl) - (long long)sc[2] * GB_NXB) + GB_NGUARD;
         int sci = gb_cidx(si, sj, sk);
-        for (int q2 = 0; q2 < gv.n; ++q2) {
-            const int64_t v = gv.slot[q2];
-            dst[v * GB_N3] = src[v * GB_N3 + sci];
-        }
+        // all loads first, then all stores: the loads are independent and in
+        // flight together (a store between them could alias the next load)
+        double val[GB_NROLE];
+#pragma unroll
+        for (int q2 = 0; q2 < GB_NROLE; ++q2)
+            if (q2 < gv.n) val[q2] = src[(int64_t)gv.slot[q2] * GB_N3 + sci];
+#pragma unroll
+        for (int q2 = 0; q2 < GB_NROLE; ++q2)
+            if (q2 < gv.n) dst[(int64_t)gv.slot[q2] * GB_N3] = val[q2];
     } else {
         // finer neighbour: mean of the fine cells covering this cell
         int r = 1 << (ls - lsl);
@@ -426,14 +454,20 @@ __global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restri
         int bj = (int)((lo[1] >> lsl) - (long long)sc[1] * GB_NXB) + GB_NGUARD;
         int bk = (int)((lo[2] >> lsl) - (long long)sc[2] * GB_NXB) + GB_NGUARD;
         double inv = 1.0 / (double)(r * r * r);
-        for (int q2 = 0; q2 < gv.n; ++q2) {
+        double val[GB_NROLE];
+#pragma unroll
+        for (int q2 = 0; q2 < GB_NROLE; ++q2) {
+            if (q2 >= gv.n) continue;
             const int64_t v = gv.slot[q2];
             double acc = 0.0;
             for (int z = 0; z < r; ++z)
                 for (int y = 0; y < r; ++y)
                     for (int x = 0; x < r; ++x) acc += src[(int64_t)v * GB_N3 + gb_cidx(bi + x, bj + y, bk + z)];
-            dst[(int64_t)v * GB_N3] = acc * inv;
+            val[q2] = acc * inv;
         }
+#pragma unroll
+        for (int q2 = 0; q2 < GB_NROLE; ++q2)
+            if (q2 < gv.n) dst[(int64_t)gv.slot[q2] * GB_N3] = val[q2];
     }
 }
 
@@ -580,7 +614,67 @@ __global__ void k_soa_to_flash(double* __restrict__ out, int nunk, const int* __
     }
 }
 
+// FLASH-layout transfers straight from / to host memory the device can
+// address (pinned host memory; on GB300 it is read and written over
+// NVLink-C2C): one CTA moves FT cells of one block; the host side is one
+// contiguous run of FT * nunk values, the store side one coalesced row per
+// variable, transposed through shared memory.
+constexpr int FT = 64;
+static_assert(GB_N3 % FT == 0, "tile");
+
+template <bool UP>
+__global__ void __launch_bounds__(FT) k_flash_direct(double* host, int nunk, const int* __restrict__ hslot, gb_dev_grid g,
+                                                     const int* __restrict__ list, int read_first)
+{
+    extern __shared__ double tile[];  // FT * nunk
+    const int q = blockIdx.y;
+    const int blk = list ? list[q] : q;
+    const int c0 = blockIdx.x * FT;
+    double* h = host + ((size_t)blk * GB_N3 + c0) * nunk;
+    const int tot = FT * nunk;
+    if (UP || read_first)
+        for (int e = threadIdx.x; e < tot; e += FT) tile[e] = h[e];
+    __syncthreads();
+    const int c = c0 + threadIdx.x;
+    for (int r = 0; r < GB_NROLE; ++r) {
+        const int hs = hslot[r], ds = g.slot[r];
+        if (hs < 0 || ds < 0) continue;
+        double* d = g.unk + ((size_t)blk * g.nvar + ds) * GB_N3 + c;
+        if (UP) *d = tile[threadIdx.x * nunk + hs];
+        else tile[threadIdx.x * nunk + hs] = *d;
+    }
+    if (!UP) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < tot; e += FT) h[e] = tile[e];
+    }
+}
+
+template <bool UP>
+__global__ void k_faces_direct(double* hx, double* hy, double* hz, gb_dev_grid g, const int* __restrict__ list)
+{
+    const int a = blockIdx.z, q = blockIdx.y;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= GB_FSZ) return;
+    const int blk = list ? list[q] : q;
+    double* h = (a == 0 ? hx : a == 1 ? hy : hz) + (size_t)blk * GB_FSZ + e;
+    double* d = g.f[a] + (size_t)blk * GB_FSZ + e;
+    if (UP) *d = *h;
+    else *h = *d;
+}
+
 }  // namespace
+
+// The device address of host memory, when kernels may address it (pinned
+// memory under unified addressing); nullptr otherwise.
+static void* device_view(const void* host)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
 
 // Allocations and the face-link table of flux conservation (before any
 // capture). Returns whether flux conservation applies to the registered
@@ -1092,7 +1186,10 @@ static int flash_copy_list(bool up, double* host, int nunk, const int* host_slot
     if (rc || n == 0) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     const size_t per = (size_t)GB_N3 * nunk;  // doubles per FLASH block
-    const size_t bytes = (size_t)n * per * sizeof(double);
+    double* hd = (double*)device_view(host);
+    // staging: the blocks themselves unless the kernel can address the host
+    // array, then the slot map and the list
+    const size_t bytes = hd ? 0 : (size_t)n * per * sizeof(double);
     rc = gb_ensure_stage(bytes + (GB_NROLE + (size_t)n) * sizeof(int));
     if (rc) return rc;
     double* stage = (double*)g_gb.d_stage;
@@ -1101,6 +1198,24 @@ static int flash_copy_list(bool up, double* host, int nunk, const int* host_slot
     if (gb_check(cudaMemcpyAsync(dslot, host_slot, GB_NROLE * sizeof(int), cudaMemcpyHostToDevice, s), "slot copy") ||
         gb_check(cudaMemcpyAsync(dlist, list, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s), "list copy"))
         return GB_ERR_CUDA;
+    if (hd) {
+        // the kernel reads / writes the host array in place: no staging
+        // copies, one launch for the whole list
+        int mapped = 0;
+        for (int r = 0; r < GB_NROLE; ++r)
+            if (host_slot[r] >= 0 && host_slot[r] < nunk && g_gb.grid.slot[r] >= 0) ++mapped;
+        const size_t smem = (size_t)FT * nunk * sizeof(double);
+        if (smem > 48 * 1024) {
+            gb_set_error("FLASH transfer: nunk %d above the %d variables one tile holds", nunk, (int)(48 * 1024 / (FT * 8)));
+            return GB_ERR_ARG;
+        }
+        dim3 grid(GB_N3 / FT, n);
+        gb_prof_begin(GBP_COPY, s);
+        if (up) k_flash_direct<true><<<grid, FT, smem, s>>>(hd, nunk, dslot, g_gb.grid, dlist, 0);
+        else k_flash_direct<false><<<grid, FT, smem, s>>>(hd, nunk, dslot, g_gb.grid, dlist, mapped < nunk);
+        gb_prof_end(GBP_COPY, s);
+        return gb_check(cudaGetLastError(), "k_flash_direct") ? GB_ERR_CUDA : GB_OK;
+    }
     const unsigned nb = (unsigned)(((int64_t)n * GB_N3 + 255) / 256);
     if (up) {
         rc = for_each_run(n, list, [&](int q0, int b0, int len) {
@@ -1147,6 +1262,19 @@ static int face_copy_list(bool up, double* const host[3], int n, const int* list
     int rc = check_host_list(n, list, up ? "gb_grid_upload_faces_list" : "gb_grid_download_faces_list");
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
+    if (n == 0) return GB_OK;
+    double* hv[3] = {(double*)device_view(host[0]), (double*)device_view(host[1]), (double*)device_view(host[2])};
+    if (hv[0] && hv[1] && hv[2]) {
+        rc = gb_ensure_stage((size_t)n * sizeof(int) + 16);
+        if (rc) return rc;
+        int* dlist = (int*)g_gb.d_stage;
+        if (gb_check(cudaMemcpyAsync(dlist, list, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s), "list copy"))
+            return GB_ERR_CUDA;
+        dim3 grid((GB_FSZ + 255) / 256, n, 3);
+        if (up) k_faces_direct<true><<<grid, 256, 0, s>>>(hv[0], hv[1], hv[2], g_gb.grid, dlist);
+        else k_faces_direct<false><<<grid, 256, 0, s>>>(hv[0], hv[1], hv[2], g_gb.grid, dlist);
+        return gb_check(cudaGetLastError(), "k_faces_direct") ? GB_ERR_CUDA : GB_OK;
+    }
     for (int a = 0; a < 3; ++a) {
         double* dev = g_gb.grid.f[a];
         double* h = host[a];

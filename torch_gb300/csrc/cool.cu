@@ -461,9 +461,9 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_unit
     const gb_cool_tabf tf = {c.Tf, c.nf, c.lamf, (float)c.T_min, (float)c.nd_min};
     const float fl = gbcoolf::cooling_floor(pf, tf, vf);
     float gam, lam;
-    const float eif = (float)ei;
+    const float eif = gb_d2f(ei);
     float f0 = gbcoolf::dei_parts(pf, tf, vf, fl, eif, &gam, &lam);
-    const float dt = (float)(dt_code * c.p.time_unit);
+    const float dt = gb_d2f(dt_code * c.p.time_unit);
     // features in FP32: dt / t_cool = dt |f| / e
     const float r = dt * fabsf(f0) / eif;
     float lr = log10f(fmaxf(r, 1e-30f));
@@ -472,7 +472,7 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_unit
     lh = fminf(fmaxf(lh, (float)-gbsur::H_CLAMP), (float)gbsur::H_CLAMP);
     reinterpret_cast<float4*>(feat)[idx] =
         make_float4((log10f(vf.ndens) - (float)gbsur::N_MID) / (float)gbsur::N_HALF,
-                    (log10f((float)temp) - (float)gbsur::T_MID) / (float)gbsur::T_HALF, lr / (float)gbsur::R_HALF,
+                    (log10f(gb_d2f(temp)) - (float)gbsur::T_MID) / (float)gbsur::T_HALF, lr / (float)gbsur::R_HALF,
                     lh / (float)gbsur::H_HALF);
     f0out[idx] = make_float2(f0, fl);
 }
@@ -505,12 +505,12 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_un
     gbcoolf::make_vars(pf, v, vf);
     const gb_cool_tabf tf = {c.Tf, c.nf, c.lamf, (float)c.T_min, (float)c.nd_min};
     const double dt = dt_code * p.time_unit;
-    const float dtf = (float)dt;
+    const float dtf = gb_d2f(dt);
     const float2 f0fl = f0a[idx];
     const float f0 = f0fl.x;
     const float flf = f0fl.y;
     const double emin_ = 0.5 * p.absTmin * v.TtoEI;
-    double Tp = (double)((float)temp0 * exp10f((float)gbsur::Y_SCALE * y[idx]));
+    double Tp = gb_f2d(gb_d2f(temp0) * exp10f((float)gbsur::Y_SCALE * y[idx]));
     bool ok = isfinite(Tp) && Tp > 0.0;
     double ein = 0.0;
     if (ok) {
@@ -518,10 +518,10 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_un
         // energy x = e - e_old (the backward-Euler residual is then
         // g = x - dt f, with no cancellation against e_old); e is formed in
         // FP64 once at the end
-        const float e0f = (float)ei0;
-        const float xmin = (float)(emin_ - ei0);
+        const float e0f = gb_d2f(ei0);
+        const float xmin = gb_d2f(emin_ - ei0);
         float xa = 0.0f, fa = f0;
-        float xb = (float)(fmax(Tp * v.TtoEI, emin_) - ei0);
+        float xb = gb_d2f(fmax(Tp * v.TtoEI, emin_) - ei0);
         float J = 1.0f;
         bool conv = false;
         for (int it = 0; it < 4; ++it) {
@@ -546,7 +546,7 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_un
                 break;
             }
         }
-        const double eb = ei0 + (double)xb;
+        const double eb = ei0 + gb_f2d(xb);
         // the converged FP32 iterate is the answer; optionally re-check the
         // backward-Euler residual (heatCool.F90:1928-1950) in FP64 with the
         // last secant slope

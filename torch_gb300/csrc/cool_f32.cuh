@@ -228,15 +228,15 @@ __device__ float dust_temperature(const gb_cool_pf& p, const gb_cool_varsf& v, f
 
 __device__ __forceinline__ void make_vars(const gb_cool_pf& p, const gb_cool_vars& v, gb_cool_varsf& f)
 {
-    f.ndens = (float)v.ndens;
-    f.rho = (float)v.rho;
-    f.conf = (float)v.conf;
-    f.Gflux = (float)v.Gflux;
-    f.ephen = (float)v.ephen;
-    f.tdust = (float)v.tdust;
-    f.TtoEI = (float)v.TtoEI;
-    f.xHp = (float)v.xHp;
-    f.mu_mol = (float)v.mu_mol;
+    f.ndens = gb_d2f(v.ndens);
+    f.rho = gb_d2f(v.rho);
+    f.conf = gb_d2f(v.conf);
+    f.Gflux = gb_d2f(v.Gflux);
+    f.ephen = gb_d2f(v.ephen);
+    f.tdust = gb_d2f(v.tdust);
+    f.TtoEI = gb_d2f(v.TtoEI);
+    f.xHp = gb_d2f(v.xHp);
+    f.mu_mol = gb_d2f(v.mu_mol);
     f.cr_pref = p.crRE * (f.ndens / f.rho);
 }
 

@@ -49,6 +49,39 @@ struct gb_dev_grid {
 };
 
 // cell size of a block: root cell size scaled by 2^-level (exact)
+// FP64 <-> FP32 conversions on the integer pipe. GB300's FP64 pipe, which
+// also executes the hardware conversions, is the bottleneck of the mixed
+// path while the integer pipe idles. Both are IEEE conversions (float ->
+// double exact, double -> float round-to-nearest-even), written from the
+// binary64/binary32 encodings; zero and normal values take the integer
+// path, everything else (subnormal results, overflow, inf, nan) the
+// hardware one.
+__device__ __forceinline__ float gb_d2f(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    if (((hi & 0x7FFFFFFFu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);  // +-0
+    const int e = (int)((hi >> 20) & 0x7FFu) - 1023 + 127;
+    if (e <= 0 || e >= 255) return (float)x;
+    // the top 23 of the 52 mantissa bits: 20 from hi, 3 from lo; 29 dropped
+    unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1FFFFFFFu, half = 0x10000000u;
+    m += (unsigned)((rem > half) | ((rem == half) & (m & 1u)));
+    // a mantissa carry (m == 2^23) moves into the exponent; e == 254 with a
+    // carry gives +-inf, the correctly rounded overflow
+    return __uint_as_float((hi & 0x80000000u) | (((unsigned)e << 23) + m));
+}
+
+__device__ __forceinline__ double gb_f2d(float x)
+{
+    const unsigned u = __float_as_uint(x);
+    const unsigned ex = (u >> 23) & 0xFFu;
+    if ((u & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);  // +-0
+    if (ex == 0u || ex == 255u) return (double)x;
+    const unsigned hi = (u & 0x80000000u) | ((ex + (1023u - 127u)) << 20) | ((u & 0x7FFFFFu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
 // 2^l as a double, built from its exponent bits (0 <= l < 1023)
 __device__ __forceinline__ double gb_pow2(int l) { return __longlong_as_double((long long)(1023 + l) << 52); }
 

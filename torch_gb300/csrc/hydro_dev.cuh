@@ -69,7 +69,7 @@ k_prim32(gb_dev_grid g, const int* __restrict__ list, float* __restrict__ p32, s
             out[(size_t)v * GB_N3] = 0.0f;
             continue;
         }
-        out[(size_t)v * GB_N3] = (float)base[(int64_t)g.slot[roles[v]] * GB_N3];
+        out[(size_t)v * GB_N3] = gb_d2f(base[(int64_t)g.slot[roles[v]] * GB_N3]);
     }
     if (MHD) {
         // face B (GB_FSZ = 14400 > GB_N3 = 13824: the last threads of the
@@ -78,8 +78,8 @@ k_prim32(gb_dev_grid g, const int* __restrict__ list, float* __restrict__ p32, s
         const int64_t fb = (int64_t)list[cb] * GB_FSZ;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            fo[(size_t)a * GB_FSZ + c] = (float)g.f[a][fb + c];
-            if (c < GB_FSZ - GB_N3) fo[(size_t)a * GB_FSZ + GB_N3 + c] = (float)g.f[a][fb + GB_N3 + c];
+            fo[(size_t)a * GB_FSZ + c] = gb_d2f(g.f[a][fb + c]);
+            if (c < GB_FSZ - GB_N3) fo[(size_t)a * GB_FSZ + GB_N3 + c] = gb_d2f(g.f[a][fb + GB_N3 + c]);
         }
     }
 }
@@ -952,7 +952,9 @@ k_emf(gb_dev_grid g, const int* __restrict__ list, const T* __restrict__ fscr, s
     R dbp = upw<R>(ma1, two * (ecc[0][1] - eb0), two * (ecc[1][1] - eb1));
     R dam = upw<R>(mb0, two * (ea0 - ecc[0][0]), two * (ea1 - ecc[0][1]));
     R dap = upw<R>(mb1, two * (ecc[1][0] - ea0), two * (ecc[1][1] - ea1));
-    escr[(size_t)cb * estride + (size_t)c * NEDGE + e] = (double)(eavg + eighth * (dbm - dbp) + eighth * (dam - dap));
+    const R ev = eavg + eighth * (dbm - dbp) + eighth * (dam - dap);
+    if constexpr (std::is_same<R, float>::value) escr[(size_t)cb * estride + (size_t)c * NEDGE + e] = gb_f2d(ev);
+    else escr[(size_t)cb * estride + (size_t)c * NEDGE + e] = ev;
 }
 
 __device__ __forceinline__ int edge_index(int c, int i, int j, int k)
@@ -1113,7 +1115,9 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
     double dtd[3];
     kp_dtdx(kp, gb_block_level(g, blk), dtd);
     auto F = [&](int d, int var, int idx) -> double {
-        return (double)fs[(size_t)d * NFLX * NFC + (size_t)var * NFC + idx];
+        const T x = fs[(size_t)d * NFLX * NFC + (size_t)var * NFC + idx];
+        if constexpr (std::is_same<T, float>::value) return gb_f2d(x);  // exact, on the integer pipe
+        else return x;
     };
     double Un[5];
 #pragma unroll
@@ -1230,19 +1234,24 @@ k_dtlimit(gb_dev_grid g, double gamma, int mhd, double dx0, double dx1, double d
         const int i = LO + t % GB_NXB, j = LO + (t / GB_NXB) % GB_NXB, k = LO + t / (GB_NXB * GB_NXB);
         const int ci = gb_cidx(i, j, k);
         const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3 + ci;
-        R rho = (R)base[(int64_t)g.slot[GB_DENS] * GB_N3], p = (R)base[(int64_t)g.slot[GB_PRES] * GB_N3];
+        auto ld = [&](int role) -> R {
+            const double x = base[(int64_t)g.slot[role] * GB_N3];
+            if constexpr (std::is_same<R, float>::value) return gb_d2f(x);
+            else return x;
+        };
+        R rho = ld(GB_DENS), p = ld(GB_PRES);
         R B[3] = {0, 0, 0};
         if (mhd) {
-            B[0] = (R)base[(int64_t)g.slot[GB_MAGX] * GB_N3];
-            B[1] = (R)base[(int64_t)g.slot[GB_MAGY] * GB_N3];
-            B[2] = (R)base[(int64_t)g.slot[GB_MAGZ] * GB_N3];
+            B[0] = ld(GB_MAGX);
+            B[1] = ld(GB_MAGY);
+            B[2] = ld(GB_MAGZ);
         }
         R gp = (R)gamma * p;
         R B2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
         R tt = (gp + B2) / rho;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            R v = fabs((R)base[(int64_t)g.slot[GB_VELX + d] * GB_N3]);
+            R v = fabs(ld(GB_VELX + d));
             R cf = sqrt((R)0.5 * (tt + sqrt(fmax(tt * tt - (R)4 * gp * B[d] * B[d] / (rho * rho), (R)0))));
             R dtc = del[d] / (v + cf);
             best = fmin(best, dtc);

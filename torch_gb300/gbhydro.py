@@ -103,6 +103,7 @@ _SIG = {
     "gb_set_dt_limits": (C.c_int, [C.c_double, C.c_double, C.c_double]),
     "gb_set_flux_correction": (C.c_int, [C.c_int]),
     "gb_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
+    "gb_selfcheck_conversions": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gb_graph_reset": (C.c_int, []),
     "gb_graph_info": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "gb_hydro_unsplit_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p,
