@@ -751,14 +751,22 @@ __device__ __forceinline__ void hlld(T gam, const T* L, const T* R, T* F, T* un)
     T byss = (sqs[0] * byst[1] + sqs[1] * byst[0] + sqs[0] * sqs[1] * (vst[1] - vst[0]) * sgn) * isum;
     T bzss = (sqs[0] * bzst[1] + sqs[1] * bzst[0] + sqs[0] * sqs[1] * (wst[1] - wst[0]) * sgn) * isum;
     T vBss = SM * bx + vss * byss + wss * bzss;
-    const int a = SM >= (T)0 ? 0 : 1;
-    T Ess = a == 0 ? Us[0][4] - sqs[0] * (vBst[0] - vBss) * sgn : Us[1][4] + sqs[1] * (vBst[1] - vBss) * sgn;
-    T Uss[NP] = {Us[a][0], Us[a][0] * SM, Us[a][0] * vss, Us[a][0] * wss, Ess, bx, byss, bzss};
-    T S = a == 0 ? SL : SR;
-    T Sst = a == 0 ? Ss0 : Ss1;
+    const bool left = SM >= (T)0;
+    // the side's states picked with selects (a runtime index into Us / Uo
+    // would put both arrays in local memory)
+    T Ua[NP], Uoa[NP];
+#pragma unroll
+    for (int s = 0; s < NP; ++s) {
+        Ua[s] = left ? Us[0][s] : Us[1][s];
+        Uoa[s] = left ? Uo[0][s] : Uo[1][s];
+    }
+    T Ess = left ? Us[0][4] - sqs[0] * (vBst[0] - vBss) * sgn : Us[1][4] + sqs[1] * (vBst[1] - vBss) * sgn;
+    T Uss[NP] = {Ua[0], Ua[0] * SM, Ua[0] * vss, Ua[0] * wss, Ess, bx, byss, bzss};
+    T S = left ? SL : SR;
+    T Sst = left ? Ss0 : Ss1;
 #pragma unroll
     for (int s = 0; s < NP; ++s)
-        F[s] = (a == 0 ? FL[s] : FR[s]) + S * (Us[a][s] - Uo[a][s]) + Sst * (Uss[s] - Us[a][s]);
+        F[s] = (left ? FL[s] : FR[s]) + S * (Ua[s] - Uoa[s]) + Sst * (Uss[s] - Ua[s]);
 }
 
 // flux box of direction d: normal faces 4..20 (17), transverse cells 3..20 (18)
