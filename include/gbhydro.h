@@ -161,11 +161,13 @@ int gb_hydro_unsplit_noalloc(int blockCount, const int* blockList_dev, double dt
 int gb_set_chunk_blocks(int n);
 
 /* Launch shapes of the hydro step: blocks per chunk (the scratch of one
- * chunk is reused across chunks; 16 blocks of mixed-precision scratch fit
- * in L2) and cells per reconstruction CTA per direction (32 or 64). Chosen
- * by torch_gb300.autotune; no counterpart in the reference. */
-int gb_set_launch_config(int chunk_blocks, int recon_tile);
-int gb_get_launch_config(int* chunk_blocks, int* recon_tile);
+ * chunk is reused across chunks), cells per reconstruction CTA per
+ * direction (32 or 64), and for the mixed path's reconstruction whether its
+ * registers are bounded for occupancy (1: at least 6 / 3 resident CTAs per
+ * SM for tile 32 / 64, with some spilling; 0: unbounded). Chosen by
+ * torch_gb300.autotune; no counterpart in the reference. */
+int gb_set_launch_config(int chunk_blocks, int recon_tile, int recon_occupancy);
+int gb_get_launch_config(int* chunk_blocks, int* recon_tile, int* recon_occupancy);
 
 /* CFL time step: writes cfl * min over interior cells of the listed blocks
  * of dx_d / (|v_d| + c_f,d) to *dt_dev (device double). The per-block

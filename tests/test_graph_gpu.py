@@ -79,8 +79,8 @@ def test_launch_shapes_do_not_change_results(gb, precision):
     gb.init_hydro(gb.hydro_params(True, precision=precision))
     out = []
     try:
-        for chunk, tile in ((16, 32), (5, 64), (64, 32)):
-            gb.set_launch_config(chunk, tile)
+        for chunk, tile, occ in ((16, 32, 0), (5, 64, 0), (64, 32, 1), (7, 64, 1)):
+            gb.set_launch_config(chunk, tile, occ)
             g = _grid(gb)
             dt = g.compute_dt().item()
             g.evolve_step(dt, cool=False)
@@ -89,7 +89,7 @@ def test_launch_shapes_do_not_change_results(gb, precision):
             del g
     finally:
         gb.set_launch_config(16, 32)
-    assert torch.equal(out[0], out[1]) and torch.equal(out[0], out[2])
+    assert all(torch.equal(out[0], o) for o in out[1:])
 
 
 def test_autotuner_picks_a_candidate_and_restores_state(gb, tmp_path, monkeypatch):
@@ -104,11 +104,11 @@ def test_autotuner_picks_a_candidate_and_restores_state(gb, tmp_path, monkeypatc
     before = g.u.clone()
     try:
         r = autotune.tune(g, cool=True, chunks=(8, 16), tiles=(32, 64), steps=1)
-        assert (r["chunk"], r["tile"]) in {(8, 32), (8, 64), (16, 32), (16, 64)}
-        assert gb.get_launch_config() == (r["chunk"], r["tile"])
-        assert len(r["trials"]) == 4 and not r["cached"]
+        assert (r["chunk"], r["tile"]) in {(8, 32), (8, 64), (16, 32), (16, 64)} and r["occ"] in (0, 1)
+        assert gb.get_launch_config() == (r["chunk"], r["tile"], r["occ"])
+        assert len(r["trials"]) == 8 and not r["cached"]
         assert torch.equal(g.u, before)
         r2 = autotune.tune(g, cool=True, chunks=(8, 16), tiles=(32, 64), steps=1)
-        assert r2["cached"] and (r2["chunk"], r2["tile"]) == (r["chunk"], r["tile"])
+        assert r2["cached"] and (r2["chunk"], r2["tile"], r2["occ"]) == (r["chunk"], r["tile"], r["occ"])
     finally:
         gb.set_launch_config(16, 32)

@@ -1,7 +1,8 @@
 """Autotuner for the launch shapes of the step.
 
 Times the whole step (the replayed CUDA graph of gb_step_graph) for each
-candidate (blocks per chunk, reconstruction tile) on the registered grid,
+candidate (blocks per chunk, reconstruction tile, and in the mixed path the
+reconstruction's occupancy bound) on the registered grid,
 restoring the grid's state after every trial so tuning does not advance the
 simulation, and keeps the fastest. Results are cached per device, block
 count, physics and precision in a JSON file beside this module (or the path
@@ -14,6 +15,7 @@ import os
 
 CHUNKS = (16, 32, 64, 128)
 TILES = (32, 64)
+OCCS = (0, 1)
 CACHE = os.environ.get("GBHYDRO_TUNE_CACHE",
                        os.path.join(os.path.dirname(os.path.abspath(__file__)), "_tune_cache.json"))
 
@@ -44,11 +46,11 @@ def _save(d: dict) -> None:
         pass
 
 
-def time_config(grid, cool: bool, chunk: int, tile: int, steps: int = 3, warmup: int = 1) -> float:
+def time_config(grid, cool: bool, chunk: int, tile: int, steps: int = 3, warmup: int = 1, occ: int = 0) -> float:
     """ms per step of the graph-replayed step at one launch shape."""
     import torch
     from . import gbhydro as G
-    G.set_launch_config(chunk, tile)
+    G.set_launch_config(chunk, tile, occ)
     s = torch.cuda.current_stream()
     for _ in range(warmup):
         grid.step_graph(cool)
@@ -61,35 +63,39 @@ def time_config(grid, cool: bool, chunk: int, tile: int, steps: int = 3, warmup:
     return a.elapsed_time(b) / steps
 
 
-def tune(grid, cool: bool = True, chunks=CHUNKS, tiles=TILES, steps: int = 3, use_cache: bool = True) -> dict:
-    """Pick and set the fastest (chunk, tile) for `grid` (registered, with
-    hydro/cooling configured). Returns {"chunk", "tile", "ms", "trials",
-    "cached"}."""
+def tune(grid, cool: bool = True, chunks=CHUNKS, tiles=TILES, occs=OCCS, steps: int = 3,
+         use_cache: bool = True) -> dict:
+    """Pick and set the fastest (chunk, tile, occ) for `grid` (registered,
+    with hydro/cooling configured; the occupancy bound only exists in the
+    mixed path). Returns {"chunk", "tile", "occ", "ms", "trials", "cached"}."""
     import torch
     from . import gbhydro as G
     key = _key(grid, cool)
     cache = _load() if use_cache else {}
     if key in cache:
         r = dict(cache[key], cached=True)
-        G.set_launch_config(r["chunk"], r["tile"])
+        G.set_launch_config(r["chunk"], r["tile"], r.get("occ", 0))
         return r
+    if G.state["precision"] != 1:
+        occs = (0,)
     saved = [grid.u.clone()] + ([a.clone() for a in (grid.fx, grid.fy, grid.fz)] if grid.mhd else [])
     trials = []
     try:
         for c in chunks:
             for t in tiles:
-                ms = time_config(grid, cool, c, t, steps=steps)
-                trials.append({"chunk": c, "tile": t, "ms": ms})
-                grid.u.copy_(saved[0])
-                if grid.mhd:
-                    for a, b in zip((grid.fx, grid.fy, grid.fz), saved[1:]):
-                        a.copy_(b)
+                for o in occs:
+                    ms = time_config(grid, cool, c, t, steps=steps, occ=o)
+                    trials.append({"chunk": c, "tile": t, "occ": o, "ms": ms})
+                    grid.u.copy_(saved[0])
+                    if grid.mhd:
+                        for a, b in zip((grid.fx, grid.fy, grid.fz), saved[1:]):
+                            a.copy_(b)
     finally:
         del saved
         torch.cuda.synchronize()
     best = min(trials, key=lambda r: r["ms"])
-    G.set_launch_config(best["chunk"], best["tile"])
-    r = {"chunk": best["chunk"], "tile": best["tile"], "ms": best["ms"], "trials": trials}
+    G.set_launch_config(best["chunk"], best["tile"], best["occ"])
+    r = {"chunk": best["chunk"], "tile": best["tile"], "occ": best["occ"], "ms": best["ms"], "trials": trials}
     if use_cache:
         cache[key] = r
         _save(cache)

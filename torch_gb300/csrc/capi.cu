@@ -786,26 +786,32 @@ int gb_dt_launch(const gbh::hydro_kparams& kp, int mhd, int nblk, const int* lis
 
 static int g_chunk_blocks = 16;
 static int g_recon_tile = 32;
+static int g_recon_occ = 0;
 
 int gb_chunk_blocks() { return g_chunk_blocks; }
 int gb_recon_tile() { return g_recon_tile; }
+int gb_recon_occupancy() { return g_recon_occ; }
 
-extern "C" int gb_set_launch_config(int chunk_blocks, int recon_tile)
+extern "C" int gb_set_launch_config(int chunk_blocks, int recon_tile, int recon_occupancy)
 {
-    if (chunk_blocks < 1 || chunk_blocks > 65535 || (recon_tile != 32 && recon_tile != 64)) {
-        gb_set_error("gb_set_launch_config: chunk %d (1..65535), recon tile %d (32 or 64)", chunk_blocks, recon_tile);
+    if (chunk_blocks < 1 || chunk_blocks > 65535 || (recon_tile != 32 && recon_tile != 64) || recon_occupancy < 0 ||
+        recon_occupancy > 1) {
+        gb_set_error("gb_set_launch_config: chunk %d (1..65535), recon tile %d (32 or 64), occupancy %d (0 or 1)",
+                     chunk_blocks, recon_tile, recon_occupancy);
         return GB_ERR_ARG;
     }
     g_chunk_blocks = chunk_blocks;
     g_recon_tile = recon_tile;
+    g_recon_occ = recon_occupancy;
     g_gb.gen += 1;
     return GB_OK;
 }
 
-extern "C" int gb_get_launch_config(int* chunk_blocks, int* recon_tile)
+extern "C" int gb_get_launch_config(int* chunk_blocks, int* recon_tile, int* recon_occupancy)
 {
     if (chunk_blocks) *chunk_blocks = g_chunk_blocks;
     if (recon_tile) *recon_tile = g_recon_tile;
+    if (recon_occupancy) *recon_occupancy = g_recon_occ;
     return GB_OK;
 }
 

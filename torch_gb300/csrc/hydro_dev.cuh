@@ -539,8 +539,11 @@ __device__ __forceinline__ void recon_transverse(const T* hd, int lane, T (*s_si
     }
 }
 
-template <typename T, bool MHD, int TILE>
-__global__ void __launch_bounds__(3 * TILE)
+// MINB: resident CTAs per SM the register allocation must allow (1 = no
+// bound); the autotuner chooses between the unbounded kernel and a bound
+// that trades spills for occupancy
+template <typename T, bool MHD, int TILE, int MINB>
+__global__ void __launch_bounds__(3 * TILE, MINB)
 k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __restrict__ scr,
         size_t scr_stride, const float* __restrict__ p32, size_t p32_stride, gb_status* st)
 {

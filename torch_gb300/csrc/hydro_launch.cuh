@@ -9,6 +9,23 @@
 
 namespace gbh {
 
+// reconstruction at the tuned shape: tile 32 or 64, register-unbounded or
+// (mixed path) bounded to 6 / 3 resident CTAs per SM
+template <typename T, bool MHD>
+void launch_recon(int tile, dim3 rg, cudaStream_t s, const gb_dev_grid& g, const hydro_kparams& kp, const int* list,
+                  T* rscr, const float* p32, gb_status* st)
+{
+    using SL = scratch_layout<T>;
+    const bool occ = std::is_same<T, float>::value && gb_recon_occupancy();
+    if (tile == 64) {
+        if (occ) k_recon<T, MHD, 64, 3><<<rg, 3 * 64, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+        else k_recon<T, MHD, 64, 1><<<rg, 3 * 64, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+    } else {
+        if (occ) k_recon<T, MHD, 32, 6><<<rg, 3 * 32, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+        else k_recon<T, MHD, 32, 1><<<rg, 3 * 32, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+    }
+}
+
 template <typename T>
 int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
                  void* scratch, gb_status* st, cudaStream_t s)
@@ -34,8 +51,7 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
     dim3 fg((NFC + 127) / 128, 3, nblk);
     if (mhd) {
         gb_prof_begin(GBP_RECON, s);
-        if (tile == 64) k_recon<T, true, 64><<<rg, 3 * 64, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
-        else k_recon<T, true, 32><<<rg, 3 * 32, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+        launch_recon<T, true>(tile, rg, s, g, kp, list, rscr, p32, st);
         gb_prof_end(GBP_RECON, s);
         gb_prof_begin(GBP_FLUX, s);
         k_flux<T, true><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);
@@ -50,8 +66,7 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
         gb_prof_end(GBP_FACEB, s);
     } else {
         gb_prof_begin(GBP_RECON, s);
-        if (tile == 64) k_recon<T, false, 64><<<rg, 3 * 64, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
-        else k_recon<T, false, 32><<<rg, 3 * 32, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+        launch_recon<T, false>(tile, rg, s, g, kp, list, rscr, p32, st);
         gb_prof_end(GBP_RECON, s);
         gb_prof_begin(GBP_FLUX, s);
         k_flux<T, false><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);

@@ -97,8 +97,8 @@ _SIG = {
     "gb_hydro_init": (C.c_int, [C.POINTER(HydroParams)]),
     "gb_hydro_unsplit": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_void_p]),
     "gb_set_chunk_blocks": (C.c_int, [C.c_int]),
-    "gb_set_launch_config": (C.c_int, [C.c_int, C.c_int]),
-    "gb_get_launch_config": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "gb_set_launch_config": (C.c_int, [C.c_int, C.c_int, C.c_int]),
+    "gb_get_launch_config": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "gb_step_graph": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gb_set_dt_limits": (C.c_int, [C.c_double, C.c_double, C.c_double]),
     "gb_set_flux_correction": (C.c_int, [C.c_int]),
@@ -376,14 +376,16 @@ def set_brent_tolerance(kelvin: float = 1.0) -> None:
     check(lib().gb_set_brent_tolerance(float(kelvin)), "gb_set_brent_tolerance")
 
 
-def set_launch_config(chunk_blocks: int, recon_tile: int) -> None:
-    check(lib().gb_set_launch_config(int(chunk_blocks), int(recon_tile)), "gb_set_launch_config")
+def set_launch_config(chunk_blocks: int, recon_tile: int, recon_occupancy: int = 0) -> None:
+    check(lib().gb_set_launch_config(int(chunk_blocks), int(recon_tile), int(recon_occupancy)),
+          "gb_set_launch_config")
 
 
 def get_launch_config() -> tuple:
-    a, b = C.c_int(), C.c_int()
-    check(lib().gb_get_launch_config(C.byref(a), C.byref(b)), "gb_get_launch_config")
-    return a.value, b.value
+    """(blocks per chunk, reconstruction tile, reconstruction occupancy bound)."""
+    a, b, c = C.c_int(), C.c_int(), C.c_int()
+    check(lib().gb_get_launch_config(C.byref(a), C.byref(b), C.byref(c)), "gb_get_launch_config")
+    return a.value, b.value, c.value
 
 
 def set_chunk_blocks(n: int) -> None:
