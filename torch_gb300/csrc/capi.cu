@@ -237,6 +237,7 @@ extern "C" int gb_register_grid(const gb_grid_desc* grid, const gb_tree_desc* tr
     g_gb.grid.level = nullptr;
     g_gb.grid_ok = true;
     g_gb.links_ok = false;
+    g_gb.rtab_ok = false;
     g_gb.gen += 1;
     g_gb.tree_ok = false;
     if (tree) {
@@ -303,6 +304,58 @@ __device__ __forceinline__ leaf_hit find_leaf(const gb_tree_desc& t, long long X
 // periodic wrap of a guard position: x lies in (-n, 2n) (a guard region is
 // narrower than the domain)
 __device__ __forceinline__ long long wrap(long long x, long long n) { return x < 0 ? x + n : (x >= n ? x - n : x); }
+
+// Region table of the guard fill: for every leaf b, the node covering each
+// of the 27 block-sized regions around it (offsets -1, 0, 1 per axis,
+// periodic; region r = rx + 3 ry + 9 rz), found by descending from the root
+// no deeper than b's level: a leaf of b's level or coarser, or a refined
+// node of b's level whose children cover the region. A guard cell then
+// needs one table load and at most one step down instead of a walk from
+// the root.
+__global__ void k_region_table(gb_tree_desc t, int* __restrict__ tab)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= t.nnodes * 27) return;
+    const int b = idx / 27, r = idx % 27;
+    tab[idx] = -1;
+    if (t.child[8 * b] >= 0) return;
+    const int L = t.level[b];
+    const long long E = (long long)GB_NXB << (t.maxlevel - L);
+    const long long N[3] = {(long long)t.nrx * GB_NXB << t.maxlevel, (long long)t.nry * GB_NXB << t.maxlevel,
+                            (long long)t.nrz * GB_NXB << t.maxlevel};
+    const int off[3] = {r % 3 - 1, (r / 3) % 3 - 1, r / 9 - 1};
+    long long X[3];
+    for (int d = 0; d < 3; ++d) X[d] = wrap((t.coord[3 * b + d] + off[d]) * E + E / 2, N[d]);
+    const int sh0 = LOG2_NXB + t.maxlevel;
+    int node = t.root[(int)(X[0] >> sh0) + t.nrx * ((int)(X[1] >> sh0) + t.nry * (int)(X[2] >> sh0))];
+    for (int l = 0; l < L && node >= 0; ++l) {
+        if (t.child[8 * node] < 0) break;
+        const int sh = sh0 - 1 - l;
+        node = t.child[8 * node + (int)((X[0] >> sh) & 1) + 2 * (int)((X[1] >> sh) & 1) + 4 * (int)((X[2] >> sh) & 1)];
+    }
+    tab[idx] = node;
+}
+
+__device__ __forceinline__ int region_of(int loc) { return loc < GB_NGUARD ? 0 : (loc >= GB_NGUARD + GB_NXB ? 2 : 1); }
+
+// The leaf covering finest-cell position X, lying in region r of block blk
+// (level L): from the region table's node when there is a table, from the
+// root otherwise.
+__device__ __forceinline__ leaf_hit leaf_near(const gb_tree_desc& t, const int* __restrict__ rtab, int blk, int r,
+                                              int L, long long X, long long Y, long long Z)
+{
+    if (!rtab) return find_leaf(t, X, Y, Z);
+    int node = __ldg(rtab + (size_t)blk * 27 + r);
+    for (int l = L; l <= t.maxlevel && node >= 0; ++l) {
+        if (__ldg(t.child + 8 * node) < 0) break;
+        const int sh = LOG2_NXB + t.maxlevel - 1 - l;
+        node = __ldg(t.child + 8 * node + ((int)((X >> sh) & 1) | ((int)((Y >> sh) & 1) << 1) | ((int)((Z >> sh) & 1) << 2)));
+    }
+    leaf_hit h;
+    h.node = node;
+    h.level = node >= 0 ? t.level[node] : 0;
+    return h;
+}
 
 // Face neighbours of every leaf: links[(b * 6 + f) * 5] = same (0), coarser
 // (1) or finer (2) neighbour across face f = 2 d + side, then the four fine
@@ -406,7 +459,8 @@ struct guard_vars {
     int slot[GB_NROLE];
 };
 
-__global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list, guard_vars gv)
+__global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list, guard_vars gv,
+                              const int* __restrict__ rtab)
 {
     const int blk = list[blockIdx.y];
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -426,7 +480,7 @@ __global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restri
         lo[d] = wrap(((long long)cd[d] * GB_NXB + loc[d] - GB_NGUARD) * s, N[d]);
         X[d] = lo[d] + (s >> 1);
     }
-    leaf_hit h = find_leaf(t, X[0], X[1], X[2]);
+    leaf_hit h = leaf_near(t, rtab, blk, region_of(i) + 3 * region_of(j) + 9 * region_of(k), L, X[0], X[1], X[2]);
     if (h.node < 0) return;
     const int lsl = t.maxlevel - h.level;
     const int* sc = t.coord + 3 * h.node;
@@ -471,7 +525,7 @@ __global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restri
     }
 }
 
-__global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list)
+__global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list, const int* __restrict__ rtab)
 {
     const int a = blockIdx.z;
     const int blk = list[blockIdx.y];
@@ -498,14 +552,16 @@ __global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restri
         lo[d] = wrap(((long long)cd[d] * GB_NXB + I[d] - GB_NGUARD) * s, N[d]);
         X[d] = lo[d] + (d == a ? 0 : (s >> 1));
     }
-    leaf_hit h = find_leaf(t, X[0], X[1], X[2]);
+    const int reg = region_of(I[0]) + 3 * region_of(I[1]) + 9 * region_of(I[2]);
+    leaf_hit h = leaf_near(t, rtab, blk, reg, L, X[0], X[1], X[2]);
     if (h.node < 0) return;
     if (h.level != L) {
         // a face on a level boundary: the copy owned by the leaf of this
         // block's level on the lower side, when there is one, so that every
         // block of a level reads the same face
-        leaf_hit h2 = find_leaf(t, a == 0 ? wrap(X[0] - 1, N[0]) : X[0], a == 1 ? wrap(X[1] - 1, N[1]) : X[1],
-                                a == 2 ? wrap(X[2] - 1, N[2]) : X[2]);
+        const int reg2 = reg + (region_of(I[a] - 1) - region_of(I[a])) * (a == 0 ? 1 : a == 1 ? 3 : 9);
+        leaf_hit h2 = leaf_near(t, rtab, blk, reg2, L, a == 0 ? wrap(X[0] - 1, N[0]) : X[0],
+                                a == 1 ? wrap(X[1] - 1, N[1]) : X[1], a == 2 ? wrap(X[2] - 1, N[2]) : X[2]);
         if (h2.node >= 0 && h2.level == L) {
             X[a] = wrap(X[a] - 1, N[a]) + 1;  // its upper face, unwrapped at the domain edge
             h = h2;
@@ -730,6 +786,39 @@ extern "C" int gb_set_flux_correction(int on)
     return GB_OK;
 }
 
+// The guard fill's region table (trees with more than one level; before
+// any capture: it allocates once per registration).
+int gb_guard_prepare(cudaStream_t s)
+{
+    if (!g_gb.tree_ok || g_gb.tree.maxlevel <= 0 || g_gb.rtab_ok) return GB_OK;
+    const int nn = g_gb.tree.nnodes;
+    if (g_gb.rtab_n < nn) {
+        if (g_gb.d_rtab) cudaFree(g_gb.d_rtab);
+        g_gb.d_rtab = nullptr;
+        g_gb.rtab_n = 0;
+        if (gb_check(cudaMalloc(&g_gb.d_rtab, (size_t)nn * 27 * sizeof(int)), "cudaMalloc(region table)"))
+            return GB_ERR_CUDA;
+        g_gb.rtab_n = nn;
+    }
+    k_region_table<<<(nn * 27 + 255) / 256, 256, 0, s>>>(g_gb.tree, g_gb.d_rtab);
+    if (gb_check(cudaGetLastError(), "k_region_table")) return GB_ERR_CUDA;
+    g_gb.rtab_ok = true;
+    return GB_OK;
+}
+
+// the table when it is ready; inside a capture that did not prepare it
+// (nothing allocates there) the kernels walk from the root instead
+static const int* guard_table(cudaStream_t s)
+{
+    if (!g_gb.tree_ok || g_gb.tree.maxlevel <= 0) return nullptr;
+    if (!g_gb.rtab_ok) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(s, &cs);
+        if (cs != cudaStreamCaptureStatusNone || gb_guard_prepare(s) != GB_OK) return nullptr;
+    }
+    return g_gb.d_rtab;
+}
+
 static guard_vars hydro_guard_vars()
 {
     guard_vars gv;
@@ -744,12 +833,13 @@ int gb_launch_guardfill(int nblk, const int* list, cudaStream_t s)
 {
     dim3 gc((GB_NGC + 127) / 128, nblk);
     gb_prof_begin(GBP_GUARD, s);
-    k_guard_cells<<<gc, 128, 0, s>>>(g_gb.grid, g_gb.tree, list, hydro_guard_vars());
+    const int* rtab = guard_table(s);
+    k_guard_cells<<<gc, 128, 0, s>>>(g_gb.grid, g_gb.tree, list, hydro_guard_vars(), rtab);
     gb_prof_end(GBP_GUARD, s);
     if (g_gb.hp.mhd && g_gb.grid.f[0]) {
         dim3 gf((GB_FSZ + 127) / 128, nblk, 3);
         gb_prof_begin(GBP_GUARD, s);
-        k_guard_faces<<<gf, 128, 0, s>>>(g_gb.grid, g_gb.tree, list);
+        k_guard_faces<<<gf, 128, 0, s>>>(g_gb.grid, g_gb.tree, list, rtab);
         gb_prof_end(GBP_GUARD, s);
     }
     return gb_check(cudaGetLastError(), "guard fill") ? GB_ERR_CUDA : GB_OK;
@@ -766,10 +856,11 @@ extern "C" int gb_fill_guardcells(int blockCount, const int* list, void* stream)
     // the face pass needs to know whether face fields exist; it is keyed on
     // the hydro parameters when set and on the grid otherwise
     dim3 gc((GB_NGC + 127) / 128, blockCount);
-    k_guard_cells<<<gc, 128, 0, (cudaStream_t)stream>>>(g_gb.grid, g_gb.tree, list, hydro_guard_vars());
+    const int* rtab = guard_table((cudaStream_t)stream);
+    k_guard_cells<<<gc, 128, 0, (cudaStream_t)stream>>>(g_gb.grid, g_gb.tree, list, hydro_guard_vars(), rtab);
     if (g_gb.grid.f[0] && g_gb.grid.f[1] && g_gb.grid.f[2]) {
         dim3 gf((GB_FSZ + 127) / 128, blockCount, 3);
-        k_guard_faces<<<gf, 128, 0, (cudaStream_t)stream>>>(g_gb.grid, g_gb.tree, list);
+        k_guard_faces<<<gf, 128, 0, (cudaStream_t)stream>>>(g_gb.grid, g_gb.tree, list, rtab);
     }
     return gb_check(cudaGetLastError(), "guard fill") ? GB_ERR_CUDA : GB_OK;
 }
@@ -1052,6 +1143,7 @@ extern "C" int gb_step_graph(int blockCount, const int* list, int cool, gb_drive
         int rc = gb_ensure_scratch(per * (size_t)chunk);
         if (!rc && cool && gb_cooling_mode() == 1) rc = gb_sur_prepare((int64_t)chunk * 4096, s);
         if (!rc) rc = gb_fc_prepare(blockCount, s);
+        if (!rc) rc = gb_guard_prepare(s);
         if (rc) return rc;
         if (gb_check(cudaStreamSynchronize(s), "graph prepare")) return GB_ERR_CUDA;
         if (gb_check(cudaStreamBeginCapture(g_graph.cap, cudaStreamCaptureModeThreadLocal), "begin capture"))

@@ -34,6 +34,10 @@ struct gb_state_t {
     size_t fcreg_bytes = 0;
     int* d_fclist = nullptr;
     int fclist_cap = 0;
+    // guard fill: the node covering each of the 27 regions around a leaf
+    int* d_rtab = nullptr;
+    int rtab_n = 0;
+    bool rtab_ok = false;
     // bumped by every call that changes what a captured step graph baked
     // in (grid, tree, parameters, tables, weights, modes)
     unsigned long long gen = 0;
@@ -52,6 +56,7 @@ int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int
 int gb_launch_dt(int nblk, const int* list, double* dt_out, cudaStream_t s);
 int gb_launch_guardfill(int nblk, const int* list, cudaStream_t s);
 int gb_sur_prepare(int64_t ncell, cudaStream_t s);
+int gb_guard_prepare(cudaStream_t s);
 // launch shapes chosen by the autotuner (gb_set_launch_config)
 int gb_chunk_blocks();
 int gb_recon_tile();
