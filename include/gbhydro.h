@@ -162,9 +162,9 @@ int gb_set_chunk_blocks(int n);
 
 /* Launch shapes of the hydro step: blocks per chunk (the scratch of one
  * chunk is reused across chunks), cells per reconstruction CTA per
- * direction (32 or 64), and for the mixed path's reconstruction whether its
- * registers are bounded for occupancy (1: at least 6 / 3 resident CTAs per
- * SM for tile 32 / 64, with some spilling; 0: unbounded). Chosen by
+ * direction (32 or 64), and for the mixed path's reconstruction a register
+ * bound for occupancy (0: unbounded; 1: 5 / 2 resident CTAs per SM for tile
+ * 32 / 64, no spills; 2: 6 / 3, with some spilling). Chosen by
  * torch_gb300.autotune; no counterpart in the reference. */
 int gb_set_launch_config(int chunk_blocks, int recon_tile, int recon_occupancy);
 int gb_get_launch_config(int* chunk_blocks, int* recon_tile, int* recon_occupancy);

@@ -15,7 +15,7 @@ import os
 
 CHUNKS = (16, 32, 64, 128)
 TILES = (32, 64)
-OCCS = (0, 1)
+OCCS = (0, 1, 2)
 CACHE = os.environ.get("GBHYDRO_TUNE_CACHE",
                        os.path.join(os.path.dirname(os.path.abspath(__file__)), "_tune_cache.json"))
 

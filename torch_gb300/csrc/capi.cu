@@ -886,8 +886,8 @@ int gb_recon_occupancy() { return g_recon_occ; }
 extern "C" int gb_set_launch_config(int chunk_blocks, int recon_tile, int recon_occupancy)
 {
     if (chunk_blocks < 1 || chunk_blocks > 65535 || (recon_tile != 32 && recon_tile != 64) || recon_occupancy < 0 ||
-        recon_occupancy > 1) {
-        gb_set_error("gb_set_launch_config: chunk %d (1..65535), recon tile %d (32 or 64), occupancy %d (0 or 1)",
+        recon_occupancy > 2) {
+        gb_set_error("gb_set_launch_config: chunk %d (1..65535), recon tile %d (32 or 64), occupancy %d (0..2)",
                      chunk_blocks, recon_tile, recon_occupancy);
         return GB_ERR_ARG;
     }

@@ -9,19 +9,23 @@
 
 namespace gbh {
 
-// reconstruction at the tuned shape: tile 32 or 64, register-unbounded or
-// (mixed path) bounded to 6 / 3 resident CTAs per SM
+// reconstruction at the tuned shape: tile 32 or 64, and in the mixed path a
+// register bound for occupancy: 0 unbounded, 1 the bound that still avoids
+// spills (5 / 2 resident CTAs per SM for tile 32 / 64), 2 a tighter one
+// that spills (6 / 3)
 template <typename T, bool MHD>
 void launch_recon(int tile, dim3 rg, cudaStream_t s, const gb_dev_grid& g, const hydro_kparams& kp, const int* list,
                   T* rscr, const float* p32, gb_status* st)
 {
     using SL = scratch_layout<T>;
-    const bool occ = std::is_same<T, float>::value && gb_recon_occupancy();
+    const int occ = std::is_same<T, float>::value ? gb_recon_occupancy() : 0;
     if (tile == 64) {
-        if (occ) k_recon<T, MHD, 64, 3><<<rg, 3 * 64, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+        if (occ == 2) k_recon<T, MHD, 64, 3><<<rg, 3 * 64, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+        else if (occ == 1) k_recon<T, MHD, 64, 2><<<rg, 3 * 64, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
         else k_recon<T, MHD, 64, 1><<<rg, 3 * 64, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
     } else {
-        if (occ) k_recon<T, MHD, 32, 6><<<rg, 3 * 32, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+        if (occ == 2) k_recon<T, MHD, 32, 6><<<rg, 3 * 32, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
+        else if (occ == 1) k_recon<T, MHD, 32, 5><<<rg, 3 * 32, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
         else k_recon<T, MHD, 32, 1><<<rg, 3 * 32, 0, s>>>(g, kp, list, rscr, SL::recon, p32, SL::prim32, st);
     }
 }
