@@ -45,6 +45,14 @@ WORKLOADS = {
 }
 TDUST0 = 18.0  # initial dust temperature [K] (sim_tdust, flash.par.turbsph_standard:19)
 
+# DRAM bytes (read + write) per interior zone of each profiler category of
+# the fast path, from one ncu capture (profiles/kernels_box128_fast_chunk128.md:
+# the 128^3 box at 128-block chunks; "recon" = primitive conversion +
+# reconstruction, "guard_fill" = cells + faces). The roofline's traffic is
+# this times the zones one launch covers.
+TRAFFIC_B_PER_ZONE = {"recon": 725.7, "update": 286.5, "flux": 443.1, "guard_fill": 415.3, "mlp_infer": 16.0,
+                      "sur_accept": 85.8, "emf": 97.1, "faceb": 65.4, "sur_feat": 36.0, "dt": 97.6}
+
 
 def build_workload(wl, device):
     """(tree, state) of a workload: state = dict(u, fx, fy, fz, root_dx) with
@@ -605,7 +613,11 @@ def main():
         "status": {"plain": {k: st_plain[k] for k in ("code", "n_fallback", "n_eint_switch", "n_bracket_fail")},
                    "fast": {k: st_fast[k] for k in ("code", "n_fallback", "n_eint_switch", "n_bracket_fail")}},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
-                     "frac": ach / hbm, "traffic": None, "peak_kind": hbm_kind, "launch_ms": dom_ms / dom_n,
+                     "frac": ach / hbm,
+                     "traffic": TRAFFIC_B_PER_ZONE[dom] * zones_per_launch if dom in TRAFFIC_B_PER_ZONE else None,
+                     "traffic_source": "ncu DRAM bytes per zone of this kernel on the 128^3 box at 128-block chunks, "
+                                       "times the zones of one launch here",
+                     "peak_kind": hbm_kind, "launch_ms": dom_ms / dom_n,
                      "algo_bytes_per_launch": 216.0 * zones_per_launch},
         "e2e": {"value": zones / (e2e_ms * 1e-3), "unit": "zone-updates/s", "h2d_bytes_per_step": e2e_bytes,
                 "d2h_bytes_per_step": e2e_bytes, "parts": e2e_parts},
