@@ -405,7 +405,7 @@ def lite_run(args, G, wl, tree, st, zones, world, rank, t_ic):
                        "launch_config": {k: pinfo["tuned"][k] for k in ("chunk", "tile")} if pinfo["tuned"] else None},
         "speedup_vs_plain_fp64": ms_plain / ms_fast,
         "l1_err_vs_fp64": l1_fast,
-        "launch_config": {k: ginfo["tuned"].get(k) for k in ("chunk", "tile", "occ")} if ginfo["tuned"] else None,
+        "launch_config": {k: ginfo["tuned"].get(k) for k in ("chunk", "tile", "occ", "streams")} if ginfo["tuned"] else None,
         "surrogate_fallback": st_fast["n_surrogate_reject"],
         "status": {"plain": st_plain["code"], "fast": st_fast["code"]},
         "gpu_launches": int(ginfo["graph_kernels_per_step"]) * args.steps,
@@ -436,7 +436,8 @@ def main():
                     help="time one path alone and print a short line (for profiler captures)")
     ap.add_argument("--chunk", type=int, default=0, help="with --only: blocks per chunk (no autotuning)")
     ap.add_argument("--tile", type=int, default=32, help="with --chunk: reconstruction tile (32 or 64)")
-    ap.add_argument("--occ", type=int, default=0, help="with --chunk: reconstruction occupancy bound (0 or 1)")
+    ap.add_argument("--occ", type=int, default=0, help="with --chunk: reconstruction occupancy bound (0, 1 or 2)")
+    ap.add_argument("--streams", type=int, default=1, help="with --chunk: streams the chunks alternate between (1 or 2)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -487,6 +488,7 @@ def main():
         del st
         if args.chunk:
             G.set_launch_config(args.chunk, args.tile, args.occ)
+            G.set_chunk_streams(args.streams)
         prec, sur, graph = {"plain": (0, False, True), "fast": (1, True, True), "eager": (1, True, False)}[args.only]
         ms, stt, info = run_path(G, g, prec, args.steps, args.warmup, surrogate=sur, graph=graph,
                                  tune=not args.no_tune and graph and not args.chunk, profile=not graph,
@@ -600,8 +602,8 @@ def main():
         "mixed_plain_cooling": {"value": zones * world / (ms_mixed * 1e-3), "ms_per_step": ms_mixed},
         "fast_eager": {"ms_per_step": ms_eager, "value": zones * world / (ms_eager * 1e-3),
                        "note": "the same fast path launched kernel by kernel with the host reading dt each step"},
-        "launch_config": {k: ginfo["tuned"].get(k) for k in ("chunk", "tile", "occ", "cached")} if ginfo["tuned"] else
-                         {"chunk": 16, "tile": 32, "occ": 0, "tuned": False},
+        "launch_config": {k: ginfo["tuned"].get(k) for k in ("chunk", "tile", "occ", "streams", "cached")}
+        if ginfo["tuned"] else {"chunk": 16, "tile": 32, "occ": 0, "streams": 1, "tuned": False},
         "kernel_ms_per_step_fast": {k: v[0] / args.steps for k, v in prof.items()},
         "kernel_launches_per_step_fast": {k: v[1] / args.steps for k, v in prof.items()},
         "temp_rel_err_vs_plain_after_steps": temp_steps,

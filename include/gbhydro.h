@@ -169,6 +169,16 @@ int gb_set_chunk_blocks(int n);
 int gb_set_launch_config(int chunk_blocks, int recon_tile, int recon_occupancy);
 int gb_get_launch_config(int* chunk_blocks, int* recon_tile, int* recon_occupancy);
 
+/* Streams the chunks of a step run on (1 or 2). With 2, consecutive chunks
+ * alternate between the caller's stream and a library stream, each with its
+ * own scratch, so that one chunk's FP64-bound kernels overlap the next
+ * chunk's FP32-bound ones; under flux conservation a chunk waits for the
+ * previous chunk's flux registration. Results are bitwise those of 1
+ * stream. Default 1; chosen by torch_gb300.autotune; no counterpart in the
+ * reference. */
+int gb_set_chunk_streams(int n);
+int gb_get_chunk_streams(void);
+
 /* CFL time step: writes cfl * min over interior cells of the listed blocks
  * of dx_d / (|v_d| + c_f,d) to *dt_dev (device double). The per-block
  * Hydro_computeDt + MPI_AllReduce(MINLOC) of

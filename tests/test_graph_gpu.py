@@ -92,6 +92,47 @@ def test_launch_shapes_do_not_change_results(gb, precision):
     assert all(torch.equal(out[0], o) for o in out[1:])
 
 
+@pytest.mark.parametrize("precision,surrogate", [(0, False), (1, True)])
+def test_two_chunk_streams_match_one(gb, precision, surrogate):
+    """Chunks alternating between two streams (with flux conservation across
+    the three levels of the tree, so chunks wait on each other's flux
+    registration) give the one-stream state bit for bit, eager and graph."""
+    import torch
+    units = gb.code_units()
+    gb.init_cooling(gb.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
+                                   time_unit=units["time_unit"]))
+    if surrogate:
+        gb.mlp_init(3)
+    gb.init_hydro(gb.hydro_params(True, precision=precision))
+    gb.set_flux_correction(True)
+    gb.set_cooling_mode(surrogate)
+    out = []
+    try:
+        for ns, graph in ((1, False), (2, False), (2, True)):
+            gb.set_launch_config(7, 32, 1 if precision == 1 else 0)
+            gb.set_chunk_streams(ns)
+            assert gb.get_chunk_streams() == ns
+            g = _grid(gb)
+            g.register()
+            for _ in range(2):
+                if graph:
+                    g.step_graph(cool=True)
+                else:
+                    g.evolve_step(g.compute_dt().item(), cool=True)
+            torch.cuda.synchronize()
+            assert g.status_read()["code"] == 0
+            out.append([g.u[g.t_leaf.long()].clone()] + [x[g.t_leaf.long()].clone() for x in (g.fx, g.fy, g.fz)])
+            del g
+    finally:
+        gb.set_chunk_streams(1)
+        gb.set_launch_config(16, 32)
+        gb.set_cooling_mode(False)
+    for o in out[1:]:
+        assert all(torch.equal(x, y) for x, y in zip(out[0], o))
+    with pytest.raises(Exception):
+        gb.set_chunk_streams(3)
+
+
 def test_autotuner_picks_a_candidate_and_restores_state(gb, tmp_path, monkeypatch):
     import torch
     from torch_gb300 import autotune
@@ -106,9 +147,11 @@ def test_autotuner_picks_a_candidate_and_restores_state(gb, tmp_path, monkeypatc
         r = autotune.tune(g, cool=True, chunks=(8, 16), tiles=(32, 64), steps=1)
         assert (r["chunk"], r["tile"]) in {(8, 32), (8, 64), (16, 32), (16, 64)} and r["occ"] in (0, 1, 2)
         assert gb.get_launch_config() == (r["chunk"], r["tile"], r["occ"])
-        assert len(r["trials"]) == 12 and not r["cached"]
+        assert gb.get_chunk_streams() == r["streams"]
+        assert len(r["trials"]) == 24 and not r["cached"]
         assert torch.equal(g.u, before)
         r2 = autotune.tune(g, cool=True, chunks=(8, 16), tiles=(32, 64), steps=1)
         assert r2["cached"] and (r2["chunk"], r2["tile"], r2["occ"]) == (r["chunk"], r["tile"], r["occ"])
     finally:
         gb.set_launch_config(16, 32)
+        gb.set_chunk_streams(1)

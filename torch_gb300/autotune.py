@@ -1,8 +1,9 @@
 """Autotuner for the launch shapes of the step.
 
 Times the whole step (the replayed CUDA graph of gb_step_graph) for each
-candidate (blocks per chunk, reconstruction tile, and in the mixed path the
-reconstruction's occupancy bound) on the registered grid,
+candidate (blocks per chunk, reconstruction tile, in the mixed path the
+reconstruction's occupancy bound, and the number of streams the chunks
+alternate between) on the registered grid,
 restoring the grid's state after every trial so tuning does not advance the
 simulation, and keeps the fastest. Results are cached per device, block
 count, physics and precision in a JSON file beside this module (or the path
@@ -16,6 +17,7 @@ import os
 CHUNKS = (16, 32, 64, 128)
 TILES = (32, 64)
 OCCS = (0, 1, 2)
+STREAMS = (1, 2)
 CACHE = os.environ.get("GBHYDRO_TUNE_CACHE",
                        os.path.join(os.path.dirname(os.path.abspath(__file__)), "_tune_cache.json"))
 
@@ -46,11 +48,13 @@ def _save(d: dict) -> None:
         pass
 
 
-def time_config(grid, cool: bool, chunk: int, tile: int, steps: int = 3, warmup: int = 1, occ: int = 0) -> float:
+def time_config(grid, cool: bool, chunk: int, tile: int, steps: int = 3, warmup: int = 1, occ: int = 0,
+                streams: int = 1) -> float:
     """ms per step of the graph-replayed step at one launch shape."""
     import torch
     from . import gbhydro as G
     G.set_launch_config(chunk, tile, occ)
+    G.set_chunk_streams(streams)
     s = torch.cuda.current_stream()
     for _ in range(warmup):
         grid.step_graph(cool)
@@ -64,10 +68,11 @@ def time_config(grid, cool: bool, chunk: int, tile: int, steps: int = 3, warmup:
 
 
 def tune(grid, cool: bool = True, chunks=CHUNKS, tiles=TILES, occs=OCCS, steps: int = 3,
-         use_cache: bool = True) -> dict:
-    """Pick and set the fastest (chunk, tile, occ) for `grid` (registered,
-    with hydro/cooling configured; the occupancy bound only exists in the
-    mixed path). Returns {"chunk", "tile", "occ", "ms", "trials", "cached"}."""
+         use_cache: bool = True, streams=STREAMS) -> dict:
+    """Pick and set the fastest (chunk, tile, occ, streams) for `grid`
+    (registered, with hydro/cooling configured; the occupancy bound only
+    exists in the mixed path). Returns {"chunk", "tile", "occ", "streams",
+    "ms", "trials", "cached"}."""
     import torch
     from . import gbhydro as G
     key = _key(grid, cool)
@@ -75,6 +80,7 @@ def tune(grid, cool: bool = True, chunks=CHUNKS, tiles=TILES, occs=OCCS, steps: 
     if key in cache:
         r = dict(cache[key], cached=True)
         G.set_launch_config(r["chunk"], r["tile"], r.get("occ", 0))
+        G.set_chunk_streams(r.get("streams", 1))
         return r
     if G.state["precision"] != 1:
         occs = (0,)
@@ -84,18 +90,21 @@ def tune(grid, cool: bool = True, chunks=CHUNKS, tiles=TILES, occs=OCCS, steps: 
         for c in chunks:
             for t in tiles:
                 for o in occs:
-                    ms = time_config(grid, cool, c, t, steps=steps, occ=o)
-                    trials.append({"chunk": c, "tile": t, "occ": o, "ms": ms})
-                    grid.u.copy_(saved[0])
-                    if grid.mhd:
-                        for a, b in zip((grid.fx, grid.fy, grid.fz), saved[1:]):
-                            a.copy_(b)
+                    for ns in streams:
+                        ms = time_config(grid, cool, c, t, steps=steps, occ=o, streams=ns)
+                        trials.append({"chunk": c, "tile": t, "occ": o, "streams": ns, "ms": ms})
+                        grid.u.copy_(saved[0])
+                        if grid.mhd:
+                            for a, b in zip((grid.fx, grid.fy, grid.fz), saved[1:]):
+                                a.copy_(b)
     finally:
         del saved
         torch.cuda.synchronize()
     best = min(trials, key=lambda r: r["ms"])
     G.set_launch_config(best["chunk"], best["tile"], best["occ"])
-    r = {"chunk": best["chunk"], "tile": best["tile"], "occ": best["occ"], "ms": best["ms"], "trials": trials}
+    G.set_chunk_streams(best["streams"])
+    r = {"chunk": best["chunk"], "tile": best["tile"], "occ": best["occ"], "streams": best["streams"],
+         "ms": best["ms"], "trials": trials}
     if use_cache:
         cache[key] = r
         _save(cache)

@@ -869,17 +869,63 @@ extern "C" int gb_fill_guardcells(int blockCount, const int* list, void* stream)
 size_t gb_hydro_scratch_bytes_fp64();
 size_t gb_hydro_scratch_bytes_mixed();
 int gb_hydro_chunk_fp64(const gbh::hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
-                        void* scratch, gb_status* st, cudaStream_t s);
+                        void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put);
 int gb_hydro_chunk_mixed(const gbh::hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
-                         void* scratch, gb_status* st, cudaStream_t s);
+                         void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put);
 int gb_dt_launch(const gbh::hydro_kparams& kp, int mhd, int nblk, const int* list,
                  unsigned long long* bits, cudaStream_t s);
 
 static int g_chunk_blocks = 16;
+static int g_chunk_streams = 1;
 static int g_recon_tile = 32;
 static int g_recon_occ = 0;
 
 int gb_chunk_blocks() { return g_chunk_blocks; }
+int gb_chunk_streams() { return g_chunk_streams; }
+extern "C" int gb_get_chunk_streams(void) { return g_chunk_streams; }
+
+// Chunks on two streams: consecutive chunks alternate between the caller's
+// stream and a library stream, each with its own scratch, so that one
+// chunk's FP64-bound kernels (update, face B, acceptance) run beside the
+// next chunk's FP32-bound ones (reconstruction, fluxes, MLP). Results do not
+// change: chunks touch disjoint blocks, and where flux conservation applies
+// a chunk starts only after the previous chunk has registered its fluxes.
+extern "C" int gb_set_chunk_streams(int n)
+{
+    if (n != 1 && n != 2) {
+        gb_set_error("gb_set_chunk_streams: %d (1 or 2)", n);
+        return GB_ERR_ARG;
+    }
+    g_chunk_streams = n;
+    g_gb.gen += 1;
+    return GB_OK;
+}
+
+namespace {
+struct chunk_aux {
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    std::vector<cudaEvent_t> put;  // one per chunk
+} g_aux;
+}  // namespace
+
+// The second stream and the events of a step of nchunks chunks (before any
+// capture: it creates them once).
+int gb_streams_prepare(int nchunks)
+{
+    if (g_chunk_streams < 2) return GB_OK;
+    if (!g_aux.s2 && gb_check(cudaStreamCreateWithFlags(&g_aux.s2, cudaStreamNonBlocking), "chunk stream"))
+        return GB_ERR_CUDA;
+    if (!g_aux.fork && (gb_check(cudaEventCreateWithFlags(&g_aux.fork, cudaEventDisableTiming), "event") ||
+                        gb_check(cudaEventCreateWithFlags(&g_aux.join, cudaEventDisableTiming), "event")))
+        return GB_ERR_CUDA;
+    while ((int)g_aux.put.size() < nchunks) {
+        cudaEvent_t e;
+        if (gb_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event")) return GB_ERR_CUDA;
+        g_aux.put.push_back(e);
+    }
+    return GB_OK;
+}
 int gb_recon_tile() { return g_recon_tile; }
 int gb_recon_occupancy() { return g_recon_occ; }
 
@@ -947,16 +993,25 @@ static gbh::hydro_kparams make_kp(double dt, const double* dtp = nullptr)
 }
 
 int gb_cooling_mode();
-int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp, gb_status* st, cudaStream_t s);
+int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp, gb_status* st, cudaStream_t s,
+                        int chain);
 
 int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int cool, gb_status* st,
                     cudaStream_t s)
 {
     const int chunk = g_chunk_blocks < nblk ? g_chunk_blocks : nblk;
     const bool mixed = g_gb.hp.precision == 1;
+    const int nchunks = (nblk + chunk - 1) / chunk;
+    // the in-library profiler times launches one by one: one stream then
+    const int ns = g_chunk_streams > 1 && nchunks > 1 && !g_prof.on ? 2 : 1;
     size_t per = mixed ? gb_hydro_scratch_bytes_mixed() : gb_hydro_scratch_bytes_fp64();
-    int rc = gb_ensure_scratch(per * (size_t)chunk);
+    const size_t chunk_bytes = (per * (size_t)chunk + 255) / 256 * 256;
+    int rc = gb_ensure_scratch(chunk_bytes * ns);
     if (rc) return rc;
+    if (ns > 1) {
+        rc = gb_streams_prepare(nchunks);
+        if (rc) return rc;
+    }
     gbh::hydro_kparams kp = make_kp(dt, dtp);
     bool fc = false;
     rc = fc_prepare(nblk, s, &fc);
@@ -970,16 +1025,35 @@ int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int
         kp.fc_links = g_gb.d_links;
         kp.fc_reg = g_gb.d_fcreg;
     }
-    for (int b0 = 0; b0 < nblk; b0 += chunk) {
+    if (ns > 1) {
+        cudaEventRecord(g_aux.fork, s);
+        cudaStreamWaitEvent(g_aux.s2, g_aux.fork, 0);
+    }
+    for (int k = 0, b0 = 0; b0 < nblk; ++k, b0 += chunk) {
         int nb = nblk - b0 < chunk ? nblk - b0 : chunk;
         const int fused = cool && gb_cooling_mode() == 0;
-        rc = mixed ? gb_hydro_chunk_mixed(kp, g_gb.hp.mhd, fused, nb, list + b0, g_gb.d_scratch, st, s)
-                   : gb_hydro_chunk_fp64(kp, g_gb.hp.mhd, fused, nb, list + b0, g_gb.d_scratch, st, s);
+        const int chain = ns > 1 ? (k & 1) : 0;
+        cudaStream_t sk = chain ? g_aux.s2 : s;
+        void* scr = (char*)g_gb.d_scratch + (size_t)chain * chunk_bytes;
+        cudaEvent_t ev_put = nullptr;
+        if (ns > 1 && fc) {
+            // the fine boundary fluxes this chunk reads were registered by
+            // earlier chunks: wait for the previous one (the chunk before it
+            // ran on this stream)
+            if (k > 0) cudaStreamWaitEvent(sk, g_aux.put[k - 1], 0);
+            ev_put = g_aux.put[k];
+        }
+        rc = mixed ? gb_hydro_chunk_mixed(kp, g_gb.hp.mhd, fused, nb, list + b0, scr, st, sk, ev_put)
+                   : gb_hydro_chunk_fp64(kp, g_gb.hp.mhd, fused, nb, list + b0, scr, st, sk, ev_put);
         if (rc) return rc;
         if (cool && !fused) {
-            rc = gb_launch_surrogate(nb, list + b0, dt, dtp, st, s);
+            rc = gb_launch_surrogate(nb, list + b0, dt, dtp, st, sk, chain);
             if (rc) return rc;
         }
+    }
+    if (ns > 1) {
+        cudaEventRecord(g_aux.join, g_aux.s2);
+        cudaStreamWaitEvent(s, g_aux.join, 0);
     }
     return GB_OK;
 }
@@ -1140,10 +1214,11 @@ extern "C" int gb_step_graph(int blockCount, const int* list, int cool, gb_drive
         // everything that allocates or uploads happens before the capture
         const int chunk = gb_chunk_blocks() < blockCount ? gb_chunk_blocks() : blockCount;
         size_t per = g_gb.hp.precision == 1 ? gb_hydro_scratch_bytes_mixed() : gb_hydro_scratch_bytes_fp64();
-        int rc = gb_ensure_scratch(per * (size_t)chunk);
+        int rc = gb_ensure_scratch((per * (size_t)chunk + 255) / 256 * 256 * (size_t)g_chunk_streams);
         if (!rc && cool && gb_cooling_mode() == 1) rc = gb_sur_prepare((int64_t)chunk * 4096, s);
         if (!rc) rc = gb_fc_prepare(blockCount, s);
         if (!rc) rc = gb_guard_prepare(s);
+        if (!rc) rc = gb_streams_prepare((blockCount + chunk - 1) / chunk);
         if (rc) return rc;
         if (gb_check(cudaStreamSynchronize(s), "graph prepare")) return GB_ERR_CUDA;
         if (gb_check(cudaStreamBeginCapture(g_graph.cap, cudaStreamCaptureModeThreadLocal), "begin capture"))

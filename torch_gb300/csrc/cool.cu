@@ -626,7 +626,7 @@ struct sur_bufs {
     int* rej = nullptr;
     int* nrej = nullptr;
     int64_t cap = 0;
-} g_sb;
+} g_sbs[2];  // one set per chunk stream
 
 gb_cool_pf make_pf(const gb_cool_params& p)
 {
@@ -656,7 +656,7 @@ gb_cool_pf make_pf(const gb_cool_params& p)
     return f;
 }
 
-int sur_ensure(int64_t ncell)
+int sur_ensure(sur_bufs& g_sb, int64_t ncell)
 {
     if (ncell <= g_sb.cap) return GB_OK;
     cudaFree(g_sb.feat);
@@ -679,14 +679,17 @@ int gb_cooling_mode() { return g_cool_mode; }
 
 int gb_sur_prepare(int64_t ncell, cudaStream_t s)
 {
-    int rc = sur_ensure(ncell);
+    int rc = sur_ensure(g_sbs[0], ncell);
+    if (!rc && gb_chunk_streams() > 1) rc = sur_ensure(g_sbs[1], ncell);
     return rc ? rc : gb_mlp_pack(s);
 }
 
-int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp, gb_status* st, cudaStream_t s)
+int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp, gb_status* st, cudaStream_t s,
+                        int chain)
 {
+    sur_bufs& g_sb = g_sbs[chain & 1];
     const int64_t ncell = (int64_t)nblk * 4096;
-    int rc = sur_ensure(ncell);
+    int rc = sur_ensure(g_sb, ncell);
     if (rc) return rc;
     const unsigned nb = (unsigned)((ncell + 127) / 128);
     gb_prof_begin(GBP_SUR_FEAT, s);

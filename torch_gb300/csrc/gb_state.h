@@ -59,5 +59,6 @@ int gb_sur_prepare(int64_t ncell, cudaStream_t s);
 int gb_guard_prepare(cudaStream_t s);
 // launch shapes chosen by the autotuner (gb_set_launch_config)
 int gb_chunk_blocks();
+int gb_chunk_streams();
 int gb_recon_tile();
 int gb_recon_occupancy();

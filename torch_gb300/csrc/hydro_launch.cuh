@@ -30,9 +30,23 @@ void launch_recon(int tile, dim3 rg, cudaStream_t s, const gb_dev_grid& g, const
     }
 }
 
+// fine-side boundary fluxes into the flux registers (as soon as the fluxes
+// exist); ev_put, when given, marks their completion for a chunk on
+// another stream
+template <typename T>
+void put_fluxes(const hydro_kparams& kp, int nblk, const int* list, T* fscr, cudaStream_t s, cudaEvent_t ev_put)
+{
+    using SL = scratch_layout<T>;
+    if (kp.fc_links) {
+        dim3 rg2(1, 6, nblk);
+        k_fc_put<T><<<rg2, GB_NXB * GB_NXB, 0, s>>>(list, kp.fc_links, (T*)kp.fc_reg, fscr, SL::flux);
+    }
+    if (ev_put) cudaEventRecord(ev_put, s);
+}
+
 template <typename T>
 int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
-                 void* scratch, gb_status* st, cudaStream_t s)
+                 void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put = nullptr)
 {
     using SL = scratch_layout<T>;
     // scratch of the chunk: [recon | flux | emf | faceb], each block-major
@@ -60,6 +74,7 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
         gb_prof_begin(GBP_FLUX, s);
         k_flux<T, true><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);
         gb_prof_end(GBP_FLUX, s);
+        put_fluxes<T>(kp, nblk, list, fscr, s, ev_put);
         dim3 eg((NEDGE + 127) / 128, 3, nblk);
         gb_prof_begin(GBP_EMF, s);
         k_emf<T><<<eg, 128, 0, s>>>(g, list, fscr, SL::flux, escr, SL::emf, p32, SL::prim32);
@@ -75,10 +90,11 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
         gb_prof_begin(GBP_FLUX, s);
         k_flux<T, false><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);
         gb_prof_end(GBP_FLUX, s);
+        put_fluxes<T>(kp, nblk, list, fscr, s, ev_put);
     }
     if (kp.fc_links) {
+        // after the edge fields, which use the block's own fluxes
         dim3 rg2(1, 6, nblk);
-        k_fc_put<T><<<rg2, GB_NXB * GB_NXB, 0, s>>>(list, kp.fc_links, (T*)kp.fc_reg, fscr, SL::flux);
         k_fc_get<T><<<rg2, GB_NXB * GB_NXB, 0, s>>>(list, kp.fc_links, (const T*)kp.fc_reg, fscr, SL::flux);
     }
     dim3 ug((GB_NXB * GB_NXB * GB_NXB + 127) / 128, nblk);

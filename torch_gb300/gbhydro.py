@@ -99,6 +99,8 @@ _SIG = {
     "gb_set_chunk_blocks": (C.c_int, [C.c_int]),
     "gb_set_launch_config": (C.c_int, [C.c_int, C.c_int, C.c_int]),
     "gb_get_launch_config": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "gb_set_chunk_streams": (C.c_int, [C.c_int]),
+    "gb_get_chunk_streams": (C.c_int, []),
     "gb_step_graph": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gb_set_dt_limits": (C.c_int, [C.c_double, C.c_double, C.c_double]),
     "gb_set_flux_correction": (C.c_int, [C.c_int]),
@@ -386,6 +388,15 @@ def get_launch_config() -> tuple:
     a, b, c = C.c_int(), C.c_int(), C.c_int()
     check(lib().gb_get_launch_config(C.byref(a), C.byref(b), C.byref(c)), "gb_get_launch_config")
     return a.value, b.value, c.value
+
+
+def set_chunk_streams(n: int) -> None:
+    """Run consecutive chunks on 1 or 2 streams (bitwise the same results)."""
+    check(lib().gb_set_chunk_streams(int(n)), "gb_set_chunk_streams")
+
+
+def get_chunk_streams() -> int:
+    return int(lib().gb_get_chunk_streams())
 
 
 def set_chunk_blocks(n: int) -> None:
