@@ -4,6 +4,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "gb_prof.h"
@@ -237,7 +238,7 @@ extern "C" int gb_register_grid(const gb_grid_desc* grid, const gb_tree_desc* tr
     g_gb.grid.level = nullptr;
     g_gb.grid_ok = true;
     g_gb.links_ok = false;
-    g_gb.rtab_ok = false;
+    g_gb.plan_ok = false;
     g_gb.gen += 1;
     g_gb.tree_ok = false;
     if (tree) {
@@ -305,57 +306,141 @@ __device__ __forceinline__ leaf_hit find_leaf(const gb_tree_desc& t, long long X
 // narrower than the domain)
 __device__ __forceinline__ long long wrap(long long x, long long n) { return x < 0 ? x + n : (x >= n ? x - n : x); }
 
-// Region table of the guard fill: for every leaf b, the node covering each
-// of the 27 block-sized regions around it (offsets -1, 0, 1 per axis,
-// periodic; region r = rx + 3 ry + 9 rz), found by descending from the root
-// no deeper than b's level: a leaf of b's level or coarser, or a refined
-// node of b's level whose children cover the region. A guard cell then
-// needs one table load and at most one step down instead of a walk from
-// the root.
-__global__ void k_region_table(gb_tree_desc t, int* __restrict__ tab)
+// Guard-fill plan, built once per registered tree: for every leaf b and
+// each of the 27 block-sized regions around it (offsets -1, 0, 1 per axis,
+// periodic; region r = rx + 3 ry + 9 rz, r = 13 being b itself), the node
+// covering the region, found by descending from the root no deeper than b's
+// level: a leaf of b's level or coarser, or a refined node of b's level
+// whose children cover the region. Two int4 per entry:
+// {node, level, flags, 0} and {cx, cy, cz, 0}. A guard cell then reads its
+// block's entry and its region's entry and takes at most one step down.
+constexpr int GP_REFINED = 1;   // a node of b's level with children
+constexpr int GP_LEAFKIDS = 2;  // ... whose children are all leaves
+
+__global__ void k_guard_plan(gb_tree_desc t, int4* __restrict__ plan)
 {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= t.nnodes * 27) return;
     const int b = idx / 27, r = idx % 27;
-    tab[idx] = -1;
-    if (t.child[8 * b] >= 0) return;
-    const int L = t.level[b];
-    const long long E = (long long)GB_NXB << (t.maxlevel - L);
-    const long long N[3] = {(long long)t.nrx * GB_NXB << t.maxlevel, (long long)t.nry * GB_NXB << t.maxlevel,
-                            (long long)t.nrz * GB_NXB << t.maxlevel};
-    const int off[3] = {r % 3 - 1, (r / 3) % 3 - 1, r / 9 - 1};
-    long long X[3];
-    for (int d = 0; d < 3; ++d) X[d] = wrap((t.coord[3 * b + d] + off[d]) * E + E / 2, N[d]);
-    const int sh0 = LOG2_NXB + t.maxlevel;
-    int node = t.root[(int)(X[0] >> sh0) + t.nrx * ((int)(X[1] >> sh0) + t.nry * (int)(X[2] >> sh0))];
-    for (int l = 0; l < L && node >= 0; ++l) {
-        if (t.child[8 * node] < 0) break;
-        const int sh = sh0 - 1 - l;
-        node = t.child[8 * node + (int)((X[0] >> sh) & 1) + 2 * (int)((X[1] >> sh) & 1) + 4 * (int)((X[2] >> sh) & 1)];
+    int4 h = make_int4(-1, 0, 0, 0), c = make_int4(0, 0, 0, 0);
+    if (t.child[8 * b] < 0) {
+        const int L = t.level[b];
+        const int off[3] = {r % 3 - 1, (r / 3) % 3 - 1, r / 9 - 1};
+        const int nr[3] = {t.nrx, t.nry, t.nrz};
+        int P[3];  // the region's block coordinates at level L, periodic
+        for (int d = 0; d < 3; ++d) {
+            const int n = nr[d] << L;
+            P[d] = t.coord[3 * b + d] + off[d];
+            P[d] = P[d] < 0 ? P[d] + n : (P[d] >= n ? P[d] - n : P[d]);
+        }
+        int node = t.root[(P[0] >> L) + t.nrx * ((P[1] >> L) + t.nry * (P[2] >> L))];
+        for (int l = 0; l < L && node >= 0; ++l) {
+            if (t.child[8 * node] < 0) break;
+            const int sh = L - 1 - l;
+            node = t.child[8 * node + ((P[0] >> sh) & 1) + 2 * ((P[1] >> sh) & 1) + 4 * ((P[2] >> sh) & 1)];
+        }
+        if (r == 13) node = b;
+        if (node >= 0) {
+            int flags = 0;
+            if (t.child[8 * node] >= 0) {
+                flags = GP_REFINED | GP_LEAFKIDS;
+                for (int q = 0; q < 8; ++q) {
+                    const int ch = t.child[8 * node + q];
+                    if (ch < 0 || t.child[8 * ch] >= 0) flags &= ~GP_LEAFKIDS;
+                }
+            }
+            h = make_int4(node, t.level[node], flags, 0);
+            c = make_int4(t.coord[3 * node], t.coord[3 * node + 1], t.coord[3 * node + 2], 0);
+        }
     }
-    tab[idx] = node;
+    plan[2 * (size_t)idx] = h;
+    plan[2 * (size_t)idx + 1] = c;
 }
 
 __device__ __forceinline__ int region_of(int loc) { return loc < GB_NGUARD ? 0 : (loc >= GB_NGUARD + GB_NXB ? 2 : 1); }
 
-// The leaf covering finest-cell position X, lying in region r of block blk
-// (level L): from the region table's node when there is a table, from the
-// root otherwise.
-__device__ __forceinline__ leaf_hit leaf_near(const gb_tree_desc& t, const int* __restrict__ rtab, int blk, int r,
-                                              int L, long long X, long long Y, long long Z)
+// Periodic level-L index of the cell (or face) at padded index I of the
+// block at coordinate c of level L; M = cells of level L across the domain.
+// With the plan every position is such a 32-bit level-local index: the
+// finest-cell position of the walk from the root is (A + 1/2) 2^(maxlevel-L)
+// for a cell centre and A 2^(maxlevel-L) for a face, so every shift of the
+// walk becomes a shift of A.
+__device__ __forceinline__ int level_index(int c, int I, int M)
 {
-    if (!rtab) return find_leaf(t, X, Y, Z);
-    int node = __ldg(rtab + (size_t)blk * 27 + r);
-    for (int l = L; l <= t.maxlevel && node >= 0; ++l) {
-        if (__ldg(t.child + 8 * node) < 0) break;
-        const int sh = LOG2_NXB + t.maxlevel - 1 - l;
-        node = __ldg(t.child + 8 * node + ((int)((X >> sh) & 1) | ((int)((Y >> sh) & 1) << 1) | ((int)((Z >> sh) & 1) << 2)));
+    const int A = (c << LOG2_NXB) + I - GB_NGUARD;
+    return A < 0 ? A + M : (A >= M ? A - M : A);
+}
+
+struct plan_hit {
+    int node, level, c[3];
+};
+
+// The leaf covering level-L position A (a face position along axis fa when
+// fa >= 0, cell centres otherwise) from the plan entry {e, ec} of its region.
+__device__ __forceinline__ plan_hit plan_leaf(const gb_tree_desc& t, int4 e, int4 ec, int L, const int* A, int fa)
+{
+    plan_hit h;
+    h.node = e.x;
+    h.level = e.y;
+    h.c[0] = ec.x;
+    h.c[1] = ec.y;
+    h.c[2] = ec.z;
+    if (h.node < 0 || !(e.z & GP_REFINED)) return h;
+    for (int dl = 0; L + dl < t.maxlevel; ++dl) {
+        const int half = (1 << dl) >> 1;
+        int q = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) q |= ((((A[d] << dl) + (d == fa ? 0 : half)) >> 3) & 1) << d;
+        h.node = __ldg(t.child + 8 * h.node + q);
+        if (h.node < 0) return h;
+        h.level = __ldg(t.level + h.node);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) h.c[d] = __ldg(t.coord + 3 * h.node + d);
+        if ((dl == 0 && (e.z & GP_LEAFKIDS)) || __ldg(t.child + 8 * h.node) < 0) break;
     }
-    leaf_hit h;
-    h.node = node;
-    h.level = node >= 0 ? t.level[node] : 0;
     return h;
 }
+
+// The q-th guard position of an N0 x N1 x N2 padded array whose interior
+// spans [GB_NGUARD, GB_NGUARD + NI) on each axis (N - NI = 2 GB_NGUARD):
+// the two z slabs, the two y slabs inside them, the two x slabs inside
+// those. x runs fastest everywhere; in the x slabs the 8 guard columns of a
+// row are consecutive, so four neighbouring threads share a 32-byte sector.
+template <int N0, int N1, int NI0, int NI1, int NI2>
+struct guard_slabs {
+    static constexpr int G = 2 * GB_NGUARD;
+    static constexpr int NZ = G * N1 * N0, NY = NI2 * G * N0, NX = NI2 * NI1 * G;
+    static constexpr int COUNT = NZ + NY + NX;
+    __device__ __forceinline__ static void at(int q, int& i, int& j, int& k)
+    {
+        if (q < NZ) {
+            const int zz = q / (N1 * N0), rr = q - zz * (N1 * N0);
+            k = zz < GB_NGUARD ? zz : NI2 + zz;
+            j = rr / N0;
+            i = rr - j * N0;
+        } else if (q < NZ + NY) {
+            q -= NZ;
+            const int kk = q / (G * N0), rr = q - kk * (G * N0);
+            const int yy = rr / N0;
+            k = GB_NGUARD + kk;
+            j = yy < GB_NGUARD ? yy : NI1 + yy;
+            i = rr - yy * N0;
+        } else {
+            q -= NZ + NY;
+            const int xx = q % G, rr = q / G;
+            i = xx < GB_NGUARD ? xx : NI0 + xx;
+            j = GB_NGUARD + rr % NI1;
+            k = GB_NGUARD + rr / NI1;
+        }
+    }
+};
+using cell_slabs = guard_slabs<GB_N, GB_N, GB_NXB, GB_NXB, GB_NXB>;
+template <int AX>
+using face_slabs = guard_slabs<GB_N + (AX == 0), GB_N + (AX == 1), GB_NXB + (AX == 0), GB_NXB + (AX == 1),
+                               GB_NXB + (AX == 2)>;
+static_assert(face_slabs<0>::COUNT == face_slabs<1>::COUNT && face_slabs<1>::COUNT == face_slabs<2>::COUNT,
+              "guard faces per axis");
+constexpr int GB_NGF = face_slabs<0>::COUNT;
 
 // Face neighbours of every leaf: links[(b * 6 + f) * 5] = same (0), coarser
 // (1) or finer (2) neighbour across face f = 2 d + side, then the four fine
@@ -459,8 +544,10 @@ struct guard_vars {
     int slot[GB_NROLE];
 };
 
-__global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list, guard_vars gv,
-                              const int* __restrict__ rtab)
+// Without a plan (a capture that did not prepare one, or a domain too wide
+// for 32-bit level indices): 64-bit finest-cell positions and a walk from
+// the root per guard cell.
+__global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list, guard_vars gv)
 {
     const int blk = list[blockIdx.y];
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -480,7 +567,7 @@ __global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restri
         lo[d] = wrap(((long long)cd[d] * GB_NXB + loc[d] - GB_NGUARD) * s, N[d]);
         X[d] = lo[d] + (s >> 1);
     }
-    leaf_hit h = leaf_near(t, rtab, blk, region_of(i) + 3 * region_of(j) + 9 * region_of(k), L, X[0], X[1], X[2]);
+    leaf_hit h = find_leaf(t, X[0], X[1], X[2]);
     if (h.node < 0) return;
     const int lsl = t.maxlevel - h.level;
     const int* sc = t.coord + 3 * h.node;
@@ -525,7 +612,7 @@ __global__ void k_guard_cells(gb_dev_grid g, gb_tree_desc t, const int* __restri
     }
 }
 
-__global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list, const int* __restrict__ rtab)
+__global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list)
 {
     const int a = blockIdx.z;
     const int blk = list[blockIdx.y];
@@ -552,16 +639,14 @@ __global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restri
         lo[d] = wrap(((long long)cd[d] * GB_NXB + I[d] - GB_NGUARD) * s, N[d]);
         X[d] = lo[d] + (d == a ? 0 : (s >> 1));
     }
-    const int reg = region_of(I[0]) + 3 * region_of(I[1]) + 9 * region_of(I[2]);
-    leaf_hit h = leaf_near(t, rtab, blk, reg, L, X[0], X[1], X[2]);
+    leaf_hit h = find_leaf(t, X[0], X[1], X[2]);
     if (h.node < 0) return;
     if (h.level != L) {
         // a face on a level boundary: the copy owned by the leaf of this
         // block's level on the lower side, when there is one, so that every
         // block of a level reads the same face
-        const int reg2 = reg + (region_of(I[a] - 1) - region_of(I[a])) * (a == 0 ? 1 : a == 1 ? 3 : 9);
-        leaf_hit h2 = leaf_near(t, rtab, blk, reg2, L, a == 0 ? wrap(X[0] - 1, N[0]) : X[0],
-                                a == 1 ? wrap(X[1] - 1, N[1]) : X[1], a == 2 ? wrap(X[2] - 1, N[2]) : X[2]);
+        leaf_hit h2 = find_leaf(t, a == 0 ? wrap(X[0] - 1, N[0]) : X[0], a == 1 ? wrap(X[1] - 1, N[1]) : X[1],
+                                a == 2 ? wrap(X[2] - 1, N[2]) : X[2]);
         if (h2.node >= 0 && h2.level == L) {
             X[a] = wrap(X[a] - 1, N[a]) + 1;  // its upper face, unwrapped at the domain edge
             h = h2;
@@ -598,6 +683,149 @@ __global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restri
             }
         *dst = acc / (double)(r * r);
     }
+}
+
+// The same fills from the guard-fill plan: each guard cell reads two plan
+// entries (its block, its region), computes 32-bit level-local indices and
+// takes at most one step down the tree; the results are those of the walks
+// from the root above, value for value.
+__global__ void __launch_bounds__(128) k_guard_cells_plan(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list,
+                                                          guard_vars gv, const int4* __restrict__ plan)
+{
+    const int blk = list[blockIdx.y];
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= cell_slabs::COUNT) return;
+    int I[3];
+    cell_slabs::at(q, I[0], I[1], I[2]);
+    const int r = region_of(I[0]) + 3 * region_of(I[1]) + 9 * region_of(I[2]);
+    const int4* pb = plan + (size_t)blk * 54;
+    const int4 se = __ldg(pb + 26), sc = __ldg(pb + 27);  // region 13: the block itself
+    const int4 e = __ldg(pb + 2 * r), ec = __ldg(pb + 2 * r + 1);
+    const int L = se.y;
+    const int cs[3] = {sc.x, sc.y, sc.z}, nr[3] = {t.nrx, t.nry, t.nrz};
+    int A[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) A[d] = level_index(cs[d], I[d], nr[d] << (L + LOG2_NXB));
+    const plan_hit h = plan_leaf(t, e, ec, L, A, -1);
+    if (h.node < 0) return;
+    double* dst = g.unk + (int64_t)blk * g.nvar * GB_N3 + gb_cidx(I[0], I[1], I[2]);
+    const double* src = g.unk + (int64_t)h.node * g.nvar * GB_N3;
+    const int k = L - h.level;
+    double val[GB_NROLE];
+    if (k >= 0) {
+        // same level: copy; coarser: injection of the covering coarse cell
+        const int sci = gb_cidx((A[0] >> k) - (h.c[0] << LOG2_NXB) + GB_NGUARD,
+                                (A[1] >> k) - (h.c[1] << LOG2_NXB) + GB_NGUARD,
+                                (A[2] >> k) - (h.c[2] << LOG2_NXB) + GB_NGUARD);
+#pragma unroll
+        for (int q2 = 0; q2 < GB_NROLE; ++q2)
+            if (q2 < gv.n) val[q2] = src[(int64_t)gv.slot[q2] * GB_N3 + sci];
+    } else {
+        // finer neighbour: mean of the fine cells covering this cell
+        const int m = -k, rr = 1 << m;
+        const int bi = (A[0] << m) - (h.c[0] << LOG2_NXB) + GB_NGUARD;
+        const int bj = (A[1] << m) - (h.c[1] << LOG2_NXB) + GB_NGUARD;
+        const int bk = (A[2] << m) - (h.c[2] << LOG2_NXB) + GB_NGUARD;
+        const double inv = 1.0 / (double)(rr * rr * rr);
+#pragma unroll
+        for (int q2 = 0; q2 < GB_NROLE; ++q2) {
+            if (q2 >= gv.n) continue;
+            const double* sv = src + (int64_t)gv.slot[q2] * GB_N3;
+            double acc = 0.0;
+            for (int z = 0; z < rr; ++z)
+                for (int y = 0; y < rr; ++y)
+                    for (int x = 0; x < rr; ++x) acc += sv[gb_cidx(bi + x, bj + y, bk + z)];
+            val[q2] = acc * inv;
+        }
+    }
+#pragma unroll
+    for (int q2 = 0; q2 < GB_NROLE; ++q2)
+        if (q2 < gv.n) dst[(int64_t)gv.slot[q2] * GB_N3] = val[q2];
+}
+
+template <int AX>
+__device__ __forceinline__ void guard_face_plan(const gb_dev_grid& g, const gb_tree_desc& t, int blk, int q,
+                                                const int4* __restrict__ pb)
+{
+    int I[3];
+    face_slabs<AX>::at(q, I[0], I[1], I[2]);
+    const int r = region_of(I[0]) + 3 * region_of(I[1]) + 9 * region_of(I[2]);
+    const int4 se = __ldg(pb + 26), sc = __ldg(pb + 27);
+    const int4 e = __ldg(pb + 2 * r), ec = __ldg(pb + 2 * r + 1);
+    const int L = se.y;
+    const int cs[3] = {sc.x, sc.y, sc.z}, nr[3] = {t.nrx, t.nry, t.nrz};
+    int A[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) A[d] = level_index(cs[d], I[d], nr[d] << (L + LOG2_NXB));
+    plan_hit h = plan_leaf(t, e, ec, L, A, AX);
+    if (h.node < 0) return;
+    if (h.level != L) {
+        // a face on a level boundary: the copy owned by the leaf of this
+        // block's level on the lower side, when there is one, so that every
+        // block of a level reads the same face
+        constexpr int stride = AX == 0 ? 1 : (AX == 1 ? 3 : 9);
+        const int r2 = r + (region_of(I[AX] - 1) - region_of(I[AX])) * stride;
+        if (r2 != r) {
+            const int4 e2 = __ldg(pb + 2 * r2);
+            if (e2.x >= 0 && !(e2.z & GP_REFINED) && e2.y == L) {
+                const int4 ec2 = __ldg(pb + 2 * r2 + 1);
+                h.node = e2.x;
+                h.level = L;
+                h.c[0] = ec2.x;
+                h.c[1] = ec2.y;
+                h.c[2] = ec2.z;
+                const int M = nr[AX] << (L + LOG2_NXB);
+                A[AX] = (A[AX] == 0 ? M : A[AX]);  // its upper face, unwrapped at the domain edge
+            }
+        }
+    }
+    const double* src = g.f[AX] + (int64_t)h.node * GB_FSZ;
+    double* dst = g.f[AX] + (int64_t)blk * GB_FSZ + gb_fidx(AX, I[0], I[1], I[2]);
+    const int k = L - h.level;
+    if (k >= 0) {
+        int S[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) S[d] = (A[d] >> k) - (h.c[d] << LOG2_NXB) + GB_NGUARD;
+        if ((A[AX] & ((1 << k) - 1)) == 0) {
+            *dst = src[gb_fidx(AX, S[0], S[1], S[2])];
+        } else {
+            // fine face inside a coarse cell: mean of the two coarse faces
+            int S1[3] = {S[0], S[1], S[2]};
+            S1[AX] += 1;
+            *dst = 0.5 * (src[gb_fidx(AX, S[0], S[1], S[2])] + src[gb_fidx(AX, S1[0], S1[1], S1[2])]);
+        }
+    } else {
+        // finer neighbour: area mean of the fine faces on this face
+        const int m = -k, rr = 1 << m;
+        int B[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) B[d] = (A[d] << m) - (h.c[d] << LOG2_NXB) + GB_NGUARD;
+        constexpr int t1 = AX == 0 ? 1 : 0, t2 = AX == 2 ? 1 : 2;
+        double acc = 0.0;
+        for (int y = 0; y < rr; ++y)
+            for (int x = 0; x < rr; ++x) {
+                int Q[3] = {B[0], B[1], B[2]};
+                Q[t1] += x;
+                Q[t2] += y;
+                acc += src[gb_fidx(AX, Q[0], Q[1], Q[2])];
+            }
+        *dst = acc / (double)(rr * rr);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_guard_faces_plan(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list,
+                                                          const int4* __restrict__ plan)
+{
+    const int blk = list[blockIdx.y];
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= GB_NGF) return;
+    const int4* pb = plan + (size_t)blk * 54;
+    if (blockIdx.z == 0)
+        guard_face_plan<0>(g, t, blk, q, pb);
+    else if (blockIdx.z == 1)
+        guard_face_plan<1>(g, t, blk, q, pb);
+    else
+        guard_face_plan<2>(g, t, blk, q, pb);
 }
 
 __global__ void k_dt_init(unsigned long long* bits) { *bits = 0x7FF0000000000000ULL; }  // +inf
@@ -786,37 +1014,69 @@ extern "C" int gb_set_flux_correction(int on)
     return GB_OK;
 }
 
-// The guard fill's region table (trees with more than one level; before
-// any capture: it allocates once per registration).
+// Whether the plan's 32-bit level-local indices hold the tree: every
+// position of the finest level, shifted once more, below 2^30.
+static bool plan_fits(const gb_tree_desc& t)
+{
+    const long long n = (long long)std::max(t.nrx, std::max(t.nry, t.nrz)) << (LOG2_NXB + t.maxlevel);
+    return n < (1LL << 29);
+}
+
+// The guard-fill plan of the registered tree (before any capture: it
+// allocates once per registration).
 int gb_guard_prepare(cudaStream_t s)
 {
-    if (!g_gb.tree_ok || g_gb.tree.maxlevel <= 0 || g_gb.rtab_ok) return GB_OK;
+    if (!g_gb.tree_ok || g_gb.plan_ok || !plan_fits(g_gb.tree)) return GB_OK;
     const int nn = g_gb.tree.nnodes;
-    if (g_gb.rtab_n < nn) {
-        if (g_gb.d_rtab) cudaFree(g_gb.d_rtab);
-        g_gb.d_rtab = nullptr;
-        g_gb.rtab_n = 0;
-        if (gb_check(cudaMalloc(&g_gb.d_rtab, (size_t)nn * 27 * sizeof(int)), "cudaMalloc(region table)"))
+    if (g_gb.plan_n < nn) {
+        if (g_gb.d_plan) cudaFree(g_gb.d_plan);
+        g_gb.d_plan = nullptr;
+        g_gb.plan_n = 0;
+        if (gb_check(cudaMalloc(&g_gb.d_plan, (size_t)nn * 54 * sizeof(int4)), "cudaMalloc(guard plan)"))
             return GB_ERR_CUDA;
-        g_gb.rtab_n = nn;
+        g_gb.plan_n = nn;
     }
-    k_region_table<<<(nn * 27 + 255) / 256, 256, 0, s>>>(g_gb.tree, g_gb.d_rtab);
-    if (gb_check(cudaGetLastError(), "k_region_table")) return GB_ERR_CUDA;
-    g_gb.rtab_ok = true;
+    k_guard_plan<<<(nn * 27 + 255) / 256, 256, 0, s>>>(g_gb.tree, (int4*)g_gb.d_plan);
+    if (gb_check(cudaGetLastError(), "k_guard_plan")) return GB_ERR_CUDA;
+    g_gb.plan_ok = true;
     return GB_OK;
 }
 
-// the table when it is ready; inside a capture that did not prepare it
+// the plan when it is ready; inside a capture that did not prepare it
 // (nothing allocates there) the kernels walk from the root instead
-static const int* guard_table(cudaStream_t s)
+static const int4* guard_plan(cudaStream_t s)
 {
-    if (!g_gb.tree_ok || g_gb.tree.maxlevel <= 0) return nullptr;
-    if (!g_gb.rtab_ok) {
+    if (!g_gb.tree_ok) return nullptr;
+    if (!g_gb.plan_ok) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         cudaStreamIsCapturing(s, &cs);
-        if (cs != cudaStreamCaptureStatusNone || gb_guard_prepare(s) != GB_OK) return nullptr;
+        if (cs != cudaStreamCaptureStatusNone || gb_guard_prepare(s) != GB_OK || !g_gb.plan_ok) return nullptr;
     }
-    return g_gb.d_rtab;
+    return (const int4*)g_gb.d_plan;
+}
+
+static guard_vars hydro_guard_vars();
+
+// guard cells and (when face fields exist) guard faces of the listed blocks
+static void launch_guard_kernels(int nblk, const int* list, bool faces, cudaStream_t s)
+{
+    const int4* plan = guard_plan(s);
+    gb_prof_begin(GBP_GUARD, s);
+    if (plan) {
+        k_guard_cells_plan<<<dim3((cell_slabs::COUNT + 127) / 128, nblk), 128, 0, s>>>(g_gb.grid, g_gb.tree, list,
+                                                                                      hydro_guard_vars(), plan);
+    } else {
+        k_guard_cells<<<dim3((GB_NGC + 127) / 128, nblk), 128, 0, s>>>(g_gb.grid, g_gb.tree, list,
+                                                                        hydro_guard_vars());
+    }
+    gb_prof_end(GBP_GUARD, s);
+    if (!faces) return;
+    gb_prof_begin(GBP_GUARD, s);
+    if (plan)
+        k_guard_faces_plan<<<dim3((GB_NGF + 127) / 128, nblk, 3), 128, 0, s>>>(g_gb.grid, g_gb.tree, list, plan);
+    else
+        k_guard_faces<<<dim3((GB_FSZ + 127) / 128, nblk, 3), 128, 0, s>>>(g_gb.grid, g_gb.tree, list);
+    gb_prof_end(GBP_GUARD, s);
 }
 
 static guard_vars hydro_guard_vars()
@@ -831,17 +1091,7 @@ static guard_vars hydro_guard_vars()
 
 int gb_launch_guardfill(int nblk, const int* list, cudaStream_t s)
 {
-    dim3 gc((GB_NGC + 127) / 128, nblk);
-    gb_prof_begin(GBP_GUARD, s);
-    const int* rtab = guard_table(s);
-    k_guard_cells<<<gc, 128, 0, s>>>(g_gb.grid, g_gb.tree, list, hydro_guard_vars(), rtab);
-    gb_prof_end(GBP_GUARD, s);
-    if (g_gb.hp.mhd && g_gb.grid.f[0]) {
-        dim3 gf((GB_FSZ + 127) / 128, nblk, 3);
-        gb_prof_begin(GBP_GUARD, s);
-        k_guard_faces<<<gf, 128, 0, s>>>(g_gb.grid, g_gb.tree, list, rtab);
-        gb_prof_end(GBP_GUARD, s);
-    }
+    launch_guard_kernels(nblk, list, g_gb.hp.mhd && g_gb.grid.f[0], s);
     return gb_check(cudaGetLastError(), "guard fill") ? GB_ERR_CUDA : GB_OK;
 }
 
@@ -853,15 +1103,9 @@ extern "C" int gb_fill_guardcells(int blockCount, const int* list, void* stream)
     }
     if (blockCount < 0 || (blockCount > 0 && !list)) return GB_ERR_ARG;
     if (blockCount == 0) return GB_OK;
-    // the face pass needs to know whether face fields exist; it is keyed on
-    // the hydro parameters when set and on the grid otherwise
-    dim3 gc((GB_NGC + 127) / 128, blockCount);
-    const int* rtab = guard_table((cudaStream_t)stream);
-    k_guard_cells<<<gc, 128, 0, (cudaStream_t)stream>>>(g_gb.grid, g_gb.tree, list, hydro_guard_vars(), rtab);
-    if (g_gb.grid.f[0] && g_gb.grid.f[1] && g_gb.grid.f[2]) {
-        dim3 gf((GB_FSZ + 127) / 128, blockCount, 3);
-        k_guard_faces<<<gf, 128, 0, (cudaStream_t)stream>>>(g_gb.grid, g_gb.tree, list, rtab);
-    }
+    // the face pass runs whenever the grid has face fields
+    launch_guard_kernels(blockCount, list, g_gb.grid.f[0] && g_gb.grid.f[1] && g_gb.grid.f[2],
+                         (cudaStream_t)stream);
     return gb_check(cudaGetLastError(), "guard fill") ? GB_ERR_CUDA : GB_OK;
 }
 

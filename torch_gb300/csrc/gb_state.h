@@ -34,10 +34,11 @@ struct gb_state_t {
     size_t fcreg_bytes = 0;
     int* d_fclist = nullptr;
     int fclist_cap = 0;
-    // guard fill: the node covering each of the 27 regions around a leaf
-    int* d_rtab = nullptr;
-    int rtab_n = 0;
-    bool rtab_ok = false;
+    // guard-fill plan: the node covering each of the 27 regions around a
+    // leaf (two int4 per entry)
+    void* d_plan = nullptr;
+    int plan_n = 0;
+    bool plan_ok = false;
     // bumped by every call that changes what a captured step graph baked
     // in (grid, tree, parameters, tables, weights, modes)
     unsigned long long gen = 0;
