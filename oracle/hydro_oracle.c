@@ -703,6 +703,88 @@ static void flux_fix(const orc_fluxfix* fx, face_flux* const* fl, int n, int lo,
     (void)reg_slots_note;
 }
 
+static int ring_index(int A, int B) { return B == 0 ? A : (B == 16 ? 17 + A : (A == 0 ? 33 + B : 48 + B)); }
+
+static void ring_edge(int q, int* A, int* B)
+{
+    if (q < 17) { *A = q; *B = 0; }
+    else if (q < 34) { *A = q - 17; *B = 16; }
+    else if (q < 49) { *A = 0; *B = q - 33; }
+    else { *A = 16; *B = q - 48; }
+}
+
+static int orc_leaf_at(const int* level, const int* child, const int* root, int nr0, int nr1, int maxlevel,
+                       long long X, long long Y, long long Z);
+static long long orc_wrap(long long x, long long n);
+
+/* Edge electric fields at fine-coarse boundaries: store this block's
+ * surface edges, then replace each surface edge that a leaf one level finer
+ * also carries by the mean of its two fine edges. The surrounding cells of
+ * an edge outside the block are tried in a fixed order ((A-1, B-1), (A,
+ * B-1), (A-1, B), (A, B) in (a, b)); the first that lies in a leaf of level
+ * L + 1 gives the fine edges (every such leaf carries the same values).
+ * EE(c, i, j, k) addresses the block's edge fields, lo its first interior
+ * index. */
+static void edge_fix(const orc_fluxfix* fx, double* const* emf, int n, int lo)
+{
+#define EEF(c, i, j, k) emf[c][(i) + (int64_t)(n + 1) * ((j) + (int64_t)(n + 1) * (k))]
+    const int b = fx->b, L = fx->level[b];
+    double* mine = fx->ereg + (size_t)b * ORC_NSURF;
+    for (int c = 0; c < 3; ++c)
+        for (int C = 0; C < 16; ++C)
+            for (int q = 0; q < ORC_NRING; ++q) {
+                int A, B, I[3];
+                ring_edge(q, &A, &B);
+                I[(c + 1) % 3] = lo + A;
+                I[(c + 2) % 3] = lo + B;
+                I[c] = lo + C;
+                mine[((size_t)c * 16 + C) * ORC_NRING + q] = EEF(c, I[0], I[1], I[2]);
+            }
+    const long long S = 1LL << (fx->maxlevel - L); /* level-L cell in finest cells */
+    for (int c = 0; c < 3; ++c) {
+        const int a = (c + 1) % 3, bb = (c + 2) % 3;
+        for (int C = 0; C < 16; ++C)
+            for (int q = 0; q < ORC_NRING; ++q) {
+                int A, B;
+                ring_edge(q, &A, &B);
+                for (int cand = 0; cand < 4; ++cand) {
+                    const int ia = cand & 1, ib = cand >> 1;
+                    const int cell[2] = {A - 1 + ia, B - 1 + ib};
+                    if (cell[0] >= 0 && cell[0] < 16 && cell[1] >= 0 && cell[1] < 16) continue;
+                    /* centre of the outside cell, finest units, periodic */
+                    int ci[3];
+                    ci[a] = cell[0];
+                    ci[bb] = cell[1];
+                    ci[c] = C;
+                    long long X[3], g[3];
+                    for (int d = 0; d < 3; ++d) {
+                        const long long M = (long long)fx->nr[d] * 16 << L; /* level-L cells across */
+                        g[d] = orc_wrap((long long)fx->coord[3 * b + d] * 16 + ci[d], M);
+                        X[d] = g[d] * S + S / 2;
+                    }
+                    const int F = orc_leaf_at(fx->level, fx->child, fx->root, fx->nr[0], fx->nr[1], fx->maxlevel,
+                                              X[0], X[1], X[2]);
+                    if (F < 0 || F >= fx->nnodes || fx->level[F] != L + 1) continue;
+                    /* the fine cells of the outside coarse cell start at
+                     * 2 g - 16 coord_F; the edge is on the upper side of
+                     * the coarse cell when ia (ib) = 0 */
+                    const int Af = (int)(2 * g[a] - 16LL * fx->coord[3 * F + a]) + (ia ? 0 : 2);
+                    const int Bf = (int)(2 * g[bb] - 16LL * fx->coord[3 * F + bb]) + (ib ? 0 : 2);
+                    const int Cf = (int)(2 * g[c] - 16LL * fx->coord[3 * F + c]);
+                    const double* r = fx->ereg + (size_t)F * ORC_NSURF + ((size_t)c * 16 + Cf) * ORC_NRING +
+                                      ring_index(Af, Bf);
+                    int I[3];
+                    I[a] = lo + A;
+                    I[bb] = lo + B;
+                    I[c] = lo + C;
+                    EEF(c, I[0], I[1], I[2]) = 0.5 * (r[0] + r[ORC_NRING]);
+                    break;
+                }
+            }
+    }
+#undef EEF
+}
+
 static int unsplit_block(const orc_hydro_params* p, double* u, double* bxf, double* byf, double* bzf,
                          double dt, double dx, double dy, double dz, const orc_fluxfix* fx);
 
@@ -848,6 +930,8 @@ static int unsplit_block(const orc_hydro_params* p, double* u, double* bxf, doub
     /* flux conservation at fine-coarse faces (after the electric fields,
      * which use the block's own fluxes) */
     if (fx) flux_fix(fx, fl, n, lo, nxb);
+    /* edge electric fields at fine-coarse boundaries */
+    if (fx && fx->ereg && p->mhd) edge_fix(fx, emf, n, lo);
 
     /* conservative update of the interior cells */
     double* unew = (double*)malloc(sizeof(double) * (size_t)(ORV_NVAR * n3));

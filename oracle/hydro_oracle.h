@@ -61,7 +61,24 @@ typedef struct orc_fluxfix {
     int type[6];
     double* store[6];
     const double* fine[6][4];
+    /* Edge electric fields at fine-coarse boundaries (MHD; ereg NULL: off).
+     * ereg holds ORC_NSURF surface-edge fields per tree node; block b
+     * stores its own and replaces each surface edge that a leaf one level
+     * finer also carries (across a face, an edge or a corner) by the mean
+     * of the two fine edges along it. The tree locates those leaves. */
+    double* ereg;
+    int b, nnodes;
+    const int *level, *coord, *child, *root;
+    int nr[3], maxlevel;
 } orc_fluxfix;
+
+/* Surface edges of a 16^3 block: per edge direction c, the 64 node
+ * positions (A, B) on the ring of the 17 x 17 node grid across c (A along
+ * (c + 1) % 3, B along (c + 2) % 3, A or B in {0, 16}; ring index A for
+ * B = 0, 17 + A for B = 16, 33 + B for A = 0, 48 + B for A = 16) times the
+ * 16 cells along c: index (c * 16 + C) * 64 + ring. */
+#define ORC_NRING 64
+#define ORC_NSURF (3 * 16 * ORC_NRING)
 
 int orc_unsplit_block_fc(const orc_hydro_params* p, double* u, double* bx, double* by, double* bz,
                          double dt, double dx, double dy, double dz, const orc_fluxfix* fx);

@@ -144,7 +144,9 @@ long orc_unsplit_tree(const orc_hydro_params* p, int nlist, const int* list, con
         if (list[q] + 1 > nnodes) nnodes = list[q] + 1;
     const size_t per_face = (size_t)p->nxb * p->nxb * ORC_NREG;
     double* reg = NULL;
+    double* ereg = NULL;
     if (flux_correct && maxlevel > 0) reg = (double*)calloc((size_t)nnodes * 6 * per_face, sizeof(double));
+    if (reg && p->mhd) ereg = (double*)calloc((size_t)nnodes * ORC_NSURF, sizeof(double));
     long total = 0;
     for (int L = maxlevel; L >= 0; --L) {
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
@@ -161,6 +163,17 @@ long orc_unsplit_tree(const orc_hydro_params* p, int nlist, const int* list, con
                 continue;
             }
             orc_fluxfix ff;
+            ff.ereg = ereg;
+            ff.b = b;
+            ff.nnodes = nnodes;
+            ff.level = level;
+            ff.coord = coord;
+            ff.child = child;
+            ff.root = root;
+            ff.nr[0] = nr0;
+            ff.nr[1] = nr1;
+            ff.nr[2] = nr2;
+            ff.maxlevel = maxlevel;
             int fine[24];
             orc_face_links(b, level, coord, child, root, nr0, nr1, nr2, maxlevel, ff.type, fine);
             for (int f = 0; f < 6; ++f) {
@@ -175,5 +188,6 @@ long orc_unsplit_tree(const orc_hydro_params* p, int nlist, const int* list, con
         }
     }
     free(reg);
+    free(ereg);
     return total;
 }

@@ -133,3 +133,63 @@ def test_flux_correction_conserves_across_levels(oracle, mhd):
         res[fc] = np.abs(after - before) / scale
     assert np.all(res[True] < 1e-14), res[True]
     assert res[False][0] > 1e-7
+
+
+def _face_deltas_matched(t, tl, oracle, before, after):
+    """max |dB(coarse face cell) - mean dB(its 2 x 2 fine face cells)| over
+    every fine-coarse face of the tree, and max |dB| for scale."""
+    worst, scale = 0.0, 0.0
+    for b in t["leaf"]:
+        types, fine = oracle.face_links(tl, b)
+        for f in range(6):
+            if types[f] != 2:
+                continue
+            d, side = f >> 1, f & 1
+            t1, t2 = (1, 2) if d == 0 else ((0, 2) if d == 1 else (0, 1))
+
+            def face(arrs, blk, I):
+                return arrs[d][blk, I[2], I[1], I[0]]
+
+            for c2 in range(16):
+                for c1 in range(16):
+                    m = fine[f][(c1 >= 8) + 2 * (c2 >= 8)]
+                    I = [0, 0, 0]
+                    I[d] = 20 if side else 4
+                    I[t1], I[t2] = 4 + c1, 4 + c2
+                    dc = face(after, b, I) - face(before, b, I)
+                    g1, g2 = 2 * (c1 % 8), 2 * (c2 % 8)
+                    df = 0.0
+                    for e2 in range(2):
+                        for e1 in range(2):
+                            J = [0, 0, 0]
+                            J[d] = 4 if side else 20
+                            J[t1], J[t2] = 4 + g1 + e1, 4 + g2 + e2
+                            df += face(after, m, J) - face(before, m, J)
+                    worst = max(worst, abs(dc - 0.25 * df))
+                    scale = max(scale, abs(dc))
+    return worst, scale
+
+
+def test_edge_fields_keep_fine_coarse_faces_matched(oracle):
+    """CT at fine-coarse boundaries: with the fine edge fields restricted to
+    the coarse edges, the change of every coarse face on a fine-coarse face
+    equals the mean change of the four fine faces on it (the magnetic flux
+    through the interface changes by the same amount on both sides);
+    without the registers the two sides drift apart."""
+    from torch_gb300 import amr
+    t, c = amr.small_tree()
+    st = amr.amr_box(t, c, seed=5, mach=1.0, device="cpu")
+    p = oracle.hydro_params(True)
+    tl = oracle.TreeLists(t)
+    res = {}
+    for fc in (True, False):
+        u = st["u"][:, :10].numpy().copy()
+        fx, fy, fz = (st[k].numpy().copy() for k in ("fx", "fy", "fz"))
+        oracle.fill_guards_tree(p, t, u, fx, fy, fz)
+        before = [a.copy() for a in (fx, fy, fz)]
+        dt = 0.8 * oracle.dt_limit_list(p, tl, t["leaf"], u, st["root_dx"])
+        oracle.unsplit_tree(p, tl, t["leaf"], u, fx, fy, fz, dt, st["root_dx"], flux_correct=fc)
+        res[fc] = _face_deltas_matched(t, tl, oracle, before, (fx, fy, fz))
+    worst, scale = res[True]
+    assert scale > 0 and worst <= 1e-13 * scale, res[True]
+    assert res[False][0] > 1e-6 * res[False][1], res[False]

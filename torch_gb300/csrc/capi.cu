@@ -314,8 +314,6 @@ __device__ __forceinline__ long long wrap(long long x, long long n) { return x <
 // whose children cover the region. Two int4 per entry:
 // {node, level, flags, 0} and {cx, cy, cz, 0}. A guard cell then reads its
 // block's entry and its region's entry and takes at most one step down.
-constexpr int GP_REFINED = 1;   // a node of b's level with children
-constexpr int GP_LEAFKIDS = 2;  // ... whose children are all leaves
 
 __global__ void k_guard_plan(gb_tree_desc t, int4* __restrict__ plan)
 {
@@ -989,6 +987,19 @@ static int fc_prepare(int nblk, cudaStream_t s, bool* active)
         if (gb_check(cudaMalloc(&g_gb.d_fcreg, reg), "cudaMalloc(flux registers)")) return GB_ERR_CUDA;
         g_gb.fcreg_bytes = reg;
     }
+    if (g_gb.hp.mhd) {
+        const size_t ereg = (size_t)nn * gbh::NSURF * sizeof(double);
+        if (g_gb.ereg_bytes < ereg) {
+            if (g_gb.d_ereg) cudaFree(g_gb.d_ereg);
+            g_gb.d_ereg = nullptr;
+            g_gb.ereg_bytes = 0;
+            if (gb_check(cudaMalloc(&g_gb.d_ereg, ereg), "cudaMalloc(edge registers)")) return GB_ERR_CUDA;
+            g_gb.ereg_bytes = ereg;
+        }
+        // the edge matching finds the finer leaves through the guard-fill plan
+        int rc = gb_guard_prepare(s);
+        if (rc) return rc;
+    }
     if (g_gb.fclist_cap < nblk) {
         if (g_gb.d_fclist) cudaFree(g_gb.d_fclist);
         g_gb.d_fclist = nullptr;
@@ -1268,6 +1279,11 @@ int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int
         list = g_gb.d_fclist;
         kp.fc_links = g_gb.d_links;
         kp.fc_reg = g_gb.d_fcreg;
+        if (g_gb.hp.mhd && g_gb.plan_ok && g_gb.d_ereg) {
+            kp.ec_plan = (const int4*)g_gb.d_plan;
+            kp.ec_child = g_gb.tree.child;
+            kp.ec_reg = g_gb.d_ereg;
+        }
     }
     if (ns > 1) {
         cudaEventRecord(g_aux.fork, s);

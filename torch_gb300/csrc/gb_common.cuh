@@ -10,6 +10,12 @@
 #define GB_N3 (GB_NB * GB_NB * GB_NB)
 #define GB_FSZ (GB_NB * GB_NB * (GB_NB + 1))
 
+// Guard-fill plan entry flags (the plan: for every leaf and each of the 27
+// block-sized regions around it, two int4 {node, level, flags, 0},
+// {cx, cy, cz, 0}; region r = rx + 3 ry + 9 rz, offsets -1..1 per axis)
+constexpr int GP_REFINED = 1;   // a node of the leaf's level with children
+constexpr int GP_LEAFKIDS = 2;  // ... whose children are all leaves
+
 // Record the first failure in the status word and count it.
 __device__ __forceinline__ void gb_fail(gb_status* st, int code, int blk, int i, int j, int k,
                                         double v)

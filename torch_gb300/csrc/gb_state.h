@@ -34,6 +34,9 @@ struct gb_state_t {
     size_t fcreg_bytes = 0;
     int* d_fclist = nullptr;
     int fclist_cap = 0;
+    // surface-edge electric-field registers (MHD): NSURF doubles per node
+    double* d_ereg = nullptr;
+    size_t ereg_bytes = 0;
     // guard-fill plan: the node covering each of the 27 regions around a
     // leaf (two int4 per entry)
     void* d_plan = nullptr;

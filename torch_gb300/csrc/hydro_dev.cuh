@@ -367,6 +367,12 @@ struct hydro_kparams {
     double inv_gm1;  // 1 / (gamma - 1), for the mixed path's update
     float dtdxf0[3];
     const float* dtdxfp;
+    // edge electric fields at fine-coarse boundaries (MHD with flux
+    // conservation; null: off): the guard-fill plan, the tree's child
+    // table and the surface-edge registers (NSURF doubles per tree node)
+    const int4* ec_plan = nullptr;
+    const int* ec_child = nullptr;
+    double* ec_reg = nullptr;
 };
 
 __device__ __forceinline__ double kp_dt(const hydro_kparams& kp) { return kp.dtp ? *kp.dtp : kp.dt; }
@@ -1025,6 +1031,96 @@ k_faceb(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const dou
     if (blockIdx.y == 0) faceb_face<0>(g, kp, list, escr, estride, bscr, bstride);
     else if (blockIdx.y == 1) faceb_face<1>(g, kp, list, escr, estride, bscr, bstride);
     else faceb_face<2>(g, kp, list, escr, estride, bscr, bstride);
+}
+
+// ---------------------------------------------------------------- edge fields at fine-coarse boundaries
+// The CT counterpart of the flux registers. Every leaf stores the electric
+// fields of its surface edges; a leaf replaces each of its surface edges
+// that a leaf one level finer also carries (across a face, an edge or a
+// corner) by the mean of the two fine edges along it. The coarse face-B
+// update on a fine-coarse face is then the mean of the four fine ones, and
+// every coarse block around such an edge takes the same value. Surface
+// edges of direction c: node positions (A, B) on the ring of the 17 x 17
+// node grid across c (A along (c + 1) % 3, B along (c + 2) % 3, A or B in
+// {0, 16}) times the 16 cells along c; register index (c 16 + C) 64 + ring.
+constexpr int NRING = 64;
+constexpr int NSURF = 3 * GB_NXB * NRING;
+
+__device__ __forceinline__ int edge_ring(int A, int B)
+{
+    return B == 0 ? A : (B == GB_NXB ? 17 + A : (A == 0 ? 33 + B : 48 + B));
+}
+
+__device__ __forceinline__ void ring_edge(int q, int& A, int& B)
+{
+    if (q < 17) { A = q; B = 0; }
+    else if (q < 34) { A = q - 17; B = GB_NXB; }
+    else if (q < 49) { A = 0; B = q - 33; }
+    else { A = GB_NXB; B = q - 48; }
+}
+
+static __global__ void __launch_bounds__(128)
+k_emf_put(const int* __restrict__ list, const double* __restrict__ escr, size_t estride, double* __restrict__ ereg)
+{
+    const int cb = blockIdx.y, t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= NSURF) return;
+    const int blk = list[cb];
+    const int c = t / (GB_NXB * NRING), C = (t / NRING) % GB_NXB;
+    int A, B;
+    ring_edge(t % NRING, A, B);
+    ereg[(size_t)blk * NSURF + t] = escr[(size_t)cb * estride + (size_t)c * NEDGE + A + 17 * (B + 17 * C)];
+}
+
+// The surrounding cells of a surface edge outside the block are tried in a
+// fixed order ((A-1, B-1), (A, B-1), (A-1, B), (A, B)); the first lying in
+// a leaf one level finer (its region's plan node is refined, the child
+// holding the cell is a leaf) gives the fine edges (every such leaf carries
+// the same values).
+template <int CD>
+__device__ __forceinline__ void emf_get_dir(const int4* __restrict__ pb, const int* __restrict__ child,
+                                            const double* __restrict__ ereg, double* __restrict__ es, int C, int q)
+{
+    constexpr int a = (CD + 1) % 3, b = (CD + 2) % 3;
+    int A, B;
+    ring_edge(q, A, B);
+#pragma unroll
+    for (int cand = 0; cand < 4; ++cand) {
+        const int ia = cand & 1, ib = cand >> 1;
+        const int ca = A - 1 + ia, cbb = B - 1 + ib;
+        const int ra = ca < 0 ? -1 : (ca >= GB_NXB ? 1 : 0), rb = cbb < 0 ? -1 : (cbb >= GB_NXB ? 1 : 0);
+        if (ra == 0 && rb == 0) continue;
+        const int r = (a == 0 ? ra + 1 : b == 0 ? rb + 1 : 1) + 3 * (a == 1 ? ra + 1 : b == 1 ? rb + 1 : 1) +
+                      9 * (a == 2 ? ra + 1 : b == 2 ? rb + 1 : 1);
+        const int4 e = __ldg(pb + 2 * r);
+        if (e.x < 0 || !(e.z & GP_REFINED)) continue;
+        const int la = ca - GB_NXB * ra, lb = cbb - GB_NXB * rb;
+        const int ba = la >= GB_NXB / 2, bbit = lb >= GB_NXB / 2, bc = C >= GB_NXB / 2;
+        const int q8 = (a == 0 ? ba : b == 0 ? bbit : bc) | ((a == 1 ? ba : b == 1 ? bbit : bc) << 1) |
+                       ((a == 2 ? ba : b == 2 ? bbit : bc) << 2);
+        const int F = __ldg(child + 8 * e.x + q8);
+        if (F < 0) continue;
+        if (!(e.z & GP_LEAFKIDS) && __ldg(child + 8 * F) >= 0) continue;
+        const int Af = 2 * la + (ia ? 0 : 2) - GB_NXB * ba, Bf = 2 * lb + (ib ? 0 : 2) - GB_NXB * bbit;
+        const int Cf = 2 * C - GB_NXB * bc;
+        const double* rf = ereg + (size_t)F * NSURF + ((size_t)CD * GB_NXB + Cf) * NRING + edge_ring(Af, Bf);
+        es[(size_t)CD * NEDGE + A + 17 * (B + 17 * C)] = 0.5 * (rf[0] + rf[NRING]);
+        return;
+    }
+}
+
+static __global__ void __launch_bounds__(128)
+k_emf_get(const int* __restrict__ list, const int4* __restrict__ plan, const int* __restrict__ child,
+          const double* __restrict__ ereg, double* __restrict__ escr, size_t estride)
+{
+    const int cb = blockIdx.z, t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= GB_NXB * NRING) return;
+    const int blk = list[cb];
+    const int4* pb = plan + (size_t)blk * 54;
+    double* es = escr + (size_t)cb * estride;
+    const int C = t / NRING, q = t % NRING;
+    if (blockIdx.y == 0) emf_get_dir<0>(pb, child, ereg, es, C, q);
+    else if (blockIdx.y == 1) emf_get_dir<1>(pb, child, ereg, es, C, q);
+    else emf_get_dir<2>(pb, child, ereg, es, C, q);
 }
 
 // ---------------------------------------------------------------- flux conservation

@@ -31,17 +31,15 @@ void launch_recon(int tile, dim3 rg, cudaStream_t s, const gb_dev_grid& g, const
 }
 
 // fine-side boundary fluxes into the flux registers (as soon as the fluxes
-// exist); ev_put, when given, marks their completion for a chunk on
-// another stream
+// exist)
 template <typename T>
-void put_fluxes(const hydro_kparams& kp, int nblk, const int* list, T* fscr, cudaStream_t s, cudaEvent_t ev_put)
+void put_fluxes(const hydro_kparams& kp, int nblk, const int* list, T* fscr, cudaStream_t s)
 {
     using SL = scratch_layout<T>;
     if (kp.fc_links) {
         dim3 rg2(1, 6, nblk);
         k_fc_put<T><<<rg2, GB_NXB * GB_NXB, 0, s>>>(list, kp.fc_links, (T*)kp.fc_reg, fscr, SL::flux);
     }
-    if (ev_put) cudaEventRecord(ev_put, s);
 }
 
 template <typename T>
@@ -74,11 +72,21 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
         gb_prof_begin(GBP_FLUX, s);
         k_flux<T, true><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);
         gb_prof_end(GBP_FLUX, s);
-        put_fluxes<T>(kp, nblk, list, fscr, s, ev_put);
+        put_fluxes<T>(kp, nblk, list, fscr, s);
         dim3 eg((NEDGE + 127) / 128, 3, nblk);
         gb_prof_begin(GBP_EMF, s);
         k_emf<T><<<eg, 128, 0, s>>>(g, list, fscr, SL::flux, escr, SL::emf, p32, SL::prim32);
+        if (kp.ec_reg) k_emf_put<<<dim3((NSURF + 127) / 128, nblk), 128, 0, s>>>(list, escr, SL::emf, kp.ec_reg);
         gb_prof_end(GBP_EMF, s);
+        // the registers this chunk wrote are complete (a chunk on another
+        // stream may read them now)
+        if (ev_put) cudaEventRecord(ev_put, s);
+        if (kp.ec_reg) {
+            gb_prof_begin(GBP_EMF, s);
+            k_emf_get<<<dim3((GB_NXB * NRING + 127) / 128, 3, nblk), 128, 0, s>>>(list, kp.ec_plan, kp.ec_child,
+                                                                                  kp.ec_reg, escr, SL::emf);
+            gb_prof_end(GBP_EMF, s);
+        }
         dim3 bg((NFB + 127) / 128, 3, nblk);
         gb_prof_begin(GBP_FACEB, s);
         k_faceb<<<bg, 128, 0, s>>>(g, kp, list, escr, SL::emf, bscr, SL::fb);
@@ -90,7 +98,8 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
         gb_prof_begin(GBP_FLUX, s);
         k_flux<T, false><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);
         gb_prof_end(GBP_FLUX, s);
-        put_fluxes<T>(kp, nblk, list, fscr, s, ev_put);
+        put_fluxes<T>(kp, nblk, list, fscr, s);
+        if (ev_put) cudaEventRecord(ev_put, s);
     }
     if (kp.fc_links) {
         // after the edge fields, which use the block's own fluxes
