@@ -90,7 +90,7 @@ template <typename T>
 __device__ __forceinline__ T face_b(const gb_dev_grid& g, int a, int blk, int fi, const float* p32b)
 {
     if constexpr (std::is_same<T, float>::value) return p32b[(size_t)NP32 * GB_N3 + (size_t)a * GB_FSZ + fi];
-    else return g.f[a][(int64_t)blk * GB_FSZ + fi];
+    else return (a == 0 ? g.f[0] : (a == 1 ? g.f[1] : g.f[2]))[(int64_t)blk * GB_FSZ + fi];  // no run-time index into the parameters
 }
 
 template <typename T>
@@ -441,105 +441,163 @@ __device__ __forceinline__ void load_prim(const gb_dev_grid& g, int blk, int ci,
 // ---------------------------------------------------------------- k_recon
 // blockDim = 3 * TILE: threads [d TILE, (d + 1) TILE) reconstruct direction d
 // for TILE cells (TILE a multiple of 32, so every warp has one direction).
-// The work of a direction is written with the direction as a template
-// parameter, so every register array is indexed by constants; the block
-// barrier between the normal and the transverse part sits in the kernel.
+// All three directions run the same instructions: a thread works in its
+// direction's rotated frame (normal velocity and field first), rotating by
+// where it loads and stores rather than by moving registers, so register
+// arrays keep constant indices and the kernel holds one copy of the PPM and
+// eigensystem code (three copies, one per direction, overflowed the
+// instruction cache). The block barrier between the normal and the
+// transverse part sits in the kernel.
 
-// normal-direction PPM and the normal MHD term of direction D
-template <typename T, bool MHD, int TILE, int D>
-__device__ __forceinline__ void recon_normal(const gb_dev_grid& g, T gam, const T* dtd, const T* hd, int blk,
-                                             int i, int j, int k, int lane, const float* p32b,
+// unrotated slot of rotated slot s for direction d (see rot_slot), for a
+// compile-time s and a run-time d: an index computation, not a register move
+template <int S>
+__device__ __forceinline__ int rot_slot_rt(int d)
+{
+    if (S == 0 || S == 4) return S;
+    constexpr int base = S < 4 ? 1 : 5, o = S - base;
+    const int r = o + d;
+    return base + (r >= 3 ? r - 3 : r);
+}
+
+template <typename T>
+__device__ __forceinline__ T pick3(int d, T a, T b, T c) { return d == 0 ? a : (d == 1 ? b : c); }
+
+// offsets (elements from the cell's first variable) of the rotated
+// primitives of direction d: FP32 copy (mixed) or FP64 store slots (plain)
+template <typename T, bool MHD>
+__device__ __forceinline__ void rot_offsets(const gb_dev_grid& g, int d, int* off)
+{
+    int u[NP];
+    u[0] = 0; u[1] = rot_slot_rt<1>(d); u[2] = rot_slot_rt<2>(d); u[3] = rot_slot_rt<3>(d); u[4] = 4;
+    u[5] = rot_slot_rt<5>(d); u[6] = rot_slot_rt<6>(d); u[7] = rot_slot_rt<7>(d);
+    if constexpr (std::is_same<T, float>::value) {
+#pragma unroll
+        for (int s = 0; s < NP; ++s) off[s] = u[s] * GB_N3;
+    } else {
+        // store slots of the primitive roles, picked by selects (the role
+        // of rotated slot s is one of three)
+        const int sv[3] = {g.slot[GB_VELX], g.slot[GB_VELY], g.slot[GB_VELZ]};
+        off[0] = g.slot[GB_DENS] * GB_N3;
+        off[4] = g.slot[GB_PRES] * GB_N3;
+#pragma unroll
+        for (int s = 1; s < 4; ++s) off[s] = pick3(u[s] - 1, sv[0], sv[1], sv[2]) * GB_N3;
+        if (MHD) {
+            const int sb[3] = {g.slot[GB_MAGX], g.slot[GB_MAGY], g.slot[GB_MAGZ]};
+#pragma unroll
+            for (int s = 5; s < 8; ++s) off[s] = pick3(u[s] - 5, sb[0], sb[1], sb[2]) * GB_N3;
+        } else {
+            off[5] = off[6] = off[7] = -1;
+        }
+    }
+}
+
+// rotated primitives of one cell (ci: padded cell index)
+template <typename T, bool MHD>
+__device__ __forceinline__ void load_rot(const gb_dev_grid& g, int blk, int ci, const float* p32b, const int* off, T* w)
+{
+    if constexpr (std::is_same<T, float>::value) {
+#pragma unroll
+        for (int s = 0; s < NP; ++s) w[s] = p32b[(size_t)off[s] + ci];
+    } else {
+        const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3 + ci;
+#pragma unroll
+        for (int s = 0; s < NP; ++s) w[s] = (MHD || s < 5) ? (T)base[off[s]] : (T)0;
+    }
+}
+
+// normal-direction PPM and the normal MHD term of direction d; wp, wn, wc
+// come back in the rotated frame, s_sig / s_abn in the unrotated one
+template <typename T, bool MHD, int TILE>
+__device__ __forceinline__ void recon_normal(const gb_dev_grid& g, T gam, const T* dtd, const T* hd, int d, int blk,
+                                             int i, int j, int k, int lane, const float* p32b, const int* off,
                                              T (*s_sig)[NP][TILE], T (*s_abn)[NP][TILE], T (*s_dnb)[TILE], T* wp,
                                              T* wn, T* wc)
 {
     T qs[5][NP];
+    const int stride = d == 0 ? 1 : (d == 1 ? GB_N : GB_N * GB_N);
+    const int c0 = gb_cidx(i, j, k);
 #pragma unroll
-    for (int m = 0; m < 5; ++m) {
-        int ii = i + (D == 0 ? m - 2 : 0), jj = j + (D == 1 ? m - 2 : 0), kk = k + (D == 2 ? m - 2 : 0);
-        T w[NP];
-        load_prim<T, MHD>(g, blk, gb_cidx(ii, jj, kk), p32b, w);
+    for (int m = 0; m < 5; ++m) load_rot<T, MHD>(g, blk, c0 + (m - 2) * stride, p32b, off, qs[m]);
 #pragma unroll
-        for (int s = 0; s < NP; ++s) qs[m][s] = w[rot_slot(D, s)];
-    }
-    T wpr[NP], wnr[NP], sgr[NP];
-    ppm_normal<T, MHD>(gam, qs, dtd[D], wpr, wnr, sgr);
+    for (int s = 0; s < NP; ++s) wc[s] = qs[2][s];
+    T sgr[NP];
+    ppm_normal<T, MHD>(gam, qs, pick3(d, dtd[0], dtd[1], dtd[2]), wp, wn, sgr);
+    const int us[NP] = {0, rot_slot_rt<1>(d), rot_slot_rt<2>(d), rot_slot_rt<3>(d), 4,
+                        rot_slot_rt<5>(d), rot_slot_rt<6>(d), rot_slot_rt<7>(d)};
 #pragma unroll
-    for (int s = 0; s < NP; ++s) {
-        const int v = rot_slot(D, s);
-        wp[v] = wpr[s];
-        wn[v] = wnr[s];
-        s_sig[D][v][lane] = sgr[s];
-    }
-    load_prim<T, MHD>(g, blk, gb_cidx(i, j, k), p32b, wc);
+    for (int s = 0; s < NP; ++s) s_sig[d][us[s]][lane] = sgr[s];
     if (MHD) {
-        // multidimensional terms (hy_uhd_dataReconstOneStep.F90:364-424)
-        T uB = wc[1] * wc[5] + wc[2] * wc[6] + wc[3] * wc[7];
-        T row[NP] = {(T)0, -wc[5] / wc[0], -wc[6] / wc[0], -wc[7] / wc[0], (gam - (T)1) * uB,
-                     (T)0, -wc[2], -wc[3]};
-        if (D == 1) { row[5] = -wc[1]; row[6] = (T)0; row[7] = -wc[3]; }
-        if (D == 2) { row[5] = -wc[1]; row[6] = -wc[2]; row[7] = (T)0; }
-        const int ip = i + (D == 0), jp = j + (D == 1), kp2 = k + (D == 2);
-        T dnb = face_b<T>(g, D, blk, gb_fidx(D, ip, jp, kp2), p32b) - face_b<T>(g, D, blk, gb_fidx(D, i, j, k), p32b);
+        // multidimensional terms (hy_uhd_dataReconstOneStep.F90:364-424),
+        // in the rotated frame; u.B sums in the unrotated order
+        const T p1 = wc[1] * wc[5], p2 = wc[2] * wc[6], p3 = wc[3] * wc[7];
+        const T uB = pick3(d, p1, p3, p2) + pick3(d, p2, p1, p3) + pick3(d, p3, p2, p1);
+        const T row[NP] = {(T)0, -wc[5] / wc[0], -wc[6] / wc[0], -wc[7] / wc[0], (gam - (T)1) * uB,
+                           (T)0, -wc[2], -wc[3]};
+        const T hdd = pick3(d, hd[0], hd[1], hd[2]);
+        const int fa = gb_fidx(d, i, j, k);
+        T dnb = face_b<T>(g, d, blk, fa + (d == 0 ? 1 : (d == 1 ? GB_N : GB_N * GB_N)), p32b) -
+                face_b<T>(g, d, blk, fa, p32b);
 #pragma unroll
-        for (int v = 0; v < NP; ++v) {
-            s_abn[D][v][lane] = row[v];
-            wp[v] = wp[v] - hd[D] * row[v] * dnb;
-            wn[v] = wn[v] - hd[D] * row[v] * dnb;
+        for (int s = 0; s < NP; ++s) {
+            s_abn[d][us[s]][lane] = row[s];
+            wp[s] = wp[s] - hdd * row[s] * dnb;
+            wn[s] = wn[s] - hdd * row[s] * dnb;
         }
-        s_dnb[D][lane] = dnb;
+        s_dnb[d][lane] = dnb;
     }
 }
 
-// transverse corrections of direction D in the vendored order
-// (hy_uhd_dataReconstOneStep.F90:1006-1089)
-template <typename T, bool MHD, int TILE, int D>
-__device__ __forceinline__ void recon_transverse(const T* hd, int lane, T (*s_sig)[NP][TILE], T (*s_abn)[NP][TILE],
-                                                 T (*s_dnb)[TILE], T* wp, T* wn)
+// transverse corrections of direction d in the vendored order
+// (hy_uhd_dataReconstOneStep.F90:1006-1089), wp / wn in d's rotated frame
+template <typename T, bool MHD, int TILE>
+__device__ __forceinline__ void recon_transverse(const T* hd, int d, int lane, T (*s_sig)[NP][TILE],
+                                                 T (*s_abn)[NP][TILE], T (*s_dnb)[TILE], T* wp, T* wn)
 {
     constexpr int nv = MHD ? 8 : 5;
+    const int us[NP] = {0, rot_slot_rt<1>(d), rot_slot_rt<2>(d), rot_slot_rt<3>(d), 4,
+                        rot_slot_rt<5>(d), rot_slot_rt<6>(d), rot_slot_rt<7>(d)};
+    if (d < 2) {
+        // the other in-plane direction first (x: y, y: x), then z
+        const int o = d == 0 ? 1 : 0;
+        const T ho = o == 0 ? hd[0] : hd[1];
 #pragma unroll
-    for (int v = 0; v < nv; ++v) {
-        if (D == 0) {
-            wn[v] = wn[v] - hd[1] * s_sig[1][v][lane];
-            wp[v] = wp[v] - hd[1] * s_sig[1][v][lane];
-        } else if (D == 1) {
-            wn[v] = wn[v] - hd[0] * s_sig[0][v][lane];
-            wp[v] = wp[v] - hd[0] * s_sig[0][v][lane];
+        for (int s = 0; s < nv; ++s) {
+            wn[s] = wn[s] - ho * s_sig[o][us[s]][lane];
+            wp[s] = wp[s] - ho * s_sig[o][us[s]][lane];
         }
-    }
-    if (MHD) {
+        if (MHD) {
 #pragma unroll
-        for (int v = 0; v < nv; ++v) {
-            if (D == 0) {
-                wn[v] = wn[v] - hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
-                wp[v] = wp[v] - hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
-            } else if (D == 1) {
-                wn[v] = wn[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane];
-                wp[v] = wp[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane];
+            for (int s = 0; s < nv; ++s) {
+                wn[s] = wn[s] - ho * s_abn[o][us[s]][lane] * s_dnb[o][lane];
+                wp[s] = wp[s] - ho * s_abn[o][us[s]][lane] * s_dnb[o][lane];
             }
         }
-    }
 #pragma unroll
-    for (int v = 0; v < nv; ++v) {
-        if (D < 2) {
-            wn[v] = wn[v] - hd[2] * s_sig[2][v][lane];
-            wp[v] = wp[v] - hd[2] * s_sig[2][v][lane];
-        } else {
-            wn[v] = wn[v] - hd[0] * s_sig[0][v][lane] - hd[1] * s_sig[1][v][lane];
-            wp[v] = wp[v] - hd[0] * s_sig[0][v][lane] - hd[1] * s_sig[1][v][lane];
+        for (int s = 0; s < nv; ++s) {
+            wn[s] = wn[s] - hd[2] * s_sig[2][us[s]][lane];
+            wp[s] = wp[s] - hd[2] * s_sig[2][us[s]][lane];
         }
-    }
-    if (MHD) {
+        if (MHD) {
 #pragma unroll
-        for (int v = 0; v < nv; ++v) {
-            if (D < 2) {
-                wn[v] = wn[v] - hd[2] * s_abn[2][v][lane] * s_dnb[2][lane];
-                wp[v] = wp[v] - hd[2] * s_abn[2][v][lane] * s_dnb[2][lane];
-            } else {
-                wn[v] = wn[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane] -
-                        hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
-                wp[v] = wp[v] - hd[0] * s_abn[0][v][lane] * s_dnb[0][lane] -
-                        hd[1] * s_abn[1][v][lane] * s_dnb[1][lane];
+            for (int s = 0; s < nv; ++s) {
+                wn[s] = wn[s] - hd[2] * s_abn[2][us[s]][lane] * s_dnb[2][lane];
+                wp[s] = wp[s] - hd[2] * s_abn[2][us[s]][lane] * s_dnb[2][lane];
+            }
+        }
+    } else {
+#pragma unroll
+        for (int s = 0; s < nv; ++s) {
+            wn[s] = wn[s] - hd[0] * s_sig[0][us[s]][lane] - hd[1] * s_sig[1][us[s]][lane];
+            wp[s] = wp[s] - hd[0] * s_sig[0][us[s]][lane] - hd[1] * s_sig[1][us[s]][lane];
+        }
+        if (MHD) {
+#pragma unroll
+            for (int s = 0; s < nv; ++s) {
+                wn[s] = wn[s] - hd[0] * s_abn[0][us[s]][lane] * s_dnb[0][lane] -
+                        hd[1] * s_abn[1][us[s]][lane] * s_dnb[1][lane];
+                wp[s] = wp[s] - hd[0] * s_abn[0][us[s]][lane] * s_dnb[0][lane] -
+                        hd[1] * s_abn[1][us[s]][lane] * s_dnb[1][lane];
             }
         }
     }
@@ -580,20 +638,12 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
     }
     const float* p32b = p32 + (size_t)cb * p32_stride;
     T wp[NP], wn[NP], wc[NP];
-    if (d == 0)
-        recon_normal<T, MHD, TILE, 0>(g, gam, dtd, hd, blk, i, j, k, lane, p32b, s_sig, s_abn, s_dnb, wp, wn, wc);
-    else if (d == 1)
-        recon_normal<T, MHD, TILE, 1>(g, gam, dtd, hd, blk, i, j, k, lane, p32b, s_sig, s_abn, s_dnb, wp, wn, wc);
-    else
-        recon_normal<T, MHD, TILE, 2>(g, gam, dtd, hd, blk, i, j, k, lane, p32b, s_sig, s_abn, s_dnb, wp, wn, wc);
+    int off[NP];
+    rot_offsets<T, MHD>(g, d, off);
+    recon_normal<T, MHD, TILE>(g, gam, dtd, hd, d, blk, i, j, k, lane, p32b, off, s_sig, s_abn, s_dnb, wp, wn, wc);
     __syncthreads();
-    if (d == 0)
-        recon_transverse<T, MHD, TILE, 0>(hd, lane, s_sig, s_abn, s_dnb, wp, wn);
-    else if (d == 1)
-        recon_transverse<T, MHD, TILE, 1>(hd, lane, s_sig, s_abn, s_dnb, wp, wn);
-    else
-        recon_transverse<T, MHD, TILE, 2>(hd, lane, s_sig, s_abn, s_dnb, wp, wn);
-    // positivity fallback
+    recon_transverse<T, MHD, TILE>(hd, d, lane, s_sig, s_abn, s_dnb, wp, wn);
+    // positivity fallback (density and pressure keep their slots in every frame)
     bool fell = (wn[0] < (T)0 || wp[0] < (T)0 || wn[4] < (T)0 || wp[4] < (T)0);
     if (fell) {
 #pragma unroll
@@ -602,10 +652,12 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
     if (!active) return;
     if (st) gb_count_warp(&st->n_fallback, fell);
     T* out = scr + (size_t)cb * scr_stride;
+    const int us[NP] = {0, rot_slot_rt<1>(d), rot_slot_rt<2>(d), rot_slot_rt<3>(d), 4,
+                        rot_slot_rt<5>(d), rot_slot_rt<6>(d), rot_slot_rt<7>(d)};
 #pragma unroll
-    for (int v = 0; v < NP; ++v) {
-        out[((size_t)(0 * 3 + d) * NP + v) * NRC + cell] = wp[v];
-        out[((size_t)(1 * 3 + d) * NP + v) * NRC + cell] = wn[v];
+    for (int s = 0; s < NP; ++s) {
+        out[((size_t)(0 * 3 + d) * NP + us[s]) * NRC + cell] = wp[s];
+        out[((size_t)(1 * 3 + d) * NP + us[s]) * NRC + cell] = wn[s];
     }
 }
 
