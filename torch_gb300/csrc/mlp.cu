@@ -136,28 +136,35 @@ __global__ void k_gather(int n, const int* __restrict__ idx, const float* __rest
 // ------------------------------------------------------------- inference
 // weights packed as BF16 in the B-operand order of mma.m16n8k16 (.col:
 // element (k, n) at n * K + k), layer 1 padded to K = 16, layer 4 to N = 8.
+// Rows of each matrix are padded by 8 elements (16 bytes): a B-fragment
+// load then has the 8 rows of a warp start 4 banks apart, so the 32 lanes
+// hit 32 distinct banks (unpadded 128-byte rows put all 8 rows on the same
+// 4 banks, an 8-way conflict).
 struct packed_layout {
+    static constexpr int P1 = 16 + 8, PH = H + 8;  // row pitches (elements)
     static constexpr int W1 = 0;                 // 64 x 16
-    static constexpr int W2 = W1 + H * 16;       // 64 x 64
-    static constexpr int W3 = W2 + H * H;        // 64 x 64
-    static constexpr int W4 = W3 + H * H;        // 8 x 64
-    static constexpr int N = W4 + 8 * H;
+    static constexpr int W2 = W1 + H * P1;       // 64 x 64
+    static constexpr int W3 = W2 + H * PH;       // 64 x 64
+    static constexpr int W4 = W3 + H * PH;       // 8 x 64
+    static constexpr int N = W4 + 8 * PH;
 };
 
 __global__ void k_pack_bf16(const float* __restrict__ w, __nv_bfloat16* __restrict__ pk, float* __restrict__ pb)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < H * 16) {
-        int n = i / 16, k = i % 16;
-        pk[packed_layout::W1 + i] = __float2bfloat16_rn(k < NIN ? w[OW1 + n * NIN + k] : 0.0f);
+    using PL = packed_layout;
+    if (i < H * PL::P1) {
+        int n = i / PL::P1, k = i % PL::P1;
+        pk[PL::W1 + i] = __float2bfloat16_rn(k < NIN ? w[OW1 + n * NIN + k] : 0.0f);
     }
-    if (i < H * H) {
-        pk[packed_layout::W2 + i] = __float2bfloat16_rn(w[OW2 + i]);
-        pk[packed_layout::W3 + i] = __float2bfloat16_rn(w[OW3 + i]);
+    if (i < H * PL::PH) {
+        int n = i / PL::PH, k = i % PL::PH;
+        pk[PL::W2 + i] = __float2bfloat16_rn(k < H ? w[OW2 + n * H + k] : 0.0f);
+        pk[PL::W3 + i] = __float2bfloat16_rn(k < H ? w[OW3 + n * H + k] : 0.0f);
     }
-    if (i < 8 * H) {
-        int n = i / H, k = i % H;
-        pk[packed_layout::W4 + i] = __float2bfloat16_rn(n == 0 ? w[OW4 + k] : 0.0f);
+    if (i < 8 * PL::PH) {
+        int n = i / PL::PH, k = i % PL::PH;
+        pk[PL::W4 + i] = __float2bfloat16_rn(n == 0 && k < H ? w[OW4 + k] : 0.0f);
     }
     // biases stay FP32 (they are added to the FP32 accumulator), rounded to
     // BF16 values to match training
@@ -184,12 +191,13 @@ __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// B fragment (two .b32) for k-tile kt, n-tile nt of a layer with K columns
-__device__ __forceinline__ void bfrag(const __nv_bfloat16* w, int K, int kt, int nt, int lane, uint32_t& b0,
+// B fragment (two .b32) for k-tile kt, n-tile nt of a layer whose rows
+// are `pitch` elements apart
+__device__ __forceinline__ void bfrag(const __nv_bfloat16* w, int pitch, int kt, int nt, int lane, uint32_t& b0,
                                       uint32_t& b1)
 {
     int g = lane >> 2, t = lane & 3;
-    const __nv_bfloat16* p = w + (nt * 8 + g) * K + kt * 16 + t * 2;
+    const __nv_bfloat16* p = w + (nt * 8 + g) * pitch + kt * 16 + t * 2;
     b0 = *reinterpret_cast<const uint32_t*>(p);
     b1 = *reinterpret_cast<const uint32_t*>(p + 8);
 }
@@ -208,6 +216,8 @@ __device__ __forceinline__ float silu_infer(float z)
     const float h = 0.5f * z;
     return fmaf(h, tanh_approx(h), h);
 }
+
+__device__ __forceinline__ uint32_t silu_pair(float z0, float z1) { return pack2(silu_infer(z0), silu_infer(z1)); }
 
 // one hidden layer for NT 16-row tiles: acc[tile][8 n-tiles][4] = A(16 x K)
 // W^T + bias, then SiLU and repack to the A fragments of the next layer.
@@ -231,7 +241,7 @@ __device__ __forceinline__ void hidden_layer(const uint32_t (*afr)[4][4], const 
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt) {
             uint32_t b0, b1;
-            bfrag(w, KT * 16, kt, nt, lane, b0, b1);
+            bfrag(w, KT * 16 + 8, kt, nt, lane, b0, b1);
 #pragma unroll
             for (int q = 0; q < NT; ++q) mma_bf16(acc[q][nt], afr[q][kt], b0, b1);
         }
@@ -239,10 +249,10 @@ __device__ __forceinline__ void hidden_layer(const uint32_t (*afr)[4][4], const 
     for (int q = 0; q < NT; ++q)
 #pragma unroll
         for (int kt = 0; kt < 4; ++kt) {
-            anext[q][kt][0] = pack2(silu_infer(acc[q][2 * kt][0]), silu_infer(acc[q][2 * kt][1]));
-            anext[q][kt][1] = pack2(silu_infer(acc[q][2 * kt][2]), silu_infer(acc[q][2 * kt][3]));
-            anext[q][kt][2] = pack2(silu_infer(acc[q][2 * kt + 1][0]), silu_infer(acc[q][2 * kt + 1][1]));
-            anext[q][kt][3] = pack2(silu_infer(acc[q][2 * kt + 1][2]), silu_infer(acc[q][2 * kt + 1][3]));
+            anext[q][kt][0] = silu_pair(acc[q][2 * kt][0], acc[q][2 * kt][1]);
+            anext[q][kt][1] = silu_pair(acc[q][2 * kt][2], acc[q][2 * kt][3]);
+            anext[q][kt][2] = silu_pair(acc[q][2 * kt + 1][0], acc[q][2 * kt + 1][1]);
+            anext[q][kt][3] = silu_pair(acc[q][2 * kt + 1][2], acc[q][2 * kt + 1][3]);
         }
 }
 
@@ -291,7 +301,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer(int64_t n, const float* __res
 #pragma unroll
         for (int kt = 0; kt < 4; ++kt) {
             uint32_t b0, b1;
-            bfrag(sw + packed_layout::W4, H, kt, 0, lane, b0, b1);
+            bfrag(sw + packed_layout::W4, packed_layout::PH, kt, 0, lane, b0, b1);
 #pragma unroll
             for (int q = 0; q < NT; ++q) mma_bf16(out[q], h1[q][kt], b0, b1);
         }
@@ -532,7 +542,7 @@ int gb_mlp_pack(cudaStream_t s)
         return GB_ERR_NOT_INIT;
     }
     if (g_mlp.packed) return GB_OK;
-    k_pack_bf16<<<(H * H + 255) / 256, 256, 0, s>>>(g_mlp.w, g_mlp.pk, g_mlp.pb);
+    k_pack_bf16<<<(H * packed_layout::PH + 255) / 256, 256, 0, s>>>(g_mlp.w, g_mlp.pk, g_mlp.pb);
     g_mlp.packed = true;
     return gb_check(cudaGetLastError(), "mlp pack") ? GB_ERR_CUDA : GB_OK;
 }
