@@ -315,7 +315,7 @@ __device__ __forceinline__ long long wrap(long long x, long long n) { return x <
 // {node, level, flags, 0} and {cx, cy, cz, 0}. A guard cell then reads its
 // block's entry and its region's entry and takes at most one step down.
 
-__global__ void k_guard_plan(gb_tree_desc t, int4* __restrict__ plan)
+__global__ void k_guard_plan(gb_tree_desc t, int4* __restrict__ plan, int* __restrict__ near)
 {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= t.nnodes * 27) return;
@@ -349,6 +349,9 @@ __global__ void k_guard_plan(gb_tree_desc t, int4* __restrict__ plan)
             }
             h = make_int4(node, t.level[node], flags, 0);
             c = make_int4(t.coord[3 * node], t.coord[3 * node + 1], t.coord[3 * node + 2], 0);
+            // per leaf: bit 0 a coarser leaf around it, bit 1 a finer one
+            const int bits = (h.y < L ? 1 : 0) | (flags & GP_REFINED ? 2 : 0);
+            if (bits) atomicOr(near + b, bits);
         }
     }
     plan[2 * (size_t)idx] = h;
@@ -1043,11 +1046,13 @@ int gb_guard_prepare(cudaStream_t s)
         if (g_gb.d_plan) cudaFree(g_gb.d_plan);
         g_gb.d_plan = nullptr;
         g_gb.plan_n = 0;
-        if (gb_check(cudaMalloc(&g_gb.d_plan, (size_t)nn * 54 * sizeof(int4)), "cudaMalloc(guard plan)"))
+        if (gb_check(cudaMalloc(&g_gb.d_plan, (size_t)nn * (54 * sizeof(int4) + sizeof(int))), "cudaMalloc(guard plan)"))
             return GB_ERR_CUDA;
         g_gb.plan_n = nn;
     }
-    k_guard_plan<<<(nn * 27 + 255) / 256, 256, 0, s>>>(g_gb.tree, (int4*)g_gb.d_plan);
+    int* near = (int*)((int4*)g_gb.d_plan + (size_t)nn * 54);
+    cudaMemsetAsync(near, 0, (size_t)nn * sizeof(int), s);
+    k_guard_plan<<<(nn * 27 + 255) / 256, 256, 0, s>>>(g_gb.tree, (int4*)g_gb.d_plan, near);
     if (gb_check(cudaGetLastError(), "k_guard_plan")) return GB_ERR_CUDA;
     g_gb.plan_ok = true;
     return GB_OK;
@@ -1281,6 +1286,7 @@ int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int
         kp.fc_reg = g_gb.d_fcreg;
         if (g_gb.hp.mhd && g_gb.plan_ok && g_gb.d_ereg) {
             kp.ec_plan = (const int4*)g_gb.d_plan;
+            kp.ec_near = (const int*)((const int4*)g_gb.d_plan + (size_t)g_gb.plan_n * 54);
             kp.ec_child = g_gb.tree.child;
             kp.ec_reg = g_gb.d_ereg;
         }

@@ -587,15 +587,11 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_un
 }
 
 // rejected cells: the plain implicit integrator (RadHeat.F90:223-423)
-__global__ void k_sur_fallback(gb_dev_grid g, gb_cool_ctx c, double gamma, const int* __restrict__ list,
-                               double dt_code, const double* __restrict__ dtp, const int* __restrict__ rej, const int* __restrict__ nrej,
-                               gb_status* st)
+__device__ void sur_fallback_cell(const gb_dev_grid& g, const gb_cool_ctx& c, double gamma, const int* __restrict__ list,
+                                  double dt_code, int64_t idx, gb_status* st)
 {
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= *nrej) return;
-    if (dtp) dt_code = *dtp;
     int blk, ci, i, j, k;
-    cell_of(rej[q], list, blk, ci, i, j, k);
+    cell_of(idx, list, blk, ci, i, j, k);
     gb_cool_vars v;
     double ei, temp;
     sur_load(g, c, gamma, blk, ci, v, ei, temp);
@@ -614,6 +610,19 @@ __global__ void k_sur_fallback(gb_dev_grid g, gb_cool_ctx c, double gamma, const
         if (d.unbracketed) gb_fail(st, GB_ST_ZERO_UNBRACKETED, blk, i, j, k, ei);
         if (d.maxiter) gb_fail(st, GB_ST_ZERO_MAXITER, blk, i, j, k, ei);
     }
+}
+
+__global__ void k_sur_fallback(gb_dev_grid g, gb_cool_ctx c, double gamma, const int* __restrict__ list,
+                               double dt_code, const double* __restrict__ dtp, const int* __restrict__ rej, const int* __restrict__ nrej,
+                               gb_status* st)
+{
+    // a fixed grid striding over the compacted list: usually nothing is
+    // rejected, and a grid sized for the worst case would launch thousands
+    // of CTAs that only read the count
+    const int n = *nrej;
+    if (dtp) dt_code = *dtp;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+        sur_fallback_cell(g, c, gamma, list, dt_code, rej[q], st);
 }
 
 int g_cool_mode = 0;
@@ -719,7 +728,8 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp,
                                                g_sur_tol, g_sb.rej, g_sb.nrej, st);
     gb_prof_end(GBP_SUR_ACCEPT, s);
     gb_prof_begin(GBP_SUR_FALLBACK, s);
-    k_sur_fallback<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, dt, dtp, g_sb.rej, g_sb.nrej, st);
+    k_sur_fallback<<<nb < 152 * 4 ? nb : 152 * 4, 128, 0, s>>>(g_gb.grid, g_gb.cool, g_gb.hp.gamma, list, dt, dtp,
+                                                               g_sb.rej, g_sb.nrej, st);
     gb_prof_end(GBP_SUR_FALLBACK, s);
     return gb_check(cudaGetLastError(), "surrogate launch") ? GB_ERR_CUDA : GB_OK;
 }

@@ -371,6 +371,7 @@ struct hydro_kparams {
     // conservation; null: off): the guard-fill plan, the tree's child
     // table and the surface-edge registers (NSURF doubles per tree node)
     const int4* ec_plan = nullptr;
+    const int* ec_near = nullptr;  // per node: bit 0 a coarser leaf around it, bit 1 a finer one
     const int* ec_child = nullptr;
     double* ec_reg = nullptr;
 };
@@ -1112,11 +1113,13 @@ __device__ __forceinline__ void ring_edge(int q, int& A, int& B)
 }
 
 static __global__ void __launch_bounds__(128)
-k_emf_put(const int* __restrict__ list, const double* __restrict__ escr, size_t estride, double* __restrict__ ereg)
+k_emf_put(const int* __restrict__ list, const int* __restrict__ near, const double* __restrict__ escr, size_t estride,
+          double* __restrict__ ereg)
 {
     const int cb = blockIdx.y, t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= NSURF) return;
     const int blk = list[cb];
+    if (!(__ldg(near + blk) & 1)) return;  // no coarser leaf reads this block's edges
     const int c = t / (GB_NXB * NRING), C = (t / NRING) % GB_NXB;
     int A, B;
     ring_edge(t % NRING, A, B);
@@ -1161,12 +1164,13 @@ __device__ __forceinline__ void emf_get_dir(const int4* __restrict__ pb, const i
 }
 
 static __global__ void __launch_bounds__(128)
-k_emf_get(const int* __restrict__ list, const int4* __restrict__ plan, const int* __restrict__ child,
-          const double* __restrict__ ereg, double* __restrict__ escr, size_t estride)
+k_emf_get(const int* __restrict__ list, const int4* __restrict__ plan, const int* __restrict__ near,
+          const int* __restrict__ child, const double* __restrict__ ereg, double* __restrict__ escr, size_t estride)
 {
     const int cb = blockIdx.z, t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= GB_NXB * NRING) return;
     const int blk = list[cb];
+    if (!(__ldg(near + blk) & 2)) return;  // no finer leaf around this block
     const int4* pb = plan + (size_t)blk * 54;
     double* es = escr + (size_t)cb * estride;
     const int C = t / NRING, q = t % NRING;

@@ -76,15 +76,16 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
         dim3 eg((NEDGE + 127) / 128, 3, nblk);
         gb_prof_begin(GBP_EMF, s);
         k_emf<T><<<eg, 128, 0, s>>>(g, list, fscr, SL::flux, escr, SL::emf, p32, SL::prim32);
-        if (kp.ec_reg) k_emf_put<<<dim3((NSURF + 127) / 128, nblk), 128, 0, s>>>(list, escr, SL::emf, kp.ec_reg);
+        if (kp.ec_reg)
+            k_emf_put<<<dim3((NSURF + 127) / 128, nblk), 128, 0, s>>>(list, kp.ec_near, escr, SL::emf, kp.ec_reg);
         gb_prof_end(GBP_EMF, s);
         // the registers this chunk wrote are complete (a chunk on another
         // stream may read them now)
         if (ev_put) cudaEventRecord(ev_put, s);
         if (kp.ec_reg) {
             gb_prof_begin(GBP_EMF, s);
-            k_emf_get<<<dim3((GB_NXB * NRING + 127) / 128, 3, nblk), 128, 0, s>>>(list, kp.ec_plan, kp.ec_child,
-                                                                                  kp.ec_reg, escr, SL::emf);
+            k_emf_get<<<dim3((GB_NXB * NRING + 127) / 128, 3, nblk), 128, 0, s>>>(
+                list, kp.ec_plan, kp.ec_near, kp.ec_child, kp.ec_reg, escr, SL::emf);
             gb_prof_end(GBP_EMF, s);
         }
         dim3 bg((NFB + 127) / 128, 3, nblk);
