@@ -285,6 +285,29 @@ int gb_set_dt_limits(double dtmin, double dtmax, double change_factor);
  * the step. Not re-entrant. */
 int gb_step_graph(int blockCount, const int* blockList_dev, int cool, gb_driver_state* drv_dev,
                   gb_status* st_dev, void* stream);
+
+/* The state of a FLASH host that keeps unk and facevar{x,y,z} in its own
+ * (pinned) arrays: the interior transfers below in one argument. */
+typedef struct gb_host_io {
+    double* unk;                 /* unk(nunk, 24, 24, 24, blocks), variable fastest */
+    int nunk;
+    int host_slot[GB_NROLE];     /* index of role r in unk's variable axis, or -1 */
+    double* facex;               /* facevar{x,y,z}; all NULL without face fields */
+    double* facey;
+    double* facez;
+} gb_host_io;
+
+/* gb_step_graph for a host-resident state: the same graph also uploads the
+ * listed blocks' interiors from io (cells and owned faces) before the CFL
+ * reduction, and downloads each chunk's interiors as soon as that chunk's
+ * update and cooling are done, while later chunks compute (a chunk's blocks
+ * are final then: later chunks read only their own blocks, guard copies and
+ * the flux / edge registers). The host arrays' guard cells and guard faces
+ * are neither read nor written. The arrays must be pinned and must not be
+ * touched by the host while the graph may run. No counterpart in the
+ * reference (FLASH's Grid keeps unk on the host and calls Hydro on it). */
+int gb_step_graph_host(int blockCount, const int* blockList_dev, int cool, gb_driver_state* drv_dev,
+                       gb_status* st_dev, const gb_host_io* io, void* stream);
 /* Drops the captured step graph. */
 int gb_graph_reset(void);
 /* Number of captures and replays of the step graph so far, and the kernel
@@ -316,6 +339,24 @@ int gb_grid_upload_faces_list(const double* fx_host, const double* fy_host, cons
                               int blockCount, const int* blockList_host, void* stream);
 int gb_grid_download_faces_list(double* fx_host, double* fy_host, double* fz_host, int blockCount,
                                 const int* blockList_host, void* stream);
+
+/* The same two transfers for the interiors only: the 16^3 interior cells
+ * of each listed block, and the faces each block owns (4..20 along the
+ * normal, 4..19 across). The step rebuilds guard cells and guard faces on
+ * the device from the neighbours' interiors (as Grid_fillGuardCells does
+ * before Hydro, Driver_computeDt.F90:243), so a host that keeps the state
+ * in its FLASH arrays between steps moves 30 % of the bytes. The host
+ * arrays keep the full FLASH shape; their guard cells and guard faces are
+ * neither read nor written. Host arrays must be pinned (the kernels read
+ * and write them in place); no counterpart in the reference. */
+int gb_grid_upload_flash_interior_list(const double* unk_host, int nunk, const int* host_slot, int blockCount,
+                                       const int* blockList_host, void* stream);
+int gb_grid_download_flash_interior_list(double* unk_host, int nunk, const int* host_slot, int blockCount,
+                                         const int* blockList_host, void* stream);
+int gb_grid_upload_faces_interior_list(const double* fx_host, const double* fy_host, const double* fz_host,
+                                       int blockCount, const int* blockList_host, void* stream);
+int gb_grid_download_faces_interior_list(double* fx_host, double* fy_host, double* fz_host, int blockCount,
+                                         const int* blockList_host, void* stream);
 
 /* ---------------------------------------------------------------- surrogate */
 /* Learned cooling surrogate (no counterpart in the reference): an MLP

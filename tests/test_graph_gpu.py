@@ -155,3 +155,63 @@ def test_autotuner_picks_a_candidate_and_restores_state(gb, tmp_path, monkeypatc
     finally:
         gb.set_launch_config(16, 32)
         gb.set_chunk_streams(1)
+
+
+@pytest.mark.parametrize("streams", [1, 2])
+def test_host_resident_step_matches_separate_transfers(gb, streams):
+    """gb_step_graph_host (interior upload, step, per-chunk downloads
+    overlapping later chunks, one graph) leaves the host arrays and the
+    device store bit for bit as interior upload + step graph + interior
+    download do."""
+    import ctypes as C
+    import torch
+    units = gb.code_units()
+    gb.init_cooling(gb.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
+                                   time_unit=units["time_unit"]))
+    gb.mlp_init(3)
+    gb.init_hydro(gb.hydro_params(True, precision=1))
+    gb.set_flux_correction(True)
+    gb.set_cooling_mode(True)
+    L = gb.lib()
+    out = []
+    try:
+        gb.set_launch_config(7, 32, 1)
+        gb.set_chunk_streams(streams)
+        for fused in (False, True):
+            g = _grid(gb)
+            g.register()
+            nunk, nn = g.nvar, g.nblocks
+            host = torch.empty((nn, 24 ** 3, nunk), dtype=torch.float64).pin_memory()
+            hf = [a.cpu().pin_memory() for a in (g.fx, g.fy, g.fz)]
+            io = gb.HostIO()
+            io.unk, io.nunk = host.data_ptr(), nunk
+            for r in range(gb.NROLE):
+                io.host_slot[r] = -1
+            for name, s in g.slots.items():
+                io.host_slot[gb.R[name]] = s
+            io.facex, io.facey, io.facez = (h.data_ptr() for h in hf)
+            gb.check(L.gb_grid_download_flash(C.c_void_p(host.data_ptr()), nunk, io.host_slot, nn, None), "init")
+            torch.cuda.synchronize()
+            leaves = np.ascontiguousarray(g.leaf, np.int32)
+            lp = leaves.ctypes.data_as(C.c_void_p)
+            fp = [C.c_void_p(h.data_ptr()) for h in hf]
+            for _ in range(2):
+                if fused:
+                    g.step_graph_host(io, cool=True)
+                else:
+                    gb.check(L.gb_grid_upload_flash_interior_list(C.c_void_p(host.data_ptr()), nunk, io.host_slot,
+                                                                  len(leaves), lp, None), "up")
+                    gb.check(L.gb_grid_upload_faces_interior_list(*fp, len(leaves), lp, None), "up faces")
+                    g.step_graph(cool=True)
+                    gb.check(L.gb_grid_download_flash_interior_list(C.c_void_p(host.data_ptr()), nunk, io.host_slot,
+                                                                    len(leaves), lp, None), "down")
+                    gb.check(L.gb_grid_download_faces_interior_list(*fp, len(leaves), lp, None), "down faces")
+            torch.cuda.synchronize()
+            assert g.status_read()["code"] == 0
+            out.append([host.clone()] + [h.clone() for h in hf] + [g.u[g.t_leaf.long()].clone()])
+            del g
+    finally:
+        gb.set_chunk_streams(1)
+        gb.set_launch_config(16, 32)
+        gb.set_cooling_mode(False)
+    assert all(torch.equal(a, b) for a, b in zip(out[0], out[1]))

@@ -934,6 +934,77 @@ __global__ void __launch_bounds__(FT) k_flash_direct(double* host, int nunk, con
     }
 }
 
+// Interior cells only: one CTA moves FT interior cells (FT / 16 rows of
+// 16 cells along i) of one block; each row is one contiguous run of
+// 16 * nunk host values.
+constexpr int IROWS = FT / GB_NXB;
+static_assert(FT % GB_NXB == 0 && (GB_NXB * GB_NXB) % IROWS == 0, "interior tile");
+
+// Work items are (block, group of IROWS rows); a grid smaller than the
+// item count strides over them (a download running beside compute kernels
+// keeps a small footprint that way).
+constexpr int ITEMS_PER_BLOCK = GB_NXB * GB_NXB / IROWS;
+
+template <bool UP>
+__global__ void __launch_bounds__(FT) k_flash_interior(double* host, int nunk, const int* __restrict__ hslot,
+                                                       gb_dev_grid g, const int* __restrict__ list, int nblk,
+                                                       int read_first)
+{
+    extern __shared__ double tile[];  // FT * nunk
+    const int run = GB_NXB * nunk;
+    const int tot = FT * nunk;
+    for (int item = blockIdx.x; item < nblk * ITEMS_PER_BLOCK; item += gridDim.x) {
+        const int blk = list[item / ITEMS_PER_BLOCK];
+        const int row0 = (item % ITEMS_PER_BLOCK) * IROWS;  // rows (j, k) of the interior, j fastest
+        auto hrow = [&](int r) {
+            const int jk = row0 + r;
+            const int ci = gb_cidx(GB_NGUARD, GB_NGUARD + jk % GB_NXB, GB_NGUARD + jk / GB_NXB);
+            return host + ((size_t)blk * GB_N3 + ci) * nunk;
+        };
+        if (UP || read_first)
+            for (int e = threadIdx.x; e < tot; e += FT) tile[e] = hrow(e / run)[e % run];
+        __syncthreads();
+        const int r = threadIdx.x / GB_NXB, i = threadIdx.x % GB_NXB;
+        const int jk = row0 + r;
+        const int c = gb_cidx(GB_NGUARD + i, GB_NGUARD + jk % GB_NXB, GB_NGUARD + jk / GB_NXB);
+        for (int q = 0; q < GB_NROLE; ++q) {
+            const int hs = hslot[q], ds = g.slot[q];
+            if (hs < 0 || ds < 0) continue;
+            double* d = g.unk + ((size_t)blk * g.nvar + ds) * GB_N3 + c;
+            if (UP) *d = tile[threadIdx.x * nunk + hs];
+            else tile[threadIdx.x * nunk + hs] = *d;
+        }
+        __syncthreads();
+        if (!UP) {
+            for (int e = threadIdx.x; e < tot; e += FT) hrow(e / run)[e % run] = tile[e];
+            __syncthreads();
+        }
+    }
+}
+
+// The faces a block owns along each axis a: normal index 4..20 (17),
+// transverse 4..19 (16 x 16); x fastest, so runs along x are contiguous on
+// both sides.
+constexpr int GB_NOWN = (GB_NXB + 1) * GB_NXB * GB_NXB;
+
+template <bool UP>
+__global__ void k_faces_interior(double* hx, double* hy, double* hz, gb_dev_grid g, const int* __restrict__ list,
+                                 int nblk)
+{
+    const int64_t n = (int64_t)nblk * 3 * GB_NOWN;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int e = (int)(t % GB_NOWN), a = (int)((t / GB_NOWN) % 3), q = (int)(t / (3 * GB_NOWN));
+        const int blk = list[q];
+        const int nx = GB_NXB + (a == 0), ny = GB_NXB + (a == 1);
+        const int I = GB_NGUARD + e % nx, J = GB_NGUARD + (e / nx) % ny, K = GB_NGUARD + e / (nx * ny);
+        const size_t off = (size_t)blk * GB_FSZ + gb_fidx(a, I, J, K);
+        double* h = (a == 0 ? hx : a == 1 ? hy : hz) + off;
+        double* d = (a == 0 ? g.f[0] : a == 1 ? g.f[1] : g.f[2]) + off;
+        if (UP) *d = *h;
+        else *h = *d;
+    }
+}
+
 template <bool UP>
 __global__ void k_faces_direct(double* hx, double* hy, double* hz, gb_dev_grid g, const int* __restrict__ list)
 {
@@ -1166,8 +1237,41 @@ struct chunk_aux {
     cudaStream_t s2 = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
     std::vector<cudaEvent_t> put;  // one per chunk
+    // per-chunk downloads of a host-resident step (gb_step_graph_host)
+    cudaStream_t s3 = nullptr;
+    cudaEvent_t dl = nullptr, dl_join = nullptr;
 } g_aux;
+
+// The device views of a host-resident state while its step is recorded
+// (nullptr otherwise).
+struct host_io_dev {
+    double* unk = nullptr;
+    int nunk = 0, read_first = 0;
+    double* f[3] = {nullptr, nullptr, nullptr};
+    int* dslot = nullptr;  // device copy of the slot map
+};
+const host_io_dev* g_hio = nullptr;
 }  // namespace
+
+static int g_io_priority = 0;  // the device's greatest stream priority
+
+static int io_streams_prepare()
+{
+    if (!g_aux.s3) {
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        g_io_priority = greatest;
+        if (gb_check(cudaStreamCreateWithPriority(&g_aux.s3, cudaStreamNonBlocking, greatest), "download stream"))
+            return GB_ERR_CUDA;
+    }
+    if (!g_aux.dl && (gb_check(cudaEventCreateWithFlags(&g_aux.dl, cudaEventDisableTiming), "event") ||
+                      gb_check(cudaEventCreateWithFlags(&g_aux.dl_join, cudaEventDisableTiming), "event")))
+        return GB_ERR_CUDA;
+    return GB_OK;
+}
+
+// interior transfers of nblk listed blocks (device list) of a host-resident state
+static void launch_io(bool up, const host_io_dev& io, int nblk, const int* list, cudaStream_t s);
 
 // The second stream and the events of a step of nchunks chunks (before any
 // capture: it creates them once).
@@ -1316,6 +1420,17 @@ int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int
             rc = gb_launch_surrogate(nb, list + b0, dt, dtp, st, sk, chain);
             if (rc) return rc;
         }
+        if (g_hio) {
+            // this chunk's blocks are final: download them on the download
+            // stream while later chunks compute
+            cudaEventRecord(g_aux.dl, sk);
+            cudaStreamWaitEvent(g_aux.s3, g_aux.dl, 0);
+            launch_io(false, *g_hio, nb, list + b0, g_aux.s3);
+        }
+    }
+    if (g_hio) {
+        cudaEventRecord(g_aux.dl_join, g_aux.s3);
+        cudaStreamWaitEvent(s, g_aux.dl_join, 0);
     }
     if (ns > 1) {
         cudaEventRecord(g_aux.join, g_aux.s2);
@@ -1427,7 +1542,17 @@ struct step_graph {
     gb_status* st = nullptr;
     unsigned long long gen = ~0ULL;
     long long launches = 0, captures = 0, kernel_nodes = 0;
+    // the host-resident state the graph was recorded for (io.unk null: none)
+    gb_host_io io = {};
+    host_io_dev dio;
 } g_graph;
+
+bool same_io(const gb_host_io* a, const gb_host_io& b)
+{
+    if (!a) return b.unk == nullptr;
+    return a->unk == b.unk && a->nunk == b.nunk && a->facex == b.facex && a->facey == b.facey &&
+           a->facez == b.facez && memcmp(a->host_slot, b.host_slot, sizeof b.host_slot) == 0;
+}
 
 void graph_drop()
 {
@@ -1438,6 +1563,10 @@ void graph_drop()
 int record_step(int n, const int* list, int cool, gb_driver_state* drv, gb_status* st, cudaStream_t s)
 {
     double* dt_dev = &drv->dt;
+    if (g_hio) {
+        launch_io(true, *g_hio, n, list, s);
+        if (gb_check(cudaGetLastError(), "interior upload")) return GB_ERR_CUDA;
+    }
     int rc = launch_dt(n, list, dt_dev, drv, s);
     if (rc) return rc;
     rc = gb_launch_guardfill(n, list, s);
@@ -1451,8 +1580,8 @@ int record_step(int n, const int* list, int cool, gb_driver_state* drv, gb_statu
 
 int gb_cooling_mode();
 
-extern "C" int gb_step_graph(int blockCount, const int* list, int cool, gb_driver_state* drv, gb_status* st,
-                             void* stream)
+static int run_step_graph(int blockCount, const int* list, int cool, gb_driver_state* drv, gb_status* st,
+                      const gb_host_io* io, void* stream)
 {
     if (!g_gb.grid_ok || !g_gb.hydro_ok || !g_gb.tree_ok) {
         gb_set_error("gb_step_graph: register grid + tree and call gb_hydro_init first");
@@ -1472,9 +1601,37 @@ extern "C" int gb_step_graph(int blockCount, const int* list, int cool, gb_drive
     }
     cudaStream_t s = (cudaStream_t)stream;
     const bool same = g_graph.exec && g_graph.list == list && g_graph.n == blockCount && g_graph.cool == cool &&
-                      g_graph.drv == drv && g_graph.st == st && g_graph.gen == g_gb.gen;
+                      g_graph.drv == drv && g_graph.st == st && g_graph.gen == g_gb.gen && same_io(io, g_graph.io);
     if (!same) {
         graph_drop();
+        g_graph.io = gb_host_io{};
+        host_io_dev dio;
+        if (io) {
+            // device views of the pinned host arrays and a device copy of
+            // the slot map (the graph bakes both in)
+            dio.unk = (double*)device_view(io->unk);
+            dio.nunk = io->nunk;
+            const bool faces = io->facex || io->facey || io->facez;
+            for (int a = 0; a < 3 && faces; ++a)
+                dio.f[a] = (double*)device_view(a == 0 ? io->facex : a == 1 ? io->facey : io->facez);
+            if (!dio.unk || io->nunk <= 0 || (size_t)FT * io->nunk * sizeof(double) > 48 * 1024 ||
+                (faces && (!dio.f[0] || !dio.f[1] || !dio.f[2] || !g_gb.grid.f[0]))) {
+                gb_set_error("gb_step_graph_host: host arrays must be pinned (nunk %d, up to %d)", io->nunk,
+                             (int)(48 * 1024 / (FT * 8)));
+                return GB_ERR_ARG;
+            }
+            int mapped = 0;
+            for (int r = 0; r < GB_NROLE; ++r)
+                if (io->host_slot[r] >= 0 && io->host_slot[r] < io->nunk && g_gb.grid.slot[r] >= 0) ++mapped;
+            dio.read_first = mapped < io->nunk;
+            if (!g_graph.dio.dslot && gb_check(cudaMalloc(&g_graph.dio.dslot, GB_NROLE * sizeof(int)), "slot map"))
+                return GB_ERR_CUDA;
+            dio.dslot = g_graph.dio.dslot;
+            if (gb_check(cudaMemcpy(dio.dslot, io->host_slot, GB_NROLE * sizeof(int), cudaMemcpyHostToDevice),
+                         "slot map") ||
+                io_streams_prepare())
+                return GB_ERR_CUDA;
+        }
         if (!g_graph.cap && gb_check(cudaStreamCreateWithFlags(&g_graph.cap, cudaStreamNonBlocking), "graph stream"))
             return GB_ERR_CUDA;
         // everything that allocates or uploads happens before the capture
@@ -1489,7 +1646,10 @@ extern "C" int gb_step_graph(int blockCount, const int* list, int cool, gb_drive
         if (gb_check(cudaStreamSynchronize(s), "graph prepare")) return GB_ERR_CUDA;
         if (gb_check(cudaStreamBeginCapture(g_graph.cap, cudaStreamCaptureModeThreadLocal), "begin capture"))
             return GB_ERR_CUDA;
+        g_graph.dio = dio.unk ? dio : host_io_dev{nullptr, 0, 0, {nullptr, nullptr, nullptr}, g_graph.dio.dslot};
+        g_hio = io ? &g_graph.dio : nullptr;
         rc = record_step(blockCount, list, cool, drv, st, g_graph.cap);
+        g_hio = nullptr;
         cudaGraph_t graph = nullptr;
         cudaError_t e = cudaStreamEndCapture(g_graph.cap, &graph);
         if (rc || gb_check(e, "end capture")) {
@@ -1518,10 +1678,27 @@ extern "C" int gb_step_graph(int blockCount, const int* list, int cool, gb_drive
         g_graph.drv = drv;
         g_graph.st = st;
         g_graph.gen = g_gb.gen;
+        g_graph.io = io ? *io : gb_host_io{};
         g_graph.captures += 1;
     }
     g_graph.launches += 1;
     return gb_check(cudaGraphLaunch(g_graph.exec, s), "graph launch") ? GB_ERR_CUDA : GB_OK;
+}
+
+extern "C" int gb_step_graph(int blockCount, const int* list, int cool, gb_driver_state* drv, gb_status* st,
+                             void* stream)
+{
+    return run_step_graph(blockCount, list, cool, drv, st, nullptr, stream);
+}
+
+extern "C" int gb_step_graph_host(int blockCount, const int* list, int cool, gb_driver_state* drv, gb_status* st,
+                                  const gb_host_io* io, void* stream)
+{
+    if (!io) {
+        gb_set_error("gb_step_graph_host: no host state");
+        return GB_ERR_ARG;
+    }
+    return run_step_graph(blockCount, list, cool, drv, st, io, stream);
 }
 
 extern "C" int gb_graph_info(long long* captures, long long* launches, long long* kernel_nodes)
@@ -1689,6 +1866,160 @@ extern "C" int gb_grid_download_flash_list(double* unk_host, int nunk, const int
                                            const int* blockList_host, void* stream)
 {
     return flash_copy_list(false, unk_host, nunk, host_slot, blockCount, blockList_host, stream);
+}
+
+// Interior transfers: the host arrays must be addressable by the device
+// (pinned); the guard cells and guard faces of the host arrays stay as
+// they are.
+static int interior_prepare(const char* who, int n, const int* list, const int* host_slot, cudaStream_t s,
+                            int** dslot, int** dlist)
+{
+    if (!g_gb.grid_ok) {
+        gb_set_error("%s before gb_register_grid", who);
+        return GB_ERR_NOT_INIT;
+    }
+    int rc = check_host_list(n, list, who);
+    if (rc || n == 0) return rc;
+    rc = gb_ensure_stage((GB_NROLE + (size_t)n) * sizeof(int));
+    if (rc) return rc;
+    *dslot = (int*)g_gb.d_stage;
+    *dlist = *dslot + GB_NROLE;
+    if (host_slot &&
+        gb_check(cudaMemcpyAsync(*dslot, host_slot, GB_NROLE * sizeof(int), cudaMemcpyHostToDevice, s), "slot copy"))
+        return GB_ERR_CUDA;
+    return gb_check(cudaMemcpyAsync(*dlist, list, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s), "list copy")
+               ? GB_ERR_CUDA
+               : GB_OK;
+}
+
+static int flash_interior_list(bool up, double* host, int nunk, const int* host_slot, int n, const int* list,
+                               void* stream)
+{
+    const char* who = up ? "gb_grid_upload_flash_interior_list" : "gb_grid_download_flash_interior_list";
+    if (!host || !host_slot || nunk <= 0) return GB_ERR_ARG;
+    double* hd = (double*)device_view(host);
+    if (!hd) {
+        gb_set_error("%s: the host array is not pinned", who);
+        return GB_ERR_ARG;
+    }
+    const size_t smem = (size_t)FT * nunk * sizeof(double);
+    if (smem > 48 * 1024) {
+        gb_set_error("%s: nunk %d above the %d variables one tile holds", who, nunk, (int)(48 * 1024 / (FT * 8)));
+        return GB_ERR_ARG;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    int *dslot = nullptr, *dlist = nullptr;
+    int rc = interior_prepare(who, n, list, host_slot, s, &dslot, &dlist);
+    if (rc || n == 0) return rc;
+    int mapped = 0;
+    for (int r = 0; r < GB_NROLE; ++r)
+        if (host_slot[r] >= 0 && host_slot[r] < nunk && g_gb.grid.slot[r] >= 0) ++mapped;
+    const unsigned grid = (unsigned)(n * ITEMS_PER_BLOCK);
+    gb_prof_begin(GBP_COPY, s);
+    if (up) k_flash_interior<true><<<grid, FT, smem, s>>>(hd, nunk, dslot, g_gb.grid, dlist, n, 0);
+    else k_flash_interior<false><<<grid, FT, smem, s>>>(hd, nunk, dslot, g_gb.grid, dlist, n, mapped < nunk);
+    gb_prof_end(GBP_COPY, s);
+    return gb_check(cudaGetLastError(), "k_flash_interior") ? GB_ERR_CUDA : GB_OK;
+}
+
+extern "C" int gb_grid_upload_flash_interior_list(const double* unk_host, int nunk, const int* host_slot,
+                                                  int blockCount, const int* blockList_host, void* stream)
+{
+    return flash_interior_list(true, const_cast<double*>(unk_host), nunk, host_slot, blockCount, blockList_host,
+                               stream);
+}
+
+extern "C" int gb_grid_download_flash_interior_list(double* unk_host, int nunk, const int* host_slot,
+                                                    int blockCount, const int* blockList_host, void* stream)
+{
+    return flash_interior_list(false, unk_host, nunk, host_slot, blockCount, blockList_host, stream);
+}
+
+static int faces_interior_list(bool up, double* const host[3], int n, const int* list, void* stream)
+{
+    const char* who = up ? "gb_grid_upload_faces_interior_list" : "gb_grid_download_faces_interior_list";
+    if (!g_gb.grid_ok || !g_gb.grid.f[0] || !g_gb.grid.f[1] || !g_gb.grid.f[2]) {
+        gb_set_error("%s: the registered grid has no face fields", who);
+        return GB_ERR_NOT_INIT;
+    }
+    if (!host[0] || !host[1] || !host[2]) return GB_ERR_ARG;
+    double* hv[3] = {(double*)device_view(host[0]), (double*)device_view(host[1]), (double*)device_view(host[2])};
+    if (!hv[0] || !hv[1] || !hv[2]) {
+        gb_set_error("%s: the host arrays are not pinned", who);
+        return GB_ERR_ARG;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    int *dslot = nullptr, *dlist = nullptr;
+    int rc = interior_prepare(who, n, list, nullptr, s, &dslot, &dlist);
+    if (rc || n == 0) return rc;
+    const unsigned grid = (unsigned)(((int64_t)n * 3 * GB_NOWN + 255) / 256);
+    gb_prof_begin(GBP_COPY, s);
+    if (up) k_faces_interior<true><<<grid, 256, 0, s>>>(hv[0], hv[1], hv[2], g_gb.grid, dlist, n);
+    else k_faces_interior<false><<<grid, 256, 0, s>>>(hv[0], hv[1], hv[2], g_gb.grid, dlist, n);
+    gb_prof_end(GBP_COPY, s);
+    return gb_check(cudaGetLastError(), "k_faces_interior") ? GB_ERR_CUDA : GB_OK;
+}
+
+extern "C" int gb_grid_upload_faces_interior_list(const double* fx_host, const double* fy_host, const double* fz_host,
+                                                  int blockCount, const int* blockList_host, void* stream)
+{
+    double* h[3] = {const_cast<double*>(fx_host), const_cast<double*>(fy_host), const_cast<double*>(fz_host)};
+    return faces_interior_list(true, h, blockCount, blockList_host, stream);
+}
+
+extern "C" int gb_grid_download_faces_interior_list(double* fx_host, double* fy_host, double* fz_host,
+                                                    int blockCount, const int* blockList_host, void* stream)
+{
+    double* h[3] = {fx_host, fy_host, fz_host};
+    return faces_interior_list(false, h, blockCount, blockList_host, stream);
+}
+
+// Downloads run beside the compute kernels of later chunks: they are
+// launched at the device's greatest priority, so the CTA scheduler hands
+// them SM slots as compute CTAs retire instead of after the compute kernels
+// queued before them (the priority is a launch attribute, kept by the
+// graph's kernel nodes).
+template <typename... P, typename... A>
+static void launch_prio(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool prio, A... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributePriority;
+    at[0].val.priority = g_io_priority;
+    cfg.attrs = at;
+    cfg.numAttrs = prio ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, k, args...);
+}
+
+// CTAs of a download running beside compute: enough rows in flight to
+// keep the host link busy (about 200 GB/s at a few microseconds of
+// latency), few enough to leave the SMs to the compute kernels. Measured
+// on the 4101-leaf step: 32 CTAs 77 ms per step, 128 41 ms, 256 and 512
+// 37.5 ms, 1024 41 ms, one CTA per row group (no limit) 47.5 ms.
+constexpr int g_io_ctas = 256;
+
+static void launch_io(bool up, const host_io_dev& io, int nblk, const int* list, cudaStream_t s)
+{
+    const size_t smem = (size_t)FT * io.nunk * sizeof(double);
+    const int items = nblk * ITEMS_PER_BLOCK;
+    const int64_t faces = (int64_t)nblk * 3 * GB_NOWN;
+    if (up) {
+        launch_prio(k_flash_interior<true>, dim3(items), dim3(FT), smem, s, false, io.unk, io.nunk,
+                    (const int*)io.dslot, g_gb.grid, list, nblk, 0);
+        if (io.f[0])
+            launch_prio(k_faces_interior<true>, dim3((unsigned)((faces + 255) / 256)), dim3(256), 0, s, false,
+                        io.f[0], io.f[1], io.f[2], g_gb.grid, list, nblk);
+        return;
+    }
+    launch_prio(k_flash_interior<false>, dim3(std::min(items, g_io_ctas)), dim3(FT), smem, s, true, io.unk,
+                io.nunk, (const int*)io.dslot, g_gb.grid, list, nblk, io.read_first);
+    if (io.f[0])
+        launch_prio(k_faces_interior<false>, dim3((unsigned)std::min<int64_t>((faces + 255) / 256, g_io_ctas / 4)),
+                    dim3(256), 0, s, true, io.f[0], io.f[1], io.f[2], g_gb.grid, list, nblk);
 }
 
 static int face_copy_list(bool up, double* const host[3], int n, const int* list, void* stream)

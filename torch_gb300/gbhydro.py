@@ -78,6 +78,12 @@ class CoolParams(C.Structure):
     ]
 
 
+class HostIO(C.Structure):
+    """gb_host_io: a FLASH host's pinned unk and facevar arrays."""
+    _fields_ = [("unk", C.c_void_p), ("nunk", C.c_int), ("host_slot", C.c_int * NROLE),
+                ("facex", C.c_void_p), ("facey", C.c_void_p), ("facez", C.c_void_p)]
+
+
 class Status(C.Structure):
     _fields_ = [("code", C.c_int), ("block", C.c_int), ("i", C.c_int), ("j", C.c_int),
                 ("k", C.c_int), ("pad", C.c_int), ("value", C.c_double),
@@ -102,6 +108,8 @@ _SIG = {
     "gb_set_chunk_streams": (C.c_int, [C.c_int]),
     "gb_get_chunk_streams": (C.c_int, []),
     "gb_step_graph": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gb_step_graph_host": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p]),
     "gb_set_dt_limits": (C.c_int, [C.c_double, C.c_double, C.c_double]),
     "gb_set_flux_correction": (C.c_int, [C.c_int]),
     "gb_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
@@ -122,6 +130,14 @@ _SIG = {
     "gb_grid_upload_flash_list": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "gb_grid_download_flash_list": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "gb_grid_upload_faces_list": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "gb_grid_upload_flash_interior_list": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                                     C.c_void_p]),
+    "gb_grid_download_flash_interior_list": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                                       C.c_void_p]),
+    "gb_grid_upload_faces_interior_list": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                                     C.c_void_p]),
+    "gb_grid_download_faces_interior_list": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                                       C.c_void_p]),
     "gb_grid_download_faces_list": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                               C.c_void_p]),
     "gb_status_reset": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -326,6 +342,18 @@ class Grid:
         drv = self.driver
         check(lib().gb_step_graph(n, _ptr(lt), int(cool), _ptr(drv), _ptr(self.status), _stream()),
               "gb_step_graph")
+        return drv[self.DRV_DT:self.DRV_DT + 1]
+
+    def step_graph_host(self, io: "HostIO", cool: bool, blockList=None):
+        """step_graph for a host-resident state: uploads the listed blocks'
+        interiors from the pinned host arrays in `io`, steps, and downloads
+        each chunk's interiors while later chunks compute (one graph)."""
+        lt, n = self.list_tensor(blockList)
+        if blockList is not None:
+            self._graph_list = lt
+        drv = self.driver
+        check(lib().gb_step_graph_host(n, _ptr(lt), int(cool), _ptr(drv), _ptr(self.status), C.byref(io),
+                                       _stream()), "gb_step_graph_host")
         return drv[self.DRV_DT:self.DRV_DT + 1]
 
     def evolve_step(self, dt: float, cool: bool, blockList=None):
