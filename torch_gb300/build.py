@@ -19,12 +19,15 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbhydro.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-# unit -> extra flags
+# unit -> extra flags (the mixed unit's FP32 reconstruction and Riemann
+# arithmetic uses the approximate FP32 division and square root: a few ulp
+# against the correctly rounded ones, far inside the mixed path's
+# tolerance; its FP64 update is unaffected)
 UNITS = {
     "capi.cu": ["-fmad=false"],
     "cool.cu": ["-fmad=false"],
     "hydro_fp64.cu": ["-fmad=false"],
-    "hydro_mixed.cu": [],
+    "hydro_mixed.cu": ["-prec-div=false", "-prec-sqrt=false"],
     "mlp.cu": [],
     "noalloc.cu": ["-fmad=false"],
 }
