@@ -690,14 +690,18 @@ __global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restri
 // entries (its block, its region), computes 32-bit level-local indices and
 // takes at most one step down the tree; the results are those of the walks
 // from the root above, value for value.
+// STEP: only the guard cells a step reads (the region of gb_step_cell);
+// otherwise all of them (FLASH's guard fill)
+template <bool STEP>
 __global__ void __launch_bounds__(128) k_guard_cells_plan(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list,
                                                           guard_vars gv, const int4* __restrict__ plan)
 {
     const int blk = list[blockIdx.y];
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= cell_slabs::COUNT) return;
+    if (q >= (STEP ? GB_STEP_GUARD_CELLS : cell_slabs::COUNT)) return;
     int I[3];
-    cell_slabs::at(q, I[0], I[1], I[2]);
+    if (STEP) gb_step_guard_cell(q, I[0], I[1], I[2]);
+    else cell_slabs::at(q, I[0], I[1], I[2]);
     const int r = region_of(I[0]) + 3 * region_of(I[1]) + 9 * region_of(I[2]);
     const int4* pb = plan + (size_t)blk * 54;
     const int4 se = __ldg(pb + 26), sc = __ldg(pb + 27);  // region 13: the block itself
@@ -744,12 +748,19 @@ __global__ void __launch_bounds__(128) k_guard_cells_plan(gb_dev_grid g, gb_tree
         if (q2 < gv.n) dst[(int64_t)gv.slot[q2] * GB_N3] = val[q2];
 }
 
-template <int AX>
+template <int AX, bool STEP>
 __device__ __forceinline__ void guard_face_plan(const gb_dev_grid& g, const gb_tree_desc& t, int blk, int q,
                                                 const int4* __restrict__ pb)
 {
     int I[3];
-    face_slabs<AX>::at(q, I[0], I[1], I[2]);
+    if (STEP) {
+        step_face_shell<AX>::at(q, I[0], I[1], I[2]);
+        I[0] += GB_BAND_LO;
+        I[1] += GB_BAND_LO;
+        I[2] += GB_BAND_LO;
+    } else {
+        face_slabs<AX>::at(q, I[0], I[1], I[2]);
+    }
     const int r = region_of(I[0]) + 3 * region_of(I[1]) + 9 * region_of(I[2]);
     const int4 se = __ldg(pb + 26), sc = __ldg(pb + 27);
     const int4 e = __ldg(pb + 2 * r), ec = __ldg(pb + 2 * r + 1);
@@ -814,19 +825,20 @@ __device__ __forceinline__ void guard_face_plan(const gb_dev_grid& g, const gb_t
     }
 }
 
+template <bool STEP>
 __global__ void __launch_bounds__(128) k_guard_faces_plan(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list,
                                                           const int4* __restrict__ plan)
 {
     const int blk = list[blockIdx.y];
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= GB_NGF) return;
+    if (q >= (STEP ? GB_STEP_GUARD_FACES : GB_NGF)) return;
     const int4* pb = plan + (size_t)blk * 54;
     if (blockIdx.z == 0)
-        guard_face_plan<0>(g, t, blk, q, pb);
+        guard_face_plan<0, STEP>(g, t, blk, q, pb);
     else if (blockIdx.z == 1)
-        guard_face_plan<1>(g, t, blk, q, pb);
+        guard_face_plan<1, STEP>(g, t, blk, q, pb);
     else
-        guard_face_plan<2>(g, t, blk, q, pb);
+        guard_face_plan<2, STEP>(g, t, blk, q, pb);
 }
 
 __global__ void k_dt_init(unsigned long long* bits) { *bits = 0x7FF0000000000000ULL; }  // +inf
@@ -1144,14 +1156,18 @@ static const int4* guard_plan(cudaStream_t s)
 
 static guard_vars hydro_guard_vars();
 
-// guard cells and (when face fields exist) guard faces of the listed blocks
-static void launch_guard_kernels(int nblk, const int* list, bool faces, cudaStream_t s)
+// guard cells and (when face fields exist) guard faces of the listed
+// blocks; step: only those a step reads
+static void launch_guard_kernels(int nblk, const int* list, bool faces, bool step, cudaStream_t s)
 {
     const int4* plan = guard_plan(s);
     gb_prof_begin(GBP_GUARD, s);
-    if (plan) {
-        k_guard_cells_plan<<<dim3((cell_slabs::COUNT + 127) / 128, nblk), 128, 0, s>>>(g_gb.grid, g_gb.tree, list,
-                                                                                      hydro_guard_vars(), plan);
+    if (plan && step) {
+        k_guard_cells_plan<true><<<dim3((GB_STEP_GUARD_CELLS + 127) / 128, nblk), 128, 0, s>>>(
+            g_gb.grid, g_gb.tree, list, hydro_guard_vars(), plan);
+    } else if (plan) {
+        k_guard_cells_plan<false><<<dim3((cell_slabs::COUNT + 127) / 128, nblk), 128, 0, s>>>(
+            g_gb.grid, g_gb.tree, list, hydro_guard_vars(), plan);
     } else {
         k_guard_cells<<<dim3((GB_NGC + 127) / 128, nblk), 128, 0, s>>>(g_gb.grid, g_gb.tree, list,
                                                                         hydro_guard_vars());
@@ -1159,8 +1175,12 @@ static void launch_guard_kernels(int nblk, const int* list, bool faces, cudaStre
     gb_prof_end(GBP_GUARD, s);
     if (!faces) return;
     gb_prof_begin(GBP_GUARD, s);
-    if (plan)
-        k_guard_faces_plan<<<dim3((GB_NGF + 127) / 128, nblk, 3), 128, 0, s>>>(g_gb.grid, g_gb.tree, list, plan);
+    if (plan && step)
+        k_guard_faces_plan<true><<<dim3((GB_STEP_GUARD_FACES + 127) / 128, nblk, 3), 128, 0, s>>>(g_gb.grid, g_gb.tree,
+                                                                                                list, plan);
+    else if (plan)
+        k_guard_faces_plan<false><<<dim3((GB_NGF + 127) / 128, nblk, 3), 128, 0, s>>>(g_gb.grid, g_gb.tree, list,
+                                                                                      plan);
     else
         k_guard_faces<<<dim3((GB_FSZ + 127) / 128, nblk, 3), 128, 0, s>>>(g_gb.grid, g_gb.tree, list);
     gb_prof_end(GBP_GUARD, s);
@@ -1178,7 +1198,7 @@ static guard_vars hydro_guard_vars()
 
 int gb_launch_guardfill(int nblk, const int* list, cudaStream_t s)
 {
-    launch_guard_kernels(nblk, list, g_gb.hp.mhd && g_gb.grid.f[0], s);
+    launch_guard_kernels(nblk, list, g_gb.hp.mhd && g_gb.grid.f[0], true, s);
     return gb_check(cudaGetLastError(), "guard fill") ? GB_ERR_CUDA : GB_OK;
 }
 
@@ -1191,7 +1211,7 @@ extern "C" int gb_fill_guardcells(int blockCount, const int* list, void* stream)
     if (blockCount < 0 || (blockCount > 0 && !list)) return GB_ERR_ARG;
     if (blockCount == 0) return GB_OK;
     // the face pass runs whenever the grid has face fields
-    launch_guard_kernels(blockCount, list, g_gb.grid.f[0] && g_gb.grid.f[1] && g_gb.grid.f[2],
+    launch_guard_kernels(blockCount, list, g_gb.grid.f[0] && g_gb.grid.f[1] && g_gb.grid.f[2], false,
                          (cudaStream_t)stream);
     return gb_check(cudaGetLastError(), "guard fill") ? GB_ERR_CUDA : GB_OK;
 }

@@ -10,6 +10,104 @@
 #define GB_N3 (GB_NB * GB_NB * GB_NB)
 #define GB_FSZ (GB_NB * GB_NB * (GB_NB + 1))
 
+// ---------------------------------------------------------------- the step's read region
+// Every cell and face a step reads, per block: the reconstruction band
+// (cells 3..20 on every axis) and the 5-point stencil's reach along one
+// axis at a time (cells 1, 2, 21, 22 on that axis, 3..20 on the others);
+// faces 3..21 along their normal and 3..20 across. The step's guard fill
+// and its FP32 primitive copy cover only this region; guard layers 0 and
+// 23 and the stencil-free corners are never read by a step.
+constexpr int GB_BAND_LO = GB_NGUARD - 1, GB_BAND = GB_NXB + 2;            // 3, 18
+constexpr int GB_ARM = 4 * GB_BAND * GB_BAND;                              // cells per axis arm set
+constexpr int GB_STEP_CELLS = GB_BAND * GB_BAND * GB_BAND + 3 * GB_ARM;    // 9720
+constexpr int GB_STEP_FACES = (GB_BAND + 1) * GB_BAND * GB_BAND;           // per axis, 6156
+
+// The q-th position of the shell of width W of an N0 x N1 x N2 box (box
+// coordinates): the two z slabs, the two y slabs inside them, the two x
+// slabs inside those, x fastest.
+template <int N0, int N1, int N2, int W>
+struct shell_slabs {
+    static constexpr int NI0 = N0 - 2 * W, NI1 = N1 - 2 * W, NI2 = N2 - 2 * W;
+    static constexpr int NZ = 2 * W * N1 * N0, NY = NI2 * 2 * W * N0, NX = NI2 * NI1 * 2 * W;
+    static constexpr int COUNT = NZ + NY + NX;
+    __device__ __forceinline__ static void at(int q, int& i, int& j, int& k)
+    {
+        if (q < NZ) {
+            const int zz = q / (N1 * N0), rr = q - zz * (N1 * N0);
+            k = zz < W ? zz : NI2 + zz;
+            j = rr / N0;
+            i = rr - j * N0;
+        } else if (q < NZ + NY) {
+            q -= NZ;
+            const int kk = q / (2 * W * N0), rr = q - kk * (2 * W * N0);
+            const int yy = rr / N0;
+            k = W + kk;
+            j = yy < W ? yy : NI1 + yy;
+            i = rr - yy * N0;
+        } else {
+            q -= NZ + NY;
+            const int xx = q % (2 * W), rr = q / (2 * W);
+            i = xx < W ? xx : NI0 + xx;
+            j = W + rr % NI1;
+            k = W + rr / NI1;
+        }
+    }
+};
+
+// arm cell a of the stencil reach (a < 3 GB_ARM): one axis at 1, 2, 21 or 22
+__device__ __forceinline__ void gb_arm_cell(int a, int& i, int& j, int& k)
+{
+    const int d = a / GB_ARM, r = a - d * GB_ARM;
+    auto arm = [](int l) { return l < 2 ? GB_BAND_LO - 2 + l : GB_BAND_LO + GB_BAND + (l - 2); };
+    if (d == 0) {
+        i = arm(r & 3);
+        j = GB_BAND_LO + (r >> 2) % GB_BAND;
+        k = GB_BAND_LO + (r >> 2) / GB_BAND;
+    } else if (d == 1) {
+        i = GB_BAND_LO + r % GB_BAND;
+        j = arm((r / GB_BAND) & 3);
+        k = GB_BAND_LO + r / (4 * GB_BAND);
+    } else {
+        i = GB_BAND_LO + r % GB_BAND;
+        j = GB_BAND_LO + (r / GB_BAND) % GB_BAND;
+        k = arm(r / (GB_BAND * GB_BAND));
+    }
+}
+
+// q-th cell of the step's read region (q < GB_STEP_CELLS): band, then arms
+__device__ __forceinline__ void gb_step_cell(int q, int& i, int& j, int& k)
+{
+    constexpr int NB = GB_BAND * GB_BAND * GB_BAND;
+    if (q < NB) {
+        i = GB_BAND_LO + q % GB_BAND;
+        j = GB_BAND_LO + (q / GB_BAND) % GB_BAND;
+        k = GB_BAND_LO + q / (GB_BAND * GB_BAND);
+    } else {
+        gb_arm_cell(q - NB, i, j, k);
+    }
+}
+
+// guard cells of the step's read region: the band's shell, then the arms
+using band_shell = shell_slabs<GB_BAND, GB_BAND, GB_BAND, 1>;
+constexpr int GB_STEP_GUARD_CELLS = band_shell::COUNT + 3 * GB_ARM;  // 5624
+__device__ __forceinline__ void gb_step_guard_cell(int q, int& i, int& j, int& k)
+{
+    if (q < band_shell::COUNT) {
+        band_shell::at(q, i, j, k);
+        i += GB_BAND_LO;
+        j += GB_BAND_LO;
+        k += GB_BAND_LO;
+    } else {
+        gb_arm_cell(q - band_shell::COUNT, i, j, k);
+    }
+}
+
+// guard faces of axis A in the step's read region: the shell of the box
+// normal 3..21, across 3..20
+template <int A>
+using step_face_shell = shell_slabs<GB_BAND + (A == 0), GB_BAND + (A == 1), GB_BAND + (A == 2), 1>;
+constexpr int GB_STEP_GUARD_FACES = (GB_BAND + 1) * GB_BAND * GB_BAND - (GB_NXB + 1) * GB_NXB * GB_NXB;  // 1804
+
 // Guard-fill plan entry flags (the plan: for every leaf and each of the 27
 // block-sized regions around it, two int4 {node, level, flags, 0},
 // {cx, cy, cz, 0}; region r = rx + 3 ry + 9 rz, offsets -1..1 per axis)

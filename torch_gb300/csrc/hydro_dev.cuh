@@ -57,31 +57,35 @@ template <bool MHD>
 __global__ void __launch_bounds__(128)
 k_prim32(gb_dev_grid g, const int* __restrict__ list, float* __restrict__ p32, size_t stride)
 {
+    // threads [0, GB_STEP_CELLS): the cells of the step's read region;
+    // then (MHD) 3 x GB_STEP_FACES faces: normal 3..21, across 3..20
     const int cb = blockIdx.y;
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= GB_N3) return;
-    const double* base = g.unk + (int64_t)list[cb] * g.nvar * GB_N3 + c;
-    float* out = p32 + (size_t)cb * stride + c;
-    const int roles[NP32] = {GB_DENS, GB_VELX, GB_VELY, GB_VELZ, GB_PRES, GB_MAGX, GB_MAGY, GB_MAGZ, GB_EINT};
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < GB_STEP_CELLS) {
+        int i, j, k;
+        gb_step_cell(q, i, j, k);
+        const int c = gb_cidx(i, j, k);
+        const double* base = g.unk + (int64_t)list[cb] * g.nvar * GB_N3 + c;
+        float* out = p32 + (size_t)cb * stride + c;
+        const int roles[NP32] = {GB_DENS, GB_VELX, GB_VELY, GB_VELZ, GB_PRES, GB_MAGX, GB_MAGY, GB_MAGZ, GB_EINT};
 #pragma unroll
-    for (int v = 0; v < NP32; ++v) {
-        if (!MHD && v >= 5 && v < 8) {
-            out[(size_t)v * GB_N3] = 0.0f;
-            continue;
+        for (int v = 0; v < NP32; ++v) {
+            if (!MHD && v >= 5 && v < 8) {
+                out[(size_t)v * GB_N3] = 0.0f;
+                continue;
+            }
+            out[(size_t)v * GB_N3] = gb_d2f(base[(int64_t)g.slot[roles[v]] * GB_N3]);
         }
-        out[(size_t)v * GB_N3] = gb_d2f(base[(int64_t)g.slot[roles[v]] * GB_N3]);
+        return;
     }
-    if (MHD) {
-        // face B (GB_FSZ = 14400 > GB_N3 = 13824: the last threads of the
-        // grid cover the rest below)
-        float* fo = p32 + (size_t)cb * stride + (size_t)NP32 * GB_N3;
-        const int64_t fb = (int64_t)list[cb] * GB_FSZ;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            fo[(size_t)a * GB_FSZ + c] = gb_d2f(g.f[a][fb + c]);
-            if (c < GB_FSZ - GB_N3) fo[(size_t)a * GB_FSZ + GB_N3 + c] = gb_d2f(g.f[a][fb + GB_N3 + c]);
-        }
-    }
+    q -= GB_STEP_CELLS;
+    if (!MHD || q >= 3 * GB_STEP_FACES) return;
+    const int a = q / GB_STEP_FACES, e = q - a * GB_STEP_FACES;
+    const int nx = GB_BAND + (a == 0), ny = GB_BAND + (a == 1);
+    const int fi = gb_fidx(a, GB_BAND_LO + e % nx, GB_BAND_LO + (e / nx) % ny, GB_BAND_LO + e / (nx * ny));
+    const double* fa = a == 0 ? g.f[0] : (a == 1 ? g.f[1] : g.f[2]);
+    p32[(size_t)cb * stride + (size_t)NP32 * GB_N3 + (size_t)a * GB_FSZ + fi] =
+        gb_d2f(fa[(int64_t)list[cb] * GB_FSZ + fi]);
 }
 
 // face B of the padded block for reconstruction precision T: the FP32
