@@ -395,7 +395,36 @@ struct sur_units {
     double e_of_T;     // its inverse: TtoEI
     double inv_mu_mp;  // 1 / (mu_mol m_p)
     double vel2, inv_vel2;
+    // FP32 copies for the surrogate kernels, whose per-cell inputs go
+    // straight to FP32 (FP64 instructions are the scarce resource there)
+    float dens_unit_f, T_of_e_f, e_of_T_f, inv_mu_mp_f, time_unit_f, mu_mol_f, xHp_const_f;
+    float emin_f;  // 0.5 absTmin TtoEI, the energy floor of the iteration
+    float absTmin_f, absTmax_f, dust_sputter_f, smallp_f, T_min_f, nd_min_f;
+    double smallp, dens_unit;
 };
+
+// The inputs of the surrogate kernels for one cell in FP32: the FP64
+// state is converted on the integer pipe and scaled in FP32. Only the
+// internal energy is also kept in FP64 (the accepted energy is formed from
+// it in FP64). Each FP32 input is within a couple of ulp of the rounded
+// FP64 value the plain loader makes.
+__device__ __forceinline__ void sur_load_f32(const gb_dev_grid& g, const gb_cool_pf& pf, const sur_units& u, int blk,
+                                             int ci, gb_cool_varsf& f, double& ei, float& eif, float& tempf)
+{
+    ei = gb_var(g, blk, GB_EINT)[ci] * u.vel2;
+    eif = gb_d2f(ei);
+    tempf = eif * u.T_of_e_f;
+    f.rho = gb_d2f(gb_var(g, blk, GB_DENS)[ci]) * u.dens_unit_f;
+    f.ndens = f.rho * u.inv_mu_mp_f;
+    f.conf = f.ndens * u.inv_mu_mp_f;  // ndens^2 / rho
+    f.tdust = gb_d2f(gb_var(g, blk, GB_TDUS)[ci]);
+    f.xHp = g.slot[GB_IHP] >= 0 ? gb_d2f(gb_var(g, blk, GB_IHP)[ci]) : u.xHp_const_f;
+    f.ephen = g.slot[GB_PHHE] >= 0 ? gb_d2f(gb_var(g, blk, GB_PHHE)[ci]) / f.rho : 0.0f;
+    f.Gflux = g.slot[GB_PEFL] >= 0 ? gb_d2f(gb_var(g, blk, GB_PEFL)[ci]) : 0.0f;
+    f.TtoEI = u.e_of_T_f;
+    f.mu_mol = u.mu_mol_f;
+    f.cr_pref = pf.crRE * (f.ndens / f.rho);
+}
 
 __device__ __forceinline__ void sur_load_fast(const gb_dev_grid& g, const gb_cool_ctx& c, const sur_units& u, int blk,
                                               int ci, gb_cool_vars& v, double& ei, double& temp)
@@ -433,6 +462,26 @@ __device__ __forceinline__ void sur_store_fast(const gb_dev_grid& g, const gb_co
     if (g.slot[GB_PEFL] >= 0) gb_var(g, blk, GB_PEFL)[ci] = 0.0;
 }
 
+// the accepted state of one cell: the FP64 update of the internal energy
+// and what follows from it (total energy, pressure, temperature); the
+// energy floor is tested in FP32 and taken in FP64 when it applies. The
+// dust temperature is written only when it changed (new_tdust).
+__device__ __forceinline__ void sur_store_f32(const gb_dev_grid& g, const sur_units& u, double gamma, int blk, int ci,
+                                              float rhof, bool new_tdust, float tdust, double ei, double temp)
+{
+    double rho = gb_var(g, blk, GB_DENS)[ci];
+    if (gb_d2f(ei) * rhof < u.smallp_f) ei = u.smallp / (rho * u.dens_unit);
+    double vx = gb_var(g, blk, GB_VELX)[ci], vy = gb_var(g, blk, GB_VELY)[ci], vz = gb_var(g, blk, GB_VELZ)[ci];
+    double e = ei * u.inv_vel2;
+    gb_var(g, blk, GB_EINT)[ci] = e;
+    gb_var(g, blk, GB_ENER)[ci] = e + 0.5 * (vx * vx + vy * vy + vz * vz);
+    gb_var(g, blk, GB_PRES)[ci] = (gamma - 1.0) * rho * e;
+    gb_var(g, blk, GB_TEMP)[ci] = temp;
+    if (new_tdust) gb_var(g, blk, GB_TDUS)[ci] = gb_f2d(tdust);
+    if (g.slot[GB_PHHE] >= 0) gb_var(g, blk, GB_PHHE)[ci] = 0.0;
+    if (g.slot[GB_PEFL] >= 0) gb_var(g, blk, GB_PEFL)[ci] = 0.0;
+}
+
 __device__ __forceinline__ void cell_of(int64_t idx, const int* list, int& blk, int& ci, int& i, int& j, int& k)
 {
     int cb = (int)(idx / 4096), t = (int)(idx % 4096);
@@ -453,17 +502,15 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_unit
     if (dtp) dt_code = *dtp;
     int blk, ci, i, j, k;
     cell_of(idx, list, blk, ci, i, j, k);
-    gb_cool_vars v;
-    double ei, temp;
-    sur_load_fast(g, c, un, blk, ci, v, ei, temp);
     gb_cool_varsf vf;
-    gbcoolf::make_vars(pf, v, vf);
-    const gb_cool_tabf tf = {c.Tf, c.nf, c.lamf, (float)c.T_min, (float)c.nd_min};
+    double ei;
+    float eif, tempf;
+    sur_load_f32(g, pf, un, blk, ci, vf, ei, eif, tempf);
+    const gb_cool_tabf tf = {c.Tf, c.nf, c.lamf, un.T_min_f, un.nd_min_f};
     const float fl = gbcoolf::cooling_floor(pf, tf, vf);
     float gam, lam;
-    const float eif = gb_d2f(ei);
     float f0 = gbcoolf::dei_parts(pf, tf, vf, fl, eif, &gam, &lam);
-    const float dt = gb_d2f(dt_code * c.p.time_unit);
+    const float dt = gb_d2f(dt_code) * un.time_unit_f;
     // features in FP32: dt / t_cool = dt |f| / e
     const float r = dt * fabsf(f0) / eif;
     float lr = log10f(fmaxf(r, 1e-30f));
@@ -472,7 +519,7 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_unit
     lh = fminf(fmaxf(lh, (float)-gbsur::H_CLAMP), (float)gbsur::H_CLAMP);
     reinterpret_cast<float4*>(feat)[idx] =
         make_float4((log10f(vf.ndens) - (float)gbsur::N_MID) / (float)gbsur::N_HALF,
-                    (log10f(gb_d2f(temp)) - (float)gbsur::T_MID) / (float)gbsur::T_HALF, lr / (float)gbsur::R_HALF,
+                    (log10f(tempf) - (float)gbsur::T_MID) / (float)gbsur::T_HALF, lr / (float)gbsur::R_HALF,
                     lh / (float)gbsur::H_HALF);
     f0out[idx] = make_float2(f0, fl);
 }
@@ -498,30 +545,28 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_un
     int blk, ci, i, j, k;
     cell_of(idx, list, blk, ci, i, j, k);
     const gb_cool_params& p = c.p;
-    gb_cool_vars v;
-    double ei0, temp0;
-    sur_load_fast(g, c, un, blk, ci, v, ei0, temp0);
     gb_cool_varsf vf;
-    gbcoolf::make_vars(pf, v, vf);
-    const gb_cool_tabf tf = {c.Tf, c.nf, c.lamf, (float)c.T_min, (float)c.nd_min};
-    const double dt = dt_code * p.time_unit;
-    const float dtf = gb_d2f(dt);
+    double ei0;
+    float e0f, temp0f;
+    sur_load_f32(g, pf, un, blk, ci, vf, ei0, e0f, temp0f);
+    const gb_cool_tabf tf = {c.Tf, c.nf, c.lamf, un.T_min_f, un.nd_min_f};
+    const float dtf = gb_d2f(dt_code) * un.time_unit_f;
+    const float rtol = (float)rel_tol;
     const float2 f0fl = f0a[idx];
     const float f0 = f0fl.x;
     const float flf = f0fl.y;
-    const double emin_ = 0.5 * p.absTmin * v.TtoEI;
-    double Tp = gb_f2d(gb_d2f(temp0) * exp10f((float)gbsur::Y_SCALE * y[idx]));
-    bool ok = isfinite(Tp) && Tp > 0.0;
+    const float Tp = temp0f * exp10f((float)gbsur::Y_SCALE * y[idx]);
+    bool ok = isfinite(Tp) && Tp > 0.0f;
     double ein = 0.0;
+    float xfin = 0.0f;
     if (ok) {
         // secant-Newton from the prediction, in FP32 on the change of the
         // energy x = e - e_old (the backward-Euler residual is then
         // g = x - dt f, with no cancellation against e_old); e is formed in
         // FP64 once at the end
-        const float e0f = gb_d2f(ei0);
-        const float xmin = gb_d2f(emin_ - ei0);
+        const float xmin = un.emin_f - e0f;
         float xa = 0.0f, fa = f0;
-        float xb = gb_d2f(fmax(Tp * v.TtoEI, emin_) - ei0);
+        float xb = fmaxf(Tp * un.e_of_T_f, un.emin_f) - e0f;
         float J = 1.0f;
         bool conv = false;
         for (int it = 0; it < 4; ++it) {
@@ -541,41 +586,50 @@ __global__ void k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_un
             xb = xn;
             // the correction is small and the secant slope local (its two
             // points within 5 % of each other)
-            if (fabsf(xb - xa) <= 0.25f * (float)rel_tol * (e0f + xb) && fabsf(de) <= 0.05f * (e0f + xa)) {
+            if (fabsf(xb - xa) <= 0.25f * rtol * (e0f + xb) && fabsf(de) <= 0.05f * (e0f + xa)) {
                 conv = true;
                 break;
             }
         }
         const double eb = ei0 + gb_f2d(xb);
+        xfin = xb;
         // the converged FP32 iterate is the answer; optionally re-check the
         // backward-Euler residual (heatCool.F90:1928-1950) in FP64 with the
         // last secant slope
         if (conv && CHECK64) {
+            gb_cool_vars v;
+            double e64, t64;
+            sur_load_fast(g, c, un, blk, ci, v, e64, t64);
+            const double dt = dt_code * p.time_unit;
             double f64 = dei_dt(c, v, cooling_floor(c, v), eb);
             double g64 = eb - dt * f64 - ei0;
             double delta = g64 / (double)J;
             ein = eb - delta;
+            xfin = gb_d2f(ein - ei0);
             ok = isfinite(ein) && ein > 0.0 && fabs(delta) <= rel_tol * ein;
         } else {
             ein = eb;
-            ok = conv && isfinite(ein) && ein > 0.0;
+            ok = conv && isfinite(xb) && e0f + xb > 0.0f;
         }
         // the solution moves the way the rate at the old state points
-        if (ok && f0 < 0.0 && ein > ei0 * (1.0 + rel_tol)) ok = false;
-        if (ok && f0 > 0.0 && ein < ei0 * (1.0 - rel_tol)) ok = false;
+        if (ok && f0 < 0.0f && xfin > e0f * rtol) ok = false;
+        if (ok && f0 > 0.0f && xfin < -e0f * rtol) ok = false;
     }
     if (ok) {
         double temp = ein * un.T_of_e;
-        if (temp < p.absTmin) {
+        float tempf = gb_d2f(temp);
+        if (tempf < un.absTmin_f) {
             temp = p.absTmin;
-            ein = p.absTmin * v.TtoEI;
+            tempf = un.absTmin_f;
+            ein = p.absTmin * un.e_of_T;
         }
-        if (p.useDustCool && temp <= p.dust_sputter_temp) v.tdust = gbcoolf::dust_temperature(pf, vf, (float)temp, vf.tdust);
-        if (temp > p.absTmax) {
-            ein = p.absTmax * v.TtoEI;
+        const bool dust = p.useDustCool && tempf <= un.dust_sputter_f;
+        const float tdust = dust ? gbcoolf::dust_temperature(pf, vf, tempf, vf.tdust) : 0.0f;
+        if (tempf > un.absTmax_f) {
+            ein = p.absTmax * un.e_of_T;
             temp = p.absTmax;
         }
-        sur_store_fast(g, c, un, gamma, blk, ci, v, ein, temp);
+        sur_store_f32(g, un, gamma, blk, ci, vf.rho, dust, tdust, ein, temp);
     } else {
         int slot = atomicAdd(nrej, 1);
         rej[slot] = (int)idx;
@@ -711,6 +765,22 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp,
         un.inv_mu_mp = 1.0 / (p.mu_mol * p.mp);
         un.vel2 = p.vel_unit * p.vel_unit;
         un.inv_vel2 = 1.0 / un.vel2;
+        un.dens_unit_f = (float)p.dens_unit;
+        un.T_of_e_f = (float)un.T_of_e;
+        un.e_of_T_f = (float)un.e_of_T;
+        un.inv_mu_mp_f = (float)un.inv_mu_mp;
+        un.time_unit_f = (float)p.time_unit;
+        un.mu_mol_f = (float)p.mu_mol;
+        un.xHp_const_f = (float)p.xHp_const;
+        un.emin_f = (float)(0.5 * p.absTmin * un.e_of_T);
+        un.absTmin_f = (float)p.absTmin;
+        un.absTmax_f = (float)p.absTmax;
+        un.dust_sputter_f = (float)p.dust_sputter_temp;
+        un.smallp_f = (float)p.smallp;
+        un.smallp = p.smallp;
+        un.dens_unit = p.dens_unit;
+        un.T_min_f = (float)g_gb.cool.T_min;
+        un.nd_min_f = (float)g_gb.cool.nd_min;
     }
     k_sur_feat<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, un, list, ncell, dt, dtp, g_sb.feat, g_sb.f0);
     gb_prof_end(GBP_SUR_FEAT, s);
