@@ -1372,6 +1372,7 @@ static gbh::hydro_kparams make_kp(double dt, const double* dtp = nullptr)
     for (int d = 0; d < 3; ++d) {
         kp.dtdx0[d] = dt / kp.dx[d];
         kp.dtdxf0[d] = (float)kp.dtdx0[d];
+        kp.iso = kp.dx[0] == kp.dx[1] && kp.dx[1] == kp.dx[2];
     }
     return kp;
 }

@@ -374,6 +374,9 @@ struct hydro_kparams {
     // edge electric fields at fine-coarse boundaries (MHD with flux
     // conservation; null: off): the guard-fill plan, the tree's child
     // table and the surface-edge registers (NSURF doubles per tree node)
+    // cubic cells (dx = dy = dz at every level): the mixed update sums the
+    // three directions' flux differences before one FP64 scaling
+    int iso = 0;
     const int4* ec_plan = nullptr;
     const int* ec_near = nullptr;  // per node: bit 0 a coarser leaf around it, bit 1 a finer one
     const int* ec_child = nullptr;
@@ -1247,6 +1250,47 @@ k_fc_get(const int* __restrict__ list, const int* __restrict__ links, const T* _
 }
 
 // ---------------------------------------------------------------- k_update
+// Error-free transformation of an FP32 sum (Knuth's TwoSum): s + e == a + b
+// exactly, s the rounded sum (needs round-to-nearest adds, no reassociation).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// (ap - am) + (bp - bm) + (cp - cm) of six FP32 fluxes as a double: the
+// cascaded TwoSum of Ogita, Rump and Oishi (SIAM J. Sci. Comput. 26, 2005,
+// "Sum2"), accurate as if summed in twice FP32's precision (relative error
+// about 2^-48 of the sum of magnitudes), then one FP64 addition. It
+// replaces three FP64 subtractions and two FP64 additions.
+__device__ __forceinline__ double flux_div(float ap, float am, float bp, float bm, float cp, float cm)
+{
+    float s0, e0, s1, e1, s2, e2, t, e3, S, e4;
+    two_sum(ap, -am, s0, e0);
+    two_sum(bp, -bm, s1, e1);
+    two_sum(cp, -cm, s2, e2);
+    two_sum(s0, s1, t, e3);
+    two_sum(t, s2, S, e4);
+    const float E = (((e0 + e1) + e2) + e3) + e4;
+    return gb_f2d(S) + gb_f2d(E);
+}
+
+// 1 / x in FP64 from an FP32 seed and two Newton-Raphson steps
+// (y <- y + y (1 - x y); each step doubles the correct bits: about 2^-22,
+// 2^-44, 2^-88), for x inside FP32's normal range; an FP64 division
+// otherwise.
+__device__ __forceinline__ double rcp_newton(double x)
+{
+    const float xf = gb_d2f(x);
+    if (!(fabsf(xf) > 1e-30f && fabsf(xf) < 1e30f)) return 1.0 / x;
+    double y = gb_f2d(1.0f / xf);
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
 template <typename T, bool MHD, bool COOL>
 __global__ void __launch_bounds__(128)
 k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restrict__ list,
@@ -1286,16 +1330,31 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
         if constexpr (std::is_same<T, float>::value) return gb_f2d(x);  // exact, on the integer pipe
         else return x;
     };
-    double Un[5];
+    double Un[5], dtdivv, ren;
+    if (RCP && kp.iso) {
+        // cubic cells: one FP64 scaling of the summed flux differences
+        auto Ff = [&](int d, int var, int idx) -> float {
+            return (float)fs[(size_t)d * NFLX * NFC + (size_t)var * NFC + idx];
+        };
+        auto div = [&](int var) {
+            return flux_div(Ff(0, var, fp[0]), Ff(0, var, fm[0]), Ff(1, var, fp[1]), Ff(1, var, fm[1]),
+                            Ff(2, var, fp[2]), Ff(2, var, fm[2]));
+        };
 #pragma unroll
-    for (int s = 0; s < 5; ++s)
-        Un[s] = Uc[s] - dtd[0] * (F(0, s, fp[0]) - F(0, s, fm[0])) - dtd[1] * (F(1, s, fp[1]) - F(1, s, fm[1])) -
-                dtd[2] * (F(2, s, fp[2]) - F(2, s, fm[2]));
-    // dt * div v from the face velocities, as sum_d (dt/dx_d) dv_d
-    double dtdivv = dtd[0] * (F(0, 9, fp[0]) - F(0, 9, fm[0])) + dtd[1] * (F(1, 9, fp[1]) - F(1, 9, fm[1])) +
-                    dtd[2] * (F(2, 9, fp[2]) - F(2, 9, fm[2]));
-    double ren = re - dtd[0] * (F(0, 8, fp[0]) - F(0, 8, fm[0])) - dtd[1] * (F(1, 8, fp[1]) - F(1, 8, fm[1])) -
-                 dtd[2] * (F(2, 8, fp[2]) - F(2, 8, fm[2])) - pr * dtdivv;
+        for (int s = 0; s < 5; ++s) Un[s] = fma(-dtd[0], div(s), Uc[s]);
+        dtdivv = dtd[0] * div(9);
+        ren = fma(-dtd[0], div(8), re) - pr * dtdivv;
+    } else {
+#pragma unroll
+        for (int s = 0; s < 5; ++s)
+            Un[s] = Uc[s] - dtd[0] * (F(0, s, fp[0]) - F(0, s, fm[0])) - dtd[1] * (F(1, s, fp[1]) - F(1, s, fm[1])) -
+                    dtd[2] * (F(2, s, fp[2]) - F(2, s, fm[2]));
+        // dt * div v from the face velocities, as sum_d (dt/dx_d) dv_d
+        dtdivv = dtd[0] * (F(0, 9, fp[0]) - F(0, 9, fm[0])) + dtd[1] * (F(1, 9, fp[1]) - F(1, 9, fm[1])) +
+                 dtd[2] * (F(2, 9, fp[2]) - F(2, 9, fm[2]));
+        ren = re - dtd[0] * (F(0, 8, fp[0]) - F(0, 8, fm[0])) - dtd[1] * (F(1, 8, fp[1]) - F(1, 8, fm[1])) -
+              dtd[2] * (F(2, 8, fp[2]) - F(2, 8, fm[2])) - pr * dtdivv;
+    }
     double Bn[3] = {0.0, 0.0, 0.0};
     if (MHD) {
         const double* bs = bscr + (size_t)cb * bstride;
@@ -1315,7 +1374,7 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
         if (k == HI) g.f[2][(int64_t)blk * GB_FSZ + gb_fidx(2, i, j, k + 1)] = bhi[2];
     }
     double rn = fmax(Un[0], kp.smlrho);
-    const double irn = RCP ? 1.0 / rn : 0.0;
+    const double irn = RCP ? rcp_newton(rn) : 0.0;
     auto over_rn = [&](double x) { return RCP ? x * irn : x / rn; };
     double ek = over_rn(0.5 * (Un[1] * Un[1] + Un[2] * Un[2] + Un[3] * Un[3]));
     double em = 0.5 * (Bn[0] * Bn[0] + Bn[1] * Bn[1] + Bn[2] * Bn[2]);
