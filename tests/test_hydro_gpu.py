@@ -74,11 +74,13 @@ def test_cfl_dt_matches_oracle(gb, oracle):
     assert g.compute_dt().item() == dt_o
 
 
-@pytest.mark.parametrize("mhd", [False, True])
-def test_conservation_and_divb(gb, oracle, mhd):
+@pytest.mark.parametrize("mhd,precision", [(False, 0), (True, 0), (False, 1), (True, 1)])
+def test_conservation_and_divb(gb, oracle, mhd, precision):
     """Periodic box: mass, momentum, energy at round-off (Mach 1, no
-    dual-energy switching) and div B at round-off after 5 steps."""
-    ic, g, p = _setup(gb, oracle, mhd, seed=5, mach=1.0, sig=0.3)
+    dual-energy switching) and div B at round-off after 5 steps, in FP64
+    and in the mixed path (FP32 fluxes summed in double-float, one FP64
+    scaling per cell)."""
+    ic, g, p = _setup(gb, oracle, mhd, seed=5, mach=1.0, sig=0.3, precision=precision)
     dx = ic["dx"]
 
     def totals():

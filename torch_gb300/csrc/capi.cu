@@ -732,15 +732,38 @@ __global__ void __launch_bounds__(128) k_guard_cells_plan(gb_dev_grid g, gb_tree
         const int bj = (A[1] << m) - (h.c[1] << LOG2_NXB) + GB_NGUARD;
         const int bk = (A[2] << m) - (h.c[2] << LOG2_NXB) + GB_NGUARD;
         const double inv = 1.0 / (double)(rr * rr * rr);
+        if (m == 1) {
+            // one level finer (every 2:1-balanced tree): the 8 loads of a
+            // variable are independent and issued together; the sum keeps
+            // the z, y, x order of the general loop below
+            const int c0 = gb_cidx(bi, bj, bk);
 #pragma unroll
-        for (int q2 = 0; q2 < GB_NROLE; ++q2) {
-            if (q2 >= gv.n) continue;
-            const double* sv = src + (int64_t)gv.slot[q2] * GB_N3;
-            double acc = 0.0;
-            for (int z = 0; z < rr; ++z)
-                for (int y = 0; y < rr; ++y)
-                    for (int x = 0; x < rr; ++x) acc += sv[gb_cidx(bi + x, bj + y, bk + z)];
-            val[q2] = acc * inv;
+            for (int q2 = 0; q2 < GB_NROLE; ++q2) {
+                if (q2 >= gv.n) continue;
+                const double* sv = src + (int64_t)gv.slot[q2] * GB_N3 + c0;
+                double w[8];
+#pragma unroll
+                for (int z = 0; z < 2; ++z)
+#pragma unroll
+                    for (int y = 0; y < 2; ++y)
+#pragma unroll
+                        for (int x = 0; x < 2; ++x) w[4 * z + 2 * y + x] = sv[x + GB_N * (y + GB_N * z)];
+                double acc = 0.0;
+#pragma unroll
+                for (int e = 0; e < 8; ++e) acc += w[e];
+                val[q2] = acc * inv;
+            }
+        } else {
+#pragma unroll
+            for (int q2 = 0; q2 < GB_NROLE; ++q2) {
+                if (q2 >= gv.n) continue;
+                const double* sv = src + (int64_t)gv.slot[q2] * GB_N3;
+                double acc = 0.0;
+                for (int z = 0; z < rr; ++z)
+                    for (int y = 0; y < rr; ++y)
+                        for (int x = 0; x < rr; ++x) acc += sv[gb_cidx(bi + x, bj + y, bk + z)];
+                val[q2] = acc * inv;
+            }
         }
     }
 #pragma unroll
@@ -814,13 +837,30 @@ __device__ __forceinline__ void guard_face_plan(const gb_dev_grid& g, const gb_t
         for (int d = 0; d < 3; ++d) B[d] = (A[d] << m) - (h.c[d] << LOG2_NXB) + GB_NGUARD;
         constexpr int t1 = AX == 0 ? 1 : 0, t2 = AX == 2 ? 1 : 2;
         double acc = 0.0;
-        for (int y = 0; y < rr; ++y)
-            for (int x = 0; x < rr; ++x) {
-                int Q[3] = {B[0], B[1], B[2]};
-                Q[t1] += x;
-                Q[t2] += y;
-                acc += src[gb_fidx(AX, Q[0], Q[1], Q[2])];
-            }
+        if (m == 1) {
+            // the four fine faces, loads issued together, summed in the
+            // order of the general loop
+            double w[4];
+#pragma unroll
+            for (int y = 0; y < 2; ++y)
+#pragma unroll
+                for (int x = 0; x < 2; ++x) {
+                    int Q[3] = {B[0], B[1], B[2]};
+                    Q[t1] += x;
+                    Q[t2] += y;
+                    w[2 * y + x] = src[gb_fidx(AX, Q[0], Q[1], Q[2])];
+                }
+            acc = ((acc + w[0]) + w[1]) + w[2];
+            acc += w[3];
+        } else {
+            for (int y = 0; y < rr; ++y)
+                for (int x = 0; x < rr; ++x) {
+                    int Q[3] = {B[0], B[1], B[2]};
+                    Q[t1] += x;
+                    Q[t2] += y;
+                    acc += src[gb_fidx(AX, Q[0], Q[1], Q[2])];
+                }
+        }
         *dst = acc / (double)(rr * rr);
     }
 }
