@@ -696,16 +696,21 @@ template <bool STEP>
 __global__ void __launch_bounds__(128) k_guard_cells_plan(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list,
                                                           guard_vars gv, const int4* __restrict__ plan)
 {
+    // every CTA serves one block: its 27 plan entries go to shared memory
+    // once, so a guard cell's only global loads before its data are none
+    // (or one child lookup next to a finer leaf)
+    __shared__ int4 pb[54];
     const int blk = list[blockIdx.y];
+    if (threadIdx.x < 54) pb[threadIdx.x] = __ldg(plan + (size_t)blk * 54 + threadIdx.x);
+    __syncthreads();
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= (STEP ? GB_STEP_GUARD_CELLS : cell_slabs::COUNT)) return;
     int I[3];
     if (STEP) gb_step_guard_cell(q, I[0], I[1], I[2]);
     else cell_slabs::at(q, I[0], I[1], I[2]);
     const int r = region_of(I[0]) + 3 * region_of(I[1]) + 9 * region_of(I[2]);
-    const int4* pb = plan + (size_t)blk * 54;
-    const int4 se = __ldg(pb + 26), sc = __ldg(pb + 27);  // region 13: the block itself
-    const int4 e = __ldg(pb + 2 * r), ec = __ldg(pb + 2 * r + 1);
+    const int4 se = pb[26], sc = pb[27];  // region 13: the block itself
+    const int4 e = pb[2 * r], ec = pb[2 * r + 1];
     const int L = se.y;
     const int cs[3] = {sc.x, sc.y, sc.z}, nr[3] = {t.nrx, t.nry, t.nrz};
     int A[3];
@@ -785,8 +790,8 @@ __device__ __forceinline__ void guard_face_plan(const gb_dev_grid& g, const gb_t
         face_slabs<AX>::at(q, I[0], I[1], I[2]);
     }
     const int r = region_of(I[0]) + 3 * region_of(I[1]) + 9 * region_of(I[2]);
-    const int4 se = __ldg(pb + 26), sc = __ldg(pb + 27);
-    const int4 e = __ldg(pb + 2 * r), ec = __ldg(pb + 2 * r + 1);
+    const int4 se = pb[26], sc = pb[27];
+    const int4 e = pb[2 * r], ec = pb[2 * r + 1];
     const int L = se.y;
     const int cs[3] = {sc.x, sc.y, sc.z}, nr[3] = {t.nrx, t.nry, t.nrz};
     int A[3];
@@ -801,9 +806,9 @@ __device__ __forceinline__ void guard_face_plan(const gb_dev_grid& g, const gb_t
         constexpr int stride = AX == 0 ? 1 : (AX == 1 ? 3 : 9);
         const int r2 = r + (region_of(I[AX] - 1) - region_of(I[AX])) * stride;
         if (r2 != r) {
-            const int4 e2 = __ldg(pb + 2 * r2);
+            const int4 e2 = pb[2 * r2];
             if (e2.x >= 0 && !(e2.z & GP_REFINED) && e2.y == L) {
-                const int4 ec2 = __ldg(pb + 2 * r2 + 1);
+                const int4 ec2 = pb[2 * r2 + 1];
                 h.node = e2.x;
                 h.level = L;
                 h.c[0] = ec2.x;
@@ -869,10 +874,12 @@ template <bool STEP>
 __global__ void __launch_bounds__(128) k_guard_faces_plan(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list,
                                                           const int4* __restrict__ plan)
 {
+    __shared__ int4 pb[54];
     const int blk = list[blockIdx.y];
+    if (threadIdx.x < 54) pb[threadIdx.x] = __ldg(plan + (size_t)blk * 54 + threadIdx.x);
+    __syncthreads();
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= (STEP ? GB_STEP_GUARD_FACES : GB_NGF)) return;
-    const int4* pb = plan + (size_t)blk * 54;
     if (blockIdx.z == 0)
         guard_face_plan<0, STEP>(g, t, blk, q, pb);
     else if (blockIdx.z == 1)
