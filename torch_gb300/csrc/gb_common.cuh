@@ -15,12 +15,76 @@
 // (cells 3..20 on every axis) and the 5-point stencil's reach along one
 // axis at a time (cells 1, 2, 21, 22 on that axis, 3..20 on the others);
 // faces 3..21 along their normal and 3..20 across. The step's guard fill
-// and its FP32 primitive copy cover only this region; guard layers 0 and
-// 23 and the stencil-free corners are never read by a step.
-constexpr int GB_BAND_LO = GB_NGUARD - 1, GB_BAND = GB_NXB + 2;            // 3, 18
-constexpr int GB_ARM = 4 * GB_BAND * GB_BAND;                              // cells per axis arm set
-constexpr int GB_STEP_CELLS = GB_BAND * GB_BAND * GB_BAND + 3 * GB_ARM;    // 9720
-constexpr int GB_STEP_FACES = (GB_BAND + 1) * GB_BAND * GB_BAND;           // per axis, 6156
+// and its FP32 primitive copy cover this region widened to whole 32-byte
+// sectors along x (full rows, or the 4-cell groups at either end of a
+// row): a partial sector would cost a read-modify-write of the sector in
+// HBM, more than the few cells the widening adds.
+constexpr int GB_BAND_LO = GB_NGUARD - 1, GB_BAND = GB_NXB + 2;  // 3, 18
+
+// guard cells: z slabs (k = 3, 20 with j = 1..22; k = 1, 2, 21, 22 with
+// j = 3..20), y slabs (k = 4..19; j = 1, 2, 3, 20, 21, 22), full rows in
+// x; x slabs (j, k = 4..19; i = 0..3, 20..23)
+constexpr int GSZ_A = 2 * (GB_N - 2) * GB_N, GSZ_B = 4 * GB_BAND * GB_N;
+constexpr int GSY = GB_NXB * 6 * GB_N, GSX = GB_NXB * GB_NXB * 8;
+constexpr int GB_STEP_GUARD_CELLS = GSZ_A + GSZ_B + GSY + GSX;  // 7136
+__device__ __forceinline__ void gb_step_guard_cell(int q, int& i, int& j, int& k)
+{
+    if (q < GSZ_A) {
+        const int zz = q / ((GB_N - 2) * GB_N), rr = q - zz * ((GB_N - 2) * GB_N);
+        k = zz ? GB_BAND_LO + GB_BAND - 1 : GB_BAND_LO;
+        j = 1 + rr / GB_N;
+        i = rr % GB_N;
+    } else if (q < GSZ_A + GSZ_B) {
+        q -= GSZ_A;
+        const int zz = q / (GB_BAND * GB_N), rr = q - zz * (GB_BAND * GB_N);
+        k = zz < 2 ? 1 + zz : GB_N - 5 + zz;  // 1, 2, 21, 22
+        j = GB_BAND_LO + rr / GB_N;
+        i = rr % GB_N;
+    } else if (q < GSZ_A + GSZ_B + GSY) {
+        q -= GSZ_A + GSZ_B;
+        const int kk = q / (6 * GB_N), rr = q - kk * (6 * GB_N);
+        const int yy = rr / GB_N;
+        k = GB_NGUARD + kk;
+        j = yy < 3 ? 1 + yy : GB_N - 7 + yy;  // 1, 2, 3, 20, 21, 22
+        i = rr % GB_N;
+    } else {
+        q -= GSZ_A + GSZ_B + GSY;
+        const int xx = q & 7, rr = q >> 3;
+        i = xx < 4 ? xx : GB_N - 8 + xx;  // 0..3, 20..23
+        j = GB_NGUARD + rr % GB_NXB;
+        k = GB_NGUARD + rr / GB_NXB;
+    }
+}
+
+// cells of the FP32 copy: whole rows (j, k) in the band, the y arms and
+// the z arms
+constexpr int GB_STEP_ROWS = GB_BAND * GB_BAND + 2 * 4 * GB_BAND;  // 468
+constexpr int GB_STEP_CELLS = GB_STEP_ROWS * GB_N;                  // 11232
+__device__ __forceinline__ void gb_step_cell(int q, int& i, int& j, int& k)
+{
+    const int row = q / GB_N;
+    i = q - row * GB_N;
+    if (row < GB_BAND * GB_BAND) {
+        j = GB_BAND_LO + row % GB_BAND;
+        k = GB_BAND_LO + row / GB_BAND;
+    } else if (row < GB_BAND * GB_BAND + 4 * GB_BAND) {
+        const int r = row - GB_BAND * GB_BAND, a = r / GB_BAND;
+        j = a < 2 ? 1 + a : GB_N - 5 + a;
+        k = GB_BAND_LO + r % GB_BAND;
+    } else {
+        const int r = row - GB_BAND * GB_BAND - 4 * GB_BAND, a = r / GB_BAND;
+        j = GB_BAND_LO + r % GB_BAND;
+        k = a < 2 ? 1 + a : GB_N - 5 + a;
+    }
+}
+
+// faces of the FP32 copy, per axis a: whole x rows, j = 3..20 (..21 for
+// a = 1), k = 3..20 (..21 for a = 2)
+__host__ __device__ constexpr int gb_step_faces(int a)
+{
+    return (GB_N + (a == 0)) * (GB_BAND + (a == 1)) * (GB_BAND + (a == 2));
+}
+constexpr int GB_STEP_FACES_ALL = gb_step_faces(0) + gb_step_faces(1) + gb_step_faces(2);
 
 // The q-th position of the shell of width W of an N0 x N1 x N2 box (box
 // coordinates): the two z slabs, the two y slabs inside them, the two x
@@ -53,54 +117,6 @@ struct shell_slabs {
         }
     }
 };
-
-// arm cell a of the stencil reach (a < 3 GB_ARM): one axis at 1, 2, 21 or 22
-__device__ __forceinline__ void gb_arm_cell(int a, int& i, int& j, int& k)
-{
-    const int d = a / GB_ARM, r = a - d * GB_ARM;
-    auto arm = [](int l) { return l < 2 ? GB_BAND_LO - 2 + l : GB_BAND_LO + GB_BAND + (l - 2); };
-    if (d == 0) {
-        i = arm(r & 3);
-        j = GB_BAND_LO + (r >> 2) % GB_BAND;
-        k = GB_BAND_LO + (r >> 2) / GB_BAND;
-    } else if (d == 1) {
-        i = GB_BAND_LO + r % GB_BAND;
-        j = arm((r / GB_BAND) & 3);
-        k = GB_BAND_LO + r / (4 * GB_BAND);
-    } else {
-        i = GB_BAND_LO + r % GB_BAND;
-        j = GB_BAND_LO + (r / GB_BAND) % GB_BAND;
-        k = arm(r / (GB_BAND * GB_BAND));
-    }
-}
-
-// q-th cell of the step's read region (q < GB_STEP_CELLS): band, then arms
-__device__ __forceinline__ void gb_step_cell(int q, int& i, int& j, int& k)
-{
-    constexpr int NB = GB_BAND * GB_BAND * GB_BAND;
-    if (q < NB) {
-        i = GB_BAND_LO + q % GB_BAND;
-        j = GB_BAND_LO + (q / GB_BAND) % GB_BAND;
-        k = GB_BAND_LO + q / (GB_BAND * GB_BAND);
-    } else {
-        gb_arm_cell(q - NB, i, j, k);
-    }
-}
-
-// guard cells of the step's read region: the band's shell, then the arms
-using band_shell = shell_slabs<GB_BAND, GB_BAND, GB_BAND, 1>;
-constexpr int GB_STEP_GUARD_CELLS = band_shell::COUNT + 3 * GB_ARM;  // 5624
-__device__ __forceinline__ void gb_step_guard_cell(int q, int& i, int& j, int& k)
-{
-    if (q < band_shell::COUNT) {
-        band_shell::at(q, i, j, k);
-        i += GB_BAND_LO;
-        j += GB_BAND_LO;
-        k += GB_BAND_LO;
-    } else {
-        gb_arm_cell(q - band_shell::COUNT, i, j, k);
-    }
-}
 
 // guard faces of axis A in the step's read region: the shell of the box
 // normal 3..21, across 3..20

@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(128)
 k_prim32(gb_dev_grid g, const int* __restrict__ list, float* __restrict__ p32, size_t stride)
 {
     // threads [0, GB_STEP_CELLS): the cells of the step's read region;
-    // then (MHD) 3 x GB_STEP_FACES faces: normal 3..21, across 3..20
+    // then (MHD) its faces, axis by axis
     const int cb = blockIdx.y;
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q < GB_STEP_CELLS) {
@@ -79,10 +79,11 @@ k_prim32(gb_dev_grid g, const int* __restrict__ list, float* __restrict__ p32, s
         return;
     }
     q -= GB_STEP_CELLS;
-    if (!MHD || q >= 3 * GB_STEP_FACES) return;
-    const int a = q / GB_STEP_FACES, e = q - a * GB_STEP_FACES;
-    const int nx = GB_BAND + (a == 0), ny = GB_BAND + (a == 1);
-    const int fi = gb_fidx(a, GB_BAND_LO + e % nx, GB_BAND_LO + (e / nx) % ny, GB_BAND_LO + e / (nx * ny));
+    if (!MHD || q >= GB_STEP_FACES_ALL) return;
+    const int a = q < gb_step_faces(0) ? 0 : (q < gb_step_faces(0) + gb_step_faces(1) ? 1 : 2);
+    const int e = q - (a == 0 ? 0 : (a == 1 ? gb_step_faces(0) : gb_step_faces(0) + gb_step_faces(1)));
+    const int nx = GB_N + (a == 0), ny = GB_BAND + (a == 1);
+    const int fi = gb_fidx(a, e % nx, GB_BAND_LO + (e / nx) % ny, GB_BAND_LO + e / (nx * ny));
     const double* fa = a == 0 ? g.f[0] : (a == 1 ? g.f[1] : g.f[2]);
     p32[(size_t)cb * stride + (size_t)NP32 * GB_N3 + (size_t)a * GB_FSZ + fi] =
         gb_d2f(fa[(int64_t)list[cb] * GB_FSZ + fi]);
