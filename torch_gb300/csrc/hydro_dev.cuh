@@ -978,18 +978,20 @@ __device__ __forceinline__ R upw(R f, R a, R b)
 // in the mixed path); it is stored as double and the face-B update that
 // consumes it stays FP64. Every edge value is shared by the four faces
 // around the edge, so div B is kept to round-off in either precision.
-template <typename T>
-__global__ void __launch_bounds__(128)
-k_emf(gb_dev_grid g, const int* __restrict__ list, const T* __restrict__ fscr, size_t fstride,
-      double* __restrict__ escr, size_t estride, const float* __restrict__ p32, size_t p32_stride)
+// the edges of direction C (a compile-time axis, so the axis permutations
+// of every index fold away)
+template <typename T, int CD>
+__device__ __forceinline__ void emf_edge(const gb_dev_grid& g, const int* __restrict__ list, const T* __restrict__ fscr,
+                                         size_t fstride, double* __restrict__ escr, size_t estride,
+                                         const float* __restrict__ p32, size_t p32_stride)
 {
     using R = T;
-    const int c = blockIdx.y;
+    constexpr int c = CD;
     const int cb = blockIdx.z;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= NEDGE) return;
     const int blk = list[cb];
-    const int a = (c + 1) % 3, b = (c + 2) % 3;
+    constexpr int a = (c + 1) % 3, b = (c + 2) % 3;
     const int A = LO + e % 17, B = LO + (e / 17) % 17, C = LO + e / (17 * 17);
     const T* fs = fscr + (size_t)cb * fstride;
     auto fl = [&](int d, int var, int x0, int x1, int x2) -> R {
@@ -1033,6 +1035,16 @@ k_emf(gb_dev_grid g, const int* __restrict__ list, const T* __restrict__ fscr, s
     const R ev = eavg + eighth * (dbm - dbp) + eighth * (dam - dap);
     if constexpr (std::is_same<R, float>::value) escr[(size_t)cb * estride + (size_t)c * NEDGE + e] = gb_f2d(ev);
     else escr[(size_t)cb * estride + (size_t)c * NEDGE + e] = ev;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_emf(gb_dev_grid g, const int* __restrict__ list, const T* __restrict__ fscr, size_t fstride,
+      double* __restrict__ escr, size_t estride, const float* __restrict__ p32, size_t p32_stride)
+{
+    if (blockIdx.y == 0) emf_edge<T, 0>(g, list, fscr, fstride, escr, estride, p32, p32_stride);
+    else if (blockIdx.y == 1) emf_edge<T, 1>(g, list, fscr, fstride, escr, estride, p32, p32_stride);
+    else emf_edge<T, 2>(g, list, fscr, fstride, escr, estride, p32, p32_stride);
 }
 
 __device__ __forceinline__ int edge_index(int c, int i, int j, int k)
