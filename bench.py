@@ -50,8 +50,8 @@ TDUST0 = 18.0  # initial dust temperature [K] (sim_tdust, flash.par.turbsph_stan
 # the 128^3 box at 128-block chunks; "recon" = primitive conversion +
 # reconstruction, "guard_fill" = cells + faces). The roofline's traffic is
 # this times the zones one launch covers.
-TRAFFIC_B_PER_ZONE = {"recon": 726.9, "update": 285.1, "flux": 443.4, "guard_fill": 402.5, "mlp_infer": 16.1,
-                      "sur_accept": 85.4, "emf": 96.7, "faceb": 65.5, "sur_feat": 36.1, "dt": 97.6}
+TRAFFIC_B_PER_ZONE = {"recon": 646.0, "update": 285.5, "flux": 442.9, "guard_fill": 304.6, "mlp_infer": 16.0,
+                      "sur_accept": 85.4, "emf": 96.7, "faceb": 65.6, "sur_feat": 36.0, "dt": 97.6}
 
 
 def build_workload(wl, device):
