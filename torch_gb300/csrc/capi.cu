@@ -1307,6 +1307,9 @@ struct chunk_aux {
     // per-chunk downloads of a host-resident step (gb_step_graph_host)
     cudaStream_t s3 = nullptr;
     cudaEvent_t dl = nullptr, dl_join = nullptr;
+    // the step graph's CFL reduction beside its guard fill
+    cudaStream_t s_dt = nullptr;
+    cudaEvent_t dt_fork = nullptr, dt_join = nullptr;
 } g_aux;
 
 // The device views of a host-resident state while its step is recorded
@@ -1319,6 +1322,16 @@ struct host_io_dev {
 };
 const host_io_dev* g_hio = nullptr;
 }  // namespace
+
+static int dt_stream_prepare()
+{
+    if (!g_aux.s_dt && gb_check(cudaStreamCreateWithFlags(&g_aux.s_dt, cudaStreamNonBlocking), "dt stream"))
+        return GB_ERR_CUDA;
+    if (!g_aux.dt_fork && (gb_check(cudaEventCreateWithFlags(&g_aux.dt_fork, cudaEventDisableTiming), "event") ||
+                           gb_check(cudaEventCreateWithFlags(&g_aux.dt_join, cudaEventDisableTiming), "event")))
+        return GB_ERR_CUDA;
+    return GB_OK;
+}
 
 static int g_io_priority = 0;  // the device's greatest stream priority
 
@@ -1635,10 +1648,16 @@ int record_step(int n, const int* list, int cool, gb_driver_state* drv, gb_statu
         launch_io(true, *g_hio, n, list, s);
         if (gb_check(cudaGetLastError(), "interior upload")) return GB_ERR_CUDA;
     }
-    int rc = launch_dt(n, list, dt_dev, drv, s);
+    // the CFL reduction reads interiors, the guard fill writes guard cells:
+    // they run side by side, and the chunks wait for both
+    cudaEventRecord(g_aux.dt_fork, s);
+    cudaStreamWaitEvent(g_aux.s_dt, g_aux.dt_fork, 0);
+    int rc = launch_dt(n, list, dt_dev, drv, g_aux.s_dt);
     if (rc) return rc;
+    cudaEventRecord(g_aux.dt_join, g_aux.s_dt);
     rc = gb_launch_guardfill(n, list, s);
     if (rc) return rc;
+    cudaStreamWaitEvent(s, g_aux.dt_join, 0);
     rc = gb_launch_hydro(n, list, 1.0, dt_dev, cool, st, s);
     if (rc) return rc;
     k_advance_clock<<<1, 1, 0, s>>>(drv);
@@ -1710,6 +1729,7 @@ static int run_step_graph(int blockCount, const int* list, int cool, gb_driver_s
         if (!rc) rc = gb_fc_prepare(blockCount, s);
         if (!rc) rc = gb_guard_prepare(s);
         if (!rc) rc = gb_streams_prepare((blockCount + chunk - 1) / chunk);
+        if (!rc) rc = dt_stream_prepare();
         if (rc) return rc;
         if (gb_check(cudaStreamSynchronize(s), "graph prepare")) return GB_ERR_CUDA;
         if (gb_check(cudaStreamBeginCapture(g_graph.cap, cudaStreamCaptureModeThreadLocal), "begin capture"))

@@ -57,13 +57,14 @@ template <bool MHD>
 __global__ void __launch_bounds__(128)
 k_prim32(gb_dev_grid g, const int* __restrict__ list, float* __restrict__ p32, size_t stride)
 {
-    // threads [0, GB_STEP_CELLS): the cells of the step's read region;
-    // then (MHD) its faces, axis by axis
+    // threads [0, GB_STEP_CELLS / 2): pairs of x-neighbouring cells of the
+    // step's read region (rows are whole and even, so a pair is one 16-byte
+    // load per variable); then (MHD) its faces, axis by axis
     const int cb = blockIdx.y;
     int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < GB_STEP_CELLS) {
+    if (q < GB_STEP_CELLS / 2) {
         int i, j, k;
-        gb_step_cell(q, i, j, k);
+        gb_step_cell(2 * q, i, j, k);
         const int c = gb_cidx(i, j, k);
         const double* base = g.unk + (int64_t)list[cb] * g.nvar * GB_N3 + c;
         float* out = p32 + (size_t)cb * stride + c;
@@ -71,14 +72,15 @@ k_prim32(gb_dev_grid g, const int* __restrict__ list, float* __restrict__ p32, s
 #pragma unroll
         for (int v = 0; v < NP32; ++v) {
             if (!MHD && v >= 5 && v < 8) {
-                out[(size_t)v * GB_N3] = 0.0f;
+                *reinterpret_cast<float2*>(out + (size_t)v * GB_N3) = make_float2(0.0f, 0.0f);
                 continue;
             }
-            out[(size_t)v * GB_N3] = gb_d2f(base[(int64_t)g.slot[roles[v]] * GB_N3]);
+            const double2 x = *reinterpret_cast<const double2*>(base + (int64_t)g.slot[roles[v]] * GB_N3);
+            *reinterpret_cast<float2*>(out + (size_t)v * GB_N3) = make_float2(gb_d2f(x.x), gb_d2f(x.y));
         }
         return;
     }
-    q -= GB_STEP_CELLS;
+    q -= GB_STEP_CELLS / 2;
     if (!MHD || q >= GB_STEP_FACES_ALL) return;
     const int a = q < gb_step_faces(0) ? 0 : (q < gb_step_faces(0) + gb_step_faces(1) ? 1 : 2);
     const int e = q - (a == 0 ? 0 : (a == 1 ? gb_step_faces(0) : gb_step_faces(0) + gb_step_faces(1)));

@@ -272,7 +272,21 @@ __global__ void __launch_bounds__(128) k_mlp_infer(int64_t n, const float* __res
     const int g = lane >> 2, t = lane & 3;
     constexpr int NT = INFER_NT;
     const int64_t ngroups = (n + 16 * NT - 1) / (16 * NT);
-    for (int64_t grp = (int64_t)blockIdx.x * 4 + warp; grp < ngroups; grp += (int64_t)gridDim.x * 4) {
+    const int64_t gstep = (int64_t)gridDim.x * 4;
+    // the features of a warp's next group are loaded while it computes the
+    // current one (the only global loads of the kernel)
+    auto load_feat = [&](int64_t grp, float4 (*fv)[2]) {
+#pragma unroll
+        for (int q = 0; q < NT; ++q) {
+            const int64_t ra = (grp * NT + q) * 16 + g, rb = ra + 8;
+            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+            fv[q][0] = (grp < ngroups && ra < n) ? reinterpret_cast<const float4*>(feat)[ra] : z;
+            fv[q][1] = (grp < ngroups && rb < n) ? reinterpret_cast<const float4*>(feat)[rb] : z;
+        }
+    };
+    float4 fnext[NT][2];
+    load_feat((int64_t)blockIdx.x * 4 + warp, fnext);
+    for (int64_t grp = (int64_t)blockIdx.x * 4 + warp; grp < ngroups; grp += gstep) {
         // layer 1 A fragments: features in columns 0..3, zero-padded to 16;
         // columns t*2, t*2+1 (only t < 2 carry features)
         uint32_t a1[NT][4][4];
@@ -280,15 +294,14 @@ __global__ void __launch_bounds__(128) k_mlp_infer(int64_t n, const float* __res
 #pragma unroll
         for (int q = 0; q < NT; ++q) {
             r0[q] = (grp * NT + q) * 16 + g;
-            const int64_t r1 = r0[q] + 8;
-            float f0[4] = {0, 0, 0, 0}, f1[4] = {0, 0, 0, 0};
-            if (r0[q] < n) { float4 v = reinterpret_cast<const float4*>(feat)[r0[q]]; f0[0] = v.x; f0[1] = v.y; f0[2] = v.z; f0[3] = v.w; }
-            if (r1 < n) { float4 v = reinterpret_cast<const float4*>(feat)[r1]; f1[0] = v.x; f1[1] = v.y; f1[2] = v.z; f1[3] = v.w; }
+            const float f0[4] = {fnext[q][0].x, fnext[q][0].y, fnext[q][0].z, fnext[q][0].w};
+            const float f1[4] = {fnext[q][1].x, fnext[q][1].y, fnext[q][1].z, fnext[q][1].w};
             a1[q][0][0] = t < 2 ? pack2(f0[t * 2], f0[t * 2 + 1]) : 0u;
             a1[q][0][1] = t < 2 ? pack2(f1[t * 2], f1[t * 2 + 1]) : 0u;
             a1[q][0][2] = 0u;
             a1[q][0][3] = 0u;
         }
+        load_feat(grp + gstep, fnext);
         uint32_t h1[NT][4][4], h2[NT][4][4];
         hidden_layer<1, NT>(a1, sw + packed_layout::W1, sbias, lane, h1);
         hidden_layer<4, NT>(h1, sw + packed_layout::W2, sbias + H, lane, h2);
