@@ -665,8 +665,12 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
     T* out = scr + (size_t)cb * scr_stride;
     const int us[NP] = {0, rot_slot_rt<1>(d), rot_slot_rt<2>(d), rot_slot_rt<3>(d), 4,
                         rot_slot_rt<5>(d), rot_slot_rt<6>(d), rot_slot_rt<7>(d)};
+    // the Riemann solver takes the normal field from the face, not from the
+    // states (and hydro has no field): those planes are neither written here
+    // nor read there
 #pragma unroll
-    for (int s = 0; s < NP; ++s) {
+    for (int s = 0; s < (MHD ? NP : 5); ++s) {
+        if (s == 5) continue;
         out[((size_t)(0 * 3 + d) * NP + us[s]) * NRC + cell] = wp[s];
         out[((size_t)(1 * 3 + d) * NP + us[s]) * NRC + cell] = wn[s];
     }
@@ -881,6 +885,13 @@ __device__ __forceinline__ void flux_face(gb_dev_grid g, hydro_kparams kp, const
     T wl[NP], wr[NP];
 #pragma unroll
     for (int v = 0; v < NP; ++v) {
+        // the normal field (v = 5 + d) comes from the face below; hydro has
+        // no field: those state planes are not written
+        if (v == 5 + d || (!MHD && v >= 5)) {
+            wl[v] = (T)0;
+            wr[v] = (T)0;
+            continue;
+        }
         wl[v] = rs[((size_t)(0 * 3 + d) * NP + v) * NRC + cl];
         wr[v] = rs[((size_t)(1 * 3 + d) * NP + v) * NRC + cr];
     }
