@@ -1267,9 +1267,9 @@ extern "C" int gb_fill_guardcells(int blockCount, const int* list, void* stream)
 size_t gb_hydro_scratch_bytes_fp64();
 size_t gb_hydro_scratch_bytes_mixed();
 int gb_hydro_chunk_fp64(const gbh::hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
-                        void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put);
+                        void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put, const sur_feat_out* sf);
 int gb_hydro_chunk_mixed(const gbh::hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
-                         void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put);
+                         void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put, const sur_feat_out* sf);
 int gb_dt_launch(const gbh::hydro_kparams& kp, int mhd, int nblk, const int* list,
                  unsigned long long* bits, cudaStream_t s);
 
@@ -1439,7 +1439,8 @@ static gbh::hydro_kparams make_kp(double dt, const double* dtp = nullptr)
 
 int gb_cooling_mode();
 int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp, gb_status* st, cudaStream_t s,
-                        int chain);
+                        int chain, bool feat_done);
+int gb_sur_feat_target(int chain, int nblk, sur_feat_out* out);
 
 int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int cool, gb_status* st,
                     cudaStream_t s)
@@ -1494,11 +1495,14 @@ int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int
             if (k > 0) cudaStreamWaitEvent(sk, g_aux.put[k - 1], 0);
             ev_put = g_aux.put[k];
         }
-        rc = mixed ? gb_hydro_chunk_mixed(kp, g_gb.hp.mhd, fused, nb, list + b0, scr, st, sk, ev_put)
-                   : gb_hydro_chunk_fp64(kp, g_gb.hp.mhd, fused, nb, list + b0, scr, st, sk, ev_put);
+        // the surrogate cools this chunk next: the update writes its features
+        sur_feat_out sf;
+        const bool feat = cool && !fused && gb_sur_feat_target(chain, nb, &sf) == GB_OK;
+        rc = mixed ? gb_hydro_chunk_mixed(kp, g_gb.hp.mhd, fused, nb, list + b0, scr, st, sk, ev_put, feat ? &sf : nullptr)
+                   : gb_hydro_chunk_fp64(kp, g_gb.hp.mhd, fused, nb, list + b0, scr, st, sk, ev_put, feat ? &sf : nullptr);
         if (rc) return rc;
         if (cool && !fused) {
-            rc = gb_launch_surrogate(nb, list + b0, dt, dtp, st, sk, chain);
+            rc = gb_launch_surrogate(nb, list + b0, dt, dtp, st, sk, chain, feat);
             if (rc) return rc;
         }
         if (g_hio) {

@@ -291,6 +291,7 @@ extern "C" int gb_cool_cells(int64_t n, const double* dens, double* ei, double* 
 #include "cool_f32.cuh"
 #include "mlp.h"
 #include "sur_common.cuh"
+#include "sur_dev.cuh"
 
 namespace {
 
@@ -386,46 +387,6 @@ __device__ __forceinline__ void sur_store(const gb_dev_grid& g, const gb_cool_ct
     if (g.slot[GB_PEFL] >= 0) gb_var(g, blk, GB_PEFL)[ci] = 0.0;
 }
 
-// Unit factors of the learned-cooling kernels, divided once on the host:
-// their loads and stores multiply instead of dividing per cell (FP64
-// division is a long sequence on the FP64 pipe). The fallback kernel, which
-// is the plain integrator, keeps sur_load's divisions.
-struct sur_units {
-    double T_of_e;     // (gamma - 1) abar m_p / k_B
-    double e_of_T;     // its inverse: TtoEI
-    double inv_mu_mp;  // 1 / (mu_mol m_p)
-    double vel2, inv_vel2;
-    // FP32 copies for the surrogate kernels, whose per-cell inputs go
-    // straight to FP32 (FP64 instructions are the scarce resource there)
-    float dens_unit_f, T_of_e_f, e_of_T_f, inv_mu_mp_f, time_unit_f, mu_mol_f, xHp_const_f;
-    float emin_f;  // 0.5 absTmin TtoEI, the energy floor of the iteration
-    float absTmin_f, absTmax_f, dust_sputter_f, smallp_f, T_min_f, nd_min_f;
-    double smallp, dens_unit;
-};
-
-// The inputs of the surrogate kernels for one cell in FP32: the FP64
-// state is converted on the integer pipe and scaled in FP32. Only the
-// internal energy is also kept in FP64 (the accepted energy is formed from
-// it in FP64). Each FP32 input is within a couple of ulp of the rounded
-// FP64 value the plain loader makes.
-__device__ __forceinline__ void sur_load_f32(const gb_dev_grid& g, const gb_cool_pf& pf, const sur_units& u, int blk,
-                                             int ci, gb_cool_varsf& f, double& ei, float& eif, float& tempf)
-{
-    ei = gb_var(g, blk, GB_EINT)[ci] * u.vel2;
-    eif = gb_d2f(ei);
-    tempf = eif * u.T_of_e_f;
-    f.rho = gb_d2f(gb_var(g, blk, GB_DENS)[ci]) * u.dens_unit_f;
-    f.ndens = f.rho * u.inv_mu_mp_f;
-    f.conf = f.ndens * u.inv_mu_mp_f;  // ndens^2 / rho
-    f.tdust = gb_d2f(gb_var(g, blk, GB_TDUS)[ci]);
-    f.xHp = g.slot[GB_IHP] >= 0 ? gb_d2f(gb_var(g, blk, GB_IHP)[ci]) : u.xHp_const_f;
-    f.ephen = g.slot[GB_PHHE] >= 0 ? gb_d2f(gb_var(g, blk, GB_PHHE)[ci]) / f.rho : 0.0f;
-    f.Gflux = g.slot[GB_PEFL] >= 0 ? gb_d2f(gb_var(g, blk, GB_PEFL)[ci]) : 0.0f;
-    f.TtoEI = u.e_of_T_f;
-    f.mu_mol = u.mu_mol_f;
-    f.cr_pref = pf.crRE * (f.ndens / f.rho);
-}
-
 __device__ __forceinline__ void sur_load_fast(const gb_dev_grid& g, const gb_cool_ctx& c, const sur_units& u, int blk,
                                               int ci, gb_cool_vars& v, double& ei, double& temp)
 {
@@ -506,22 +467,11 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_unit
     double ei;
     float eif, tempf;
     sur_load_f32(g, pf, un, blk, ci, vf, ei, eif, tempf);
-    const gb_cool_tabf tf = {c.Tf, c.nf, c.lamf, un.T_min_f, un.nd_min_f};
-    const float fl = gbcoolf::cooling_floor(pf, tf, vf);
-    float gam, lam;
-    float f0 = gbcoolf::dei_parts(pf, tf, vf, fl, eif, &gam, &lam);
-    const float dt = gb_d2f(dt_code) * un.time_unit_f;
-    // features in FP32: dt / t_cool = dt |f| / e
-    const float r = dt * fabsf(f0) / eif;
-    float lr = log10f(fmaxf(r, 1e-30f));
-    lr = fminf(fmaxf(lr, (float)-gbsur::R_CLAMP), (float)gbsur::R_CLAMP);
-    float lh = log10f(fmaxf(gam, 1e-30f)) - log10f(fmaxf(lam, 1e-30f));
-    lh = fminf(fmaxf(lh, (float)-gbsur::H_CLAMP), (float)gbsur::H_CLAMP);
-    reinterpret_cast<float4*>(feat)[idx] =
-        make_float4((log10f(vf.ndens) - (float)gbsur::N_MID) / (float)gbsur::N_HALF,
-                    (log10f(tempf) - (float)gbsur::T_MID) / (float)gbsur::T_HALF, lr / (float)gbsur::R_HALF,
-                    lh / (float)gbsur::H_HALF);
-    f0out[idx] = make_float2(f0, fl);
+    float4 x;
+    float2 f0fl;
+    sur_features(c, pf, un, vf, eif, tempf, dt_code, x, f0fl);
+    reinterpret_cast<float4*>(feat)[idx] = x;
+    f0out[idx] = f0fl;
 }
 
 // acceptance test: starting from the network's prediction, at most four
@@ -747,16 +697,9 @@ int gb_sur_prepare(int64_t ncell, cudaStream_t s)
     return rc ? rc : gb_mlp_pack(s);
 }
 
-int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp, gb_status* st, cudaStream_t s,
-                        int chain)
+// the unit factors of the surrogate kernels
+static sur_units make_units()
 {
-    sur_bufs& g_sb = g_sbs[chain & 1];
-    const int64_t ncell = (int64_t)nblk * 4096;
-    int rc = sur_ensure(g_sb, ncell);
-    if (rc) return rc;
-    const unsigned nb = (unsigned)((ncell + 127) / 128);
-    gb_prof_begin(GBP_SUR_FEAT, s);
-    const gb_cool_pf pf = make_pf(g_gb.cool.p);
     sur_units un;
     {
         const gb_cool_params& p = g_gb.cool.p;
@@ -782,8 +725,39 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp,
         un.T_min_f = (float)g_gb.cool.T_min;
         un.nd_min_f = (float)g_gb.cool.nd_min;
     }
-    k_sur_feat<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, un, list, ncell, dt, dtp, g_sb.feat, g_sb.f0);
-    gb_prof_end(GBP_SUR_FEAT, s);
+    return un;
+}
+
+// Where the hydro update of a chunk of nblk blocks on chain `chain` writes
+// the surrogate's features (its buffers, allocated here when they are too
+// small: callers inside a capture prepared them before)
+int gb_sur_feat_target(int chain, int nblk, sur_feat_out* out)
+{
+    sur_bufs& g_sb = g_sbs[chain & 1];
+    int rc = sur_ensure(g_sb, (int64_t)nblk * 4096);
+    if (rc) return rc;
+    out->feat = reinterpret_cast<float4*>(g_sb.feat);
+    out->f0 = g_sb.f0;
+    out->pf = make_pf(g_gb.cool.p);
+    out->un = make_units();
+    return GB_OK;
+}
+
+int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp, gb_status* st, cudaStream_t s,
+                        int chain, bool feat_done)
+{
+    sur_bufs& g_sb = g_sbs[chain & 1];
+    const int64_t ncell = (int64_t)nblk * 4096;
+    int rc = sur_ensure(g_sb, ncell);
+    if (rc) return rc;
+    const unsigned nb = (unsigned)((ncell + 127) / 128);
+    const gb_cool_pf pf = make_pf(g_gb.cool.p);
+    const sur_units un = make_units();
+    if (!feat_done) {
+        gb_prof_begin(GBP_SUR_FEAT, s);
+        k_sur_feat<<<nb, 128, 0, s>>>(g_gb.grid, g_gb.cool, pf, un, list, ncell, dt, dtp, g_sb.feat, g_sb.f0);
+        gb_prof_end(GBP_SUR_FEAT, s);
+    }
     gb_prof_begin(GBP_MLP, s);
     rc = gb_mlp_launch_infer(ncell, g_sb.feat, g_sb.y, s);
     gb_prof_end(GBP_MLP, s);

@@ -86,7 +86,7 @@ __device__ __forceinline__ int find(const float* x, float x0, int N)
 
 // de/dt split into heating Gamma and cooling Lambda (as dei_parts);
 // floor_ is the cooling at the floors (state-independent per cell)
-__device__ float dei_parts(const gb_cool_pf& p, const gb_cool_tabf& t, const gb_cool_varsf& v, float floor_,
+static __device__ float dei_parts(const gb_cool_pf& p, const gb_cool_tabf& t, const gb_cool_varsf& v, float floor_,
                            float ei, float* gam, float* lam)
 {
     float T = ei / v.TtoEI;
@@ -171,7 +171,7 @@ __device__ float dei_parts(const gb_cool_pf& p, const gb_cool_tabf& t, const gb_
 // T_dust after a step (heatCool.F90:430-443 + get_dust_temperature,
 // :703-884) in FP32: dust heating by FUV photons that did not eject
 // photo-electrons plus cosmic rays, Newton on the dust energy balance
-__device__ float dust_temperature(const gb_cool_pf& p, const gb_cool_varsf& v, float T, float tdust_in)
+static __device__ float dust_temperature(const gb_cool_pf& p, const gb_cool_varsf& v, float T, float tdust_in)
 {
     const float sqT = sqrtf(T);
     const float lam_j = v.ndens / v.rho * sqrtf(p.jeansK * T / v.ndens);
@@ -241,7 +241,7 @@ __device__ __forceinline__ void make_vars(const gb_cool_pf& p, const gb_cool_var
 }
 
 // cooling at the floors (heatCool.F90:1509-1519) in FP32
-__device__ float cooling_floor(const gb_cool_pf& p, const gb_cool_tabf& t, const gb_cool_varsf& v)
+static __device__ float cooling_floor(const gb_cool_pf& p, const gb_cool_tabf& t, const gb_cool_varsf& v)
 {
     float emin = 0.0f;
     const float T = p.tradmin;

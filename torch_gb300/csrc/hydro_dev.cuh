@@ -20,6 +20,7 @@
 
 #include "cool_dev.cuh"
 #include "gb_common.cuh"
+#include "sur_dev.cuh"
 
 namespace gbh {
 
@@ -1317,11 +1318,14 @@ __device__ __forceinline__ double rcp_newton(double x)
     return fma(y, e, y);
 }
 
-template <typename T, bool MHD, bool COOL>
+// FEAT: also write the learned-cooling surrogate's features of the new
+// state (what the feature kernel would compute next): FP32 work beside this
+// FP64-bound kernel instead of a kernel of its own
+template <typename T, bool MHD, bool COOL, bool FEAT>
 __global__ void __launch_bounds__(128)
 k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restrict__ list,
          const T* __restrict__ fscr, size_t fstride, const double* __restrict__ bscr, size_t bstride,
-         gb_status* st)
+         gb_status* st, sur_feat_out sf)
 {
     const int cb = blockIdx.y;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1465,6 +1469,19 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
         if (!(Un[0] > 0.0)) gb_fail(st, GB_ST_NEG_DENS, blk, i, j, k, Un[0]);
         else if (!isfinite(pn) || !isfinite(Un[4])) gb_fail(st, GB_ST_NONFINITE, blk, i, j, k, pn);
         else if (floored) gb_fail(st, GB_ST_NEG_PRES, blk, i, j, k, eiE);
+    }
+    if constexpr (FEAT) {
+        // the inputs are read back as stored (this thread wrote them)
+        gb_cool_varsf vf;
+        double eid;
+        float eif, tempf;
+        sur_load_f32(g, sf.pf, sf.un, blk, ci, vf, eid, eif, tempf);
+        float4 x;
+        float2 f0fl;
+        sur_features(cool, sf.pf, sf.un, vf, eif, tempf, kp_dt(kp), x, f0fl);
+        const int64_t idx = (int64_t)cb * (GB_NXB * GB_NXB * GB_NXB) + t;
+        sf.feat[idx] = x;
+        sf.f0[idx] = f0fl;
     }
 }
 

@@ -5,9 +5,10 @@
 size_t gb_hydro_scratch_bytes_fp64() { return gbh::scratch_layout<double>::bytes; }
 
 int gb_hydro_chunk_fp64(const gbh::hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
-                        void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put)
+                        void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put,
+                         const sur_feat_out* sf)
 {
-    return gbh::launch_chunk<double>(kp, mhd, cool, nblk, list, scratch, st, s, ev_put);
+    return gbh::launch_chunk<double>(kp, mhd, cool, nblk, list, scratch, st, s, ev_put, sf);
 }
 
 int gb_dt_launch_f32(const gbh::hydro_kparams& kp, int mhd, int nblk, const int* list,

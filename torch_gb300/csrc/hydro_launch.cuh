@@ -44,7 +44,8 @@ void put_fluxes(const hydro_kparams& kp, int nblk, const int* list, T* fscr, cud
 
 template <typename T>
 int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
-                 void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put = nullptr)
+                 void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put = nullptr,
+                 const sur_feat_out* sf = nullptr)
 {
     using SL = scratch_layout<T>;
     // scratch of the chunk: [recon | flux | emf | faceb], each block-major
@@ -109,12 +110,16 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
     }
     dim3 ug((GB_NXB * GB_NXB * GB_NXB + 127) / 128, nblk);
     gb_prof_begin(GBP_UPDATE, s);
+    const sur_feat_out sfv = sf ? *sf : sur_feat_out{};
+    const bool feat = !cool && sfv.feat;
     if (mhd) {
-        if (cool) k_update<T, true, true><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st);
-        else k_update<T, true, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st);
+        if (cool) k_update<T, true, true, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
+        else if (feat) k_update<T, true, false, true><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
+        else k_update<T, true, false, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
     } else {
-        if (cool) k_update<T, false, true><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st);
-        else k_update<T, false, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st);
+        if (cool) k_update<T, false, true, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
+        else if (feat) k_update<T, false, false, true><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
+        else k_update<T, false, false, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
     }
     gb_prof_end(GBP_UPDATE, s);
     return gb_check(cudaGetLastError(), "hydro chunk launch") ? GB_ERR_CUDA : GB_OK;
