@@ -258,7 +258,7 @@ __device__ __forceinline__ void hidden_layer(const uint32_t (*afr)[4][4], const 
 
 constexpr int INFER_NT = 2;  // 16-row tiles per warp iteration
 
-__global__ void __launch_bounds__(128) k_mlp_infer(int64_t n, const float* __restrict__ feat,
+__global__ void __launch_bounds__(128, 4) k_mlp_infer(int64_t n, const float* __restrict__ feat,
                                                    const __nv_bfloat16* __restrict__ wpk,
                                                    const float* __restrict__ bias, float* __restrict__ y)
 {
