@@ -968,8 +968,10 @@ __device__ __forceinline__ void flux_face(gb_dev_grid g, hydro_kparams kp, const
     fs[(size_t)9 * NFC + f] = un;
 }
 
+// mixed path: eight resident CTAs per SM (64 registers, no spills) to hide
+// the latency of the face-state loads; the FP64 Riemann solvers need more
 template <typename T, bool MHD>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, std::is_same<T, float>::value ? 8 : 1)
 k_flux(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* __restrict__ rscr,
        size_t rstride, T* __restrict__ fscr, size_t fstride, const float* __restrict__ p32, size_t p32_stride)
 {
@@ -1321,8 +1323,11 @@ __device__ __forceinline__ double rcp_newton(double x)
 // FEAT: also write the learned-cooling surrogate's features of the new
 // state (what the feature kernel would compute next): FP32 work beside this
 // FP64-bound kernel instead of a kernel of its own
+// mixed path without the fused plain cooling: eight resident CTAs per SM
+// (64 registers, no spills); the FP64 path and the fused integrator need
+// more registers than that
 template <typename T, bool MHD, bool COOL, bool FEAT>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, (std::is_same<T, float>::value && !COOL) ? 8 : 1)
 k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restrict__ list,
          const T* __restrict__ fscr, size_t fstride, const double* __restrict__ bscr, size_t bstride,
          gb_status* st, sur_feat_out sf)
