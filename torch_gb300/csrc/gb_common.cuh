@@ -206,14 +206,25 @@ __device__ __forceinline__ double gb_f2d(float x)
 // 2^l as a double, built from its exponent bits (0 <= l < 1023)
 __device__ __forceinline__ double gb_pow2(int l) { return __longlong_as_double((long long)(1023 + l) << 52); }
 
+// x 2^l for a normal, finite x whose scaled exponent stays normal (dt / dx
+// of a level): the exponent field moves by l on the integer pipe, the same
+// value as the FP64 multiplication, without an FP64 instruction
+__device__ __forceinline__ double gb_scale_pow2(double x, int l)
+{
+    const long long b = __double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0 || e == 0x7FF || e + l <= 0 || e + l >= 0x7FF) return x * gb_pow2(l);
+    return __longlong_as_double(b + ((long long)l << 52));
+}
+
 __device__ __forceinline__ int gb_block_level(const gb_dev_grid& g, int blk) { return g.level ? __ldg(g.level + blk) : 0; }
 
 __device__ __forceinline__ void gb_block_dx(const gb_dev_grid& g, const double* dx0, int blk, double* dx)
 {
-    double sc = g.level ? ldexp(1.0, -__ldg(g.level + blk)) : 1.0;
-    dx[0] = dx0[0] * sc;
-    dx[1] = dx0[1] * sc;
-    dx[2] = dx0[2] * sc;
+    const int l = g.level ? __ldg(g.level + blk) : 0;
+    dx[0] = gb_scale_pow2(dx0[0], -l);
+    dx[1] = gb_scale_pow2(dx0[1], -l);
+    dx[2] = gb_scale_pow2(dx0[2], -l);
 }
 
 __device__ __forceinline__ double* gb_var(const gb_dev_grid& g, int blk, int role)

@@ -407,16 +407,10 @@ __device__ __forceinline__ void kp_dtdxf(const hydro_kparams& kp, int level, flo
 
 __device__ __forceinline__ void kp_dtdx(const hydro_kparams& kp, int level, double* out)
 {
-    const double sc = gb_pow2(level);
-    if (kp.dtdxp) {
-        out[0] = kp.dtdxp[0] * sc;
-        out[1] = kp.dtdxp[1] * sc;
-        out[2] = kp.dtdxp[2] * sc;
-    } else {
-        out[0] = kp.dtdx0[0] * sc;
-        out[1] = kp.dtdx0[1] * sc;
-        out[2] = kp.dtdx0[2] * sc;
-    }
+    const double* d = kp.dtdxp ? kp.dtdxp : kp.dtdx0;
+    out[0] = gb_scale_pow2(d[0], level);
+    out[1] = gb_scale_pow2(d[1], level);
+    out[2] = gb_scale_pow2(d[2], level);
 }
 
 // primitive 8-vector of a cell of the padded block
