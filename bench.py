@@ -257,7 +257,7 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
-def e2e_run(G, g, steps, warmup):
+def e2e_run(G, g, steps, warmup, tune=False):
     """Fast path through the C ABI as a FLASH host would drive it: the host
     owns unk (FLASH order, variable fastest) and facevar{x,y,z} in pinned
     memory. Each step is one gb_step_graph_host call: upload of the leaf
@@ -282,9 +282,22 @@ def e2e_run(G, g, steps, warmup):
     io.facex, io.facey, io.facez = (h.data_ptr() for h in hf)
     L = G.lib()
     st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    G.check(L.gb_grid_download_flash(C.c_void_p(host.data_ptr()), nunk, io.host_slot, nn, st), "init")
-    for h, d in zip(hf, (g.fx, g.fy, g.fz)):
-        h.copy_(d.cpu())
+    def host_from_device():
+        G.check(L.gb_grid_download_flash(C.c_void_p(host.data_ptr()), nunk, io.host_slot, nn, st), "init")
+        for h, d in zip(hf, (g.fx, g.fy, g.fz)):
+            h.copy_(d.cpu())
+        torch.cuda.synchronize()
+
+    host_from_device()
+    if tune:
+        # the host-resident step picks its own chunk size: its downloads
+        # overlap later chunks, so smaller chunks than the device-only
+        # step's can win
+        from torch_gb300 import autotune
+        t0, o0, s0 = G.get_launch_config()[1], G.get_launch_config()[2], G.get_chunk_streams()
+        autotune.tune(g, cool=True, chunks=(64, 128, 256, 512), tiles=(t0,), occs=(o0,), streams=(s0,),
+                      step_fn=lambda: g.step_graph_host(io, cool=True), restore_fn=host_from_device,
+                      variant="host")
     leaves = np.ascontiguousarray(g.leaf, np.int32)
     lp, nl = leaves.ctypes.data_as(C.c_void_p), len(leaves)
     hp = C.c_void_p(host.data_ptr())
@@ -562,7 +575,7 @@ def main():
     del a, b, c, d, Ta, Tb
     one_step = cooling_one_step(G, (g_plain, g_fast, g_tight), g_mixed, lv)
     G.set_cooling_mode(True)
-    e2e_ms, e2e_bytes, e2e_parts = e2e_run(G, g_fast, max(2, args.steps // 2), 3)
+    e2e_ms, e2e_bytes, e2e_parts = e2e_run(G, g_fast, max(2, args.steps // 2), 3, tune=not args.no_tune)
     G.set_cooling_mode(False)
     hbm, hbm_kind = peaks()
     # FP64-pipe roofline of the plain path: flops per zone-update counted by

@@ -49,33 +49,38 @@ def _save(d: dict) -> None:
 
 
 def time_config(grid, cool: bool, chunk: int, tile: int, steps: int = 3, warmup: int = 1, occ: int = 0,
-                streams: int = 1) -> float:
-    """ms per step of the graph-replayed step at one launch shape."""
+                streams: int = 1, step_fn=None) -> float:
+    """ms per step of the graph-replayed step at one launch shape (step_fn:
+    the step to time, grid.step_graph(cool) by default)."""
     import torch
     from . import gbhydro as G
     G.set_launch_config(chunk, tile, occ)
     G.set_chunk_streams(streams)
+    step = step_fn or (lambda: grid.step_graph(cool))
     s = torch.cuda.current_stream()
     for _ in range(warmup):
-        grid.step_graph(cool)
+        step()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(s)
     for _ in range(steps):
-        grid.step_graph(cool)
+        step()
     b.record(s)
     torch.cuda.synchronize()
     return a.elapsed_time(b) / steps
 
 
 def tune(grid, cool: bool = True, chunks=CHUNKS, tiles=TILES, occs=OCCS, steps: int = 3,
-         use_cache: bool = True, streams=STREAMS) -> dict:
+         use_cache: bool = True, streams=STREAMS, step_fn=None, restore_fn=None, variant: str = "") -> dict:
     """Pick and set the fastest (chunk, tile, occ, streams) for `grid`
     (registered, with hydro/cooling configured; the occupancy bound only
-    exists in the mixed path). Returns {"chunk", "tile", "occ", "streams",
-    "ms", "trials", "cached"}."""
+    exists in the mixed path). step_fn replaces the timed step (for example
+    the host-resident step) and restore_fn runs after each trial's device
+    state is restored (for example to restore host arrays); variant names
+    that choice in the cache key. Returns {"chunk", "tile", "occ",
+    "streams", "ms", "trials", "cached"}."""
     import torch
     from . import gbhydro as G
-    key = _key(grid, cool)
+    key = _key(grid, cool) + (f"|{variant}" if variant else "")
     cache = _load() if use_cache else {}
     if key in cache:
         r = dict(cache[key], cached=True)
@@ -91,12 +96,14 @@ def tune(grid, cool: bool = True, chunks=CHUNKS, tiles=TILES, occs=OCCS, steps: 
             for t in tiles:
                 for o in occs:
                     for ns in streams:
-                        ms = time_config(grid, cool, c, t, steps=steps, occ=o, streams=ns)
+                        ms = time_config(grid, cool, c, t, steps=steps, occ=o, streams=ns, step_fn=step_fn)
                         trials.append({"chunk": c, "tile": t, "occ": o, "streams": ns, "ms": ms})
                         grid.u.copy_(saved[0])
                         if grid.mhd:
                             for a, b in zip((grid.fx, grid.fy, grid.fz), saved[1:]):
                                 a.copy_(b)
+                        if restore_fn:
+                            restore_fn()
     finally:
         del saved
         torch.cuda.synchronize()
