@@ -331,7 +331,9 @@ def e2e_run(G, g, steps, warmup, tune=False):
     ms = a.elapsed_time(b) / steps
     nbytes = nl * (16 ** 3 * nunk + 3 * 17 * 16 * 16) * 8
     separate()
+    c, t, o = G.get_launch_config()
     return ms, nbytes, {"upload_ms": parts[0], "step_ms": parts[1], "download_ms": parts[2],
+                        "launch_config": {"chunk": c, "tile": t, "occ": o, "streams": G.get_chunk_streams()},
                         "note": "parts from one step run as separate calls; the timed steps overlap the "
                                 "download of each chunk with the compute of later chunks"}
 
