@@ -46,12 +46,13 @@ WORKLOADS = {
 TDUST0 = 18.0  # initial dust temperature [K] (sim_tdust, flash.par.turbsph_standard:19)
 
 # DRAM bytes (read + write) per interior zone of each profiler category of
-# the fast path, from one ncu capture (profiles/kernels_box128_fast_chunk128.md:
-# the 128^3 box at 128-block chunks; "recon" = primitive conversion +
-# reconstruction, "guard_fill" = cells + faces). The roofline's traffic is
-# this times the zones one launch covers.
-TRAFFIC_B_PER_ZONE = {"recon": 646.0, "update": 285.5, "flux": 442.9, "guard_fill": 304.6, "mlp_infer": 16.0,
-                      "sur_accept": 85.4, "emf": 96.7, "faceb": 65.6, "sur_feat": 36.0, "dt": 97.6}
+# the fast path, from one ncu capture (profiles/kernels_box128_fast_chunk512.md:
+# the 128^3 box at 512-block chunks; "recon" = primitive conversion +
+# reconstruction, "guard_fill" = cells + faces, "sur_feat" from an earlier
+# capture of the feature kernel, which the update now replaces). The
+# roofline's traffic is this times the zones one launch covers.
+TRAFFIC_B_PER_ZONE = {"recon": 708.9, "update": 363.6, "flux": 478.9, "guard_fill": 304.4, "mlp_infer": 16.0,
+                      "sur_accept": 111.0, "emf": 114.2, "faceb": 81.2, "sur_feat": 36.0, "dt": 97.8}
 
 
 def build_workload(wl, device):
