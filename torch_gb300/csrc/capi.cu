@@ -1267,9 +1267,11 @@ extern "C" int gb_fill_guardcells(int blockCount, const int* list, void* stream)
 size_t gb_hydro_scratch_bytes_fp64();
 size_t gb_hydro_scratch_bytes_mixed();
 int gb_hydro_chunk_fp64(const gbh::hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
-                        void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put, const sur_feat_out* sf);
+                        void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put, const sur_feat_out* sf,
+                        cudaEvent_t ev_wait);
 int gb_hydro_chunk_mixed(const gbh::hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
-                         void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put, const sur_feat_out* sf);
+                         void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put, const sur_feat_out* sf,
+                         cudaEvent_t ev_wait);
 int gb_dt_launch(const gbh::hydro_kparams& kp, int mhd, int nblk, const int* list,
                  unsigned long long* bits, cudaStream_t s);
 
@@ -1487,19 +1489,23 @@ int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int
         const int chain = ns > 1 ? (k & 1) : 0;
         cudaStream_t sk = chain ? g_aux.s2 : s;
         void* scr = (char*)g_gb.d_scratch + (size_t)chain * chunk_bytes;
-        cudaEvent_t ev_put = nullptr;
+        cudaEvent_t ev_put = nullptr, ev_wait = nullptr;
         if (ns > 1 && fc) {
-            // the fine boundary fluxes this chunk reads were registered by
-            // earlier chunks: wait for the previous one (the chunk before it
-            // ran on this stream)
-            if (k > 0) cudaStreamWaitEvent(sk, g_aux.put[k - 1], 0);
+            // the fine boundary fluxes and edge fields this chunk reads were
+            // registered by earlier chunks: before its first register read it
+            // waits for the previous chunk's registration event. That covers
+            // every earlier chunk: the ones on the other stream ran before the
+            // previous chunk there, the ones on this stream before this one.
+            if (k > 0) ev_wait = g_aux.put[k - 1];
             ev_put = g_aux.put[k];
         }
         // the surrogate cools this chunk next: the update writes its features
         sur_feat_out sf;
         const bool feat = cool && !fused && gb_sur_feat_target(chain, nb, &sf) == GB_OK;
-        rc = mixed ? gb_hydro_chunk_mixed(kp, g_gb.hp.mhd, fused, nb, list + b0, scr, st, sk, ev_put, feat ? &sf : nullptr)
-                   : gb_hydro_chunk_fp64(kp, g_gb.hp.mhd, fused, nb, list + b0, scr, st, sk, ev_put, feat ? &sf : nullptr);
+        rc = mixed ? gb_hydro_chunk_mixed(kp, g_gb.hp.mhd, fused, nb, list + b0, scr, st, sk, ev_put,
+                                          feat ? &sf : nullptr, ev_wait)
+                   : gb_hydro_chunk_fp64(kp, g_gb.hp.mhd, fused, nb, list + b0, scr, st, sk, ev_put,
+                                         feat ? &sf : nullptr, ev_wait);
         if (rc) return rc;
         if (cool && !fused) {
             rc = gb_launch_surrogate(nb, list + b0, dt, dtp, st, sk, chain, feat);

@@ -6,9 +6,9 @@ size_t gb_hydro_scratch_bytes_fp64() { return gbh::scratch_layout<double>::bytes
 
 int gb_hydro_chunk_fp64(const gbh::hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
                         void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put,
-                         const sur_feat_out* sf)
+                         const sur_feat_out* sf, cudaEvent_t ev_wait)
 {
-    return gbh::launch_chunk<double>(kp, mhd, cool, nblk, list, scratch, st, s, ev_put, sf);
+    return gbh::launch_chunk<double>(kp, mhd, cool, nblk, list, scratch, st, s, ev_put, sf, ev_wait);
 }
 
 int gb_dt_launch_f32(const gbh::hydro_kparams& kp, int mhd, int nblk, const int* list,

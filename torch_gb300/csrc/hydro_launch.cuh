@@ -45,7 +45,7 @@ void put_fluxes(const hydro_kparams& kp, int nblk, const int* list, T* fscr, cud
 template <typename T>
 int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
                  void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put = nullptr,
-                 const sur_feat_out* sf = nullptr)
+                 const sur_feat_out* sf = nullptr, cudaEvent_t ev_wait = nullptr)
 {
     using SL = scratch_layout<T>;
     // scratch of the chunk: [recon | flux | emf | faceb], each block-major
@@ -81,8 +81,12 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
             k_emf_put<<<dim3((NSURF + 127) / 128, nblk), 128, 0, s>>>(list, kp.ec_near, escr, SL::emf, kp.ec_reg);
         gb_prof_end(GBP_EMF, s);
         // the registers this chunk wrote are complete (a chunk on another
-        // stream may read them now)
+        // stream may read them now); the registers it reads next were
+        // written by earlier chunks: wait for them only here, so that this
+        // chunk's reconstruction, fluxes and edge fields overlap the
+        // previous chunk's
         if (ev_put) cudaEventRecord(ev_put, s);
+        if (ev_wait) cudaStreamWaitEvent(s, ev_wait, 0);
         if (kp.ec_reg) {
             gb_prof_begin(GBP_EMF, s);
             k_emf_get<<<dim3((GB_NXB * NRING + 127) / 128, 3, nblk), 128, 0, s>>>(
@@ -102,6 +106,7 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
         gb_prof_end(GBP_FLUX, s);
         put_fluxes<T>(kp, nblk, list, fscr, s);
         if (ev_put) cudaEventRecord(ev_put, s);
+        if (ev_wait) cudaStreamWaitEvent(s, ev_wait, 0);
     }
     if (kp.fc_links) {
         // after the edge fields, which use the block's own fluxes

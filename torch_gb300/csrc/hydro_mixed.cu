@@ -7,9 +7,9 @@ size_t gb_hydro_scratch_bytes_mixed() { return gbh::scratch_layout<float>::bytes
 
 int gb_hydro_chunk_mixed(const gbh::hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
                          void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put,
-                         const sur_feat_out* sf)
+                         const sur_feat_out* sf, cudaEvent_t ev_wait)
 {
-    return gbh::launch_chunk<float>(kp, mhd, cool, nblk, list, scratch, st, s, ev_put, sf);
+    return gbh::launch_chunk<float>(kp, mhd, cool, nblk, list, scratch, st, s, ev_put, sf, ev_wait);
 }
 
 // CFL limit of the mixed path: FP32 arithmetic on the FP64 state
