@@ -46,3 +46,19 @@ def test_entry_points_reject_bad_arguments_without_gpu():
     assert L.gb_hydro_unsplit(1, None, 1.0, 1.0, None, None) == -3
     assert L.gb_heat(1, None, 1.0, 0.0, None, None) == -3
     assert b"gb_heat" in L.gb_last_error()
+
+
+def test_block_lists_are_checked_on_the_host():
+    """FLASH block ids (1-based) are checked before any launch: ids outside
+    the store, ids of refined (non-leaf) blocks and repeated ids are
+    rejected; the empty list and any order of distinct leaves pass."""
+    import numpy as np
+    import pytest
+    from torch_gb300 import gbhydro as G
+    leaf = np.array([0, 2, 3, 5], np.int32)  # blocks 1, 4 (0-based) are refined
+    assert G.check_leaf_ids([], 6, leaf).size == 0
+    assert np.array_equal(G.check_leaf_ids([6, 1, 4], 6, leaf), [5, 0, 3])
+    for bad, what in (([0], "outside"), ([7], "outside"), ([-2], "outside"), ([2], "not a leaf"),
+                      ([5], "not a leaf"), ([1, 3, 1], "more than once"), ([1.0], "integers")):
+        with pytest.raises(G.GBError, match=what):
+            G.check_leaf_ids(bad, 6, leaf)

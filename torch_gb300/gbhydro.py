@@ -245,6 +245,29 @@ def uniform_tree(nbx: int, nby: int, nbz: int):
                 root=ids.astype(np.int32), nr=(nbx, nby, nbz), maxlevel=0, leaf=ids.astype(np.int32))
 
 
+def check_leaf_ids(blockList, nblocks: int, leaf) -> np.ndarray:
+    """0-based int32 copy of a list of FLASH (1-based) block ids, checked on
+    the host before any launch: every id names a leaf block of the store and
+    appears once. The C entry points take device lists and index the block
+    store with them unchecked, so a bad id must not get that far: FLASH's
+    own callers pass the leaf list of the local blocks, each once."""
+    ids = np.asarray(blockList).reshape(-1)
+    if ids.size and not np.issubdtype(ids.dtype, np.integer):
+        raise GBError(f"block ids must be integers, not {ids.dtype}")
+    ids = ids.astype(np.int64) - 1  # FLASH ids are 1-based
+    bad = (ids < 0) | (ids >= nblocks)
+    if bad.any():
+        raise GBError(f"block id {int(ids[bad][0]) + 1} outside 1..{nblocks}")
+    isleaf = np.zeros(nblocks, bool)
+    isleaf[np.asarray(leaf, np.int64)] = True
+    if not isleaf[ids].all():
+        raise GBError(f"block id {int(ids[~isleaf[ids]][0]) + 1} is not a leaf block")
+    u, n = np.unique(ids, return_counts=True)
+    if (n > 1).any():
+        raise GBError(f"block id {int(u[n > 1][0]) + 1} listed more than once")
+    return ids.astype(np.int32)
+
+
 class Grid:
     """Device block store + block tree registered with the library."""
 
@@ -309,7 +332,7 @@ class Grid:
     def list_tensor(self, blockList=None):
         if blockList is None:
             return self.t_leaf, len(self.leaf)
-        ids = np.asarray(blockList, np.int32) - 1  # FLASH ids are 1-based
+        ids = check_leaf_ids(blockList, self.nblocks, self.leaf)
         return self.torch.as_tensor(ids, device=self.u.device), len(ids)
 
     def fill_guardcells(self, blockList=None):
@@ -461,8 +484,12 @@ def Heat(blockCount: int, blockList, dt: float, time: float):
 
 def Driver_computeDt(blockCount: int, blockList) -> float:
     """CFL minimum over the listed leaf blocks (the device reduction that
-    replaces Hydro_computeDt + MPI_AllReduce MINLOC)."""
+    replaces Hydro_computeDt + MPI_AllReduce MINLOC). With no blocks the
+    local limit stays at its start value, huge(1.0) (Driver_computeDt.F90:114,
+    222), as on a rank that holds no leaf blocks."""
     g = _require()
+    if blockCount == 0:
+        return float(np.finfo(np.float64).max)
     return float(g.compute_dt(np.asarray(blockList)[:blockCount]).item())
 
 
