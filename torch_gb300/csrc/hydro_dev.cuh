@@ -988,54 +988,65 @@ __device__ __forceinline__ R upw(R f, R a, R b)
 // in the mixed path); it is stored as double and the face-B update that
 // consumes it stays FP64. Every edge value is shared by the four faces
 // around the edge, so div B is kept to round-off in either precision.
-// the edges of direction C (a compile-time axis, so the axis permutations
-// of every index fold away)
+// One CTA takes one plane C of the edges of direction CD (a compile-time
+// axis, so the axis permutations of every index fold away): the cell-centred
+// field of the plane's 18 x 18 cells is computed once into shared memory
+// (each value serves four edges), then each thread makes one of the 17 x 17
+// edges from its four face fluxes and four cell values.
+constexpr int EMF_THREADS = 320;
+constexpr int EMF_CELLS = RB * RB;     // cells 3..20 across the plane
+constexpr int EMF_EDGES = 17 * 17;     // edges 4..20 across the plane
+
 template <typename T, int CD>
-__device__ __forceinline__ void emf_edge(const gb_dev_grid& g, const int* __restrict__ list, const T* __restrict__ fscr,
-                                         size_t fstride, double* __restrict__ escr, size_t estride,
-                                         const float* __restrict__ p32, size_t p32_stride)
+__device__ __forceinline__ void emf_plane(const gb_dev_grid& g, const int* __restrict__ list, const T* __restrict__ fscr,
+                                          size_t fstride, double* __restrict__ escr, size_t estride,
+                                          const float* __restrict__ p32, size_t p32_stride, T* s_ecc)
 {
     using R = T;
     constexpr int c = CD;
-    const int cb = blockIdx.z;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= NEDGE) return;
-    const int blk = list[cb];
     constexpr int a = (c + 1) % 3, b = (c + 2) % 3;
-    const int A = LO + e % 17, B = LO + (e / 17) % 17, C = LO + e / (17 * 17);
+    const int cb = blockIdx.z;
+    const int blk = list[cb];
+    const int C = LO + blockIdx.x;
+    int t[3];
+    auto at = [&](int av, int bv, int cv) { t[a] = av; t[b] = bv; t[c] = cv; };
+    const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
+    const float* pb = p32 + (size_t)cb * p32_stride;
+    for (int q = threadIdx.x; q < EMF_CELLS; q += EMF_THREADS) {
+        at(RLO + q % RB, RLO + q / RB, C);
+        const int ci = gb_cidx(t[0], t[1], t[2]);
+        R va, vb, Ba, Bb;
+        if constexpr (std::is_same<T, float>::value) {
+            va = pb[(size_t)(1 + a) * GB_N3 + ci];
+            vb = pb[(size_t)(1 + b) * GB_N3 + ci];
+            Ba = pb[(size_t)(5 + a) * GB_N3 + ci];
+            Bb = pb[(size_t)(5 + b) * GB_N3 + ci];
+        } else {
+            va = base[(int64_t)g.slot[GB_VELX + a] * GB_N3 + ci];
+            vb = base[(int64_t)g.slot[GB_VELX + b] * GB_N3 + ci];
+            Ba = base[(int64_t)g.slot[GB_MAGX + a] * GB_N3 + ci];
+            Bb = base[(int64_t)g.slot[GB_MAGX + b] * GB_N3 + ci];
+        }
+        s_ecc[q] = vb * Ba - va * Bb;
+    }
+    __syncthreads();
+    const int q = threadIdx.x;
+    if (q >= EMF_EDGES) return;
+    const int A = LO + q % 17, B = LO + q / 17;
+    const int e = q + EMF_EDGES * (C - LO);
     const T* fs = fscr + (size_t)cb * fstride;
     auto fl = [&](int d, int var, int x0, int x1, int x2) -> R {
         return (R)fs[(size_t)d * NFLX * NFC + (size_t)var * NFC + flux_index(d, x0, x1, x2)];
     };
-    int t[3];
-    auto at = [&](int av, int bv, int cv) { t[a] = av; t[b] = bv; t[c] = cv; };
     at(A, B - 1, C); R ea0 = -fl(a, 5 + b, t[0], t[1], t[2]); R ma0 = fl(a, 0, t[0], t[1], t[2]);
     at(A, B, C);     R ea1 = -fl(a, 5 + b, t[0], t[1], t[2]); R ma1 = fl(a, 0, t[0], t[1], t[2]);
     at(A - 1, B, C); R eb0 = fl(b, 5 + a, t[0], t[1], t[2]);  R mb0 = fl(b, 0, t[0], t[1], t[2]);
     at(A, B, C);     R eb1 = fl(b, 5 + a, t[0], t[1], t[2]);  R mb1 = fl(b, 0, t[0], t[1], t[2]);
-    const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
-    const float* pb = p32 + (size_t)cb * p32_stride;
     R ecc[2][2];
 #pragma unroll
     for (int ia = 0; ia < 2; ++ia)
 #pragma unroll
-        for (int ib = 0; ib < 2; ++ib) {
-            at(A - 1 + ia, B - 1 + ib, C);
-            int ci = gb_cidx(t[0], t[1], t[2]);
-            R va, vb, Ba, Bb;
-            if constexpr (std::is_same<T, float>::value) {
-                va = pb[(size_t)(1 + a) * GB_N3 + ci];
-                vb = pb[(size_t)(1 + b) * GB_N3 + ci];
-                Ba = pb[(size_t)(5 + a) * GB_N3 + ci];
-                Bb = pb[(size_t)(5 + b) * GB_N3 + ci];
-            } else {
-                va = base[(int64_t)g.slot[GB_VELX + a] * GB_N3 + ci];
-                vb = base[(int64_t)g.slot[GB_VELX + b] * GB_N3 + ci];
-                Ba = base[(int64_t)g.slot[GB_MAGX + a] * GB_N3 + ci];
-                Bb = base[(int64_t)g.slot[GB_MAGX + b] * GB_N3 + ci];
-            }
-            ecc[ia][ib] = vb * Ba - va * Bb;
-        }
+        for (int ib = 0; ib < 2; ++ib) ecc[ia][ib] = s_ecc[(A - 1 + ia - RLO) + RB * (B - 1 + ib - RLO)];
     const R two = (R)2, eighth = (R)0.125;
     R eavg = (R)0.25 * (ea0 + ea1 + eb0 + eb1);
     R dbm = upw<R>(ma0, two * (eb0 - ecc[0][0]), two * (eb1 - ecc[1][0]));
@@ -1047,14 +1058,16 @@ __device__ __forceinline__ void emf_edge(const gb_dev_grid& g, const int* __rest
     else escr[(size_t)cb * estride + (size_t)c * NEDGE + e] = ev;
 }
 
+// grid (16 planes, 3 directions, blocks)
 template <typename T>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(EMF_THREADS)
 k_emf(gb_dev_grid g, const int* __restrict__ list, const T* __restrict__ fscr, size_t fstride,
       double* __restrict__ escr, size_t estride, const float* __restrict__ p32, size_t p32_stride)
 {
-    if (blockIdx.y == 0) emf_edge<T, 0>(g, list, fscr, fstride, escr, estride, p32, p32_stride);
-    else if (blockIdx.y == 1) emf_edge<T, 1>(g, list, fscr, fstride, escr, estride, p32, p32_stride);
-    else emf_edge<T, 2>(g, list, fscr, fstride, escr, estride, p32, p32_stride);
+    __shared__ T s_ecc[EMF_CELLS];
+    if (blockIdx.y == 0) emf_plane<T, 0>(g, list, fscr, fstride, escr, estride, p32, p32_stride, s_ecc);
+    else if (blockIdx.y == 1) emf_plane<T, 1>(g, list, fscr, fstride, escr, estride, p32, p32_stride, s_ecc);
+    else emf_plane<T, 2>(g, list, fscr, fstride, escr, estride, p32, p32_stride, s_ecc);
 }
 
 __device__ __forceinline__ int edge_index(int c, int i, int j, int k)
