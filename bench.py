@@ -648,7 +648,7 @@ def main():
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
                      "frac": ach / hbm,
                      "traffic": TRAFFIC_B_PER_ZONE[dom] * zones_per_launch if dom in TRAFFIC_B_PER_ZONE else None,
-                     "traffic_source": "ncu DRAM bytes per zone of this kernel on the 128^3 box at 128-block chunks, "
+                     "traffic_source": "ncu DRAM bytes per zone of this kernel on the 128^3 box at 512-block chunks, "
                                        "times the zones of one launch here",
                      "peak_kind": hbm_kind, "launch_ms": dom_ms / dom_n,
                      "algo_bytes_per_launch": 216.0 * zones_per_launch},

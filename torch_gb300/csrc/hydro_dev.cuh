@@ -106,6 +106,13 @@ __device__ __forceinline__ T two3() { return (T)(2.0 / 3.0); }
 template <>
 __device__ __forceinline__ float two3<float>() { return 2.0f / 3.0f; }
 
+// x / 6: the oracle's division in FP64; in FP32 (whose divisions are
+// approximate in the mixed path anyway) a product with the rounded 1/6
+template <typename T>
+__device__ __forceinline__ T over6(T x) { return x / (T)6; }
+template <>
+__device__ __forceinline__ float over6<float>(float x) { return x * (1.0f / 6.0f); }
+
 template <typename T>
 __device__ __forceinline__ T minmod(T a, T b)
 {
@@ -238,22 +245,29 @@ __device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* 
     T lam[MAXW], R[MAXW][MAXW], L[MAXW][MAXW];
     if (MHD) eig_mhd<T>(gam, qs[2], lam, R, L);
     else eig_hydro<T>(gam, qs[2], lam, R, L);
+    // characteristic differences L (q[m+1] - q[m]) of the four stencil
+    // intervals, each formed once: cell m's limited slope takes intervals
+    // m - 1 and m (the same sums, in the same order, as forming both per cell)
+    T ld[4][MAXW];
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+        for (int k = 0; k < nw; ++k) {
+            T acc = (T)0;
+#pragma unroll
+            for (int s = 0; s < nw; ++s) {
+                const int qq = wslot(s);
+                if (!nz_L<MHD>(k, s)) continue;
+                acc = acc + L[k][s] * (qs[m + 1][qq] - qs[m][qq]);
+            }
+            ld[m][k] = acc;
+        }
     T dwm[3][MAXW];
 #pragma unroll
     for (int m = 1; m <= 3; ++m) {
         T da[MAXW];
 #pragma unroll
-        for (int k = 0; k < nw; ++k) {
-            T sl = (T)0, srr = (T)0;
-#pragma unroll
-            for (int s = 0; s < nw; ++s) {
-                const int qq = wslot(s);
-                if (!nz_L<MHD>(k, s)) continue;
-                sl = sl + L[k][s] * (qs[m][qq] - qs[m - 1][qq]);
-                srr = srr + L[k][s] * (qs[m + 1][qq] - qs[m][qq]);
-            }
-            da[k] = minmod<T>(sl, srr);
-        }
+        for (int k = 0; k < nw; ++k) da[k] = minmod<T>(ld[m - 1][k], ld[m][k]);
 #pragma unroll
         for (int s = 0; s < nw; ++s) {
             T acc = (T)0;
@@ -268,8 +282,8 @@ __device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* 
     for (int s = 0; s < nw; ++s) {
         const int qq = wslot(s);
         T qm = qs[1][qq], q0 = qs[2][qq], qp = qs[3][qq];
-        T wl = (T)0.5 * (qm + q0) - (dwm[1][s] - dwm[0][s]) / (T)6;
-        T wr = (T)0.5 * (q0 + qp) - (dwm[2][s] - dwm[1][s]) / (T)6;
+        T wl = (T)0.5 * (qm + q0) - over6<T>(dwm[1][s] - dwm[0][s]);
+        T wr = (T)0.5 * (q0 + qp) - over6<T>(dwm[2][s] - dwm[1][s]);
         wl = fmax(fmin(q0, qm), wl);
         wl = fmin(fmax(q0, qm), wl);
         wr = fmax(fmin(q0, qp), wr);
