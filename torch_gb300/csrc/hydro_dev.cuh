@@ -854,21 +854,22 @@ __device__ __forceinline__ void hlld(T gam, const T* L, const T* R, T* F, T* un)
         F[s] = (left ? FL[s] : FR[s]) + S * (Ua[s] - Uoa[s]) + Sst * (Uss[s] - Ua[s]);
 }
 
-// flux box of direction d: normal faces 4..20 (17), transverse cells 3..20 (18)
+// flux box of direction d: along d faces 4..20 (17), across d cells 3..20
+// (18), x fastest whatever d is, so that neighbouring threads read
+// neighbouring cells and faces in every direction (a normal-first order
+// puts neighbouring y and z faces 18 and 324 cells apart)
 __device__ __forceinline__ void flux_coords(int d, int f, int* I)
 {
-    int e0 = f % 17, e1 = (f / 17) % RB, e2 = f / (17 * RB);
-    // axis order: normal first, then the two transverse axes in x<y<z order
-    int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
-    I[d] = LO + e0;
-    I[t1] = RLO + e1;
-    I[t2] = RLO + e2;
+    const int n0 = d == 0 ? 17 : RB, n1 = d == 1 ? 17 : RB;
+    const int e0 = f % n0, e1 = (f / n0) % n1, e2 = f / (n0 * n1);
+    I[0] = (d == 0 ? LO : RLO) + e0;
+    I[1] = (d == 1 ? LO : RLO) + e1;
+    I[2] = (d == 2 ? LO : RLO) + e2;
 }
 __device__ __forceinline__ int flux_index(int d, int i, int j, int k)
 {
-    int I[3] = {i, j, k};
-    int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
-    return (I[d] - LO) + 17 * ((I[t1] - RLO) + RB * (I[t2] - RLO));
+    const int n0 = d == 0 ? 17 : RB, n1 = d == 1 ? 17 : RB;
+    return (i - (d == 0 ? LO : RLO)) + n0 * ((j - (d == 1 ? LO : RLO)) + n1 * (k - (d == 2 ? LO : RLO)));
 }
 __device__ __forceinline__ int rc_index(int i, int j, int k)
 {
@@ -1026,8 +1027,11 @@ __device__ __forceinline__ void emf_plane(const gb_dev_grid& g, const int* __res
     auto at = [&](int av, int bv, int cv) { t[a] = av; t[b] = bv; t[c] = cv; };
     const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
     const float* pb = p32 + (size_t)cb * p32_stride;
+    // x runs fastest across the threads where the plane has an x axis (it is
+    // a for c = 2 and b for c = 1), so that their loads are contiguous
     for (int q = threadIdx.x; q < EMF_CELLS; q += EMF_THREADS) {
-        at(RLO + q % RB, RLO + q / RB, C);
+        const int qa = c == 1 ? q / RB : q % RB, qb = c == 1 ? q % RB : q / RB;
+        at(RLO + qa, RLO + qb, C);
         const int ci = gb_cidx(t[0], t[1], t[2]);
         R va, vb, Ba, Bb;
         if constexpr (std::is_same<T, float>::value) {
@@ -1041,13 +1045,13 @@ __device__ __forceinline__ void emf_plane(const gb_dev_grid& g, const int* __res
             Ba = base[(int64_t)g.slot[GB_MAGX + a] * GB_N3 + ci];
             Bb = base[(int64_t)g.slot[GB_MAGX + b] * GB_N3 + ci];
         }
-        s_ecc[q] = vb * Ba - va * Bb;
+        s_ecc[qa + RB * qb] = vb * Ba - va * Bb;
     }
     __syncthreads();
     const int q = threadIdx.x;
     if (q >= EMF_EDGES) return;
-    const int A = LO + q % 17, B = LO + q / 17;
-    const int e = q + EMF_EDGES * (C - LO);
+    const int A = LO + (c == 1 ? q / 17 : q % 17), B = LO + (c == 1 ? q % 17 : q / 17);
+    const int e = (A - LO) + 17 * (B - LO) + EMF_EDGES * (C - LO);
     const T* fs = fscr + (size_t)cb * fstride;
     auto fl = [&](int d, int var, int x0, int x1, int x2) -> R {
         return (R)fs[(size_t)d * NFLX * NFC + (size_t)var * NFC + flux_index(d, x0, x1, x2)];
