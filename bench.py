@@ -46,13 +46,13 @@ WORKLOADS = {
 TDUST0 = 18.0  # initial dust temperature [K] (sim_tdust, flash.par.turbsph_standard:19)
 
 # DRAM bytes (read + write) per interior zone of each profiler category of
-# the fast path, from one ncu capture (profiles/kernels_box128_fast_chunk512.md:
-# the 128^3 box at 512-block chunks; "recon" = primitive conversion +
-# reconstruction, "guard_fill" = cells + faces, "sur_feat" from an earlier
-# capture of the feature kernel, which the update now replaces). The
-# roofline's traffic is this times the zones one launch covers.
-TRAFFIC_B_PER_ZONE = {"recon": 708.9, "update": 363.6, "flux": 478.9, "guard_fill": 304.4, "mlp_infer": 16.0,
-                      "sur_accept": 111.0, "emf": 114.2, "faceb": 81.2, "sur_feat": 36.0, "dt": 97.8}
+# the fast path, from ncu captures of the 128^3 box at 512-block chunks
+# ("recon" = primitive conversion + reconstruction, "guard_fill" = cells +
+# faces, "sur_feat" from an earlier capture of the feature kernel, which the
+# update now replaces). The roofline's traffic is this times the zones one
+# launch covers.
+TRAFFIC_B_PER_ZONE = {"recon": 709.1, "update": 367.4, "flux": 477.5, "guard_fill": 304.4, "mlp_infer": 16.0,
+                      "sur_accept": 111.0, "emf": 114.5, "faceb": 81.2, "sur_feat": 36.0, "dt": 97.8}
 
 
 def build_workload(wl, device):
