@@ -1095,19 +1095,20 @@ __device__ __forceinline__ int edge_index(int c, int i, int j, int k)
     return (I[a] - LO) + 17 * ((I[b] - LO) + 17 * (I[c] - LO));
 }
 
-// interior face box of direction a: normal 4..20 (17), transverse 4..19 (16)
+// interior face box of direction a: along a 4..20 (17), across a 4..19
+// (16), x fastest whatever a is (neighbouring threads take neighbouring
+// faces and cells)
 __device__ __forceinline__ void fb_coords(int a, int f, int* I)
 {
-    int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
-    I[a] = LO + f % 17;
-    I[t1] = LO + (f / 17) % 16;
-    I[t2] = LO + f / (17 * 16);
+    const int n0 = a == 0 ? 17 : 16, n1 = a == 1 ? 17 : 16;
+    I[0] = LO + f % n0;
+    I[1] = LO + (f / n0) % n1;
+    I[2] = LO + f / (n0 * n1);
 }
 __device__ __forceinline__ int fb_index(int a, int i, int j, int k)
 {
-    int I[3] = {i, j, k};
-    int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
-    return (I[a] - LO) + 17 * ((I[t1] - LO) + 16 * (I[t2] - LO));
+    const int n0 = a == 0 ? 17 : 16, n1 = a == 1 ? 17 : 16;
+    return (i - LO) + n0 * ((j - LO) + n1 * (k - LO));
 }
 
 template <int A>
@@ -1438,11 +1439,15 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
     auto over_rn = [&](double x) { return RCP ? x * irn : x / rn; };
     double ek = over_rn(0.5 * (Un[1] * Un[1] + Un[2] * Un[2] + Un[3] * Un[3]));
     double em = 0.5 * (Bn[0] * Bn[0] + Bn[1] * Bn[1] + Bn[2] * Bn[2]);
-    double eiE = over_rn((Un[4] - ek) - em);
+    const double xE = (Un[4] - ek) - em;  // rho e from the total energy
+    double eiE = over_rn(xE);
     double eia = over_rn(ren);
-    bool use_E = eiE > kp.eint_switch * over_rn(Un[4]);
+    // the mixed path compares and forms the pressure before the division by
+    // rho (the same quantities with two FP64 operations fewer); the FP64 path
+    // keeps the oracle's operations
+    bool use_E = RCP ? xE > kp.eint_switch * Un[4] : eiE > kp.eint_switch * over_rn(Un[4]);
     double ei = use_E ? eiE : eia;
-    double pn = gm1 * rn * ei;
+    double pn = RCP ? gm1 * (use_E ? xE : ren) : gm1 * rn * ei;
     bool floored = false;
     if (pn < kp.smallp) {
         pn = kp.smallp;
@@ -1450,7 +1455,9 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
         floored = true;
     }
     double vxn = over_rn(Un[1]), vyn = over_rn(Un[2]), vzn = over_rn(Un[3]);
-    double ekin_s = 0.5 * (vxn * vxn + vyn * vyn + vzn * vzn);
+    // specific kinetic energy: ek / rho in the mixed path (one FP64 product
+    // instead of four)
+    double ekin_s = RCP ? ek * irn : 0.5 * (vxn * vxn + vyn * vyn + vzn * vzn);
     if (COOL) {
         // fused heating/cooling epilogue (RadHeat.F90:223-423 on the new state)
         const gb_cool_params& p = cool.p;
