@@ -483,11 +483,11 @@ __global__ void k_sur_feat(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_unit
 // slope (its two points within 5 % of each other) and the energy moved
 // the way the rate at the old state points; otherwise it goes to the
 // fallback list and the plain integrator solves it.
-// seven resident CTAs per SM (68 registers, no spills): the kernel waits
-// on memory and on the rate evaluations' MUFU results, and more warps hide
-// that
+// eight resident CTAs per SM (64 registers, no spills; seven with the FP64
+// re-check, which would spill at eight): the kernel waits on memory and on
+// the rate evaluations' MUFU results, and more warps hide that
 template <bool CHECK64>
-__global__ void __launch_bounds__(128, 7) k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_units un, double gamma,
+__global__ void __launch_bounds__(128, CHECK64 ? 7 : 8) k_sur_accept(gb_dev_grid g, gb_cool_ctx c, gb_cool_pf pf, sur_units un, double gamma,
                              const int* __restrict__ list, int64_t ncell, double dt_code, const double* __restrict__ dtp,
                              const float* __restrict__ y, const float2* __restrict__ f0a, double rel_tol,
                              int* __restrict__ rej, int* __restrict__ nrej, gb_status* st)

@@ -60,7 +60,7 @@ __device__ __forceinline__ void gb_step_guard_cell(int q, int& i, int& j, int& k
 // the z arms
 constexpr int GB_STEP_ROWS = GB_BAND * GB_BAND + 2 * 4 * GB_BAND;  // 468
 constexpr int GB_STEP_CELLS = GB_STEP_ROWS * GB_N;                  // 11232
-static_assert(GB_N % 2 == 0 && (GB_N3 * 8) % 16 == 0, "cell pairs of the FP32 copy are 16-byte aligned");
+static_assert(GB_N % 4 == 0 && (GB_N3 * 8) % 32 == 0, "four-cell groups of the FP32 copy are 16-byte aligned");
 __device__ __forceinline__ void gb_step_cell(int q, int& i, int& j, int& k)
 {
     const int row = q / GB_N;

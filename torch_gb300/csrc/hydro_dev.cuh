@@ -50,6 +50,13 @@ struct scratch_layout {
     static constexpr size_t bytes =
         recon * sizeof(T) + flux * sizeof(T) + (emf + fb) * sizeof(double) + prim32 * sizeof(float);
 };
+// the FP32 copy of each block starts on a 16-byte boundary (k_prim32 stores
+// four cells at a time): every section before it and its own stride are
+// multiples of 16 bytes
+static_assert((scratch_layout<float>::recon * 4 + scratch_layout<float>::flux * 4 +
+               (scratch_layout<float>::emf + scratch_layout<float>::fb) * 8) % 16 == 0 &&
+                  (scratch_layout<float>::prim32 * 4) % 16 == 0,
+              "FP32 copy 16-byte aligned");
 
 // FP32 copy of the primitive variables of the padded blocks: the mixed
 // path converts each double once here instead of at every stencil read
@@ -58,14 +65,15 @@ template <bool MHD>
 __global__ void __launch_bounds__(128)
 k_prim32(gb_dev_grid g, const int* __restrict__ list, float* __restrict__ p32, size_t stride)
 {
-    // threads [0, GB_STEP_CELLS / 2): pairs of x-neighbouring cells of the
-    // step's read region (rows are whole and even, so a pair is one 16-byte
-    // load per variable); then (MHD) its faces, axis by axis
+    // threads [0, GB_STEP_CELLS / 4): groups of four x-neighbouring cells of
+    // the step's read region (rows are whole and a multiple of four long, so
+    // a group is two 16-byte loads and one 16-byte store per variable); then
+    // (MHD) its faces, axis by axis
     const int cb = blockIdx.y;
     int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < GB_STEP_CELLS / 2) {
+    if (q < GB_STEP_CELLS / 4) {
         int i, j, k;
-        gb_step_cell(2 * q, i, j, k);
+        gb_step_cell(4 * q, i, j, k);
         const int c = gb_cidx(i, j, k);
         const double* base = g.unk + (int64_t)list[cb] * g.nvar * GB_N3 + c;
         float* out = p32 + (size_t)cb * stride + c;
@@ -73,15 +81,18 @@ k_prim32(gb_dev_grid g, const int* __restrict__ list, float* __restrict__ p32, s
 #pragma unroll
         for (int v = 0; v < NP32; ++v) {
             if (!MHD && v >= 5 && v < 8) {
-                *reinterpret_cast<float2*>(out + (size_t)v * GB_N3) = make_float2(0.0f, 0.0f);
+                *reinterpret_cast<float4*>(out + (size_t)v * GB_N3) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 continue;
             }
-            const double2 x = *reinterpret_cast<const double2*>(base + (int64_t)g.slot[roles[v]] * GB_N3);
-            *reinterpret_cast<float2*>(out + (size_t)v * GB_N3) = make_float2(gb_d2f(x.x), gb_d2f(x.y));
+            const double* src = base + (int64_t)g.slot[roles[v]] * GB_N3;
+            const double2 x0 = *reinterpret_cast<const double2*>(src);
+            const double2 x1 = *reinterpret_cast<const double2*>(src + 2);
+            *reinterpret_cast<float4*>(out + (size_t)v * GB_N3) =
+                make_float4(gb_d2f(x0.x), gb_d2f(x0.y), gb_d2f(x1.x), gb_d2f(x1.y));
         }
         return;
     }
-    q -= GB_STEP_CELLS / 2;
+    q -= GB_STEP_CELLS / 4;
     if (!MHD || q >= GB_STEP_FACES_ALL) return;
     const int a = q < gb_step_faces(0) ? 0 : (q < gb_step_faces(0) + gb_step_faces(1) ? 1 : 2);
     const int e = q - (a == 0 ? 0 : (a == 1 ? gb_step_faces(0) : gb_step_faces(0) + gb_step_faces(1)));

@@ -57,7 +57,7 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
     float* p32 = (float*)(bscr + (size_t)nblk * SL::fb);
     const gb_dev_grid& g = g_gb.grid;
     if constexpr (SL::prim32 > 0) {
-        dim3 pg((GB_STEP_CELLS / 2 + (mhd ? GB_STEP_FACES_ALL : 0) + 127) / 128, nblk);
+        dim3 pg((GB_STEP_CELLS / 4 + (mhd ? GB_STEP_FACES_ALL : 0) + 127) / 128, nblk);
         gb_prof_begin(GBP_RECON, s);
         if (mhd) k_prim32<true><<<pg, 128, 0, s>>>(g, list, p32, SL::prim32);
         else k_prim32<false><<<pg, 128, 0, s>>>(g, list, p32, SL::prim32);
