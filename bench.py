@@ -51,8 +51,8 @@ TDUST0 = 18.0  # initial dust temperature [K] (sim_tdust, flash.par.turbsph_stan
 # faces, "sur_feat" from an earlier capture of the feature kernel, which the
 # update now replaces). The roofline's traffic is this times the zones one
 # launch covers.
-TRAFFIC_B_PER_ZONE = {"recon": 709.1, "update": 367.4, "flux": 477.5, "guard_fill": 304.4, "mlp_infer": 16.0,
-                      "sur_accept": 111.0, "emf": 114.5, "faceb": 81.2, "sur_feat": 36.0, "dt": 97.8}
+TRAFFIC_B_PER_ZONE = {"recon": 708.6, "update": 367.4, "flux": 477.5, "guard_fill": 304.4, "mlp_infer": 16.0,
+                      "sur_accept": 111.5, "emf": 114.5, "faceb": 81.2, "sur_feat": 36.0, "dt": 97.8}
 
 
 def build_workload(wl, device):
