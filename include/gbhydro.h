@@ -136,7 +136,11 @@ int gb_hydro_init(const gb_hydro_params* p);
 /* One unsplit step over blockCount leaf blocks (blockList: device int
  * array of store block ids, 0-based). Replaces hy_uhd_unsplit; dtOld is
  * accepted for signature parity and unused (as in the second-order
- * unsplit scheme). Guard cells must have been filled. st: device status. */
+ * unsplit scheme). Guard cells must have been filled. st: device status.
+ * The ids of this and every other device block list index the store
+ * unchecked: each must name a leaf block below maxblocks, once, as the
+ * leaf lists FLASH passes to Hydro do (the Python layer checks host lists
+ * before it copies them). */
 int gb_hydro_unsplit(int blockCount, const int* blockList_dev, double dt, double dtOld,
                      gb_status* st_dev, void* stream);
 
