@@ -14,7 +14,7 @@ from __future__ import annotations
 import json
 import os
 
-CHUNKS = (32, 64, 128, 256, 512)
+CHUNKS = (32, 64, 128, 256, 512, 1024)
 TILES = (32, 64)
 OCCS = (0, 1, 2)
 STREAMS = (1, 2)

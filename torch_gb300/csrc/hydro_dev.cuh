@@ -982,8 +982,10 @@ __device__ __forceinline__ void flux_face(gb_dev_grid g, hydro_kparams kp, const
         }
     }
     T* fs = fscr + (size_t)cb * fstride + (size_t)d * NFLX * NFC;
+    // the normal field's flux (and hydro's field fluxes) are never read: not stored
 #pragma unroll
-    for (int s = 0; s < NP; ++s) fs[(size_t)s * NFC + f] = out[s];
+    for (int s = 0; s < NP; ++s)
+        if (s != 5 + d && (MHD || s < 5)) fs[(size_t)s * NFC + f] = out[s];
     fs[(size_t)8 * NFC + f] = feint;
     fs[(size_t)9 * NFC + f] = un;
 }
