@@ -85,6 +85,16 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def clocks_csv_path(args):
+    """Where the sampled clocks go: --clocks-csv, else a file in the system's
+    temporary directory (the JSON line carries their summary either way)."""
+    import tempfile
+    path = args.clocks_csv or os.path.join(tempfile.gettempdir(), "gbhydro_bench_clocks.csv")
+    d = os.path.dirname(os.path.abspath(path))
+    os.makedirs(d, exist_ok=True)
+    return path
+
+
 class ClockSampler:
     def __init__(self, path):
         self.path = path
@@ -399,8 +409,7 @@ def lite_run(args, G, wl, tree, st, zones, world, rank, t_ic):
     g_fast = make_grid(G, tree, st)
     del st
     torch.cuda.empty_cache()
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    clk = ClockSampler(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv"))
+    clk = ClockSampler(clocks_csv_path(args))
     with clk:
         ms_plain, st_plain, pinfo = run_path(G, g_plain, 0, args.steps, args.warmup, graph=True,
                                              tune=not args.no_tune,
@@ -450,6 +459,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (16 blocks, tile 32)")
     ap.add_argument("--weights", default=None, help="load surrogate weights (.npy) instead of training")
+    ap.add_argument("--clocks-csv", default=None,
+                    help="file for the nvidia-smi clock samples of the timed region (default: a temporary file)")
     # (--workload amr16k: the 16381-block, 5-level case; ~90 GB on the device)
     ap.add_argument("--save-weights", default=None)
     ap.add_argument("--ncu-range", action="store_true",
@@ -541,8 +552,7 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         cs = CpuStep(wl, tree, st)
     del st
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    clk = ClockSampler(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv"))
+    clk = ClockSampler(clocks_csv_path(args))
     if world > 1:
         dist.barrier()
     with clk:
