@@ -483,8 +483,9 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     from torch_gb300 import gbhydro as G
     wl = WORKLOADS[args.workload]
-    # replicas: every rank runs its own copy of the workload (the step has no
-    # cross-GPU exchange on one-GPU machines)
+    # replicas: every rank runs its own copy of the workload; the only
+    # cross-rank exchange is the timing reduction (and the CFL minimum, when
+    # ranks share one grid, in blocklist.global_dt)
     t0 = time.perf_counter()
     tree, st = build_workload(wl, "cuda")
     t_ic = time.perf_counter() - t0
