@@ -350,13 +350,20 @@ def e2e_run(G, g, steps, warmup, tune=False):
 
 
 def rel_stats(x, ref):
-    """Distribution of |x - ref| / ref over interior cells (torch tensors)."""
+    """Distribution of |x - ref| / ref over interior cells (torch tensors).
+    Cells where either value is non-finite, or the reference is zero, are
+    counted apart (n_bad) and left out of the quantiles."""
     import torch
-    r = ((x - ref).abs() / ref.abs()).flatten()
+    x, ref = x.flatten(), ref.flatten()
+    ok = torch.isfinite(x) & torch.isfinite(ref) & (ref != 0)
+    n_bad = int((~ok).sum())
+    r = (x[ok] - ref[ok]).abs() / ref[ok].abs()
+    if r.numel() == 0:
+        return {"p50": None, "p99": None, "p999": None, "max": None, "frac_within_1pct": 0.0, "n_bad": n_bad}
     sub = r[torch.randperm(r.numel(), device=r.device)[:1 << 22]]
     q = torch.quantile(sub, torch.tensor([0.5, 0.99, 0.999], dtype=r.dtype, device=r.device)).tolist()
     return {"p50": q[0], "p99": q[1], "p999": q[2], "max": float(r.max()),
-            "frac_within_1pct": float((r <= 0.01).double().mean())}
+            "frac_within_1pct": float((r <= 0.01).double().sum()) / x.numel(), "n_bad": n_bad}
 
 
 def cooling_one_step(G, grids, src, leaves):
@@ -654,8 +661,9 @@ def main():
                       "train_loss_final": float(np.mean(losses[-200:])),
                       "accepted": st_fast["n_surrogate"], "fallback": st_fast["n_surrogate_reject"],
                       "fallback_frac": st_fast["n_surrogate_reject"] / max(1, st_fast["n_surrogate"] + st_fast["n_surrogate_reject"])},
-        "status": {"plain": {k: st_plain[k] for k in ("code", "n_fallback", "n_eint_switch", "n_bracket_fail")},
-                   "fast": {k: st_fast[k] for k in ("code", "n_fallback", "n_eint_switch", "n_bracket_fail")}},
+        "status": {name: {k: stt[k] for k in ("code", "n_code", "n_fallback", "n_rh_fallback", "n_eint_switch",
+                                                 "n_bracket_fail", "n_clamped")}
+                   for name, stt in (("plain", st_plain), ("fast", st_fast), ("mixed_plain_cooling", st_mixed))},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
                      "frac": ach / hbm,
                      "traffic": TRAFFIC_B_PER_ZONE[dom] * zones_per_launch if dom in TRAFFIC_B_PER_ZONE else None,

@@ -36,7 +36,8 @@ typedef enum gb_rc {
     GB_ERR_LIMIT = -5       /* request beyond a documented maximum */
 } gb_rc;
 
-/* kernel status codes (gb_status.code; first error wins) */
+/* kernel status codes (gb_status.code holds the first; n_code[c] counts
+ * every cell that raised code c, so a later or rarer code is never hidden) */
 enum {
     GB_ST_OK = 0,
     GB_ST_NEG_DENS = 1,     /* density <= 0 after the update */
@@ -60,6 +61,9 @@ typedef struct gb_status {
     unsigned long long n_eint_switch;  /* dual-energy switch chose the advected e_int */
     unsigned long long n_surrogate;    /* cells cooled by the learned surrogate */
     unsigned long long n_surrogate_reject; /* surrogate rejected -> plain integrator */
+    unsigned long long n_code[8];      /* cells that raised each status code (index = code) */
+    unsigned long long n_rh_fallback;  /* hybrid order: face states of a direction that failed
+                                          the Rankine-Hugoniot check -> first order */
 } gb_status;
 
 /* ---------------------------------------------------------------- grid */
@@ -128,7 +132,22 @@ typedef struct gb_hydro_params {
     double eint_switch;     /* :164 */
     double smlrho, smallp;  /* floors in grid units */
     int precision;          /* 0 = all FP64, 1 = FP32 reconstruction/Riemann, FP64 update */
-    int pad;
+    int energy_fix;         /* energyFix (:213): the gas energy is taken from the total
+                               energy less the magnetic energy of the flux-updated cell
+                               field; the stored field is the staggered faces' mean */
+    int hybrid_order;       /* use_hybridOrder (:206): first-order face states where the
+                               flow compresses and a reconstructed state fails the
+                               Rankine-Hugoniot check (hy_uhd_dataReconstOneStep.F90:934-999,
+                               :1150-1218) */
+    int fallback_lower_cfl; /* hy_fallbackLowerCFL (:207) */
+    double hybrid_kappa;    /* hy_hybridOrderKappa: compression threshold, in units of the
+                               cell's fast speed (FLASH's default 0) */
+    double cfl_fallback_factor; /* hy_cflFallbackFactor (:208) */
+    int cfl_sum;            /* 1: the CFL limit of a cell is 1 / sum_d (|v_d| + c_f,d) / dx_d
+                               (stable for the unsplit step, whose transverse terms vanish
+                               on grid-scale modes); 0: min_d dx_d / (|v_d| + c_f,d) */
+    int shock_detect;       /* shockDetect + shockLowerCFL (:225-226): cells of a strong
+                               compressive shock take a lowered CFL in the next dt */
 } gb_hydro_params;
 
 int gb_hydro_init(const gb_hydro_params* p);
@@ -159,6 +178,15 @@ int gb_hydro_unsplit(int blockCount, const int* blockList_dev, double dt, double
 #define GB_NOALLOC_MAX_BLOCKS 4
 int gb_hydro_unsplit_noalloc(int blockCount, const int* blockList_dev, double dt, double dtOld,
                              gb_status* st_dev, void* stream);
+
+/* Per-cell CFL codes: every step's reconstruction records, for each
+ * interior cell, whether its states fell back to first order (positivity,
+ * or the hybrid-order Rankine-Hugoniot checks), and the next CFL limit
+ * scales that cell's limit by the lowered CFL over cfl (0.9 / 3 or 0.25;
+ * hy_uhd_dataReconstOneStep.F90:972, :1207-1216, :1240, the cellCfl
+ * argument). gb_register_grid clears them; this clears them again (e.g.
+ * after the caller restored an earlier state). */
+int gb_cfl_codes_reset(void* stream);
 
 /* Blocks per launch chunk of the hydro kernels (scratch = chunk x per-block
  * scratch; the autotuner picks it). Default 16. */

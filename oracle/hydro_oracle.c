@@ -7,9 +7,20 @@
  *   - multidimensional MHD terms aBn, dnBn            (:364-424)
  *   - normal-direction PPM per dimension              (:628-638 / :844-853)
  *   - transverse-flux corrections, hydro then MHD     (:1006-1089)
+ *   - hybrid-order fallback to first order where the flow compresses and
+ *     a face state fails the Rankine-Hugoniot check, before (:934-999) and
+ *     after (:1150-1218) the transverse corrections, with the per-cell CFL
+ *     lowering of hy_fallbackLowerCFL (:972, :1207-1216)
  *   - positivity fallback to first order              (:1230-1272)
- * The hybrid-order Rankine-Hugoniot fallback (:934-999, :1150-1218) calls
- * hy_uhd_checkRHjumpCond, whose body is not vendored; it is not applied.
+ * hy_uhd_checkRHjumpCond's body is not vendored (interface
+ * hy_uhd_interface.F90:798-807); rh_fail below writes it from the
+ * Rankine-Hugoniot relations: no single shock compresses an ideal gas by
+ * more than (gamma + 1) / (gamma - 1) (Toro 1997 eq. 3.58's strong-shock
+ * limit), so a face state whose density differs from its cell's by more is
+ * not shock-connected to it. Compression is Balsara & Spicer's (1999)
+ * undivided velocity divergence below kappa times the cell's fast speed,
+ * the minimum over the +-k4 box (k4 = 1 MHD, 2 hydro; :275-278) clipped to
+ * the reconstruction band, whose cells all have filled neighbours.
  *
  * The normal-direction PPM (interface hy_uhd_interface.F90:200-228) is
  * written from Colella & Woodward (1984) eqs. 1.6, 1.10, 1.12 with
@@ -48,6 +59,22 @@ void orc_hydro_default_params(orc_hydro_params* p, int mhd)
     p->mhd = mhd;
     p->nxb = 16;
     p->nguard = 4;
+    p->energy_fix = 1;
+    p->cfl_sum = 1;
+    p->hybrid_order = 1;
+    p->fallback_lower_cfl = 1;
+    p->hybrid_kappa = 0.0;
+    p->cfl_fallback_factor = 0.9;
+    p->cfl = 0.8;
+    p->cflc = NULL;
+}
+
+double orc_cfl_scale(const orc_hydro_params* p, int code)
+{
+    double s = 1.0;
+    if (code & 1) s = fmin(s, (p->cfl_fallback_factor / 3.0) / p->cfl);
+    if (code & 2) s = fmin(s, 0.25 / p->cfl);
+    return s;
 }
 
 /* ------------------------------------------------------------ indexing */
@@ -325,8 +352,17 @@ typedef struct recon_out {
     double wp[3][NP], wn[3][NP];
 } recon_out;
 
+/* hy_uhd_checkRHjumpCond for one face state: see the header */
+static int rh_fail(double gam, double rho_c, double rho_f)
+{
+    const double lim = (gam + 1.0) / (gam - 1.0);
+    return rho_f > lim * rho_c || rho_c > lim * rho_f;
+}
+
+/* flags: bit 0 positivity fallback, bit 1 first Rankine-Hugoniot fallback,
+ * bit 2 second one (any direction); codes[d] the CFL code of direction d */
 static int recon_cell(const orc_hydro_params* p, const blk* b, int i, int j, int k, double dt,
-                      const double* del, recon_out* o)
+                      const double* del, double divu_min, recon_out* o, unsigned char* codes)
 {
     const int nv = p->mhd ? 8 : 5;
     double wc[NP];
@@ -396,6 +432,27 @@ static int recon_cell(const orc_hydro_params* p, const blk* b, int i, int j, int
         }
     }
 
+    /* (Ia) hybrid order before the transverse corrections, :934-999 */
+    int comp = 0, flags = 0;
+    unsigned char code[3] = {0, 0, 0};
+    if (p->hybrid_order) {
+        double cs = p->gamma * wc[4] + (wc[5] * wc[5] + wc[6] * wc[6] + wc[7] * wc[7]);
+        cs = sqrt(cs / wc[0]);
+        comp = divu_min < p->hybrid_kappa * cs;
+        if (comp) {
+            for (int d = 0; d < 3; ++d) {
+                if (rh_fail(p->gamma, wc[0], o->wp[d][0]) || rh_fail(p->gamma, wc[0], o->wn[d][0])) {
+                    for (int v = 0; v < NP; ++v) {
+                        o->wp[d][v] = wc[v];
+                        o->wn[d][v] = wc[v];
+                    }
+                    if (p->fallback_lower_cfl) code[d] |= 1;
+                    flags |= 2;
+                }
+            }
+        }
+    }
+
     /* (II) transverse corrections, :1006-1089 */
     for (int v = 0; v < nv; ++v) {
         o->wn[0][v] = o->wn[0][v] - hd[1] * sig[1][v];
@@ -430,18 +487,38 @@ static int recon_cell(const orc_hydro_params* p, const blk* b, int i, int j, int
         }
     }
 
-    /* (IV) positivity fallback, :1230-1272 */
-    int fell = 0;
+    /* (Ib) hybrid order after the transverse corrections, :1150-1218; any
+     * direction's fallback lowers the cell's CFL to 0.25 (3-D) */
+    if (comp) {
+        for (int d = 0; d < 3; ++d) {
+            if (rh_fail(p->gamma, wc[0], o->wp[d][0]) || rh_fail(p->gamma, wc[0], o->wn[d][0])) {
+                for (int v = 0; v < NP; ++v) {
+                    o->wp[d][v] = wc[v];
+                    o->wn[d][v] = wc[v];
+                }
+                code[d] |= 2;
+                flags |= 4;
+            }
+        }
+    }
+
+    /* (IV) positivity fallback, :1230-1272, lowering the cell's CFL */
     for (int d = 0; d < 3; ++d) {
         if (o->wn[d][0] < 0.0 || o->wp[d][0] < 0.0 || o->wn[d][4] < 0.0 || o->wp[d][4] < 0.0) {
             for (int v = 0; v < NP; ++v) {
                 o->wn[d][v] = wc[v];
                 o->wp[d][v] = wc[v];
             }
-            fell = 1;
+            code[d] |= 1;
+            flags |= 1;
         }
     }
-    return fell;
+    if (codes) {
+        codes[0] = code[0];
+        codes[1] = code[1];
+        codes[2] = code[2];
+    }
+    return flags;
 }
 
 /* ------------------------------------------------------------ Riemann */
@@ -812,11 +889,38 @@ static int unsplit_block(const orc_hydro_params* p, double* u, double* bxf, doub
     const double gm1 = p->gamma - 1.0;
 
     recon_out* rec = (recon_out*)calloc((size_t)n3, sizeof(recon_out));
+    /* undivided velocity divergence over the band (hybrid order) */
+    double* divu = (double*)calloc((size_t)n3, sizeof(double));
+    if (p->hybrid_order) {
+        for (int k = rlo; k <= rhi; ++k)
+            for (int j = rlo; j <= rhi; ++j)
+                for (int i = rlo; i <= rhi; ++i)
+                    divu[cidx(n, i, j, k)] = 0.5 * (U(&b, ORV_VELX, i + 1, j, k) - U(&b, ORV_VELX, i - 1, j, k)) +
+                                             0.5 * (U(&b, ORV_VELY, i, j + 1, k) - U(&b, ORV_VELY, i, j - 1, k)) +
+                                             0.5 * (U(&b, ORV_VELZ, i, j, k + 1) - U(&b, ORV_VELZ, i, j, k - 1));
+    }
+    const int k4 = p->mhd ? 1 : 2;
     int nfall = 0;
     for (int k = rlo; k <= rhi; ++k)
         for (int j = rlo; j <= rhi; ++j)
-            for (int i = rlo; i <= rhi; ++i)
-                nfall += recon_cell(p, &b, i, j, k, dt, del, &rec[cidx(n, i, j, k)]);
+            for (int i = rlo; i <= rhi; ++i) {
+                double dmin = 1e300;
+                if (p->hybrid_order) {
+                    for (int kk = k - k4; kk <= k + k4; ++kk)
+                        for (int jj = j - k4; jj <= j + k4; ++jj)
+                            for (int ii = i - k4; ii <= i + k4; ++ii) {
+                                if (ii < rlo || ii > rhi || jj < rlo || jj > rhi || kk < rlo || kk > rhi) continue;
+                                double x = divu[cidx(n, ii, jj, kk)];
+                                if (x < dmin) dmin = x;
+                            }
+                }
+                unsigned char codes[3];
+                int fl = recon_cell(p, &b, i, j, k, dt, del, dmin, &rec[cidx(n, i, j, k)], codes);
+                nfall += fl & 1;
+                if (p->cflc && i >= lo && i <= hi && j >= lo && j <= hi && k >= lo && k <= hi)
+                    p->cflc[(i - lo) + nxb * ((j - lo) + nxb * (k - lo))] = (unsigned char)(codes[0] | codes[1] | codes[2]);
+            }
+    free(divu);
 
     /* fluxes: face index I = left face of cell I; faces lo..hi+1 in the
      * normal direction, cells rlo..rhi across */
@@ -998,6 +1102,7 @@ static int unsplit_block(const orc_hydro_params* p, double* u, double* bxf, doub
                 double rn = fmax(Un[0], p->smlrho);
                 double ek = 0.5 * (Un[1] * Un[1] + Un[2] * Un[2] + Un[3] * Un[3]) / rn;
                 double em = 0.5 * (Bn[0] * Bn[0] + Bn[1] * Bn[1] + Bn[2] * Bn[2]);
+                if (p->mhd && p->energy_fix) em = 0.5 * (Un[5] * Un[5] + Un[6] * Un[6] + Un[7] * Un[7]);
                 double eiE = ((Un[4] - ek) - em) / rn;
                 double eia = ren / rn;
                 double ei = (eiE > p->eint_switch * (Un[4] / rn)) ? eiE : eia;
@@ -1053,11 +1158,31 @@ double orc_block_dt_limit(const orc_hydro_params* p, const double* u, double dx,
                 if (p->mhd) for (int q = 0; q < 3; ++q) B[q] = u[(ORV_MAGX + q) * n3 + c];
                 double B2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
                 double t = (gp + B2) / rho;
+                double rate = 0.0, cell = 1e300;
                 for (int d = 0; d < 3; ++d) {
                     double v = fabs(u[(ORV_VELX + d) * n3 + c]);
                     double cf = sqrt(0.5 * (t + sqrt(fmax(t * t - 4.0 * gp * B[d] * B[d] / (rho * rho), 0.0))));
-                    double dtc = del[d] / (v + cf);
-                    if (dtc < best) best = dtc;
+                    if (p->cfl_sum) {
+                        rate = rate + (v + cf) / del[d];
+                    } else {
+                        double dtc = del[d] / (v + cf);
+                        if (dtc < cell) cell = dtc;
+                    }
+                }
+                if (!p->cfl_sum) {
+                    if (p->cflc) {
+                        int code = p->cflc[(i - ng) + nxb * ((j - ng) + nxb * (k - ng))];
+                        if (code) cell = cell * orc_cfl_scale(p, code);
+                    }
+                    if (cell < best) best = cell;
+                }
+                if (p->cfl_sum) {
+                    double lim = 1.0 / rate;
+                    if (p->cflc) {
+                        int code = p->cflc[(i - ng) + nxb * ((j - ng) + nxb * (k - ng))];
+                        if (code) lim = lim * orc_cfl_scale(p, code);
+                    }
+                    if (lim < best) best = lim;
                 }
             }
     return best;

@@ -36,7 +36,24 @@ typedef struct orc_hydro_params {
     double smlrho, smallp;
     int mhd;           /* 0: hydro (HLLC), 1: USM MHD (HLLD + CT) */
     int nxb, nguard;   /* 16, 4 */
+    int energy_fix;    /* energyFix, :213: gas energy from the flux-updated cell field */
+    int cfl_sum;       /* CFL limit 1 / sum_d (|v_d| + c_f,d) / dx_d instead of min_d */
+    int hybrid_order;  /* use_hybridOrder, :206 */
+    int fallback_lower_cfl; /* hy_fallbackLowerCFL, :207 */
+    double hybrid_kappa;    /* hy_hybridOrderKappa (FLASH default 0) */
+    double cfl_fallback_factor; /* hy_cflFallbackFactor, :208 */
+    double cfl;        /* cfl, :163 (the lowered CFL of a cell is a ratio to it) */
+    /* per-cell CFL codes (NULL: not kept): ORC_CFLC bytes per store block,
+     * interior cells x fastest; written by the step, read by the CFL limit
+     * of the next one. Bit 0: the fallback factor / 3 (first-order states
+     * from the positivity check, or from the first Rankine-Hugoniot check
+     * with fallback_lower_cfl); bit 1: 0.25 (second check). */
+    unsigned char* cflc;
 } orc_hydro_params;
+
+#define ORC_CFLC 4096
+/* CFL limit scale of a cell code (a ratio to p->cfl, at most 1) */
+double orc_cfl_scale(const orc_hydro_params* p, int code);
 
 void orc_hydro_default_params(orc_hydro_params* p, int mhd);
 

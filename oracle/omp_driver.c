@@ -30,6 +30,14 @@ void orc_set_num_threads(int n)
 #endif
 }
 
+/* params of block b: the per-cell CFL codes point at the block's own */
+static orc_hydro_params at_block(const orc_hydro_params* p, int b)
+{
+    orc_hydro_params q = *p;
+    if (p->cflc) q.cflc = p->cflc + (int64_t)b * ORC_CFLC;
+    return q;
+}
+
 /* One unsplit step over nblocks consecutive blocks (block-major storage as
  * in hydro_oracle.h). Returns the total fallback-cell count. */
 long orc_unsplit_blocks(const orc_hydro_params* p, int nblocks, double* u, double* bx, double* by,
@@ -44,7 +52,8 @@ long orc_unsplit_blocks(const orc_hydro_params* p, int nblocks, double* u, doubl
         double* fx = p->mhd ? bx + (int64_t)b * fsz : NULL;
         double* fy = p->mhd ? by + (int64_t)b * fsz : NULL;
         double* fz = p->mhd ? bz + (int64_t)b * fsz : NULL;
-        total += orc_unsplit_block(p, ub, fx, fy, fz, dt, dx, dy, dz);
+        orc_hydro_params pb = at_block(p, b);
+        total += orc_unsplit_block(&pb, ub, fx, fy, fz, dt, dx, dy, dz);
     }
     return total;
 }
@@ -57,7 +66,8 @@ double orc_dt_limit_blocks(const orc_hydro_params* p, int nblocks, const double*
     double best = 1e300;
 #pragma omp parallel for reduction(min : best)
     for (int b = 0; b < nblocks; ++b) {
-        double v = orc_block_dt_limit(p, u + (int64_t)b * ORV_NVAR * n3, dx, dy, dz);
+        orc_hydro_params pb = at_block(p, b);
+        double v = orc_block_dt_limit(&pb, u + (int64_t)b * ORV_NVAR * n3, dx, dy, dz);
         if (v < best) best = v;
     }
     return best;
@@ -108,7 +118,8 @@ double orc_dt_limit_list(const orc_hydro_params* p, int nlist, const int* list, 
     for (int q = 0; q < nlist; ++q) {
         const int b = list[q];
         const double dx = ldexp(root_dx, -level[b]);
-        double v = orc_block_dt_limit(p, u + (int64_t)b * ORV_NVAR * n3, dx, dx, dx);
+        orc_hydro_params pb = at_block(p, b);
+        double v = orc_block_dt_limit(&pb, u + (int64_t)b * ORV_NVAR * n3, dx, dx, dx);
         if (v < best) best = v;
     }
     return best;
@@ -128,7 +139,8 @@ long orc_unsplit_list(const orc_hydro_params* p, int nlist, const int* list, con
         double* fx = p->mhd ? bx + (int64_t)b * fsz : NULL;
         double* fy = p->mhd ? by + (int64_t)b * fsz : NULL;
         double* fz = p->mhd ? bz + (int64_t)b * fsz : NULL;
-        total += orc_unsplit_block(p, ub, fx, fy, fz, dt, dx, dx, dx);
+        orc_hydro_params pb = at_block(p, b);
+        total += orc_unsplit_block(&pb, ub, fx, fy, fz, dt, dx, dx, dx);
     }
     return total;
 }
@@ -158,8 +170,9 @@ long orc_unsplit_tree(const orc_hydro_params* p, int nlist, const int* list, con
             double* fx = p->mhd ? bx + (int64_t)b * fsz : NULL;
             double* fy = p->mhd ? by + (int64_t)b * fsz : NULL;
             double* fz = p->mhd ? bz + (int64_t)b * fsz : NULL;
+            orc_hydro_params pb = at_block(p, b);
             if (!reg) {
-                total += orc_unsplit_block(p, ub, fx, fy, fz, dt, dx, dx, dx);
+                total += orc_unsplit_block(&pb, ub, fx, fy, fz, dt, dx, dx, dx);
                 continue;
             }
             orc_fluxfix ff;
@@ -184,7 +197,7 @@ long orc_unsplit_tree(const orc_hydro_params* p, int nlist, const int* list, con
                     ff.fine[f][qq] = m >= 0 && m < nnodes ? reg + ((size_t)m * 6 + (f ^ 1)) * per_face : NULL;
                 }
             }
-            total += orc_unsplit_block_fc(p, ub, fx, fy, fz, dt, dx, dx, dx, &ff);
+            total += orc_unsplit_block_fc(&pb, ub, fx, fy, fz, dt, dx, dx, dx, &ff);
         }
     }
     free(reg);

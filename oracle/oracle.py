@@ -52,8 +52,17 @@ class HydroParams(C.Structure):
     _fields_ = [
         ("gamma", C.c_double), ("cvisc", C.c_double), ("use_avisc", C.c_int),
         ("eint_switch", C.c_double), ("smlrho", C.c_double), ("smallp", C.c_double),
-        ("mhd", C.c_int), ("nxb", C.c_int), ("nguard", C.c_int),
+        ("mhd", C.c_int), ("nxb", C.c_int), ("nguard", C.c_int), ("energy_fix", C.c_int), ("cfl_sum", C.c_int),
+        ("hybrid_order", C.c_int), ("fallback_lower_cfl", C.c_int), ("hybrid_kappa", C.c_double),
+        ("cfl_fallback_factor", C.c_double), ("cfl", C.c_double), ("cflc", C.c_void_p),
     ]
+
+    def keep_cfl_codes(self, nblocks: int):
+        """Per-cell CFL codes for nblocks store blocks (the array stays
+        alive with the params object)."""
+        self._cflc = np.zeros((nblocks, 4096), np.uint8)
+        self.cflc = self._cflc.ctypes.data_as(C.c_void_p)
+        return self._cflc
 
 
 _lib = None

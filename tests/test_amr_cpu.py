@@ -112,11 +112,12 @@ def test_flux_correction_conserves_across_levels(oracle, mhd):
     mass, momentum and energy are conserved to round-off (with MHD as well:
     the guard faces on a level boundary come from the copy owned by the
     reader's own level, so same-level neighbours compute the same fluxes);
-    without it they drift."""
+    without it they drift. energyFix off: the strictly conservative form of
+    the energy update."""
     from torch_gb300 import amr
     t, c = amr.small_tree()
     st = amr.amr_box(t, c, seed=5, mach=1.0, device="cpu")
-    p = oracle.hydro_params(mhd)
+    p = oracle.hydro_params(mhd, energy_fix=0)
     tl = oracle.TreeLists(t)
     res = {}
     for fc in (True, False):

@@ -37,7 +37,7 @@ def test_cool_cells_match_oracle(gb, oracle, dt):
     e_o, T_o, td_o, flags = _run_oracle(oracle, rho, ei, T, tdust, dt)
     dev = lambda a: torch.as_tensor(a.copy(), device="cuda")
     d_rho, d_ei, d_T, d_td = dev(rho), dev(ei), dev(T), dev(tdust)
-    st = torch.zeros(16, dtype=torch.float64, device="cuda")
+    st = gb.status_buffer()
     gb.cool_cells(d_rho, d_ei, d_T, d_td, dt, status=st)
     torch.cuda.synchronize()
     T_g, td_g = d_T.cpu().numpy(), d_td.cpu().numpy()

@@ -251,7 +251,28 @@ extern "C" int gb_register_grid(const gb_grid_desc* grid, const gb_tree_desc* tr
         g_gb.grid.level = tree->level;
         g_gb.tree_ok = true;
     }
+    // per-cell CFL codes start at zero (no cell lowered) for a new grid
+    const size_t cb = (size_t)grid->maxblocks * 3 * GB_NXB * GB_NXB * GB_NXB;
+    if (cb > g_gb.cflc_bytes) {
+        if (g_gb.d_cflc) cudaFree(g_gb.d_cflc);
+        g_gb.d_cflc = nullptr;
+        g_gb.cflc_bytes = 0;
+        if (gb_check(cudaMalloc(&g_gb.d_cflc, cb), "cudaMalloc(cfl codes)")) return GB_ERR_CUDA;
+        g_gb.cflc_bytes = cb;
+    }
+    if (gb_check(cudaMemset(g_gb.d_cflc, 0, cb), "cudaMemset(cfl codes)")) return GB_ERR_CUDA;
     return GB_OK;
+}
+
+extern "C" int gb_cfl_codes_reset(void* stream)
+{
+    if (!g_gb.grid_ok) {
+        gb_set_error("gb_cfl_codes_reset: call gb_register_grid first");
+        return GB_ERR_NOT_INIT;
+    }
+    return gb_check(cudaMemsetAsync(g_gb.d_cflc, 0, g_gb.cflc_bytes, (cudaStream_t)stream), "cfl codes reset")
+               ? GB_ERR_CUDA
+               : GB_OK;
 }
 
 extern "C" int gb_hydro_init(const gb_hydro_params* p)
@@ -1406,7 +1427,7 @@ extern "C" int gb_set_chunk_blocks(int n)
     return GB_OK;
 }
 
-static gbh::hydro_kparams make_kp(double dt, const double* dtp = nullptr)
+gbh::hydro_kparams gb_make_kp(double dt, const double* dtp)
 {
     gbh::hydro_kparams kp;
     kp.dtp = dtp;
@@ -1423,6 +1444,18 @@ static gbh::hydro_kparams make_kp(double dt, const double* dtp = nullptr)
     kp.smlrho = g_gb.hp.smlrho;
     kp.smallp = g_gb.hp.smallp;
     kp.use_avisc = g_gb.hp.use_avisc;
+    kp.energy_fix = g_gb.hp.mhd && g_gb.hp.energy_fix;
+    kp.hybrid = g_gb.hp.hybrid_order;
+    kp.lower_cfl = g_gb.hp.fallback_lower_cfl;
+    kp.kappa = g_gb.hp.hybrid_kappa;
+    kp.cflc = g_gb.d_cflc;
+    kp.cfl_sum = g_gb.hp.cfl_sum;
+    {
+        // a code's scale: the lowered CFL over cfl, at most 1
+        const double s1 = fmin(1.0, (g_gb.hp.cfl_fallback_factor / 3.0) / g_gb.hp.cfl);
+        const double s2 = fmin(1.0, 0.25 / g_gb.hp.cfl);
+        kp.cflsc = {{1.0, s1, s2, fmin(s1, s2)}};
+    }
     kp.dt = dt;
     if (g_gb.tree_ok) {
         kp.dx[0] = g_gb.tree.root_dx[0];
@@ -1460,7 +1493,7 @@ int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int
         rc = gb_streams_prepare(nchunks);
         if (rc) return rc;
     }
-    gbh::hydro_kparams kp = make_kp(dt, dtp);
+    gbh::hydro_kparams kp = gb_make_kp(dt, dtp);
     bool fc = false;
     rc = fc_prepare(nblk, s, &fc);
     if (rc) return rc;
@@ -1567,7 +1600,7 @@ extern "C" int gb_set_dt_limits(double dtmin, double dtmax, double change_factor
 static int launch_dt(int nblk, const int* list, double* dt_out, gb_driver_state* drv, cudaStream_t s)
 {
     k_dt_init<<<1, 1, 0, s>>>((unsigned long long*)g_gb.d_dtmin);
-    gbh::hydro_kparams kp = make_kp(1.0);
+    gbh::hydro_kparams kp = gb_make_kp(1.0, nullptr);
     gb_prof_begin(GBP_DT, s);
     int rc = gb_dt_launch(kp, g_gb.hp.mhd, nblk, list, (unsigned long long*)g_gb.d_dtmin, s);
     if (rc) return rc;

@@ -82,7 +82,7 @@ int read_table(const char* path, std::vector<int>& logT, std::vector<int>& logn,
     return GB_OK;
 }
 
-__device__ __forceinline__ bool finite_pos(double x) { return isfinite(x) && x > 0.0; }
+__device__ __forceinline__ bool finite_pos(double x) { return gb_finite_pos(x); }
 
 // RadHeat.F90:223-423 for one cell of a registered grid.
 __global__ void k_heat_blocks(gb_dev_grid g, gb_cool_ctx c, const int* __restrict__ list,
@@ -603,6 +603,10 @@ __device__ void sur_fallback_cell(const gb_dev_grid& g, const gb_cool_ctx& c, do
     double ei, temp;
     sur_load(g, c, gamma, blk, ci, v, ei, temp);
     gb_cool_diag d = {0, 0, 0, 0, 0};
+    if (!(finite_pos(v.rho) && finite_pos(ei) && finite_pos(temp))) {
+        gb_fail(st, GB_ST_NONFINITE, blk, i, j, k, temp);
+        return;
+    }
     heating_and_cooling(c, v, &ei, dt_code * c.p.time_unit, &temp, &d);
     bool clamped = false;
     if (temp > c.p.absTmax) {
@@ -614,6 +618,7 @@ __device__ void sur_fallback_cell(const gb_dev_grid& g, const gb_cool_ctx& c, do
     if (st) {
         gb_count_warp(&st->n_bracket_fail, d.bracket_fail != 0);
         gb_count_warp(&st->n_clamped, clamped);
+        if (clamped) gb_fail(st, GB_ST_OVERHEAT, blk, i, j, k, temp);
         if (d.unbracketed) gb_fail(st, GB_ST_ZERO_UNBRACKETED, blk, i, j, k, ei);
         if (d.maxiter) gb_fail(st, GB_ST_ZERO_MAXITER, blk, i, j, k, ei);
     }

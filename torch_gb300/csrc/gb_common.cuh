@@ -131,11 +131,15 @@ constexpr int GB_STEP_GUARD_FACES = (GB_BAND + 1) * GB_BAND * GB_BAND - (GB_NXB 
 constexpr int GP_REFINED = 1;   // a node of the leaf's level with children
 constexpr int GP_LEAFKIDS = 2;  // ... whose children are all leaves
 
-// Record the first failure in the status word and count it.
+// finite and positive (the cooling solve's input guard)
+__device__ __forceinline__ bool gb_finite_pos(double x) { return isfinite(x) && x > 0.0; }
+
+// Record the first failure in the status word and count it under its code.
 __device__ __forceinline__ void gb_fail(gb_status* st, int code, int blk, int i, int j, int k,
                                         double v)
 {
     if (!st) return;
+    atomicAdd(&st->n_code[code & 7], 1ull);
     if (atomicCAS(&st->code, 0, code) == 0) {
         st->block = blk;
         st->i = i;

@@ -42,6 +42,10 @@ struct gb_state_t {
     void* d_plan = nullptr;
     int plan_n = 0;
     bool plan_ok = false;
+    // per-cell CFL codes of the interior cells (store block x 3 directions x
+    // 4096 bytes): written by the reconstruction, read by the next CFL limit
+    unsigned char* d_cflc = nullptr;
+    size_t cflc_bytes = 0;
     // bumped by every call that changes what a captured step graph baked
     // in (grid, tree, parameters, tables, weights, modes)
     unsigned long long gen = 0;

@@ -47,8 +47,11 @@ struct scratch_layout {
     // FP32 primitives of the padded block (mixed path only)
     // (+ the three face-B arrays, FP32, after the cell variables)
     static constexpr size_t prim32 = std::is_same<T, float>::value ? (size_t)NP32 * GB_N3 + 3 * GB_FSZ : 0;  // float
+    // hybrid order: the minimum undivided velocity divergence over each
+    // band cell's box (T)
+    static constexpr size_t divu = (size_t)NRC;
     static constexpr size_t bytes =
-        recon * sizeof(T) + flux * sizeof(T) + (emf + fb) * sizeof(double) + prim32 * sizeof(float);
+        recon * sizeof(T) + flux * sizeof(T) + (emf + fb) * sizeof(double) + prim32 * sizeof(float) + divu * sizeof(T);
 };
 // the FP32 copy of each block starts on a 16-byte boundary (k_prim32 stores
 // four cells at a time): every section before it and its own stride are
@@ -377,6 +380,12 @@ __device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* 
     wn[5] = qs[2][5];
 }
 
+// CFL limit scale of a cell's code (bit 0: the fallback factor / 3, bit 1:
+// 0.25; a ratio to cfl, at most 1)
+struct cfl_scale {
+    double s[4];
+};
+
 struct hydro_kparams {
     double gamma, cvisc, eint_switch, smlrho, smallp;
     int use_avisc;
@@ -406,6 +415,19 @@ struct hydro_kparams {
     // cubic cells (dx = dy = dz at every level): the mixed update sums the
     // three directions' flux differences before one FP64 scaling
     int iso = 0;
+    int energy_fix = 0;  // energyFix: gas energy from the flux-updated cell field
+    // hybrid order (use_hybridOrder): first-order states where the flow
+    // compresses and a state fails the Rankine-Hugoniot check; the minimum
+    // divergence per band cell comes from k_divu. lower_cfl: the first
+    // check's fallback lowers the cell's CFL (hy_fallbackLowerCFL)
+    int hybrid = 0, lower_cfl = 0;
+    double kappa = 0.0;
+    const void* divu = nullptr;
+    // per-cell CFL codes of the interior cells (store block x 3 directions
+    // x 4096 bytes; null: not kept), read by the next CFL limit
+    unsigned char* cflc = nullptr;
+    int cfl_sum = 0;
+    cfl_scale cflsc = {{1.0, 1.0, 1.0, 1.0}};
     const int4* ec_plan = nullptr;
     const int* ec_near = nullptr;  // per node: bit 0 a coarser leaf around it, bit 1 a finer one
     const int* ec_child = nullptr;
@@ -467,6 +489,66 @@ __device__ __forceinline__ void load_prim(const gb_dev_grid& g, int blk, int ci,
     } else {
         load_w<T, MHD>(g, blk, ci, w);
     }
+}
+
+// ---------------------------------------------------------------- k_divu
+// Hybrid order's compression measure (hy_uhd_dataReconstOneStep.F90:934-948,
+// 1150-1164): the undivided velocity divergence (Balsara & Spicer 1999)
+// sum_d (v_d(c + e_d) - v_d(c - e_d)) / 2 of every band cell, then per band
+// cell its minimum over the +-k4 box (k4 = 1 MHD, 2 hydro) clipped to the
+// band, whose cells all have filled neighbours. One CTA per block; the
+// divergences stay in shared memory.
+constexpr int DIVU_THREADS = 256;
+template <typename T, bool MHD>
+__global__ void __launch_bounds__(DIVU_THREADS)
+k_divu(gb_dev_grid g, const int* __restrict__ list, const float* __restrict__ p32, size_t p32_stride,
+       T* __restrict__ out, size_t out_stride)
+{
+    __shared__ T s_div[NRC];
+    const int cb = blockIdx.y;
+    const int blk = list[cb];
+    const float* p32b = p32 + (size_t)cb * p32_stride;
+    auto vel = [&](int d, int ci) -> T {
+        if constexpr (std::is_same<T, float>::value) return p32b[(size_t)(1 + d) * GB_N3 + ci];
+        else return g.unk[((int64_t)blk * g.nvar + g.slot[GB_VELX + d]) * GB_N3 + ci];
+    };
+    for (int c = threadIdx.x; c < NRC; c += DIVU_THREADS) {
+        const int i = RLO + c % RB, j = RLO + (c / RB) % RB, k = RLO + c / (RB * RB);
+        const int ci = gb_cidx(i, j, k);
+        s_div[c] = (T)0.5 * (vel(0, ci + 1) - vel(0, ci - 1)) + (T)0.5 * (vel(1, ci + GB_N) - vel(1, ci - GB_N)) +
+                   (T)0.5 * (vel(2, ci + GB_N * GB_N) - vel(2, ci - GB_N * GB_N));
+    }
+    __syncthreads();
+    constexpr int K4 = MHD ? 1 : 2;
+    T* o = out + (size_t)cb * out_stride;
+    for (int c = threadIdx.x; c < NRC; c += DIVU_THREADS) {
+        const int i = c % RB, j = (c / RB) % RB, k = c / (RB * RB);
+        T m = (T)1e30;
+        for (int kk = k - K4; kk <= k + K4; ++kk) {
+            if (kk < 0 || kk >= RB) continue;
+            for (int jj = j - K4; jj <= j + K4; ++jj) {
+                if (jj < 0 || jj >= RB) continue;
+                for (int ii = i - K4; ii <= i + K4; ++ii) {
+                    if (ii < 0 || ii >= RB) continue;
+                    const T x = s_div[ii + RB * (jj + RB * kk)];
+                    if (x < m) m = x;
+                }
+            }
+        }
+        o[c] = m;
+    }
+}
+
+// hy_uhd_checkRHjumpCond for one face state, written from the
+// Rankine-Hugoniot relations: no single shock compresses an ideal gas by
+// more than (gamma + 1) / (gamma - 1) (the strong-shock limit, Toro 1997
+// eq. 3.58), so a face state whose density differs from its cell's by more
+// is not shock-connected to it
+template <typename T>
+__device__ __forceinline__ bool rh_fail(T gam, T rho_c, T rho_f)
+{
+    const T lim = (gam + (T)1) / (gam - (T)1);
+    return rho_f > lim * rho_c || rho_c > lim * rho_f;
 }
 
 // ---------------------------------------------------------------- k_recon
@@ -672,16 +754,51 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
     int off[NP];
     rot_offsets<T, MHD>(g, d, off);
     recon_normal<T, MHD, TILE>(g, gam, dtd, hd, d, blk, i, j, k, lane, p32b, off, s_sig, s_abn, s_dnb, wp, wn, wc);
+    // hybrid order before the transverse corrections
+    // (hy_uhd_dataReconstOneStep.F90:934-999): where the flow compresses, a
+    // direction whose states fail the Rankine-Hugoniot check falls back to
+    // the cell's state (the transverse terms already computed stay)
+    bool comp = false, rh = false;
+    unsigned code = 0;
+    if (kp.hybrid) {
+        // (gamma p + B.B) / rho, B.B summed in x, y, z order
+        const T b0 = wc[5] * wc[5], b1 = wc[6] * wc[6], b2 = wc[7] * wc[7];
+        T cs = gam * wc[4] + ((pick3(d, b0, b2, b1) + pick3(d, b1, b0, b2)) + pick3(d, b2, b1, b0));
+        cs = sqrt(cs / wc[0]);
+        comp = ((const T*)kp.divu)[(size_t)cb * NRC + cc] < (T)kp.kappa * cs;
+        if (comp && (rh_fail(gam, wc[0], wp[0]) || rh_fail(gam, wc[0], wn[0]))) {
+#pragma unroll
+            for (int v = 0; v < NP; ++v) { wn[v] = wc[v]; wp[v] = wc[v]; }
+            if (kp.lower_cfl) code |= 1u;
+            rh = true;
+        }
+    }
     __syncthreads();
     recon_transverse<T, MHD, TILE>(hd, d, lane, s_sig, s_abn, s_dnb, wp, wn);
-    // positivity fallback (density and pressure keep their slots in every frame)
+    // hybrid order after them (:1150-1218): a fallback in any direction
+    // lowers the cell's CFL to 0.25 (3-D)
+    if (comp && (rh_fail(gam, wc[0], wp[0]) || rh_fail(gam, wc[0], wn[0]))) {
+#pragma unroll
+        for (int v = 0; v < NP; ++v) { wn[v] = wc[v]; wp[v] = wc[v]; }
+        code |= 2u;
+        rh = true;
+    }
+    // positivity fallback (density and pressure keep their slots in every
+    // frame), lowering the cell's CFL (:1230-1272)
     bool fell = (wn[0] < (T)0 || wp[0] < (T)0 || wn[4] < (T)0 || wp[4] < (T)0);
     if (fell) {
 #pragma unroll
         for (int v = 0; v < NP; ++v) { wn[v] = wc[v]; wp[v] = wc[v]; }
+        code |= 1u;
     }
     if (!active) return;
-    if (st) gb_count_warp(&st->n_fallback, fell);
+    if (st) {
+        gb_count_warp(&st->n_fallback, fell);
+        if (kp.hybrid) gb_count_warp(&st->n_rh_fallback, rh);
+    }
+    if (kp.cflc && i >= LO && i <= HI && j >= LO && j <= HI && k >= LO && k <= HI)
+        kp.cflc[((size_t)blk * 3 + d) * (GB_NXB * GB_NXB * GB_NXB) + (i - LO) + GB_NXB * ((j - LO) + GB_NXB * (k - LO))] =
+            (unsigned char)code;
     T* out = scr + (size_t)cb * scr_stride;
     const int us[NP] = {0, rot_slot_rt<1>(d), rot_slot_rt<2>(d), rot_slot_rt<3>(d), 4,
                         rot_slot_rt<5>(d), rot_slot_rt<6>(d), rot_slot_rt<7>(d)};
@@ -1452,6 +1569,34 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
     auto over_rn = [&](double x) { return RCP ? x * irn : x / rn; };
     double ek = over_rn(0.5 * (Un[1] * Un[1] + Un[2] * Un[2] + Un[3] * Un[3]));
     double em = 0.5 * (Bn[0] * Bn[0] + Bn[1] * Bn[1] + Bn[2] * Bn[2]);
+    if (MHD && kp.energy_fix) {
+        // energyFix (Balsara & Spicer 1999): the gas energy is the updated
+        // total energy less the magnetic energy of the cell field advanced by
+        // the same fluxes (component c by the two directions across it; the
+        // normal direction's flux of B_c is zero); the stored field and the
+        // total energy built from it next step use the staggered faces' mean
+        double Bf[3];
+        if constexpr (std::is_same<T, float>::value) {
+            // the field's change in FP32 (its relative error reaches em only
+            // through the change), the field itself in FP64
+            float dtf[3];
+            kp_dtdxf(kp, gb_block_level(g, blk), dtf);
+            auto Fq = [&](int d, int var, int idx) -> float {
+                return (float)fs[(size_t)d * NFLX * NFC + (size_t)var * NFC + idx];
+            };
+            const float d0 = -(dtf[1] * (Fq(1, 5, fp[1]) - Fq(1, 5, fm[1]))) - dtf[2] * (Fq(2, 5, fp[2]) - Fq(2, 5, fm[2]));
+            const float d1 = -(dtf[0] * (Fq(0, 6, fp[0]) - Fq(0, 6, fm[0]))) - dtf[2] * (Fq(2, 6, fp[2]) - Fq(2, 6, fm[2]));
+            const float d2 = -(dtf[0] * (Fq(0, 7, fp[0]) - Fq(0, 7, fm[0]))) - dtf[1] * (Fq(1, 7, fp[1]) - Fq(1, 7, fm[1]));
+            Bf[0] = Uc[5] + gb_f2d(d0);
+            Bf[1] = Uc[6] + gb_f2d(d1);
+            Bf[2] = Uc[7] + gb_f2d(d2);
+        } else {
+            Bf[0] = (Uc[5] - dtd[1] * (F(1, 5, fp[1]) - F(1, 5, fm[1]))) - dtd[2] * (F(2, 5, fp[2]) - F(2, 5, fm[2]));
+            Bf[1] = (Uc[6] - dtd[0] * (F(0, 6, fp[0]) - F(0, 6, fm[0]))) - dtd[2] * (F(2, 6, fp[2]) - F(2, 6, fm[2]));
+            Bf[2] = (Uc[7] - dtd[0] * (F(0, 7, fp[0]) - F(0, 7, fm[0]))) - dtd[1] * (F(1, 7, fp[1]) - F(1, 7, fm[1]));
+        }
+        em = 0.5 * (Bf[0] * Bf[0] + Bf[1] * Bf[1] + Bf[2] * Bf[2]);
+    }
     const double xE = (Un[4] - ek) - em;  // rho e from the total energy
     double eiE = over_rn(xE);
     double eia = over_rn(ren);
@@ -1485,23 +1630,31 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
         v.mu_mol = p.mu_mol;
         v.strat_factor = 1.0;
         gb_cool_diag dg = {0, 0, 0, 0, 0};
-        gbcool::heating_and_cooling(cool, v, &eic, kp_dt(kp) * p.time_unit, &temp, &dg);
+        // the input guard of gb_heat: a non-finite or non-positive state is
+        // reported and keeps its hydro values (the root finder would spend
+        // its whole iteration budget on it)
+        const bool good = gb_finite_pos(v.rho) && gb_finite_pos(eic) && gb_finite_pos(temp);
         bool clamped = false;
-        if (temp > p.absTmax) {
-            eic = p.absTmax * v.TtoEI;
-            temp = p.absTmax;
-            clamped = true;
+        if (good) {
+            gbcool::heating_and_cooling(cool, v, &eic, kp_dt(kp) * p.time_unit, &temp, &dg);
+            if (temp > p.absTmax) {
+                eic = p.absTmax * v.TtoEI;
+                temp = p.absTmax;
+                clamped = true;
+            }
+            if (eic < p.smallp / v.rho) eic = p.smallp / v.rho;
+            ei = eic / (p.vel_unit * p.vel_unit);
+            pn = gm1 * rn * ei;
+            UV(GB_TEMP) = temp;
+            UV(GB_TDUS) = v.tdust;
+            if (g.slot[GB_PHHE] >= 0) UV(GB_PHHE) = 0.0;
+            if (g.slot[GB_PEFL] >= 0) UV(GB_PEFL) = 0.0;
         }
-        if (eic < p.smallp / v.rho) eic = p.smallp / v.rho;
-        ei = eic / (p.vel_unit * p.vel_unit);
-        pn = gm1 * rn * ei;
-        UV(GB_TEMP) = temp;
-        UV(GB_TDUS) = v.tdust;
-        if (g.slot[GB_PHHE] >= 0) UV(GB_PHHE) = 0.0;
-        if (g.slot[GB_PEFL] >= 0) UV(GB_PEFL) = 0.0;
         if (st) {
+            if (!good) gb_fail(st, GB_ST_NONFINITE, blk, i, j, k, temp);
             gb_count_warp(&st->n_bracket_fail, dg.bracket_fail != 0);
             gb_count_warp(&st->n_clamped, clamped);
+            if (clamped) gb_fail(st, GB_ST_OVERHEAT, blk, i, j, k, temp);
             if (dg.unbracketed) gb_fail(st, GB_ST_ZERO_UNBRACKETED, blk, i, j, k, eic);
             if (dg.maxiter) gb_fail(st, GB_ST_ZERO_MAXITER, blk, i, j, k, eic);
         }
@@ -1538,10 +1691,16 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
 // ---------------------------------------------------------------- CFL
 // R = double: the oracle's arithmetic; R = float (mixed path): the same
 // limit from FP32 arithmetic on the FP64 state (dt to ~1e-7 relative)
+// Per cell the limit is min_d dx_d / (|v_d| + c_f,d), or with cfl_sum
+// 1 / sum_d (|v_d| + c_f,d) / dx_d; a cell whose reconstruction fell back
+// last step (its CFL code, the OR over the three directions) has it scaled
+// by sc[code] (the lowered CFL over cfl).
+
 template <typename R>
 static __global__ void __launch_bounds__(256)
 k_dtlimit(gb_dev_grid g, double gamma, int mhd, double dx0, double dx1, double dx2,
-          const int* __restrict__ list, unsigned long long* __restrict__ out_bits)
+          const int* __restrict__ list, unsigned long long* __restrict__ out_bits, int cfl_sum,
+          const unsigned char* __restrict__ cflc, cfl_scale sc)
 {
     const int blk = list[blockIdx.y];
     const double root[3] = {dx0, dx1, dx2};
@@ -1568,13 +1727,25 @@ k_dtlimit(gb_dev_grid g, double gamma, int mhd, double dx0, double dx1, double d
         R gp = (R)gamma * p;
         R B2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
         R tt = (gp + B2) / rho;
+        R rate = (R)0, cell = (R)1e30;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             R v = fabs(ld(GB_VELX + d));
             R cf = sqrt((R)0.5 * (tt + sqrt(fmax(tt * tt - (R)4 * gp * B[d] * B[d] / (rho * rho), (R)0))));
-            R dtc = del[d] / (v + cf);
-            best = fmin(best, dtc);
+            if (cfl_sum) {
+                rate = rate + (v + cf) / del[d];
+            } else {
+                R dtc = del[d] / (v + cf);
+                cell = fmin(cell, dtc);
+            }
         }
+        if (cfl_sum) cell = (R)1 / rate;
+        if (cflc) {
+            const unsigned char* cc = cflc + (size_t)blk * 3 * (GB_NXB * GB_NXB * GB_NXB) + t;
+            const int code = cc[0] | cc[GB_NXB * GB_NXB * GB_NXB] | cc[2 * GB_NXB * GB_NXB * GB_NXB];
+            if (code) cell = cell * (R)(code == 1 ? sc.s[1] : (code == 2 ? sc.s[2] : sc.s[3]));
+        }
+        best = fmin(best, cell);
     }
     // warp shuffle then block reduction of the minimum
 #pragma unroll

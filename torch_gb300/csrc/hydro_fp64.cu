@@ -20,6 +20,7 @@ int gb_dt_launch(const gbh::hydro_kparams& kp, int mhd, int nblk, const int* lis
     dim3 g(4, nblk);
     if (g_gb.hp.precision == 1)
         return gb_dt_launch_f32(kp, mhd, nblk, list, bits, s);
-    gbh::k_dtlimit<double><<<g, 256, 0, s>>>(g_gb.grid, kp.gamma, mhd, kp.dx[0], kp.dx[1], kp.dx[2], list, bits);
+    gbh::k_dtlimit<double><<<g, 256, 0, s>>>(g_gb.grid, kp.gamma, mhd, kp.dx[0], kp.dx[1], kp.dx[2], list, bits,
+                                            kp.cfl_sum, kp.cflc, kp.cflsc);
     return gb_check(cudaGetLastError(), "k_dtlimit") ? GB_ERR_CUDA : GB_OK;
 }

@@ -43,24 +43,34 @@ void put_fluxes(const hydro_kparams& kp, int nblk, const int* list, T* fscr, cud
 }
 
 template <typename T>
-int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
+int launch_chunk(const hydro_kparams& kp_in, int mhd, int cool, int nblk, const int* list,
                  void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put = nullptr,
                  const sur_feat_out* sf = nullptr, cudaEvent_t ev_wait = nullptr)
 {
     using SL = scratch_layout<T>;
-    // scratch of the chunk: [recon | flux | emf | faceb], each block-major
+    // scratch of the chunk: [recon | flux | emf | faceb | prim32 | divu],
+    // each block-major
     char* base = (char*)scratch;
     T* rscr = (T*)base;
     T* fscr = (T*)(base + (size_t)nblk * SL::recon * sizeof(T));
     double* escr = (double*)(base + (size_t)nblk * (SL::recon + SL::flux) * sizeof(T));
     double* bscr = escr + (size_t)nblk * SL::emf;
     float* p32 = (float*)(bscr + (size_t)nblk * SL::fb);
+    T* dscr = (T*)(p32 + (size_t)nblk * SL::prim32);
+    hydro_kparams kp = kp_in;
+    kp.divu = dscr;
     const gb_dev_grid& g = g_gb.grid;
     if constexpr (SL::prim32 > 0) {
         dim3 pg((GB_STEP_CELLS / 4 + (mhd ? GB_STEP_FACES_ALL : 0) + 127) / 128, nblk);
         gb_prof_begin(GBP_RECON, s);
         if (mhd) k_prim32<true><<<pg, 128, 0, s>>>(g, list, p32, SL::prim32);
         else k_prim32<false><<<pg, 128, 0, s>>>(g, list, p32, SL::prim32);
+        gb_prof_end(GBP_RECON, s);
+    }
+    if (kp.hybrid) {
+        gb_prof_begin(GBP_RECON, s);
+        if (mhd) k_divu<T, true><<<dim3(1, nblk), DIVU_THREADS, 0, s>>>(g, list, p32, SL::prim32, dscr, SL::divu);
+        else k_divu<T, false><<<dim3(1, nblk), DIVU_THREADS, 0, s>>>(g, list, p32, SL::prim32, dscr, SL::divu);
         gb_prof_end(GBP_RECON, s);
     }
     const int tile = gb_recon_tile();
@@ -131,3 +141,7 @@ int launch_chunk(const hydro_kparams& kp, int mhd, int cool, int nblk, const int
 }
 
 }  // namespace gbh
+
+// kernel parameters of a step with dt (or, with dtp, dt read from the
+// device) from the registered grid and the hydro parameters (capi.cu)
+gbh::hydro_kparams gb_make_kp(double dt, const double* dtp);

@@ -17,6 +17,7 @@ int gb_dt_launch_f32(const gbh::hydro_kparams& kp, int mhd, int nblk, const int*
                      unsigned long long* bits, cudaStream_t s)
 {
     dim3 g(4, nblk);
-    gbh::k_dtlimit<float><<<g, 256, 0, s>>>(g_gb.grid, kp.gamma, mhd, kp.dx[0], kp.dx[1], kp.dx[2], list, bits);
+    gbh::k_dtlimit<float><<<g, 256, 0, s>>>(g_gb.grid, kp.gamma, mhd, kp.dx[0], kp.dx[1], kp.dx[2], list, bits,
+                                            kp.cfl_sum, kp.cflc, kp.cflsc);
     return gb_check(cudaGetLastError(), "k_dtlimit<float>") ? GB_ERR_CUDA : GB_OK;
 }

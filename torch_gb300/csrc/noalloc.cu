@@ -82,25 +82,12 @@ extern "C" int gb_hydro_unsplit_noalloc(int blockCount, const int* blockList_dev
     void* scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);
     if (rc) return rc;
-    gbh::hydro_kparams kp;
-    kp.gamma = g_gb.hp.gamma;
-    kp.cvisc = g_gb.hp.cvisc;
-    kp.eint_switch = g_gb.hp.eint_switch;
-    kp.smlrho = g_gb.hp.smlrho;
-    kp.smallp = g_gb.hp.smallp;
-    kp.use_avisc = g_gb.hp.use_avisc;
-    kp.dt = dt;
-    kp.dtp = nullptr;
-    for (int d = 0; d < 3; ++d) kp.dx[d] = g_gb.tree_ok ? g_gb.tree.root_dx[d] : 1.0;
-    for (int d = 0; d < 3; ++d) kp.dtdx0[d] = dt / kp.dx[d];
-    kp.dtdxp = nullptr;
-    kp.fc_links = nullptr;  // no flux registers without allocation
+    // the allocating entry point's parameters; no flux registers (they
+    // would need allocation)
+    gbh::hydro_kparams kp = gb_make_kp(dt, nullptr);
+    kp.fc_links = nullptr;
     kp.fc_reg = nullptr;
-    kp.gammaf = (float)kp.gamma;
-    kp.inv_gm1 = 1.0 / (kp.gamma - 1.0);
-    kp.cviscf = (float)kp.cvisc;
-    for (int d = 0; d < 3; ++d) kp.dtdxf0[d] = (float)kp.dtdx0[d];
-    kp.dtdxfp = nullptr;
+    kp.ec_reg = nullptr;
     return gbh::launch_chunk<double>(kp, g_gb.hp.mhd, 0, blockCount, blockList_dev, scratch, st_dev,
                                      (cudaStream_t)stream);
 }

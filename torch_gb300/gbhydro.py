@@ -59,7 +59,9 @@ class HydroParams(C.Structure):
     _fields_ = [("gamma", C.c_double), ("cfl", C.c_double), ("cvisc", C.c_double),
                 ("use_avisc", C.c_int), ("mhd", C.c_int), ("eint_switch", C.c_double),
                 ("smlrho", C.c_double), ("smallp", C.c_double), ("precision", C.c_int),
-                ("pad", C.c_int)]
+                ("energy_fix", C.c_int), ("hybrid_order", C.c_int), ("fallback_lower_cfl", C.c_int),
+                ("hybrid_kappa", C.c_double), ("cfl_fallback_factor", C.c_double), ("cfl_sum", C.c_int),
+                ("shock_detect", C.c_int)]
 
 
 class CoolParams(C.Structure):
@@ -90,10 +92,19 @@ class Status(C.Structure):
                 ("n_fallback", C.c_ulonglong), ("n_bracket_fail", C.c_ulonglong),
                 ("n_dust_noconv", C.c_ulonglong), ("n_clamped", C.c_ulonglong),
                 ("n_eint_switch", C.c_ulonglong), ("n_surrogate", C.c_ulonglong),
-                ("n_surrogate_reject", C.c_ulonglong)]
+                ("n_surrogate_reject", C.c_ulonglong), ("n_code", C.c_ulonglong * 8),
+                ("n_rh_fallback", C.c_ulonglong)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("pad", "n_code")}
+        d["n_code"] = {ST_NAMES[c]: int(self.n_code[c]) for c in ST_NAMES if self.n_code[c]}
+        return d
+
+
+def status_buffer(device="cuda"):
+    """Zeroed device memory for one gb_status."""
+    import torch
+    return torch.zeros((C.sizeof(Status) + 7) // 8, dtype=torch.float64, device=device)
 
 
 # every entry point the header declares: name -> (restype, argtypes)
@@ -111,6 +122,7 @@ _SIG = {
     "gb_step_graph_host": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p]),
     "gb_set_dt_limits": (C.c_int, [C.c_double, C.c_double, C.c_double]),
+    "gb_cfl_codes_reset": (C.c_int, [C.c_void_p]),
     "gb_set_flux_correction": (C.c_int, [C.c_int]),
     "gb_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
     "gb_selfcheck_conversions": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -194,10 +206,14 @@ def _stream():
 
 # ------------------------------------------------------------------ parameters
 def hydro_params(mhd: bool, precision: int = 0, **over) -> HydroParams:
-    """Values of flash.par.turbsph_standard (:33, :163-165, :197-198) in
-    code units; floors are code-unit values."""
+    """Values of flash.par.turbsph_standard (:33, :163-165, :197-198,
+    :206-208, :213) in code units; floors are code-unit values. The CFL
+    limit is the summed form (cfl_sum), the one the unsplit step is stable
+    under at cfl 0.8."""
     p = HydroParams(gamma=5.0 / 3.0, cfl=0.8, cvisc=0.1, use_avisc=1, mhd=int(mhd),
-                    eint_switch=1.0e-4, smlrho=1e-30, smallp=1e-30, precision=precision, pad=0)
+                    eint_switch=1.0e-4, smlrho=1e-30, smallp=1e-30, precision=precision,
+                    energy_fix=1, hybrid_order=1, fallback_lower_cfl=1, hybrid_kappa=0.0,
+                    cfl_fallback_factor=0.9, cfl_sum=1, shock_detect=0)
     for k, v in over.items():
         setattr(p, k, v)
     return p
@@ -291,7 +307,7 @@ class Grid:
         self.t_root = t(tree["root"])
         self.tree = tree
         self.root_dx = root_dx
-        self.status = torch.zeros(16, dtype=torch.float64, device=device)  # >= sizeof(gb_status)
+        self.status = status_buffer(device)
         self.leaf = np.nonzero(tree["child"][:, 0] < 0)[0].astype(np.int32)
         self.t_leaf = t(self.leaf)
         self.register()
