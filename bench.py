@@ -95,6 +95,18 @@ def clocks_csv_path(args):
     return path
 
 
+def current_gpu_id() -> str:
+    """nvidia-smi's id of the GPU this process computes on: its PCI bus id
+    (nvidia-smi ignores CUDA_VISIBLE_DEVICES, so an index would name
+    another GPU of the machine), or "0" when torch cannot say."""
+    try:
+        import torch
+        pr = torch.cuda.get_device_properties(torch.cuda.current_device())
+        return f"{pr.pci_domain_id:08x}:{pr.pci_bus_id:02x}:{pr.pci_device_id:02x}.0"
+    except Exception:
+        return "0"
+
+
 class ClockSampler:
     def __init__(self, path):
         self.path = path
@@ -107,7 +119,8 @@ class ClockSampler:
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                          "-lms", "200", "-i", "0"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                          "-lms", "200", "-i", current_gpu_id()], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
         return self
@@ -407,6 +420,56 @@ def l1(a, b, leaves, v):
     return float((x - y).abs().sum() / x.abs().sum())
 
 
+def accuracy_condition(l1_fast, l1_mixed, l1_fast_exact, roundoff, v_fast, sp_fast, v_mixed, sp_mixed, bound=1e-4):
+    """Which path meets the metric's L1 <= 1e-4 (density and pressure after
+    the run's steps): against the all-FP64 plain path, and for the learned
+    path also against the backward-Euler root trajectory (the plain
+    integrator with Brent's tolerance floor at 1e-3 K)."""
+    ok = lambda d: d is not None and max(d.values()) <= bound
+    paths = {
+        "fast_vs_plain_fp64": {"l1": l1_fast, "meets": ok(l1_fast), "value": v_fast, "speedup_vs_plain_fp64": sp_fast},
+        "fast_vs_backward_euler_root": {"l1": l1_fast_exact, "meets": ok(l1_fast_exact), "value": v_fast,
+                                        "speedup_vs_plain_fp64": sp_fast},
+        "mixed_plain_cooling_vs_plain_fp64": {"l1": l1_mixed, "meets": ok(l1_mixed), "value": v_mixed,
+                                              "speedup_vs_plain_fp64": sp_mixed},
+    }
+    return {"bound": bound, "paths": paths,
+            "plain_fp64_roundoff_drift_max": max(max(v.values()) for v in roundoff.values()) if roundoff else None,
+            "note": "plain_fp64_roundoff_drift_max: L1 between two plain FP64 runs whose initial densities differ "
+                    "by one ulp; a path cannot be held to a bound below its reference's own drift"}
+
+
+def roundoff_divergence(G, tree, st, checkpoints=(10, 20)):
+    """How far two plain FP64 runs drift apart from the same state when one
+    of them starts with every density nudged by one ulp: density and
+    pressure L1 (interior cells of the leaves) at each checkpoint step. The
+    plain path's own sensitivity to round-off, against which a path's L1
+    error after the same steps has to be read."""
+    import torch
+    ga = make_grid(G, tree, st)
+    gbb = make_grid(G, tree, st)
+    d = gbb.u[:, gbb.slots["DENS"]]
+    d.copy_(torch.nextafter(d, torch.full_like(d, float("inf"))))
+    G.init_hydro(G.hydro_params(True, precision=0))
+    lv = torch.as_tensor(tree["leaf"].astype(np.int64), device="cuda")
+    snap = {}
+    for name, g in (("a", ga), ("b", gbb)):
+        g.register()
+        done = 0
+        for n in checkpoints:
+            for _ in range(n - done):
+                g.step_graph(True)
+            done = n
+            snap[name, n] = [g.u[lv, v, 4:20, 4:20, 4:20].clone() for v in (0, 4)]
+    out = {}
+    for n in checkpoints:
+        out[str(n)] = {v: float((snap["a", n][q] - snap["b", n][q]).abs().sum() / snap["a", n][q].abs().sum())
+                       for q, v in enumerate(("dens", "pres"))}
+    del ga, gbb, snap
+    torch.cuda.empty_cache()
+    return out
+
+
 def lite_run(args, G, wl, tree, st, zones, world, rank, t_ic):
     """The full-scale workload: plain FP64 and fast paths only (each grid
     holds ~30 GB), both graph-replayed with tuned launch shapes."""
@@ -559,7 +622,6 @@ def main():
     cs = None
     if rank == 0 and not args.no_cpu_baseline:
         cs = CpuStep(wl, tree, st)
-    del st
     clk = ClockSampler(clocks_csv_path(args))
     if world > 1:
         dist.barrier()
@@ -571,8 +633,13 @@ def main():
                                            tune=not args.no_tune, ncu_range=args.ncu_range)
         # the same path launched eagerly with the in-library profiler on:
         # per-kernel times (the profiler cannot time inside a graph)
-        ms_eager, _, prof = run_path(G, g_eager, 1, args.steps, args.warmup, surrogate=True, profile=True)
+        ms_eager, st_eager, prof = run_path(G, g_eager, 1, args.steps, args.warmup, surrogate=True, profile=True)
         ms_mixed, st_mixed, _ = run_path(G, g_mixed, 1, args.steps, args.warmup)
+    # diagnostic, untimed: the plain path's own drift under a one-ulp
+    # nudge of the initial density (what an L1 error after 10 and 20 steps
+    # can be read against)
+    roundoff = roundoff_divergence(G, tree, st)
+    del st
     # diagnostic, untimed: mixed hydro + the plain integrator with Brent's
     # tolerance floor at 1e-3 K (the backward-Euler trajectory)
     G.set_brent_tolerance(1e-3)
@@ -603,26 +670,61 @@ def main():
     # the oracle's counting build (roofline_constants.json) over the
     # measured FP64 FMA peak of this GPU
     fp64 = None
+    step_roof = None
+    rc = {}
     try:
         with open(os.path.join(ROOT, "roofline_constants.json")) as f:
             rc = json.load(f)
         fpz = rc["mhd_cooling_step"]["flops"]
         peak64 = G.measure_fp64_peak()
+        peak32 = G.measure_fp32_peak()
         ach64 = zones * fpz / (ms_plain * 1e-3) / 1e12
         fp64 = {"path": "plain_fp64", "flops_per_zone": fpz, "achieved_tflops": ach64, "peak_tflops": peak64,
                 "frac": ach64 / peak64, "peak_kind": "measured FP64 FMA loop on this GPU",
                 "note": "flops = + - * / sqrt of the oracle's MHD step + CFL + implicit cooling per zone; "
                         "a division or sqrt issues several FP64 instructions, so the pipe is busier than "
                         "this fraction"}
+        # the fast path: reconstruction, Riemann solve and edge fields in
+        # FP32, the update in FP64 (the learned cooling's FP32 rate
+        # evaluations are not counted); HBM: 216 B per zone-update
+        ph = rc["mhd_hlld_ct_phases"]
+        f32 = ph["recon"]["flops"] + ph["flux"]["flops"] + ph["emf"]["flops"]
+        f64 = ph["update"]["flops"]
+        t_fast = ms_fast * 1e-3
+        step_roof = {
+            "plain_fp64": {"pipe": "fp64", "frac": ach64 / peak64},
+            "fast": {"fp32": {"flops_per_zone": f32, "achieved_tflops": zones * f32 / t_fast / 1e12,
+                              "peak_tflops": peak32, "frac": zones * f32 / t_fast / 1e12 / peak32},
+                     "fp64": {"flops_per_zone": f64, "achieved_tflops": zones * f64 / t_fast / 1e12,
+                              "peak_tflops": peak64, "frac": zones * f64 / t_fast / 1e12 / peak64},
+                     "hbm": {"bytes_per_zone": 216.0, "achieved_gbs": zones * 216.0 / t_fast / 1e9,
+                             "peak_gbs": hbm, "frac": zones * 216.0 / t_fast / 1e9 / hbm}},
+            "peak_kind": "FP32 and FP64: measured FMA loops on this GPU; HBM: " + hbm_kind,
+            "note": "flops per zone from the oracle's counting build split by phase (roofline_constants.json)"}
     except (OSError, KeyError, ValueError, G.GBError):
         pass
     # dominant kernel: largest share of the fast path's timed region.
-    # Algorithmic bytes = 216 B per zone-update (12 FP64 MHD words + 3
-    # cooling words, read once + written once) x the zones a launch covers.
+    # Algorithmic bytes = 216 B per unit (12 FP64 MHD words + 3 cooling
+    # words, read once + written once) x the units a launch covers: zones,
+    # or for the plain-integrator fallback the cells it was handed.
     dom = max(prof, key=lambda k: prof[k][0])
     dom_ms, dom_n = prof[dom][0], prof[dom][1]
-    zones_per_launch = zones * args.steps / dom_n
-    ach = 216.0 * zones_per_launch / (dom_ms / dom_n * 1e-3) / 1e9
+    units_total = zones * args.steps
+    if dom == "sur_fallback":
+        units_total = st_eager["n_surrogate_reject"]
+    zones_per_launch = units_total / dom_n
+    launch_s = dom_ms / dom_n * 1e-3
+    ach = 216.0 * zones_per_launch / launch_s / 1e9
+    compute = None
+    phase = {"recon": "recon", "flux": "flux", "emf": "emf"}.get(dom)
+    if phase and rc.get("mhd_hlld_ct_phases") and step_roof:
+        fz = rc["mhd_hlld_ct_phases"][phase]["flops"]
+        a32 = fz * zones_per_launch / launch_s / 1e12
+        compute = {"pipe": "fp32", "flops_per_zone": fz, "achieved_tflops": a32,
+                   "peak_tflops": step_roof["fast"]["fp32"]["peak_tflops"],
+                   "frac": a32 / step_roof["fast"]["fp32"]["peak_tflops"],
+                   "note": "algorithmic flops of this phase (the oracle's count, which includes products with "
+                           "the eigenvectors' structural zeros that the kernel skips)"}
     launches = int(ginfo["graph_kernels_per_step"]) * args.steps
     if rank != 0:
         return
@@ -648,7 +750,12 @@ def main():
                    "all-FP64; l1_reference_integrator_tolerance: the plain integrator with Brent stopped at 1 K "
                    "(the reference) vs at 1e-3 K, both on mixed hydro; l1_err_vs_backward_euler_root: fast "
                    "path vs the 1e-3 K run",
-        "mixed_plain_cooling": {"value": zones * world / (ms_mixed * 1e-3), "ms_per_step": ms_mixed},
+        "mixed_plain_cooling": {"value": zones * world / (ms_mixed * 1e-3), "ms_per_step": ms_mixed,
+                                "speedup_vs_plain_fp64": ms_plain / ms_mixed},
+        "roundoff_divergence_plain_fp64": roundoff,
+        "accuracy_condition": accuracy_condition(l1_fast, l1_mixed, l1_fast_exact, roundoff,
+                                                 zones * world / (ms_fast * 1e-3), ms_plain / ms_fast,
+                                                 zones * world / (ms_mixed * 1e-3), ms_plain / ms_mixed),
         "fast_eager": {"ms_per_step": ms_eager, "value": zones * world / (ms_eager * 1e-3),
                        "note": "the same fast path launched kernel by kernel with the host reading dt each step"},
         "launch_config": {k: ginfo["tuned"].get(k) for k in ("chunk", "tile", "occ", "streams", "cached")}
@@ -670,7 +777,8 @@ def main():
                      "traffic_source": "ncu DRAM bytes per zone of this kernel on the 128^3 box at 512-block chunks, "
                                        "times the zones of one launch here",
                      "peak_kind": hbm_kind, "launch_ms": dom_ms / dom_n,
-                     "algo_bytes_per_launch": 216.0 * zones_per_launch},
+                     "algo_bytes_per_launch": 216.0 * zones_per_launch, "compute": compute},
+        "step_roofline": step_roof,
         "e2e": {"value": zones / (e2e_ms * 1e-3), "unit": "zone-updates/s", "h2d_bytes_per_step": e2e_bytes,
                 "d2h_bytes_per_step": e2e_bytes, "parts": e2e_parts},
         "fp64_roofline": fp64,

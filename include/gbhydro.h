@@ -169,8 +169,8 @@ int gb_hydro_unsplit(int blockCount, const int* blockList_dev, double dt, double
  * must not call cudaMalloc because it can synchronise the whole device.
  * Runs the same plain FP64 kernels as gb_hydro_unsplit (no fused cooling,
  * whatever gb_hydro_params.precision says) with their scratch in a static
- * device array sized for GB_NOALLOC_MAX_BLOCKS blocks (about 3.6 MB per
- * block, ~14.4 MB held on every GPU that loads the library until exit).
+ * device array sized for GB_NOALLOC_MAX_BLOCKS blocks (about 3.7 MB per
+ * block, ~14.6 MB held on every GPU that loads the library until exit).
  * blockCount above GB_NOALLOC_MAX_BLOCKS returns GB_ERR_LIMIT. The first
  * call on each device looks up the array's device address (make it before
  * any stream capture). Calls share the array: calls that overlap on the GPU
@@ -445,6 +445,8 @@ int gb_prof_read(double* ms, long long* launches, int n);
  * FMA; a few milliseconds of independent FMA chains on every SM): the
  * denominator of the FP64-pipe roofline. */
 int gb_measure_fp64_peak(double* tflops);
+/* The same for FP32 FMA (the denominator of the mixed path's FP32 work). */
+int gb_measure_fp32_peak(double* tflops);
 
 /* Self-check of the mixed path's integer-pipe FP64 <-> FP32 conversions
  * against the hardware conversions: for the n device values, counts into

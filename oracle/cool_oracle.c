@@ -345,6 +345,11 @@ static double dust_cooling(const orc_cool_params* p, double n, double T, double 
     return cool_dg;
 }
 
+double orc_dust_cooling(const orc_cool_params* p, double n, double T, double tdust, double rho)
+{
+    return dust_cooling(p, n, T, tdust, rho);
+}
+
 double orc_dei_dt(const orc_cool_params* p, const orc_table* t, orc_cool_vars* v, double t_in,
                   double ei_in)
 {

@@ -63,6 +63,21 @@ static inline cdouble ldexp(cdouble a, int e) { return cdouble(::ldexp(a.v, e));
 static inline bool isfinite(cdouble a) { return std::isfinite(a.v); }
 static inline bool isnan(cdouble a) { return std::isnan(a.v); }
 
+// per-phase counts of the block step (hydro_oracle.c's ORC_PHASE marks)
+static fc_counts g_mark, g_phase[4];
+static void fc_phase(int k)
+{
+    if (k >= 0 && k < 4) {
+        g_phase[k].add += g_fc.add - g_mark.add;
+        g_phase[k].mul += g_fc.mul - g_mark.mul;
+        g_phase[k].div += g_fc.div - g_mark.div;
+        g_phase[k].sqrt += g_fc.sqrt - g_mark.sqrt;
+        g_phase[k].trans += g_fc.trans - g_mark.trans;
+    }
+    g_mark = g_fc;
+}
+#define ORC_PHASE(k) fc_phase(k)
+
 #define double cdouble
 #include "cool_oracle.c"
 #include "hydro_oracle.c"
@@ -70,7 +85,22 @@ static inline bool isnan(cdouble a) { return std::isnan(a.v); }
 
 #define FC_API extern "C" __attribute__((visibility("default")))
 
-FC_API void fc_reset(void) { memset(&g_fc, 0, sizeof g_fc); }
+FC_API void fc_reset(void)
+{
+    memset(&g_fc, 0, sizeof g_fc);
+    memset(&g_mark, 0, sizeof g_mark);
+    memset(g_phase, 0, sizeof g_phase);
+}
+FC_API void fc_phase_read(unsigned long long* out)
+{
+    for (int k = 0; k < 4; ++k) {
+        out[5 * k + 0] = g_phase[k].add;
+        out[5 * k + 1] = g_phase[k].mul;
+        out[5 * k + 2] = g_phase[k].div;
+        out[5 * k + 3] = g_phase[k].sqrt;
+        out[5 * k + 4] = g_phase[k].trans;
+    }
+}
 FC_API void fc_read(unsigned long long* out)
 {
     out[0] = g_fc.add;

@@ -29,6 +29,7 @@ def build():
     subprocess.run(["make", "-s", "-C", HERE, "liboracle_fc.so"], check=True)
     L = C.CDLL(os.path.join(HERE, "liboracle_fc.so"))
     L.fc_read.argtypes = [C.c_void_p]
+    L.fc_phase_read.argtypes = [C.c_void_p]
     L.fc_unsplit_blocks.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_double, C.c_double]
     L.fc_dt_blocks.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_double]
@@ -44,6 +45,19 @@ def counts(L):
     return {"add": a, "mul": m, "div": d, "sqrt": s, "flops": a + m + d + s, "transcendental": t}
 
 
+PHASES = ("recon", "flux", "emf", "update")
+
+
+def phase_counts(L):
+    out = np.zeros(20, np.uint64)
+    L.fc_phase_read(out.ctypes.data_as(C.c_void_p))
+    res = {}
+    for k, name in enumerate(PHASES):
+        a, m, d, s, t = (int(x) for x in out[5 * k:5 * k + 5])
+        res[name] = {"add": a, "mul": m, "div": d, "sqrt": s, "flops": a + m + d + s, "transcendental": t}
+    return res
+
+
 def per(c, n):
     return {k: v / n for k, v in c.items()}
 
@@ -56,7 +70,10 @@ def main():
     L = build()
     out = {"definition": "per interior zone-update; + - * / sqrt = 1 flop each (add, mul, div, sqrt), "
                          "exp/log/pow counted as transcendental; negation, fabs, min/max, compares not counted",
-           "source": "oracle/flopcount.py (counting-scalar build of the oracle)"}
+           "source": "oracle/flopcount.py (counting-scalar build of the oracle)",
+           "phases": "*_phases: the same counts split by the step's phases (recon: reconstruction with the "
+                     "hybrid-order divergence; flux: Riemann solves and artificial viscosity; emf: edge "
+                     "electric fields; update: face field and cell update), per interior zone-update"}
     zones = 8 * 4096
     for name, mhd, mach, sig in (("hydro_hllc", False, 2.0, 0.5), ("mhd_hlld_ct", True, 5.0, 1.0)):
         ic = W.turbulent_box(2, 2, 2, seed=41 + int(mhd), sigma_ln=sig, mach=mach, mhd=mhd, nvar=10)
@@ -73,6 +90,7 @@ def main():
         L.fc_reset()
         L.fc_unsplit_blocks(C.byref(p), 8, ptr(u), ptr(fx), ptr(fy), ptr(fz), dt, dx)
         out[name] = per(counts(L), zones)
+        out[name + "_phases"] = {k: per(v, zones) for k, v in phase_counts(L).items()}
         if mhd:
             units = G.code_units()
             sl = (slice(None), slice(4, 20), slice(4, 20), slice(4, 20))

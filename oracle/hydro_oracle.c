@@ -30,7 +30,9 @@
  * limited parabola. Riemann solvers: HLLC (Toro 1997 ch. 10, Davis wave
  * speeds) and HLLD (Miyoshi & Kusano 2005). Artificial viscosity follows
  * docs/torch_manual/main.tex:375-408. Electric fields: Gardiner & Stone
- * (2005) eq. 41/50 (contact-upwinded CT). Internal energy: Bryan et al.
+ * (2005) eq. 41/50 (contact-upwinded CT) with the cell-centred reference
+ * field at t + dt/2 (from the cell's face states along the edge).
+ * Internal energy: Bryan et al.
  * (1995) dual-energy formalism with eintSwitch.
  *
  * Every expression is written in the order the GPU kernels evaluate it;
@@ -46,6 +48,14 @@
 #define NP 8   /* primitive vars rho, vx, vy, vz, p, Bx, By, Bz */
 
 static const double TWO3 = 2.0 / 3.0;
+
+/* Phase marks of one block step for the flop-counting build (flopcount.cpp
+ * attributes the arithmetic since the previous mark to phase k: 0
+ * reconstruction, 1 Riemann fluxes, 2 edge electric fields, 3 face field
+ * and cell update; -1 only sets the mark). No-ops otherwise. */
+#ifndef ORC_PHASE
+#define ORC_PHASE(k) ((void)0)
+#endif
 
 void orc_hydro_default_params(orc_hydro_params* p, int mhd)
 {
@@ -888,6 +898,7 @@ static int unsplit_block(const orc_hydro_params* p, double* u, double* bxf, doub
     double del[3] = {dx, dy, dz};
     const double gm1 = p->gamma - 1.0;
 
+    ORC_PHASE(-1);
     recon_out* rec = (recon_out*)calloc((size_t)n3, sizeof(recon_out));
     /* undivided velocity divergence over the band (hybrid order) */
     double* divu = (double*)calloc((size_t)n3, sizeof(double));
@@ -921,6 +932,7 @@ static int unsplit_block(const orc_hydro_params* p, double* u, double* bxf, doub
                     p->cflc[(i - lo) + nxb * ((j - lo) + nxb * (k - lo))] = (unsigned char)(codes[0] | codes[1] | codes[2]);
             }
     free(divu);
+    ORC_PHASE(0);
 
     /* fluxes: face index I = left face of cell I; faces lo..hi+1 in the
      * normal direction, cells rlo..rhi across */
@@ -981,6 +993,7 @@ static int unsplit_block(const orc_hydro_params* p, double* u, double* bxf, doub
                 }
     }
 
+    ORC_PHASE(1);
     /* edge electric fields (mhd), Gardiner & Stone 2005 eqs. 41, 50 */
     double* emf[3] = {NULL, NULL, NULL};
     if (p->mhd) {
@@ -1006,15 +1019,23 @@ static int unsplit_block(const orc_hydro_params* p, double* u, double* bxf, doub
                         AT(t, A, B, C);     face_flux* fb1 = &FF(bb, t[0], t[1], t[2]);
                         double ea0 = -fa0->f[5 + bb], ea1 = -fa1->f[5 + bb];
                         double eb0 = fb0->f[5 + a], eb1 = fb1->f[5 + a];
-                        /* cell-centred reference E_c = -(v x B)_c at the four cells */
+                        /* cell-centred reference E_c = -(v x B)_c at the four
+                         * cells, at the fluxes' time level t + dt/2: from the
+                         * mean of the cell's own two face states along c (time
+                         * centred by the tracing and by the transverse terms of
+                         * the other two directions; v_a, v_b, B_a, B_b are
+                         * tangential to c). A plane-parallel flow then gets the
+                         * 1-D Riemann flux at every edge, as the method requires
+                         * (Gardiner & Stone 2005 sec. 3) */
                         double ecc[2][2];
                         for (int ia = 0; ia < 2; ++ia)
                             for (int ib = 0; ib < 2; ++ib) {
                                 AT(t, A - 1 + ia, B - 1 + ib, C);
-                                double va = U(&b, ORV_VELX + a, t[0], t[1], t[2]);
-                                double vb = U(&b, ORV_VELX + bb, t[0], t[1], t[2]);
-                                double Ba = U(&b, ORV_MAGX + a, t[0], t[1], t[2]);
-                                double Bb = U(&b, ORV_MAGX + bb, t[0], t[1], t[2]);
+                                const recon_out* rc = &rec[cidx(n, t[0], t[1], t[2])];
+                                double va = 0.5 * (rc->wp[c][1 + a] + rc->wn[c][1 + a]);
+                                double vb = 0.5 * (rc->wp[c][1 + bb] + rc->wn[c][1 + bb]);
+                                double Ba = 0.5 * (rc->wp[c][5 + a] + rc->wn[c][5 + a]);
+                                double Bb = 0.5 * (rc->wp[c][5 + bb] + rc->wn[c][5 + bb]);
                                 ecc[ia][ib] = vb * Ba - va * Bb;
                             }
                         double eavg = 0.25 * (ea0 + ea1 + eb0 + eb1);
@@ -1031,6 +1052,7 @@ static int unsplit_block(const orc_hydro_params* p, double* u, double* bxf, doub
         }
     }
 
+    ORC_PHASE(2);
     /* flux conservation at fine-coarse faces (after the electric fields,
      * which use the block's own fluxes) */
     if (fx) flux_fix(fx, fl, n, lo, nxb);
@@ -1125,6 +1147,7 @@ static int unsplit_block(const orc_hydro_params* p, double* u, double* bxf, doub
                     unew[ORV_MAGZ * n3 + ci] = Bn[2];
                 }
             }
+    ORC_PHASE(3);
     memcpy(u, unew, sizeof(double) * (size_t)(ORV_NVAR * n3));
     if (p->mhd) {
         for (int d = 0; d < 3; ++d) {

@@ -84,6 +84,8 @@ void orc_table_from_ilog(orc_table* t, const int32_t* logT_e4, const int32_t* lo
 
 int orc_find(const double* x, double x0, int N); /* find.F90:9-42, 1-based */
 double orc_radloss(double T);                     /* heatCool.F90:1590-1667 */
+/* dust_cooling, heatCool.F90:1305-1390: gas-dust cooling [erg/g/s] */
+double orc_dust_cooling(const orc_cool_params* p, double n, double T, double tdust, double rho);
 double orc_lin_interp(double x1, double y1, double x2, double y2, double x);
 
 /* heating_and_cooling(ei, timestep, temp, ncount), heatCool.F90:41-700.

@@ -90,6 +90,11 @@ def lib():
         L.orc_find.restype = C.c_int
         L.orc_radloss.argtypes = [C.c_double]
         L.orc_radloss.restype = C.c_double
+        L.orc_dust_cooling.argtypes = [C.POINTER(CoolParams), C.c_double, C.c_double, C.c_double, C.c_double]
+        L.orc_dust_cooling.restype = C.c_double
+        L.orc_heating_and_cooling.argtypes = [C.POINTER(CoolParams), C.POINTER(Table), C.POINTER(CoolVars),
+                                              C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_double),
+                                              C.c_void_p]
         L.orc_dei_dt.argtypes = [C.POINTER(CoolParams), C.POINTER(Table), C.POINTER(CoolVars),
                                  C.c_double, C.c_double]
         L.orc_dei_dt.restype = C.c_double

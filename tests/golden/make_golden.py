@@ -71,4 +71,6 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2 and not os.environ.get("GBHYDRO_REFERENCE"):
+        sys.exit("usage: make_golden.py REFERENCE_ROOT (or set GBHYDRO_REFERENCE)")
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ["GBHYDRO_REFERENCE"])

@@ -56,3 +56,19 @@ def test_noalloc_rejects_more_blocks_than_its_scratch(gb):
     rc = gb.lib().gb_hydro_unsplit_noalloc(5, C.c_void_p(too_many.data_ptr()), 1e-3, 1e-3, None, None)
     assert rc == -5
     assert b"outside 0..4" in gb.lib().gb_last_error()
+
+
+def test_noalloc_argument_checks(gb):
+    """Arguments are checked before any launch: no blocks is a no-op, a
+    non-positive dt or a missing list with blocks is rejected."""
+    import torch
+    g, _ = _grid(gb)
+    gb.init_hydro(gb.hydro_params(True, precision=0))
+    g.register()
+    L = gb.lib()
+    lst = C.c_void_p(g.t_leaf.data_ptr())
+    assert L.gb_hydro_unsplit_noalloc(0, None, 1e-3, 1e-3, None, None) == 0
+    assert L.gb_hydro_unsplit_noalloc(4, lst, 0.0, 1e-3, None, None) == -1
+    assert L.gb_hydro_unsplit_noalloc(4, lst, -1e-3, 1e-3, None, None) == -1
+    assert L.gb_hydro_unsplit_noalloc(2, None, 1e-3, 1e-3, None, None) == -1
+    torch.cuda.synchronize()

@@ -81,52 +81,61 @@ extern "C" int gb_prof_read(double* ms, long long* launches, int n)
 }
 
 // FP64 FMA throughput probe: 8 independent dependency chains per thread
-__global__ void __launch_bounds__(256) k_fp64_fma(double* out, int iters, double a, double b)
+// NCH independent FMA chains per thread (enough to hide the pipe latency)
+template <typename T, int NCH>
+__global__ void __launch_bounds__(256) k_fma_peak(T* out, int iters, T a, T b)
 {
-    double x[8];
+    T x[NCH];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) x[q] = 1e-3 * (threadIdx.x + q);
+    for (int q = 0; q < NCH; ++q) x[q] = (T)1e-3 * (T)(threadIdx.x + q);
     for (int it = 0; it < iters; ++it) {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) x[q] = fma(x[q], a, b);
+        for (int q = 0; q < NCH; ++q) x[q] = fma(x[q], a, b);
     }
-    double s = 0.0;
+    T s = (T)0;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) s += x[q];
-    if (s == -1.0) out[0] = s;  // keeps the chains live; never true
+    for (int q = 0; q < NCH; ++q) s += x[q];
+    if (s == (T)-1) out[0] = s;  // keeps the chains live; never true
 }
 
-extern "C" int gb_measure_fp64_peak(double* tflops)
+// FMA throughput of the current GPU in TFLOP/s (2 flops per FMA), best of
+// five timed launches of a few milliseconds over 8 CTAs per SM
+template <typename T, int NCH>
+static int measure_fma_peak(double* tflops)
 {
     if (!tflops) return GB_ERR_ARG;
     int dev = 0, nsm = 0;
     if (gb_check(cudaGetDevice(&dev), "device") ||
         gb_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "sm count"))
         return GB_ERR_CUDA;
-    double* d = nullptr;
-    if (gb_check(cudaMalloc(&d, sizeof(double)), "probe alloc")) return GB_ERR_CUDA;
+    T* d = nullptr;
+    if (gb_check(cudaMalloc(&d, sizeof(T)), "probe alloc")) return GB_ERR_CUDA;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    const int iters = 1 << 14, blocks = nsm * 8, threads = 256;
-    k_fp64_fma<<<blocks, threads>>>(d, iters, 0.9999999, 1e-7);
+    const int iters = sizeof(T) == 8 ? 1 << 14 : 1 << 16, blocks = nsm * 8, threads = 256;
+    const T a = (T)0.9999999, b = (T)1e-7;
+    k_fma_peak<T, NCH><<<blocks, threads>>>(d, iters, a, b);
     float best = 1e30f;
     for (int r = 0; r < 5; ++r) {
         cudaEventRecord(e0);
-        k_fp64_fma<<<blocks, threads>>>(d, iters, 0.9999999, 1e-7);
+        k_fma_peak<T, NCH><<<blocks, threads>>>(d, iters, a, b);
         cudaEventRecord(e1);
         cudaEventSynchronize(e1);
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, e0, e1);
         if (ms < best) best = ms;
     }
-    int rc = gb_check(cudaGetLastError(), "k_fp64_fma") ? GB_ERR_CUDA : GB_OK;
+    int rc = gb_check(cudaGetLastError(), "k_fma_peak") ? GB_ERR_CUDA : GB_OK;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(d);
-    *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+    *tflops = 2.0 * NCH * (double)iters * (double)blocks * threads / (best * 1e-3) / 1e12;
     return rc;
 }
+
+extern "C" int gb_measure_fp64_peak(double* tflops) { return measure_fma_peak<double, 8>(tflops); }
+extern "C" int gb_measure_fp32_peak(double* tflops) { return measure_fma_peak<float, 16>(tflops); }
 
 // the integer-pipe conversions against the hardware ones, bit for bit
 __global__ void k_check_conv(int64_t n, const double* __restrict__ d, const float* __restrict__ f,

@@ -544,11 +544,28 @@ k_divu(gb_dev_grid g, const int* __restrict__ list, const float* __restrict__ p3
 // more than (gamma + 1) / (gamma - 1) (the strong-shock limit, Toro 1997
 // eq. 3.58), so a face state whose density differs from its cell's by more
 // is not shock-connected to it
+//
+// The check's arithmetic uses explicitly rounded operations: they share no
+// subexpression with the reconstruction and are never contracted, so the
+// check leaves the compiler's fusing of the reconstruction's own
+// arithmetic (and with it the mixed path's results) the same in every
+// launch-shape instantiation.
+__device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float rn_div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float rn_sqrt(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rn_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double rn_div(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double rn_sqrt(double a) { return __dsqrt_rn(a); }
+
 template <typename T>
 __device__ __forceinline__ bool rh_fail(T gam, T rho_c, T rho_f)
 {
-    const T lim = (gam + (T)1) / (gam - (T)1);
-    return rho_f > lim * rho_c || rho_c > lim * rho_f;
+    const T lim = rn_div(rn_add(gam, (T)1), rn_sub(gam, (T)1));
+    return rho_f > rn_mul(lim, rho_c) || rho_c > rn_mul(lim, rho_f);
 }
 
 // ---------------------------------------------------------------- k_recon
@@ -762,10 +779,10 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
     unsigned code = 0;
     if (kp.hybrid) {
         // (gamma p + B.B) / rho, B.B summed in x, y, z order
-        const T b0 = wc[5] * wc[5], b1 = wc[6] * wc[6], b2 = wc[7] * wc[7];
-        T cs = gam * wc[4] + ((pick3(d, b0, b2, b1) + pick3(d, b1, b0, b2)) + pick3(d, b2, b1, b0));
-        cs = sqrt(cs / wc[0]);
-        comp = ((const T*)kp.divu)[(size_t)cb * NRC + cc] < (T)kp.kappa * cs;
+        const T b0 = rn_mul(wc[5], wc[5]), b1 = rn_mul(wc[6], wc[6]), b2 = rn_mul(wc[7], wc[7]);
+        T cs = rn_add(rn_mul(gam, wc[4]), rn_add(rn_add(pick3(d, b0, b2, b1), pick3(d, b1, b0, b2)), pick3(d, b2, b1, b0)));
+        cs = rn_sqrt(rn_div(cs, wc[0]));
+        comp = ((const T*)kp.divu)[(size_t)cb * NRC + cc] < rn_mul((T)kp.kappa, cs);
         if (comp && (rh_fail(gam, wc[0], wp[0]) || rh_fail(gam, wc[0], wn[0]))) {
 #pragma unroll
             for (int v = 0; v < NP; ++v) { wn[v] = wc[v]; wp[v] = wc[v]; }
@@ -1143,38 +1160,33 @@ constexpr int EMF_CELLS = RB * RB;     // cells 3..20 across the plane
 constexpr int EMF_EDGES = 17 * 17;     // edges 4..20 across the plane
 
 template <typename T, int CD>
-__device__ __forceinline__ void emf_plane(const gb_dev_grid& g, const int* __restrict__ list, const T* __restrict__ fscr,
-                                          size_t fstride, double* __restrict__ escr, size_t estride,
-                                          const float* __restrict__ p32, size_t p32_stride, T* s_ecc)
+__device__ __forceinline__ void emf_plane(const int* __restrict__ list, const T* __restrict__ rscr, size_t rstride,
+                                          const T* __restrict__ fscr, size_t fstride, double* __restrict__ escr,
+                                          size_t estride, T* s_ecc)
 {
     using R = T;
     constexpr int c = CD;
     constexpr int a = (c + 1) % 3, b = (c + 2) % 3;
     const int cb = blockIdx.z;
-    const int blk = list[cb];
     const int C = LO + blockIdx.x;
     int t[3];
     auto at = [&](int av, int bv, int cv) { t[a] = av; t[b] = bv; t[c] = cv; };
-    const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
-    const float* pb = p32 + (size_t)cb * p32_stride;
-    // x runs fastest across the threads where the plane has an x axis (it is
-    // a for c = 2 and b for c = 1), so that their loads are contiguous
+    const T* rs = rscr + (size_t)cb * rstride;
+    // the cell-centred reference field at the fluxes' time level t + dt/2:
+    // from the mean of the cell's two face states along c (time centred by
+    // the tracing and the other directions' transverse terms; v and B along
+    // a and b are tangential to c, so both states carry them), so that a
+    // plane-parallel flow gets the 1-D Riemann flux at every edge
+    // (Gardiner & Stone 2005 sec. 3). x runs fastest across the threads
+    // where the plane has an x axis (a for c = 2, b for c = 1).
     for (int q = threadIdx.x; q < EMF_CELLS; q += EMF_THREADS) {
         const int qa = c == 1 ? q / RB : q % RB, qb = c == 1 ? q % RB : q / RB;
         at(RLO + qa, RLO + qb, C);
-        const int ci = gb_cidx(t[0], t[1], t[2]);
-        R va, vb, Ba, Bb;
-        if constexpr (std::is_same<T, float>::value) {
-            va = pb[(size_t)(1 + a) * GB_N3 + ci];
-            vb = pb[(size_t)(1 + b) * GB_N3 + ci];
-            Ba = pb[(size_t)(5 + a) * GB_N3 + ci];
-            Bb = pb[(size_t)(5 + b) * GB_N3 + ci];
-        } else {
-            va = base[(int64_t)g.slot[GB_VELX + a] * GB_N3 + ci];
-            vb = base[(int64_t)g.slot[GB_VELX + b] * GB_N3 + ci];
-            Ba = base[(int64_t)g.slot[GB_MAGX + a] * GB_N3 + ci];
-            Bb = base[(int64_t)g.slot[GB_MAGX + b] * GB_N3 + ci];
-        }
+        const int rc = rc_index(t[0], t[1], t[2]);
+        auto sv = [&](int var) -> R {
+            return (R)0.5 * (rs[((size_t)(0 * 3 + c) * NP + var) * NRC + rc] + rs[((size_t)(1 * 3 + c) * NP + var) * NRC + rc]);
+        };
+        const R va = sv(1 + a), vb = sv(1 + b), Ba = sv(5 + a), Bb = sv(5 + b);
         s_ecc[qa + RB * qb] = vb * Ba - va * Bb;
     }
     __syncthreads();
@@ -1209,13 +1221,13 @@ __device__ __forceinline__ void emf_plane(const gb_dev_grid& g, const int* __res
 // grid (16 planes, 3 directions, blocks)
 template <typename T>
 __global__ void __launch_bounds__(EMF_THREADS)
-k_emf(gb_dev_grid g, const int* __restrict__ list, const T* __restrict__ fscr, size_t fstride,
-      double* __restrict__ escr, size_t estride, const float* __restrict__ p32, size_t p32_stride)
+k_emf(const int* __restrict__ list, const T* __restrict__ rscr, size_t rstride, const T* __restrict__ fscr,
+      size_t fstride, double* __restrict__ escr, size_t estride)
 {
     __shared__ T s_ecc[EMF_CELLS];
-    if (blockIdx.y == 0) emf_plane<T, 0>(g, list, fscr, fstride, escr, estride, p32, p32_stride, s_ecc);
-    else if (blockIdx.y == 1) emf_plane<T, 1>(g, list, fscr, fstride, escr, estride, p32, p32_stride, s_ecc);
-    else emf_plane<T, 2>(g, list, fscr, fstride, escr, estride, p32, p32_stride, s_ecc);
+    if (blockIdx.y == 0) emf_plane<T, 0>(list, rscr, rstride, fscr, fstride, escr, estride, s_ecc);
+    else if (blockIdx.y == 1) emf_plane<T, 1>(list, rscr, rstride, fscr, fstride, escr, estride, s_ecc);
+    else emf_plane<T, 2>(list, rscr, rstride, fscr, fstride, escr, estride, s_ecc);
 }
 
 __device__ __forceinline__ int edge_index(int c, int i, int j, int k)

@@ -86,7 +86,7 @@ int launch_chunk(const hydro_kparams& kp_in, int mhd, int cool, int nblk, const 
         put_fluxes<T>(kp, nblk, list, fscr, s);
         dim3 eg(GB_NXB, 3, nblk);
         gb_prof_begin(GBP_EMF, s);
-        k_emf<T><<<eg, EMF_THREADS, 0, s>>>(g, list, fscr, SL::flux, escr, SL::emf, p32, SL::prim32);
+        k_emf<T><<<eg, EMF_THREADS, 0, s>>>(list, rscr, SL::recon, fscr, SL::flux, escr, SL::emf);
         if (kp.ec_reg)
             k_emf_put<<<dim3((NSURF + 127) / 128, nblk), 128, 0, s>>>(list, kp.ec_near, escr, SL::emf, kp.ec_reg);
         gb_prof_end(GBP_EMF, s);

@@ -125,6 +125,7 @@ _SIG = {
     "gb_cfl_codes_reset": (C.c_int, [C.c_void_p]),
     "gb_set_flux_correction": (C.c_int, [C.c_int]),
     "gb_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
+    "gb_measure_fp32_peak": (C.c_int, [C.POINTER(C.c_double)]),
     "gb_selfcheck_conversions": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gb_graph_reset": (C.c_int, []),
     "gb_graph_info": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
@@ -430,6 +431,13 @@ def measure_fp64_peak() -> float:
     """FP64 FMA throughput of this GPU, TFLOP/s."""
     v = C.c_double()
     check(lib().gb_measure_fp64_peak(C.byref(v)), "gb_measure_fp64_peak")
+    return v.value
+
+
+def measure_fp32_peak() -> float:
+    """FP32 FMA throughput of this GPU, TFLOP/s."""
+    v = C.c_double()
+    check(lib().gb_measure_fp32_peak(C.byref(v)), "gb_measure_fp32_peak")
     return v.value
 
 
