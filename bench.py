@@ -541,6 +541,7 @@ def main():
     ap.add_argument("--tile", type=int, default=32, help="with --chunk: reconstruction tile (32 or 64)")
     ap.add_argument("--occ", type=int, default=0, help="with --chunk: reconstruction occupancy bound (0, 1 or 2)")
     ap.add_argument("--streams", type=int, default=1, help="with --chunk: streams the chunks alternate between (1 or 2)")
+    ap.add_argument("--fused", type=int, default=0, help="with --chunk: reconstruction and Riemann solve fused per block")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -593,6 +594,7 @@ def main():
         if args.chunk:
             G.set_launch_config(args.chunk, args.tile, args.occ)
             G.set_chunk_streams(args.streams)
+            G.set_fused(bool(args.fused))
         if args.only == "e2e":
             # the fast path (launch shapes as given) end to end from host arrays
             G.set_cooling_mode(True)
@@ -758,7 +760,7 @@ def main():
                                                  zones * world / (ms_mixed * 1e-3), ms_plain / ms_mixed),
         "fast_eager": {"ms_per_step": ms_eager, "value": zones * world / (ms_eager * 1e-3),
                        "note": "the same fast path launched kernel by kernel with the host reading dt each step"},
-        "launch_config": {k: ginfo["tuned"].get(k) for k in ("chunk", "tile", "occ", "streams", "cached")}
+        "launch_config": {k: ginfo["tuned"].get(k) for k in ("chunk", "tile", "occ", "streams", "fused", "cached")}
         if ginfo["tuned"] else {"chunk": 16, "tile": 32, "occ": 0, "streams": 1, "tuned": False},
         "kernel_ms_per_step_fast": {k: v[0] / args.steps for k, v in prof.items()},
         "kernel_launches_per_step_fast": {k: v[1] / args.steps for k, v in prof.items()},

@@ -45,7 +45,8 @@ enum {
     GB_ST_NONFINITE = 3,    /* NaN/Inf in the updated state */
     GB_ST_ZERO_UNBRACKETED = 4, /* Brent entered without a sign change (Fortran `stop`) */
     GB_ST_ZERO_MAXITER = 5, /* Brent iteration cap (Fortran `stop`) */
-    GB_ST_OVERHEAT = 6      /* T > absTmax clamped (RadHeat.F90:380-405) */
+    GB_ST_OVERHEAT = 6,     /* T > absTmax clamped (RadHeat.F90:380-405) */
+    GB_ST_TIMEOUT = 7       /* a bounded wait for a tensor-memory copy gave up */
 };
 
 /* Device-resident status word: the first failure plus counters. */
@@ -200,6 +201,16 @@ int gb_set_chunk_blocks(int n);
  * torch_gb300.autotune; no counterpart in the reference. */
 int gb_set_launch_config(int chunk_blocks, int recon_tile, int recon_occupancy);
 int gb_get_launch_config(int* chunk_blocks, int* recon_tile, int* recon_occupancy);
+
+/* Reconstruction and Riemann solve as one kernel per block (1) or as two
+ * kernels over a chunk with the face states in between in device memory
+ * (0, the default). The fused kernel keeps each plane's face states in
+ * shared memory and, in the mixed path, stages a rolling window of the
+ * block's FP32 primitives with the tensor memory accelerator. The same
+ * arithmetic either way; chosen by torch_gb300.autotune; no counterpart in
+ * the reference. */
+int gb_set_fused(int on);
+int gb_get_fused(void);
 
 /* Streams the chunks of a step run on (1 or 2). With 2, consecutive chunks
  * alternate between the caller's stream and a library stream, each with its

@@ -122,3 +122,90 @@ def test_brent_tolerance_knob(gb, oracle):
     assert np.any(T_tight[ok] != T_ref[ok])
     with pytest.raises(gb.GBError):
         gb.set_brent_tolerance(0.0)
+
+
+def test_euler_integrator_matches_oracle(gb, oracle):
+    """The subcycled explicit Euler branch (heatCool.F90:119-214, he_subfactor
+    0.3) against the oracle's on 4000 cells: the same subcycles, so the
+    temperatures agree to the accumulated rounding of the rate functions
+    (CUDA's exp/pow against the C library's)."""
+    import torch
+    from torch_gb300 import tables
+    gb.init_cooling(gb.cool_params(int_method=1))
+    try:
+        rho, ei, T, tdust, _ = _cells(4000, 21)
+        dt = 1e9
+        p = oracle.cool_params(int_method=1)
+        t = oracle.table_from_ilog(*tables.read_compact())
+        e_o, T_o, td_o = ei.copy(), T.copy(), tdust.copy()
+        oracle.radheat_cells(p, t, dt, rho.copy(), ei.copy(), e_o, T_o, td_o, threads=8)
+        dev = lambda a: torch.as_tensor(a.copy(), device="cuda")
+        d_rho, d_ei, d_T, d_td = dev(rho), dev(ei), dev(T), dev(tdust)
+        gb.cool_cells(d_rho, d_ei, d_T, d_td, dt)
+        torch.cuda.synchronize()
+        T_g = d_T.cpu().numpy()
+    finally:
+        gb.init_cooling(gb.cool_params())
+    rel = np.abs(T_g - T_o) / T_o
+    assert np.all(np.isfinite(T_g))
+    assert np.median(rel) < 1e-12 and rel.max() < 1e-6, (np.median(rel), rel.max())
+
+
+def test_fused_cooling_epilogue_matches_oracle(gb, oracle):
+    """One plain FP64 MHD step with the cooling fused into the update's
+    epilogue on the 128^3 box (8^3 blocks; sigma_ln 1, Mach 5, beta 1, the
+    reference's second configuration) against the oracle on a sample of 16
+    blocks: hydro step, then RadHeat on the new state (temperature from the
+    new internal energy, as the hydro's EOS call leaves it). Density,
+    velocity and field to 1e-12; internal energy, temperature and dust
+    temperature within the root finder's tolerance max(1 K, 1e-6 T)."""
+    from torch_gb300 import tables
+    from torch_gb300 import workloads as W
+    ic = W.turbulent_box(8, 8, 8, seed=44, sigma_ln=1.0, mach=5.0, mhd=True, beta=1.0, dA=0.1, nvar=10)
+    g = gb.grid_from_workload(ic, mhd=True, cooling=True)
+    units = gb.code_units()
+    mu, gm1 = 24.0 / 11.0, 2.0 / 3.0
+    Tof = units["vel_unit"] ** 2 * gm1 * mu * gb.MP / gb.KB
+    g.u[:, g.slots["TEMP"]] = g.u[:, g.slots["EINT"]] * Tof
+    g.u[:, g.slots["TDUS"]] = 18.0
+    gb.init_cooling(gb.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
+                                   time_unit=units["time_unit"]))
+    gb.init_hydro(gb.hydro_params(True, precision=0))
+    gb.set_cooling_mode(False)
+    g.register()
+    dt = g.compute_dt().item()
+    g.status_reset()
+    g.evolve_step(dt, cool=True)
+    out = g.u.cpu().numpy()
+    st = g.status_read()
+    # the oracle on 16 sampled blocks
+    p = oracle.hydro_params(True)
+    u, fx, fy, fz = (ic[k].copy() for k in ("u", "fx", "fy", "fz"))
+    oracle.fill_guards_periodic(p, 8, 8, 8, u, fx, fy, fz)
+    dx = ic["dx"]
+    assert dt == 0.8 * oracle.dt_limit(p, u, dx, dx, dx)
+    sample = np.arange(0, 512, 32, dtype=np.int32)
+    tl = oracle.TreeLists({"level": np.zeros(512, np.int32), "coord": np.zeros((512, 3), np.int32),
+                           "child": -np.ones((512, 8), np.int32), "root": np.arange(512, dtype=np.int32),
+                           "nr": (8, 8, 8), "maxlevel": 0})
+    oracle.unsplit_list(p, tl, sample, u, fx, fy, fz, dt, dx)
+    I = (sample[:, None, None, None], slice(4, 20), slice(4, 20), slice(4, 20))
+    rho = np.ascontiguousarray(u[:, 0][I] * units["dens_unit"]).ravel()
+    ei = np.ascontiguousarray(u[:, 6][I] * units["vel_unit"] ** 2).ravel()
+    T = ei * gm1 * mu * gb.MP / gb.KB
+    td = np.full_like(T, 18.0)
+    cp = oracle.cool_params()
+    tab = oracle.table_from_ilog(*tables.read_compact())
+    _, flags = oracle.radheat_cells(cp, tab, dt * units["time_unit"], rho, ei.copy(), ei, T, td, threads=8)
+    ok = (flags & (4 | 8)) == 0
+    for v in (0, 1, 2, 3, 7, 8, 9):
+        a, b = out[:, v][I].ravel(), u[:, v][I].ravel()
+        assert np.max(np.abs(a - b) / (np.abs(b) + 1e-300)) <= 1e-12, v
+    tol = 2.0 * np.maximum(1.0, 1e-6 * T)
+    T_g = out[:, g.slots["TEMP"]][I].ravel()
+    assert np.all(np.abs(T_g - T)[ok] <= tol[ok])
+    e_g = out[:, 6][I].ravel() * units["vel_unit"] ** 2
+    assert np.all((np.abs(e_g - ei) <= tol / T * ei)[ok])
+    td_g = out[:, g.slots["TDUS"]][I].ravel()
+    assert np.all((np.abs(td_g - td) <= 1e-3 * td + 0.1)[ok])
+    assert ok.mean() > 0.99 and st["code"] in (0, 6), st

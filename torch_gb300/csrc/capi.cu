@@ -1403,6 +1403,24 @@ int gb_streams_prepare(int nchunks)
     return GB_OK;
 }
 int gb_recon_tile() { return g_recon_tile; }
+
+static int g_fused = 0;
+int gb_fused_step() { return g_fused; }
+int gb_fused_attr_fp64();
+int gb_fused_attr_mixed();
+
+extern "C" int gb_set_fused(int on)
+{
+    if (on) {
+        // the fused kernels' shared memory beyond the default 48 KB
+        if (gb_fused_attr_fp64() || gb_fused_attr_mixed()) return GB_ERR_CUDA;
+    }
+    g_fused = on ? 1 : 0;
+    g_gb.gen += 1;
+    return GB_OK;
+}
+
+extern "C" int gb_get_fused(void) { return g_fused; }
 int gb_recon_occupancy() { return g_recon_occ; }
 
 extern "C" int gb_set_launch_config(int chunk_blocks, int recon_tile, int recon_occupancy)

@@ -70,3 +70,4 @@ int gb_chunk_blocks();
 int gb_chunk_streams();
 int gb_recon_tile();
 int gb_recon_occupancy();
+int gb_fused_step();

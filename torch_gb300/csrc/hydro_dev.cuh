@@ -50,8 +50,11 @@ struct scratch_layout {
     // hybrid order: the minimum undivided velocity divergence over each
     // band cell's box (T)
     static constexpr size_t divu = (size_t)NRC;
-    static constexpr size_t bytes =
-        recon * sizeof(T) + flux * sizeof(T) + (emf + fb) * sizeof(double) + prim32 * sizeof(float) + divu * sizeof(T);
+    // the edge fields' cell-centred reference, -(v x B)_d of the mean face
+    // state along d, per direction and band cell (T)
+    static constexpr size_t ecc = (size_t)3 * NRC;
+    static constexpr size_t bytes = recon * sizeof(T) + flux * sizeof(T) + (emf + fb) * sizeof(double) +
+                                    prim32 * sizeof(float) + divu * sizeof(T) + ecc * sizeof(T);
 };
 // the FP32 copy of each block starts on a 16-byte boundary (k_prim32 stores
 // four cells at a time): every section before it and its own stride are
@@ -423,6 +426,9 @@ struct hydro_kparams {
     int hybrid = 0, lower_cfl = 0;
     double kappa = 0.0;
     const void* divu = nullptr;
+    // the edge fields' reference per direction and band cell (T, 3 x NRC
+    // per chunk block), written by the reconstruction
+    void* ecc = nullptr;
     // per-cell CFL codes of the interior cells (store block x 3 directions
     // x 4096 bytes; null: not kept), read by the next CFL limit
     unsigned char* cflc = nullptr;
@@ -638,17 +644,16 @@ __device__ __forceinline__ void load_rot(const gb_dev_grid& g, int blk, int ci, 
 
 // normal-direction PPM and the normal MHD term of direction d; wp, wn, wc
 // come back in the rotated frame, s_sig / s_abn in the unrotated one
-template <typename T, bool MHD, int TILE>
-__device__ __forceinline__ void recon_normal(const gb_dev_grid& g, T gam, const T* dtd, const T* hd, int d, int blk,
-                                             int i, int j, int k, int lane, const float* p32b, const int* off,
-                                             T (*s_sig)[NP][TILE], T (*s_abn)[NP][TILE], T (*s_dnb)[TILE], T* wp,
-                                             T* wn, T* wc)
+// ld(m, w): the rotated primitives of stencil point m (0..4, centre 2)
+template <typename T, bool MHD, int TILE, typename LD>
+__device__ __forceinline__ void recon_normal_ld(const gb_dev_grid& g, T gam, const T* dtd, const T* hd, int d, int blk,
+                                                int i, int j, int k, int lane, const float* p32b, const LD& ld,
+                                                T (*s_sig)[NP][TILE], T (*s_abn)[NP][TILE], T (*s_dnb)[TILE], T* wp,
+                                                T* wn, T* wc)
 {
     T qs[5][NP];
-    const int stride = d == 0 ? 1 : (d == 1 ? GB_N : GB_N * GB_N);
-    const int c0 = gb_cidx(i, j, k);
 #pragma unroll
-    for (int m = 0; m < 5; ++m) load_rot<T, MHD>(g, blk, c0 + (m - 2) * stride, p32b, off, qs[m]);
+    for (int m = 0; m < 5; ++m) ld(m, qs[m]);
 #pragma unroll
     for (int s = 0; s < NP; ++s) wc[s] = qs[2][s];
     T sgr[NP];
@@ -676,6 +681,30 @@ __device__ __forceinline__ void recon_normal(const gb_dev_grid& g, T gam, const 
         }
         s_dnb[d][lane] = dnb;
     }
+}
+
+template <typename T, bool MHD, int TILE>
+__device__ __forceinline__ void recon_normal(const gb_dev_grid& g, T gam, const T* dtd, const T* hd, int d, int blk,
+                                             int i, int j, int k, int lane, const float* p32b, const int* off,
+                                             T (*s_sig)[NP][TILE], T (*s_abn)[NP][TILE], T (*s_dnb)[TILE], T* wp,
+                                             T* wn, T* wc)
+{
+    const int stride = d == 0 ? 1 : (d == 1 ? GB_N : GB_N * GB_N);
+    const int c0 = gb_cidx(i, j, k);
+    auto ld = [&](int m, T* w) { load_rot<T, MHD>(g, blk, c0 + (m - 2) * stride, p32b, off, w); };
+    recon_normal_ld<T, MHD, TILE>(g, gam, dtd, hd, d, blk, i, j, k, lane, p32b, ld, s_sig, s_abn, s_dnb, wp, wn, wc);
+}
+
+// the cell-centred electric field along d, -(v x B)_d, of the mean of the
+// cell's two face states along d (rotated frame: slots 2, 3 are the
+// velocities along a = (d + 1) % 3 and b = (d + 2) % 3, slots 6, 7 their
+// fields): the edge fields' reference at the fluxes' time level
+template <typename T>
+__device__ __forceinline__ T ecc_of(const T* wp, const T* wn)
+{
+    const T va = (T)0.5 * (wp[2] + wn[2]), vb = (T)0.5 * (wp[3] + wn[3]);
+    const T Ba = (T)0.5 * (wp[6] + wn[6]), Bb = (T)0.5 * (wp[7] + wn[7]);
+    return vb * Ba - va * Bb;
 }
 
 // transverse corrections of direction d in the vendored order
@@ -733,28 +762,12 @@ __device__ __forceinline__ void recon_transverse(const T* hd, int d, int lane, T
     }
 }
 
-// MINB: resident CTAs per SM the register allocation must allow (1 = no
-// bound); the autotuner chooses between the unbounded kernel and a bound
-// that trades spills for occupancy
-template <typename T, bool MHD, int TILE, int MINB>
-__global__ void __launch_bounds__(3 * TILE, MINB)
-k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __restrict__ scr,
-        size_t scr_stride, const float* __restrict__ p32, size_t p32_stride, gb_status* st)
+// gamma, dt/dx and dt/(2 dx) of a block for reconstruction precision T:
+// FP32 throughout in the mixed path (no FP64 instruction), the oracle's
+// FP64 values otherwise
+template <typename T>
+__device__ __forceinline__ void recon_consts(const gb_dev_grid& g, const hydro_kparams& kp, int blk, T& gam, T* dtd, T* hd)
 {
-    __shared__ T s_sig[3][NP][TILE];
-    __shared__ T s_abn[3][NP][TILE];
-    __shared__ T s_dnb[3][TILE];
-    const int lane = threadIdx.x % TILE;
-    const int d = threadIdx.x / TILE;
-    const int cb = blockIdx.y;
-    const int blk = list[cb];
-    const int cell = blockIdx.x * TILE + lane;
-    const bool active = cell < NRC;
-    const int cc = active ? cell : 0;
-    const int i = RLO + cc % RB, j = RLO + (cc / RB) % RB, k = RLO + cc / (RB * RB);
-    // time step over cell size: FP32 throughout in the mixed path (no FP64
-    // instruction in this kernel), the oracle's FP64 values otherwise
-    T gam, dtd[3], hd[3];
     if constexpr (std::is_same<T, float>::value) {
         gam = kp.gammaf;
         kp_dtdxf(kp, gb_block_level(g, blk), dtd);
@@ -766,11 +779,24 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
 #pragma unroll
         for (int q = 0; q < 3; ++q) hd[q] = 0.5 * dtd[q];
     }
-    const float* p32b = p32 + (size_t)cb * p32_stride;
-    T wp[NP], wn[NP], wc[NP];
-    int off[NP];
-    rot_offsets<T, MHD>(g, d, off);
-    recon_normal<T, MHD, TILE>(g, gam, dtd, hd, d, blk, i, j, k, lane, p32b, off, s_sig, s_abn, s_dnb, wp, wn, wc);
+}
+
+// One cell and direction of the reconstruction (every thread of the CTA
+// calls it together: it holds the barrier between the normal and the
+// transverse part): normal-direction PPM and MHD term, hybrid-order check,
+// transverse corrections, second hybrid-order check, positivity fallback;
+// counts, the cell's CFL code and (MHD) the edge fields' reference. wp, wn
+// come back in d's rotated frame. ld(m, w) loads stencil point m; cell is
+// the band index (cc the one read when the thread has no cell).
+template <typename T, bool MHD, int TILE, typename LD>
+__device__ __forceinline__ void recon_item(const gb_dev_grid& g, const hydro_kparams& kp, int cb, int blk, int d,
+                                           int lane, int cell, int cc, bool active, int i, int j, int k, T gam,
+                                           const T* dtd, const T* hd, const float* p32b, const LD& ld,
+                                           T (*s_sig)[NP][TILE], T (*s_abn)[NP][TILE], T (*s_dnb)[TILE],
+                                           gb_status* st, T* wp, T* wn)
+{
+    T wc[NP];
+    recon_normal_ld<T, MHD, TILE>(g, gam, dtd, hd, d, blk, i, j, k, lane, p32b, ld, s_sig, s_abn, s_dnb, wp, wn, wc);
     // hybrid order before the transverse corrections
     // (hy_uhd_dataReconstOneStep.F90:934-999): where the flow compresses, a
     // direction whose states fail the Rankine-Hugoniot check falls back to
@@ -816,6 +842,40 @@ k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __rest
     if (kp.cflc && i >= LO && i <= HI && j >= LO && j <= HI && k >= LO && k <= HI)
         kp.cflc[((size_t)blk * 3 + d) * (GB_NXB * GB_NXB * GB_NXB) + (i - LO) + GB_NXB * ((j - LO) + GB_NXB * (k - LO))] =
             (unsigned char)code;
+    if (MHD) ((T*)kp.ecc)[((size_t)cb * 3 + d) * NRC + cell] = ecc_of(wp, wn);
+}
+
+// MINB: resident CTAs per SM the register allocation must allow (1 = no
+// bound); the autotuner chooses between the unbounded kernel and a bound
+// that trades spills for occupancy
+template <typename T, bool MHD, int TILE, int MINB>
+__global__ void __launch_bounds__(3 * TILE, MINB)
+k_recon(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* __restrict__ scr,
+        size_t scr_stride, const float* __restrict__ p32, size_t p32_stride, gb_status* st)
+{
+    __shared__ T s_sig[3][NP][TILE];
+    __shared__ T s_abn[3][NP][TILE];
+    __shared__ T s_dnb[3][TILE];
+    const int lane = threadIdx.x % TILE;
+    const int d = threadIdx.x / TILE;
+    const int cb = blockIdx.y;
+    const int blk = list[cb];
+    const int cell = blockIdx.x * TILE + lane;
+    const bool active = cell < NRC;
+    const int cc = active ? cell : 0;
+    const int i = RLO + cc % RB, j = RLO + (cc / RB) % RB, k = RLO + cc / (RB * RB);
+    T gam, dtd[3], hd[3];
+    recon_consts<T>(g, kp, blk, gam, dtd, hd);
+    const float* p32b = p32 + (size_t)cb * p32_stride;
+    int off[NP];
+    rot_offsets<T, MHD>(g, d, off);
+    const int stride = d == 0 ? 1 : (d == 1 ? GB_N : GB_N * GB_N);
+    const int c0 = gb_cidx(i, j, k);
+    auto ld = [&](int m, T* w) { load_rot<T, MHD>(g, blk, c0 + (m - 2) * stride, p32b, off, w); };
+    T wp[NP], wn[NP];
+    recon_item<T, MHD, TILE>(g, kp, cb, blk, d, lane, cell, cc, active, i, j, k, gam, dtd, hd, p32b, ld, s_sig, s_abn,
+                             s_dnb, st, wp, wn);
+    if (!active) return;
     T* out = scr + (size_t)cb * scr_stride;
     const int us[NP] = {0, rot_slot_rt<1>(d), rot_slot_rt<2>(d), rot_slot_rt<3>(d), 4,
                         rot_slot_rt<5>(d), rot_slot_rt<6>(d), rot_slot_rt<7>(d)};
@@ -1022,35 +1082,17 @@ __device__ __forceinline__ int rc_index(int i, int j, int k)
 }
 
 // ---------------------------------------------------------------- k_flux
-template <typename T, bool MHD, int D>
-__device__ __forceinline__ void flux_face(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* __restrict__ rscr,
-       size_t rstride, T* __restrict__ fscr, size_t fstride, const float* __restrict__ p32, size_t p32_stride)
+// The flux at one face of direction D from the left cell's + state wl and
+// the right cell's - state wr (unrotated; the normal field bnf from the
+// face): HLLC / HLLD, the rho e_int flux upwinded by the mass flux, and
+// artificial viscosity from the cell values U(role, ci) of the two cells
+// (cell indices cil, cir). out is unrotated.
+template <typename T, bool MHD, int D, typename UL>
+__device__ __forceinline__ void face_flux_core(const hydro_kparams& kp, const T* wl, const T* wr, T bnf, const UL& U,
+                                               int cil, int cir, T* out, T& feint, T& un)
 {
     constexpr int d = D;
-    const int cb = blockIdx.z;
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= NFC) return;
-    const int blk = list[cb];
-    int I[3];
-    flux_coords(d, f, I);
-    int Il[3] = {I[0], I[1], I[2]};
-    Il[d] -= 1;
-    const T* rs = rscr + (size_t)cb * rstride;
-    const int cl = rc_index(Il[0], Il[1], Il[2]), cr = rc_index(I[0], I[1], I[2]);
-    T wl[NP], wr[NP];
-#pragma unroll
-    for (int v = 0; v < NP; ++v) {
-        // the normal field (v = 5 + d) comes from the face below; hydro has
-        // no field: those state planes are not written
-        if (v == 5 + d || (!MHD && v >= 5)) {
-            wl[v] = (T)0;
-            wr[v] = (T)0;
-            continue;
-        }
-        wl[v] = rs[((size_t)(0 * 3 + d) * NP + v) * NRC + cl];
-        wr[v] = rs[((size_t)(1 * 3 + d) * NP + v) * NRC + cr];
-    }
-    T Lr[NP], Rr[NP], Fr[NP], un;
+    T Lr[NP], Rr[NP], Fr[NP];
 #pragma unroll
     for (int s = 0; s < NP; ++s) {
         Lr[s] = wl[rot_slot(d, s)];
@@ -1058,31 +1100,18 @@ __device__ __forceinline__ void flux_face(gb_dev_grid g, hydro_kparams kp, const
     }
     const T gam = std::is_same<T, float>::value ? (T)kp.gammaf : (T)kp.gamma;
     if (MHD) {
-        T bnf = face_b<T>(g, d, blk, gb_fidx(d, I[0], I[1], I[2]), p32 + (size_t)cb * p32_stride);
         Lr[5] = bnf;
         Rr[5] = bnf;
         hlld<T>(gam, Lr, Rr, Fr, &un);
     } else {
         hllc<T>(gam, Lr, Rr, Fr, &un);
     }
-    T out[NP];
 #pragma unroll
     for (int s = 0; s < NP; ++s) out[rot_slot(d, s)] = Fr[s];
     const T gm1 = gam - (T)1;
     T eL = Lr[4] / (gm1 * Lr[0]), eR = Rr[4] / (gm1 * Rr[0]);
-    T feint = Fr[0] * (Fr[0] >= (T)0 ? eL : eR);
+    feint = Fr[0] * (Fr[0] >= (T)0 ? eL : eR);
     if (kp.use_avisc) {
-        const int cil = gb_cidx(Il[0], Il[1], Il[2]), cir = gb_cidx(I[0], I[1], I[2]);
-        const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
-        const float* pb = p32 + (size_t)cb * p32_stride;
-        auto U = [&](int role, int ci) -> T {
-            if constexpr (std::is_same<T, float>::value) {
-                const int v = role == GB_EINT ? 8 : (role >= GB_MAGX ? 5 + (role - GB_MAGX) : role);
-                return pb[(size_t)v * GB_N3 + ci];
-            } else {
-                return (T)base[(int64_t)g.slot[role] * GB_N3 + ci];
-            }
-        };
         T dv = U(GB_VELX + d, cir) - U(GB_VELX + d, cil);
         T vis = (std::is_same<T, float>::value ? (T)kp.cviscf : (T)kp.cvisc) * fmax(-dv, (T)0);
         if (vis > (T)0) {
@@ -1115,13 +1144,65 @@ __device__ __forceinline__ void flux_face(gb_dev_grid g, hydro_kparams kp, const
             feint = feint + vis * (el - er);
         }
     }
-    T* fs = fscr + (size_t)cb * fstride + (size_t)d * NFLX * NFC;
-    // the normal field's flux (and hydro's field fluxes) are never read: not stored
+}
+
+// the face's fluxes into the flux scratch of its block (f: index in the
+// direction's flux box); the normal field's flux (and hydro's field
+// fluxes) are never read: not stored
+template <typename T, bool MHD, int D>
+__device__ __forceinline__ void face_flux_store(T* fs, int f, const T* out, T feint, T un)
+{
+    constexpr int d = D;
 #pragma unroll
     for (int s = 0; s < NP; ++s)
         if (s != 5 + d && (MHD || s < 5)) fs[(size_t)s * NFC + f] = out[s];
     fs[(size_t)8 * NFC + f] = feint;
     fs[(size_t)9 * NFC + f] = un;
+}
+
+template <typename T, bool MHD, int D>
+__device__ __forceinline__ void flux_face(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, const T* __restrict__ rscr,
+       size_t rstride, T* __restrict__ fscr, size_t fstride, const float* __restrict__ p32, size_t p32_stride)
+{
+    constexpr int d = D;
+    const int cb = blockIdx.z;
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= NFC) return;
+    const int blk = list[cb];
+    int I[3];
+    flux_coords(d, f, I);
+    int Il[3] = {I[0], I[1], I[2]};
+    Il[d] -= 1;
+    const T* rs = rscr + (size_t)cb * rstride;
+    const int cl = rc_index(Il[0], Il[1], Il[2]), cr = rc_index(I[0], I[1], I[2]);
+    T wl[NP], wr[NP];
+#pragma unroll
+    for (int v = 0; v < NP; ++v) {
+        // the normal field (v = 5 + d) comes from the face below; hydro has
+        // no field: those state planes are not written
+        if (v == 5 + d || (!MHD && v >= 5)) {
+            wl[v] = (T)0;
+            wr[v] = (T)0;
+            continue;
+        }
+        wl[v] = rs[((size_t)(0 * 3 + d) * NP + v) * NRC + cl];
+        wr[v] = rs[((size_t)(1 * 3 + d) * NP + v) * NRC + cr];
+    }
+    const float* pb = p32 + (size_t)cb * p32_stride;
+    const T bnf = MHD ? face_b<T>(g, d, blk, gb_fidx(d, I[0], I[1], I[2]), pb) : (T)0;
+    const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
+    auto U = [&](int role, int ci) -> T {
+        if constexpr (std::is_same<T, float>::value) {
+            const int v = role == GB_EINT ? 8 : (role >= GB_MAGX ? 5 + (role - GB_MAGX) : role);
+            return pb[(size_t)v * GB_N3 + ci];
+        } else {
+            return (T)base[(int64_t)g.slot[role] * GB_N3 + ci];
+        }
+    };
+    T out[NP], feint, un;
+    face_flux_core<T, MHD, D>(kp, wl, wr, bnf, U, gb_cidx(Il[0], Il[1], Il[2]), gb_cidx(I[0], I[1], I[2]), out, feint,
+                              un);
+    face_flux_store<T, MHD, D>(fscr + (size_t)cb * fstride + (size_t)d * NFLX * NFC, f, out, feint, un);
 }
 
 // mixed path: eight resident CTAs per SM (64 registers, no spills) to hide
@@ -1171,23 +1252,18 @@ __device__ __forceinline__ void emf_plane(const int* __restrict__ list, const T*
     const int C = LO + blockIdx.x;
     int t[3];
     auto at = [&](int av, int bv, int cv) { t[a] = av; t[b] = bv; t[c] = cv; };
-    const T* rs = rscr + (size_t)cb * rstride;
-    // the cell-centred reference field at the fluxes' time level t + dt/2:
-    // from the mean of the cell's two face states along c (time centred by
-    // the tracing and the other directions' transverse terms; v and B along
-    // a and b are tangential to c, so both states carry them), so that a
-    // plane-parallel flow gets the 1-D Riemann flux at every edge
-    // (Gardiner & Stone 2005 sec. 3). x runs fastest across the threads
-    // where the plane has an x axis (a for c = 2, b for c = 1).
+    // the cell-centred reference field at the fluxes' time level t + dt/2,
+    // -(v x B)_c of the mean of the cell's two face states along c (time
+    // centred by the tracing and the other directions' transverse terms; v
+    // and B along a and b are tangential to c), written by the
+    // reconstruction: a plane-parallel flow then gets the 1-D Riemann flux
+    // at every edge (Gardiner & Stone 2005 sec. 3). x runs fastest across
+    // the threads where the plane has an x axis (a for c = 2, b for c = 1).
+    const T* es = rscr + (size_t)cb * rstride + (size_t)c * NRC;
     for (int q = threadIdx.x; q < EMF_CELLS; q += EMF_THREADS) {
         const int qa = c == 1 ? q / RB : q % RB, qb = c == 1 ? q % RB : q / RB;
         at(RLO + qa, RLO + qb, C);
-        const int rc = rc_index(t[0], t[1], t[2]);
-        auto sv = [&](int var) -> R {
-            return (R)0.5 * (rs[((size_t)(0 * 3 + c) * NP + var) * NRC + rc] + rs[((size_t)(1 * 3 + c) * NP + var) * NRC + rc]);
-        };
-        const R va = sv(1 + a), vb = sv(1 + b), Ba = sv(5 + a), Bb = sv(5 + b);
-        s_ecc[qa + RB * qb] = vb * Ba - va * Bb;
+        s_ecc[qa + RB * qb] = es[rc_index(t[0], t[1], t[2])];
     }
     __syncthreads();
     const int q = threadIdx.x;

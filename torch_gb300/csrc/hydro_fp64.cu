@@ -4,6 +4,8 @@
 
 size_t gb_hydro_scratch_bytes_fp64() { return gbh::scratch_layout<double>::bytes; }
 
+int gb_fused_attr_fp64() { return gbh::fused_set_attr<double>(); }
+
 int gb_hydro_chunk_fp64(const gbh::hydro_kparams& kp, int mhd, int cool, int nblk, const int* list,
                         void* scratch, gb_status* st, cudaStream_t s, cudaEvent_t ev_put,
                          const sur_feat_out* sf, cudaEvent_t ev_wait)

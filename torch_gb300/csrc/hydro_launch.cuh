@@ -6,6 +6,7 @@
 #include "gb_prof.h"
 #include "gb_state.h"
 #include "hydro_dev.cuh"
+#include "hydro_fused.cuh"
 
 namespace gbh {
 
@@ -30,6 +31,48 @@ void launch_recon(int tile, dim3 rg, cudaStream_t s, const gb_dev_grid& g, const
     }
 }
 
+// the fused kernels' dynamic shared memory limit (both physics)
+template <typename T>
+int fused_set_attr()
+{
+    constexpr bool TMA = std::is_same<T, float>::value;
+    const int bytes = (int)fused_layout<T, TMA>::bytes;
+    if (gb_check(cudaFuncSetAttribute(k_recon_flux<T, true, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
+                 "fused kernel shared memory") ||
+        gb_check(cudaFuncSetAttribute(k_recon_flux<T, false, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
+                 "fused kernel shared memory"))
+        return GB_ERR_CUDA;
+    return GB_OK;
+}
+
+// reconstruction then fluxes: fused per block, or the two chunk kernels
+template <typename T, bool MHD>
+int recon_and_flux(int tile, dim3 rg, dim3 fg, cudaStream_t s, const gb_dev_grid& g, const hydro_kparams& kp, int nblk,
+                   const int* list, T* rscr, T* fscr, float* p32, gb_status* st)
+{
+    using SL = scratch_layout<T>;
+    if (gb_fused_step()) {
+        constexpr bool TMA = std::is_same<T, float>::value;
+        CUtensorMap tm;
+        memset(&tm, 0, sizeof tm);
+        if constexpr (TMA) {
+            if (gb_encode_p32_map(&tm, p32, nblk, SL::prim32)) return GB_ERR_CUDA;
+        }
+        gb_prof_begin(GBP_RECON, s);
+        k_recon_flux<T, MHD, TMA><<<nblk, FUSED_THREADS, fused_layout<T, TMA>::bytes, s>>>(g, kp, list, fscr, SL::flux,
+                                                                                        p32, SL::prim32, tm, st);
+        gb_prof_end(GBP_RECON, s);
+        return GB_OK;
+    }
+    gb_prof_begin(GBP_RECON, s);
+    launch_recon<T, MHD>(tile, rg, s, g, kp, list, rscr, p32, st);
+    gb_prof_end(GBP_RECON, s);
+    gb_prof_begin(GBP_FLUX, s);
+    k_flux<T, MHD><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);
+    gb_prof_end(GBP_FLUX, s);
+    return GB_OK;
+}
+
 // fine-side boundary fluxes into the flux registers (as soon as the fluxes
 // exist)
 template <typename T>
@@ -48,8 +91,8 @@ int launch_chunk(const hydro_kparams& kp_in, int mhd, int cool, int nblk, const 
                  const sur_feat_out* sf = nullptr, cudaEvent_t ev_wait = nullptr)
 {
     using SL = scratch_layout<T>;
-    // scratch of the chunk: [recon | flux | emf | faceb | prim32 | divu],
-    // each block-major
+    // scratch of the chunk: [recon | flux | emf | faceb | prim32 | divu |
+    // ecc], each block-major
     char* base = (char*)scratch;
     T* rscr = (T*)base;
     T* fscr = (T*)(base + (size_t)nblk * SL::recon * sizeof(T));
@@ -57,8 +100,10 @@ int launch_chunk(const hydro_kparams& kp_in, int mhd, int cool, int nblk, const 
     double* bscr = escr + (size_t)nblk * SL::emf;
     float* p32 = (float*)(bscr + (size_t)nblk * SL::fb);
     T* dscr = (T*)(p32 + (size_t)nblk * SL::prim32);
+    T* cscr = dscr + (size_t)nblk * SL::divu;
     hydro_kparams kp = kp_in;
     kp.divu = dscr;
+    kp.ecc = cscr;
     const gb_dev_grid& g = g_gb.grid;
     if constexpr (SL::prim32 > 0) {
         dim3 pg((GB_STEP_CELLS / 4 + (mhd ? GB_STEP_FACES_ALL : 0) + 127) / 128, nblk);
@@ -77,16 +122,11 @@ int launch_chunk(const hydro_kparams& kp_in, int mhd, int cool, int nblk, const 
     dim3 rg((NRC + tile - 1) / tile, nblk);
     dim3 fg((NFC + 127) / 128, 3, nblk);
     if (mhd) {
-        gb_prof_begin(GBP_RECON, s);
-        launch_recon<T, true>(tile, rg, s, g, kp, list, rscr, p32, st);
-        gb_prof_end(GBP_RECON, s);
-        gb_prof_begin(GBP_FLUX, s);
-        k_flux<T, true><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);
-        gb_prof_end(GBP_FLUX, s);
+        if (int rc = recon_and_flux<T, true>(tile, rg, fg, s, g, kp, nblk, list, rscr, fscr, p32, st)) return rc;
         put_fluxes<T>(kp, nblk, list, fscr, s);
         dim3 eg(GB_NXB, 3, nblk);
         gb_prof_begin(GBP_EMF, s);
-        k_emf<T><<<eg, EMF_THREADS, 0, s>>>(list, rscr, SL::recon, fscr, SL::flux, escr, SL::emf);
+        k_emf<T><<<eg, EMF_THREADS, 0, s>>>(list, cscr, SL::ecc, fscr, SL::flux, escr, SL::emf);
         if (kp.ec_reg)
             k_emf_put<<<dim3((NSURF + 127) / 128, nblk), 128, 0, s>>>(list, kp.ec_near, escr, SL::emf, kp.ec_reg);
         gb_prof_end(GBP_EMF, s);
@@ -108,12 +148,7 @@ int launch_chunk(const hydro_kparams& kp_in, int mhd, int cool, int nblk, const 
         k_faceb<<<bg, 128, 0, s>>>(g, kp, list, escr, SL::emf, bscr, SL::fb);
         gb_prof_end(GBP_FACEB, s);
     } else {
-        gb_prof_begin(GBP_RECON, s);
-        launch_recon<T, false>(tile, rg, s, g, kp, list, rscr, p32, st);
-        gb_prof_end(GBP_RECON, s);
-        gb_prof_begin(GBP_FLUX, s);
-        k_flux<T, false><<<fg, 128, 0, s>>>(g, kp, list, rscr, SL::recon, fscr, SL::flux, p32, SL::prim32);
-        gb_prof_end(GBP_FLUX, s);
+        if (int rc = recon_and_flux<T, false>(tile, rg, fg, s, g, kp, nblk, list, rscr, fscr, p32, st)) return rc;
         put_fluxes<T>(kp, nblk, list, fscr, s);
         if (ev_put) cudaEventRecord(ev_put, s);
         if (ev_wait) cudaStreamWaitEvent(s, ev_wait, 0);

@@ -35,7 +35,8 @@ N3 = NB ** 3
 FSZ = NB * NB * (NB + 1)
 
 ST_NAMES = {0: "ok", 1: "negative density", 2: "pressure floored", 3: "non-finite state",
-            4: "root finder not bracketed", 5: "root finder iteration cap", 6: "overheated (T > absTmax)"}
+            4: "root finder not bracketed", 5: "root finder iteration cap", 6: "overheated (T > absTmax)",
+            7: "copy wait timed out"}
 
 
 class GBError(RuntimeError):
@@ -116,6 +117,8 @@ _SIG = {
     "gb_set_chunk_blocks": (C.c_int, [C.c_int]),
     "gb_set_launch_config": (C.c_int, [C.c_int, C.c_int, C.c_int]),
     "gb_get_launch_config": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "gb_set_fused": (C.c_int, [C.c_int]),
+    "gb_get_fused": (C.c_int, []),
     "gb_set_chunk_streams": (C.c_int, [C.c_int]),
     "gb_get_chunk_streams": (C.c_int, []),
     "gb_step_graph": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -463,6 +466,15 @@ def get_launch_config() -> tuple:
     a, b, c = C.c_int(), C.c_int(), C.c_int()
     check(lib().gb_get_launch_config(C.byref(a), C.byref(b), C.byref(c)), "gb_get_launch_config")
     return a.value, b.value, c.value
+
+
+def set_fused(on: bool) -> None:
+    """Reconstruction and Riemann solve fused per block (gb_set_fused)."""
+    check(lib().gb_set_fused(int(bool(on))), "gb_set_fused")
+
+
+def get_fused() -> bool:
+    return bool(lib().gb_get_fused())
 
 
 def set_chunk_streams(n: int) -> None:
