@@ -148,13 +148,17 @@ def test_autotuner_picks_a_candidate_and_restores_state(gb, tmp_path, monkeypatc
         assert (r["chunk"], r["tile"]) in {(8, 32), (8, 64), (16, 32), (16, 64)} and r["occ"] in (0, 1, 2)
         assert gb.get_launch_config() == (r["chunk"], r["tile"], r["occ"])
         assert gb.get_chunk_streams() == r["streams"]
-        assert len(r["trials"]) == 24 and not r["cached"]
+        # 2 chunks x 2 tiles x 3 bounds x 2 stream counts, and the fused
+        # kernel once per chunk size and stream count
+        assert len(r["trials"]) == 24 + 4 and not r["cached"]
+        assert gb.get_fused() == bool(r["fused"])
         assert torch.equal(g.u, before)
         r2 = autotune.tune(g, cool=True, chunks=(8, 16), tiles=(32, 64), steps=1)
         assert r2["cached"] and (r2["chunk"], r2["tile"], r2["occ"]) == (r["chunk"], r["tile"], r["occ"])
     finally:
         gb.set_launch_config(16, 32)
         gb.set_chunk_streams(1)
+        gb.set_fused(False)
 
 
 @pytest.mark.parametrize("streams", [1, 2])
