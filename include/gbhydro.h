@@ -189,6 +189,13 @@ int gb_hydro_unsplit_noalloc(int blockCount, const int* blockList_dev, double dt
  * after the caller restored an earlier state). */
 int gb_cfl_codes_reset(void* stream);
 
+/* Copy the registered grid's CFL codes (maxblocks x 3 x 16^3 bytes, an
+ * opaque per-cell record) to or from a caller buffer in host or device
+ * memory, stream-ordered: what a checkpoint keeps so that a restart takes
+ * the same next dt as the uninterrupted run. nbytes must equal that size. */
+int gb_cfl_codes_save(void* dst, size_t nbytes, void* stream);
+int gb_cfl_codes_load(const void* src, size_t nbytes, void* stream);
+
 /* Blocks per launch chunk of the hydro kernels (scratch = chunk x per-block
  * scratch; the autotuner picks it). Default 16. */
 int gb_set_chunk_blocks(int n);
@@ -275,6 +282,16 @@ int gb_heat(int blockCount, const int* blockList_dev, double dt, double time,
 int gb_cool_cells(int64_t n, const double* dens, double* ei, double* temp, double* tdust,
                   const double* xhp, const double* phhe, const double* gflux, double dt,
                   gb_status* st_dev, void* stream);
+
+/* Formulation of the rate function (de/dt) that gb_cool_cells integrates:
+ * 0 (default) = heatCool.F90's terms as written (a pow per power law),
+ * 1 = the same terms with the transcendentals shared (one ln T and one
+ * sqrt T per evaluation, x^a as exp(a ln x), the column density and the
+ * FUV field's logarithm from per-cell constants). Form 1 is what the mixed
+ * hydro path's fused cooling epilogue always uses; the FP64 path's
+ * epilogue and gb_heat always use form 0. No counterpart in the
+ * reference's interface. */
+int gb_set_rate_form(int form);
 
 /* ---------------------------------------------------------------- step */
 /* One full step over the registered grid as FLASH's Driver_evolveFlash

@@ -53,6 +53,48 @@ def test_cool_cells_match_oracle(gb, oracle, dt):
     assert np.all(np.abs(td_g - td_o)[ok] <= 1e-3 * td_o[ok] + 1e-9)
 
 
+@pytest.mark.parametrize("dt,extra", [(1e10, False), (3e12, False), (3e12, True)])
+def test_restated_rates_match_oracle(gb, oracle, dt, extra):
+    """The rate function with shared transcendentals (one ln T and one
+    sqrt T per evaluation), which the mixed path's fused epilogue
+    integrates, against the oracle's reference terms: every cell within the
+    root finder's tolerance, as the reference formulation is. extra: a
+    per-cell ionisation fraction and external FUV flux (the photoelectric
+    term's other branch)."""
+    import torch
+    from torch_gb300 import tables
+    gb.init_cooling(gb.cool_params())
+    rho, ei, T, tdust, _ = _cells(20000, 11)
+    rng = np.random.default_rng(5)
+    xhp = 10 ** rng.uniform(-5, 0, rho.size) if extra else None
+    pefl = rng.uniform(0.0, 5.0, rho.size) * (rng.uniform(size=rho.size) < 0.7) if extra else None
+    p = oracle.cool_params()
+    t = oracle.table_from_ilog(*tables.read_compact())
+    e_o, T_o, td_o = ei.copy(), T.copy(), tdust.copy()
+    _, flags = oracle.radheat_cells(p, t, dt, rho.copy(), ei.copy(), e_o, T_o, td_o,
+                                    xhp=None if xhp is None else xhp.copy(),
+                                    pefl=None if pefl is None else pefl.copy(), threads=8)
+    dev = lambda a: None if a is None else torch.as_tensor(a.copy(), device="cuda")
+    d_rho, d_ei, d_T, d_td = dev(rho), dev(ei), dev(T), dev(tdust)
+    st = gb.status_buffer()
+    gb.set_rate_form(1)
+    try:
+        gb.cool_cells(d_rho, d_ei, d_T, d_td, dt, xhp=dev(xhp), gflux=dev(pefl), status=st)
+        torch.cuda.synchronize()
+    finally:
+        gb.set_rate_form(0)
+    T_g, td_g = d_T.cpu().numpy(), d_td.cpu().numpy()
+    ok = (flags & (4 | 8)) == 0
+    tolT = np.maximum(1.0, 1e-6 * T_o) * 2.0 + 1e-9 * T_o
+    bad = ok & (np.abs(T_g - T_o) > tolT)
+    assert bad.sum() == 0, (bad.sum(), np.abs(T_g - T_o)[ok].max())
+    rel = np.abs(T_g - T_o) / T_o
+    assert np.median(rel[ok]) < 1e-7
+    assert np.all(np.abs(td_g - td_o)[ok] <= 1e-3 * td_o[ok] + 1e-9)
+    with pytest.raises(Exception):
+        gb.set_rate_form(2)
+
+
 def test_heat_on_grid_matches_oracle(gb, oracle):
     """gb_heat over registered blocks (RadHeat's block loop) equals the
     per-cell oracle on the same interior cells."""

@@ -284,6 +284,33 @@ extern "C" int gb_cfl_codes_reset(void* stream)
                : GB_OK;
 }
 
+// copies the registered grid's CFL codes between the library and a caller
+// buffer (host or device memory, cudaMemcpyDefault)
+static int cfl_codes_copy(void* dst, const void* src, size_t nbytes, void* stream, const char* who)
+{
+    if (!g_gb.grid_ok) {
+        gb_set_error("%s: call gb_register_grid first", who);
+        return GB_ERR_NOT_INIT;
+    }
+    const size_t need = (size_t)g_gb.grid.maxblocks * 3 * GB_NXB * GB_NXB * GB_NXB;
+    if (nbytes != need || !dst || !src) {
+        gb_set_error("%s: %zu bytes given, the registered grid's codes take %zu", who, nbytes, need);
+        return GB_ERR_ARG;
+    }
+    return gb_check(cudaMemcpyAsync(dst, src, nbytes, cudaMemcpyDefault, (cudaStream_t)stream), who) ? GB_ERR_CUDA
+                                                                                                      : GB_OK;
+}
+
+extern "C" int gb_cfl_codes_save(void* dst, size_t nbytes, void* stream)
+{
+    return cfl_codes_copy(dst, g_gb.d_cflc, nbytes, stream, "gb_cfl_codes_save");
+}
+
+extern "C" int gb_cfl_codes_load(const void* src, size_t nbytes, void* stream)
+{
+    return cfl_codes_copy(g_gb.d_cflc, src, nbytes, stream, "gb_cfl_codes_load");
+}
+
 extern "C" int gb_hydro_init(const gb_hydro_params* p)
 {
     if (!p || !(p->gamma > 1.0) || p->precision < 0 || p->precision > 1) {

@@ -142,7 +142,9 @@ __global__ void k_heat_blocks(gb_dev_grid g, gb_cool_ctx c, const int* __restric
     }
 }
 
-// The same per-cell solve on plain CGS arrays.
+// The same per-cell solve on plain CGS arrays (FR: the restated rates the
+// mixed hydro path's fused epilogue uses).
+template <bool FR>
 __global__ void k_cool_cells(gb_cool_ctx c, int64_t n, const double* __restrict__ dens,
                              double* ei_a, double* temp_a, double* tdust_a,
                              const double* __restrict__ xhp, const double* __restrict__ phhe,
@@ -164,7 +166,7 @@ __global__ void k_cool_cells(gb_cool_ctx c, int64_t n, const double* __restrict_
         gb_fail(st, GB_ST_NONFINITE, -1, (int)(idx & 0x7fffffff), 0, 0, temp);
         return;
     }
-    heating_and_cooling(c, v, &ei, dt, &temp, &d);
+    heating_and_cooling<FR>(c, v, &ei, dt, &temp, &d);
     bool clamped = false;
     if (temp > c.p.absTmax) {
         ei = c.p.absTmax * v.TtoEI;
@@ -187,6 +189,17 @@ __global__ void k_cool_cells(gb_cool_ctx c, int64_t n, const double* __restrict_
 }  // namespace
 
 static double g_brent_tol_K = 1.0;
+static int g_rate_form = 0;
+
+extern "C" int gb_set_rate_form(int form)
+{
+    if (form != 0 && form != 1) {
+        gb_set_error("gb_set_rate_form: form %d is neither 0 nor 1", form);
+        return GB_ERR_ARG;
+    }
+    g_rate_form = form;
+    return GB_OK;
+}
 
 extern "C" int gb_set_brent_tolerance(double kelvin)
 {
@@ -282,8 +295,12 @@ extern "C" int gb_cool_cells(int64_t n, const double* dens, double* ei, double* 
     if (n == 0) return GB_OK;
     int tpb = 128;
     int64_t nb = (n + tpb - 1) / tpb;
-    k_cool_cells<<<(unsigned)nb, tpb, 0, (cudaStream_t)stream>>>(g_gb.cool, n, dens, ei, temp, tdust,
-                                                                  xhp, phhe, gflux, dt, st);
+    if (g_rate_form)
+        k_cool_cells<true><<<(unsigned)nb, tpb, 0, (cudaStream_t)stream>>>(g_gb.cool, n, dens, ei, temp, tdust,
+                                                                        xhp, phhe, gflux, dt, st);
+    else
+        k_cool_cells<false><<<(unsigned)nb, tpb, 0, (cudaStream_t)stream>>>(g_gb.cool, n, dens, ei, temp, tdust,
+                                                                         xhp, phhe, gflux, dt, st);
     return gb_check(cudaGetLastError(), "k_cool_cells") ? GB_ERR_CUDA : GB_OK;
 }
 

@@ -318,21 +318,32 @@ static __device__ double dei_parts(const gb_cool_ctx& c, const gb_cool_vars& v, 
     return eplus + PeHeat - emin - cool_pw - cool_dg + floor_;
 }
 
+template <bool FR = false>
 static __device__ double get_dust_temperature(const gb_cool_params& p, double tdust_in, double temp_in,
                                        double nden, double phen_heat, gb_cool_diag* d)
 {
-    // heatCool.F90:703-884
+    // heatCool.F90:703-884; the gas temperature is fixed during the Newton
+    // iterations, so its collision factor and square root are formed once
+    // (the same values). FR: T_dust^6 as a product instead of pow.
     const double tol = 1.e-4, smallt = .1;
     double error = 10. * tol;
     double tdust = tdust_in;
     if (tdust < p.absTmin) tdust = p.absTmin;
     double tg = (temp_in < p.absTmin) ? p.absTmin : temp_in;
+    const double acoll = 3.8 * nden * (1.0 - 0.8 * exp(-75.0 / tg)), sq = sqrt(tg);
     int l = 1;
     while ((l <= 100) && (error > tol)) {
-        double lambda_dust = 6.8 * pow(tdust, 6.0);
-        double coll = 3.8 * nden * (1.0 - 0.8 * exp(-75.0 / tg)) * (tg - tdust) * sqrt(tg);
+        double t6;
+        if (FR) {
+            const double t2 = tdust * tdust;
+            t6 = t2 * t2 * t2;
+        } else {
+            t6 = pow(tdust, 6.0);
+        }
+        double lambda_dust = 6.8 * t6;
+        double coll = acoll * (tg - tdust) * sq;
         double eqfunc = phen_heat + coll - lambda_dust;
-        double det = -(6.0 * lambda_dust / tdust) - 3.8 * nden * (1.0 - 0.8 * exp(-75.0 / tg)) * sqrt(tg);
+        double det = -(6.0 * lambda_dust / tdust) - acoll * sq;
         double tnew = tdust - eqfunc / det;
         error = fabs(tnew - tdust) / tdust;
         tdust = tnew;
@@ -347,6 +358,7 @@ static __device__ double get_dust_temperature(const gb_cool_params& p, double td
     return tdust;
 }
 
+template <bool FR = false>
 static __device__ void dust_update(const gb_cool_ctx& c, gb_cool_vars& v, double temp, gb_cool_diag* d)
 {
     // heatCool.F90:430-443
@@ -358,24 +370,189 @@ static __device__ void dust_update(const gb_cool_ctx& c, gb_cool_vars& v, double
     cr = cr * v.rho;
     dust_heat = dust_heat + cr;
     dust_heat = dust_heat / (v.ndens * 1e-33);
-    v.tdust = get_dust_temperature(p, v.tdust, temp, v.ndens, dust_heat, d);
+    v.tdust = get_dust_temperature<FR>(p, v.tdust, temp, v.ndens, dust_heat, d);
 }
 
-__device__ __forceinline__ double one_step(const gb_cool_ctx& c, const gb_cool_vars& v,
+// ---- dei_dt restated for the mixed path (FR): the same rate terms with
+// the transcendentals shared. Per evaluation one ln T and one sqrt(T);
+// every power x^a becomes exp(a ln x); the column density (Jeans length
+// times n, proportional to sqrt(T)) and the FUV field's logarithm (the
+// shielding exponent when no external flux is given) come from per-cell
+// constants. Algebraically the reference's rates; they round differently
+// by a few ulp, which moves the implicit solve by far less than its
+// tolerance.
+struct fr_consts {
+    double kJ;     // column density = kJ sqrt(T)
+    double lnK;    // ln(column / crIonNH) - ln(T) / 2
+    double lnG0;   // ln(Gzero strat) (used when Gflux == 0)
+    double lnxn;   // ln(x_l n): the photoelectric grain-charging denominator
+    double rn;     // rho / n
+};
+
+__device__ __forceinline__ fr_consts make_fr(const gb_cool_params& p, const gb_cool_vars& v)
+{
+    const double pi = 3.1415926535897932384, newton = 6.6725985e-8;
+    fr_consts f;
+    f.rn = v.rho / v.ndens;
+    f.kJ = sqrt(5. / 3. * pi * p.boltz / v.ndens / newton) / f.rn * v.ndens;
+    f.lnK = log(f.kJ) - log(p.crIonNH);
+    f.lnG0 = log(p.Gzero * v.strat_factor);
+    const double xl = (v.xHp == 0.0) ? 1e-8 : v.xHp;
+    f.lnxn = log(xl * v.ndens);
+    return f;
+}
+
+// radloss (heatCool.F90:1590-1667) from ln T and sqrt(T)
+__device__ __forceinline__ double radloss_fr(double T, double lnT, double sqT)
+{
+    double radia;
+    if (T >= 1.70e4) {
+        if (T >= 5.62e5) {
+            if (T >= 2.75e6) {
+                if (T >= 3.16e7) radia = 3.090e-27 * sqT;
+                else radia = 5.188e-21 * exp(-0.33 * lnT);
+            } else {
+                if (T >= 1.78e6) radia = 3.890e-4 * exp(-2.95 * lnT);
+                else radia = 1.3e-22 * exp(0.01 * (lnT - 11.918390573078392));  // (T / 1.5e5)^0.01
+            }
+        } else {
+            if (T >= 7.94e4) {
+                if (T >= 2.51e5) radia = 3.98e-11 / (T * T);
+                else radia = 6.31e-22 * exp(0.01 * (lnT - 13.815510557964274));  // (T / 1e6)^0.01
+            } else {
+                if (T >= 3.98e4) radia = 1.e-31 * (T * T);
+                else radia = 1.479e-21 * exp(-0.216 * lnT);
+            }
+        }
+    } else {
+        if (T >= 1.e3) {
+            if (T >= 6.31e3) {
+                if (T >= 1.0e4) radia = 7.63e-81 * exp(13.8 * lnT);
+                else radia = 3.13e-27 * exp(0.396 * lnT);
+            } else {
+                if (T >= 3.16e3) radia = 2.64e-26 * exp(0.152 * lnT);
+                else radia = 5.28e-27 * exp(0.352 * lnT);
+            }
+        } else {
+            if (T >= 3.98e1) {
+                if (T >= 2.00e2) radia = 3.06e-27 * exp(0.431 * lnT);
+                else radia = 1.52e-28 * exp(0.997 * lnT);
+            } else {
+                if (T >= 2.51e1) radia = 2.39e-29 * (T * sqT);
+                else radia = 1.095e-32 * exp(3.885 * lnT);
+            }
+        }
+    }
+    return radia;
+}
+
+__device__ __forceinline__ double ramp(double x, double ll, double ul)
+{
+    const double ll10 = ll + 0.1 * ll, ul10 = ul - 0.1 * ul;
+    if (x >= ul10) return lin_interp(ul10, 1.0, ul, 0.0, x);
+    if (x <= ll10) return lin_interp(ll, 0.0, ll10, 1.0, x);
+    return 1.0;
+}
+
+static __device__ double dei_dt_fr(const gb_cool_ctx& c, const gb_cool_vars& v, const fr_consts& f, double floor_,
+                                   double ei_in)
+{
+    const gb_cool_params& p = c.p;
+    double T = ei_in / v.TtoEI;
+    if (T < 0.0) T = 1.0;
+    const double lnT = log(T), sqT = sqrt(T);
+    const double ncol = f.kJ * sqT;
+    const double Av = ncol * 0.01 / 1.87e21;
+    // CR heating (heatCool.F90:890-964)
+    double eplus = 0.0;
+    if ((T <= p.theatmax) && (T >= p.theatmin)) {
+        if (p.use_cr_heating) {
+            if (p.crIonNH == 1.0 && p.crIonExp == 1.0) {
+                eplus = v.strat_factor * p.crIonRate * p.crIonEnergy / f.rn;
+            } else {
+                const double L = 0.5 * lnT + f.lnK;  // ln(column / NH)
+                const double pw = L > 0.0 ? exp(-p.crIonExp * L) : 1.0;
+                eplus = v.strat_factor * (p.crIonRate * p.crIonEnergy * pw) / f.rn;
+            }
+        }
+        eplus = eplus * ramp(T, p.theatmin, p.theatmax);
+    }
+    // photoelectric heating, WD01 (:970-1110), with the shielded FUV field
+    const double fext = exp(-3.5 * Av);
+    const double fuv = v.Gflux + p.Gzero * fext * v.strat_factor;
+    double PeHeat = 0.0;
+    if (p.pe_recipe != 0) {
+        double dh;
+        pe_heating(p, fuv, v.xHp, v.ndens, T, v.rho, &PeHeat, &dh);
+    } else if ((T <= fmn(p.theatmax, p.dust_sputter_temp)) && (T >= p.theatmin)) {
+        const double C0 = 7.64, C1 = 4.52, C2 = 0.04371, C3 = 0.00557, C4 = 0.132, C5 = 0.452, C6 = 0.675;
+        double den = 1.0;
+        if (fuv > 0.0) {
+            const double lnfuv = v.Gflux == 0.0 ? f.lnG0 - 3.5 * Av : log(fuv);
+            const double lnGf = lnfuv + 0.5 * lnT - f.lnxn;
+            den = 1.0 + (C2 * exp(C5 * lnGf)) * (1.0 + C3 * exp(C6 * lnGf));
+        }
+        const double eff = (C0 + C1 * exp(C4 * lnT)) / den;
+        PeHeat = 1e-26 * eff * fuv / f.rn;
+        PeHeat = PeHeat * ramp(T, p.theatmin, fmn(p.theatmax, p.dust_sputter_temp));
+    }
+    eplus = eplus + v.ephen;
+    // atomic cooling (:1116-1200)
+    double emin = 0.0;
+    if ((T <= p.tradmax && T >= p.tradmin) && (v.ndens >= p.dradmin && v.ndens <= p.dradmax)) {
+        emin = radloss_fr(T, lnT, sqT);
+        if (v.xHp > 1e-2 && T < 1.2e4) {
+            double DG = lin_interp(1e-2, 1.0, 1e-1, 5.0, fmn(1e-1, v.xHp));
+            emin = emin * DG;
+            if (T > 1e4) {
+                double q = lin_interp(1e4, 1.0, 1.2e4, sqrt(DG), T);
+                emin = emin / (q * q);
+            }
+        } else if (v.xHp < 1e-2 && T < 1e4) {
+            double DG = lin_interp(1e-4, 0.35, 1e-2, 1.0, fmx(1e-4, v.xHp));
+            emin = emin * DG;
+            if (T > 9e3) emin = emin / lin_interp(9e3, 1.0, 1e4, DG, T);
+        }
+        emin = emin * ramp(T, p.tradmin, p.tradmax);
+        emin = emin * v.conf;
+    }
+    double cool_pw = 0.0, cool_dg = 0.0;
+    if (p.useDustCool) {
+        cool_pw = molecular_cooling(c, v.ndens, T, v.mu_mol);
+        if (T <= p.dust_sputter_temp) {
+            const double lambda_gd = 3.8e-33 * (v.ndens * v.ndens) * (1.0 - 0.8 * exp(-75.0 / T)) * (T - v.tdust) * sqT;
+            const double ul = p.dust_sputter_temp, ul10 = ul - 0.1 * ul;
+            cool_dg = lambda_gd / v.rho * (T >= ul10 ? lin_interp(ul10, 1.0, ul, 0.0, T) : 1.0);
+        }
+    }
+    return eplus + PeHeat - emin - cool_pw - cool_dg + floor_;
+}
+
+template <bool FR>
+__device__ __forceinline__ double rate(const gb_cool_ctx& c, const gb_cool_vars& v, const fr_consts& f,
+                                       double floor_, double y)
+{
+    if (FR) return dei_dt_fr(c, v, f, floor_, y);
+    return dei_dt(c, v, floor_, y);
+}
+
+template <bool FR = false>
+__device__ __forceinline__ double one_step(const gb_cool_ctx& c, const gb_cool_vars& v, const fr_consts& f,
                                            double floor_, double dx, double y, double yold)
 {
     // heatCool.F90:1928-1950
-    return y - dx * dei_dt(c, v, floor_, y) - yold;
+    return y - dx * rate<FR>(c, v, f, floor_, y) - yold;
 }
 
-static __device__ double zero(const gb_cool_ctx& c, const gb_cool_vars& v, double floor_, double a,
-                       double b, double a_old, double machep, double tt, double dt,
+template <bool FR = false>
+static __device__ double zero(const gb_cool_ctx& c, const gb_cool_vars& v, const fr_consts& f, double floor_,
+                       double a, double b, double a_old, double machep, double tt, double dt,
                        gb_cool_diag* d)
 {
     // heatCool.F90:1981-2197 (Brent)
     double sa = a, sb = b;
-    double fa = one_step(c, v, floor_, dt, sa, a_old);
-    double fb = one_step(c, v, floor_, dt, sb, a_old);
+    double fa = one_step<FR>(c, v, f, floor_, dt, sa, a_old);
+    double fb = one_step<FR>(c, v, f, floor_, dt, sb, a_old);
     double cc = sa, fc = fa, e = sb - sa, dd = e;
     int n_tries = 0;
     if ((fa > 0.0 && fb > 0.0) || (fa < 0.0 && fb < 0.0)) {
@@ -420,7 +597,7 @@ static __device__ double zero(const gb_cool_ctx& c, const gb_cool_vars& v, doubl
         if (tol < fabs(dd)) sb = sb + dd;
         else if (0.0 < m) sb = sb + tol;
         else sb = sb - tol;
-        fb = one_step(c, v, floor_, dt, sb, a_old);
+        fb = one_step<FR>(c, v, f, floor_, dt, sb, a_old);
         if ((0.0 < fb && 0.0 < fc) || (fb <= 0.0 && fc <= 0.0)) {
             cc = sa;
             fc = fa;
@@ -437,23 +614,24 @@ static __device__ double zero(const gb_cool_ctx& c, const gb_cool_vars& v, doubl
     return sb;
 }
 
-static __device__ int zbrac(const gb_cool_ctx& c, const gb_cool_vars& v, double floor_, double* x1,
-                     double* x2, double xold, double dt)
+template <bool FR = false>
+static __device__ int zbrac(const gb_cool_ctx& c, const gb_cool_vars& v, const fr_consts& f, double floor_,
+                     double* x1, double* x2, double xold, double dt)
 {
     // heatCool.F90:2294-2348
     const double FACTOR = 1.6;
-    double f1 = one_step(c, v, floor_, dt, *x1, xold);
-    double f2 = one_step(c, v, floor_, dt, *x2, xold);
+    double f1 = one_step<FR>(c, v, f, floor_, dt, *x1, xold);
+    double f2 = one_step<FR>(c, v, f, floor_, dt, *x2, xold);
     for (int j = 1; j <= 5000; ++j) {
         if (f1 * f2 < 0.0) return 1;
         if (fabs(f1) < fabs(f2)) {
             *x1 = *x1 + FACTOR * (*x1 - *x2);
             if (*x1 < 0.0) *x1 = v.TtoEI * 1.0;
-            f1 = one_step(c, v, floor_, dt, *x1, xold);
+            f1 = one_step<FR>(c, v, f, floor_, dt, *x1, xold);
         } else {
             *x2 = *x2 + FACTOR * (*x2 - *x1);
             if (*x2 < 0.0) *x2 = v.TtoEI * 1.0;
-            f2 = one_step(c, v, floor_, dt, *x2, xold);
+            f2 = one_step<FR>(c, v, f, floor_, dt, *x2, xold);
         }
     }
     return 0;
@@ -461,6 +639,7 @@ static __device__ int zbrac(const gb_cool_ctx& c, const gb_cool_vars& v, double 
 
 // heating_and_cooling, "Implicit" (default) or "Euler" branch, for one
 // cell. v must hold rho, Gflux, ephen, tdust, xHp, strat_factor, mu_mol.
+template <bool FR = false>
 static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v, double* ei_io,
                                     double timestep, double* temp_io, gb_cool_diag* d)
 {
@@ -472,11 +651,13 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
     v.TtoEI = ei / temp;
     v.conf = v.ndens * v.ndens / v.rho;
     double fl = cooling_floor(c, v);
+    fr_consts frc = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (FR) frc = make_fr(p, v);
     if (p.int_method == 1) {
         // Euler, heatCool.F90:119-214
         int ncount = 0;
         for (;;) {
-            double dei = dei_dt(c, v, fl, ei);
+            double dei = rate<FR>(c, v, frc, fl, ei);
             double dt1 = p.subfactor * ei / fmx(fabs(dei), 1e-50);
             double dt0 = fmn((timestep - total_time), dt1);
             ei = ei + dei * dt0;
@@ -491,13 +672,13 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
             ei = p.absTmin * v.TtoEI;
         }
         if (p.useDustCool && temp <= p.dust_sputter_temp)
-            v.tdust = get_dust_temperature(p, v.tdust, temp, v.ndens, 0.0, d);
+            v.tdust = get_dust_temperature<FR>(p, v.tdust, temp, v.ndens, 0.0, d);
     } else {
         // Implicit, heatCool.F90:216-514 (one pass: dt0 = timestep)
         while ((timestep - total_time) > (1e-6 * timestep)) {
             double eiolder = ei;
             double eiold = ei;
-            double dei = dei_dt(c, v, fl, eiold);
+            double dei = rate<FR>(c, v, frc, fl, eiold);
             double dt0 = timestep;
             eiold = eiolder + dei * dt0 * 1.0e-3;
             double ei1 = eiolder, ei2 = eiold;
@@ -505,23 +686,23 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
                 dt0 = (timestep - total_time);
                 ei = eiolder + dei * dt0;
                 temp = ei / v.TtoEI;
-                if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update(c, v, temp, d);
+                if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update<FR>(c, v, temp, d);
                 total_time = total_time + dt0;
                 continue;
             }
-            int found = zbrac(c, v, fl, &ei1, &ei2, eiolder, dt0);
+            int found = zbrac<FR>(c, v, frc, fl, &ei1, &ei2, eiolder, dt0);
             if (!found) d->bracket_fail = 1;
             if (ei1 < 0.0 || ei2 < 0.0) {
                 ei1 = fmx(ei1, v.TtoEI * 1.0);
                 ei2 = fmx(ei2, v.TtoEI * 1.0);
             }
             if (found)
-                ei = zero(c, v, fl, ei1, ei2, eiolder, 3e-16, fmx(v.TtoEI * c.brent_tol_K, eiold * err_tol), dt0, d);
+                ei = zero<FR>(c, v, frc, fl, ei1, ei2, eiolder, 3e-16, fmx(v.TtoEI * c.brent_tol_K, eiold * err_tol), dt0, d);
             else
-                ei = zero(c, v, fl, v.TtoEI * 1.0, v.TtoEI * 1.0e9, eiolder, 3e-16,
+                ei = zero<FR>(c, v, frc, fl, v.TtoEI * 1.0, v.TtoEI * 1.0e9, eiolder, 3e-16,
                           fmx(v.TtoEI * c.brent_tol_K, eiold * err_tol), dt0, d);
             temp = ei / v.TtoEI;
-            if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update(c, v, temp, d);
+            if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update<FR>(c, v, temp, d);
             total_time = total_time + dt0;
         }
         if (temp < p.absTmin) {

@@ -1724,7 +1724,10 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
         const bool good = gb_finite_pos(v.rho) && gb_finite_pos(eic) && gb_finite_pos(temp);
         bool clamped = false;
         if (good) {
-            gbcool::heating_and_cooling(cool, v, &eic, kp_dt(kp) * p.time_unit, &temp, &dg);
+            // the mixed path evaluates the rates with shared transcendentals
+            // (one ln T and one sqrt T per evaluation); the FP64 path keeps
+            // the reference's formulation
+            gbcool::heating_and_cooling<RCP>(cool, v, &eic, kp_dt(kp) * p.time_unit, &temp, &dg);
             if (temp > p.absTmax) {
                 eic = p.absTmax * v.TtoEI;
                 temp = p.absTmax;

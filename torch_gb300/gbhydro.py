@@ -137,6 +137,9 @@ _SIG = {
     "gb_compute_dt": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gb_cool_init": (C.c_int, [C.c_char_p, C.POINTER(CoolParams)]),
     "gb_set_brent_tolerance": (C.c_int, [C.c_double]),
+    "gb_set_rate_form": (C.c_int, [C.c_int]),
+    "gb_cfl_codes_save": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p]),
+    "gb_cfl_codes_load": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p]),
     "gb_heat": (C.c_int, [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_void_p]),
     "gb_cool_cells": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                 C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]),
@@ -454,6 +457,13 @@ def graph_info() -> tuple:
 def set_brent_tolerance(kelvin: float = 1.0) -> None:
     """Brent tolerance floor of the plain implicit step (1 K = heatCool.F90)."""
     check(lib().gb_set_brent_tolerance(float(kelvin)), "gb_set_brent_tolerance")
+
+
+def set_rate_form(form: int = 0) -> None:
+    """Rate formulation gb_cool_cells integrates: 0 = heatCool.F90's terms
+    as written, 1 = the same terms with shared transcendentals (the mixed
+    hydro path's fused epilogue)."""
+    check(lib().gb_set_rate_form(int(form)), "gb_set_rate_form")
 
 
 def set_launch_config(chunk_blocks: int, recon_tile: int, recon_occupancy: int = 0) -> None:
