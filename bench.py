@@ -161,13 +161,15 @@ def make_grid(G, tree, st, cooling=True):
 
 
 def run_path(G, g, precision, steps, warmup, cool=True, surrogate=False, profile=False, ncu_range=False,
-             graph=False, tune=False, tune_kw=None):
+             graph=False, tune=False, tune_kw=None, cool_mode=None):
     """Time `steps` steps of one path after `warmup` untimed ones. Eager: dt
     read back by the host each step, then the step's launches; graph: the
-    whole step (dt on the device) replayed as one CUDA graph."""
+    whole step (dt on the device) replayed as one CUDA graph. cool_mode
+    overrides the cooling mode surrogate implies (2: the plain integrator
+    on FP32 rates)."""
     import torch
     G.init_hydro(G.hydro_params(True, precision=precision))
-    G.set_cooling_mode(surrogate)
+    G.set_cooling_mode(surrogate if cool_mode is None else cool_mode)
     g.register()
     s = torch.cuda.current_stream()
     tuned = None
@@ -420,11 +422,13 @@ def l1(a, b, leaves, v):
     return float((x - y).abs().sum() / x.abs().sum())
 
 
-def accuracy_condition(l1_fast, l1_mixed, l1_fast_exact, roundoff, v_fast, sp_fast, v_mixed, sp_mixed, bound=1e-4):
+def accuracy_condition(l1_fast, l1_mixed, l1_fast_exact, roundoff, v_fast, sp_fast, v_mixed, sp_mixed, bound=1e-4,
+                       more=None):
     """Which path meets the metric's L1 <= 1e-4 (density and pressure after
     the run's steps): against the all-FP64 plain path, and for the learned
     path also against the backward-Euler root trajectory (the plain
-    integrator with Brent's tolerance floor at 1e-3 K)."""
+    integrator with Brent's tolerance floor at 1e-3 K). more: further
+    paths, name -> (l1, value, speedup), compared with the plain path."""
     ok = lambda d: d is not None and max(d.values()) <= bound
     paths = {
         "fast_vs_plain_fp64": {"l1": l1_fast, "meets": ok(l1_fast), "value": v_fast, "speedup_vs_plain_fp64": sp_fast},
@@ -433,6 +437,8 @@ def accuracy_condition(l1_fast, l1_mixed, l1_fast_exact, roundoff, v_fast, sp_fa
         "mixed_plain_cooling_vs_plain_fp64": {"l1": l1_mixed, "meets": ok(l1_mixed), "value": v_mixed,
                                               "speedup_vs_plain_fp64": sp_mixed},
     }
+    for name, (l1v, val, sp) in (more or {}).items():
+        paths[name + "_vs_plain_fp64"] = {"l1": l1v, "meets": ok(l1v), "value": val, "speedup_vs_plain_fp64": sp}
     meeting = [(k, v) for k, v in paths.items() if v["meets"] and k.endswith("vs_plain_fp64")]
     best = max(meeting, key=lambda kv: kv[1]["value"]) if meeting else None
     return {"bound": bound, "paths": paths,
@@ -540,7 +546,7 @@ def main():
     ap.add_argument("--save-weights", default=None)
     ap.add_argument("--ncu-range", action="store_true",
                     help="bracket the fast path's timed region with cudaProfilerStart/Stop")
-    ap.add_argument("--only", choices=["plain", "fast", "eager", "e2e"], default=None,
+    ap.add_argument("--only", choices=["plain", "fast", "eager", "e2e", "mixed", "mixed32"], default=None,
                     help="time one path alone and print a short line (for profiler captures)")
     ap.add_argument("--chunk", type=int, default=0, help="with --only: blocks per chunk (no autotuning)")
     ap.add_argument("--tile", type=int, default=32, help="with --chunk: reconstruction tile (32 or 64)")
@@ -609,10 +615,12 @@ def main():
                                   "value": zones * world / (ms * 1e-3), "unit": "zone-updates/s",
                                   "h2d_bytes_per_step": nbytes, "parts": parts}))
             return
-        prec, sur, graph = {"plain": (0, False, True), "fast": (1, True, True), "eager": (1, True, False)}[args.only]
+        prec, sur, graph, cm = {"plain": (0, False, True, None), "fast": (1, True, True, None),
+                                "eager": (1, True, False, None), "mixed": (1, False, True, None),
+                                "mixed32": (1, False, True, 2)}[args.only]
         ms, stt, info = run_path(G, g, prec, args.steps, args.warmup, surrogate=sur, graph=graph,
                                  tune=not args.no_tune and graph and not args.chunk, profile=not graph,
-                                 ncu_range=args.ncu_range)
+                                 ncu_range=args.ncu_range, cool_mode=cm)
         if rank == 0:
             print(json.dumps({"path": args.only, "workload": wl["name"], "ms_per_step": ms,
                               "value": zones * world / (ms * 1e-3), "unit": "zone-updates/s",
@@ -624,6 +632,7 @@ def main():
     g_plain = make_grid(G, tree, st)
     g_fast = make_grid(G, tree, st)
     g_mixed = make_grid(G, tree, st)
+    g_m32 = make_grid(G, tree, st)
     g_tight = make_grid(G, tree, st)
     g_eager = make_grid(G, tree, st)
     cs = None
@@ -648,6 +657,9 @@ def main():
             G.set_chunk_streams(ginfo["tuned"]["streams"])
             G.set_fused(bool(ginfo["tuned"].get("fused", 0)))
         ms_mixed, st_mixed, _ = run_path(G, g_mixed, 1, args.steps, args.warmup, graph=True)
+        # the same with the integrator's rate function in FP32 (Brent's
+        # iterates in FP64)
+        ms_m32, st_m32, _ = run_path(G, g_m32, 1, args.steps, args.warmup, graph=True, cool_mode=2)
     # diagnostic, untimed: the plain path's own drift under a one-ulp
     # nudge of the initial density (what an L1 error after 10 and 20 steps
     # can be read against)
@@ -661,12 +673,14 @@ def main():
     if world > 1:
         from torch_gb300.blocklist import max_over_ranks
         ms_plain, ms_fast = max_over_ranks(ms_plain), max_over_ranks(ms_fast)
+        ms_mixed, ms_m32 = max_over_ranks(ms_mixed), max_over_ranks(ms_m32)
     # accuracy of the fast path against the plain one after the same steps
     lv = torch.as_tensor(leaves.astype(np.int64), device="cuda")
     a, b, c, d = g_plain.u, g_fast.u, g_mixed.u, g_tight.u
     fields = (("dens", 0), ("pres", 4))
     l1_fast = {v: l1(a, b, lv, i) for v, i in fields}
     l1_mixed = {v: l1(a, c, lv, i) for v, i in fields}
+    l1_m32 = {v: l1(a, g_m32.u, lv, i) for v, i in fields}
     l1_tol = {v: l1(d, c, lv, i) for v, i in fields}
     l1_fast_exact = {v: l1(d, b, lv, i) for v, i in fields}
     sT = g_plain.slots["TEMP"]
@@ -764,11 +778,20 @@ def main():
                    "(the reference) vs at 1e-3 K, both on mixed hydro; l1_err_vs_backward_euler_root: fast "
                    "path vs the 1e-3 K run",
         "mixed_plain_cooling": {"value": zones * world / (ms_mixed * 1e-3), "ms_per_step": ms_mixed,
-                                "speedup_vs_plain_fp64": ms_plain / ms_mixed},
+                                "speedup_vs_plain_fp64": ms_plain / ms_mixed,
+                                "note": "mixed hydro; the plain integrator fused into the update, its rate "
+                                        "function in FP64 with shared transcendentals"},
+        "mixed_fp32_rates_cooling": {"value": zones * world / (ms_m32 * 1e-3), "ms_per_step": ms_m32,
+                                     "speedup_vs_plain_fp64": ms_plain / ms_m32, "l1_err_vs_fp64": l1_m32,
+                                     "note": "mixed hydro; the plain integrator fused into the update with its "
+                                             "rate function in FP32 (Brent's and the bracket search's iterates "
+                                             "and the residual in FP64)"},
         "roundoff_divergence_plain_fp64": roundoff,
         "accuracy_condition": accuracy_condition(l1_fast, l1_mixed, l1_fast_exact, roundoff,
                                                  zones * world / (ms_fast * 1e-3), ms_plain / ms_fast,
-                                                 zones * world / (ms_mixed * 1e-3), ms_plain / ms_mixed),
+                                                 zones * world / (ms_mixed * 1e-3), ms_plain / ms_mixed,
+                                                 more={"mixed_fp32_rates_cooling": (
+                                                     l1_m32, zones * world / (ms_m32 * 1e-3), ms_plain / ms_m32)}),
         "fast_eager": {"ms_per_step": ms_eager, "value": zones * world / (ms_eager * 1e-3),
                        "note": "the same fast path launched kernel by kernel with the host reading dt each step"},
         "launch_config": {k: ginfo["tuned"].get(k) for k in ("chunk", "tile", "occ", "streams", "fused", "cached")}
@@ -783,7 +806,8 @@ def main():
                       "fallback_frac": st_fast["n_surrogate_reject"] / max(1, st_fast["n_surrogate"] + st_fast["n_surrogate_reject"])},
         "status": {name: {k: stt[k] for k in ("code", "n_code", "n_fallback", "n_rh_fallback", "n_eint_switch",
                                                  "n_bracket_fail", "n_clamped")}
-                   for name, stt in (("plain", st_plain), ("fast", st_fast), ("mixed_plain_cooling", st_mixed))},
+                   for name, stt in (("plain", st_plain), ("fast", st_fast), ("mixed_plain_cooling", st_mixed),
+                                     ("mixed_fp32_rates_cooling", st_m32))},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
                      "frac": ach / hbm,
                      "traffic": TRAFFIC_B_PER_ZONE[dom] * zones_per_launch if dom in TRAFFIC_B_PER_ZONE else None,

@@ -287,10 +287,11 @@ int gb_cool_cells(int64_t n, const double* dens, double* ei, double* temp, doubl
  * 0 (default) = heatCool.F90's terms as written (a pow per power law),
  * 1 = the same terms with the transcendentals shared (one ln T and one
  * sqrt T per evaluation, x^a as exp(a ln x), the column density and the
- * FUV field's logarithm from per-cell constants). Form 1 is what the mixed
- * hydro path's fused cooling epilogue always uses; the FP64 path's
- * epilogue and gb_heat always use form 0. No counterpart in the
- * reference's interface. */
+ * FUV field's logarithm from per-cell constants), 2 = the terms evaluated
+ * in FP32 (Brent's iterates stay FP64). The mixed hydro path's fused
+ * cooling epilogue uses form 1, or form 2 under gb_set_cooling_mode(2);
+ * the FP64 path's epilogue and gb_heat always use form 0. No counterpart
+ * in the reference's interface. */
 int gb_set_rate_form(int form);
 
 /* ---------------------------------------------------------------- step */
@@ -452,7 +453,10 @@ int gb_surrogate_samples(int64_t n, uint64_t seed, float* feat_dev, float* targe
                          void* stream);
 /* Cooling mode of gb_evolve_step(cool = 1): 0 = plain integrator fused in
  * the update, 1 = surrogate with per-cell acceptance test and plain
- * fallback. The network's prediction starts at most four FP32 secant-Newton
+ * fallback, 2 = the plain integrator fused in the update with its rate
+ * function de/dt evaluated in FP32 (the mixed path; Brent's and the
+ * bracket search's iterates and the residual stay FP64; the FP64 path
+ * keeps its reference rates in every mode but 1). The network's prediction starts at most four FP32 secant-Newton
  * iterations on the backward-Euler residual; a cell is accepted when a
  * correction below rel_tol * e came from a local slope and the energy
  * moved the way the initial rate points. check_fp64 = 1 re-evaluates the

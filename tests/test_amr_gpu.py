@@ -61,6 +61,33 @@ def test_amr_fp64_step_matches_oracle(gb, oracle, mhd, fc):
     assert np.max(np.abs(gu - ou) / (np.abs(ou) + 1e-300)) <= 1e-12
 
 
+def test_amr_step_after_a_larger_grid(gb, oracle):
+    """The guard-fill plan's allocation outlives a registration: after a
+    216-block grid, the 3-level MHD tree's step with flux conservation and
+    edge-field matching still equals the oracle's (the per-node flags that
+    the edge matching reads sit where the plan build wrote them)."""
+    from torch_gb300 import workloads as W
+    ic = W.turbulent_box(6, 6, 6, seed=3, sigma_ln=0.5, mach=2.0, mhd=True, nvar=10)
+    big = gb.grid_from_workload(ic, mhd=True, cooling=False)
+    gb.init_hydro(gb.hydro_params(True))
+    big.register()
+    big.evolve_step(big.compute_dt().item(), cool=False)
+    del big
+    t, st, g = _state(gb, True)
+    g.register()
+    u, (fx, fy, fz) = _oracle_arrays(st, True)
+    p = oracle.hydro_params(True)
+    tl = oracle.TreeLists(t)
+    oracle.fill_guards_tree(p, t, u, fx, fy, fz)
+    dt = g.compute_dt().item()
+    g.evolve_step(dt, cool=False)
+    oracle.unsplit_tree(p, tl, t["leaf"], u, fx, fy, fz, dt, st["root_dx"], flux_correct=True)
+    leaf = t["leaf"]
+    gu = g.u.cpu().numpy()[leaf, :10, 4:20, 4:20, 4:20]
+    ou = u[leaf, :10, 4:20, 4:20, 4:20]
+    assert np.max(np.abs(gu - ou) / (np.abs(ou) + 1e-300)) <= 1e-12
+
+
 @pytest.mark.parametrize("mhd", [False, True])
 def test_amr_mixed_precision_l1(gb, mhd):
     t, st, g64 = _state(gb, mhd)

@@ -53,14 +53,20 @@ def test_cool_cells_match_oracle(gb, oracle, dt):
     assert np.all(np.abs(td_g - td_o)[ok] <= 1e-3 * td_o[ok] + 1e-9)
 
 
-@pytest.mark.parametrize("dt,extra", [(1e10, False), (3e12, False), (3e12, True)])
-def test_restated_rates_match_oracle(gb, oracle, dt, extra):
-    """The rate function with shared transcendentals (one ln T and one
-    sqrt T per evaluation), which the mixed path's fused epilogue
-    integrates, against the oracle's reference terms: every cell within the
-    root finder's tolerance, as the reference formulation is. extra: a
-    per-cell ionisation fraction and external FUV flux (the photoelectric
-    term's other branch)."""
+@pytest.mark.parametrize("form,dt,extra", [(1, 1e10, False), (1, 3e12, False), (1, 3e12, True),
+                                            (2, 1e10, False), (2, 3e12, False), (2, 3e12, True)])
+def test_restated_rates_match_oracle(gb, oracle, form, dt, extra):
+    """The rate function in the mixed path's forms against the oracle's
+    reference terms. Form 1 (shared transcendentals, one ln T and one sqrt T
+    per evaluation): every cell within the root finder's tolerance, as the
+    reference formulation is. Form 2 (the rates in FP32, Brent's iterates in
+    FP64): within that tolerance plus 1e-4 T, the FP32 rates' relative error
+    (about 1e-6, 1e-5 on the steepest power law) carried through the
+    residual: at the root the residual's rate term is the step's energy
+    change, so the FP32 error moves the root by at most that error times the
+    change, 2e-5 |T_new - T_old| more. The median stays below 1e-5.
+    extra: a per-cell ionisation fraction and external FUV flux (the
+    photoelectric term's other branch)."""
     import torch
     from torch_gb300 import tables
     gb.init_cooling(gb.cool_params())
@@ -77,7 +83,7 @@ def test_restated_rates_match_oracle(gb, oracle, dt, extra):
     dev = lambda a: None if a is None else torch.as_tensor(a.copy(), device="cuda")
     d_rho, d_ei, d_T, d_td = dev(rho), dev(ei), dev(T), dev(tdust)
     st = gb.status_buffer()
-    gb.set_rate_form(1)
+    gb.set_rate_form(form)
     try:
         gb.cool_cells(d_rho, d_ei, d_T, d_td, dt, xhp=dev(xhp), gflux=dev(pefl), status=st)
         torch.cuda.synchronize()
@@ -85,14 +91,16 @@ def test_restated_rates_match_oracle(gb, oracle, dt, extra):
         gb.set_rate_form(0)
     T_g, td_g = d_T.cpu().numpy(), d_td.cpu().numpy()
     ok = (flags & (4 | 8)) == 0
-    tolT = np.maximum(1.0, 1e-6 * T_o) * 2.0 + 1e-9 * T_o
+    tolT = np.maximum(1.0, 1e-6 * T_o) * 2.0 + (1e-9 if form == 1 else 1e-4) * T_o
+    if form == 2:
+        tolT = tolT + 2e-5 * np.abs(T_o - T)
     bad = ok & (np.abs(T_g - T_o) > tolT)
     assert bad.sum() == 0, (bad.sum(), np.abs(T_g - T_o)[ok].max())
     rel = np.abs(T_g - T_o) / T_o
-    assert np.median(rel[ok]) < 1e-7
+    assert np.median(rel[ok]) < (1e-7 if form == 1 else 1e-5)
     assert np.all(np.abs(td_g - td_o)[ok] <= 1e-3 * td_o[ok] + 1e-9)
     with pytest.raises(Exception):
-        gb.set_rate_form(2)
+        gb.set_rate_form(3)
 
 
 def test_heat_on_grid_matches_oracle(gb, oracle):

@@ -1237,7 +1237,10 @@ int gb_guard_prepare(cudaStream_t s)
             return GB_ERR_CUDA;
         g_gb.plan_n = nn;
     }
-    int* near = (int*)((int4*)g_gb.d_plan + (size_t)nn * 54);
+    // the per-node flags follow the entries of plan_n nodes (the allocation's
+    // capacity, which a larger tree registered earlier may have set): the
+    // edge matching reads them at the same place
+    int* near = (int*)((int4*)g_gb.d_plan + (size_t)g_gb.plan_n * 54);
     cudaMemsetAsync(near, 0, (size_t)nn * sizeof(int), s);
     k_guard_plan<<<(nn * 27 + 255) / 256, 256, 0, s>>>(g_gb.tree, (int4*)g_gb.d_plan, near);
     if (gb_check(cudaGetLastError(), "k_guard_plan")) return GB_ERR_CUDA;
@@ -1572,7 +1575,9 @@ int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int
     }
     for (int k = 0, b0 = 0; b0 < nblk; ++k, b0 += chunk) {
         int nb = nblk - b0 < chunk ? nblk - b0 : chunk;
-        const int fused = cool && gb_cooling_mode() == 0;
+        // the plain integrator fused into the update: 1 on the precision
+        // path's own rates, 2 on FP32 rates (mixed path; FP64 ignores it)
+        const int fused = !cool ? 0 : gb_cooling_mode() == 0 ? 1 : gb_cooling_mode() == 2 ? 2 : 0;
         const int chain = ns > 1 ? (k & 1) : 0;
         cudaStream_t sk = chain ? g_aux.s2 : s;
         void* scr = (char*)g_gb.d_scratch + (size_t)chain * chunk_bytes;

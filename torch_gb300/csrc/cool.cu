@@ -142,9 +142,9 @@ __global__ void k_heat_blocks(gb_dev_grid g, gb_cool_ctx c, const int* __restric
     }
 }
 
-// The same per-cell solve on plain CGS arrays (FR: the restated rates the
-// mixed hydro path's fused epilogue uses).
-template <bool FR>
+// The same per-cell solve on plain CGS arrays (FORM: the rate formulation,
+// as heating_and_cooling's template argument).
+template <int FORM>
 __global__ void k_cool_cells(gb_cool_ctx c, int64_t n, const double* __restrict__ dens,
                              double* ei_a, double* temp_a, double* tdust_a,
                              const double* __restrict__ xhp, const double* __restrict__ phhe,
@@ -166,7 +166,7 @@ __global__ void k_cool_cells(gb_cool_ctx c, int64_t n, const double* __restrict_
         gb_fail(st, GB_ST_NONFINITE, -1, (int)(idx & 0x7fffffff), 0, 0, temp);
         return;
     }
-    heating_and_cooling<FR>(c, v, &ei, dt, &temp, &d);
+    heating_and_cooling<FORM>(c, v, &ei, dt, &temp, &d);
     bool clamped = false;
     if (temp > c.p.absTmax) {
         ei = c.p.absTmax * v.TtoEI;
@@ -191,10 +191,14 @@ __global__ void k_cool_cells(gb_cool_ctx c, int64_t n, const double* __restrict_
 static double g_brent_tol_K = 1.0;
 static int g_rate_form = 0;
 
+namespace {
+gb_cool_pf make_pf(const gb_cool_params& p);
+}
+
 extern "C" int gb_set_rate_form(int form)
 {
-    if (form != 0 && form != 1) {
-        gb_set_error("gb_set_rate_form: form %d is neither 0 nor 1", form);
+    if (form < 0 || form > 2) {
+        gb_set_error("gb_set_rate_form: form %d is not 0, 1 or 2", form);
         return GB_ERR_ARG;
     }
     g_rate_form = form;
@@ -246,6 +250,7 @@ extern "C" int gb_cool_init(const char* path, const gb_cool_params* p)
     g_gb.cool.nf = d_tabf + GB_TEMP_PTS;
     g_gb.cool.lamf = d_tabf + GB_TEMP_PTS + GB_DENS_PTS;
     g_gb.cool.p = *p;
+    g_gb.cool.pf = make_pf(*p);
     g_gb.cool.T = g_gb.d_table;
     g_gb.cool.n = g_gb.d_table + GB_TEMP_PTS;
     g_gb.cool.lam = g_gb.d_table + GB_TEMP_PTS + GB_DENS_PTS;
@@ -295,12 +300,15 @@ extern "C" int gb_cool_cells(int64_t n, const double* dens, double* ei, double* 
     if (n == 0) return GB_OK;
     int tpb = 128;
     int64_t nb = (n + tpb - 1) / tpb;
-    if (g_rate_form)
-        k_cool_cells<true><<<(unsigned)nb, tpb, 0, (cudaStream_t)stream>>>(g_gb.cool, n, dens, ei, temp, tdust,
-                                                                        xhp, phhe, gflux, dt, st);
+    if (g_rate_form == 2)
+        k_cool_cells<2><<<(unsigned)nb, tpb, 0, (cudaStream_t)stream>>>(g_gb.cool, n, dens, ei, temp, tdust, xhp,
+                                                                     phhe, gflux, dt, st);
+    else if (g_rate_form == 1)
+        k_cool_cells<1><<<(unsigned)nb, tpb, 0, (cudaStream_t)stream>>>(g_gb.cool, n, dens, ei, temp, tdust, xhp,
+                                                                     phhe, gflux, dt, st);
     else
-        k_cool_cells<false><<<(unsigned)nb, tpb, 0, (cudaStream_t)stream>>>(g_gb.cool, n, dens, ei, temp, tdust,
-                                                                         xhp, phhe, gflux, dt, st);
+        k_cool_cells<0><<<(unsigned)nb, tpb, 0, (cudaStream_t)stream>>>(g_gb.cool, n, dens, ei, temp, tdust, xhp,
+                                                                     phhe, gflux, dt, st);
     return gb_check(cudaGetLastError(), "k_cool_cells") ? GB_ERR_CUDA : GB_OK;
 }
 
@@ -805,7 +813,7 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp,
 
 extern "C" int gb_set_cooling_mode(int mode, double rel_tol, int check_fp64)
 {
-    if (mode < 0 || mode > 1 || !(rel_tol > 0.0) || rel_tol > 0.5) return GB_ERR_ARG;
+    if (mode < 0 || mode > 2 || !(rel_tol > 0.0) || rel_tol > 0.5) return GB_ERR_ARG;
     g_cool_mode = mode;
     g_gb.gen += 1;
     g_sur_tol = rel_tol;

@@ -12,36 +12,8 @@
 #pragma once
 
 #include "gb_common.cuh"
-
-#define GB_TEMP_PTS 320
-#define GB_DENS_PTS 190
-
-struct gb_cool_ctx {
-    gb_cool_params p;
-    const double* T;    // cool_dat(1, :, 1), TEMP_PTS
-    const double* n;    // cool_dat(:, 1, 2), DENS_PTS
-    const double* lam;  // cool_dat(:, :, 3), dens fastest
-    double T_min, nd_min;
-    // Brent tolerance floor of the implicit step in kelvin (heatCool.F90
-    // passes TtoEI * 1 K; other values are a diagnostic of that tolerance)
-    double brent_tol_K;
-    // FP32 copies for the learned-cooling path: axes, and cool_dat(:, :, 3)
-    // divided by mu_mol m_p (the molecular power per gram)
-    const float* Tf;
-    const float* nf;
-    const float* lamf;
-};
-
-// FP32 parameter block of the learned-cooling path (cool_f32.cuh)
-struct gb_cool_pf;
-
-struct gb_cool_vars {
-    double ndens, rho, conf, Gflux, ephen, tdust, TtoEI, xHp, strat_factor, mu_mol;
-};
-
-struct gb_cool_diag {
-    int bracket_fail, dust_noconv, unbracketed, maxiter, iters;
-};
+#include "cool_types.cuh"
+#include "cool_f32.cuh"
 
 namespace gbcool {
 
@@ -318,13 +290,13 @@ static __device__ double dei_parts(const gb_cool_ctx& c, const gb_cool_vars& v, 
     return eplus + PeHeat - emin - cool_pw - cool_dg + floor_;
 }
 
-template <bool FR = false>
+template <int FORM = 0>
 static __device__ double get_dust_temperature(const gb_cool_params& p, double tdust_in, double temp_in,
                                        double nden, double phen_heat, gb_cool_diag* d)
 {
     // heatCool.F90:703-884; the gas temperature is fixed during the Newton
     // iterations, so its collision factor and square root are formed once
-    // (the same values). FR: T_dust^6 as a product instead of pow.
+    // (the same values). FORM >= 1: T_dust^6 as a product instead of pow.
     const double tol = 1.e-4, smallt = .1;
     double error = 10. * tol;
     double tdust = tdust_in;
@@ -334,7 +306,7 @@ static __device__ double get_dust_temperature(const gb_cool_params& p, double td
     int l = 1;
     while ((l <= 100) && (error > tol)) {
         double t6;
-        if (FR) {
+        if (FORM >= 1) {
             const double t2 = tdust * tdust;
             t6 = t2 * t2 * t2;
         } else {
@@ -358,7 +330,7 @@ static __device__ double get_dust_temperature(const gb_cool_params& p, double td
     return tdust;
 }
 
-template <bool FR = false>
+template <int FORM = 0>
 static __device__ void dust_update(const gb_cool_ctx& c, gb_cool_vars& v, double temp, gb_cool_diag* d)
 {
     // heatCool.F90:430-443
@@ -370,7 +342,7 @@ static __device__ void dust_update(const gb_cool_ctx& c, gb_cool_vars& v, double
     cr = cr * v.rho;
     dust_heat = dust_heat + cr;
     dust_heat = dust_heat / (v.ndens * 1e-33);
-    v.tdust = get_dust_temperature<FR>(p, v.tdust, temp, v.ndens, dust_heat, d);
+    v.tdust = get_dust_temperature<FORM>(p, v.tdust, temp, v.ndens, dust_heat, d);
 }
 
 // ---- dei_dt restated for the mixed path (FR): the same rate terms with
@@ -387,6 +359,11 @@ struct fr_consts {
     double lnG0;   // ln(Gzero strat) (used when Gflux == 0)
     double lnxn;   // ln(x_l n): the photoelectric grain-charging denominator
     double rn;     // rho / n
+    // FORM 2: the cell's state and the cooling at the floors in FP32, and
+    // the FP32 tables
+    gb_cool_varsf vf;
+    float fl32;
+    gb_cool_tabf tf;
 };
 
 __device__ __forceinline__ fr_consts make_fr(const gb_cool_params& p, const gb_cool_vars& v)
@@ -400,6 +377,19 @@ __device__ __forceinline__ fr_consts make_fr(const gb_cool_params& p, const gb_c
     const double xl = (v.xHp == 0.0) ? 1e-8 : v.xHp;
     f.lnxn = log(xl * v.ndens);
     return f;
+}
+
+// FORM 2 (the plain integrator on FP32 rates): the backward-Euler residual
+// and Brent's and zbrac's iterates stay FP64; only the rate function de/dt
+// runs in FP32 (gbcoolf::dei_parts with the library's exp/log), from the
+// cell's state converted once. The rate's relative error, about 1e-6 (1e-5
+// on the steepest power law), moves the residual's root by far less than
+// Brent's stopping tolerance max(TtoEI * 1 K, 1e-6 e) in most cells.
+__device__ __forceinline__ void make_fr32(const gb_cool_ctx& c, const gb_cool_vars& v, double fl, fr_consts& f)
+{
+    gbcoolf::make_vars(c.pf, v, f.vf);
+    f.fl32 = gb_d2f(fl);
+    f.tf = gb_cool_tabf{c.Tf, c.nf, c.lamf, gb_d2f(c.T_min), gb_d2f(c.nd_min)};
 }
 
 // radloss (heatCool.F90:1590-1667) from ln T and sqrt(T)
@@ -528,31 +518,35 @@ static __device__ double dei_dt_fr(const gb_cool_ctx& c, const gb_cool_vars& v, 
     return eplus + PeHeat - emin - cool_pw - cool_dg + floor_;
 }
 
-template <bool FR>
+template <int FORM>
 __device__ __forceinline__ double rate(const gb_cool_ctx& c, const gb_cool_vars& v, const fr_consts& f,
                                        double floor_, double y)
 {
-    if (FR) return dei_dt_fr(c, v, f, floor_, y);
+    if (FORM == 2) {
+        float gam, lam;
+        return gb_f2d(gbcoolf::dei_parts<true>(c.pf, f.tf, f.vf, f.fl32, gb_d2f(y), &gam, &lam));
+    }
+    if (FORM == 1) return dei_dt_fr(c, v, f, floor_, y);
     return dei_dt(c, v, floor_, y);
 }
 
-template <bool FR = false>
+template <int FORM = 0>
 __device__ __forceinline__ double one_step(const gb_cool_ctx& c, const gb_cool_vars& v, const fr_consts& f,
                                            double floor_, double dx, double y, double yold)
 {
     // heatCool.F90:1928-1950
-    return y - dx * rate<FR>(c, v, f, floor_, y) - yold;
+    return y - dx * rate<FORM>(c, v, f, floor_, y) - yold;
 }
 
-template <bool FR = false>
+template <int FORM = 0>
 static __device__ double zero(const gb_cool_ctx& c, const gb_cool_vars& v, const fr_consts& f, double floor_,
                        double a, double b, double a_old, double machep, double tt, double dt,
                        gb_cool_diag* d)
 {
     // heatCool.F90:1981-2197 (Brent)
     double sa = a, sb = b;
-    double fa = one_step<FR>(c, v, f, floor_, dt, sa, a_old);
-    double fb = one_step<FR>(c, v, f, floor_, dt, sb, a_old);
+    double fa = one_step<FORM>(c, v, f, floor_, dt, sa, a_old);
+    double fb = one_step<FORM>(c, v, f, floor_, dt, sb, a_old);
     double cc = sa, fc = fa, e = sb - sa, dd = e;
     int n_tries = 0;
     if ((fa > 0.0 && fb > 0.0) || (fa < 0.0 && fb < 0.0)) {
@@ -597,7 +591,7 @@ static __device__ double zero(const gb_cool_ctx& c, const gb_cool_vars& v, const
         if (tol < fabs(dd)) sb = sb + dd;
         else if (0.0 < m) sb = sb + tol;
         else sb = sb - tol;
-        fb = one_step<FR>(c, v, f, floor_, dt, sb, a_old);
+        fb = one_step<FORM>(c, v, f, floor_, dt, sb, a_old);
         if ((0.0 < fb && 0.0 < fc) || (fb <= 0.0 && fc <= 0.0)) {
             cc = sa;
             fc = fa;
@@ -614,24 +608,24 @@ static __device__ double zero(const gb_cool_ctx& c, const gb_cool_vars& v, const
     return sb;
 }
 
-template <bool FR = false>
+template <int FORM = 0>
 static __device__ int zbrac(const gb_cool_ctx& c, const gb_cool_vars& v, const fr_consts& f, double floor_,
                      double* x1, double* x2, double xold, double dt)
 {
     // heatCool.F90:2294-2348
     const double FACTOR = 1.6;
-    double f1 = one_step<FR>(c, v, f, floor_, dt, *x1, xold);
-    double f2 = one_step<FR>(c, v, f, floor_, dt, *x2, xold);
+    double f1 = one_step<FORM>(c, v, f, floor_, dt, *x1, xold);
+    double f2 = one_step<FORM>(c, v, f, floor_, dt, *x2, xold);
     for (int j = 1; j <= 5000; ++j) {
         if (f1 * f2 < 0.0) return 1;
         if (fabs(f1) < fabs(f2)) {
             *x1 = *x1 + FACTOR * (*x1 - *x2);
             if (*x1 < 0.0) *x1 = v.TtoEI * 1.0;
-            f1 = one_step<FR>(c, v, f, floor_, dt, *x1, xold);
+            f1 = one_step<FORM>(c, v, f, floor_, dt, *x1, xold);
         } else {
             *x2 = *x2 + FACTOR * (*x2 - *x1);
             if (*x2 < 0.0) *x2 = v.TtoEI * 1.0;
-            f2 = one_step<FR>(c, v, f, floor_, dt, *x2, xold);
+            f2 = one_step<FORM>(c, v, f, floor_, dt, *x2, xold);
         }
     }
     return 0;
@@ -639,7 +633,7 @@ static __device__ int zbrac(const gb_cool_ctx& c, const gb_cool_vars& v, const f
 
 // heating_and_cooling, "Implicit" (default) or "Euler" branch, for one
 // cell. v must hold rho, Gflux, ephen, tdust, xHp, strat_factor, mu_mol.
-template <bool FR = false>
+template <int FORM = 0>
 static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v, double* ei_io,
                                     double timestep, double* temp_io, gb_cool_diag* d)
 {
@@ -651,13 +645,14 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
     v.TtoEI = ei / temp;
     v.conf = v.ndens * v.ndens / v.rho;
     double fl = cooling_floor(c, v);
-    fr_consts frc = {0.0, 0.0, 0.0, 0.0, 0.0};
-    if (FR) frc = make_fr(p, v);
+    fr_consts frc;
+    if (FORM == 1) frc = make_fr(p, v);
+    if (FORM == 2) make_fr32(c, v, fl, frc);
     if (p.int_method == 1) {
         // Euler, heatCool.F90:119-214
         int ncount = 0;
         for (;;) {
-            double dei = rate<FR>(c, v, frc, fl, ei);
+            double dei = rate<FORM>(c, v, frc, fl, ei);
             double dt1 = p.subfactor * ei / fmx(fabs(dei), 1e-50);
             double dt0 = fmn((timestep - total_time), dt1);
             ei = ei + dei * dt0;
@@ -672,13 +667,13 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
             ei = p.absTmin * v.TtoEI;
         }
         if (p.useDustCool && temp <= p.dust_sputter_temp)
-            v.tdust = get_dust_temperature<FR>(p, v.tdust, temp, v.ndens, 0.0, d);
+            v.tdust = get_dust_temperature<FORM>(p, v.tdust, temp, v.ndens, 0.0, d);
     } else {
         // Implicit, heatCool.F90:216-514 (one pass: dt0 = timestep)
         while ((timestep - total_time) > (1e-6 * timestep)) {
             double eiolder = ei;
             double eiold = ei;
-            double dei = rate<FR>(c, v, frc, fl, eiold);
+            double dei = rate<FORM>(c, v, frc, fl, eiold);
             double dt0 = timestep;
             eiold = eiolder + dei * dt0 * 1.0e-3;
             double ei1 = eiolder, ei2 = eiold;
@@ -686,23 +681,23 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
                 dt0 = (timestep - total_time);
                 ei = eiolder + dei * dt0;
                 temp = ei / v.TtoEI;
-                if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update<FR>(c, v, temp, d);
+                if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update<FORM>(c, v, temp, d);
                 total_time = total_time + dt0;
                 continue;
             }
-            int found = zbrac<FR>(c, v, frc, fl, &ei1, &ei2, eiolder, dt0);
+            int found = zbrac<FORM>(c, v, frc, fl, &ei1, &ei2, eiolder, dt0);
             if (!found) d->bracket_fail = 1;
             if (ei1 < 0.0 || ei2 < 0.0) {
                 ei1 = fmx(ei1, v.TtoEI * 1.0);
                 ei2 = fmx(ei2, v.TtoEI * 1.0);
             }
             if (found)
-                ei = zero<FR>(c, v, frc, fl, ei1, ei2, eiolder, 3e-16, fmx(v.TtoEI * c.brent_tol_K, eiold * err_tol), dt0, d);
+                ei = zero<FORM>(c, v, frc, fl, ei1, ei2, eiolder, 3e-16, fmx(v.TtoEI * c.brent_tol_K, eiold * err_tol), dt0, d);
             else
-                ei = zero<FR>(c, v, frc, fl, v.TtoEI * 1.0, v.TtoEI * 1.0e9, eiolder, 3e-16,
+                ei = zero<FORM>(c, v, frc, fl, v.TtoEI * 1.0, v.TtoEI * 1.0e9, eiolder, 3e-16,
                           fmx(v.TtoEI * c.brent_tol_K, eiold * err_tol), dt0, d);
             temp = ei / v.TtoEI;
-            if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update<FR>(c, v, temp, d);
+            if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update<FORM>(c, v, temp, d);
             total_time = total_time + dt0;
         }
         if (temp < p.absTmin) {

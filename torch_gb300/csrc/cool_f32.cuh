@@ -7,29 +7,8 @@
 // quantities are scaled the same way where a product would leave it.
 #pragma once
 
-#include "cool_dev.cuh"
-
-struct gb_cool_tabf {
-    const float* T;    // TEMP_PTS
-    const float* n;    // DENS_PTS
-    const float* lam;  // cool_dat(:, :, 3) / (mu_mol m_p): molecular power per gram
-    float T_min, nd_min;
-};
-
-struct gb_cool_varsf {
-    float ndens, rho, conf, Gflux, ephen, tdust, TtoEI, xHp, mu_mol;
-    float cr_pref;  // strat * crIonRate * crIonEnergy / (rho / n)
-};
-
-// the runtime parameters in FP32, converted once on the host (values far
-// below FP32's range, such as 1e-99, become 0, which leaves every
-// comparison they take part in unchanged)
-struct gb_cool_pf {
-    float theatmin, theatmax, tradmin, tradmax, dradmin, dradmax, dust_sputter_temp;
-    float Gzero, pe_norm, crIonExp, crIonNH, lnNH, crRE, T_cool_min, nd_cool_min, nd_cool_max, absTmin;
-    float jeansK;  // 5/3 pi k_B / G_Newton (heatCool.F90:1687)
-    int use_cr_heating, cr_uniform, pe_recipe, useDustCool;
-};
+#include "cool_types.cuh"
+#include "gb_common.cuh"
 
 namespace gbcoolf {
 
@@ -38,26 +17,40 @@ __device__ __forceinline__ float lin(float x1, float y1, float x2, float y2, flo
     return (y2 - y1) / (x2 - x1) * (x - x1) + y1;
 }
 
-__device__ __forceinline__ float pw(float lnC, float a, float lnT) { return __expf(lnC + a * lnT); }
+// ACC: the correctly rounded-to-a-few-ulp library functions (expf, logf,
+// powf) instead of the hardware approximations (__expf, whose error grows
+// with |x|: about 60 ulp at the power laws' x ~ -50). The plain integrator
+// run on FP32 rates takes ACC; the surrogate's features and Newton steps
+// do not need it.
+template <bool ACC>
+__device__ __forceinline__ float ex(float x) { return ACC ? expf(x) : __expf(x); }
+template <bool ACC>
+__device__ __forceinline__ float lg(float x) { return ACC ? logf(x) : __logf(x); }
+template <bool ACC>
+__device__ __forceinline__ float pwr(float x, float y) { return ACC ? powf(x, y) : __powf(x, y); }
+
+template <bool ACC = false>
+__device__ __forceinline__ float pw(float lnC, float a, float lnT) { return ex<ACC>(lnC + a * lnT); }
 
 // Radloss (heatCool.F90:1590-1667) in log space
+template <bool ACC = false>
 __device__ __forceinline__ float radloss(float T)
 {
-    const float l = __logf(T);
+    const float l = lg<ACC>(T);
     if (T >= 1.70e4f) {
         if (T >= 5.62e5f) {
-            if (T >= 2.75e6f) return T >= 3.16e7f ? pw(-61.0416264f, 0.5f, l) : pw(-46.7079387f, -0.33f, l);
-            return T >= 1.78e6f ? pw(-7.85193121f, -2.95f, l) : pw(-50.5136917f, 0.01f, l);
+            if (T >= 2.75e6f) return T >= 3.16e7f ? pw<ACC>(-61.0416264f, 0.5f, l) : pw<ACC>(-46.7079387f, -0.33f, l);
+            return T >= 1.78e6f ? pw<ACC>(-7.85193121f, -2.95f, l) : pw<ACC>(-50.5136917f, 0.01f, l);
         }
-        if (T >= 7.94e4f) return T >= 2.51e5f ? pw(-23.9471542f, -2.0f, l) : pw(-48.9528915f, 0.01f, l);
-        return T >= 3.98e4f ? pw(-71.3801379f, 2.0f, l) : pw(-47.9629208f, -0.216f, l);
+        if (T >= 7.94e4f) return T >= 2.51e5f ? pw<ACC>(-23.9471542f, -2.0f, l) : pw<ACC>(-48.9528915f, 0.01f, l);
+        return T >= 3.98e4f ? pw<ACC>(-71.3801379f, 2.0f, l) : pw<ACC>(-47.9629208f, -0.216f, l);
     }
     if (T >= 1.e3f) {
-        if (T >= 6.31e3f) return T >= 1.0e4f ? pw(-184.477305f, 13.8f, l) : pw(-61.0287645f, 0.396f, l);
-        return T >= 3.16e3f ? pw(-58.8964335f, 0.152f, l) : pw(-60.5058714f, 0.352f, l);
+        if (T >= 6.31e3f) return T >= 1.0e4f ? pw<ACC>(-184.477305f, 13.8f, l) : pw<ACC>(-61.0287645f, 0.396f, l);
+        return T >= 3.16e3f ? pw<ACC>(-58.8964335f, 0.152f, l) : pw<ACC>(-60.5058714f, 0.352f, l);
     }
-    if (T >= 3.98e1f) return T >= 2.00e2f ? pw(-61.0513826f, 0.431f, l) : pw(-64.0536723f, 0.997f, l);
-    return T >= 2.51e1f ? pw(-65.9036743f, 1.5f, l) : pw(-73.5919686f, 3.885f, l);
+    if (T >= 3.98e1f) return T >= 2.00e2f ? pw<ACC>(-61.0513826f, 0.431f, l) : pw<ACC>(-64.0536723f, 0.997f, l);
+    return T >= 2.51e1f ? pw<ACC>(-65.9036743f, 1.5f, l) : pw<ACC>(-73.5919686f, 3.885f, l);
 }
 
 __device__ __forceinline__ float fmx(float a, float b) { return a > b ? a : b; }
@@ -86,6 +79,7 @@ __device__ __forceinline__ int find(const float* x, float x0, int N)
 
 // de/dt split into heating Gamma and cooling Lambda (as dei_parts);
 // floor_ is the cooling at the floors (state-independent per cell)
+template <bool ACC = false>
 static __device__ float dei_parts(const gb_cool_pf& p, const gb_cool_tabf& t, const gb_cool_varsf& v, float floor_,
                            float ei, float* gam, float* lam)
 {
@@ -99,11 +93,11 @@ static __device__ float dei_parts(const gb_cool_pf& p, const gb_cool_tabf& t, co
     if (T <= p.theatmax && T >= p.theatmin) {
         if (p.use_cr_heating) {
             if (p.cr_uniform) eplus = v.cr_pref;
-            else eplus = v.cr_pref * __expf(-p.crIonExp * (__logf(fmx(p.crIonNH, ncol)) - p.lnNH));
+            else eplus = v.cr_pref * ex<ACC>(-p.crIonExp * (lg<ACC>(fmx(p.crIonNH, ncol)) - p.lnNH));
         }
         eplus *= ramp_T(T, p.theatmin, p.theatmax);
     }
-    const float fext = __expf(-3.5f * (ncol * 0.01f / 1.87e21f));
+    const float fext = ex<ACC>(-3.5f * (ncol * 0.01f / 1.87e21f));
     const float G = v.Gflux + p.Gzero * fext;
     float PeHeat = 0.0f;
     const float ulpe = fmn(p.theatmax, p.dust_sputter_temp);
@@ -112,13 +106,13 @@ static __device__ float dei_parts(const gb_cool_pf& p, const gb_cool_tabf& t, co
         float eff;
         if (p.pe_recipe == 1) {
             float Gf = G * sqT / (xl * v.ndens * 0.5f);
-            eff = 4.9e-2f / (1.0f + 4.0e-3f * __powf(Gf, 0.73f)) + 3.7e-2f * __powf(T * 1e-4f, 0.7f) / (1.0f + 2.0e-4f * Gf);
+            eff = 4.9e-2f / (1.0f + 4.0e-3f * pwr<ACC>(Gf, 0.73f)) + 3.7e-2f * pwr<ACC>(T * 1e-4f, 0.7f) / (1.0f + 2.0e-4f * Gf);
             PeHeat = p.pe_norm * eff * G * (v.ndens / v.rho);
         } else if (p.pe_recipe == 0) {
             float Gf = G * sqT / (xl * v.ndens);
-            float gp = Gf > 0.0f ? __logf(Gf) : -1e30f;
-            eff = (7.64f + 4.52f * __expf(0.132f * __logf(T))) /
-                  (1.0f + (0.04371f * __expf(0.452f * gp)) * (1.0f + 0.00557f * __expf(0.675f * gp)));
+            float gp = Gf > 0.0f ? lg<ACC>(Gf) : -1e30f;
+            eff = (7.64f + 4.52f * ex<ACC>(0.132f * lg<ACC>(T))) /
+                  (1.0f + (0.04371f * ex<ACC>(0.452f * gp)) * (1.0f + 0.00557f * ex<ACC>(0.675f * gp)));
             // 1e-26 * eff * G / (rho / n), with rho/n ~ 4e-24 kept in range
             PeHeat = 1e-26f * eff * G * (v.ndens / v.rho);
         } else {
@@ -130,7 +124,7 @@ static __device__ float dei_parts(const gb_cool_pf& p, const gb_cool_tabf& t, co
     // atomic cooling (heatCool.F90:1116-1200)
     float emin = 0.0f;
     if (T <= p.tradmax && T >= p.tradmin && v.ndens >= p.dradmin && v.ndens <= p.dradmax) {
-        emin = radloss(T);
+        emin = radloss<ACC>(T);
         if (v.xHp > 1e-2f && T < 1.2e4f) {
             float DG = lin(1e-2f, 1.0f, 1e-1f, 5.0f, fmn(1e-1f, v.xHp));
             emin *= DG;
@@ -158,7 +152,7 @@ static __device__ float dei_parts(const gb_cool_pf& p, const gb_cool_tabf& t, co
         }
         if (T <= p.dust_sputter_temp) {
             // 3.8e-33 n^2 (...) / rho  ->  3.8e-33 n (n / rho) (...)
-            cool_dg = 3.8e-33f * v.ndens * (v.ndens / v.rho) * (1.0f - 0.8f * __expf(-75.0f / T)) * (T - v.tdust) * sqT;
+            cool_dg = 3.8e-33f * v.ndens * (v.ndens / v.rho) * (1.0f - 0.8f * ex<ACC>(-75.0f / T)) * (T - v.tdust) * sqT;
             float ul = p.dust_sputter_temp, ul10 = ul - 0.1f * ul;
             if (T >= ul10) cool_dg *= lin(ul10, 1.0f, ul, 0.0f, T);
         }

@@ -1570,7 +1570,7 @@ __device__ __forceinline__ double rcp_newton(double x)
 // mixed path without the fused plain cooling: eight resident CTAs per SM
 // (64 registers, no spills); the FP64 path and the fused integrator need
 // more registers than that
-template <typename T, bool MHD, bool COOL, bool FEAT>
+template <typename T, bool MHD, int COOL, bool FEAT>
 __global__ void __launch_bounds__(128, (std::is_same<T, float>::value && !COOL) ? 8 : 1)
 k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restrict__ list,
          const T* __restrict__ fscr, size_t fstride, const double* __restrict__ bscr, size_t bstride,
@@ -1725,9 +1725,9 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
         bool clamped = false;
         if (good) {
             // the mixed path evaluates the rates with shared transcendentals
-            // (one ln T and one sqrt T per evaluation); the FP64 path keeps
-            // the reference's formulation
-            gbcool::heating_and_cooling<RCP>(cool, v, &eic, kp_dt(kp) * p.time_unit, &temp, &dg);
+            // (one ln T and one sqrt T per evaluation; COOL 2: in FP32); the
+            // FP64 path keeps the reference's formulation
+            gbcool::heating_and_cooling<RCP ? COOL : 0>(cool, v, &eic, kp_dt(kp) * p.time_unit, &temp, &dg);
             if (temp > p.absTmax) {
                 eic = p.absTmax * v.TtoEI;
                 temp = p.absTmax;

@@ -162,14 +162,19 @@ int launch_chunk(const hydro_kparams& kp_in, int mhd, int cool, int nblk, const 
     gb_prof_begin(GBP_UPDATE, s);
     const sur_feat_out sfv = sf ? *sf : sur_feat_out{};
     const bool feat = !cool && sfv.feat;
+    // cool 2 (the plain integrator on FP32 rates) exists for the mixed path;
+    // the FP64 path runs its reference rates
+    constexpr int C2 = std::is_same<T, float>::value ? 2 : 1;
     if (mhd) {
-        if (cool) k_update<T, true, true, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
-        else if (feat) k_update<T, true, false, true><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
-        else k_update<T, true, false, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
+        if (cool == 2) k_update<T, true, C2, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
+        else if (cool) k_update<T, true, 1, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
+        else if (feat) k_update<T, true, 0, true><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
+        else k_update<T, true, 0, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
     } else {
-        if (cool) k_update<T, false, true, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
-        else if (feat) k_update<T, false, false, true><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
-        else k_update<T, false, false, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
+        if (cool == 2) k_update<T, false, C2, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
+        else if (cool) k_update<T, false, 1, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
+        else if (feat) k_update<T, false, 0, true><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
+        else k_update<T, false, 0, false><<<ug, 128, 0, s>>>(g, kp, g_gb.cool, list, fscr, SL::flux, bscr, SL::fb, st, sfv);
     }
     gb_prof_end(GBP_UPDATE, s);
     return gb_check(cudaGetLastError(), "hydro chunk launch") ? GB_ERR_CUDA : GB_OK;

@@ -626,9 +626,14 @@ def mlp_infer(feat, tensor_cores: bool = True):
     return y
 
 
-def set_cooling_mode(surrogate: bool, rel_tol: float = 2e-3, check_fp64: bool = False):
-    check(lib().gb_set_cooling_mode(int(surrogate), rel_tol, int(check_fp64)), "gb_set_cooling_mode")
-    state["surrogate"] = bool(surrogate)
+def set_cooling_mode(mode, rel_tol: float = 2e-3, check_fp64: bool = False):
+    """Cooling of a step with cool=True: 0 (False) the plain integrator fused
+    into the update, 1 (True) the learned surrogate with the plain
+    integrator as fallback, 2 the plain integrator on FP32 rates (the mixed
+    path; the FP64 path keeps its reference rates)."""
+    m = int(mode)
+    check(lib().gb_set_cooling_mode(m, rel_tol, int(check_fp64)), "gb_set_cooling_mode")
+    state["surrogate"] = m == 1
 
 
 PROF_NAMES = ["guard_fill", "recon", "flux", "emf", "faceb", "update", "dt", "heat", "sur_feat", "mlp_infer",
