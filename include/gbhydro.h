@@ -170,8 +170,8 @@ int gb_hydro_unsplit(int blockCount, const int* blockList_dev, double dt, double
  * must not call cudaMalloc because it can synchronise the whole device.
  * Runs the same plain FP64 kernels as gb_hydro_unsplit (no fused cooling,
  * whatever gb_hydro_params.precision says) with their scratch in a static
- * device array sized for GB_NOALLOC_MAX_BLOCKS blocks (about 3.7 MB per
- * block, ~14.6 MB held on every GPU that loads the library until exit).
+ * device array sized for GB_NOALLOC_MAX_BLOCKS blocks (about 3.9 MiB per
+ * block, ~15.7 MiB held on every GPU that loads the library until exit).
  * blockCount above GB_NOALLOC_MAX_BLOCKS returns GB_ERR_LIMIT. The first
  * call on each device looks up the array's device address (make it before
  * any stream capture). Calls share the array: calls that overlap on the GPU

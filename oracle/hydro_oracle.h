@@ -49,6 +49,11 @@ typedef struct orc_hydro_params {
      * from the positivity check, or from the first Rankine-Hugoniot check
      * with fallback_lower_cfl); bit 1: 0.25 (second check). */
     unsigned char* cflc;
+    /* edge electric fields: 0 = Gardiner & Stone (2005) eq. 41/50, the
+     * arithmetic mean of the four face fields plus contact-upwinded
+     * derivative terms (the scheme the GPU runs); 1 = the arithmetic mean
+     * alone (Balsara & Spicer 1999), a comparison point only */
+    int emf_average;
 } orc_hydro_params;
 
 #define ORC_CFLC 4096

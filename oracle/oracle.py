@@ -55,6 +55,7 @@ class HydroParams(C.Structure):
         ("mhd", C.c_int), ("nxb", C.c_int), ("nguard", C.c_int), ("energy_fix", C.c_int), ("cfl_sum", C.c_int),
         ("hybrid_order", C.c_int), ("fallback_lower_cfl", C.c_int), ("hybrid_kappa", C.c_double),
         ("cfl_fallback_factor", C.c_double), ("cfl", C.c_double), ("cflc", C.c_void_p),
+        ("emf_average", C.c_int),
     ]
 
     def keep_cfl_codes(self, nblocks: int):

@@ -385,11 +385,21 @@ __device__ __forceinline__ fr_consts make_fr(const gb_cool_params& p, const gb_c
 // cell's state converted once. The rate's relative error, about 1e-6 (1e-5
 // on the steepest power law), moves the residual's root by far less than
 // Brent's stopping tolerance max(TtoEI * 1 K, 1e-6 e) in most cells.
-__device__ __forceinline__ void make_fr32(const gb_cool_ctx& c, const gb_cool_vars& v, double fl, fr_consts& f)
+__device__ __forceinline__ void make_fr32(const gb_cool_ctx& c, const gb_cool_vars& v, fr_consts& f)
 {
     gbcoolf::make_vars(c.pf, v, f.vf);
-    f.fl32 = gb_d2f(fl);
     f.tf = gb_cool_tabf{c.Tf, c.nf, c.lamf, gb_d2f(c.T_min), gb_d2f(c.nd_min)};
+    f.fl32 = gbcoolf::cooling_floor<true>(c.pf, f.tf, f.vf);
+}
+
+// the dust temperature after the step (heatCool.F90:430-443): FORM 2 in
+// FP32 (the same dust heating and Newton iteration, gbcoolf::dust_temperature)
+template <int FORM>
+__device__ __forceinline__ void dust_after_step(const gb_cool_ctx& c, gb_cool_vars& v, const fr_consts& f, double temp,
+                                                gb_cool_diag* d)
+{
+    if (FORM == 2) v.tdust = gb_f2d(gbcoolf::dust_temperature<true>(c.pf, f.vf, gb_d2f(temp), gb_d2f(v.tdust)));
+    else dust_update<FORM>(c, v, temp, d);
 }
 
 // radloss (heatCool.F90:1590-1667) from ln T and sqrt(T)
@@ -538,12 +548,26 @@ __device__ __forceinline__ double one_step(const gb_cool_ctx& c, const gb_cool_v
     return y - dx * rate<FORM>(c, v, f, floor_, y) - yold;
 }
 
+// |a| < |b| and friends on the integer pipe: for non-NaN doubles the
+// magnitudes order as their bit patterns without the sign bit, and the
+// sign tests read the sign bit, so these take exactly FP64's decisions
+__device__ __forceinline__ unsigned long long mag_bits(double x)
+{
+    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ bool pos_bits(double x) { return __double_as_longlong(x) > 0; }
+
 template <int FORM = 0>
 static __device__ double zero(const gb_cool_ctx& c, const gb_cool_vars& v, const fr_consts& f, double floor_,
                        double a, double b, double a_old, double machep, double tt, double dt,
                        gb_cool_diag* d)
 {
-    // heatCool.F90:1981-2197 (Brent)
+    // heatCool.F90:1981-2197 (Brent). FORM 2 (the mixed path's integrator on
+    // FP32 rates) takes every comparison on the integer pipe (the same
+    // decisions) and forms the inverse-quadratic / secant trial step in FP32
+    // (a trial point a few ulp of FP32 from FP64's, which Brent's own
+    // acceptance test and bisection fallback then treat alike); the iterates,
+    // the bracket and the tolerance stay FP64.
     double sa = a, sb = b;
     double fa = one_step<FORM>(c, v, f, floor_, dt, sa, a_old);
     double fb = one_step<FORM>(c, v, f, floor_, dt, sb, a_old);
@@ -554,16 +578,44 @@ static __device__ double zero(const gb_cool_ctx& c, const gb_cool_vars& v, const
         return sb;
     }
     for (;;) {
-        if (fabs(fc) < fabs(fb)) {
+        if (FORM == 2 ? mag_bits(fc) < mag_bits(fb) : fabs(fc) < fabs(fb)) {
             sa = sb; sb = cc; cc = sa;
             fa = fb; fb = fc; fc = fa;
         }
         double tol = 2.0 * machep * fabs(sb) + tt;
         double m = 0.5 * (cc - sb);
-        if (fabs(m) <= tol || fb == 0.0) break;
-        if (fabs(e) < tol || fabs(fa) <= fabs(fb)) {
+        if (FORM == 2) {
+            if (mag_bits(m) <= mag_bits(tol) || mag_bits(fb) == 0ull) break;
+        } else {
+            if (fabs(m) <= tol || fb == 0.0) break;
+        }
+        if (FORM == 2 ? (mag_bits(e) < mag_bits(tol) || mag_bits(fa) <= mag_bits(fb))
+                      : (fabs(e) < tol || fabs(fa) <= fabs(fb))) {
             e = m;
             dd = e;
+        } else if (FORM == 2) {
+            const float faf = gb_d2f(fa), fbf = gb_d2f(fb), fcf = gb_d2f(fc), mf = gb_d2f(m);
+            float s = fbf / faf, pp, q, r;
+            if (sa == cc) {
+                pp = 2.0f * mf * s;
+                q = 1.0f - s;
+            } else {
+                q = faf / fcf;
+                r = fbf / fcf;
+                pp = s * (2.0f * mf * q * (q - r) - gb_d2f(sb - sa) * (r - 1.0f));
+                q = (q - 1.0f) * (r - 1.0f) * (s - 1.0f);
+            }
+            if (0.0f < pp) q = -q;
+            else pp = -pp;
+            const float sf = gb_d2f(e);
+            e = dd;
+            // non-finite FP32 intermediates fail the test: bisection
+            if (2.0f * pp < 3.0f * mf * q - fabsf(gb_d2f(tol) * q) && pp < fabsf(0.5f * sf * q)) {
+                dd = gb_f2d(pp / q);
+            } else {
+                e = m;
+                dd = e;
+            }
         } else {
             double s = fb / fa, pp, q, r;
             if (sa == cc) {
@@ -588,11 +640,12 @@ static __device__ double zero(const gb_cool_ctx& c, const gb_cool_vars& v, const
         }
         sa = sb;
         fa = fb;
-        if (tol < fabs(dd)) sb = sb + dd;
-        else if (0.0 < m) sb = sb + tol;
+        if (FORM == 2 ? mag_bits(tol) < mag_bits(dd) : tol < fabs(dd)) sb = sb + dd;
+        else if (FORM == 2 ? pos_bits(m) : 0.0 < m) sb = sb + tol;
         else sb = sb - tol;
         fb = one_step<FORM>(c, v, f, floor_, dt, sb, a_old);
-        if ((0.0 < fb && 0.0 < fc) || (fb <= 0.0 && fc <= 0.0)) {
+        if (FORM == 2 ? pos_bits(fb) == pos_bits(fc)
+                      : ((0.0 < fb && 0.0 < fc) || (fb <= 0.0 && fc <= 0.0))) {
             cc = sa;
             fc = fa;
             e = sb - sa;
@@ -644,10 +697,11 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
     v.ndens = v.rho / (v.mu_mol * p.mp);
     v.TtoEI = ei / temp;
     v.conf = v.ndens * v.ndens / v.rho;
-    double fl = cooling_floor(c, v);
+    // FORM 2 forms the floors' cooling in FP32 with its rates
+    double fl = FORM == 2 ? 0.0 : cooling_floor(c, v);
     fr_consts frc;
     if (FORM == 1) frc = make_fr(p, v);
-    if (FORM == 2) make_fr32(c, v, fl, frc);
+    if (FORM == 2) make_fr32(c, v, frc);
     if (p.int_method == 1) {
         // Euler, heatCool.F90:119-214
         int ncount = 0;
@@ -681,7 +735,7 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
                 dt0 = (timestep - total_time);
                 ei = eiolder + dei * dt0;
                 temp = ei / v.TtoEI;
-                if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update<FORM>(c, v, temp, d);
+                if (p.useDustCool && temp <= p.dust_sputter_temp) dust_after_step<FORM>(c, v, frc, temp, d);
                 total_time = total_time + dt0;
                 continue;
             }
@@ -697,7 +751,7 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
                 ei = zero<FORM>(c, v, frc, fl, v.TtoEI * 1.0, v.TtoEI * 1.0e9, eiolder, 3e-16,
                           fmx(v.TtoEI * c.brent_tol_K, eiold * err_tol), dt0, d);
             temp = ei / v.TtoEI;
-            if (p.useDustCool && temp <= p.dust_sputter_temp) dust_update<FORM>(c, v, temp, d);
+            if (p.useDustCool && temp <= p.dust_sputter_temp) dust_after_step<FORM>(c, v, frc, temp, d);
             total_time = total_time + dt0;
         }
         if (temp < p.absTmin) {

@@ -165,12 +165,13 @@ static __device__ float dei_parts(const gb_cool_pf& p, const gb_cool_tabf& t, co
 // T_dust after a step (heatCool.F90:430-443 + get_dust_temperature,
 // :703-884) in FP32: dust heating by FUV photons that did not eject
 // photo-electrons plus cosmic rays, Newton on the dust energy balance
+template <bool ACC = false>
 static __device__ float dust_temperature(const gb_cool_pf& p, const gb_cool_varsf& v, float T, float tdust_in)
 {
     const float sqT = sqrtf(T);
     const float lam_j = v.ndens / v.rho * sqrtf(p.jeansK * T / v.ndens);
     const float ncol = lam_j * v.ndens;
-    const float G = v.Gflux + p.Gzero * __expf(-3.5f * (ncol * 0.01f / 1.87e21f));
+    const float G = v.Gflux + p.Gzero * ex<ACC>(-3.5f * (ncol * 0.01f / 1.87e21f));
     // dust heating / (n 1e-33): photo-electric remainder + CR heating * rho
     float heat = 0.0f;
     const float ulpe = fmn(p.theatmax, p.dust_sputter_temp);
@@ -179,13 +180,13 @@ static __device__ float dust_temperature(const gb_cool_pf& p, const gb_cool_vars
         float eff = 0.05f, dh;
         if (p.pe_recipe == 0) {
             float Gf = G * sqT / (xl * v.ndens);
-            float gp = Gf > 0.0f ? __logf(Gf) : -1e30f;
-            eff = (7.64f + 4.52f * __expf(0.132f * __logf(T))) /
-                  (1.0f + (0.04371f * __expf(0.452f * gp)) * (1.0f + 0.00557f * __expf(0.675f * gp)));
+            float gp = Gf > 0.0f ? lg<ACC>(Gf) : -1e30f;
+            eff = (7.64f + 4.52f * ex<ACC>(0.132f * lg<ACC>(T))) /
+                  (1.0f + (0.04371f * ex<ACC>(0.452f * gp)) * (1.0f + 0.00557f * ex<ACC>(0.675f * gp)));
             dh = fmx((p.pe_norm * 1e26f - eff) * G * 1e7f, 0.0f);  // (pe_norm - 1e-26 eff) G n / (n 1e-33)
         } else if (p.pe_recipe == 1) {
             float Gf = G * sqT / (xl * v.ndens * 0.5f);
-            eff = 4.9e-2f / (1.0f + 4.0e-3f * __powf(Gf, 0.73f)) + 3.7e-2f * __powf(T * 1e-4f, 0.7f) / (1.0f + 2.0e-4f * Gf);
+            eff = 4.9e-2f / (1.0f + 4.0e-3f * pwr<ACC>(Gf, 0.73f)) + 3.7e-2f * pwr<ACC>(T * 1e-4f, 0.7f) / (1.0f + 2.0e-4f * Gf);
             dh = p.pe_norm * 1e33f * fmx(0.0f, 1.0f - eff) * G;
         } else {
             dh = p.pe_norm * 1e33f * 0.95f * G;
@@ -195,14 +196,14 @@ static __device__ float dust_temperature(const gb_cool_pf& p, const gb_cool_vars
     if (p.use_cr_heating && T <= p.theatmax && T >= p.theatmin) {
         float cr = v.cr_pref;
         if (!p.cr_uniform)
-            cr *= __expf(-p.crIonExp * (__logf(fmx(p.crIonNH, ncol)) - p.lnNH));
+            cr *= ex<ACC>(-p.crIonExp * (lg<ACC>(fmx(p.crIonNH, ncol)) - p.lnNH));
         cr *= ramp_T(T, p.theatmin, p.theatmax);
         heat += cr * (v.rho / v.ndens) * 1e33f;
     }
     const float absTmin = p.absTmin;
     float td = tdust_in < absTmin ? absTmin : tdust_in;
     const float tg = T < absTmin ? absTmin : T;
-    const float cfac = 3.8f * v.ndens * (1.0f - 0.8f * __expf(-75.0f / tg)) * sqrtf(tg);
+    const float cfac = 3.8f * v.ndens * (1.0f - 0.8f * ex<ACC>(-75.0f / tg)) * sqrtf(tg);
     float err = 1e-3f;
     for (int l = 0; l < 100 && err > 1e-4f; ++l) {
         float t3 = td * td * td;
@@ -235,12 +236,13 @@ __device__ __forceinline__ void make_vars(const gb_cool_pf& p, const gb_cool_var
 }
 
 // cooling at the floors (heatCool.F90:1509-1519) in FP32
+template <bool ACC = false>
 static __device__ float cooling_floor(const gb_cool_pf& p, const gb_cool_tabf& t, const gb_cool_varsf& v)
 {
     float emin = 0.0f;
     const float T = p.tradmin;
     if (T <= p.tradmax && T >= p.tradmin && v.ndens >= p.dradmin && v.ndens <= p.dradmax) {
-        emin = radloss(T);
+        emin = radloss<ACC>(T);
         if (v.xHp > 1e-2f && T < 1.2e4f) {
             float DG = lin(1e-2f, 1.0f, 1e-1f, 5.0f, fmn(1e-1f, v.xHp));
             emin *= DG;

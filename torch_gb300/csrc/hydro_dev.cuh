@@ -29,6 +29,11 @@ constexpr int MAXW = 7;
 constexpr int RB = 18;     // reconstruction band: cells 3..20
 constexpr int RLO = GB_NGUARD - 1;
 constexpr int NRC = RB * RB * RB;
+// time-n edge fields for the half-step normal field of the Riemann
+// problems: edges along c at A - 1/2, B - 1/2 (A, B in 3..21 along c + 1,
+// c + 2) and cell C (3..20) along c, per direction
+constexpr int EB = RB + 1;
+constexpr int NEN = EB * EB * RB;
 constexpr int LO = GB_NGUARD, HI = GB_NGUARD + GB_NXB - 1;
 constexpr int NFC = 17 * RB * RB;             // faces per direction in the flux box
 constexpr int NFLX = 10;                      // 8 fluxes + rho*e_int flux + face velocity
@@ -53,8 +58,11 @@ struct scratch_layout {
     // the edge fields' cell-centred reference, -(v x B)_d of the mean face
     // state along d, per direction and band cell (T)
     static constexpr size_t ecc = (size_t)3 * NRC;
+    // MHD: the time-n edge fields of the normal-field half step (T)
+    static constexpr size_t edgen = (size_t)3 * NEN;
     static constexpr size_t bytes = recon * sizeof(T) + flux * sizeof(T) + (emf + fb) * sizeof(double) +
-                                    prim32 * sizeof(float) + divu * sizeof(T) + ecc * sizeof(T);
+                                    prim32 * sizeof(float) + divu * sizeof(T) + ecc * sizeof(T) +
+                                    edgen * sizeof(T);
 };
 // the FP32 copy of each block starts on a 16-byte boundary (k_prim32 stores
 // four cells at a time): every section before it and its own stride are
@@ -429,6 +437,9 @@ struct hydro_kparams {
     // the edge fields' reference per direction and band cell (T, 3 x NRC
     // per chunk block), written by the reconstruction
     void* ecc = nullptr;
+    // the time-n edge fields (T, 3 x NEN per chunk block), written by
+    // k_edge_n, read by the Riemann solves for the half-step normal field
+    const void* edgen = nullptr;
     // per-cell CFL codes of the interior cells (store block x 3 directions
     // x 4096 bytes; null: not kept), read by the next CFL limit
     unsigned char* cflc = nullptr;
@@ -1063,6 +1074,76 @@ __device__ __forceinline__ void hlld(T gam, const T* L, const T* R, T* F, T* un)
 // (18), x fastest whatever d is, so that neighbouring threads read
 // neighbouring cells and faces in every direction (a normal-first order
 // puts neighbouring y and z faces 18 and 324 cells apart)
+// ---- the normal field of the Riemann problems at t + dt/2
+// (Gardiner & Stone 2005 sec. 4, 2008 sec. 5): dB_d/dt = -(d_a E_b - d_b E_a)
+// over half a step with time-n edge fields, each the mean of the four
+// cell-centred E_c = v_b B_a - v_a B_b around the edge (a = c + 1, b = c + 2
+// cyclically), summed in a fixed order. Only the edges some flux-box face
+// needs are formed: at most one of A, B outside the interior faces 4..20,
+// so every cell read lies in the step's filled read region.
+__device__ __forceinline__ int en_index(int A, int B, int C)
+{
+    return (A - RLO) + EB * ((B - RLO) + EB * (C - RLO));
+}
+
+template <typename T, bool MHD>
+__global__ void __launch_bounds__(128)
+k_edge_n(gb_dev_grid g, const int* __restrict__ list, const float* __restrict__ p32, size_t p32_stride,
+         T* __restrict__ escr, size_t estride)
+{
+    const int cb = blockIdx.y;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!MHD || q >= 3 * NEN) return;
+    const int c = q / NEN, e = q % NEN;
+    const int A = RLO + e % EB, B = RLO + (e / EB) % EB, C = RLO + e / (EB * EB);
+    T* out = escr + (size_t)cb * estride + q;
+    if ((A < LO || A > HI + 1) && (B < LO || B > HI + 1)) {
+        *out = (T)0;  // no face needs it (and its corner cell is not filled)
+        return;
+    }
+    const int a = c == 2 ? 0 : c + 1, bb = c == 0 ? 2 : c - 1;
+    const int blk = list[cb];
+    const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
+    const float* pb = p32 + (size_t)cb * p32_stride;
+    T ev[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        int x[3];
+        x[a] = A - 1 + (m >> 1);
+        x[bb] = B - 1 + (m & 1);
+        x[c] = C;
+        const int ci = gb_cidx(x[0], x[1], x[2]);
+        T va, vb, Ba, Bb;
+        if constexpr (std::is_same<T, float>::value) {
+            va = pb[(size_t)(1 + a) * GB_N3 + ci];
+            vb = pb[(size_t)(1 + bb) * GB_N3 + ci];
+            Ba = pb[(size_t)(5 + a) * GB_N3 + ci];
+            Bb = pb[(size_t)(5 + bb) * GB_N3 + ci];
+        } else {
+            va = base[(int64_t)g.slot[GB_VELX + a] * GB_N3 + ci];
+            vb = base[(int64_t)g.slot[GB_VELX + bb] * GB_N3 + ci];
+            Ba = base[(int64_t)g.slot[GB_MAGX + a] * GB_N3 + ci];
+            Bb = base[(int64_t)g.slot[GB_MAGX + bb] * GB_N3 + ci];
+        }
+        ev[m] = vb * Ba - va * Bb;
+    }
+    *out = (T)0.25 * (((ev[0] + ev[1]) + ev[2]) + ev[3]);
+}
+
+// the half-step normal field of flux-box face (I) of direction D
+template <typename T, int D>
+__device__ __forceinline__ T face_b_half(T bnf, const T* en, const int* I, const T* dtd)
+{
+    constexpr int d = D, a = (D + 1) % 3, bb = (D + 2) % 3;
+    // edges along bb (their c + 1 = d, c + 2 = a) at a -/+ 1/2; along a
+    // (c + 1 = bb, c + 2 = d) at bb -/+ 1/2
+    const T eb_lo = en[(size_t)bb * NEN + en_index(I[d], I[a], I[bb])];
+    const T eb_hi = en[(size_t)bb * NEN + en_index(I[d], I[a] + 1, I[bb])];
+    const T ea_lo = en[(size_t)a * NEN + en_index(I[bb], I[d], I[a])];
+    const T ea_hi = en[(size_t)a * NEN + en_index(I[bb] + 1, I[d], I[a])];
+    return bnf - (T)0.5 * (dtd[a] * (eb_hi - eb_lo) - dtd[bb] * (ea_hi - ea_lo));
+}
+
 __device__ __forceinline__ void flux_coords(int d, int f, int* I)
 {
     const int n0 = d == 0 ? 17 : RB, n1 = d == 1 ? 17 : RB;
@@ -1189,7 +1270,14 @@ __device__ __forceinline__ void flux_face(gb_dev_grid g, hydro_kparams kp, const
         wr[v] = rs[((size_t)(1 * 3 + d) * NP + v) * NRC + cr];
     }
     const float* pb = p32 + (size_t)cb * p32_stride;
-    const T bnf = MHD ? face_b<T>(g, d, blk, gb_fidx(d, I[0], I[1], I[2]), pb) : (T)0;
+    T bnf = (T)0;
+    if (MHD) {
+        T dtd[3];
+        if constexpr (std::is_same<T, float>::value) kp_dtdxf(kp, gb_block_level(g, blk), dtd);
+        else kp_dtdx(kp, gb_block_level(g, blk), dtd);
+        bnf = face_b_half<T, D>(face_b<T>(g, d, blk, gb_fidx(d, I[0], I[1], I[2]), pb),
+                                (const T*)kp.edgen + (size_t)cb * scratch_layout<T>::edgen, I, dtd);
+    }
     const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
     auto U = [&](int role, int ci) -> T {
         if constexpr (std::is_same<T, float>::value) {
@@ -1571,7 +1659,7 @@ __device__ __forceinline__ double rcp_newton(double x)
 // (64 registers, no spills); the FP64 path and the fused integrator need
 // more registers than that
 template <typename T, bool MHD, int COOL, bool FEAT>
-__global__ void __launch_bounds__(128, (std::is_same<T, float>::value && !COOL) ? 8 : 1)
+__global__ void __launch_bounds__(128, (std::is_same<T, float>::value && !COOL) ? 8 : COOL == 2 ? 3 : 1)
 k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restrict__ list,
          const T* __restrict__ fscr, size_t fstride, const double* __restrict__ bscr, size_t bstride,
          gb_status* st, sur_feat_out sf)

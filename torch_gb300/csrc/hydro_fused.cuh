@@ -119,6 +119,12 @@ k_recon_flux(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* _
     const int tid = threadIdx.x, lane = tid % FT, d = tid / FT;
     const int cb = blockIdx.x;
     const int blk = list[cb];
+    // the half-step normal field of the Riemann problems (k_edge_n's
+    // time-n edge fields of this block)
+    T dtdh[3];
+    if constexpr (std::is_same<T, float>::value) kp_dtdxf(kp, gb_block_level(g, blk), dtdh);
+    else kp_dtdx(kp, gb_block_level(g, blk), dtdh);
+    const T* enb = (const T*)kp.edgen + (size_t)cb * scratch_layout<T>::edgen;
     T gam, dtd[3], hd[3];
     recon_consts<T>(g, kp, blk, gam, dtd, hd);
     const float* p32b = p32 + (size_t)cb * p32_stride;
@@ -257,15 +263,18 @@ k_recon_flux(gb_dev_grid g, hydro_kparams kp, const int* __restrict__ list, T* _
             T* fs = fscr + (size_t)cb * fstride + (size_t)dir * NFLX * NFC;
             const int fi = flux_index(dir, I[0], I[1], I[2]);
             if (dir == 0) {
-                const T bnf = MHD ? face_b<T>(g, 0, blk, gb_fidx(0, I[0], I[1], I[2]), p32b) : (T)0;
+                const T bnf = MHD ? face_b_half<T, 0>(face_b<T>(g, 0, blk, gb_fidx(0, I[0], I[1], I[2]), p32b), enb, I, dtdh)
+                                  : (T)0;
                 face_flux_core<T, MHD, 0>(kp, wl, wr, bnf, U, cil, cir, out, feint, un);
                 face_flux_store<T, MHD, 0>(fs, fi, out, feint, un);
             } else if (dir == 1) {
-                const T bnf = MHD ? face_b<T>(g, 1, blk, gb_fidx(1, I[0], I[1], I[2]), p32b) : (T)0;
+                const T bnf = MHD ? face_b_half<T, 1>(face_b<T>(g, 1, blk, gb_fidx(1, I[0], I[1], I[2]), p32b), enb, I, dtdh)
+                                  : (T)0;
                 face_flux_core<T, MHD, 1>(kp, wl, wr, bnf, U, cil, cir, out, feint, un);
                 face_flux_store<T, MHD, 1>(fs, fi, out, feint, un);
             } else {
-                const T bnf = MHD ? face_b<T>(g, 2, blk, gb_fidx(2, I[0], I[1], I[2]), p32b) : (T)0;
+                const T bnf = MHD ? face_b_half<T, 2>(face_b<T>(g, 2, blk, gb_fidx(2, I[0], I[1], I[2]), p32b), enb, I, dtdh)
+                                  : (T)0;
                 face_flux_core<T, MHD, 2>(kp, wl, wr, bnf, U, cil, cir, out, feint, un);
                 face_flux_store<T, MHD, 2>(fs, fi, out, feint, un);
             }

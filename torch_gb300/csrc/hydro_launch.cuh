@@ -92,7 +92,7 @@ int launch_chunk(const hydro_kparams& kp_in, int mhd, int cool, int nblk, const 
 {
     using SL = scratch_layout<T>;
     // scratch of the chunk: [recon | flux | emf | faceb | prim32 | divu |
-    // ecc], each block-major
+    // ecc | edgen], each block-major
     char* base = (char*)scratch;
     T* rscr = (T*)base;
     T* fscr = (T*)(base + (size_t)nblk * SL::recon * sizeof(T));
@@ -101,9 +101,11 @@ int launch_chunk(const hydro_kparams& kp_in, int mhd, int cool, int nblk, const 
     float* p32 = (float*)(bscr + (size_t)nblk * SL::fb);
     T* dscr = (T*)(p32 + (size_t)nblk * SL::prim32);
     T* cscr = dscr + (size_t)nblk * SL::divu;
+    T* nscr = cscr + (size_t)nblk * SL::ecc;
     hydro_kparams kp = kp_in;
     kp.divu = dscr;
     kp.ecc = cscr;
+    kp.edgen = nscr;
     const gb_dev_grid& g = g_gb.grid;
     if constexpr (SL::prim32 > 0) {
         dim3 pg((GB_STEP_CELLS / 4 + (mhd ? GB_STEP_FACES_ALL : 0) + 127) / 128, nblk);
@@ -117,6 +119,12 @@ int launch_chunk(const hydro_kparams& kp_in, int mhd, int cool, int nblk, const 
         if (mhd) k_divu<T, true><<<dim3(1, nblk), DIVU_THREADS, 0, s>>>(g, list, p32, SL::prim32, dscr, SL::divu);
         else k_divu<T, false><<<dim3(1, nblk), DIVU_THREADS, 0, s>>>(g, list, p32, SL::prim32, dscr, SL::divu);
         gb_prof_end(GBP_RECON, s);
+    }
+    if (mhd) {
+        // time-n edge fields for the Riemann problems' half-step normal field
+        gb_prof_begin(GBP_FLUX, s);
+        k_edge_n<T, true><<<dim3((3 * NEN + 127) / 128, nblk), 128, 0, s>>>(g, list, p32, SL::prim32, nscr, SL::edgen);
+        gb_prof_end(GBP_FLUX, s);
     }
     const int tile = gb_recon_tile();
     dim3 rg((NRC + tile - 1) / tile, nblk);
