@@ -666,18 +666,24 @@ static __device__ int zbrac(const gb_cool_ctx& c, const gb_cool_vars& v, const f
                      double* x1, double* x2, double xold, double dt)
 {
     // heatCool.F90:2294-2348
+    // FORM 2 takes the sign and magnitude tests on the integer pipe (the
+    // same decisions: a product of two energies-sized residuals never
+    // underflows, so f1 f2 < 0 is opposite nonzero signs)
     const double FACTOR = 1.6;
     double f1 = one_step<FORM>(c, v, f, floor_, dt, *x1, xold);
     double f2 = one_step<FORM>(c, v, f, floor_, dt, *x2, xold);
     for (int j = 1; j <= 5000; ++j) {
-        if (f1 * f2 < 0.0) return 1;
-        if (fabs(f1) < fabs(f2)) {
+        if (FORM == 2 ? (((__double_as_longlong(f1) ^ __double_as_longlong(f2)) < 0) && mag_bits(f1) != 0ull &&
+                         mag_bits(f2) != 0ull)
+                      : f1 * f2 < 0.0)
+            return 1;
+        if (FORM == 2 ? mag_bits(f1) < mag_bits(f2) : fabs(f1) < fabs(f2)) {
             *x1 = *x1 + FACTOR * (*x1 - *x2);
-            if (*x1 < 0.0) *x1 = v.TtoEI * 1.0;
+            if (FORM == 2 ? __double_as_longlong(*x1) < 0 && mag_bits(*x1) != 0ull : *x1 < 0.0) *x1 = v.TtoEI * 1.0;
             f1 = one_step<FORM>(c, v, f, floor_, dt, *x1, xold);
         } else {
             *x2 = *x2 + FACTOR * (*x2 - *x1);
-            if (*x2 < 0.0) *x2 = v.TtoEI * 1.0;
+            if (FORM == 2 ? __double_as_longlong(*x2) < 0 && mag_bits(*x2) != 0ull : *x2 < 0.0) *x2 = v.TtoEI * 1.0;
             f2 = one_step<FORM>(c, v, f, floor_, dt, *x2, xold);
         }
     }

@@ -30,10 +30,12 @@ constexpr int RB = 18;     // reconstruction band: cells 3..20
 constexpr int RLO = GB_NGUARD - 1;
 constexpr int NRC = RB * RB * RB;
 // time-n edge fields for the half-step normal field of the Riemann
-// problems: edges along c at A - 1/2, B - 1/2 (A, B in 3..21 along c + 1,
-// c + 2) and cell C (3..20) along c, per direction
+// problems: per direction c a box of 19^3 positions (3..21 on every axis;
+// along c the index is a cell, across it an edge at index - 1/2), x fastest
+// whatever c, so that faces next to each other along x read edges next to
+// each other
 constexpr int EB = RB + 1;
-constexpr int NEN = EB * EB * RB;
+constexpr int NEN = EB * EB * EB;
 constexpr int LO = GB_NGUARD, HI = GB_NGUARD + GB_NXB - 1;
 constexpr int NFC = 17 * RB * RB;             // faces per direction in the flux box
 constexpr int NFLX = 10;                      // 8 fluxes + rho*e_int flux + face velocity
@@ -1081,9 +1083,9 @@ __device__ __forceinline__ void hlld(T gam, const T* L, const T* R, T* F, T* un)
 // cyclically), summed in a fixed order. Only the edges some flux-box face
 // needs are formed: at most one of A, B outside the interior faces 4..20,
 // so every cell read lies in the step's filled read region.
-__device__ __forceinline__ int en_index(int A, int B, int C)
+__device__ __forceinline__ int en_index(int x, int y, int z)
 {
-    return (A - RLO) + EB * ((B - RLO) + EB * (C - RLO));
+    return (x - RLO) + EB * ((y - RLO) + EB * (z - RLO));
 }
 
 template <typename T, bool MHD>
@@ -1095,13 +1097,15 @@ k_edge_n(gb_dev_grid g, const int* __restrict__ list, const float* __restrict__ 
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (!MHD || q >= 3 * NEN) return;
     const int c = q / NEN, e = q % NEN;
-    const int A = RLO + e % EB, B = RLO + (e / EB) % EB, C = RLO + e / (EB * EB);
+    int X[3] = {RLO + e % EB, RLO + (e / EB) % EB, RLO + e / (EB * EB)};
     T* out = escr + (size_t)cb * estride + q;
-    if ((A < LO || A > HI + 1) && (B < LO || B > HI + 1)) {
+    const int a = c == 2 ? 0 : c + 1, bb = c == 0 ? 2 : c - 1;
+    // A along a and B along bb locate the edge, C along c its cell
+    const int A = X[a], B = X[bb], C = X[c];
+    if (((A < LO || A > HI + 1) && (B < LO || B > HI + 1)) || C > HI + 1) {
         *out = (T)0;  // no face needs it (and its corner cell is not filled)
         return;
     }
-    const int a = c == 2 ? 0 : c + 1, bb = c == 0 ? 2 : c - 1;
     const int blk = list[cb];
     const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
     const float* pb = p32 + (size_t)cb * p32_stride;
@@ -1135,12 +1139,15 @@ template <typename T, int D>
 __device__ __forceinline__ T face_b_half(T bnf, const T* en, const int* I, const T* dtd)
 {
     constexpr int d = D, a = (D + 1) % 3, bb = (D + 2) % 3;
-    // edges along bb (their c + 1 = d, c + 2 = a) at a -/+ 1/2; along a
-    // (c + 1 = bb, c + 2 = d) at bb -/+ 1/2
-    const T eb_lo = en[(size_t)bb * NEN + en_index(I[d], I[a], I[bb])];
-    const T eb_hi = en[(size_t)bb * NEN + en_index(I[d], I[a] + 1, I[bb])];
-    const T ea_lo = en[(size_t)a * NEN + en_index(I[bb], I[d], I[a])];
-    const T ea_hi = en[(size_t)a * NEN + en_index(I[bb] + 1, I[d], I[a])];
+    // edges along bb at a -/+ 1/2 and along a at bb -/+ 1/2, each at the
+    // face's own position otherwise (x, y, z addressing)
+    int Ia[3] = {I[0], I[1], I[2]}, Ib[3] = {I[0], I[1], I[2]};
+    Ia[a] += 1;
+    Ib[bb] += 1;
+    const T eb_lo = en[(size_t)bb * NEN + en_index(I[0], I[1], I[2])];
+    const T eb_hi = en[(size_t)bb * NEN + en_index(Ia[0], Ia[1], Ia[2])];
+    const T ea_lo = en[(size_t)a * NEN + en_index(I[0], I[1], I[2])];
+    const T ea_hi = en[(size_t)a * NEN + en_index(Ib[0], Ib[1], Ib[2])];
     return bnf - (T)0.5 * (dtd[a] * (eb_hi - eb_lo) - dtd[bb] * (ea_hi - ea_lo));
 }
 
