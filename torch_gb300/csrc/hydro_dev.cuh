@@ -276,32 +276,82 @@ __device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* 
     // intervals, each formed once: cell m's limited slope takes intervals
     // m - 1 and m (the same sums, in the same order, as forming both per cell)
     T ld[4][MAXW];
-#pragma unroll
-    for (int m = 0; m < 4; ++m)
-#pragma unroll
-        for (int k = 0; k < nw; ++k) {
-            T acc = (T)0;
-#pragma unroll
-            for (int s = 0; s < nw; ++s) {
-                const int qq = wslot(s);
-                if (!nz_L<MHD>(k, s)) continue;
-                acc = acc + L[k][s] * (qs[m + 1][qq] - qs[m][qq]);
-            }
-            ld[m][k] = acc;
-        }
     T dwm[3][MAXW];
-#pragma unroll
-    for (int m = 1; m <= 3; ++m) {
-        T da[MAXW];
-#pragma unroll
-        for (int k = 0; k < nw; ++k) da[k] = minmod<T>(ld[m - 1][k], ld[m][k]);
+    if constexpr (std::is_same<T, float>::value) {
+        // FP32: the projections that share a matrix row run as packed pairs
+        // (fma.rn.f32x2: two lanes per instruction, each lane the same
+        // rounding as the scalar fused multiply-add): intervals (0, 1) and
+        // (2, 3) of L . dq, and cells 1 and 2 of R . da
+        float2 d01[MAXW], d23[MAXW];
 #pragma unroll
         for (int s = 0; s < nw; ++s) {
-            T acc = (T)0;
+            const int qq = wslot(s);
+            d01[s] = make_float2(qs[1][qq] - qs[0][qq], qs[2][qq] - qs[1][qq]);
+            d23[s] = make_float2(qs[3][qq] - qs[2][qq], qs[4][qq] - qs[3][qq]);
+        }
+#pragma unroll
+        for (int k = 0; k < nw; ++k) {
+            float2 a01 = make_float2(0.0f, 0.0f), a23 = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int s = 0; s < nw; ++s) {
+                if (!nz_L<MHD>(k, s)) continue;
+                const float2 l2 = make_float2(L[k][s], L[k][s]);
+                a01 = __ffma2_rn(l2, d01[s], a01);
+                a23 = __ffma2_rn(l2, d23[s], a23);
+            }
+            ld[0][k] = a01.x;
+            ld[1][k] = a01.y;
+            ld[2][k] = a23.x;
+            ld[3][k] = a23.y;
+        }
+        float2 da12[MAXW];
+        float da3[MAXW];
+#pragma unroll
+        for (int k = 0; k < nw; ++k) {
+            da12[k] = make_float2(minmod<float>(ld[0][k], ld[1][k]), minmod<float>(ld[1][k], ld[2][k]));
+            da3[k] = minmod<float>(ld[2][k], ld[3][k]);
+        }
+#pragma unroll
+        for (int s = 0; s < nw; ++s) {
+            float2 a12 = make_float2(0.0f, 0.0f);
+            float a3 = 0.0f;
 #pragma unroll
             for (int k = 0; k < nw; ++k)
-                if (nz_R<MHD>(s, k)) acc = acc + R[s][k] * da[k];
-            dwm[m - 1][s] = acc;
+                if (nz_R<MHD>(s, k)) {
+                    a12 = __ffma2_rn(make_float2(R[s][k], R[s][k]), da12[k], a12);
+                    a3 = __fmaf_rn(R[s][k], da3[k], a3);
+                }
+            dwm[0][s] = a12.x;
+            dwm[1][s] = a12.y;
+            dwm[2][s] = a3;
+        }
+    } else {
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+#pragma unroll
+            for (int k = 0; k < nw; ++k) {
+                T acc = (T)0;
+#pragma unroll
+                for (int s = 0; s < nw; ++s) {
+                    const int qq = wslot(s);
+                    if (!nz_L<MHD>(k, s)) continue;
+                    acc = acc + L[k][s] * (qs[m + 1][qq] - qs[m][qq]);
+                }
+                ld[m][k] = acc;
+            }
+#pragma unroll
+        for (int m = 1; m <= 3; ++m) {
+            T da[MAXW];
+#pragma unroll
+            for (int k = 0; k < nw; ++k) da[k] = minmod<T>(ld[m - 1][k], ld[m][k]);
+#pragma unroll
+            for (int s = 0; s < nw; ++s) {
+                T acc = (T)0;
+#pragma unroll
+                for (int k = 0; k < nw; ++k)
+                    if (nz_R<MHD>(s, k)) acc = acc + R[s][k] * da[k];
+                dwm[m - 1][s] = acc;
+            }
         }
     }
     T WL[MAXW], WR[MAXW], dW[MAXW], W6[MAXW];
@@ -331,17 +381,35 @@ __device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* 
         W6[s] = (T)6 * (q0 - (T)0.5 * (wl + wr));
     }
     T ldW[MAXW], lW6[MAXW];
+    if constexpr (std::is_same<T, float>::value) {
+        // L . dW and L . W6 as one packed pair per matrix entry
+        float2 w2[MAXW];
 #pragma unroll
-    for (int k = 0; k < nw; ++k) {
-        T a = (T)0, b = (T)0;
+        for (int s = 0; s < nw; ++s) w2[s] = make_float2(dW[s], W6[s]);
 #pragma unroll
-        for (int s = 0; s < nw; ++s) {
-            if (!nz_L<MHD>(k, s)) continue;
-            a = a + L[k][s] * dW[s];
-            b = b + L[k][s] * W6[s];
+        for (int k = 0; k < nw; ++k) {
+            float2 ab = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int s = 0; s < nw; ++s) {
+                if (!nz_L<MHD>(k, s)) continue;
+                ab = __ffma2_rn(make_float2(L[k][s], L[k][s]), w2[s], ab);
+            }
+            ldW[k] = ab.x;
+            lW6[k] = ab.y;
         }
-        ldW[k] = a;
-        lW6[k] = b;
+    } else {
+#pragma unroll
+        for (int k = 0; k < nw; ++k) {
+            T a = (T)0, b = (T)0;
+#pragma unroll
+            for (int s = 0; s < nw; ++s) {
+                if (!nz_L<MHD>(k, s)) continue;
+                a = a + L[k][s] * dW[s];
+                b = b + L[k][s] * W6[s];
+            }
+            ldW[k] = a;
+            lW6[k] = b;
+        }
     }
     const T t3 = two3<T>();
     T sK = lam[nw - 1] * dtdx;
@@ -1088,50 +1156,84 @@ __device__ __forceinline__ int en_index(int x, int y, int z)
     return (x - RLO) + EB * ((y - RLO) + EB * (z - RLO));
 }
 
+// One CTA per block, direction c and half of the band along c (9 cells):
+// the cell-centred E_c of the 20 x 20 x 9 cells around its edges once into
+// shared memory, then each edge the mean of its four, written x-fastest.
+constexpr int EN_HALF = RB / 2;  // cells along c per CTA
+constexpr int EN_THREADS = 256;
+
+template <typename T, int C>
+__device__ __forceinline__ void edge_n_dir(const gb_dev_grid& g, int blk, const float* __restrict__ pb,
+                                           T* __restrict__ out, int half, T (*ec)[20][20])
+{
+    // ec: [along c][along bb][along a], positions 2..21 across
+    constexpr int c = C, a = (C + 1) % 3, bb = (C + 2) % 3;
+    constexpr int NCELL = EN_HALF * 20 * 20;
+    const int C0 = RLO + half * EN_HALF;
+    const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
+    for (int t = threadIdx.x; t < NCELL; t += EN_THREADS) {
+        const int ai = t % 20, bi = (t / 20) % 20, ci = t / 400;
+        int x[3];
+        x[a] = 2 + ai;
+        x[bb] = 2 + bi;
+        x[c] = C0 + ci;
+        T e = (T)0;
+        // cells outside the band along both a and bb lie outside the step's
+        // filled read region and feed only edges no face needs
+        if ((ai >= 1 && ai <= 18) || (bi >= 1 && bi <= 18)) {
+            const int cidx = gb_cidx(x[0], x[1], x[2]);
+            T va, vb, Ba, Bb;
+            if constexpr (std::is_same<T, float>::value) {
+                va = pb[(size_t)(1 + a) * GB_N3 + cidx];
+                vb = pb[(size_t)(1 + bb) * GB_N3 + cidx];
+                Ba = pb[(size_t)(5 + a) * GB_N3 + cidx];
+                Bb = pb[(size_t)(5 + bb) * GB_N3 + cidx];
+            } else {
+                va = base[(int64_t)g.slot[GB_VELX + a] * GB_N3 + cidx];
+                vb = base[(int64_t)g.slot[GB_VELX + bb] * GB_N3 + cidx];
+                Ba = base[(int64_t)g.slot[GB_MAGX + a] * GB_N3 + cidx];
+                Bb = base[(int64_t)g.slot[GB_MAGX + bb] * GB_N3 + cidx];
+            }
+            e = vb * Ba - va * Bb;
+        }
+        ec[ci][bi][ai] = e;
+    }
+    __syncthreads();
+    // edge positions x-fastest: 19 along each axis but c (9)
+    constexpr int E0 = c == 0 ? EN_HALF : EB, E1 = c == 1 ? EN_HALF : EB;
+    constexpr int NE = EN_HALF * EB * EB;
+    for (int t = threadIdx.x; t < NE; t += EN_THREADS) {
+        int X[3];
+        X[0] = (c == 0 ? C0 : RLO) + t % E0;
+        X[1] = (c == 1 ? C0 : RLO) + (t / E0) % E1;
+        X[2] = (c == 2 ? C0 : RLO) + t / (E0 * E1);
+        const int A = X[a], B = X[bb];
+        T v = (T)0;
+        if ((A >= LO && A <= HI + 1) || (B >= LO && B <= HI + 1)) {
+            // cells A - 1 + ia along a, B - 1 + ib along bb: shared index
+            // A - 3 + ia, B - 3 + ib
+            const int ci = X[c] - C0, a0 = A - RLO, b0 = B - RLO;
+            v = (T)0.25 * (((ec[ci][b0][a0] + ec[ci][b0 + 1][a0]) + ec[ci][b0][a0 + 1]) + ec[ci][b0 + 1][a0 + 1]);
+        }
+        out[(size_t)c * NEN + en_index(X[0], X[1], X[2])] = v;
+    }
+}
+
 template <typename T, bool MHD>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(EN_THREADS)
 k_edge_n(gb_dev_grid g, const int* __restrict__ list, const float* __restrict__ p32, size_t p32_stride,
          T* __restrict__ escr, size_t estride)
 {
+    if (!MHD) return;
     const int cb = blockIdx.y;
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!MHD || q >= 3 * NEN) return;
-    const int c = q / NEN, e = q % NEN;
-    int X[3] = {RLO + e % EB, RLO + (e / EB) % EB, RLO + e / (EB * EB)};
-    T* out = escr + (size_t)cb * estride + q;
-    const int a = c == 2 ? 0 : c + 1, bb = c == 0 ? 2 : c - 1;
-    // A along a and B along bb locate the edge, C along c its cell
-    const int A = X[a], B = X[bb], C = X[c];
-    if (((A < LO || A > HI + 1) && (B < LO || B > HI + 1)) || C > HI + 1) {
-        *out = (T)0;  // no face needs it (and its corner cell is not filled)
-        return;
-    }
     const int blk = list[cb];
-    const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
     const float* pb = p32 + (size_t)cb * p32_stride;
-    T ev[4];
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        int x[3];
-        x[a] = A - 1 + (m >> 1);
-        x[bb] = B - 1 + (m & 1);
-        x[c] = C;
-        const int ci = gb_cidx(x[0], x[1], x[2]);
-        T va, vb, Ba, Bb;
-        if constexpr (std::is_same<T, float>::value) {
-            va = pb[(size_t)(1 + a) * GB_N3 + ci];
-            vb = pb[(size_t)(1 + bb) * GB_N3 + ci];
-            Ba = pb[(size_t)(5 + a) * GB_N3 + ci];
-            Bb = pb[(size_t)(5 + bb) * GB_N3 + ci];
-        } else {
-            va = base[(int64_t)g.slot[GB_VELX + a] * GB_N3 + ci];
-            vb = base[(int64_t)g.slot[GB_VELX + bb] * GB_N3 + ci];
-            Ba = base[(int64_t)g.slot[GB_MAGX + a] * GB_N3 + ci];
-            Bb = base[(int64_t)g.slot[GB_MAGX + bb] * GB_N3 + ci];
-        }
-        ev[m] = vb * Ba - va * Bb;
-    }
-    *out = (T)0.25 * (((ev[0] + ev[1]) + ev[2]) + ev[3]);
+    T* out = escr + (size_t)cb * estride;
+    __shared__ T ec[EN_HALF][20][20];
+    const int c = blockIdx.x >> 1, half = blockIdx.x & 1;
+    if (c == 0) edge_n_dir<T, 0>(g, blk, pb, out, half, ec);
+    else if (c == 1) edge_n_dir<T, 1>(g, blk, pb, out, half, ec);
+    else edge_n_dir<T, 2>(g, blk, pb, out, half, ec);
 }
 
 // the half-step normal field of flux-box face (I) of direction D

@@ -122,9 +122,10 @@ int launch_chunk(const hydro_kparams& kp_in, int mhd, int cool, int nblk, const 
     }
     if (mhd) {
         // time-n edge fields for the Riemann problems' half-step normal field
-        gb_prof_begin(GBP_FLUX, s);
-        k_edge_n<T, true><<<dim3((3 * NEN + 127) / 128, nblk), 128, 0, s>>>(g, list, p32, SL::prim32, nscr, SL::edgen);
-        gb_prof_end(GBP_FLUX, s);
+        // (timed with the edge-field kernels)
+        gb_prof_begin(GBP_EMF, s);
+        k_edge_n<T, true><<<dim3(6, nblk), EN_THREADS, 0, s>>>(g, list, p32, SL::prim32, nscr, SL::edgen);
+        gb_prof_end(GBP_EMF, s);
     }
     const int tile = gb_recon_tile();
     dim3 rg((NRC + tile - 1) / tile, nblk);
