@@ -569,8 +569,13 @@ static __device__ double zero(const gb_cool_ctx& c, const gb_cool_vars& v, const
     // acceptance test and bisection fallback then treat alike); the iterates,
     // the bracket and the tolerance stay FP64.
     double sa = a, sb = b;
-    double fa = one_step<FORM>(c, v, f, floor_, dt, sa, a_old);
-    double fb = one_step<FORM>(c, v, f, floor_, dt, sb, a_old);
+    double fa = 0.0, fb = 0.0;
+#pragma unroll 1
+    for (int i = 0; i < 2; ++i) {  // one call site for both (see zbrac)
+        const double fv = one_step<FORM>(c, v, f, floor_, dt, i == 0 ? sa : sb, a_old);
+        if (i == 0) fa = fv;
+        else fb = fv;
+    }
     double cc = sa, fc = fa, e = sb - sa, dd = e;
     int n_tries = 0;
     if ((fa > 0.0 && fb > 0.0) || (fa < 0.0 && fb < 0.0)) {
@@ -669,22 +674,32 @@ static __device__ int zbrac(const gb_cool_ctx& c, const gb_cool_vars& v, const f
     // FORM 2 takes the sign and magnitude tests on the integer pipe (the
     // same decisions: a product of two energies-sized residuals never
     // underflows, so f1 f2 < 0 is opposite nonzero signs)
+    // The residual is evaluated at one call site in the loop (and one for
+    // the two starting points): the rate function is long, and copies of it
+    // at every call site overflowed the instruction cache.
     const double FACTOR = 1.6;
-    double f1 = one_step<FORM>(c, v, f, floor_, dt, *x1, xold);
-    double f2 = one_step<FORM>(c, v, f, floor_, dt, *x2, xold);
+    double f1 = 0.0, f2 = 0.0;
+#pragma unroll 1
+    for (int i = 0; i < 2; ++i) {
+        const double fv = one_step<FORM>(c, v, f, floor_, dt, i == 0 ? *x1 : *x2, xold);
+        if (i == 0) f1 = fv;
+        else f2 = fv;
+    }
     for (int j = 1; j <= 5000; ++j) {
         if (FORM == 2 ? (((__double_as_longlong(f1) ^ __double_as_longlong(f2)) < 0) && mag_bits(f1) != 0ull &&
                          mag_bits(f2) != 0ull)
                       : f1 * f2 < 0.0)
             return 1;
-        if (FORM == 2 ? mag_bits(f1) < mag_bits(f2) : fabs(f1) < fabs(f2)) {
-            *x1 = *x1 + FACTOR * (*x1 - *x2);
-            if (FORM == 2 ? __double_as_longlong(*x1) < 0 && mag_bits(*x1) != 0ull : *x1 < 0.0) *x1 = v.TtoEI * 1.0;
-            f1 = one_step<FORM>(c, v, f, floor_, dt, *x1, xold);
+        const bool first = FORM == 2 ? mag_bits(f1) < mag_bits(f2) : fabs(f1) < fabs(f2);
+        double xn = first ? *x1 + FACTOR * (*x1 - *x2) : *x2 + FACTOR * (*x2 - *x1);
+        if (FORM == 2 ? __double_as_longlong(xn) < 0 && mag_bits(xn) != 0ull : xn < 0.0) xn = v.TtoEI * 1.0;
+        const double fn = one_step<FORM>(c, v, f, floor_, dt, xn, xold);
+        if (first) {
+            *x1 = xn;
+            f1 = fn;
         } else {
-            *x2 = *x2 + FACTOR * (*x2 - *x1);
-            if (FORM == 2 ? __double_as_longlong(*x2) < 0 && mag_bits(*x2) != 0ull : *x2 < 0.0) *x2 = v.TtoEI * 1.0;
-            f2 = one_step<FORM>(c, v, f, floor_, dt, *x2, xold);
+            *x2 = xn;
+            f2 = fn;
         }
     }
     return 0;

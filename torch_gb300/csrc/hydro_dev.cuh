@@ -1164,23 +1164,27 @@ constexpr int EN_THREADS = 256;
 
 template <typename T, int C>
 __device__ __forceinline__ void edge_n_dir(const gb_dev_grid& g, int blk, const float* __restrict__ pb,
-                                           T* __restrict__ out, int half, T (*ec)[20][20])
+                                           T* __restrict__ out, int half, T* ec)
 {
-    // ec: [along c][along bb][along a], positions 2..21 across
+    // ec: the cells' E_c over a box of 9 cells along c (this CTA's half)
+    // and 20 across (2..21), x fastest like the store: both passes run x
+    // fastest, so global loads coalesce and shared accesses do not conflict
     constexpr int c = C, a = (C + 1) % 3, bb = (C + 2) % 3;
-    constexpr int NCELL = EN_HALF * 20 * 20;
+    constexpr int X0 = c == 0 ? EN_HALF : 20, X1 = c == 1 ? EN_HALF : 20, X2 = c == 2 ? EN_HALF : 20;
+    constexpr int NCELL = X0 * X1 * X2;
+    constexpr int SA = a == 0 ? 1 : (a == 1 ? X0 : X0 * X1), SB = bb == 0 ? 1 : (bb == 1 ? X0 : X0 * X1);
     const int C0 = RLO + half * EN_HALF;
+    const int o[3] = {c == 0 ? C0 : RLO - 1, c == 1 ? C0 : RLO - 1, c == 2 ? C0 : RLO - 1};
     const double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
     for (int t = threadIdx.x; t < NCELL; t += EN_THREADS) {
-        const int ai = t % 20, bi = (t / 20) % 20, ci = t / 400;
         int x[3];
-        x[a] = 2 + ai;
-        x[bb] = 2 + bi;
-        x[c] = C0 + ci;
+        x[0] = o[0] + t % X0;
+        x[1] = o[1] + (t / X0) % X1;
+        x[2] = o[2] + t / (X0 * X1);
         T e = (T)0;
         // cells outside the band along both a and bb lie outside the step's
         // filled read region and feed only edges no face needs
-        if ((ai >= 1 && ai <= 18) || (bi >= 1 && bi <= 18)) {
+        if ((x[a] >= RLO && x[a] <= RLO + RB - 1) || (x[bb] >= RLO && x[bb] <= RLO + RB - 1)) {
             const int cidx = gb_cidx(x[0], x[1], x[2]);
             T va, vb, Ba, Bb;
             if constexpr (std::is_same<T, float>::value) {
@@ -1196,10 +1200,10 @@ __device__ __forceinline__ void edge_n_dir(const gb_dev_grid& g, int blk, const 
             }
             e = vb * Ba - va * Bb;
         }
-        ec[ci][bi][ai] = e;
+        ec[t] = e;
     }
     __syncthreads();
-    // edge positions x-fastest: 19 along each axis but c (9)
+    // edge positions: 19 along each axis but c (9), x fastest
     constexpr int E0 = c == 0 ? EN_HALF : EB, E1 = c == 1 ? EN_HALF : EB;
     constexpr int NE = EN_HALF * EB * EB;
     for (int t = threadIdx.x; t < NE; t += EN_THREADS) {
@@ -1210,10 +1214,9 @@ __device__ __forceinline__ void edge_n_dir(const gb_dev_grid& g, int blk, const 
         const int A = X[a], B = X[bb];
         T v = (T)0;
         if ((A >= LO && A <= HI + 1) || (B >= LO && B <= HI + 1)) {
-            // cells A - 1 + ia along a, B - 1 + ib along bb: shared index
-            // A - 3 + ia, B - 3 + ib
-            const int ci = X[c] - C0, a0 = A - RLO, b0 = B - RLO;
-            v = (T)0.25 * (((ec[ci][b0][a0] + ec[ci][b0 + 1][a0]) + ec[ci][b0][a0 + 1]) + ec[ci][b0 + 1][a0 + 1]);
+            // the cell at A - 1, B - 1 and its neighbours +1 along a and bb
+            const int s00 = (X[0] - o[0]) + X0 * ((X[1] - o[1]) + X1 * (X[2] - o[2])) - SA - SB;
+            v = (T)0.25 * (((ec[s00] + ec[s00 + SB]) + ec[s00 + SA]) + ec[s00 + SA + SB]);
         }
         out[(size_t)c * NEN + en_index(X[0], X[1], X[2])] = v;
     }
@@ -1229,7 +1232,7 @@ k_edge_n(gb_dev_grid g, const int* __restrict__ list, const float* __restrict__ 
     const int blk = list[cb];
     const float* pb = p32 + (size_t)cb * p32_stride;
     T* out = escr + (size_t)cb * estride;
-    __shared__ T ec[EN_HALF][20][20];
+    __shared__ T ec[EN_HALF * 20 * 20];
     const int c = blockIdx.x >> 1, half = blockIdx.x & 1;
     if (c == 0) edge_n_dir<T, 0>(g, blk, pb, out, half, ec);
     else if (c == 1) edge_n_dir<T, 1>(g, blk, pb, out, half, ec);
@@ -1765,10 +1768,11 @@ __device__ __forceinline__ double rcp_newton(double x)
 // state (what the feature kernel would compute next): FP32 work beside this
 // FP64-bound kernel instead of a kernel of its own
 // mixed path without the fused plain cooling: eight resident CTAs per SM
-// (64 registers, no spills); the FP64 path and the fused integrator need
-// more registers than that
+// (64 registers, no spills); with the integrator on FP32 rates four (117
+// registers, no spills: the integrator is latency-bound, so resident warps
+// pay); the FP64 path and the FP64-rate integrator need more registers
 template <typename T, bool MHD, int COOL, bool FEAT>
-__global__ void __launch_bounds__(128, (std::is_same<T, float>::value && !COOL) ? 8 : COOL == 2 ? 3 : 1)
+__global__ void __launch_bounds__(128, (std::is_same<T, float>::value && !COOL) ? 8 : COOL == 2 ? 4 : 1)
 k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restrict__ list,
          const T* __restrict__ fscr, size_t fstride, const double* __restrict__ bscr, size_t bstride,
          gb_status* st, sur_feat_out sf)
