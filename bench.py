@@ -46,13 +46,13 @@ WORKLOADS = {
 TDUST0 = 18.0  # initial dust temperature [K] (sim_tdust, flash.par.turbsph_standard:19)
 
 # DRAM bytes (read + write) per interior zone of each profiler category of
-# the fast path, from ncu captures of the 128^3 box at 512-block chunks
-# ("recon" = primitive conversion + reconstruction, "guard_fill" = cells +
-# faces, "sur_feat" from an earlier capture of the feature kernel, which the
-# update now replaces). The roofline's traffic is this times the zones one
-# launch covers.
-TRAFFIC_B_PER_ZONE = {"recon": 708.6, "update": 367.4, "flux": 477.5, "guard_fill": 304.4, "mlp_infer": 16.0,
-                      "sur_accept": 111.5, "emf": 114.5, "faceb": 81.2, "sur_feat": 36.0, "dt": 97.8}
+# the fast path, from one-kernel ncu captures of the 128^3 box (one
+# 512-block launch per kernel): "recon" = FP32 copy + velocity divergence +
+# reconstruction, "emf" = time-n edge fields + edge fields, "guard_fill" =
+# cells + faces. The roofline's traffic is this times the zones one launch
+# covers.
+TRAFFIC_B_PER_ZONE = {"recon": 760.0, "update": 398.0, "flux": 484.0, "guard_fill": 305.0, "mlp_infer": 16.0,
+                      "sur_accept": 111.0, "emf": 151.0, "faceb": 81.0, "dt": 101.0}
 
 
 def build_workload(wl, device):
@@ -811,8 +811,9 @@ def main():
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
                      "frac": ach / hbm,
                      "traffic": TRAFFIC_B_PER_ZONE[dom] * zones_per_launch if dom in TRAFFIC_B_PER_ZONE else None,
-                     "traffic_source": "ncu DRAM bytes per zone of this kernel on the 128^3 box at 512-block chunks, "
-                                       "times the zones of one launch here",
+                     "traffic_source": "ncu DRAM bytes per zone of the kernels this profiler bucket times (one-kernel "
+                                       "captures on the 128^3 box, one 512-block launch each), times the zones of "
+                                       "one launch here",
                      "peak_kind": hbm_kind, "launch_ms": dom_ms / dom_n,
                      "algo_bytes_per_launch": 216.0 * zones_per_launch, "compute": compute},
         "step_roofline": step_roof,
