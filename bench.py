@@ -619,7 +619,7 @@ def main():
         if args.chunk:
             G.set_launch_config(args.chunk, args.tile, args.occ)
             G.set_chunk_streams(args.streams)
-            G.set_fused(bool(args.fused))
+            G.set_fused(int(args.fused))
         if args.only == "e2e":
             # the fast path (launch shapes as given) end to end from host arrays
             G.set_cooling_mode(True)
@@ -669,7 +669,7 @@ def main():
         if ginfo["tuned"]:
             G.set_launch_config(ginfo["tuned"]["chunk"], ginfo["tuned"]["tile"], ginfo["tuned"]["occ"])
             G.set_chunk_streams(ginfo["tuned"]["streams"])
-            G.set_fused(bool(ginfo["tuned"].get("fused", 0)))
+            G.set_fused(int(ginfo["tuned"].get("fused", 0)))
         ms_mixed, st_mixed, _ = run_path(G, g_mixed, 1, args.steps, args.warmup, graph=True)
         # the same with the integrator's rate function in FP32 (Brent's
         # iterates in FP64)

@@ -209,13 +209,15 @@ int gb_set_chunk_blocks(int n);
 int gb_set_launch_config(int chunk_blocks, int recon_tile, int recon_occupancy);
 int gb_get_launch_config(int* chunk_blocks, int* recon_tile, int* recon_occupancy);
 
-/* Reconstruction and Riemann solve as one kernel per block (1) or as two
- * kernels over a chunk with the face states in between in device memory
- * (0, the default). The fused kernel keeps each plane's face states in
- * shared memory and, in the mixed path, stages a rolling window of the
- * block's FP32 primitives with the tensor memory accelerator. The same
- * arithmetic either way; chosen by torch_gb300.autotune; no counterpart in
- * the reference. */
+/* Reconstruction and Riemann solve as one kernel per block (1, 2) or as
+ * two kernels over a chunk with the face states in between in device
+ * memory (0, the default). The fused kernel keeps each plane's face states
+ * in shared memory; in the mixed path mode 1 stages a rolling window of the
+ * block's FP32 primitives with the tensor memory accelerator (one CTA per
+ * SM), mode 2 reads them through L1 (no window: two CTAs per SM); the FP64
+ * path reads its stencils from the store in both. The same arithmetic
+ * either way; chosen by torch_gb300.autotune; no counterpart in the
+ * reference. */
 int gb_set_fused(int on);
 int gb_get_fused(void);
 

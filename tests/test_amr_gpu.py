@@ -142,3 +142,51 @@ def test_amr_conserves_with_flux_correction(gb, mhd):
     assert g.status_read()["n_eint_switch"] == 0
     rel = np.abs(after - before) / np.abs(before[[0, 0, 0, 0, 4]])
     assert np.all(rel < 1e-13), rel
+
+
+@pytest.mark.parametrize("mode", [0, 2])
+def test_amr_mixed_with_cooling_meets_the_accuracy_bound(gb, mode):
+    """The metric's accuracy condition on the 3-level MHD tree with cooling:
+    10 graph-replayed steps of the mixed path with the plain integrator
+    (mode 0: restated FP64 rates; mode 2: FP32 rates, FP64 iterates) against
+    the all-FP64 step with the reference integrator, density and pressure
+    L1 <= 1e-4, and every cooled temperature within 1 % of the FP64 path's
+    (both solve the same backward-Euler step with the same Brent path up to
+    round-off)."""
+    import torch
+    from torch_gb300 import amr
+    t, c = amr.small_tree()
+    units = gb.code_units()
+    gb.init_cooling(gb.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
+                                   time_unit=units["time_unit"]))
+
+    def grid():
+        st = amr.amr_box(t, c, seed=7, device="cuda")
+        g = gb.grid_from_amr(t, st, mhd=True, cooling=True)
+        g.u[:, g.slots["TEMP"]] = g.u[:, g.slots["EINT"]] * units["vel_unit"] ** 2 * (2.0 / 3.0) * (24.0 / 11.0) \
+            * gb.MP / gb.KB
+        g.u[:, g.slots["TDUS"]] = 18.0
+        return g
+
+    out = []
+    try:
+        for precision, cm in ((0, 0), (1, mode)):
+            gb.init_hydro(gb.hydro_params(True, precision=precision))
+            gb.set_cooling_mode(cm)
+            g = grid()
+            g.register()
+            for _ in range(10):
+                g.step_graph(cool=True)
+            torch.cuda.synchronize()
+            assert g.status_read()["code"] == 0
+            out.append(g.u[g.t_leaf.long()][:, :, 4:20, 4:20, 4:20].clone())
+            del g
+    finally:
+        gb.set_cooling_mode(0)
+        gb.check(gb.lib().gb_graph_reset(), "gb_graph_reset")
+    a, b = out
+    for v in (0, 4):
+        assert float((a[:, v] - b[:, v]).abs().sum() / a[:, v].abs().sum()) <= 1e-4, v
+    sT = 10
+    Ta, Tb = a[:, sT], b[:, sT]
+    assert bool(((Ta - Tb).abs() <= 0.01 * Ta).all())

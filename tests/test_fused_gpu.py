@@ -52,8 +52,8 @@ def _tree_grid(gb, mhd, device="cuda"):
     return gb.grid_from_amr(t, st, mhd=mhd, cooling=False)
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_fused_equals_two_kernels_on_tree(gb, precision):
+@pytest.mark.parametrize("precision,mode", [(0, 1), (1, 1), (1, 2)])
+def test_fused_equals_two_kernels_on_tree(gb, precision, mode):
     """Three MHD steps over the 3-level tree with flux conservation and two
     chunk streams: the fused step equals the two-kernel step (FP64 to the
     last bit; the mixed path, whose FP32 arithmetic the compiler may fuse
@@ -64,7 +64,7 @@ def test_fused_equals_two_kernels_on_tree(gb, precision):
     try:
         gb.set_chunk_streams(2)
         gb.set_launch_config(16, 32, 0)
-        for fused in (False, True):
+        for fused in (0, mode):
             gb.set_fused(fused)
             gb.init_hydro(gb.hydro_params(True, precision=precision))
             g = _tree_grid(gb, True)

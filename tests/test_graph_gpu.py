@@ -18,20 +18,22 @@ def _grid(gb):
     return g
 
 
-@pytest.mark.parametrize("precision,surrogate", [(0, False), (1, False), (1, True)])
-def test_graph_step_matches_eager(gb, precision, surrogate):
+@pytest.mark.parametrize("precision,mode", [(0, 0), (1, 0), (1, 1), (1, 2)])
+def test_graph_step_matches_eager(gb, precision, mode):
+    """mode: the cooling mode (plain integrator, learned surrogate, plain
+    integrator on FP32 rates)."""
     import torch
     units = gb.code_units()
     gb.init_cooling(gb.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
                                    time_unit=units["time_unit"]))
-    if surrogate:
+    if mode == 1:
         gb.mlp_init(3)
     gb.init_hydro(gb.hydro_params(True, precision=precision))
     a, b = _grid(gb), _grid(gb)
     gb.set_chunk_blocks(16)
     dts = []
     a.register()
-    gb.set_cooling_mode(surrogate)
+    gb.set_cooling_mode(mode)
     for _ in range(3):
         dt = a.compute_dt().item()
         dts.append(dt)
@@ -148,10 +150,10 @@ def test_autotuner_picks_a_candidate_and_restores_state(gb, tmp_path, monkeypatc
         assert (r["chunk"], r["tile"]) in {(8, 32), (8, 64), (16, 32), (16, 64)} and r["occ"] in (0, 1, 2)
         assert gb.get_launch_config() == (r["chunk"], r["tile"], r["occ"])
         assert gb.get_chunk_streams() == r["streams"]
-        # 2 chunks x 2 tiles x 3 bounds x 2 stream counts, and the fused
-        # kernel once per chunk size and stream count
-        assert len(r["trials"]) == 24 + 4 and not r["cached"]
-        assert gb.get_fused() == bool(r["fused"])
+        # 2 chunks x 2 tiles x 3 bounds x 2 stream counts, and each of the
+        # two fused modes once per chunk size and stream count
+        assert len(r["trials"]) == 24 + 8 and not r["cached"]
+        assert gb.get_fused() == r["fused"]
         assert torch.equal(g.u, before)
         r2 = autotune.tune(g, cool=True, chunks=(8, 16), tiles=(32, 64), steps=1)
         assert r2["cached"] and (r2["chunk"], r2["tile"], r2["occ"]) == (r["chunk"], r["tile"], r["occ"])

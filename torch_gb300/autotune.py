@@ -19,7 +19,7 @@ CHUNKS = (32, 64, 128, 256, 512, 1024)
 TILES = (32, 64)
 OCCS = (0, 1, 2)
 STREAMS = (1, 2)
-FUSED = (0, 1)
+FUSED = (0, 1, 2)
 CACHE = os.environ.get("GBHYDRO_TUNE_CACHE",
                        os.path.join(os.path.dirname(os.path.abspath(__file__)), "_tune_cache.json"))
 
@@ -58,7 +58,7 @@ def time_config(grid, cool: bool, chunk: int, tile: int, steps: int = 3, warmup:
     from . import gbhydro as G
     G.set_launch_config(chunk, tile, occ)
     G.set_chunk_streams(streams)
-    G.set_fused(bool(fused))
+    G.set_fused(int(fused))
     step = step_fn or (lambda: grid.step_graph(cool))
     s = torch.cuda.current_stream()
     for _ in range(warmup):
@@ -92,15 +92,17 @@ def tune(grid, cool: bool = True, chunks=CHUNKS, tiles=TILES, occs=OCCS, steps: 
         r = dict(cache[key], cached=True)
         G.set_launch_config(r["chunk"], r["tile"], r.get("occ", 0))
         G.set_chunk_streams(r.get("streams", 1))
-        G.set_fused(bool(r.get("fused", 0)))
+        G.set_fused(int(r.get("fused", 0)))
         return r
     if G.state["precision"] != 1:
         occs = (0,)
     saved = [grid.u.clone()] + ([a.clone() for a in (grid.fx, grid.fy, grid.fz)] if grid.mhd else [])
     trials = []
     shapes = [(c, t, o, ns, 0) for c in chunks for t in tiles for o in occs for ns in streams if 0 in fused]
-    if 1 in fused:
-        shapes += [(c, tiles[0], 0, ns, 1) for c in chunks for ns in streams]
+    for fu in (1, 2):
+        # mode 2 differs from 1 only in the mixed path
+        if fu in fused and (fu == 1 or G.state["precision"] == 1):
+            shapes += [(c, tiles[0], 0, ns, fu) for c in chunks for ns in streams]
     try:
         for c, t, o, ns, fu in shapes:
             ms = time_config(grid, cool, c, t, steps=steps, occ=o, streams=ns, step_fn=step_fn, fused=fu)
@@ -118,7 +120,7 @@ def tune(grid, cool: bool = True, chunks=CHUNKS, tiles=TILES, occs=OCCS, steps: 
     best = min(trials, key=lambda r: r["ms"])
     G.set_launch_config(best["chunk"], best["tile"], best["occ"])
     G.set_chunk_streams(best["streams"])
-    G.set_fused(bool(best["fused"]))
+    G.set_fused(int(best["fused"]))
     r = {"chunk": best["chunk"], "tile": best["tile"], "occ": best["occ"], "streams": best["streams"],
          "fused": best["fused"], "ms": best["ms"], "trials": trials}
     if use_cache:

@@ -1441,11 +1441,15 @@ int gb_fused_attr_mixed();
 
 extern "C" int gb_set_fused(int on)
 {
+    if (on < 0 || on > 2) {
+        gb_set_error("gb_set_fused: mode %d is not 0, 1 or 2", on);
+        return GB_ERR_ARG;
+    }
     if (on) {
         // the fused kernels' shared memory beyond the default 48 KB
         if (gb_fused_attr_fp64() || gb_fused_attr_mixed()) return GB_ERR_CUDA;
     }
-    g_fused = on ? 1 : 0;
+    g_fused = on;
     g_gb.gen += 1;
     return GB_OK;
 }

@@ -42,6 +42,15 @@ int fused_set_attr()
         gb_check(cudaFuncSetAttribute(k_recon_flux<T, false, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
                  "fused kernel shared memory"))
         return GB_ERR_CUDA;
+    if constexpr (TMA) {
+        // mode 2: the mixed kernel without the window
+        const int b2 = (int)fused_layout<T, false>::bytes;
+        if (gb_check(cudaFuncSetAttribute(k_recon_flux<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b2),
+                     "fused kernel shared memory") ||
+            gb_check(cudaFuncSetAttribute(k_recon_flux<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b2),
+                     "fused kernel shared memory"))
+            return GB_ERR_CUDA;
+    }
     return GB_OK;
 }
 
@@ -51,16 +60,22 @@ int recon_and_flux(int tile, dim3 rg, dim3 fg, cudaStream_t s, const gb_dev_grid
                    const int* list, T* rscr, T* fscr, float* p32, gb_status* st)
 {
     using SL = scratch_layout<T>;
-    if (gb_fused_step()) {
+    if (const int fm = gb_fused_step()) {
         constexpr bool TMA = std::is_same<T, float>::value;
         CUtensorMap tm;
         memset(&tm, 0, sizeof tm);
-        if constexpr (TMA) {
-            if (gb_encode_p32_map(&tm, p32, nblk, SL::prim32)) return GB_ERR_CUDA;
-        }
         gb_prof_begin(GBP_RECON, s);
-        k_recon_flux<T, MHD, TMA><<<nblk, FUSED_THREADS, fused_layout<T, TMA>::bytes, s>>>(g, kp, list, fscr, SL::flux,
-                                                                                        p32, SL::prim32, tm, st);
+        if (TMA && fm == 2) {
+            // mixed path without the window: stencils through L1
+            k_recon_flux<T, MHD, false><<<nblk, FUSED_THREADS, fused_layout<T, false>::bytes, s>>>(
+                g, kp, list, fscr, SL::flux, p32, SL::prim32, tm, st);
+        } else {
+            if constexpr (TMA) {
+                if (gb_encode_p32_map(&tm, p32, nblk, SL::prim32)) return GB_ERR_CUDA;
+            }
+            k_recon_flux<T, MHD, TMA><<<nblk, FUSED_THREADS, fused_layout<T, TMA>::bytes, s>>>(
+                g, kp, list, fscr, SL::flux, p32, SL::prim32, tm, st);
+        }
         gb_prof_end(GBP_RECON, s);
         return GB_OK;
     }

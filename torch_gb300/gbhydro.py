@@ -478,13 +478,15 @@ def get_launch_config() -> tuple:
     return a.value, b.value, c.value
 
 
-def set_fused(on: bool) -> None:
-    """Reconstruction and Riemann solve fused per block (gb_set_fused)."""
-    check(lib().gb_set_fused(int(bool(on))), "gb_set_fused")
+def set_fused(mode) -> None:
+    """Reconstruction and Riemann solve fused per block (gb_set_fused): 0
+    (False) two kernels, 1 (True) fused with the TMA window in the mixed
+    path, 2 fused with the mixed path's stencils read through L1."""
+    check(lib().gb_set_fused(int(mode)), "gb_set_fused")
 
 
-def get_fused() -> bool:
-    return bool(lib().gb_get_fused())
+def get_fused() -> int:
+    return int(lib().gb_get_fused())
 
 
 def set_chunk_streams(n: int) -> None:
