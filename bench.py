@@ -525,7 +525,8 @@ def lite_run(args, G, wl, tree, st, zones, world, rank, t_ic):
             "metric_compliant_path": {"path": "mixed hydro + batched graph + plain integrator on FP32 rates",
                                       "value": zones * world / (ms_m32 * 1e-3),
                                       "speedup_vs_plain_fp64": ms_plain / ms_m32,
-                                      "l1_vs_plain_fp64": l1_m32},
+                                      "l1_vs_plain_fp64": l1_m32,
+                                      "frac_temps_within_1pct_of_plain": temp_m32["frac_within_1pct"]},
             "note": "the learned path solves the backward-Euler step to ~1e-8 of its root; the reference "
                     "integrator stops Brent at 1 K, which alone moves pressure L1 by "
                     "l1_reference_integrator_tolerance; the metric-compliant path keeps the reference "
@@ -701,7 +702,10 @@ def main():
     Ta, Tb = a[lv, sT, 4:20, 4:20, 4:20], b[lv, sT, 4:20, 4:20, 4:20]
     temp_steps = dict(rel_stats(Tb, Ta), frac_within_1pct_or_2K=float(((Ta - Tb).abs() <= 0.01 * Ta + 2.0)
                                                                         .double().mean()))
-    del a, b, c, d, Ta, Tb
+    # the metric-compliant path's cooled temperatures against the plain path's
+    Tm = g_m32.u[lv, sT, 4:20, 4:20, 4:20]
+    temp_m32 = rel_stats(Tm, Ta)
+    del a, b, c, d, Ta, Tb, Tm
     one_step = cooling_one_step(G, (g_plain, g_fast, g_tight), g_mixed, lv)
     G.set_cooling_mode(True)
     e2e_ms, e2e_bytes, e2e_parts = e2e_run(G, g_fast, max(2, args.steps // 2), 3, tune=not args.no_tune)
@@ -797,6 +801,7 @@ def main():
                                         "function in FP64 with shared transcendentals"},
         "mixed_fp32_rates_cooling": {"value": zones * world / (ms_m32 * 1e-3), "ms_per_step": ms_m32,
                                      "speedup_vs_plain_fp64": ms_plain / ms_m32, "l1_err_vs_fp64": l1_m32,
+                                     "temp_rel_err_vs_plain_after_steps": temp_m32,
                                      "note": "mixed hydro; the plain integrator fused into the update with its "
                                              "rate function in FP32 (Brent's and the bracket search's iterates "
                                              "and the residual in FP64)"},
