@@ -418,31 +418,58 @@ __device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* 
 #pragma unroll
     for (int s = 0; s < nw; ++s)
         Wp[s] = refK ? WR[s] - (T)0.5 * sK * (dW[s] - ((T)1 - t3 * sK) * W6[s]) : WR[s];
-#pragma unroll
-    for (int k = 0; k < nw; ++k) {
-        if (lam[k] > (T)0) {
-            T sg = lam[k] * dtdx;
-            T gK = refK ? (T)0.5 * sK * (ldW[k] - ((T)1 - t3 * sK) * lW6[k]) : (T)0;
-            T c = gK - (T)0.5 * sg * (ldW[k] - ((T)1 - t3 * sg) * lW6[k]);
-#pragma unroll
-            for (int s = 0; s < nw; ++s)
-                if (nz_R<MHD>(s, k)) Wp[s] = Wp[s] + c * R[s][k];
-        }
-    }
     T s0 = lam[0] * dtdx;
     bool ref0 = lam[0] < (T)0;
 #pragma unroll
     for (int s = 0; s < nw; ++s)
         Wn[s] = ref0 ? WL[s] - (T)0.5 * s0 * (dW[s] + ((T)1 + t3 * s0) * W6[s]) : WL[s];
+    if constexpr (std::is_same<T, float>::value) {
+        // each wave corrects the + state (lam > 0) or the - state (lam < 0):
+        // one packed pair per matrix entry with the other side's coefficient
+        // 0 (adding 0 R leaves a state unchanged), and no branch on the wave
+        // speeds' signs, which differ between the cells of a warp
+        float2 wpn[MAXW];
 #pragma unroll
-    for (int k = 0; k < nw; ++k) {
-        if (lam[k] < (T)0) {
-            T sg = lam[k] * dtdx;
-            T g0 = ref0 ? (T)0.5 * s0 * (ldW[k] + ((T)1 + t3 * s0) * lW6[k]) : (T)0;
-            T c = g0 - (T)0.5 * sg * (ldW[k] + ((T)1 + t3 * sg) * lW6[k]);
+        for (int s = 0; s < nw; ++s) wpn[s] = make_float2(Wp[s], Wn[s]);
+#pragma unroll
+        for (int k = 0; k < nw; ++k) {
+            const T sg = lam[k] * dtdx;
+            const T gK = refK ? (T)0.5 * sK * (ldW[k] - ((T)1 - t3 * sK) * lW6[k]) : (T)0;
+            const T cp = gK - (T)0.5 * sg * (ldW[k] - ((T)1 - t3 * sg) * lW6[k]);
+            const T g0 = ref0 ? (T)0.5 * s0 * (ldW[k] + ((T)1 + t3 * s0) * lW6[k]) : (T)0;
+            const T cn = g0 - (T)0.5 * sg * (ldW[k] + ((T)1 + t3 * sg) * lW6[k]);
+            const float2 c2 = make_float2(lam[k] > (T)0 ? cp : (T)0, lam[k] < (T)0 ? cn : (T)0);
 #pragma unroll
             for (int s = 0; s < nw; ++s)
-                if (nz_R<MHD>(s, k)) Wn[s] = Wn[s] + c * R[s][k];
+                if (nz_R<MHD>(s, k)) wpn[s] = __ffma2_rn(c2, make_float2(R[s][k], R[s][k]), wpn[s]);
+        }
+#pragma unroll
+        for (int s = 0; s < nw; ++s) {
+            Wp[s] = wpn[s].x;
+            Wn[s] = wpn[s].y;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < nw; ++k) {
+            if (lam[k] > (T)0) {
+                T sg = lam[k] * dtdx;
+                T gK = refK ? (T)0.5 * sK * (ldW[k] - ((T)1 - t3 * sK) * lW6[k]) : (T)0;
+                T c = gK - (T)0.5 * sg * (ldW[k] - ((T)1 - t3 * sg) * lW6[k]);
+#pragma unroll
+                for (int s = 0; s < nw; ++s)
+                    if (nz_R<MHD>(s, k)) Wp[s] = Wp[s] + c * R[s][k];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < nw; ++k) {
+            if (lam[k] < (T)0) {
+                T sg = lam[k] * dtdx;
+                T g0 = ref0 ? (T)0.5 * s0 * (ldW[k] + ((T)1 + t3 * s0) * lW6[k]) : (T)0;
+                T c = g0 - (T)0.5 * sg * (ldW[k] + ((T)1 + t3 * sg) * lW6[k]);
+#pragma unroll
+                for (int s = 0; s < nw; ++s)
+                    if (nz_R<MHD>(s, k)) Wn[s] = Wn[s] + c * R[s][k];
+            }
         }
     }
 #pragma unroll
