@@ -474,15 +474,46 @@ __device__ __forceinline__ void ppm_normal(T gam, const T (*qs)[NP], T dtdx, T* 
     }
 #pragma unroll
     for (int s = 0; s < NP; ++s) { wp[s] = (T)0; wn[s] = (T)0; sig[s] = (T)0; }
+    if constexpr (std::is_same<T, float>::value) {
+        // rows s and s + 1 of R (lam ldW) as packed pairs (a row's structural
+        // zero adds 0 to its lane, as skipping it would)
+        float lw[MAXW];
 #pragma unroll
-    for (int s = 0; s < nw; ++s) {
-        T acc = (T)0;
+        for (int k = 0; k < nw; ++k) lw[k] = lam[k] * ldW[k];
 #pragma unroll
-        for (int k = 0; k < nw; ++k)
-            if (nz_R<MHD>(s, k)) acc = acc + (lam[k] * ldW[k]) * R[s][k];
-        wp[wslot(s)] = Wp[s];
-        wn[wslot(s)] = Wn[s];
-        sig[wslot(s)] = acc;
+        for (int s = 0; s < nw; s += 2) {
+            if (s + 1 < nw) {
+                float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+                for (int k = 0; k < nw; ++k)
+                    if (nz_R<MHD>(s, k) || nz_R<MHD>(s + 1, k))
+                        acc = __ffma2_rn(make_float2(lw[k], lw[k]), make_float2(R[s][k], R[s + 1][k]), acc);
+                sig[wslot(s)] = acc.x;
+                sig[wslot(s + 1)] = acc.y;
+            } else {
+                float acc = 0.0f;
+#pragma unroll
+                for (int k = 0; k < nw; ++k)
+                    if (nz_R<MHD>(s, k)) acc = __fmaf_rn(lw[k], R[s][k], acc);
+                sig[wslot(s)] = acc;
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < nw; ++s) {
+            wp[wslot(s)] = Wp[s];
+            wn[wslot(s)] = Wn[s];
+        }
+    } else {
+#pragma unroll
+        for (int s = 0; s < nw; ++s) {
+            T acc = (T)0;
+#pragma unroll
+            for (int k = 0; k < nw; ++k)
+                if (nz_R<MHD>(s, k)) acc = acc + (lam[k] * ldW[k]) * R[s][k];
+            wp[wslot(s)] = Wp[s];
+            wn[wslot(s)] = Wn[s];
+            sig[wslot(s)] = acc;
+        }
     }
     wp[5] = qs[2][5];
     wn[5] = qs[2][5];
@@ -815,6 +846,22 @@ __device__ __forceinline__ T ecc_of(const T* wp, const T* wn)
     return vb * Ba - va * Bb;
 }
 
+// wn[s] -= a b and wp[s] -= a b: both states take the same correction, so
+// the mixed path applies it to the pair in one packed fma.rn.f32x2 (each
+// lane the scalar fused multiply-add's rounding)
+template <typename T>
+__device__ __forceinline__ void sub_both(T* wn, T* wp, int s, T a, T b)
+{
+    if constexpr (std::is_same<T, float>::value) {
+        const float2 r = __ffma2_rn(make_float2(-a, -a), make_float2(b, b), make_float2(wn[s], wp[s]));
+        wn[s] = r.x;
+        wp[s] = r.y;
+    } else {
+        wn[s] = wn[s] - a * b;
+        wp[s] = wp[s] - a * b;
+    }
+}
+
 // transverse corrections of direction d in the vendored order
 // (hy_uhd_dataReconstOneStep.F90:1006-1089), wp / wn in d's rotated frame
 template <typename T, bool MHD, int TILE>
@@ -829,42 +876,28 @@ __device__ __forceinline__ void recon_transverse(const T* hd, int d, int lane, T
         const int o = d == 0 ? 1 : 0;
         const T ho = o == 0 ? hd[0] : hd[1];
 #pragma unroll
-        for (int s = 0; s < nv; ++s) {
-            wn[s] = wn[s] - ho * s_sig[o][us[s]][lane];
-            wp[s] = wp[s] - ho * s_sig[o][us[s]][lane];
-        }
+        for (int s = 0; s < nv; ++s) sub_both<T>(wn, wp, s, ho, s_sig[o][us[s]][lane]);
         if (MHD) {
 #pragma unroll
-            for (int s = 0; s < nv; ++s) {
-                wn[s] = wn[s] - ho * s_abn[o][us[s]][lane] * s_dnb[o][lane];
-                wp[s] = wp[s] - ho * s_abn[o][us[s]][lane] * s_dnb[o][lane];
-            }
+            for (int s = 0; s < nv; ++s) sub_both<T>(wn, wp, s, ho * s_abn[o][us[s]][lane], s_dnb[o][lane]);
         }
 #pragma unroll
-        for (int s = 0; s < nv; ++s) {
-            wn[s] = wn[s] - hd[2] * s_sig[2][us[s]][lane];
-            wp[s] = wp[s] - hd[2] * s_sig[2][us[s]][lane];
-        }
+        for (int s = 0; s < nv; ++s) sub_both<T>(wn, wp, s, hd[2], s_sig[2][us[s]][lane]);
         if (MHD) {
 #pragma unroll
-            for (int s = 0; s < nv; ++s) {
-                wn[s] = wn[s] - hd[2] * s_abn[2][us[s]][lane] * s_dnb[2][lane];
-                wp[s] = wp[s] - hd[2] * s_abn[2][us[s]][lane] * s_dnb[2][lane];
-            }
+            for (int s = 0; s < nv; ++s) sub_both<T>(wn, wp, s, hd[2] * s_abn[2][us[s]][lane], s_dnb[2][lane]);
         }
     } else {
 #pragma unroll
         for (int s = 0; s < nv; ++s) {
-            wn[s] = wn[s] - hd[0] * s_sig[0][us[s]][lane] - hd[1] * s_sig[1][us[s]][lane];
-            wp[s] = wp[s] - hd[0] * s_sig[0][us[s]][lane] - hd[1] * s_sig[1][us[s]][lane];
+            sub_both<T>(wn, wp, s, hd[0], s_sig[0][us[s]][lane]);
+            sub_both<T>(wn, wp, s, hd[1], s_sig[1][us[s]][lane]);
         }
         if (MHD) {
 #pragma unroll
             for (int s = 0; s < nv; ++s) {
-                wn[s] = wn[s] - hd[0] * s_abn[0][us[s]][lane] * s_dnb[0][lane] -
-                        hd[1] * s_abn[1][us[s]][lane] * s_dnb[1][lane];
-                wp[s] = wp[s] - hd[0] * s_abn[0][us[s]][lane] * s_dnb[0][lane] -
-                        hd[1] * s_abn[1][us[s]][lane] * s_dnb[1][lane];
+                sub_both<T>(wn, wp, s, hd[0] * s_abn[0][us[s]][lane], s_dnb[0][lane]);
+                sub_both<T>(wn, wp, s, hd[1] * s_abn[1][us[s]][lane], s_dnb[1][lane]);
             }
         }
     }
