@@ -705,20 +705,6 @@ static __device__ int zbrac(const gb_cool_ctx& c, const gb_cool_vars& v, const f
     return 0;
 }
 
-// 1 / x from an FP32 reciprocal and two Newton steps in FP64 (about 2^-88
-// relative before the final rounding), for normal x inside FP32's range;
-// the FP64 division otherwise
-__device__ __forceinline__ double rcp_nr(double x)
-{
-    const float xf = gb_d2f(x);
-    if (!(fabsf(xf) > 1e-30f && fabsf(xf) < 1e30f)) return 1.0 / x;
-    double y = gb_f2d(__frcp_rn(xf));
-    double e = fma(-x, y, 1.0);
-    y = fma(y, e, y);
-    e = fma(-x, y, 1.0);
-    return fma(y, e, y);
-}
-
 // heating_and_cooling, "Implicit" (default) or "Euler" branch, for one
 // cell. v must hold rho, Gflux, ephen, tdust, xHp, strat_factor, mu_mol.
 template <int FORM = 0>
@@ -729,21 +715,9 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
     const double err_tol = 1e-6;
     double ei = *ei_io, temp = *temp_io;
     double total_time = 0.0;
-    // FORM 2 replaces the per-cell FP64 divisions by reciprocals from an
-    // FP32 seed and two Newton steps (a few DFMA against a division's longer
-    // sequence; within an ulp or two of the quotient)
-    double itte = 0.0;  // 1 / TtoEI (FORM 2)
-    if (FORM == 2) {
-        const double irho = rcp_nr(v.rho);
-        v.ndens = v.rho * rcp_nr(v.mu_mol * p.mp);
-        v.TtoEI = ei * rcp_nr(temp);
-        itte = temp * rcp_nr(ei);
-        v.conf = v.ndens * v.ndens * irho;
-    } else {
-        v.ndens = v.rho / (v.mu_mol * p.mp);
-        v.TtoEI = ei / temp;
-        v.conf = v.ndens * v.ndens / v.rho;
-    }
+    v.ndens = v.rho / (v.mu_mol * p.mp);
+    v.TtoEI = ei / temp;
+    v.conf = v.ndens * v.ndens / v.rho;
     // FORM 2 forms the floors' cooling in FP32 with its rates
     double fl = FORM == 2 ? 0.0 : cooling_floor(c, v);
     fr_consts frc;
@@ -757,7 +731,7 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
             double dt1 = p.subfactor * ei / fmx(fabs(dei), 1e-50);
             double dt0 = fmn((timestep - total_time), dt1);
             ei = ei + dei * dt0;
-            temp = FORM == 2 ? ei * itte : ei / v.TtoEI;
+            temp = ei / v.TtoEI;
             total_time = total_time + dt0;
             ncount = ncount + 1;
             if (ncount > 100000) break;
@@ -781,7 +755,7 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
             if (fabs((ei1 - ei2) / ei1) < (err_tol * dt0 / (timestep - total_time))) {
                 dt0 = (timestep - total_time);
                 ei = eiolder + dei * dt0;
-                temp = FORM == 2 ? ei * itte : ei / v.TtoEI;
+                temp = ei / v.TtoEI;
                 if (p.useDustCool && temp <= p.dust_sputter_temp) dust_after_step<FORM>(c, v, frc, temp, d);
                 total_time = total_time + dt0;
                 continue;
@@ -797,7 +771,7 @@ static __device__ void heating_and_cooling(const gb_cool_ctx& c, gb_cool_vars& v
             else
                 ei = zero<FORM>(c, v, frc, fl, v.TtoEI * 1.0, v.TtoEI * 1.0e9, eiolder, 3e-16,
                           fmx(v.TtoEI * c.brent_tol_K, eiold * err_tol), dt0, d);
-            temp = FORM == 2 ? ei * itte : ei / v.TtoEI;
+            temp = ei / v.TtoEI;
             if (p.useDustCool && temp <= p.dust_sputter_temp) dust_after_step<FORM>(c, v, frc, temp, d);
             total_time = total_time + dt0;
         }

@@ -1853,14 +1853,11 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
     // reciprocal of the density (FP64 divisions are long instruction
     // sequences on the FP64 pipe); the FP64 path keeps the oracle's operations
     constexpr bool RCP = std::is_same<T, float>::value;
-    // x / 2: the mixed path halves on the integer pipe (the exponent moves
-    // by one: the same value as the FP64 product, one FP64 instruction fewer)
-    auto half = [&](double x) { return RCP ? gb_scale_pow2(x, -1) : 0.5 * x; };
     double Uc[NP];
     Uc[0] = rho;
     Uc[1] = rho * vx; Uc[2] = rho * vy; Uc[3] = rho * vz;
-    Uc[4] = (RCP ? pr * kp.inv_gm1 : pr / gm1) + half(rho) * (vx * vx + vy * vy + vz * vz) +
-            half(Bc[0] * Bc[0] + Bc[1] * Bc[1] + Bc[2] * Bc[2]);
+    Uc[4] = (RCP ? pr * kp.inv_gm1 : pr / gm1) + 0.5 * rho * (vx * vx + vy * vy + vz * vz) +
+            0.5 * (Bc[0] * Bc[0] + Bc[1] * Bc[1] + Bc[2] * Bc[2]);
     Uc[5] = Bc[0]; Uc[6] = Bc[1]; Uc[7] = Bc[2];
     double re = rho * UV(GB_EINT);
     const T* fs = fscr + (size_t)cb * fstride;
@@ -1906,7 +1903,7 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
         double bhi[3] = {bs[0 * NFB + fb_index(0, i + 1, j, k)], bs[1 * NFB + fb_index(1, i, j + 1, k)],
                          bs[2 * NFB + fb_index(2, i, j, k + 1)]};
 #pragma unroll
-        for (int d = 0; d < 3; ++d) Bn[d] = half(blo[d] + bhi[d]);
+        for (int d = 0; d < 3; ++d) Bn[d] = 0.5 * (blo[d] + bhi[d]);
         // write back the interior faces: low faces by every cell, high
         // faces by the cells on the upper boundary
         g.f[0][(int64_t)blk * GB_FSZ + gb_fidx(0, i, j, k)] = blo[0];
@@ -1919,8 +1916,8 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
     double rn = fmax(Un[0], kp.smlrho);
     const double irn = RCP ? rcp_newton(rn) : 0.0;
     auto over_rn = [&](double x) { return RCP ? x * irn : x / rn; };
-    double ek = over_rn(half(Un[1] * Un[1] + Un[2] * Un[2] + Un[3] * Un[3]));
-    double em = half(Bn[0] * Bn[0] + Bn[1] * Bn[1] + Bn[2] * Bn[2]);
+    double ek = over_rn(0.5 * (Un[1] * Un[1] + Un[2] * Un[2] + Un[3] * Un[3]));
+    double em = 0.5 * (Bn[0] * Bn[0] + Bn[1] * Bn[1] + Bn[2] * Bn[2]);
     if (MHD && kp.energy_fix) {
         // energyFix (Balsara & Spicer 1999): the gas energy is the updated
         // total energy less the magnetic energy of the cell field advanced by
@@ -1947,7 +1944,7 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
             Bf[1] = (Uc[6] - dtd[0] * (F(0, 6, fp[0]) - F(0, 6, fm[0]))) - dtd[2] * (F(2, 6, fp[2]) - F(2, 6, fm[2]));
             Bf[2] = (Uc[7] - dtd[0] * (F(0, 7, fp[0]) - F(0, 7, fm[0]))) - dtd[1] * (F(1, 7, fp[1]) - F(1, 7, fm[1]));
         }
-        em = half(Bf[0] * Bf[0] + Bf[1] * Bf[1] + Bf[2] * Bf[2]);
+        em = 0.5 * (Bf[0] * Bf[0] + Bf[1] * Bf[1] + Bf[2] * Bf[2]);
     }
     const double xE = (Un[4] - ek) - em;  // rho e from the total energy
     double eiE = over_rn(xE);
