@@ -514,7 +514,8 @@ def lite_run(args, G, wl, tree, st, zones, world, rank, t_ic):
                    "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (state %.1f GB)" % (g_fast.u.numel() * 8 / 1e9)},
         "plain_fp64": {"value": zones * world / (ms_plain * 1e-3), "ms_per_step": ms_plain,
-                       "launch_config": {k: pinfo["tuned"][k] for k in ("chunk", "tile")} if pinfo["tuned"] else None},
+                       "launch_config": {k: pinfo["tuned"][k] for k in ("chunk", "tile", "streams", "fused")}
+                       if pinfo["tuned"] else None},
         "speedup_vs_plain_fp64": ms_plain / ms_fast,
         # which accuracy the headline (the learned-cooling path) meets, and
         # the fastest path that meets the metric's bound against plain FP64
@@ -659,7 +660,7 @@ def main():
     with clk:
         ms_plain, st_plain, pinfo = run_path(G, g_plain, 0, args.steps, args.warmup, graph=True,
                                              tune=not args.no_tune,
-                                             tune_kw={"chunks": (16, 32, 64), "steps": 1})
+                                             tune_kw={"chunks": (64, 256, 1024), "steps": 1})
         ms_fast, st_fast, ginfo = run_path(G, g_fast, 1, args.steps, args.warmup, surrogate=True, graph=True,
                                            tune=not args.no_tune, ncu_range=args.ncu_range)
         # the same path launched eagerly with the in-library profiler on:
