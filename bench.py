@@ -785,7 +785,8 @@ def main():
                    "physics": "MHD HLLD+CT, PPM, implicit heating/cooling", "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (state %.1f GB)" % (g_fast.u.numel() * 8 / 1e9)},
         "plain_fp64": {"value": zones * world / (ms_plain * 1e-3), "ms_per_step": ms_plain,
-                       "launch_config": {k: pinfo["tuned"][k] for k in ("chunk", "tile")} if pinfo["tuned"] else None},
+                       "launch_config": {k: pinfo["tuned"][k] for k in ("chunk", "tile", "streams", "fused")}
+                       if pinfo["tuned"] else None},
         "speedup_vs_plain_fp64": ms_plain / ms_fast,
         "l1_err_vs_fp64": l1_fast,
         "l1_err_mixed_hydro_vs_fp64": l1_mixed,
