@@ -749,9 +749,6 @@ __global__ void k_guard_faces(gb_dev_grid g, gb_tree_desc t, const int* __restri
 // from the root above, value for value.
 // STEP: only the guard cells a step reads (the region of gb_step_cell);
 // otherwise all of them (FLASH's guard fill)
-constexpr int GUARD_SPLIT = 2;
-constexpr int GUARD_VPT = (GB_NROLE + GUARD_SPLIT - 1) / GUARD_SPLIT;
-
 template <bool STEP>
 __global__ void __launch_bounds__(128) k_guard_cells_plan(gb_dev_grid g, gb_tree_desc t, const int* __restrict__ list,
                                                           guard_vars gv, const int4* __restrict__ plan)
@@ -781,19 +778,15 @@ __global__ void __launch_bounds__(128) k_guard_cells_plan(gb_dev_grid g, gb_tree
     double* dst = g.unk + (int64_t)blk * g.nvar * GB_N3 + gb_cidx(I[0], I[1], I[2]);
     const double* src = g.unk + (int64_t)h.node * g.nvar * GB_N3;
     const int k = L - h.level;
-    // this CTA's share of the variables (blockIdx.z of GUARD_SPLIT): half
-    // the loads in flight per thread at half the registers, so twice the
-    // threads keep the gathers' latency covered
-    const int q_lo = (int)blockIdx.z * GUARD_VPT, q_hi = min(gv.n, q_lo + GUARD_VPT);
-    double val[GUARD_VPT];
+    double val[GB_NROLE];
     if (k >= 0) {
         // same level: copy; coarser: injection of the covering coarse cell
         const int sci = gb_cidx((A[0] >> k) - (h.c[0] << LOG2_NXB) + GB_NGUARD,
                                 (A[1] >> k) - (h.c[1] << LOG2_NXB) + GB_NGUARD,
                                 (A[2] >> k) - (h.c[2] << LOG2_NXB) + GB_NGUARD);
 #pragma unroll
-        for (int e = 0; e < GUARD_VPT; ++e)
-            if (q_lo + e < q_hi) val[e] = src[(int64_t)gv.slot[q_lo + e] * GB_N3 + sci];
+        for (int q2 = 0; q2 < GB_NROLE; ++q2)
+            if (q2 < gv.n) val[q2] = src[(int64_t)gv.slot[q2] * GB_N3 + sci];
     } else {
         // finer neighbour: mean of the fine cells covering this cell
         const int m = -k, rr = 1 << m;
@@ -807,9 +800,9 @@ __global__ void __launch_bounds__(128) k_guard_cells_plan(gb_dev_grid g, gb_tree
             // the z, y, x order of the general loop below
             const int c0 = gb_cidx(bi, bj, bk);
 #pragma unroll
-            for (int e = 0; e < GUARD_VPT; ++e) {
-                if (q_lo + e >= q_hi) continue;
-                const double* sv = src + (int64_t)gv.slot[q_lo + e] * GB_N3 + c0;
+            for (int q2 = 0; q2 < GB_NROLE; ++q2) {
+                if (q2 >= gv.n) continue;
+                const double* sv = src + (int64_t)gv.slot[q2] * GB_N3 + c0;
                 double w[8];
 #pragma unroll
                 for (int z = 0; z < 2; ++z)
@@ -819,25 +812,25 @@ __global__ void __launch_bounds__(128) k_guard_cells_plan(gb_dev_grid g, gb_tree
                         for (int x = 0; x < 2; ++x) w[4 * z + 2 * y + x] = sv[x + GB_N * (y + GB_N * z)];
                 double acc = 0.0;
 #pragma unroll
-                for (int m8 = 0; m8 < 8; ++m8) acc += w[m8];
-                val[e] = acc * inv;
+                for (int e = 0; e < 8; ++e) acc += w[e];
+                val[q2] = acc * inv;
             }
         } else {
 #pragma unroll
-            for (int e = 0; e < GUARD_VPT; ++e) {
-                if (q_lo + e >= q_hi) continue;
-                const double* sv = src + (int64_t)gv.slot[q_lo + e] * GB_N3;
+            for (int q2 = 0; q2 < GB_NROLE; ++q2) {
+                if (q2 >= gv.n) continue;
+                const double* sv = src + (int64_t)gv.slot[q2] * GB_N3;
                 double acc = 0.0;
                 for (int z = 0; z < rr; ++z)
                     for (int y = 0; y < rr; ++y)
                         for (int x = 0; x < rr; ++x) acc += sv[gb_cidx(bi + x, bj + y, bk + z)];
-                val[e] = acc * inv;
+                val[q2] = acc * inv;
             }
         }
     }
 #pragma unroll
-    for (int e = 0; e < GUARD_VPT; ++e)
-        if (q_lo + e < q_hi) dst[(int64_t)gv.slot[q_lo + e] * GB_N3] = val[e];
+    for (int q2 = 0; q2 < GB_NROLE; ++q2)
+        if (q2 < gv.n) dst[(int64_t)gv.slot[q2] * GB_N3] = val[q2];
 }
 
 template <int AX, bool STEP>
@@ -1277,10 +1270,10 @@ static void launch_guard_kernels(int nblk, const int* list, bool faces, bool ste
     const int4* plan = guard_plan(s);
     gb_prof_begin(GBP_GUARD, s);
     if (plan && step) {
-        k_guard_cells_plan<true><<<dim3((GB_STEP_GUARD_CELLS + 127) / 128, nblk, GUARD_SPLIT), 128, 0, s>>>(
+        k_guard_cells_plan<true><<<dim3((GB_STEP_GUARD_CELLS + 127) / 128, nblk), 128, 0, s>>>(
             g_gb.grid, g_gb.tree, list, hydro_guard_vars(), plan);
     } else if (plan) {
-        k_guard_cells_plan<false><<<dim3((cell_slabs::COUNT + 127) / 128, nblk, GUARD_SPLIT), 128, 0, s>>>(
+        k_guard_cells_plan<false><<<dim3((cell_slabs::COUNT + 127) / 128, nblk), 128, 0, s>>>(
             g_gb.grid, g_gb.tree, list, hydro_guard_vars(), plan);
     } else {
         k_guard_cells<<<dim3((GB_NGC + 127) / 128, nblk), 128, 0, s>>>(g_gb.grid, g_gb.tree, list,
