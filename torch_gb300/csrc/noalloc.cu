@@ -18,6 +18,8 @@
 // reads only regions an earlier kernel of the same call wrote. Calls that
 // overlap on the GPU (two streams, two host threads) race on the array.
 // Compiled with -fmad=false, as the allocating FP64 path.
+#include <atomic>
+
 #include "hydro_launch.cuh"
 
 namespace {
@@ -27,7 +29,9 @@ constexpr size_t kBlockBytes = gbh::scratch_layout<double>::bytes;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[GB_NOALLOC_MAX_BLOCKS * kBlockBytes];
 
 constexpr int kMaxDevices = 64;
-void* g_scratch_addr[kMaxDevices] = {nullptr};
+// looked up once per device; threads that race on the first call store the
+// same address (atomics keep that free of a data race)
+std::atomic<void*> g_scratch_addr[kMaxDevices];
 
 // per-device set-up: the device address of the static scratch array
 int scratch_for_current_device(void** out)
@@ -38,13 +42,13 @@ int scratch_for_current_device(void** out)
         gb_set_error("gb_hydro_unsplit_noalloc: device ordinal %d beyond %d", dev, kMaxDevices);
         return GB_ERR_LIMIT;
     }
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
+    void* p = g_scratch_addr[dev].load(std::memory_order_acquire);
+    if (!p) {
         if (gb_check(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(noalloc scratch)"))
             return GB_ERR_CUDA;
-        g_scratch_addr[dev] = p;
+        g_scratch_addr[dev].store(p, std::memory_order_release);
     }
-    *out = g_scratch_addr[dev];
+    *out = p;
     return GB_OK;
 }
 
