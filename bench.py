@@ -51,7 +51,7 @@ TDUST0 = 18.0  # initial dust temperature [K] (sim_tdust, flash.par.turbsph_stan
 # reconstruction, "emf" = time-n edge fields + edge fields, "guard_fill" =
 # cells + faces. The roofline's traffic is this times the zones one launch
 # covers.
-TRAFFIC_B_PER_ZONE = {"recon": 760.0, "update": 398.0, "flux": 484.0, "guard_fill": 305.0, "mlp_infer": 16.0,
+TRAFFIC_B_PER_ZONE = {"recon": 764.0, "update": 398.0, "flux": 484.0, "guard_fill": 305.0, "mlp_infer": 16.0,
                       "sur_accept": 111.0, "emf": 151.0, "faceb": 81.0, "dt": 101.0}
 
 
