@@ -1,8 +1,9 @@
 """CPU oracle of the cooling-surrogate MLP (test infrastructure only).
 
 Float64 NumPy forward and backward of the 4 -> 64 -> 64 -> 64 -> 1 SiLU
-network with the weights rounded to BF16 in the forward pass, as the GPU
-training kernels do; used to check the GPU gradients.
+network with the weights rounded to BF16, as the GPU kernels use them, and
+optionally the BF16 roundings of the tensor-core training pass; used to
+check the GPU gradients and inference.
 """
 from __future__ import annotations
 
@@ -42,25 +43,32 @@ def dsilu(z):
     return s * (1.0 + z * (1.0 - s))
 
 
-def loss_and_grad(w, x, t):
+def loss_and_grad(w, x, t, bf16_operands=False):
+    """Loss and gradient of one batch. bf16_operands restates the
+    tensor-core training pass (torch_gb300/csrc/mlp.cu, k_mlp_train_tc):
+    the inputs, the activations and the gradient operands of the MMAs (dy for
+    layer 4, dz for layers 1-3) rounded to BF16, every product accumulated
+    exactly; without it, the exact network with BF16 weights."""
     W1, b1, W2, b2, W3, b3, W4, b4 = unpack(w)
-    x = np.asarray(x, np.float64)
+    q = bf16 if bf16_operands else (lambda a: np.asarray(a, np.float64))
+    x = q(x)
     t = np.asarray(t, np.float64)
-    z1 = x @ W1.T + b1; a1 = silu(z1)
-    z2 = a1 @ W2.T + b2; a2 = silu(z2)
-    z3 = a2 @ W3.T + b3; a3 = silu(z3)
+    z1 = x @ W1.T + b1; a1 = q(silu(z1))
+    z2 = a1 @ W2.T + b2; a2 = q(silu(z2))
+    z3 = a2 @ W3.T + b3; a3 = q(silu(z3))
     y = (a3 @ W4.T + b4)[:, 0]
     n = x.shape[0]
     r = y - t
     loss = np.mean(r * r)
     dy = (2.0 * r / n)[:, None]
     g = np.zeros(NPAR)
-    g[OW4:OB4] = (dy.T @ a3).ravel(); g[OB4] = dy.sum()
-    d3 = (dy @ W4) * dsilu(z3)
+    dyq = q(dy)
+    g[OW4:OB4] = (dyq.T @ a3).ravel(); g[OB4] = dyq.sum()
+    d3 = q((dy @ W4) * dsilu(z3))
     g[OW3:OB3] = (d3.T @ a2).ravel(); g[OB3:OW4] = d3.sum(0)
-    d2 = (d3 @ W3) * dsilu(z2)
+    d2 = q((d3 @ W3) * dsilu(z2))
     g[OW2:OB2] = (d2.T @ a1).ravel(); g[OB2:OW3] = d2.sum(0)
-    d1 = (d2 @ W2) * dsilu(z1)
+    d1 = q((d2 @ W2) * dsilu(z1))
     g[OW1:OB1] = (d1.T @ x).ravel(); g[OB1:OW2] = d1.sum(0)
     return loss, g
 

@@ -24,17 +24,26 @@ def trained(gb):
 
 
 def test_gpu_gradient_matches_cpu_oracle(gb):
+    """The tensor-core training pass against the oracle restating its BF16
+    operands (inputs, activations, gradient operands), and against the exact
+    network, where those roundings account for the difference."""
     import torch
     from oracle import mlp_oracle as M
     gb.mlp_init(11)
     rng = np.random.default_rng(2)
-    x = rng.normal(0, 1, (512, 4)).astype(np.float32)
-    t = rng.normal(0, 0.3, 512).astype(np.float32)
-    g, loss = gb.mlp_grad(torch.as_tensor(x, device="cuda"), torch.as_tensor(t, device="cuda"))
-    w = gb.mlp_weights()
-    loss_o, g_o = M.loss_and_grad(w, x, t)
-    assert abs(loss - loss_o) <= 1e-4 * abs(loss_o)
-    assert np.linalg.norm(g - g_o) <= 1e-3 * np.linalg.norm(g_o)
+    for n in (512, 300):  # whole tiles and a ragged last tile
+        x = rng.normal(0, 1, (n, 4)).astype(np.float32)
+        t = rng.normal(0, 0.3, n).astype(np.float32)
+        g, loss = gb.mlp_grad(torch.as_tensor(x, device="cuda"), torch.as_tensor(t, device="cuda"))
+        w = gb.mlp_weights()
+        loss_o, g_o = M.loss_and_grad(w, x, t, bf16_operands=True)
+        loss_e, g_e = M.loss_and_grad(w, x, t)
+        err = np.linalg.norm(g - g_o) / np.linalg.norm(g_o)
+        err_e = np.linalg.norm(g - g_e) / np.linalg.norm(g_e)
+        print("gradient relative error", n, "vs BF16-operand oracle", err, "vs exact", err_e)
+        assert abs(loss - loss_o) <= 1e-4 * abs(loss_o)
+        assert err <= 5e-4
+        assert err_e <= 2e-2
 
 
 def test_training_reduces_loss(trained):

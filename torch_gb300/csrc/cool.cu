@@ -792,7 +792,7 @@ int gb_launch_surrogate(int nblk, const int* list, double dt, const double* dtp,
         gb_prof_end(GBP_SUR_FEAT, s);
     }
     gb_prof_begin(GBP_MLP, s);
-    rc = gb_mlp_launch_infer(ncell, g_sb.feat, g_sb.y, s);
+    rc = gb_mlp_launch_infer(ncell, g_sb.feat, g_sb.y, st, s);
     gb_prof_end(GBP_MLP, s);
     if (rc) return rc;
     cudaMemsetAsync(g_sb.nrej, 0, sizeof(int), s);
