@@ -436,16 +436,21 @@ int gb_grid_download_faces_interior_list(double* fx_host, double* fy_host, doubl
 int gb_mlp_init_random(uint64_t seed);
 int gb_mlp_set_weights(const float* host, int n);
 int gb_mlp_get_weights(float* host, int n);
-/* Loss and gradient of the mean squared error on n device samples
- * (feat: n x 4, target: n) into host buffers (for gradient checks). */
+/* Loss and gradient of the mean squared error on n <= 2^20 device samples
+ * (feat: n x 4, 16-byte aligned; target: n) into host buffers, from the
+ * tensor-core training pass (BF16 inputs, activations and gradient
+ * operands, FP32 accumulation). */
 int gb_mlp_grad(const float* feat_dev, const float* target_dev, int n, float* grad_host, float* loss_host,
                 void* stream);
-/* Adam training on device samples: `steps` mini-batches of `batch` drawn
- * with a seeded generator; per-step loss written to loss_host (may be NULL). */
+/* Adam training on device samples: `steps` mini-batches of `batch` drawn on
+ * the device with a seeded counter hash, each step one tensor-core
+ * forward/backward kernel and one Adam kernel (no host synchronisation
+ * between steps); per-step loss written to loss_host (may be NULL). */
 int gb_mlp_train(const float* feat_dev, const float* target_dev, int64_t n, int steps, int batch, float lr,
                  uint64_t seed, float* loss_host, void* stream);
-/* Inference on n cells; tensor_cores = 1 uses the BF16 mma path, 0 a
- * CUDA-core FP32 path with the same BF16-rounded weights. */
+/* Inference on n cells (feat 16-byte aligned); tensor_cores = 1 uses the
+ * tcgen05 path (BF16 operands, FP32 accumulators in tensor memory), 0 a
+ * CUDA-core FP32 reference with the same BF16-rounded weights. */
 int gb_mlp_infer(int64_t n, const float* feat_dev, float* y_dev, int tensor_cores, void* stream);
 /* Training samples from the plain implicit integrator: log n ~ U[-2, 6],
  * log T ~ U[1, 8], log(dt/t_cool) ~ U[-3, 3], log G ~ U[-1, 1]; writes
