@@ -283,6 +283,26 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
+def host_link_gbs(nbytes=1 << 29, reps=3):
+    """Bandwidth of the host link (pinned host memory <-> HBM) with plain
+    copies of one large buffer, best of `reps`: the ceiling of the
+    end-to-end path's transfers."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = [0.0, 0.0]
+    for _ in range(reps):
+        for k, (dst, src) in enumerate(((d, h), (h, d))):
+            a.record()
+            dst.copy_(src, non_blocking=True)
+            b.record()
+            torch.cuda.synchronize()
+            best[k] = max(best[k], nbytes / (a.elapsed_time(b) * 1e-3) / 1e9)
+    del h, d
+    return best[0], best[1]
+
+
 def e2e_run(G, g, steps, warmup, tune=False):
     """Fast path through the C ABI as a FLASH host would drive it: the host
     owns unk (FLASH order, variable fastest) and facevar{x,y,z} in pinned
@@ -358,10 +378,21 @@ def e2e_run(G, g, steps, warmup, tune=False):
     nbytes = nl * (16 ** 3 * nunk + 3 * 17 * 16 * 16) * 8
     separate()
     c, t, o = G.get_launch_config()
+    # the link's ceiling: the upload precedes the step (the guard fill needs
+    # every leaf), the download can hide under the compute
+    h2d, d2h = host_link_gbs()
+    t_up, t_down = nbytes / (h2d * 1e9) * 1e3, nbytes / (d2h * 1e9) * 1e3
+    bound = t_up + max(parts[1], t_down)
     return ms, nbytes, {"upload_ms": parts[0], "step_ms": parts[1], "download_ms": parts[2],
+                        "link_h2d_gbs": h2d, "link_d2h_gbs": d2h,
+                        "upload_gbs": nbytes / (parts[0] * 1e-3) / 1e9,
+                        "download_gbs": nbytes / (parts[2] * 1e-3) / 1e9,
+                        "bound_ms": bound, "frac_of_bound": bound / ms,
                         "launch_config": {"chunk": c, "tile": t, "occ": o, "streams": G.get_chunk_streams()},
                         "note": "parts from one step run as separate calls; the timed steps overlap the "
-                                "download of each chunk with the compute of later chunks"}
+                                "download of each chunk with the compute of later chunks; bound_ms = the "
+                                "bytes over the measured link rate for the upload, plus the larger of the "
+                                "device step and the download"}
 
 
 def rel_stats(x, ref):
