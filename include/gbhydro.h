@@ -480,6 +480,13 @@ int gb_set_cooling_mode(int mode, double rel_tol, int check_fp64);
 int gb_prof_enable(int on);
 int gb_prof_read(double* ms, long long* launches, int n);
 
+/* Self-check of the bounded waits in the tcgen05 and TMA kernels: one
+ * thread waits, for at most limit_cycles (1e3 .. 4e9) SM cycles, on an
+ * mbarrier that nothing arrives on (arrive = 0) or on one it arrived on
+ * itself (arrive = 1). *result_host: 1 the wait completed, 2 it gave up and
+ * recorded GB_ST_TIMEOUT in st (may be NULL). Nothing is left in flight, so
+ * the context stays usable. */
+int gb_check_bounded_wait(long long limit_cycles, int arrive, gb_status* st, int* result_host, void* stream);
 /* Measured FP64 FMA throughput of the current GPU in TFLOP/s (2 flops per
  * FMA; a few milliseconds of independent FMA chains on every SM): the
  * denominator of the FP64-pipe roofline. */

@@ -881,6 +881,35 @@ int gb_mlp_launch_infer(int64_t n, const float* feat, float* y, gb_status* st, c
     return gb_check(cudaGetLastError(), "k_mlp_infer_tc") ? GB_ERR_CUDA : GB_OK;
 }
 
+// Self-check of the bounded mbarrier wait the tcgen05 kernels use: one
+// thread waits, for at most `limit` SM cycles, on a barrier that nothing
+// arrives on (or, with `arrive`, on one it arrived on itself, which must
+// complete at once) and records GB_ST_TIMEOUT when the wait gives up. No
+// copy or MMA is in flight, so the context stays usable either way.
+__global__ void k_wait_check(long long limit, int arrive, gb_status* st, int* result)
+{
+    __shared__ unsigned long long bar;
+    if (threadIdx.x != 0) return;
+    tc05::mbar_init(&bar, 1);
+    if (arrive) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc05::saddr(&bar)) : "memory");
+    const bool ok = tc05::mbar_wait(&bar, 0u, limit);
+    if (!ok) gb_fail(st, GB_ST_TIMEOUT, -1, 0, 0, 0, (double)limit);
+    *result = ok ? 1 : 2;
+}
+
+extern "C" int gb_check_bounded_wait(long long limit_cycles, int arrive, gb_status* st, int* result_host, void* stream)
+{
+    if (limit_cycles < 1000 || limit_cycles > 4000000000LL || !result_host) return GB_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    int* d = nullptr;
+    if (gb_check(cudaMalloc(&d, sizeof(int)), "wait check")) return GB_ERR_CUDA;
+    k_wait_check<<<1, 32, 0, s>>>(limit_cycles, arrive, st, d);
+    cudaMemcpyAsync(result_host, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+    const bool bad = gb_check(cudaStreamSynchronize(s), "k_wait_check");
+    cudaFree(d);
+    return bad ? GB_ERR_CUDA : GB_OK;
+}
+
 extern "C" int gb_mlp_infer(int64_t n, const float* feat, float* y, int tensor_cores, void* stream)
 {
     if (n < 0 || (n > 0 && (!feat || !y || !aligned16(feat)))) return GB_ERR_ARG;

@@ -129,6 +129,7 @@ _SIG = {
     "gb_set_flux_correction": (C.c_int, [C.c_int]),
     "gb_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
     "gb_measure_fp32_peak": (C.c_int, [C.POINTER(C.c_double)]),
+    "gb_check_bounded_wait": (C.c_int, [C.c_longlong, C.c_int, C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
     "gb_selfcheck_conversions": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gb_graph_reset": (C.c_int, []),
     "gb_graph_info": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
@@ -438,6 +439,18 @@ def measure_fp64_peak() -> float:
     v = C.c_double()
     check(lib().gb_measure_fp64_peak(C.byref(v)), "gb_measure_fp64_peak")
     return v.value
+
+
+def check_bounded_wait(limit_cycles: int, arrive: bool):
+    """Run the bounded-wait self-check: (1 completed or 2 gave up, the
+    status it recorded as a dict)."""
+    st = status_buffer()
+    r = C.c_int(0)
+    check(lib().gb_check_bounded_wait(int(limit_cycles), int(arrive), _ptr(st), C.byref(r), _stream()),
+          "gb_check_bounded_wait")
+    s = Status()
+    check(lib().gb_status_read(_ptr(st), C.byref(s)), "gb_status_read")
+    return r.value, s.as_dict()
 
 
 def measure_fp32_peak() -> float:
