@@ -77,3 +77,52 @@ def test_fullsize_amr_conservation_and_divb(gb, config, precision):
     assert abs(t1[0] - t0[0]) <= 1e-12 * t0[0], (t0[0], t1[0])
     assert np.all(np.abs(t1[1:] - t0[1:]) <= 1e-12 * m0[1:]), (t0, t1, m0)
     assert divb() <= 1e-12
+
+
+def test_fullsize_amr_compliant_path_with_cooling(gb):
+    """The metric-compliant path (mixed hydro, the plain integrator on FP32
+    rates) with cooling on the 4101-leaf configuration: two graph-replayed
+    steps keep mass and momentum to round-off (cooling changes neither), div B
+    at round-off, a clean status (no root-finder failure, no floor), and
+    finite temperatures inside the integrator's bounds."""
+    import torch
+    tree, st = _state(3)
+    units = gb.code_units()
+    gb.init_cooling(gb.cool_params(dens_unit=units["dens_unit"], vel_unit=units["vel_unit"],
+                                   time_unit=units["time_unit"]))
+    g = gb.grid_from_amr(tree, st, mhd=True, cooling=True)
+    root_dx = st["root_dx"]
+    del st
+    s = g.slots
+    g.u[:, s["TEMP"]] = g.u[:, s["EINT"]] * units["vel_unit"] ** 2 * (2.0 / 3.0) * (24.0 / 11.0) * gb.MP / gb.KB
+    g.u[:, s["TDUS"]] = 18.0
+    gb.init_hydro(gb.hydro_params(True, precision=1))
+    gb.set_cooling_mode(2)
+    try:
+        g.register()
+        leaf = g.t_leaf.long()
+        lv = torch.as_tensor(np.asarray(tree["level"])[g.leaf], dtype=torch.float64, device="cuda")
+        vol = (root_dx / 2 ** lv) ** 3
+
+        def mass_mom():
+            u = g.u[leaf][:, :, 4:20, 4:20, 4:20]
+            rho = u[:, s["DENS"]]
+            q = [rho, rho * u[:, s["VELX"]], rho * u[:, s["VELY"]], rho * u[:, s["VELZ"]]]
+            return (torch.stack([(x.sum(dim=(1, 2, 3)) * vol).sum() for x in q]).cpu().numpy(),
+                    torch.stack([(x.abs().sum(dim=(1, 2, 3)) * vol).sum() for x in q]).cpu().numpy())
+
+        t0, m0 = mass_mom()
+        g.status_reset()
+        for _ in range(2):
+            g.step_graph(cool=True)
+        torch.cuda.synchronize()
+        t1, _ = mass_mom()
+        stt = g.status_read()
+        assert stt["code"] == 0 and not stt["n_code"], stt
+        T = g.u[leaf][:, s["TEMP"], 4:20, 4:20, 4:20]
+        p = gb.cool_params()
+        assert bool(torch.isfinite(T).all()) and float(T.min()) >= p.absTmin and float(T.max()) <= p.absTmax
+        assert abs(t1[0] - t0[0]) <= 1e-12 * t0[0]
+        assert np.all(np.abs(t1[1:] - t0[1:]) <= 1e-12 * m0[1:])
+    finally:
+        gb.set_cooling_mode(0)
