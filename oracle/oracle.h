@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY. Nothing in the product library links, loads or
  * calls this code; only tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline use it, as the checker that GPU results are compared against.
+ * baseline use it, as the reference the GPU results are compared against.
  *
  * Cooling part: a statement-level C restatement of the vendored Fortran
  *   src/flash/source/physics/sourceTerms/Heat/HeatMain/HeatCool/phenHeat/

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/liboracle.so).
 
-Test infrastructure only: used by tests/, by ``__graft_entry__.smoke()`` as
-the checker, and by ``bench.py`` for the timed CPU baseline. The product
+Test infrastructure only: used by tests/, by ``__graft_entry__.smoke()`` to
+compare GPU results against, and by ``bench.py`` for the timed CPU baseline. The product
 library never imports this module.
 """
 from __future__ import annotations
