@@ -31,7 +31,9 @@ def test_gpu_gradient_matches_cpu_oracle(gb):
     from oracle import mlp_oracle as M
     gb.mlp_init(11)
     rng = np.random.default_rng(2)
-    for n in (512, 300):  # whole tiles and a ragged last tile
+    # whole tiles, a ragged last tile, and more tiles than SMs (each CTA
+    # then sums two or three tiles' weight gradients in tensor memory)
+    for n in (512, 300, 40000):
         x = rng.normal(0, 1, (n, 4)).astype(np.float32)
         t = rng.normal(0, 0.3, n).astype(np.float32)
         g, loss = gb.mlp_grad(torch.as_tensor(x, device="cuda"), torch.as_tensor(t, device="cuda"))
