@@ -86,7 +86,9 @@ struct tc_layout {
     static constexpr int ONES = WBYTES;                // K-groups 8 (ones column) and 9 (zero)
     static constexpr int TILE0 = ONES + 2 * A_LBO;     // per warpgroup: A1 (2 groups) then A (8 groups)
     static constexpr int A1_OFF = 0, A_OFF = 2 * A_LBO, TILE_BYTES = 10 * A_LBO;
-    static constexpr int BAR = TILE0 + WG * TILE_BYTES;  // WG mbarriers, then the TMEM address
+    // WG mbarriers, the TMEM address, the weight copy's mbarrier
+    static constexpr int BAR = TILE0 + WG * TILE_BYTES;
+    static constexpr int WBAR = BAR + 8 * WG + 8;
     static constexpr int BYTES = BAR + 8 * WG + 16;
     static constexpr uint32_t COLS_PER_WG = 64, TMEM_COLS = COLS_PER_WG * WG;
 };
@@ -119,8 +121,9 @@ struct tr_layout {
     static constexpr int DTA = XT + 16 * XT_LBO;  // rows: dz3^T (0-63), dy^T (64), zeros
     static constexpr int DTB = DTA + 16 * DT_LBO;  // rows: dz2^T (0-63), dz1^T (64-127)
     static constexpr int RED = DTB + 16 * DT_LBO;  // 4 floats: the warps' loss sums
-    static constexpr int BAR = RED + 16;
-    static constexpr int BYTES = BAR + 16;
+    static constexpr int BAR = RED + 16;  // the MMA barrier, the TMEM address, the weight copy's barrier
+    static constexpr int WBAR = BAR + 16;
+    static constexpr int BYTES = BAR + 24;
     // tensor-memory columns: pre-activations (the data gradients overwrite
     // them once read), the output, and the weight-gradient accumulators
     // (128 lanes; only the rows the A stack makes meaningful are read)
@@ -129,7 +132,7 @@ struct tr_layout {
 };
 static_assert(tr_layout::BYTES <= 227 * 1024, "tcgen05 MLP training fits shared memory");
 static_assert(tr_layout::G4 + 80 <= tr_layout::TMEM_COLS, "training accumulators fit tensor memory");
-static_assert(tr_layout::AT1 % 16 == 0 && tr_layout::XT % 16 == 0 && tr_layout::DTA % 16 == 0 &&
+static_assert(tr_layout::AT1 % 16 == 0 && tr_layout::XT % 16 == 0 && tr_layout::DTA % 16 == 0 && tr_layout::WT3 % 16 == 0 &&
                   tr_layout::DTB % 16 == 0 && tr_layout::RED % 16 == 0,
               "16-byte operands");
 
@@ -185,7 +188,13 @@ __global__ void __launch_bounds__(128 * tc_layout::WG) k_mlp_infer_tc(int64_t n,
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + L::BAR + 8 * L::WG);
     unsigned char* tile_sm = sm + L::TILE0 + wg * L::TILE_BYTES;
 
-    for (int i = tid; i < L::WBYTES / 16; i += blockDim.x) reinterpret_cast<uint4*>(sm)[i] = wimg[i];
+    // the weight image arrives by one bulk copy while the CTA sets up
+    unsigned long long* wbar = reinterpret_cast<unsigned long long*>(sm + L::WBAR);
+    if (tid == 0) {
+        tc05::mbar_init(wbar, 1);
+        tc05::mbar_expect_tx(wbar, L::WBYTES);
+        tc05::bulk_g2s(sm, wimg, L::WBYTES, wbar);
+    }
     // constant parts of the A operands: the shared ones block, and the zero
     // second K-group of each layer-1 A
     const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
@@ -274,7 +283,7 @@ __global__ void __launch_bounds__(128 * tc_layout::WG) k_mlp_infer_tc(int64_t n,
     int64_t tile = (int64_t)blockIdx.x * L::WG + wg;
     float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
     if (tile < ntiles && tile * L::M + t < n) f = feat[tile * L::M + t];
-    bool done = true;
+    bool done = tc05::mbar_wait(wbar, 0u, TC_WAIT_CYCLES);  // the weights (a failure ends the loop at once)
     for (; tile < ntiles; tile += tstep) {
         const int64_t row = tile * L::M + t;
         reinterpret_cast<uint4*>(tile_sm + L::A1_OFF)[t] =
@@ -312,6 +321,7 @@ __global__ void __launch_bounds__(128 * tc_layout::WG) k_mlp_infer_tc(int64_t n,
             if (tile * L::M + t < n) y[tile * L::M + t] = __int_as_float(0x7fc00000);
         if (t == 0) gb_fail(st, GB_ST_TIMEOUT, -1, 0, 0, 0, 0.0);
         tc05::mbar_wait(bar, phase ^ 1u, TC_WAIT_CYCLES);
+        tc05::mbar_wait(wbar, 0u, TC_WAIT_CYCLES);
     }
     tc05::fence_before_sync();
     __syncthreads();
@@ -362,8 +372,14 @@ k_mlp_train_tc(const float4* __restrict__ feat, const float* __restrict__ target
     float* red = reinterpret_cast<float*>(sm + T::RED);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
 
-    for (int i = t; i < L::WBYTES / 16; i += blockDim.x) reinterpret_cast<uint4*>(sm)[i] = fw[i];
-    for (int i = t; i < 2 * T::WT_BYTES / 16; i += blockDim.x) reinterpret_cast<uint4*>(sm + T::WT3)[i] = wt[i];
+    // the weight images arrive by two bulk copies while the CTA sets up
+    unsigned long long* wbar = reinterpret_cast<unsigned long long*>(sm + T::WBAR);
+    if (t == 0) {
+        tc05::mbar_init(wbar, 1);
+        tc05::mbar_expect_tx(wbar, L::WBYTES + 2 * T::WT_BYTES);
+        tc05::bulk_g2s(sm, fw, L::WBYTES, wbar);
+        tc05::bulk_g2s(sm + T::WT3, wt, 2 * T::WT_BYTES, wbar);
+    }
     // constant operand parts: the forward ones block and layer 1's zero
     // K-group; rows 64 (ones) .. 79 of the activation operands, rows 4
     // (ones) .. 15 of x's, rows 65 .. 127 of the layer-3/4 stack (zeros)
@@ -487,7 +503,7 @@ k_mlp_train_tc(const float4* __restrict__ feat, const float* __restrict__ target
     };
 
     float loss = 0.0f;
-    bool done = true;
+    bool done = tc05::mbar_wait(wbar, 0u, TC_WAIT_CYCLES);  // the weights (a failure ends the loop at once)
     const int ntiles = (batch + 127) / 128;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int b = tile * 128 + t;
@@ -626,6 +642,7 @@ k_mlp_train_tc(const float4* __restrict__ feat, const float* __restrict__ target
         for (int i = t; i < PSTRIDE; i += blockDim.x) out[i] = __int_as_float(0x7fc00000);
         if (t == 0) gb_fail(st, GB_ST_TIMEOUT, -1, 0, 0, 0, 0.0);
         tc05::mbar_wait(bar, phase ^ 1u, TC_WAIT_CYCLES);
+        tc05::mbar_wait(wbar, 0u, TC_WAIT_CYCLES);
     }
     tc05::fence_before_sync();
     __syncthreads();

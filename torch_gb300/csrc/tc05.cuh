@@ -80,6 +80,24 @@ __device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t coun
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+// announce `bytes` of asynchronous copies completing on the barrier (one
+// arrival by this thread)
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+}
+
+// bulk copy (the TMA engine, no tensor map) of `bytes` from global to this
+// CTA's shared memory, completing on the barrier: both addresses 16-byte
+// aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, unsigned long long* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(saddr(dst)),
+        "l"(src), "r"(bytes), "r"(saddr(bar))
+        : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity)
 {
     uint32_t ok;
