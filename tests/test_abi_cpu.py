@@ -62,3 +62,27 @@ def test_block_lists_are_checked_on_the_host():
                       ([5], "not a leaf"), ([1, 3, 1], "more than once"), ([1.0], "integers")):
         with pytest.raises(G.GBError, match=what):
             G.check_leaf_ids(bad, 6, leaf)
+
+
+def test_mlp_and_wait_entries_reject_bad_arguments_without_gpu():
+    """The surrogate MLP's entries and the bounded-wait self-check reject
+    bad arguments before any device work: null or unaligned feature
+    arrays, empty or oversized batches, an inference without weights, a
+    wait limit outside 1e3 .. 4e9 cycles."""
+    import ctypes as C
+    from torch_gb300 import gbhydro as G
+    L = G.lib()
+    ERR_ARG = -1
+    assert L.gb_mlp_train(None, None, 10, 1, 16, C.c_float(1e-3), 1, None, None) == ERR_ARG
+    assert L.gb_mlp_train(C.c_void_p(16), C.c_void_p(16), 10, 0, 16, C.c_float(1e-3), 1, None, None) == ERR_ARG
+    assert L.gb_mlp_train(C.c_void_p(16), C.c_void_p(16), 10, 1, (1 << 20) + 1, C.c_float(1e-3), 1, None,
+                          None) == ERR_ARG
+    assert L.gb_mlp_train(C.c_void_p(20), C.c_void_p(16), 10, 1, 16, C.c_float(1e-3), 1, None, None) == ERR_ARG
+    assert L.gb_mlp_grad(None, None, 10, None, None, None) == ERR_ARG
+    assert L.gb_mlp_grad(C.c_void_p(16), C.c_void_p(16), 0, None, None, None) == ERR_ARG
+    assert L.gb_mlp_infer(-1, None, None, 1, None) == ERR_ARG
+    assert L.gb_mlp_infer(4, C.c_void_p(20), C.c_void_p(16), 1, None) == ERR_ARG
+    r = C.c_int(0)
+    assert L.gb_check_bounded_wait(10, 0, None, C.byref(r), None) == ERR_ARG
+    assert L.gb_check_bounded_wait(5_000_000_000, 0, None, C.byref(r), None) == ERR_ARG
+    assert L.gb_check_bounded_wait(2_000_000, 0, None, None, None) == ERR_ARG
