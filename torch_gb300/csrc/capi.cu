@@ -2190,10 +2190,10 @@ static void launch_prio(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cud
 }
 
 // CTAs of a download running beside compute: enough rows in flight to
-// keep the host link busy (about 200 GB/s at a few microseconds of
-// latency), few enough to leave the SMs to the compute kernels. Measured
-// on the 4101-leaf step: 32 CTAs 77 ms per step, 128 41 ms, 256 and 512
-// 37.5 ms, 1024 41 ms, one CTA per row group (no limit) 47.5 ms.
+// keep the host link busy (about 190 GB/s device to host at a few
+// microseconds of latency), few enough to leave the SMs to the compute
+// kernels. Measured on the 4101-leaf host-resident step (256-block chunks):
+// 128 CTAs 35.0 ms per step, 192 33.1 ms, 256 31.6 ms, 384 32.2 ms.
 constexpr int g_io_ctas = 256;
 
 static void launch_io(bool up, const host_io_dev& io, int nblk, const int* list, cudaStream_t s)
