@@ -835,9 +835,9 @@ def main():
         "mixed_fp32_rates_cooling": {"value": zones * world / (ms_m32 * 1e-3), "ms_per_step": ms_m32,
                                      "speedup_vs_plain_fp64": ms_plain / ms_m32, "l1_err_vs_fp64": l1_m32,
                                      "temp_rel_err_vs_plain_after_steps": temp_m32,
-                                     "note": "mixed hydro; the plain integrator fused into the update with its "
-                                             "rate function in FP32 (Brent's and the bracket search's iterates "
-                                             "and the residual in FP64)"},
+                                     "note": "mixed hydro; the plain integrator as a pass of its own after the "
+                                             "update, its rate function in FP32 (Brent's and the bracket search's "
+                                             "iterates and the residual in FP64)"},
         "roundoff_divergence_plain_fp64": roundoff,
         "accuracy_condition": accuracy_condition(l1_fast, l1_mixed, l1_fast_exact, roundoff,
                                                  zones * world / (ms_fast * 1e-3), ms_plain / ms_fast,

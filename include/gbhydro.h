@@ -460,8 +460,8 @@ int gb_surrogate_samples(int64_t n, uint64_t seed, float* feat_dev, float* targe
                          void* stream);
 /* Cooling mode of gb_evolve_step(cool = 1): 0 = plain integrator fused in
  * the update, 1 = surrogate with per-cell acceptance test and plain
- * fallback, 2 = the plain integrator fused in the update with its rate
- * function de/dt evaluated in FP32 (the mixed path; Brent's and the
+ * fallback, 2 = the plain integrator, as a pass of its own after the
+ * update, with its rate function de/dt evaluated in FP32 (the mixed path; Brent's and the
  * bracket search's iterates and the residual stay FP64; the FP64 path
  * keeps its reference rates in every mode but 1). The network's prediction starts at most four FP32 secant-Newton
  * iterations on the backward-Euler residual; a cell is accepted when a

@@ -1579,8 +1579,9 @@ int gb_launch_hydro(int nblk, const int* list, double dt, const double* dtp, int
     }
     for (int k = 0, b0 = 0; b0 < nblk; ++k, b0 += chunk) {
         int nb = nblk - b0 < chunk ? nblk - b0 : chunk;
-        // the plain integrator fused into the update: 1 on the precision
-        // path's own rates, 2 on FP32 rates (mixed path; FP64 ignores it)
+        // the plain integrator after the update: 1 fused into it on the
+        // precision path's own rates, 2 on FP32 rates (mixed path: a pass of
+        // its own after the update; FP64 takes it as 1)
         const int fused = !cool ? 0 : gb_cooling_mode() == 0 ? 1 : gb_cooling_mode() == 2 ? 2 : 0;
         const int chain = ns > 1 ? (k & 1) : 0;
         cudaStream_t sk = chain ? g_aux.s2 : s;

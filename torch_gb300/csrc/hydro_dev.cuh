@@ -1828,11 +1828,10 @@ __device__ __forceinline__ double rcp_newton(double x)
 // state (what the feature kernel would compute next): FP32 work beside this
 // FP64-bound kernel instead of a kernel of its own
 // mixed path without the fused plain cooling: eight resident CTAs per SM
-// (64 registers, no spills); with the integrator on FP32 rates four (117
-// registers, no spills: the integrator is latency-bound, so resident warps
-// pay); the FP64 path and the FP64-rate integrator need more registers
+// (64 registers, no spills); the FP64 path and the FP64-rate integrator need
+// more registers (the FP32-rate integrator runs in k_cool_pass)
 template <typename T, bool MHD, int COOL, bool FEAT>
-__global__ void __launch_bounds__(128, (std::is_same<T, float>::value && !COOL) ? 8 : COOL == 2 ? 4 : 1)
+__global__ void __launch_bounds__(128, (std::is_same<T, float>::value && !COOL) ? 8 : 1)
 k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restrict__ list,
          const T* __restrict__ fscr, size_t fstride, const double* __restrict__ bscr, size_t bstride,
          gb_status* st, sur_feat_out sf)
@@ -1986,8 +1985,8 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
         bool clamped = false;
         if (good) {
             // the mixed path evaluates the rates with shared transcendentals
-            // (one ln T and one sqrt T per evaluation; COOL 2: in FP32); the
-            // FP64 path keeps the reference's formulation
+            // (one ln T and one sqrt T per evaluation); the FP64 path keeps
+            // the reference's formulation
             gbcool::heating_and_cooling<RCP ? COOL : 0>(cool, v, &eic, kp_dt(kp) * p.time_unit, &temp, &dg);
             if (temp > p.absTmax) {
                 eic = p.absTmax * v.TtoEI;
@@ -2037,6 +2036,68 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
         const int64_t idx = (int64_t)cb * (GB_NXB * GB_NXB * GB_NXB) + t;
         sf.feat[idx] = x;
         sf.f0[idx] = f0fl;
+    }
+}
+
+// The plain integrator on FP32 rates (the mixed path's cooling mode 2) as a
+// pass of its own over a chunk's interior cells, after the update without
+// it: the inputs of the fused epilogue of k_update (the new density and
+// internal energy, the stored dust temperature and source terms) and its
+// stores; the specific kinetic energy of the total energy comes from the
+// stored velocities. Its own kernel keeps the integrator's long code apart
+// from the update's.
+static __global__ void __launch_bounds__(128, 4)
+k_cool_pass(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restrict__ list, gb_status* st)
+{
+    const int cb = blockIdx.y;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= GB_NXB * GB_NXB * GB_NXB) return;
+    const int blk = list[cb];
+    const int i = LO + t % GB_NXB, j = LO + (t / GB_NXB) % GB_NXB, k = LO + t / (GB_NXB * GB_NXB);
+    const int ci = gb_cidx(i, j, k);
+    double* base = g.unk + (int64_t)blk * g.nvar * GB_N3;
+    auto UV = [&](int role) -> double& { return base[(int64_t)g.slot[role] * GB_N3 + ci]; };
+    const double gm1 = kp.gamma - 1.0;
+    const double rn = UV(GB_DENS);
+    const gb_cool_params& p = cool.p;
+    gb_cool_vars v;
+    v.rho = rn * p.dens_unit;
+    double eic = UV(GB_EINT) * (p.vel_unit * p.vel_unit);
+    double temp = eic * (gm1 * p.eos_abar * p.mp / p.boltz);
+    v.tdust = UV(GB_TDUS);
+    v.xHp = g.slot[GB_IHP] >= 0 ? UV(GB_IHP) : p.xHp_const;
+    v.ephen = g.slot[GB_PHHE] >= 0 ? UV(GB_PHHE) / v.rho : 0.0;
+    v.Gflux = g.slot[GB_PEFL] >= 0 ? UV(GB_PEFL) : 0.0;
+    v.mu_mol = p.mu_mol;
+    v.strat_factor = 1.0;
+    gb_cool_diag dg = {0, 0, 0, 0, 0};
+    const bool good = gb_finite_pos(v.rho) && gb_finite_pos(eic) && gb_finite_pos(temp);
+    bool clamped = false;
+    if (good) {
+        gbcool::heating_and_cooling<2>(cool, v, &eic, kp_dt(kp) * p.time_unit, &temp, &dg);
+        if (temp > p.absTmax) {
+            eic = p.absTmax * v.TtoEI;
+            temp = p.absTmax;
+            clamped = true;
+        }
+        if (eic < p.smallp / v.rho) eic = p.smallp / v.rho;
+        const double ei = eic / (p.vel_unit * p.vel_unit);
+        const double vx = UV(GB_VELX), vy = UV(GB_VELY), vz = UV(GB_VELZ);
+        UV(GB_TEMP) = temp;
+        UV(GB_TDUS) = v.tdust;
+        if (g.slot[GB_PHHE] >= 0) UV(GB_PHHE) = 0.0;
+        if (g.slot[GB_PEFL] >= 0) UV(GB_PEFL) = 0.0;
+        UV(GB_PRES) = gm1 * rn * ei;
+        UV(GB_EINT) = ei;
+        UV(GB_ENER) = ei + 0.5 * (vx * vx + vy * vy + vz * vz);
+    }
+    if (st) {
+        if (!good) gb_fail(st, GB_ST_NONFINITE, blk, i, j, k, temp);
+        gb_count_warp(&st->n_bracket_fail, dg.bracket_fail != 0);
+        gb_count_warp(&st->n_clamped, clamped);
+        if (clamped) gb_fail(st, GB_ST_OVERHEAT, blk, i, j, k, temp);
+        if (dg.unbracketed) gb_fail(st, GB_ST_ZERO_UNBRACKETED, blk, i, j, k, eic);
+        if (dg.maxiter) gb_fail(st, GB_ST_ZERO_MAXITER, blk, i, j, k, eic);
     }
 }
 
