@@ -2045,8 +2045,9 @@ k_update(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restric
 // internal energy, the stored dust temperature and source terms) and its
 // stores; the specific kinetic energy of the total energy comes from the
 // stored velocities. Its own kernel keeps the integrator's long code apart
-// from the update's.
-static __global__ void __launch_bounds__(128, 4)
+// from the update's. Five resident CTAs per SM (90 registers, no spills):
+// 22.29 ms per 4101-leaf step against 22.53 at four and 22.58 at six
+static __global__ void __launch_bounds__(128, 5)
 k_cool_pass(gb_dev_grid g, hydro_kparams kp, gb_cool_ctx cool, const int* __restrict__ list, gb_status* st)
 {
     const int cb = blockIdx.y;
